@@ -1,0 +1,351 @@
+"""Assemblers and affine FE operators over libgfe, mirroring Gridap's
+SparseMatrixAssembler / assemble_* / AffineFEOperator API (FESpaces/SparseMatrixAssemblers.jl,
+FESpaces/Assemblers.jl, FESpaces/AffineFEOperators.jl).
+
+Gridap's `!`-suffixed functions appear here without the `!` (Python names cannot carry it):
+`symbolic_loop_matrix`, `numeric_loop_matrix`, `numeric_loop_vector`, `assemble_matrix_`.
+Matrices stay on the GPU inside a `DeviceMatrix`; vectors are numpy arrays (host) or torch
+CUDA tensors (device), whichever the caller passes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .celldata import CellField, NodalField, SinSum, classify_bilinear, classify_linear
+from .fespaces import FESpace, TrialFESpace, _space
+from .geometry import Measure
+
+_CTX = {}
+
+
+class Context:
+    """One GPU, one CUDA stream (gfe_ctx)."""
+
+    def __init__(self, device: int = 0):
+        lib = _lib.load()
+        h = C.c_void_p()
+        _lib.check(lib.gfe_ctx_create(device, C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _lib.check(_lib.load().gfe_ctx_stream(self.handle, C.byref(s)))
+        return s.value or 0
+
+    def synchronize(self) -> None:
+        _lib.check(_lib.load().gfe_ctx_synchronize(self.handle))
+
+    def kernel_launches(self) -> int:
+        n = C.c_int64()
+        _lib.check(_lib.load().gfe_ctx_kernel_launches(self.handle, C.byref(n)))
+        return n.value
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _lib.load().gfe_ctx_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def default_context(device: int = 0) -> Context:
+    if device not in _CTX:
+        _CTX[device] = Context(device)
+    return _CTX[device]
+
+
+class DeviceMatrix:
+    """A sparse matrix resident on the GPU (gfe_matrix): CSR with sorted unique columns."""
+
+    def __init__(self, handle, ctx: Context):
+        self.handle = handle
+        self.ctx = ctx
+        r, c, z = C.c_int64(), C.c_int64(), C.c_int64()
+        _lib.check(_lib.load().gfe_matrix_info(handle, C.byref(r), C.byref(c), C.byref(z)))
+        self.shape = (r.value, c.value)
+        self.nnz = z.value
+
+    def export_csr(self, index_base: int = 0):
+        """(rowptr, colval, nzval) as int64/int64/float64 host arrays."""
+        rp = np.empty(self.shape[0] + 1, dtype=np.int64)
+        cv = np.empty(self.nnz, dtype=np.int64)
+        nz = np.empty(self.nnz, dtype=np.float64)
+        _lib.check(_lib.load().gfe_matrix_export_csr(self.handle, index_base, _lib.ptr(rp),
+                                                     _lib.ptr(cv), _lib.ptr(nz)))
+        return rp, cv, nz
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        rp, cv, nz = self.export_csr(0)
+        return sp.csr_matrix((nz, cv, rp), shape=self.shape)
+
+    def matvec(self, x, y=None):
+        if y is None:
+            y = np.empty(self.shape[0]) if isinstance(x, np.ndarray) else x.new_empty(self.shape[0])
+        _lib.check(_lib.load().gfe_matrix_mul(self.ctx.handle, self.handle, _lib.ptr(x),
+                                              _lib.ptr(y)))
+        return y
+
+    def fillstored_zero(self):
+        _lib.check(_lib.load().gfe_matrix_fillstored_zero(self.handle))
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _lib.load().gfe_matrix_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class SparseMatrixAssembler:
+    """SparseMatrixAssembler(U, V): assembles into device CSR matrices and dense vectors.
+    `precision` selects the arithmetic of fused cell integrals ("fp64" or "fp32"); the
+    scatter-add always accumulates in FP64."""
+
+    def __init__(self, trial, test, precision: str = "fp64", ctx: Context | None = None):
+        self.trial = _space(trial)
+        self.test = _space(test)
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self.precision = precision
+        self.ctx = ctx or default_context()
+
+    def get_rows(self):
+        return self.test.num_free_dofs()
+
+    def get_cols(self):
+        return self.trial.num_free_dofs()
+
+
+# ---- protocol-level entry points (FESpaces/SparseMatrixAssemblers.jl:174-316) ------------
+def symbolic_loop_matrix(assem: SparseMatrixAssembler, matdata) -> DeviceMatrix:
+    """Pattern of assembling matdata = (cellmats, cell_rows, cell_cols) (cellmats unused)."""
+    _, rows, cols = matdata
+    rows = _as_ids(rows)
+    cols = _as_ids(cols)
+    h = C.c_void_p()
+    _lib.check(_lib.load().gfe_symbolic_loop_matrix(
+        assem.ctx.handle, rows.shape[0], rows.shape[1], _lib.ptr(rows), _lib.ptr(cols),
+        assem.get_rows(), assem.get_cols(), C.byref(h)))
+    return DeviceMatrix(h, assem.ctx)
+
+
+def numeric_loop_matrix(A: DeviceMatrix, assem: SparseMatrixAssembler, matdata) -> DeviceMatrix:
+    """Adds cell matrices (ncells, nd, nd) [row, col] into A in cell order."""
+    cellmats = matdata[0]
+    cm = _cellmats_colmajor(cellmats)
+    _lib.check(_lib.load().gfe_numeric_loop_matrix(assem.ctx.handle, A.handle, _lib.ptr(cm)))
+    return A
+
+
+def numeric_loop_vector(b, assem: SparseMatrixAssembler, vecdata):
+    cellvecs, rows = vecdata
+    rows = _as_ids(rows)
+    cv = np.ascontiguousarray(cellvecs, dtype=np.float64) if isinstance(cellvecs, np.ndarray) \
+        else cellvecs.contiguous()
+    _lib.check(_lib.load().gfe_numeric_loop_vector(
+        assem.ctx.handle, rows.shape[0], rows.shape[1], _lib.ptr(rows), _lib.ptr(cv),
+        b.shape[0], _lib.ptr(b)))
+    return b
+
+
+def _as_ids(a):
+    if isinstance(a, np.ndarray):
+        return np.ascontiguousarray(a, dtype=np.int32)
+    return a.contiguous()
+
+
+def _cellmats_colmajor(cellmats):
+    """Gridap cell matrices are column-major nd x nd; numpy (ncells, nd, nd)[c, i, j] is
+    transposed into that layout."""
+    if isinstance(cellmats, np.ndarray):
+        return np.ascontiguousarray(np.transpose(cellmats, (0, 2, 1)), dtype=np.float64)
+    return cellmats.transpose(1, 2).contiguous()
+
+
+# ---- weak-form driven assembly ------------------------------------------------------------
+class _Prepared:
+    """A gfe_problem plus the arrays it points to (kept alive for the call)."""
+
+    def __init__(self):
+        self.keep = []
+        self.p = _lib.Problem()
+
+
+def _coef_to_problem(prep: _Prepared, coef, ncells):
+    p = prep.p
+    if coef is None:
+        p.coef_kind = _lib.GFE_COEF_ONE
+    elif isinstance(coef, (int, float)):
+        arr = np.array([float(coef)])
+        prep.keep.append(arr)
+        p.coef_kind, p.coef = _lib.GFE_COEF_CONST, _lib.ptr(arr)
+    elif isinstance(coef, CellField):
+        v = coef.values
+        if isinstance(v, np.ndarray):
+            v = np.ascontiguousarray(v, dtype=np.float64)
+        if v.shape[0] != ncells:
+            raise ValueError("per-cell coefficient has the wrong length")
+        prep.keep.append(v)
+        p.coef_kind, p.coef = _lib.GFE_COEF_CELL, _lib.ptr(v)
+    else:
+        raise NotImplementedError(f"coefficient of type {type(coef)}")
+
+
+def _qpoints(model, measure: Measure) -> np.ndarray:
+    """Physical quadrature points of every cell (host glue for Python-callable sources)."""
+    D = model.dim
+    n = measure.degree // 2 + 1
+    x1, w1 = np.polynomial.legendre.leggauss(n)
+    x1 = (x1 + 1) / 2
+    k = np.arange(n ** D)
+    xi = np.stack([x1[(k // n ** d) % n] for d in range(D)], axis=1)  # first coord fastest
+    nv = 2 ** D
+    phi = np.ones((xi.shape[0], nv))
+    for a in range(nv):
+        for d in range(D):
+            phi[:, a] *= xi[:, d] if (a >> d) & 1 else 1 - xi[:, d]
+    X = model.node_coords[model.cell_node_ids - 1]  # (ncells, nv, D)
+    return np.einsum("qa,cad->cqd", phi, X)
+
+
+def _source_to_problem(prep: _Prepared, f, model, measure):
+    p = prep.p
+    if f is None:
+        p.source_kind = _lib.GFE_SRC_NONE
+    elif isinstance(f, (int, float)):
+        arr = np.array([float(f)])
+        prep.keep.append(arr)
+        p.source_kind, p.source, p.source_len = _lib.GFE_SRC_CONST, _lib.ptr(arr), 1
+    elif isinstance(f, NodalField):
+        v = f.values
+        if isinstance(v, np.ndarray):
+            v = np.ascontiguousarray(v, dtype=np.float64)
+        prep.keep.append(v)
+        p.source_kind, p.source, p.source_len = _lib.GFE_SRC_NODAL, _lib.ptr(v), v.shape[0]
+    elif isinstance(f, SinSum) and model.cartesian:
+        arr = np.concatenate([[f.terms.shape[0]], f.terms.reshape(-1)]).astype(np.float64)
+        prep.keep.append(arr)
+        p.source_kind, p.source, p.source_len = _lib.GFE_SRC_SINSUM, _lib.ptr(arr), arr.size
+    elif callable(f):
+        xq = _qpoints(model, measure)
+        vals = np.ascontiguousarray(
+            np.asarray(f(xq.reshape(-1, model.dim)), dtype=np.float64).reshape(-1))
+        prep.keep.append(vals)
+        p.source_kind, p.source, p.source_len = _lib.GFE_SRC_QPOINT, _lib.ptr(vals), vals.size
+    else:
+        raise NotImplementedError(f"source of type {type(f)}")
+
+
+def prepare_problem(U, V, measure: Measure, coef=None, source=None, precision="fp64",
+                    cell_dof_ids=None) -> _Prepared:
+    """The gfe_problem for ∫ coef ∇v⋅∇u dΩ and ∫ source v dΩ on V (U == V for square)."""
+    V = _space(V)
+    model = V.model
+    prep = _Prepared()
+    p = prep.p
+    D = model.dim
+    p.dim, p.reffe, p.ncomp, p.degree = D, _lib.GFE_REFFE_Q1, V.reffe.ncomp, measure.degree
+    p.ncells = model.num_cells()
+    p.nd = V.ndofs_per_cell()
+    ids = V.cell_dof_ids if cell_dof_ids is None else cell_dof_ids
+    prep.keep.append(ids)
+    p.cell_dof_ids = _lib.ptr(ids)
+    p.nfree = V.num_free_dofs()
+    for d in range(D):
+        p.partition[d] = model.partition[d]
+        p.domain[2 * d] = model.domain[2 * d]
+        p.domain[2 * d + 1] = model.domain[2 * d + 1]
+    p.nnodes = model.num_nodes()
+    if model.cartesian:
+        p.geometry = _lib.GFE_GEOM_CARTESIAN
+    else:
+        p.geometry = _lib.GFE_GEOM_NODAL
+        prep.keep.append(model.node_coords)
+        p.node_coords = _lib.ptr(model.node_coords)
+        prep.keep.append(model.cell_node_ids)
+        p.cell_node_ids = _lib.ptr(model.cell_node_ids)
+    p.form = _lib.GFE_FORM_DIFFUSION
+    _coef_to_problem(prep, coef, p.ncells)
+    _source_to_problem(prep, source, model, measure)
+    p.precision = _lib.GFE_PREC_FP32 if precision == "fp32" else _lib.GFE_PREC_FP64
+    return prep
+
+
+def _forms(a, l, U, V):
+    """Evaluates user forms a(u,v), l(v) into (measure, coef, source)."""
+    from .celldata import get_fe_basis, get_trial_fe_basis
+    u, v = get_trial_fe_basis(U), get_fe_basis(V)
+    coef = source = None
+    meas = None
+    if a is not None:
+        dc = a(u, v)
+        if len(dc.terms) != 1:
+            raise NotImplementedError("one bilinear term is provided")
+        expr, meas = dc.terms[0]
+        _, coef = classify_bilinear(expr)
+    if l is not None:
+        dc = l(v)
+        if len(dc.terms) != 1:
+            raise NotImplementedError("one linear term is provided")
+        expr, m2 = dc.terms[0]
+        if meas is not None and m2.degree != meas.degree:
+            raise NotImplementedError("bilinear and linear forms on different measures")
+        meas = m2
+        _, source = classify_linear(expr)
+    return meas, coef, source
+
+
+def assemble_matrix_and_vector(a, l, U, V, assem: SparseMatrixAssembler | None = None,
+                               b_out=None):
+    """(A, b) for the weak forms a(u,v), l(v) (FESpaces/Assemblers.jl:372-400)."""
+    assem = assem or SparseMatrixAssembler(U, V)
+    meas, coef, source = _forms(a, l, U, V)
+    Vs = _space(V)
+    prep = prepare_problem(U, V, meas, coef, source if l is not None else None, assem.precision)
+    A = None
+    if a is not None:
+        ids = Vs.cell_dof_ids
+        A = symbolic_loop_matrix(assem, (None, ids, ids))
+    b = None
+    if l is not None:
+        b = np.zeros(Vs.num_free_dofs()) if b_out is None else b_out
+    _lib.check(_lib.load().gfe_assemble_matrix_and_vector(
+        assem.ctx.handle, C.byref(prep.p), A.handle if A is not None else None,
+        _lib.ptr(b) if b is not None else None))
+    return A, b
+
+
+def assemble_matrix(a, U, V, assem: SparseMatrixAssembler | None = None) -> DeviceMatrix:
+    return assemble_matrix_and_vector(a, None, U, V, assem)[0]
+
+
+def assemble_vector(l, V, assem: SparseMatrixAssembler | None = None):
+    return assemble_matrix_and_vector(None, l, V, V, assem)[1]
+
+
+class AffineFEOperator:
+    """AffineFEOperator(a, l, U, V[, assem]): the assembled system A x = b
+    (FESpaces/AffineFEOperators.jl:23-54)."""
+
+    def __init__(self, a, l, U, V, assem: SparseMatrixAssembler | None = None):
+        self.trial = U
+        self.test = V
+        self.assem = assem or SparseMatrixAssembler(U, V)
+        self.A, self.b = assemble_matrix_and_vector(a, l, U, V, self.assem)
+
+    def get_matrix(self) -> DeviceMatrix:
+        return self.A
+
+    def get_vector(self):
+        return self.b
+
+    def get_trial(self):
+        return self.trial
+
+    def get_test(self):
+        return self.test

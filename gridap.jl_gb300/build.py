@@ -1,0 +1,57 @@
+"""Builds libgfe.so (the CUDA library behind include/gfe.h) for sm_103a, in-tree.
+
+Each translation unit is compiled in parallel with nvcc, then linked into
+gridap.jl_gb300/_build/libgfe.so. Only sm_103a code is generated.
+"""
+import concurrent.futures
+import os
+import pathlib
+import subprocess
+import sys
+
+HERE = pathlib.Path(__file__).resolve().parent
+CSRC = HERE / "csrc"
+OUT = HERE / "_build"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC = os.environ.get("NVCC", "nvcc")
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(HERE.parent / "include")]
+
+
+def _sources():
+    return sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")))
+
+
+def _compile(src: pathlib.Path) -> pathlib.Path:
+    obj = OUT / (src.stem + ".o")
+    deps = [src] + list(CSRC.glob("*.h")) + [HERE.parent / "include" / "gfe.h"]
+    if obj.exists() and all(obj.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return obj
+    cmd = [NVCC, *ARCH, *COMMON, "-c", str(src), "-o", str(obj)]
+    if src.suffix == ".cpp":
+        cmd = [NVCC, *COMMON, "-x", "c++", "-c", str(src), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
+    return obj
+
+
+def build(verbose: bool = False) -> pathlib.Path:
+    OUT.mkdir(exist_ok=True)
+    srcs = _sources()
+    with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(_compile, srcs))
+    lib = OUT / "libgfe.so"
+    if lib.exists() and all(lib.stat().st_mtime >= o.stat().st_mtime for o in objs):
+        return lib
+    cmd = [NVCC, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    if verbose:
+        print(f"built {lib}")
+    return lib
+
+
+if __name__ == "__main__":
+    build(verbose=True)
+    sys.exit(0)

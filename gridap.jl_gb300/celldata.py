@@ -1,0 +1,148 @@
+"""Weak forms as small expression trees, recognised into the closed set of integrands the
+device kernels evaluate.
+
+Gridap builds cell arrays lazily from Julia expressions such as
+`∫( κ*∇(v)⋅∇(u) )dΩ` (CellData/CellQuadratures.jl:138-202). The drop-in cannot ship
+arbitrary Julia code to the GPU, so it recognises the integrands it provides and passes an
+enum plus coefficient arrays across the C ABI:
+
+  - bilinear  `κ * inner(grad(v), grad(u))`  (κ: number, per-cell CellField, or absent);
+  - linear    `f * v`  (f: number, NodalField, SinSum, or a Python callable of x).
+
+Anything else raises NotImplementedError; in Gridap that integrand would stay on Gridap's
+own CPU path.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+class CellField:
+    """A field with one value per cell (piecewise constant), e.g. a per-cell coefficient."""
+
+    def __init__(self, values, trian=None):
+        self.values = values
+        self.trian = trian
+
+
+class NodalField:
+    """A Q1 FE function given by its values at every mesh node (node order)."""
+
+    def __init__(self, values, model=None):
+        self.values = values
+        self.model = model
+
+
+class SinSum:
+    """f(x) = sum_k a_k prod_d sin(pi m_kd x_d); `terms` rows are (a_k, m_k1, ..., m_kD)."""
+
+    def __init__(self, terms):
+        self.terms = np.asarray(terms, dtype=np.float64)
+
+    def __call__(self, x):
+        x = np.atleast_2d(x)
+        D = x.shape[1]
+        out = np.zeros(x.shape[0])
+        for t in self.terms:
+            p = np.full(x.shape[0], t[0])
+            for d in range(D):
+                p = p * np.sin(np.pi * t[1 + d] * x[:, d])
+            out += p
+        return out
+
+
+class _Expr:
+    def __mul__(self, other):
+        return _Scaled(other, self)
+
+    def __rmul__(self, other):
+        return _Scaled(other, self)
+
+
+class _Basis(_Expr):
+    def __init__(self, space, trial: bool):
+        self.space = space
+        self.trial = trial
+
+
+class _Grad(_Expr):
+    def __init__(self, arg):
+        self.arg = arg
+
+
+class _Inner(_Expr):
+    def __init__(self, a, b):
+        self.a = a
+        self.b = b
+
+
+class _Scaled(_Expr):
+    def __init__(self, coef, expr):
+        self.coef = coef
+        self.expr = expr
+
+
+def get_trial_fe_basis(U) -> _Basis:
+    return _Basis(U, True)
+
+
+def get_fe_basis(V) -> _Basis:
+    return _Basis(V, False)
+
+
+def gradient(a):
+    return _Grad(a)
+
+
+grad = gradient
+
+
+def inner(a, b):
+    return _Inner(a, b)
+
+
+dot = inner
+
+
+class DomainContribution:
+    def __init__(self, terms):
+        self.terms = list(terms)
+
+    def __add__(self, other):
+        return DomainContribution(self.terms + other.terms)
+
+
+def integrate(expr, measure) -> DomainContribution:
+    return DomainContribution([(expr, measure)])
+
+
+def _strip_scale(e):
+    coef = None
+    while isinstance(e, _Scaled):
+        if coef is not None:
+            raise NotImplementedError("nested coefficients")
+        coef, e = e.coef, e.expr
+    return coef, e
+
+
+def classify_bilinear(expr):
+    """Returns ("diffusion", coef) for κ ∇v⋅∇u forms."""
+    coef, e = _strip_scale(expr)
+    if isinstance(e, _Inner):
+        ca, a = _strip_scale(e.a)
+        cb, b = _strip_scale(e.b)
+        if isinstance(a, _Grad) and isinstance(b, _Grad) and isinstance(a.arg, _Basis) \
+                and isinstance(b.arg, _Basis) and a.arg.trial != b.arg.trial:
+            coefs = [c for c in (coef, ca, cb) if c is not None]
+            if len(coefs) > 1:
+                raise NotImplementedError("more than one coefficient in the bilinear form")
+            return "diffusion", (coefs[0] if coefs else None)
+    raise NotImplementedError("bilinear form not recognised (provided: κ*inner(grad(v),grad(u)))")
+
+
+def classify_linear(expr):
+    """Returns ("source", f) for f*v forms."""
+    coef, e = _strip_scale(expr)
+    if isinstance(e, _Basis) and not e.trial:
+        return "source", (1.0 if coef is None else coef)
+    raise NotImplementedError("linear form not recognised (provided: f*v)")

@@ -1,0 +1,292 @@
+// gfe_api.cu -- the exported C ABI (include/gfe.h): argument checking, host/device data
+// movement and dispatch to the kernels. No exception or process exit crosses this layer.
+#include <cstring>
+
+#include "gfe_internal.h"
+
+using namespace gfe;
+
+namespace {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace
+
+extern "C" const char* gfe_last_error(void) { return g_last_error_ptr(); }
+
+extern "C" const char* gfe_version(void) { return "gfe 0.1.0 (sm_103a)"; }
+
+extern "C" int gfe_ctx_create(int device, gfe_ctx** out) {
+  clear_error();
+  if (!out) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_ctx_create: out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  GFE_CUDA_TRY(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_ctx_create: device %d of %d", device, ndev);
+  DeviceGuard g(device);
+  gfe_ctx* c = new gfe_ctx();
+  c->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount,
+                                                   device);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, sizeof(DevError));
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(DevError), c->stream);
+  if (e == cudaSuccess) e = cudaMallocHost(&c->h_pinned, 4096);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    int code = set_error(GFE_ERR_CUDA, "gfe_ctx_create: %s", cudaGetErrorString(e));
+    gfe_ctx_destroy(c);
+    return code;
+  }
+  *out = c;
+  return GFE_OK;
+}
+
+extern "C" int gfe_ctx_destroy(gfe_ctx* c) {
+  if (!c) return GFE_OK;
+  DeviceGuard g(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& s : c->scratch) s.release();
+  if (c->d_err) cudaFree(c->d_err);
+  if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return GFE_OK;
+}
+
+extern "C" int gfe_ctx_stream(gfe_ctx* c, void** stream) {
+  clear_error();
+  if (!c || !stream) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_ctx_stream: NULL");
+  *stream = (void*)c->stream;
+  return GFE_OK;
+}
+
+extern "C" int gfe_ctx_synchronize(gfe_ctx* c) {
+  clear_error();
+  if (!c) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_ctx_synchronize: NULL");
+  DeviceGuard g(c->device);
+  GFE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return check_device_error(c, "synchronize");
+}
+
+extern "C" int gfe_ctx_kernel_launches(gfe_ctx* c, int64_t* count) {
+  clear_error();
+  if (!c || !count) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_ctx_kernel_launches: NULL");
+  *count = c->launches;
+  return GFE_OK;
+}
+
+// ---- symbolic -----------------------------------------------------------------------------
+extern "C" int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd,
+                                        const int32_t* cell_rows, const int32_t* cell_cols,
+                                        int64_t nrows, int64_t ncols, gfe_matrix** out) {
+  clear_error();
+  if (!ctx || !out || nd < 1 || ncells < 0 || nrows < 0 || ncols < 0 ||
+      (ncells > 0 && (!cell_rows || !cell_cols)))
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_symbolic_loop_matrix: bad arguments");
+  if (nrows > INT32_MAX || ncols > INT32_MAX)
+    return set_error(GFE_ERR_UNSUPPORTED, "gfe_symbolic_loop_matrix: more than 2^31 rows");
+  *out = nullptr;
+  DeviceGuard g(ctx->device);
+  gfe_matrix* A = new gfe_matrix();
+  A->ctx = ctx;
+  A->nrows = nrows;
+  A->ncols = ncols;
+  A->nd = nd;
+  A->ncells = ncells;
+  const size_t idsz = sizeof(int32_t) * (size_t)ncells * nd;
+  int s = A->cell_rows.reserve(idsz);
+  if (s == GFE_OK) s = A->cell_cols.reserve(idsz);
+  if (s == GFE_OK && idsz) {
+    cudaError_t e = cudaMemcpyAsync(A->cell_rows.ptr, cell_rows, idsz, cudaMemcpyDefault,
+                                    ctx->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(A->cell_cols.ptr, cell_cols, idsz, cudaMemcpyDefault, ctx->stream);
+    if (e != cudaSuccess) s = set_error(GFE_ERR_CUDA, "copy cell ids: %s", cudaGetErrorString(e));
+  }
+  if (s == GFE_OK) s = build_pattern(ctx, A);
+  if (s != GFE_OK) {
+    delete A;
+    return s;
+  }
+  *out = A;
+  return GFE_OK;
+}
+
+extern "C" int gfe_matrix_destroy(gfe_matrix* A) {
+  if (!A) return GFE_OK;
+  DeviceGuard g(A->ctx->device);
+  cudaStreamSynchronize(A->ctx->stream);
+  delete A;
+  return GFE_OK;
+}
+
+extern "C" int gfe_matrix_info(gfe_matrix* A, int64_t* nrows, int64_t* ncols, int64_t* nnz) {
+  clear_error();
+  if (!A) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_matrix_info: NULL");
+  if (nrows) *nrows = A->nrows;
+  if (ncols) *ncols = A->ncols;
+  if (nnz) *nnz = A->nnz;
+  return GFE_OK;
+}
+
+__global__ void k_widen(const int32_t* __restrict__ in, int64_t* __restrict__ out, int64_t n,
+                        int64_t base) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (int64_t)in[i] + base;
+}
+
+extern "C" int gfe_matrix_export_csr(gfe_matrix* A, int index_base, int64_t* rowptr,
+                                     int64_t* colval, double* nzval) {
+  clear_error();
+  if (!A || (index_base != 0 && index_base != 1))
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_matrix_export_csr: bad arguments");
+  gfe_ctx* ctx = A->ctx;
+  DeviceGuard g(ctx->device);
+  auto widen = [&](const int32_t* src, int64_t n, int64_t* dst) -> int {
+    if (!dst || n == 0) return GFE_OK;
+    const bool dev = is_device_ptr(dst);
+    int64_t* d = dst;
+    if (!dev) {
+      GFE_TRY(ctx->scratch[SCR_TMP3].reserve(sizeof(int64_t) * n));
+      d = ctx->scratch[SCR_TMP3].as<int64_t>();
+    }
+    k_widen<<<grid_for(n, 256), 256, 0, ctx->stream>>>(src, d, n, index_base);
+    ctx->launches++;
+    GFE_CUDA_TRY(cudaGetLastError());
+    if (!dev) GFE_TRY(copy_out(ctx, dst, d, sizeof(int64_t) * n));
+    return GFE_OK;
+  };
+  GFE_TRY(widen(A->rowptr.as<int32_t>(), A->nrows + 1, rowptr));
+  GFE_TRY(widen(A->colval.as<int32_t>(), A->nnz, colval));
+  if (nzval) GFE_TRY(copy_out(ctx, nzval, A->val.ptr, sizeof(double) * A->nnz));
+  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return GFE_OK;
+}
+
+extern "C" int gfe_matrix_fillstored_zero(gfe_matrix* A) {
+  clear_error();
+  if (!A) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_matrix_fillstored_zero: NULL");
+  DeviceGuard g(A->ctx->device);
+  if (A->nnz)
+    GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * A->nnz, A->ctx->stream));
+  A->plan_valid = false;
+  return GFE_OK;
+}
+
+// ---- numeric, caller-provided cell arrays -------------------------------------------------
+extern "C" int gfe_numeric_loop_matrix(gfe_ctx* ctx, gfe_matrix* A, const double* cellmats) {
+  clear_error();
+  if (!ctx || !A || (A->ncells > 0 && !cellmats) || A->ctx != ctx)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_numeric_loop_matrix: bad arguments");
+  DeviceGuard g(ctx->device);
+  const void* d;
+  GFE_TRY(device_view(ctx, cellmats, sizeof(double) * (size_t)A->ncells * A->nd * A->nd,
+                      SCR_CELLMAT, &d));
+  GFE_TRY(assemble_cellmats(ctx, A, (const double*)d));
+  A->plan_valid = false;
+  return GFE_OK;
+}
+
+extern "C" int gfe_numeric_loop_vector(gfe_ctx* ctx, int64_t ncells, int nd,
+                                       const int32_t* cell_rows, const double* cellvecs,
+                                       int64_t nrows, double* b) {
+  clear_error();
+  if (!ctx || nd < 1 || ncells < 0 || nrows < 0 || !b ||
+      (ncells > 0 && (!cell_rows || !cellvecs)))
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_numeric_loop_vector: bad arguments");
+  DeviceGuard g(ctx->device);
+  const void* dr;
+  const void* dv;
+  GFE_TRY(device_view(ctx, cell_rows, sizeof(int32_t) * (size_t)ncells * nd, SCR_CELLIDS, &dr));
+  GFE_TRY(device_view(ctx, cellvecs, sizeof(double) * (size_t)ncells * nd, SCR_CELLVEC, &dv));
+  const bool bdev = is_device_ptr(b);
+  double* db = b;
+  if (!bdev) {
+    GFE_TRY(ctx->scratch[SCR_VEC_B].reserve(sizeof(double) * (nrows > 0 ? nrows : 1)));
+    db = ctx->scratch[SCR_VEC_B].as<double>();
+    GFE_CUDA_TRY(cudaMemcpyAsync(db, b, sizeof(double) * nrows, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  }
+  GFE_TRY(assemble_cellvecs(ctx, ncells, nd, (const int32_t*)dr, (const double*)dv, nrows, db));
+  if (!bdev) GFE_TRY(copy_out(ctx, b, db, sizeof(double) * nrows));
+  return GFE_OK;
+}
+
+// ---- fused --------------------------------------------------------------------------------
+extern "C" int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* p,
+                                              gfe_matrix* A, double* b) {
+  clear_error();
+  if (!ctx || !p || (!A && !b) || p->ncells < 0 || (p->ncells > 0 && !p->cell_dof_ids))
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_assemble_matrix_and_vector: bad arguments");
+  if (A && A->ctx != ctx)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_assemble_matrix_and_vector: foreign matrix");
+  if (A && A->nrows != p->nfree)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_assemble_matrix_and_vector: nfree %lld != "
+                     "matrix rows %lld", (long long)p->nfree, (long long)A->nrows);
+  DeviceGuard g(ctx->device);
+  const bool bdev = b && is_device_ptr(b);
+  double* db = b;
+  if (b && !bdev) {
+    GFE_TRY(ctx->scratch[SCR_VEC_B].reserve(sizeof(double) * (p->nfree > 0 ? p->nfree : 1)));
+    db = ctx->scratch[SCR_VEC_B].as<double>();
+  }
+  GFE_TRY(assemble_problem(ctx, p, A, db));
+  if (A) A->plan_valid = false;
+  if (b && !bdev) GFE_TRY(copy_out(ctx, b, db, sizeof(double) * p->nfree));
+  return GFE_OK;
+}
+
+// ---- solve --------------------------------------------------------------------------------
+extern "C" int gfe_solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* opts,
+                         const double* b, double* x, gfe_solve_report* report) {
+  clear_error();
+  if (!ctx || !A || !opts || !b || !x || A->ctx != ctx)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_solve: bad arguments");
+  if (!(opts->rtol > 0.0))
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_solve: rtol must be positive");
+  DeviceGuard g(ctx->device);
+  const size_t n8 = sizeof(double) * (size_t)A->nrows;
+  const void* db;
+  GFE_TRY(device_view(ctx, b, n8, SCR_VEC_B, &db));
+  const bool xdev = is_device_ptr(x);
+  double* dx = x;
+  if (!xdev) {
+    GFE_TRY(ctx->scratch[SCR_VEC_X].reserve(n8 + 8));
+    dx = ctx->scratch[SCR_VEC_X].as<double>();
+  }
+  gfe_solve_report rep;
+  memset(&rep, 0, sizeof(rep));
+  GFE_TRY(solve(ctx, A, opts, (const double*)db, dx, &rep));
+  if (!xdev) GFE_TRY(copy_out(ctx, x, dx, n8));
+  if (report) *report = rep;
+  return check_device_error(ctx, "gfe_solve");
+}
+
+extern "C" int gfe_matrix_mul(gfe_ctx* ctx, gfe_matrix* A, const double* x, double* y) {
+  clear_error();
+  if (!ctx || !A || !x || !y || A->ctx != ctx)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_matrix_mul: bad arguments");
+  DeviceGuard g(ctx->device);
+  const void* dx;
+  GFE_TRY(device_view(ctx, x, sizeof(double) * (size_t)A->ncols, SCR_TMP2, &dx));
+  const bool ydev = is_device_ptr(y);
+  double* dy = y;
+  if (!ydev) {
+    GFE_TRY(ctx->scratch[SCR_TMP3].reserve(sizeof(double) * (size_t)A->nrows + 8));
+    dy = ctx->scratch[SCR_TMP3].as<double>();
+  }
+  GFE_TRY(spmv64(ctx, A, (const double*)dx, dy));
+  if (!ydev) GFE_TRY(copy_out(ctx, y, dy, sizeof(double) * (size_t)A->nrows));
+  return GFE_OK;
+}

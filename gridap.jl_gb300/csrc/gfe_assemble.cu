@@ -1,0 +1,757 @@
+// gfe_assemble.cu -- numeric assembly on the device.
+//
+// Gridap's numeric loop walks cells in order and adds every cell matrix entry into the
+// sparse matrix (InserterCSC: binary search in the column, then `+=`), so each stored value
+// is the sum of its cell contributions in ascending cell order
+// (FESpaces/SparseMatrixAssemblers.jl:214-248, Algebra/SparseMatrixCSC.jl:124-150).
+//
+// Here every matrix row is owned by one thread. The thread walks the row's cell references
+// (sorted by cell, built with the pattern), finds each contribution's column by binary search
+// in the row's sorted column list and accumulates in shared memory. Each stored value thus
+// receives exactly the additions Gridap makes, in the same order, with no atomics and no
+// colouring: the result is deterministic and, for identical cell values, bit-identical to
+// Gridap's. A block of R rows then writes its contiguous slice of the CSR values with
+// coalesced stores.
+//
+// Cell values come from a source functor:
+//   - StoredCells: cell matrices/vectors in memory (the caller's, or an element kernel's);
+//   - CartesianDiffusionQ1: kappa_K * Kref on uniform Cartesian cells, where every cell has
+//     Jt = diag(h) (Geometry/CartesianGrids.jl:247-276) and hence the same reference
+//     stiffness; the source term from the cell's node values or quadrature-point values.
+#include <cmath>
+
+#include "gfe_internal.h"
+
+namespace gfe {
+
+__device__ __forceinline__ void raise_err(DevError* err, int code, long long index) {
+  if (atomicCAS(&err->code, 0, code) == 0) err->index = index;
+}
+
+struct RowArgs {
+  int64_t nrows;
+  int nd;
+  const int32_t* rowptr;
+  const int32_t* colval;
+  const int64_t* ref_ptr;
+  const int32_t* refs;
+  const int32_t* cell_cols;  // column ids per cell (Gridap convention)
+  double* val;               // may be null (vector only)
+  double* b;                 // may be null (matrix only)
+  DevError* err;
+};
+
+// ---- cell value sources -------------------------------------------------------------------
+// Stored cell arrays. Entry (cell, li, lj) at mat[cell*cs + (li + lj*nd)*es].
+struct StoredCells {
+  const double* mat;
+  const double* vec;
+  int64_t cs, es;    // cell stride, entry stride of mat
+  int64_t vcs, ves;  // same for vec
+  int ntab;          // no tables
+  __device__ void load_tables(double*) const {}
+  __device__ __forceinline__ double m(const double*, int64_t cell, int li, int lj, int nd) const {
+    return __ldg(mat + cell * cs + (int64_t)(li + lj * nd) * es);
+  }
+  __device__ __forceinline__ double v(const double*, int64_t cell, int li) const {
+    return __ldg(vec + cell * vcs + (int64_t)li * ves);
+  }
+};
+
+// Uniform Cartesian Q1 diffusion. Tables (built on the host, FP64):
+//   Kref[nd*nd]  = sum_q (invJt grad phi_i).(invJt grad phi_j) |det Jt| w_q   (col-major)
+//   Mref[nd*nd]  = sum_q phi_i phi_a |det Jt| w_q                             (col-major)
+//   mref[nd]     = sum_q phi_i |det Jt| w_q
+//   PW[nq*nd]    = phi_i(xi_q) |det Jt| w_q
+template <int D, bool FP32>
+struct CartesianDiffusionQ1 {
+  static constexpr int NV = 1 << D;
+  const double* tables;  // Kref | Mref | mref | PW
+  int nq;
+  int coef_kind;         // GFE_COEF_*
+  const double* coef;
+  int src_kind;          // GFE_SRC_* (SINSUM arrives here as QPOINT values)
+  const double* src;
+  int64_t n0, n1;        // cells per direction
+  const int32_t* cell_nodes;  // optional explicit node ids
+  int ntab;
+  __device__ void load_tables(double* s) const {
+    for (int i = threadIdx.x; i < ntab; i += blockDim.x) s[i] = tables[i];
+  }
+  __device__ __forceinline__ double kappa(int64_t cell) const {
+    if (coef_kind == GFE_COEF_CELL) return __ldg(coef + cell);
+    if (coef_kind == GFE_COEF_CONST) return __ldg(coef);
+    return 1.0;
+  }
+  __device__ __forceinline__ double m(const double* s, int64_t cell, int li, int lj, int) const {
+    const double k = s[li + lj * NV];
+    if (coef_kind == GFE_COEF_ONE) return k;
+    if (FP32) return (double)((float)kappa(cell) * (float)k);
+    return kappa(cell) * k;
+  }
+  __device__ __forceinline__ int64_t node(int64_t cell, int a) const {
+    if (cell_nodes) return (int64_t)__ldg(cell_nodes + cell * NV + a) - 1;
+    const int64_t i = cell % n0, r = cell / n0, j = r % n1, k = r / n1;
+    const int64_t np0 = n0 + 1, np1 = n1 + 1;
+    return (i + (a & 1)) + np0 * ((j + ((a >> 1) & 1)) + np1 * (k + ((a >> 2) & 1)));
+  }
+  __device__ __forceinline__ double v(const double* s, int64_t cell, int li) const {
+    const double* Mref = s + NV * NV;
+    const double* mref = Mref + NV * NV;
+    const double* PW = mref + NV;
+    if (src_kind == GFE_SRC_CONST) return __ldg(src) * mref[li];
+    if (src_kind == GFE_SRC_NODAL) {
+      double acc = 0.0;
+#pragma unroll
+      for (int a = 0; a < NV; ++a) acc = fma(Mref[li + a * NV], __ldg(src + node(cell, a)), acc);
+      return acc;
+    }
+    if (src_kind == GFE_SRC_QPOINT) {
+      double acc = 0.0;
+      for (int q = 0; q < nq; ++q) acc = fma(__ldg(src + cell * nq + q), PW[q * NV + li], acc);
+      return acc;
+    }
+    return 0.0;
+  }
+};
+
+// ---- the row-gather kernel ----------------------------------------------------------------
+template <int MAXW, int R, class Src>
+__global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
+  extern __shared__ double smem[];
+  double* acc = smem;                 // acc[k*R + t]
+  double* tab = smem + MAXW * R;      // source tables
+  __shared__ int32_t lrp[R + 1];      // block-relative row starts
+  const int t = threadIdx.x;
+  const int64_t r0 = (int64_t)blockIdx.x * R;
+  const int64_t r = r0 + t;
+  src.load_tables(tab);
+
+  int32_t start = 0, n = 0;
+  if (r < a.nrows) {
+    start = a.rowptr[r];
+    n = a.rowptr[r + 1] - start;
+  }
+  const int64_t rend = (r0 + R < a.nrows) ? r0 + R : a.nrows;
+  const int32_t bstart = a.rowptr[r0 < a.nrows ? r0 : a.nrows];
+  lrp[t] = (r < a.nrows ? start : a.rowptr[rend]) - bstart;
+  if (t == 0) lrp[R] = a.rowptr[rend] - bstart;
+  if (a.val)
+    for (int k = 0; k < n; ++k) acc[k * R + t] = 0.0;
+  __syncthreads();
+
+  double bacc = 0.0;
+  if (r < a.nrows) {
+    const int32_t* cols = a.colval + start;
+    for (int64_t q = a.ref_ptr[r]; q < a.ref_ptr[r + 1]; ++q) {
+      const int32_t e = a.refs[q];
+      const int64_t cell = e / a.nd;
+      const int li = e - (int)(cell * a.nd);
+      if (a.val) {
+        const int32_t* cc = a.cell_cols + cell * a.nd;
+        for (int lj = 0; lj < a.nd; ++lj) {
+          const int32_t c = __ldg(cc + lj) - 1;
+          if (c < 0) continue;
+          int lo = 0, hi = n;
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(cols + mid) < c) lo = mid + 1; else hi = mid;
+          }
+          if (lo >= n || __ldg(cols + lo) != c) {
+            raise_err(a.err, GFE_ERR_INVALID_ARGUMENT, r);
+            continue;
+          }
+          acc[lo * R + t] += src.m(tab, cell, li, lj, a.nd);
+        }
+      }
+      if (a.b) bacc += src.v(tab, cell, li);
+    }
+    if (a.b) a.b[r] = bacc;
+  }
+  if (!a.val) return;
+  __syncthreads();
+  // coalesced write-out of the block's CSR slice
+  const int32_t total = lrp[R];
+  double* out = a.val + bstart;
+  for (int32_t l = t; l < total; l += R) {
+    int lo = 0, hi = R;  // largest row t' with lrp[t'] <= l
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (lrp[mid] <= l) lo = mid; else hi = mid;
+    }
+    out[l] = acc[(l - lrp[lo]) * R + lo];
+  }
+}
+
+template <int MAXW, int R, class Src>
+static int launch_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src) {
+  const size_t smem = sizeof(double) * ((size_t)MAXW * R + (size_t)src.ntab);
+  auto kern = k_assemble_rows<MAXW, R, Src>;
+  if (smem > 48 * 1024)
+    GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  kern<<<grid_for(a.nrows, R), R, smem, ctx->stream>>>(a, src);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+// Maximum row width of a matrix (device reduction over rowptr differences).
+__global__ void k_max_width(const int32_t* __restrict__ rowptr, int64_t n, int32_t* out) {
+  int32_t m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t w = rowptr[i + 1] - rowptr[i];
+    m = w > m ? w : m;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const int32_t o = __shfl_down_sync(0xffffffffu, m, off);
+    m = o > m ? o : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+static int max_row_width(gfe_ctx* ctx, gfe_matrix* A, int* out) {
+  GFE_TRY(ctx->scratch[SCR_REDUCE].reserve(256));
+  int32_t* d = ctx->scratch[SCR_REDUCE].as<int32_t>();
+  GFE_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(int32_t), ctx->stream));
+  k_max_width<<<grid_for(A->nrows, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+      A->rowptr.as<int32_t>(), A->nrows, d);
+  ctx->launches++;
+  int32_t h = 0;
+  GFE_TRY(copy_out(ctx, &h, d, sizeof(int32_t)));
+  *out = h;
+  return GFE_OK;
+}
+
+template <class Src>
+static int run_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src, int maxw) {
+  if (maxw <= 16) return launch_rows<16, 128>(ctx, a, src);
+  if (maxw <= 32) return launch_rows<32, 128>(ctx, a, src);
+  if (maxw <= 64) return launch_rows<64, 128>(ctx, a, src);
+  if (maxw <= 128) return launch_rows<128, 64>(ctx, a, src);
+  if (maxw <= 256) return launch_rows<256, 32>(ctx, a, src);
+  return set_error(GFE_ERR_ROW_TOO_WIDE, "assembly: row width %d exceeds 256", maxw);
+}
+
+static RowArgs row_args(gfe_ctx* ctx, gfe_matrix* A, double* b, bool with_matrix) {
+  RowArgs a;
+  a.nrows = A->nrows;
+  a.nd = A->nd;
+  a.rowptr = A->rowptr.as<int32_t>();
+  a.colval = A->colval.as<int32_t>();
+  a.ref_ptr = A->ref_ptr.as<int64_t>();
+  a.refs = A->refs.as<int32_t>();
+  a.cell_cols = A->cell_cols.as<int32_t>();
+  a.val = with_matrix ? A->val.as<double>() : nullptr;
+  a.b = b;
+  a.err = ctx->d_err;
+  return a;
+}
+
+// Vector-only gather: b[r] (+)= the row's cell contributions in cell order.
+template <class Src, bool ADD>
+__global__ void k_vector_rows(RowArgs a, Src src) {
+  extern __shared__ double tab[];
+  src.load_tables(tab);
+  __syncthreads();
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.nrows) return;
+  double acc = 0.0;
+  for (int64_t q = a.ref_ptr[r]; q < a.ref_ptr[r + 1]; ++q) {
+    const int32_t e = a.refs[q];
+    const int64_t cell = e / a.nd;
+    acc += src.v(tab, cell, e - (int)(cell * a.nd));
+  }
+  if (ADD) a.b[r] += acc; else a.b[r] = acc;
+}
+
+template <class Src, bool ADD = false>
+static int vector_only_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src) {
+  k_vector_rows<Src, ADD><<<grid_for(a.nrows, 256), 256, sizeof(double) * src.ntab,
+                            ctx->stream>>>(a, src);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+// ---- caller-provided cell matrices (Gridap's numeric_loop_matrix!) -----------------------
+int assemble_cellmats(gfe_ctx* ctx, gfe_matrix* A, const double* d_cellmats) {
+  int maxw = 0;
+  GFE_TRY(max_row_width(ctx, A, &maxw));
+  StoredCells src{};
+  src.mat = d_cellmats;
+  src.vec = nullptr;
+  src.cs = (int64_t)A->nd * A->nd;
+  src.es = 1;
+  src.ntab = 0;
+  RowArgs a = row_args(ctx, A, nullptr, true);
+  GFE_TRY(run_rows(ctx, a, src, maxw));
+  return check_device_error(ctx, "numeric_loop_matrix");
+}
+
+// ---- caller-provided cell vectors (numeric_loop_vector!) ---------------------------------
+// Builds the row references of the given cell ids in scratch, then gathers per row.
+int assemble_cellvecs(gfe_ctx* ctx, int64_t ncells, int nd, const int32_t* d_rows,
+                      const double* d_cellvecs, int64_t nrows, double* d_b) {
+  // A temporary matrix object carries the references (no pattern needed).
+  gfe_matrix T;
+  T.ctx = ctx;
+  T.nrows = nrows;
+  T.ncols = nrows;
+  T.nd = nd;
+  T.ncells = ncells;
+  const size_t idsz = sizeof(int32_t) * (size_t)ncells * nd;
+  GFE_TRY(T.cell_rows.reserve(idsz));
+  GFE_CUDA_TRY(cudaMemcpyAsync(T.cell_rows.ptr, d_rows, idsz, cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+  GFE_TRY(build_refs(ctx, &T));
+  StoredCells src{};
+  src.mat = nullptr;
+  src.vec = d_cellvecs;
+  src.vcs = nd;
+  src.ves = 1;
+  src.ntab = 0;
+  RowArgs a;
+  a.nrows = nrows;
+  a.nd = nd;
+  a.rowptr = nullptr;
+  a.colval = nullptr;
+  a.ref_ptr = T.ref_ptr.as<int64_t>();
+  a.refs = T.refs.as<int32_t>();
+  a.cell_cols = nullptr;
+  a.val = nullptr;
+  a.b = d_b;
+  a.err = ctx->d_err;
+  GFE_TRY((vector_only_rows<StoredCells, true>(ctx, a, src)));
+  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // T's buffers are freed at return
+  return check_device_error(ctx, "numeric_loop_vector");
+}
+
+// ---- element kernel: Q1 cells with nodal (possibly distorted) geometry --------------------
+// One thread per cell, following the per-quadrature-point steps of Gridap's lazy cell
+// arrays: Jt_q = sum_a grad phi_a(xi_q) (x) x_a (Geometry/Grids.jl:237-241), inv and det
+// (TensorValues/Operations.jl:875-934), grad phi_i = invJt . grad phi_hat_i
+// (Fields/FieldsInterfaces.jl:98-106), K_ij += ((kappa grad v_i) . grad u_j) |det Jt| w_q
+// (Fields/FieldsInterfaces.jl:708-720). Output in entry-major layout
+// K[(li + lj*nd)*ncells + cell], b[li*ncells + cell] for coalesced stores and loads.
+template <int D, typename T>
+__global__ void k_q1_cells_nodal(int64_t ncells, const int32_t* __restrict__ cell_nodes,
+                                 const double* __restrict__ coords,
+                                 const double* __restrict__ tabs, int nq, int coef_kind,
+                                 const double* __restrict__ coef, int src_kind,
+                                 const double* __restrict__ src, double* __restrict__ K,
+                                 double* __restrict__ bvec, DevError* err) {
+  constexpr int NV = 1 << D;
+  extern __shared__ double st[];  // w[nq] | phi[nq*NV] | dphi[nq*NV*D]
+  const int ntab = nq * (1 + NV + NV * D);
+  for (int i = threadIdx.x; i < ntab; i += blockDim.x) st[i] = tabs[i];
+  __syncthreads();
+  const double* w = st;
+  const double* phi = w + nq;
+  const double* dphi = phi + nq * NV;
+  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncells) return;
+  T x[NV][D];
+  int64_t nid[NV];
+#pragma unroll
+  for (int a = 0; a < NV; ++a) {
+    nid[a] = (int64_t)__ldg(cell_nodes + cell * NV + a) - 1;
+#pragma unroll
+    for (int d = 0; d < D; ++d) x[a][d] = (T)__ldg(coords + nid[a] * D + d);
+  }
+  T kap = (T)1;
+  if (coef_kind == GFE_COEF_CELL) kap = (T)__ldg(coef + cell);
+  else if (coef_kind == GFE_COEF_CONST) kap = (T)__ldg(coef);
+  T Ke[NV][NV];
+  T be[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    be[i] = (T)0;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) Ke[i][j] = (T)0;
+  }
+  for (int q = 0; q < nq; ++q) {
+    T Jt[D][D];
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+#pragma unroll
+      for (int l = 0; l < D; ++l) Jt[k][l] = (T)0;
+#pragma unroll
+    for (int a = 0; a < NV; ++a)
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        const T g = (T)dphi[(q * NV + a) * D + k];
+#pragma unroll
+        for (int l = 0; l < D; ++l) Jt[k][l] += g * x[a][l];
+      }
+    T det, iJ[D][D];
+    if (D == 2) {
+      det = Jt[0][0] * Jt[1][1] - Jt[0][1] * Jt[1][0];
+      const T c = (T)1 / det;
+      iJ[0][0] = Jt[1][1] * c;
+      iJ[0][1] = -Jt[0][1] * c;
+      iJ[1][0] = -Jt[1][0] * c;
+      iJ[1][1] = Jt[0][0] * c;
+    } else {
+      const T a11 = Jt[0][0], a12 = Jt[0][1], a13 = Jt[0][2];
+      const T a21 = Jt[1][0], a22 = Jt[1][1], a23 = Jt[1][2];
+      const T a31 = Jt[2][0], a32 = Jt[2][1], a33 = Jt[2][2];
+      det = a11 * a22 * a33 + a12 * a23 * a31 + a13 * a21 * a32 -
+            (a11 * a23 * a32 + a12 * a21 * a33 + a13 * a22 * a31);
+      const T c = (T)1 / det;
+      iJ[0][0] = (a22 * a33 - a23 * a32) * c;
+      iJ[1][0] = -(a21 * a33 - a23 * a31) * c;
+      iJ[2][0] = (a21 * a32 - a22 * a31) * c;
+      iJ[0][1] = -(a12 * a33 - a13 * a32) * c;
+      iJ[1][1] = (a11 * a33 - a13 * a31) * c;
+      iJ[2][1] = -(a11 * a32 - a12 * a31) * c;
+      iJ[0][2] = (a12 * a23 - a13 * a22) * c;
+      iJ[1][2] = -(a11 * a23 - a13 * a21) * c;
+      iJ[2][2] = (a11 * a22 - a12 * a21) * c;
+    }
+    if (!(det != (T)0) || !isfinite((double)det)) {
+      raise_err(err, GFE_ERR_DEGENERATE_CELL, cell);
+      return;
+    }
+    const T dV = (det < (T)0 ? -det : det) * (T)w[q];
+    T g[NV][D];
+#pragma unroll
+    for (int a = 0; a < NV; ++a)
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        T s = (T)0;
+#pragma unroll
+        for (int l = 0; l < D; ++l) s += iJ[k][l] * (T)dphi[(q * NV + a) * D + l];
+        g[a][k] = s;
+      }
+#pragma unroll
+    for (int j = 0; j < NV; ++j)
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        T s = (T)0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) s += (kap * g[i][k]) * g[j][k];
+        Ke[i][j] += s * dV;
+      }
+    if (src_kind != GFE_SRC_NONE) {
+      T fq = (T)0;
+      if (src_kind == GFE_SRC_CONST) fq = (T)__ldg(src);
+      else if (src_kind == GFE_SRC_NODAL) {
+#pragma unroll
+        for (int a = 0; a < NV; ++a) fq += (T)__ldg(src + nid[a]) * (T)phi[q * NV + a];
+      } else if (src_kind == GFE_SRC_QPOINT) fq = (T)__ldg(src + cell * nq + q);
+#pragma unroll
+      for (int i = 0; i < NV; ++i) be[i] += (fq * (T)phi[q * NV + i]) * dV;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NV; ++j)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) K[(int64_t)(i + j * NV) * ncells + cell] = (double)Ke[i][j];
+  if (bvec)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) bvec[(int64_t)i * ncells + cell] = (double)be[i];
+}
+
+// ---- f(x) = sum_k a_k prod_d sin(pi m_kd x_d) at the quadrature points of Cartesian cells
+template <int D>
+__global__ void k_sinsum_qpoints(int64_t ncells, int64_t n0, int64_t n1, double x0, double y0,
+                                 double z0, double hx, double hy, double hz,
+                                 const double* __restrict__ qx, int nq,
+                                 const double* __restrict__ terms, int nterms,
+                                 double* __restrict__ fq) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= ncells * nq) return;
+  const int64_t cell = idx / nq;
+  const int q = (int)(idx - cell * nq);
+  const int64_t I[3] = {cell % n0, (cell / n0) % n1, cell / (n0 * n1)};
+  const double o[3] = {x0, y0, z0}, h[3] = {hx, hy, hz};
+  double x[3];
+  for (int d = 0; d < D; ++d) {
+    // physical point: xi . diag(h) + cell origin (Fields/AffineMaps.jl:57-62)
+    const double org = o[d] + (double)I[d] * h[d];
+    x[d] = qx[q * D + d] * h[d] + org;
+  }
+  const double pi = 3.14159265358979323846;
+  double f = 0.0;
+  for (int k = 0; k < nterms; ++k) {
+    const double* t = terms + k * (1 + D);
+    double p = t[0];
+    for (int d = 0; d < D; ++d) p *= sin(pi * t[1 + d] * x[d]);
+    f += p;
+  }
+  fq[idx] = f;
+}
+
+__global__ void k_check_finite(const double* __restrict__ v, int64_t n, DevError* err) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if (!isfinite(v[i])) raise_err(err, GFE_ERR_NONFINITE, i);
+}
+
+// ---- host: reference tables ---------------------------------------------------------------
+static void q1_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
+                      std::vector<double>& dphi) {
+  const int nv = 1 << D;
+  phi.assign((size_t)nq * nv, 0.0);
+  dphi.assign((size_t)nq * nv * D, 0.0);
+  for (int q = 0; q < nq; ++q)
+    for (int a = 0; a < nv; ++a) {
+      double f[3], g[3];
+      for (int d = 0; d < D; ++d) {
+        const bool hi = (a >> d) & 1;
+        f[d] = hi ? qx[q * D + d] : 1.0 - qx[q * D + d];
+        g[d] = hi ? 1.0 : -1.0;
+      }
+      double v = 1.0;
+      for (int d = 0; d < D; ++d) v *= f[d];
+      phi[(size_t)q * nv + a] = v;
+      for (int k = 0; k < D; ++k) {
+        double dv = 1.0;
+        for (int d = 0; d < D; ++d) dv *= (d == k) ? g[d] : f[d];
+        dphi[((size_t)q * nv + a) * D + k] = dv;
+      }
+    }
+}
+
+// Reference tables of a uniform Cartesian cell with sizes h (FP64, same steps as the
+// per-cell integral with Jt = diag(h)).
+static void cartesian_tables(int D, const double* h, int nq, const std::vector<double>& qx,
+                             const std::vector<double>& qw, std::vector<double>& out) {
+  const int nv = 1 << D;
+  std::vector<double> phi, dphi;
+  q1_shapes(D, nq, qx.data(), phi, dphi);
+  out.assign((size_t)nv * nv * 2 + nv + (size_t)nq * nv, 0.0);
+  double* K = out.data();
+  double* M = K + nv * nv;
+  double* m = M + nv * nv;
+  double* PW = m + nv;
+  double det = 1.0;
+  for (int d = 0; d < D; ++d) det *= h[d];
+  for (int q = 0; q < nq; ++q) {
+    const double dV = std::fabs(det) * qw[q];
+    double g[8][3];
+    for (int a = 0; a < nv; ++a)
+      for (int k = 0; k < D; ++k) g[a][k] = (1.0 / h[k]) * dphi[((size_t)q * nv + a) * D + k];
+    for (int j = 0; j < nv; ++j)
+      for (int i = 0; i < nv; ++i) {
+        double s = 0.0;
+        for (int k = 0; k < D; ++k) s += g[i][k] * g[j][k];
+        K[i + j * nv] += s * dV;
+        M[i + j * nv] += (phi[(size_t)q * nv + i] * phi[(size_t)q * nv + j]) * dV;
+      }
+    for (int i = 0; i < nv; ++i) {
+      m[i] += phi[(size_t)q * nv + i] * dV;
+      PW[q * nv + i] = phi[(size_t)q * nv + i] * dV;
+    }
+  }
+}
+
+// ---- host: fused integrate + assemble -----------------------------------------------------
+int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* d_b) {
+  const int D = p->dim;
+  if (p->reffe != GFE_REFFE_Q1 || p->ncomp != 1 || p->form != GFE_FORM_DIFFUSION)
+    return set_error(GFE_ERR_UNSUPPORTED, "assemble: only scalar Q1 diffusion is provided");
+  if (D != 2 && D != 3) return set_error(GFE_ERR_UNSUPPORTED, "assemble: dim must be 2 or 3");
+  const int nv = 1 << D;
+  if (p->nd != nv) return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: nd != 2^dim for Q1");
+  if (A && (A->ncells != p->ncells || A->nd != p->nd))
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: matrix pattern built for other cells");
+  std::vector<double> qx, qw;
+  GFE_TRY(tensor_quadrature(D, p->degree, qx, qw));
+  const int nq = (int)qw.size();
+  const int64_t ncells = p->ncells;
+  const bool fp32 = p->precision == GFE_PREC_FP32;
+
+  // coefficient / source to the device
+  const double* d_coef = nullptr;
+  if (p->coef_kind == GFE_COEF_CONST || p->coef_kind == GFE_COEF_CELL) {
+    const size_t n = p->coef_kind == GFE_COEF_CELL ? (size_t)ncells : 1;
+    const void* v;
+    GFE_TRY(device_view(ctx, p->coef, sizeof(double) * n, SCR_COEF, &v));
+    d_coef = (const double*)v;
+    k_check_finite<<<grid_for((int64_t)n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+        d_coef, (int64_t)n, ctx->d_err);
+    ctx->launches++;
+  }
+  int src_kind = p->source_kind;
+  const double* d_src = nullptr;
+  if (src_kind == GFE_SRC_CONST || src_kind == GFE_SRC_NODAL || src_kind == GFE_SRC_QPOINT) {
+    const void* v;
+    GFE_TRY(device_view(ctx, p->source, sizeof(double) * p->source_len, SCR_SRC, &v));
+    d_src = (const double*)v;
+  } else if (src_kind == GFE_SRC_SINSUM) {
+    if (p->geometry != GFE_GEOM_CARTESIAN)
+      return set_error(GFE_ERR_UNSUPPORTED, "assemble: SINSUM source needs Cartesian cells");
+    const int nterms = (int)p->source[0];
+    if (nterms < 0 || p->source_len < 1 + (int64_t)nterms * (1 + D))
+      return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: malformed SINSUM source");
+    // terms + quadrature points to the device, evaluate f at all quadrature points
+    const size_t tb = sizeof(double) * (size_t)nterms * (1 + D), qb = sizeof(double) * qx.size();
+    GFE_TRY(ctx->scratch[SCR_TMP2].reserve(tb + qb + 64));
+    double* dterms = ctx->scratch[SCR_TMP2].as<double>();
+    double* dqx = dterms + (size_t)nterms * (1 + D);
+    if (tb) GFE_CUDA_TRY(cudaMemcpyAsync(dterms, p->source + 1, tb, cudaMemcpyHostToDevice,
+                                         ctx->stream));
+    GFE_CUDA_TRY(cudaMemcpyAsync(dqx, qx.data(), qb, cudaMemcpyHostToDevice, ctx->stream));
+    GFE_TRY(ctx->scratch[SCR_SRC].reserve(sizeof(double) * (size_t)ncells * nq));
+    double h[3] = {1, 1, 1}, o[3] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) {
+      o[d] = p->domain[2 * d];
+      h[d] = (p->domain[2 * d + 1] - p->domain[2 * d]) / (double)p->partition[d];
+    }
+    const int64_t nt = ncells * nq;
+    if (D == 2)
+      k_sinsum_qpoints<2><<<grid_for(nt, 256), 256, 0, ctx->stream>>>(
+          ncells, p->partition[0], p->partition[1], o[0], o[1], o[2], h[0], h[1], h[2], dqx, nq,
+          dterms, nterms, ctx->scratch[SCR_SRC].as<double>());
+    else
+      k_sinsum_qpoints<3><<<grid_for(nt, 256), 256, 0, ctx->stream>>>(
+          ncells, p->partition[0], p->partition[1], o[0], o[1], o[2], h[0], h[1], h[2], dqx, nq,
+          dterms, nterms, ctx->scratch[SCR_SRC].as<double>());
+    ctx->launches++;
+    d_src = ctx->scratch[SCR_SRC].as<double>();
+    src_kind = GFE_SRC_QPOINT;
+  }
+  if (d_src && src_kind != GFE_SRC_NONE) {
+    const int64_t n = src_kind == GFE_SRC_QPOINT ? ncells * nq : p->source_len;
+    k_check_finite<<<grid_for(n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(d_src, n,
+                                                                              ctx->d_err);
+    ctx->launches++;
+  }
+  GFE_CUDA_TRY(cudaGetLastError());
+
+  // rows of the assembly: the matrix's rows, or (vector only) the problem's cell ids
+  gfe_matrix* R = A;
+  gfe_matrix tmp;
+  if (!R) {
+    tmp.ctx = ctx;
+    tmp.nrows = p->nfree;
+    tmp.ncols = p->nfree;
+    tmp.nd = p->nd;
+    tmp.ncells = ncells;
+    const void* v;
+    const size_t idsz = sizeof(int32_t) * (size_t)ncells * p->nd;
+    GFE_TRY(device_view(ctx, p->cell_dof_ids, idsz, SCR_CELLIDS, &v));
+    GFE_TRY(tmp.cell_rows.reserve(idsz));
+    GFE_CUDA_TRY(cudaMemcpyAsync(tmp.cell_rows.ptr, v, idsz, cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
+    GFE_TRY(build_refs(ctx, &tmp));
+    R = &tmp;
+  }
+  int maxw = 1;
+  if (A) GFE_TRY(max_row_width(ctx, A, &maxw));
+
+  if (p->geometry == GFE_GEOM_CARTESIAN) {
+    double h[3] = {1, 1, 1};
+    for (int d = 0; d < D; ++d)
+      h[d] = (p->domain[2 * d + 1] - p->domain[2 * d]) / (double)p->partition[d];
+    std::vector<double> tabs;
+    cartesian_tables(D, h, nq, qx, qw, tabs);
+    GFE_TRY(ctx->scratch[SCR_TMP1].reserve(sizeof(double) * tabs.size()));
+    GFE_CUDA_TRY(cudaMemcpyAsync(ctx->scratch[SCR_TMP1].ptr, tabs.data(),
+                                 sizeof(double) * tabs.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    const int32_t* cn = nullptr;
+    if (p->cell_node_ids && src_kind == GFE_SRC_NODAL) {
+      const void* v;
+      GFE_TRY(device_view(ctx, p->cell_node_ids, sizeof(int32_t) * (size_t)ncells * nv,
+                          SCR_CELLNODES, &v));
+      cn = (const int32_t*)v;
+    }
+    RowArgs a = row_args(ctx, R, d_b, A != nullptr);
+    if (!A) a.rowptr = nullptr;
+#define GFE_CART(DD, F32)                                                               \
+  {                                                                                     \
+    CartesianDiffusionQ1<DD, F32> s;                                                    \
+    s.tables = ctx->scratch[SCR_TMP1].as<double>();                                     \
+    s.nq = nq;                                                                          \
+    s.coef_kind = p->coef_kind;                                                         \
+    s.coef = d_coef;                                                                    \
+    s.src_kind = src_kind;                                                              \
+    s.src = d_src;                                                                      \
+    s.n0 = p->partition[0];                                                             \
+    s.n1 = p->partition[1];                                                             \
+    s.cell_nodes = cn;                                                                  \
+    s.ntab = (int)tabs.size();                                                          \
+    if (A) {                                                                            \
+      GFE_TRY(run_rows(ctx, a, s, maxw));                                               \
+    } else {                                                                            \
+      GFE_TRY(vector_only_rows(ctx, a, s));                                             \
+    }                                                                                   \
+  }
+    if (D == 2 && !fp32) GFE_CART(2, false)
+    else if (D == 2) GFE_CART(2, true)
+    else if (!fp32) GFE_CART(3, false)
+    else GFE_CART(3, true)
+#undef GFE_CART
+  } else {
+    // nodal geometry: element kernel into entry-major scratch, then the row gather
+    if (!p->node_coords || !p->cell_node_ids)
+      return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: nodal geometry needs coordinates");
+    const void* vc;
+    const void* vn;
+    GFE_TRY(device_view(ctx, p->node_coords, sizeof(double) * (size_t)p->nnodes * D, SCR_COORDS,
+                        &vc));
+    GFE_TRY(device_view(ctx, p->cell_node_ids, sizeof(int32_t) * (size_t)ncells * nv,
+                        SCR_CELLNODES, &vn));
+    std::vector<double> phi, dphi;
+    q1_shapes(D, nq, qx.data(), phi, dphi);
+    std::vector<double> tabs(qw);
+    tabs.insert(tabs.end(), phi.begin(), phi.end());
+    tabs.insert(tabs.end(), dphi.begin(), dphi.end());
+    GFE_TRY(ctx->scratch[SCR_TMP1].reserve(sizeof(double) * tabs.size()));
+    GFE_CUDA_TRY(cudaMemcpyAsync(ctx->scratch[SCR_TMP1].ptr, tabs.data(),
+                                 sizeof(double) * tabs.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    GFE_TRY(ctx->scratch[SCR_CELLMAT].reserve(sizeof(double) * (size_t)ncells * nv * nv));
+    GFE_TRY(ctx->scratch[SCR_CELLVEC].reserve(sizeof(double) * (size_t)ncells * nv));
+    const size_t sm = sizeof(double) * tabs.size();
+    const int blk = 128;
+    if (D == 2) {
+      if (fp32)
+        k_q1_cells_nodal<2, float><<<grid_for(ncells, blk), blk, sm, ctx->stream>>>(
+            ncells, (const int32_t*)vn, (const double*)vc, ctx->scratch[SCR_TMP1].as<double>(),
+            nq, p->coef_kind, d_coef, src_kind, d_src, ctx->scratch[SCR_CELLMAT].as<double>(),
+            ctx->scratch[SCR_CELLVEC].as<double>(), ctx->d_err);
+      else
+        k_q1_cells_nodal<2, double><<<grid_for(ncells, blk), blk, sm, ctx->stream>>>(
+            ncells, (const int32_t*)vn, (const double*)vc, ctx->scratch[SCR_TMP1].as<double>(),
+            nq, p->coef_kind, d_coef, src_kind, d_src, ctx->scratch[SCR_CELLMAT].as<double>(),
+            ctx->scratch[SCR_CELLVEC].as<double>(), ctx->d_err);
+    } else {
+      if (fp32)
+        k_q1_cells_nodal<3, float><<<grid_for(ncells, blk), blk, sm, ctx->stream>>>(
+            ncells, (const int32_t*)vn, (const double*)vc, ctx->scratch[SCR_TMP1].as<double>(),
+            nq, p->coef_kind, d_coef, src_kind, d_src, ctx->scratch[SCR_CELLMAT].as<double>(),
+            ctx->scratch[SCR_CELLVEC].as<double>(), ctx->d_err);
+      else
+        k_q1_cells_nodal<3, double><<<grid_for(ncells, blk), blk, sm, ctx->stream>>>(
+            ncells, (const int32_t*)vn, (const double*)vc, ctx->scratch[SCR_TMP1].as<double>(),
+            nq, p->coef_kind, d_coef, src_kind, d_src, ctx->scratch[SCR_CELLMAT].as<double>(),
+            ctx->scratch[SCR_CELLVEC].as<double>(), ctx->d_err);
+    }
+    ctx->launches++;
+    GFE_CUDA_TRY(cudaGetLastError());
+    GFE_TRY(check_device_error(ctx, "assemble (cell integrals)"));
+    StoredCells s{};
+    s.mat = ctx->scratch[SCR_CELLMAT].as<double>();
+    s.vec = ctx->scratch[SCR_CELLVEC].as<double>();
+    s.cs = 1;
+    s.es = ncells;
+    s.vcs = 1;
+    s.ves = ncells;
+    s.ntab = 0;
+    RowArgs a = row_args(ctx, R, d_b, A != nullptr);
+    if (A) {
+      GFE_TRY(run_rows(ctx, a, s, maxw));
+    } else {
+      GFE_TRY(vector_only_rows(ctx, a, s));
+    }
+  }
+  if (!A) GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // tmp freed at return
+  return check_device_error(ctx, "assemble_matrix_and_vector");
+}
+
+}  // namespace gfe

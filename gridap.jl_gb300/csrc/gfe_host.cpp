@@ -1,0 +1,279 @@
+// gfe_host.cpp -- host-side set-up of libgfe: errors, device buffers, Cartesian model
+// arrays, face labels, CLagrangian dof numbering and quadrature tables.
+//
+// This is the part of Gridap's FE-space construction that fixes the sparsity pattern
+// (dof numbering runs once per mesh on the host); it produces exactly the arrays Gridap
+// hands across the boundary, so callers without Gridap get identical numbering.
+#include <cmath>
+#include <cstring>
+
+#include "gfe_internal.h"
+
+namespace gfe {
+
+// ---- errors -------------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+const char* g_last_error_ptr() { return g_last_error.c_str(); }
+
+// ---- device buffers -----------------------------------------------------------------------
+DevBuf::~DevBuf() { release(); }
+
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+int DevBuf::reserve(size_t nbytes) {
+  if (nbytes <= bytes && ptr) return GFE_OK;
+  release();
+  size_t n = nbytes < 256 ? 256 : nbytes;
+  cudaError_t e = cudaMalloc(&ptr, n);
+  if (e != cudaSuccess) {
+    ptr = nullptr;
+    (void)cudaGetLastError();
+    return set_error(GFE_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu bytes) failed: %s", n,
+                     cudaGetErrorString(e));
+  }
+  bytes = n;
+  return GFE_OK;
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int device_view(gfe_ctx* ctx, const void* p, size_t n, int slot, const void** out) {
+  if (!p || n == 0) {
+    *out = p;
+    return GFE_OK;
+  }
+  if (is_device_ptr(p)) {
+    *out = p;
+    return GFE_OK;
+  }
+  GFE_TRY(ctx->scratch[slot].reserve(n));
+  GFE_CUDA_TRY(cudaMemcpyAsync(ctx->scratch[slot].ptr, p, n, cudaMemcpyHostToDevice,
+                               ctx->stream));
+  *out = ctx->scratch[slot].ptr;
+  return GFE_OK;
+}
+
+int copy_out(gfe_ctx* ctx, void* dst, const void* src, size_t n) {
+  if (n == 0) return GFE_OK;
+  GFE_CUDA_TRY(cudaMemcpyAsync(dst, src, n, cudaMemcpyDefault, ctx->stream));
+  if (!is_device_ptr(dst)) GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return GFE_OK;
+}
+
+int check_device_error(gfe_ctx* ctx, const char* where) {
+  DevError h;
+  GFE_CUDA_TRY(cudaMemcpyAsync(&h, ctx->d_err, sizeof(DevError), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (h.code != GFE_OK) {
+    GFE_CUDA_TRY(cudaMemsetAsync(ctx->d_err, 0, sizeof(DevError), ctx->stream));
+    const char* what = "device error";
+    switch (h.code) {
+      case GFE_ERR_DEGENERATE_CELL: what = "degenerate cell (det J <= 0 or not finite)"; break;
+      case GFE_ERR_ROW_TOO_WIDE: what = "matrix row wider than supported"; break;
+      case GFE_ERR_INVALID_ARGUMENT: what = "id out of range"; break;
+      case GFE_ERR_NONFINITE: what = "non-finite value"; break;
+      case GFE_ERR_TIMEOUT: what = "bounded wait ran out"; break;
+      default: break;
+    }
+    return set_error(h.code, "%s: %s at index %lld", where, what, h.index);
+  }
+  return GFE_OK;
+}
+
+// ---- quadrature ---------------------------------------------------------------------------
+// Gauss-Legendre rule with n points: Newton's method on the Legendre three-term recurrence
+// from the Tricomi initial guesses; nodes/weights mapped from [-1,1] to [0,1]. Tensor
+// product over dimensions, first coordinate fastest, weight = product of 1-D weights.
+static void gauss01(int n, double* x, double* w) {
+  // extended precision for the iteration and the weight formula, rounded at the end
+  typedef long double R;
+  const R pi = 3.141592653589793238462643383279502884L;
+  auto legendre = [n](R t, R* pn, R* pn1) {
+    R pm = 1.0L, pc = t;
+    for (int k = 1; k < n; ++k) {
+      const R pk = ((2 * k + 1) * t * pc - k * pm) / (k + 1);
+      pm = pc;
+      pc = pk;
+    }
+    *pn = pc;
+    *pn1 = pm;
+  };
+  for (int i = 1; i <= n; ++i) {
+    R t = std::cos(pi * (4.0L * i - 1.0L) / (4.0L * n + 2.0L));
+    for (int it = 0; it < 64; ++it) {
+      R pn, pn1;
+      legendre(t, &pn, &pn1);
+      const R dpn = (n == 1) ? 1.0L : n * (pn1 - t * pn) / (1.0L - t * t);
+      const R step = pn / dpn;
+      t -= step;
+      if (std::fabs(step) <= 1e-30L) break;
+    }
+    R pn, pn1;
+    legendre(t, &pn, &pn1);
+    const R dpn = (n == 1) ? 1.0L : n * (pn1 - t * pn) / (1.0L - t * t);
+    const int j = n - i;  // ascending order
+    x[j] = (double)(0.5L * (t + 1.0L));
+    w[j] = (double)(1.0L / ((1.0L - t * t) * dpn * dpn));
+  }
+}
+
+int tensor_quadrature(int D, int degree, std::vector<double>& x, std::vector<double>& w) {
+  if (D < 1 || D > 3 || degree < 0 || degree > 60)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "quadrature: bad dim %d / degree %d", D, degree);
+  int n = degree / 2 + 1;
+  double x1[32], w1[32];
+  gauss01(n, x1, w1);
+  int np = 1;
+  for (int d = 0; d < D; ++d) np *= n;
+  x.assign((size_t)np * D, 0.0);
+  w.assign(np, 1.0);
+  for (int k = 0; k < np; ++k) {
+    int r = k;
+    for (int d = 0; d < D; ++d) {
+      int i = r % n;
+      r /= n;
+      x[(size_t)k * D + d] = x1[i];
+      w[k] *= w1[i];
+    }
+  }
+  return GFE_OK;
+}
+
+}  // namespace gfe
+
+using namespace gfe;
+
+// ---- Cartesian model ----------------------------------------------------------------------
+// Entity id of a point of the box [0,1]^D lying in the interior of the face with extrusion
+// mask `e` (bit d set = the face spans direction d) and anchor mask `a` (bit d set = on the
+// upper side of direction d). Faces are ranked by dimension, then by extrusion mask, then by
+// anchor mask compressed to the non-extruded directions -- Gridap's n-cube face order
+// (ReferenceFEs/ExtrusionPolytopes.jl:460-481).
+static int32_t box_entity(int D, unsigned e, unsigned a) {
+  int k = __builtin_popcount(e);
+  static const int binom[4][4] = {{1, 0, 0, 0}, {1, 1, 0, 0}, {1, 2, 1, 0}, {1, 3, 3, 1}};
+  int id = 0;
+  for (int j = 0; j < k; ++j) id += binom[D][j] << (D - j);  // faces of lower dimension
+  int rank_e = 0;
+  for (unsigned m = 0; m < e; ++m)
+    if (__builtin_popcount(m) == k) ++rank_e;
+  int rank_a = 0, bit = 0;
+  for (int d = 0; d < D; ++d) {
+    if (e & (1u << d)) continue;
+    if (a & (1u << d)) rank_a |= 1 << bit;
+    ++bit;
+  }
+  return 1 + id + rank_e * (1 << (D - k)) + rank_a;
+}
+
+extern "C" int gfe_cartesian_model(int dim, const int64_t* partition, const double* domain,
+                                   double* node_coords, int32_t* cell_node_ids,
+                                   int32_t* node_entity) {
+  clear_error();
+  if (dim < 1 || dim > 3 || !partition)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_cartesian_model: bad dim or partition");
+  int64_t n[3] = {1, 1, 1}, np[3] = {1, 1, 1};
+  double x0[3] = {0, 0, 0}, h[3] = {1, 1, 1};
+  for (int d = 0; d < dim; ++d) {
+    if (partition[d] < 1)
+      return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_cartesian_model: partition[%d] < 1", d);
+    n[d] = partition[d];
+    np[d] = n[d] + 1;
+    if (domain) {
+      x0[d] = domain[2 * d];
+      h[d] = (domain[2 * d + 1] - domain[2 * d]) / (double)n[d];
+    }
+  }
+  const int64_t nnodes = np[0] * np[1] * np[2];
+  if (node_coords || node_entity) {
+    for (int64_t id = 0; id < nnodes; ++id) {
+      int64_t I[3] = {id % np[0], (id / np[0]) % np[1], id / (np[0] * np[1])};
+      unsigned e = 0, a = 0;
+      for (int d = 0; d < dim; ++d) {
+        if (node_coords) node_coords[id * dim + d] = x0[d] + (double)I[d] * h[d];
+        if (I[d] != 0 && I[d] != n[d]) e |= 1u << d;
+        if (I[d] == n[d]) a |= 1u << d;
+      }
+      if (node_entity) node_entity[id] = box_entity(dim, e, a);
+    }
+  }
+  if (cell_node_ids) {
+    const int nv = 1 << dim;
+    const int64_t ncells = n[0] * n[1] * n[2];
+    for (int64_t c = 0; c < ncells; ++c) {
+      int64_t i = c % n[0], j = (c / n[0]) % n[1], k = c / (n[0] * n[1]);
+      int64_t base = i + np[0] * (j + np[1] * k);
+      for (int l = 0; l < nv; ++l) {
+        int64_t off = (l & 1) + ((l >> 1) & 1) * np[0] + ((l >> 2) & 1) * np[0] * np[1];
+        cell_node_ids[c * nv + l] = (int32_t)(base + off + 1);
+      }
+    }
+  }
+  return GFE_OK;
+}
+
+extern "C" int gfe_clagrangian_dofs(int64_t nnodes, const int8_t* node_to_tag, int ncomp,
+                                    const uint8_t* tag_masks, int64_t ncells, int nv,
+                                    const int32_t* cell_node_ids,
+                                    const int32_t* lnode_comp_to_ldof,
+                                    int32_t* node_comp_to_dof, int32_t* cell_dof_ids,
+                                    int32_t* nfree, int32_t* ndiri) {
+  clear_error();
+  if (nnodes < 0 || ncomp < 1 || !node_to_tag || !node_comp_to_dof || !nfree || !ndiri)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_clagrangian_dofs: bad arguments");
+  int64_t f = 0, g = 0;
+  for (int64_t node = 0; node < nnodes; ++node) {
+    const int tag = node_to_tag[node];
+    for (int c = 0; c < ncomp; ++c) {
+      const bool diri = tag > 0 && tag_masks && tag_masks[(size_t)(tag - 1) * ncomp + c];
+      node_comp_to_dof[node * ncomp + c] = diri ? (int32_t)-(++g) : (int32_t)(++f);
+    }
+  }
+  if (f > INT32_MAX || g > INT32_MAX)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_clagrangian_dofs: too many dofs");
+  *nfree = (int32_t)f;
+  *ndiri = (int32_t)g;
+  if (cell_dof_ids && cell_node_ids) {
+    const int ndc = nv * ncomp;
+    for (int64_t cell = 0; cell < ncells; ++cell)
+      for (int l = 0; l < nv; ++l) {
+        const int64_t node = cell_node_ids[cell * nv + l] - 1;
+        if (node < 0 || node >= nnodes)
+          return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_clagrangian_dofs: node id %lld",
+                           (long long)(node + 1));
+        for (int c = 0; c < ncomp; ++c) {
+          const int ld = lnode_comp_to_ldof ? lnode_comp_to_ldof[l * ncomp + c]
+                                            : c * nv + l + 1;  // component-major local
+          cell_dof_ids[cell * ndc + ld - 1] = node_comp_to_dof[node * ncomp + c];
+        }
+      }
+  }
+  return GFE_OK;
+}

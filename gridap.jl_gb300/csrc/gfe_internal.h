@@ -1,0 +1,153 @@
+// gfe_internal.h -- shared definitions of libgfe (not part of the public ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/gfe.h"
+
+namespace gfe {
+
+// ---- errors -------------------------------------------------------------------------------
+int set_error(int code, const char* fmt, ...);
+void clear_error();
+const char* g_last_error_ptr();
+
+#define GFE_CUDA_TRY(expr)                                                                 \
+  do {                                                                                     \
+    cudaError_t e_ = (expr);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return ::gfe::set_error(e_ == cudaErrorMemoryAllocation ? GFE_ERR_OUT_OF_MEMORY      \
+                                                              : GFE_ERR_CUDA,              \
+                              "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_),      \
+                              __FILE__, __LINE__);                                         \
+  } while (0)
+
+#define GFE_TRY(expr)            \
+  do {                           \
+    int s_ = (expr);             \
+    if (s_ != GFE_OK) return s_; \
+  } while (0)
+
+// Device-side error word: kernels write the first failure code and an index.
+struct DevError {
+  int code;
+  int pad;
+  long long index;
+};
+
+// ---- device buffers -----------------------------------------------------------------------
+// A growable device allocation owned by a context or matrix.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  ~DevBuf();
+  int reserve(size_t nbytes);  // keeps contents only if no growth is needed
+  void release();
+  template <class T>
+  T* as() const { return static_cast<T*>(ptr); }
+};
+
+// ---- context ------------------------------------------------------------------------------
+struct ScratchSlot;
+
+}  // namespace gfe
+
+struct gfe_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  long long launches = 0;
+  gfe::DevError* d_err = nullptr;  // device error word
+  // named scratch buffers reused across calls
+  gfe::DevBuf scratch[16];
+  // pinned staging for small device->host reads
+  void* h_pinned = nullptr;
+};
+
+struct gfe_matrix {
+  gfe_ctx* ctx = nullptr;
+  int64_t nrows = 0, ncols = 0, nnz = 0;
+  int32_t nd = 0;
+  int64_t ncells = 0;
+  // CSR pattern and values (0-based, int32 indices)
+  gfe::DevBuf rowptr, colval, val;
+  // cell ids the pattern was built from (device copies)
+  gfe::DevBuf cell_rows, cell_cols;
+  // row -> (cell*nd + local) references, sorted by cell: the row-gather assembly lists
+  gfe::DevBuf ref_ptr, refs;
+  // solver plan (sliced ELL copy with 32-row slices), built lazily
+  bool plan_valid = false;
+  int64_t nslices = 0, sell_nnz = 0;
+  gfe::DevBuf sell_ptr, sell_col, sell_val64, sell_val32, dinv64, dinv32;
+};
+
+namespace gfe {
+
+// scratch slot ids in gfe_ctx::scratch
+enum ScratchId {
+  SCR_TMP0 = 0,
+  SCR_TMP1,
+  SCR_TMP2,
+  SCR_TMP3,
+  SCR_CELLIDS,
+  SCR_COEF,
+  SCR_SRC,
+  SCR_CELLMAT,
+  SCR_CELLVEC,
+  SCR_COORDS,
+  SCR_CELLNODES,
+  SCR_VEC_B,
+  SCR_VEC_X,
+  SCR_SOLVER,
+  SCR_SOLVER2,
+  SCR_REDUCE
+};
+
+// pointer classification
+bool is_device_ptr(const void* p);
+// Returns a device view of `n` bytes at `p`: `p` itself if it is device memory, else an
+// async H2D copy into scratch slot `slot`.
+int device_view(gfe_ctx* ctx, const void* p, size_t n, int slot, const void** out);
+// Copies n bytes from device memory `src` to `dst` (host or device) and waits if host.
+int copy_out(gfe_ctx* ctx, void* dst, const void* src, size_t n);
+// Reads and resets the device error word; returns its code (GFE_OK if none).
+int check_device_error(gfe_ctx* ctx, const char* where);
+
+inline unsigned grid_for(int64_t n, int block, int64_t cap = 1 << 30) {
+  int64_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (unsigned)g;
+}
+
+// ---- kernel launch wrappers implemented in the .cu files ----------------------------------
+// exclusive scan of n int64 counts (in) to out[0..n] (out[n] = total). in/out device.
+int scan_exclusive_i64(gfe_ctx* ctx, const int64_t* in, int64_t* out, int64_t n);
+int scan_exclusive_i32_to_i64(gfe_ctx* ctx, const int32_t* in, int64_t* out, int64_t n);
+int narrow_i64_to_i32(gfe_ctx* ctx, const int64_t* in, int32_t* out, int64_t n);
+
+// pattern (gfe_pattern.cu)
+int build_refs(gfe_ctx* ctx, gfe_matrix* A);
+int build_pattern(gfe_ctx* ctx, gfe_matrix* A);
+
+// assembly (gfe_assemble.cu)
+int assemble_cellmats(gfe_ctx* ctx, gfe_matrix* A, const double* d_cellmats);
+int assemble_cellvecs(gfe_ctx* ctx, int64_t ncells, int nd, const int32_t* d_rows,
+                      const double* d_cellvecs, int64_t nrows, double* d_b);
+int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* d_b);
+
+// solver (gfe_solve.cu)
+int build_solver_plan(gfe_ctx* ctx, gfe_matrix* A);
+int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d_b,
+          double* d_x, gfe_solve_report* rep);
+int spmv64(gfe_ctx* ctx, gfe_matrix* A, const double* d_x, double* d_y);
+
+// host set-up (gfe_host.cpp)
+int tensor_quadrature(int D, int degree, std::vector<double>& x, std::vector<double>& w);
+
+}  // namespace gfe

@@ -1,0 +1,343 @@
+// gfe_pattern.cu -- symbolic assembly on the device: from cell dof ids to the CSR pattern.
+//
+// Gridap builds the pattern with a counting pass over all (row, col) touches of every cell
+// (duplicates included), an over-allocated CSC, binary-search insertion and a compaction
+// (FESpaces/SparseMatrixAssemblers.jl:174-210, Algebra/SparseMatrixCSC.jl:72-283). The
+// result is a function of the cell ids alone: per column, the sorted unique rows that some
+// cell couples to it. Here the same set is computed row by row without any insertion:
+//
+//   1. refs:   for every row r, the flattened positions e = cell*nd + li with
+//              cell_rows[e] == r+1, in ascending order (so cells in ascending order);
+//   2. widths: thread per row, the union of the positive column ids of the cells in its
+//              ref list, kept sorted and unique in registers/local memory;
+//   3. scan of widths -> rowptr; second pass writes colval.
+//
+// Both the pattern and the ref lists are reused by every numeric assembly afterwards.
+#include "gfe_internal.h"
+
+namespace gfe {
+
+// ---- scans --------------------------------------------------------------------------------
+constexpr int kScanBlock = 512;
+constexpr int kScanItems = 4;  // per thread
+constexpr int kScanTile = kScanBlock * kScanItems;
+
+template <class TIn>
+__global__ void k_scan_tiles(const TIn* __restrict__ in, int64_t* __restrict__ out, int64_t n,
+                             int64_t* __restrict__ tile_sums) {
+  __shared__ int64_t s[kScanBlock];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int64_t v[kScanItems];
+  int64_t run = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    int64_t idx = base + i;
+    v[i] = idx < n ? (int64_t)in[idx] : 0;
+    run += v[i];
+  }
+  s[threadIdx.x] = run;
+  __syncthreads();
+  // Hillis-Steele inclusive scan of per-thread totals
+  for (int off = 1; off < kScanBlock; off <<= 1) {
+    int64_t t = threadIdx.x >= off ? s[threadIdx.x - off] : 0;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  int64_t excl = s[threadIdx.x] - run;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    int64_t idx = base + i;
+    if (idx < n) out[idx] = excl;
+    excl += v[i];
+  }
+  if (threadIdx.x == kScanBlock - 1) tile_sums[blockIdx.x] = s[kScanBlock - 1];
+}
+
+__global__ void k_add_tile_offsets(int64_t* __restrict__ out, int64_t n,
+                                   const int64_t* __restrict__ tile_offsets) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < n) out[idx] += tile_offsets[idx / kScanTile];
+}
+
+__global__ void k_set_total(int64_t* out, int64_t n, const int64_t* last_in_excl,
+                            const int64_t* tile_total) {
+  (void)last_in_excl;
+  out[n] = *tile_total;
+}
+
+// out has n+1 entries; out[n] = sum. Tiles scanned, tile sums scanned recursively.
+template <class TIn>
+static int scan_impl(gfe_ctx* ctx, const TIn* in, int64_t* out, int64_t n, int depth) {
+  if (depth > 6) return set_error(GFE_ERR_INVALID_ARGUMENT, "scan: input too large");
+  const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+  const int64_t nt = ntiles < 1 ? 1 : ntiles;
+  DevBuf sums;  // tile sums and their scan (small; allocated per level)
+  GFE_TRY(sums.reserve(sizeof(int64_t) * (2 * nt + 2)));
+  int64_t* tile_sums = sums.as<int64_t>();
+  int64_t* tile_offs = tile_sums + nt;  // nt+1 entries
+  if (n > 0) {
+    k_scan_tiles<TIn><<<(unsigned)nt, kScanBlock, 0, ctx->stream>>>(in, out, n, tile_sums);
+    ctx->launches++;
+  } else {
+    GFE_CUDA_TRY(cudaMemsetAsync(tile_sums, 0, sizeof(int64_t), ctx->stream));
+  }
+  if (nt > 1) {
+    GFE_TRY(scan_impl<int64_t>(ctx, tile_sums, tile_offs, nt, depth + 1));
+    k_add_tile_offsets<<<grid_for(n, 256), 256, 0, ctx->stream>>>(out, n, tile_offs);
+    ctx->launches++;
+    k_set_total<<<1, 1, 0, ctx->stream>>>(out, n, nullptr, tile_offs + nt);
+    ctx->launches++;
+  } else {
+    k_set_total<<<1, 1, 0, ctx->stream>>>(out, n, nullptr, tile_sums);
+    ctx->launches++;
+  }
+  GFE_CUDA_TRY(cudaGetLastError());
+  // `sums` is freed at scope exit: make sure the kernels reading it are done.
+  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return GFE_OK;
+}
+
+int scan_exclusive_i64(gfe_ctx* ctx, const int64_t* in, int64_t* out, int64_t n) {
+  return scan_impl<int64_t>(ctx, in, out, n, 0);
+}
+int scan_exclusive_i32_to_i64(gfe_ctx* ctx, const int32_t* in, int64_t* out, int64_t n) {
+  return scan_impl<int32_t>(ctx, in, out, n, 0);
+}
+
+__global__ void k_narrow(const int64_t* __restrict__ in, int32_t* __restrict__ out, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (int32_t)in[i];
+}
+
+int narrow_i64_to_i32(gfe_ctx* ctx, const int64_t* in, int32_t* out, int64_t n) {
+  k_narrow<<<grid_for(n, 256), 256, 0, ctx->stream>>>(in, out, n);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+// ---- device error helper ------------------------------------------------------------------
+__device__ __forceinline__ void raise(DevError* err, int code, long long index) {
+  if (atomicCAS(&err->code, 0, code) == 0) err->index = index;
+}
+
+// ---- 1. row -> cell references ------------------------------------------------------------
+__global__ void k_count_refs(const int32_t* __restrict__ ids, int64_t n, int64_t nrows,
+                             int32_t* __restrict__ cnt, DevError* err) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t d = ids[e];
+    if (d > 0) {
+      if (d > nrows) {
+        raise(err, GFE_ERR_INVALID_ARGUMENT, e);
+        continue;
+      }
+      atomicAdd(&cnt[d - 1], 1);
+    }
+  }
+}
+
+__global__ void k_fill_refs(const int32_t* __restrict__ ids, int64_t n, int64_t nrows,
+                            const int64_t* __restrict__ ptr, int32_t* __restrict__ fill,
+                            int32_t* __restrict__ refs) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t d = ids[e];
+    if (d > 0 && d <= nrows) {
+      const int32_t slot = atomicAdd(&fill[d - 1], 1);
+      refs[ptr[d - 1] + slot] = (int32_t)e;
+    }
+  }
+}
+
+// Atomic slots arrive in any order; sorting each (short) list restores ascending cells.
+__global__ void k_sort_refs(const int64_t* __restrict__ ptr, int32_t* __restrict__ refs,
+                            int64_t nrows) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int64_t a = ptr[r], b = ptr[r + 1];
+  for (int64_t i = a + 1; i < b; ++i) {
+    const int32_t v = refs[i];
+    int64_t j = i - 1;
+    while (j >= a && refs[j] > v) {
+      refs[j + 1] = refs[j];
+      --j;
+    }
+    refs[j + 1] = v;
+  }
+}
+
+// ---- 2./3. row widths and column lists ---------------------------------------------------
+// Insert c into the sorted unique list cols[0..n); returns the new length (MAXW+1 signals
+// overflow).
+template <int MAXW>
+__device__ __forceinline__ int insert_unique(int32_t* cols, int n, int32_t c) {
+  int pos = n;
+  while (pos > 0 && cols[pos - 1] > c) --pos;
+  if (pos > 0 && cols[pos - 1] == c) return n;
+  if (n >= MAXW) return MAXW + 1;
+  for (int k = n; k > pos; --k) cols[k] = cols[k - 1];
+  cols[pos] = c;
+  return n + 1;
+}
+
+template <int MAXW, bool WRITE>
+__global__ void k_row_pattern(int64_t nrows, int nd, const int64_t* __restrict__ ref_ptr,
+                              const int32_t* __restrict__ refs,
+                              const int32_t* __restrict__ cell_cols, int64_t ncols,
+                              int64_t* __restrict__ width, const int64_t* __restrict__ rowptr,
+                              int32_t* __restrict__ colval, DevError* err) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  int32_t cols[MAXW];
+  int n = 0;
+  for (int64_t q = ref_ptr[r]; q < ref_ptr[r + 1]; ++q) {
+    const int32_t e = refs[q];
+    const int32_t cell = e / nd;
+    const int32_t* cc = cell_cols + (int64_t)cell * nd;
+    for (int lj = 0; lj < nd; ++lj) {
+      const int32_t c = cc[lj];
+      if (c <= 0) continue;
+      if (c > ncols) {
+        raise(err, GFE_ERR_INVALID_ARGUMENT, (long long)cell * nd + lj);
+        continue;
+      }
+      n = insert_unique<MAXW>(cols, n, c - 1);
+      if (n > MAXW) {
+        raise(err, GFE_ERR_ROW_TOO_WIDE, r);
+        return;
+      }
+    }
+  }
+  if (!WRITE) {
+    width[r] = n;
+  } else {
+    const int64_t start = rowptr[r];
+    for (int k = 0; k < n; ++k) colval[start + k] = cols[k];
+  }
+}
+
+template <int MAXW>
+static void launch_row_pattern(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cell_cols,
+                               bool write, int64_t* width, const int64_t* rowptr64) {
+  const int64_t* ref_ptr = A->ref_ptr.as<int64_t>();
+  if (!write)
+    k_row_pattern<MAXW, false><<<grid_for(A->nrows, 128), 128, 0, ctx->stream>>>(
+        A->nrows, A->nd, ref_ptr, A->refs.as<int32_t>(), cell_cols, A->ncols, width, nullptr,
+        nullptr, ctx->d_err);
+  else
+    k_row_pattern<MAXW, true><<<grid_for(A->nrows, 128), 128, 0, ctx->stream>>>(
+        A->nrows, A->nd, ref_ptr, A->refs.as<int32_t>(), cell_cols, A->ncols, nullptr,
+        rowptr64, A->colval.as<int32_t>(), ctx->d_err);
+  ctx->launches++;
+}
+
+static void row_pattern(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cell_cols, bool write,
+                        int64_t* width, const int64_t* rowptr64, int maxw) {
+  if (maxw <= 32)
+    launch_row_pattern<32>(ctx, A, cell_cols, write, width, rowptr64);
+  else if (maxw <= 64)
+    launch_row_pattern<64>(ctx, A, cell_cols, write, width, rowptr64);
+  else if (maxw <= 128)
+    launch_row_pattern<128>(ctx, A, cell_cols, write, width, rowptr64);
+  else
+    launch_row_pattern<512>(ctx, A, cell_cols, write, width, rowptr64);
+}
+
+__global__ void k_max_i32(const int32_t* __restrict__ v, int64_t n, int32_t* out) {
+  int32_t m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    m = v[i] > m ? v[i] : m;
+  for (int off = 16; off > 0; off >>= 1) {
+    int32_t o = __shfl_down_sync(0xffffffffu, m, off);
+    m = o > m ? o : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// ---- driver -------------------------------------------------------------------------------
+// Row references of A->cell_rows: A->ref_ptr (int64, nrows+1) and A->refs (sorted).
+int build_refs(gfe_ctx* ctx, gfe_matrix* A) {
+  const int64_t n = A->ncells * A->nd;
+  if (n > (int64_t)INT32_MAX)
+    return set_error(GFE_ERR_UNSUPPORTED, "assembly: ncells*nd = %lld exceeds int32",
+                     (long long)n);
+  const int32_t* rows = A->cell_rows.as<int32_t>();
+  const int64_t nrows = A->nrows;
+  GFE_TRY(ctx->scratch[SCR_TMP0].reserve(sizeof(int32_t) * (nrows + 1)));
+  int32_t* cnt = ctx->scratch[SCR_TMP0].as<int32_t>();
+  GFE_TRY(A->ref_ptr.reserve(sizeof(int64_t) * (nrows + 1)));
+  GFE_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nrows + 1), ctx->stream));
+  const unsigned g = grid_for(n, 256, (int64_t)ctx->num_sms * 16);
+  k_count_refs<<<g, 256, 0, ctx->stream>>>(rows, n, nrows, cnt, ctx->d_err);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  GFE_TRY(check_device_error(ctx, "assembly (row ids)"));
+  GFE_TRY(scan_exclusive_i32_to_i64(ctx, cnt, A->ref_ptr.as<int64_t>(), nrows));
+  int64_t nrefs = 0;
+  GFE_TRY(copy_out(ctx, &nrefs, A->ref_ptr.as<int64_t>() + nrows, sizeof(int64_t)));
+  GFE_TRY(A->refs.reserve(sizeof(int32_t) * (nrefs > 0 ? nrefs : 1)));
+  GFE_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nrows + 1), ctx->stream));
+  k_fill_refs<<<g, 256, 0, ctx->stream>>>(rows, n, nrows, A->ref_ptr.as<int64_t>(), cnt,
+                                          A->refs.as<int32_t>());
+  ctx->launches++;
+  k_sort_refs<<<grid_for(nrows, 256), 256, 0, ctx->stream>>>(A->ref_ptr.as<int64_t>(),
+                                                             A->refs.as<int32_t>(), nrows);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
+  const int32_t* cols = A->cell_cols.as<int32_t>();
+  const int64_t nrows = A->nrows;
+  // 1. refs (ctx scratch TMP0 keeps the per-row reference counts afterwards)
+  GFE_TRY(build_refs(ctx, A));
+  const int32_t* cnt = ctx->scratch[SCR_TMP0].as<int32_t>();
+
+  // 2. widths. The local column list is sized by a template bound: the largest number of
+  // cells sharing a row times nd (capped by ncols) picks the smallest adequate bound; rows
+  // wider than the largest bound raise GFE_ERR_ROW_TOO_WIDE.
+  int maxw;
+  {
+    DevBuf dmax;
+    GFE_TRY(dmax.reserve(sizeof(int32_t)));
+    GFE_CUDA_TRY(cudaMemsetAsync(dmax.ptr, 0, sizeof(int32_t), ctx->stream));
+    k_max_i32<<<grid_for(nrows, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+        cnt, nrows, dmax.as<int32_t>());
+    ctx->launches++;
+    int32_t hmax = 0;
+    GFE_TRY(copy_out(ctx, &hmax, dmax.ptr, sizeof(int32_t)));
+    int64_t bound = (int64_t)hmax * A->nd;
+    if (bound > A->ncols) bound = A->ncols;
+    maxw = bound < 1 ? 1 : (bound > 512 ? 512 : (int)bound);
+  }
+  DevBuf width, rowptr64;
+  GFE_TRY(width.reserve(sizeof(int64_t) * (nrows + 1)));
+  GFE_TRY(rowptr64.reserve(sizeof(int64_t) * (nrows + 1)));
+  row_pattern(ctx, A, cols, false, width.as<int64_t>(), nullptr, maxw);
+  GFE_CUDA_TRY(cudaGetLastError());
+  GFE_TRY(check_device_error(ctx, "symbolic_loop_matrix (column ids)"));
+  GFE_TRY(scan_exclusive_i64(ctx, width.as<int64_t>(), rowptr64.as<int64_t>(), nrows));
+  int64_t nnz = 0;
+  GFE_TRY(copy_out(ctx, &nnz, rowptr64.as<int64_t>() + nrows, sizeof(int64_t)));
+  if (nnz > (int64_t)INT32_MAX - 64)
+    return set_error(GFE_ERR_UNSUPPORTED, "symbolic_loop_matrix: nnz %lld exceeds int32",
+                     (long long)nnz);
+  A->nnz = nnz;
+  GFE_TRY(A->rowptr.reserve(sizeof(int32_t) * (nrows + 1)));
+  GFE_TRY(A->colval.reserve(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
+  GFE_TRY(A->val.reserve(sizeof(double) * (nnz > 0 ? nnz : 1)));
+  GFE_TRY(narrow_i64_to_i32(ctx, rowptr64.as<int64_t>(), A->rowptr.as<int32_t>(), nrows + 1));
+  row_pattern(ctx, A, cols, true, nullptr, rowptr64.as<int64_t>(), maxw);
+  GFE_CUDA_TRY(cudaGetLastError());
+  GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * (nnz > 0 ? nnz : 1),
+                               ctx->stream));
+  GFE_TRY(check_device_error(ctx, "symbolic_loop_matrix (fill)"));
+  A->plan_valid = false;
+  return GFE_OK;
+}
+
+}  // namespace gfe

@@ -1,0 +1,544 @@
+// gfe_solve.cu -- Krylov solvers on the device: FP64 PCG and FP32-inner / FP64-refinement
+// PCG, the LinearSolver a Gridap user plugs in through solve!(x, ns, b)
+// (Algebra/LinearSolvers.jl:58-129,202-209).
+//
+// Matrix layout for the solver: a sliced-ELL copy of the CSR with 32-row slices. Slice s
+// stores its rows' k-th entries contiguously (entry k of row 32s+l at ptr[s] + 32k + l),
+// padded to the slice's widest row. One thread owns one row: every load of values and
+// column ids is a full 32-lane coalesced transaction and each row's sum is a chain of FMAs
+// in one thread -- no shuffle reductions. On GB300 an FP64 warp instruction costs the same
+// whatever the active-lane mask, so thread-per-row also minimises FP64 instruction issue.
+//
+// Each CG iteration is three kernels (SpMV+dot, update+dots, direction update). Dot products
+// reduce deterministically: fixed grids, per-block partials, the last block to finish sums
+// the partials in a fixed order and computes the scalar (alpha, beta) on the device. A done
+// flag set on the device makes later kernels return immediately, so the host launches
+// chunks of iterations and checks convergence once per chunk.
+#include <cmath>
+
+#include "gfe_internal.h"
+
+namespace gfe {
+
+constexpr int kVecBlock = 256;
+constexpr int kSpmvBlock = 256;
+
+struct SolverState {
+  double bb;      // ||b||^2 of the system being solved
+  double tol2;    // rtol^2 * bb
+  double rz;      // r.z
+  double rz_new;
+  double rr;      // r.r
+  double pq;      // p.Ap
+  double alpha, beta;
+  int iter, done, converged, maxit;
+  unsigned ticket[4];
+};
+
+__device__ __forceinline__ void raise_e(DevError* err, int code, long long index) {
+  if (atomicCAS(&err->code, 0, code) == 0) err->index = index;
+}
+
+// Block sum of a double (all threads get the result in thread 0).
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NT / 32; ++i) s += sh[i];
+  __syncthreads();
+  return s;
+}
+
+// Called by every block after writing its partial(s). Returns true in the last block, with
+// the partial sums of all blocks reduced in block order into out[0..nv).
+template <int NT, int NV>
+__device__ bool last_block_reduce(unsigned* ticket, const double* partials, int nblocks,
+                                  double* out, double* sh) {
+  __shared__ bool last;
+  __threadfence();
+  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  for (int v = 0; v < NV; ++v) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nblocks; i += NT) s += __ldcg(partials + (size_t)i * NV + v);
+    s = block_sum<NT>(s, sh);
+    if (threadIdx.x == 0) out[v] = s;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+  return true;
+}
+
+// ---- sliced-ELL plan ----------------------------------------------------------------------
+__global__ void k_slice_widths(const int32_t* __restrict__ rowptr, int64_t nrows,
+                               int64_t nslices, int64_t* __restrict__ w) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslices) return;
+  int32_t m = 0;
+  for (int l = 0; l < 32; ++l) {
+    const int64_t r = s * 32 + l;
+    if (r < nrows) {
+      const int32_t n = rowptr[r + 1] - rowptr[r];
+      m = n > m ? n : m;
+    }
+  }
+  w[s] = (int64_t)m * 32;
+}
+
+__global__ void k_sell_fill(const int32_t* __restrict__ rowptr,
+                            const int32_t* __restrict__ colval, const double* __restrict__ val,
+                            int64_t nrows, int64_t nslices, const int64_t* __restrict__ sptr,
+                            int32_t* __restrict__ scol, double* __restrict__ sv64,
+                            float* __restrict__ sv32, double* __restrict__ dinv64,
+                            float* __restrict__ dinv32) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nslices * 32) return;
+  const int64_t s = r >> 5;
+  const int l = (int)(r & 31);
+  const int64_t base = sptr[s];
+  const int32_t w = (int32_t)((sptr[s + 1] - base) >> 5);
+  int32_t start = 0, n = 0;
+  if (r < nrows) {
+    start = rowptr[r];
+    n = rowptr[r + 1] - start;
+  }
+  double diag = 0.0;
+  for (int32_t k = 0; k < w; ++k) {
+    const int64_t idx = base + (int64_t)k * 32 + l;
+    int32_t c = r < nrows ? (int32_t)r : 0;
+    double v = 0.0;
+    if (k < n) {
+      c = colval[start + k];
+      v = val[start + k];
+      if (c == r) diag = v;
+    }
+    scol[idx] = c;
+    sv64[idx] = v;
+    sv32[idx] = (float)v;
+  }
+  if (r < nrows) {
+    const double d = (diag != 0.0 && isfinite(diag)) ? 1.0 / diag : 1.0;
+    dinv64[r] = d;
+    dinv32[r] = (float)d;
+  }
+}
+
+int build_solver_plan(gfe_ctx* ctx, gfe_matrix* A) {
+  if (A->plan_valid) return GFE_OK;
+  const int64_t nrows = A->nrows;
+  const int64_t nslices = (nrows + 31) / 32;
+  DevBuf w;
+  GFE_TRY(w.reserve(sizeof(int64_t) * (nslices + 1)));
+  GFE_TRY(A->sell_ptr.reserve(sizeof(int64_t) * (nslices + 1)));
+  k_slice_widths<<<grid_for(nslices, 256), 256, 0, ctx->stream>>>(A->rowptr.as<int32_t>(), nrows,
+                                                                  nslices, w.as<int64_t>());
+  ctx->launches++;
+  GFE_TRY(scan_exclusive_i64(ctx, w.as<int64_t>(), A->sell_ptr.as<int64_t>(), nslices));
+  int64_t total = 0;
+  GFE_TRY(copy_out(ctx, &total, A->sell_ptr.as<int64_t>() + nslices, sizeof(int64_t)));
+  A->nslices = nslices;
+  A->sell_nnz = total;
+  GFE_TRY(A->sell_col.reserve(sizeof(int32_t) * (total > 0 ? total : 1)));
+  GFE_TRY(A->sell_val64.reserve(sizeof(double) * (total > 0 ? total : 1)));
+  GFE_TRY(A->sell_val32.reserve(sizeof(float) * (total > 0 ? total : 1)));
+  GFE_TRY(A->dinv64.reserve(sizeof(double) * (nrows > 0 ? nrows : 1)));
+  GFE_TRY(A->dinv32.reserve(sizeof(float) * (nrows > 0 ? nrows : 1)));
+  k_sell_fill<<<grid_for(nslices * 32, 256), 256, 0, ctx->stream>>>(
+      A->rowptr.as<int32_t>(), A->colval.as<int32_t>(), A->val.as<double>(), nrows, nslices,
+      A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(),
+      A->sell_val32.as<float>(), A->dinv64.as<double>(), A->dinv32.as<float>());
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // w freed at return
+  A->plan_valid = true;
+  return GFE_OK;
+}
+
+// ---- SpMV ---------------------------------------------------------------------------------
+// y = A x on the sliced-ELL copy; thread per row, FMA chain in the accumulation type of TV.
+template <typename TV, typename TX>
+__device__ __forceinline__ TV sell_row(int64_t r, const int64_t* __restrict__ sptr,
+                                       const int32_t* __restrict__ scol,
+                                       const TV* __restrict__ sval, const TX* __restrict__ x) {
+  const int64_t s = r >> 5;
+  const int l = (int)(r & 31);
+  const int64_t base = __ldg(sptr + s) + l;
+  const int32_t w = (int32_t)((__ldg(sptr + s + 1) - __ldg(sptr + s)) >> 5);
+  TV acc = (TV)0;
+  int32_t k = 0;
+  for (; k + 4 <= w; k += 4) {
+    const int64_t i = base + (int64_t)k * 32;
+    const int32_t c0 = __ldcs(scol + i), c1 = __ldcs(scol + i + 32), c2 = __ldcs(scol + i + 64),
+                  c3 = __ldcs(scol + i + 96);
+    const TV v0 = __ldcs(sval + i), v1 = __ldcs(sval + i + 32), v2 = __ldcs(sval + i + 64),
+             v3 = __ldcs(sval + i + 96);
+    acc = fma(v0, (TV)__ldg(x + c0), acc);
+    acc = fma(v1, (TV)__ldg(x + c1), acc);
+    acc = fma(v2, (TV)__ldg(x + c2), acc);
+    acc = fma(v3, (TV)__ldg(x + c3), acc);
+  }
+  for (; k < w; ++k) {
+    const int64_t i = base + (int64_t)k * 32;
+    acc = fma(__ldcs(sval + i), (TV)__ldg(x + __ldcs(scol + i)), acc);
+  }
+  return acc;
+}
+
+template <typename TV, typename TX, typename TY>
+__global__ void __launch_bounds__(kSpmvBlock)
+    k_spmv(int64_t nrows, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
+           const TV* __restrict__ sval, const TX* __restrict__ x, TY* __restrict__ y) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  y[r] = (TY)sell_row<TV, TX>(r, sptr, scol, sval, x);
+}
+
+int spmv64(gfe_ctx* ctx, gfe_matrix* A, const double* d_x, double* d_y) {
+  GFE_TRY(build_solver_plan(ctx, A));
+  k_spmv<double, double, double><<<grid_for(A->nrows, kSpmvBlock), kSpmvBlock, 0, ctx->stream>>>(
+      A->nrows, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(),
+      A->sell_val64.as<double>(), d_x, d_y);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+// ---- CG kernels (T: vector/matrix type; dot products accumulate in double) ----------------
+// q = A p and partial p.q; the last block computes alpha = rz / pq.
+template <typename T>
+__global__ void __launch_bounds__(kSpmvBlock)
+    k_cg_spmv_dot(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
+                  const T* __restrict__ sval, const T* __restrict__ p, T* __restrict__ q,
+                  double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kSpmvBlock / 32];
+  if (S->done) return;
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double d = 0.0;
+  if (r < n) {
+    const T y = sell_row<T, T>(r, sptr, scol, sval, p);
+    q[r] = y;
+    d = (double)p[r] * (double)y;
+  }
+  d = block_sum<kSpmvBlock>(d, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = d;
+  double tot[1];
+  if (last_block_reduce<kSpmvBlock, 1>(&S->ticket[0], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->pq = tot[0];
+    S->alpha = tot[0] != 0.0 ? S->rz / tot[0] : 0.0;
+  }
+}
+
+// x += alpha p; r -= alpha q; partial r.z (z = dinv r) and r.r; the last block decides.
+template <typename T>
+__global__ void __launch_bounds__(kVecBlock)
+    k_cg_update(int64_t n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                const T* __restrict__ q, const T* __restrict__ dinv,
+                double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kVecBlock / 32];
+  if (S->done) return;
+  const T alpha = (T)S->alpha;
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = fma(alpha, p[i], x[i]);
+    const T ri = fma(-alpha, q[i], r[i]);
+    r[i] = ri;
+    rz += (double)ri * (double)(dinv[i] * ri);
+    rr += (double)ri * (double)ri;
+  }
+  rz = block_sum<kVecBlock>(rz, sh);
+  rr = block_sum<kVecBlock>(rr, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = rz;
+    partials[2 * blockIdx.x + 1] = rr;
+  }
+  double tot[2];
+  if (last_block_reduce<kVecBlock, 2>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->iter += 1;
+    S->rr = tot[1];
+    if (!isfinite(tot[1]) || !isfinite(tot[0])) {
+      S->done = 1;
+      S->converged = 0;
+    } else if (tot[1] <= S->tol2) {
+      S->done = 1;
+      S->converged = 1;
+    } else if (S->iter >= S->maxit) {
+      S->done = 1;
+    }
+    S->beta = S->rz != 0.0 ? tot[0] / S->rz : 0.0;
+    S->rz = tot[0];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kVecBlock)
+    k_cg_direction(int64_t n, T* __restrict__ p, const T* __restrict__ r,
+                   const T* __restrict__ dinv, const SolverState* S) {
+  if (S->done) return;
+  const T beta = (T)S->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = fma(beta, p[i], dinv[i] * r[i]);
+}
+
+// CG start from x = 0: r = s*rhs (T), z = dinv r, p = z; partials of r.z and r.r.
+template <typename T, typename TR>
+__global__ void __launch_bounds__(kVecBlock)
+    k_cg_init(int64_t n, const TR* __restrict__ rhs, double scale, T* __restrict__ x,
+              T* __restrict__ r, T* __restrict__ p, const T* __restrict__ dinv,
+              double* __restrict__ partials, SolverState* S, double rtol2) {
+  __shared__ double sh[kVecBlock / 32];
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T ri = (T)((double)rhs[i] * scale);
+    x[i] = (T)0;
+    r[i] = ri;
+    const T zi = dinv[i] * ri;
+    p[i] = zi;
+    rz += (double)ri * (double)zi;
+    rr += (double)ri * (double)ri;
+  }
+  rz = block_sum<kVecBlock>(rz, sh);
+  rr = block_sum<kVecBlock>(rr, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = rz;
+    partials[2 * blockIdx.x + 1] = rr;
+  }
+  double tot[2];
+  if (last_block_reduce<kVecBlock, 2>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->rz = tot[0];
+    S->rr = tot[1];
+    S->bb = tot[1];
+    S->tol2 = rtol2 * tot[1];
+    S->iter = 0;
+    S->converged = 0;
+    S->done = (tot[1] == 0.0) ? 1 : 0;
+    if (tot[1] == 0.0) S->converged = 1;
+  }
+}
+
+// FP64 residual of the refinement loop: r = b - A x (A in FP64), partial r.r.
+__global__ void __launch_bounds__(kSpmvBlock)
+    k_residual64(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
+                 const double* __restrict__ sval, const double* __restrict__ x,
+                 const double* __restrict__ b, double* __restrict__ r,
+                 double* __restrict__ partials, double* out_rr, unsigned* ticket) {
+  __shared__ double sh[kSpmvBlock / 32];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double d = 0.0;
+  if (i < n) {
+    const double ri = b[i] - sell_row<double, double>(i, sptr, scol, sval, x);
+    r[i] = ri;
+    d = ri * ri;
+  }
+  d = block_sum<kSpmvBlock>(d, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = d;
+  double tot[1];
+  if (last_block_reduce<kSpmvBlock, 1>(ticket, partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0)
+    *out_rr = tot[0];
+}
+
+// x64 += s * d32
+__global__ void k_refine_update(int64_t n, double* __restrict__ x, const float* __restrict__ d,
+                                double s) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += s * (double)d[i];
+}
+
+__global__ void k_dot_self(int64_t n, const double* __restrict__ v, double* __restrict__ partials,
+                           double* out, unsigned* ticket) {
+  __shared__ double sh[kVecBlock / 32];
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s += v[i] * v[i];
+  s = block_sum<kVecBlock>(s, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+  double tot[1];
+  if (last_block_reduce<kVecBlock, 1>(ticket, partials, gridDim.x, tot, sh) && threadIdx.x == 0)
+    *out = tot[0];
+}
+
+// ---- host drivers -------------------------------------------------------------------------
+struct SolverWork {
+  SolverState* S;      // device
+  SolverState* hS;     // pinned host mirror
+  double* partials;    // device
+  unsigned* tickets;   // device (inside S)
+};
+
+static int read_state(gfe_ctx* ctx, SolverWork& w) {
+  GFE_CUDA_TRY(cudaMemcpyAsync(w.hS, w.S, sizeof(SolverState), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return GFE_OK;
+}
+
+// Runs PCG on A (values of type T) for rhs*scale from x=0 until done; returns iterations.
+template <typename T>
+static int run_pcg(gfe_ctx* ctx, gfe_matrix* A, const T* sval, const T* dinv, const void* rhs,
+                   bool rhs_is_double, double scale, T* x, T* r, T* p, T* q, double rtol,
+                   int maxit, int check_every, SolverWork& w, int* iters, int* converged) {
+  const int64_t n = A->nrows;
+  const unsigned gv = (unsigned)(ctx->num_sms * 4);
+  const unsigned gs = grid_for(n, kSpmvBlock);
+  GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
+  int maxit_field = maxit;
+  GFE_CUDA_TRY(cudaMemcpyAsync(&w.S->maxit, &maxit_field, sizeof(int), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  if (rhs_is_double)
+    k_cg_init<T, double><<<gv, kVecBlock, 0, ctx->stream>>>(
+        n, (const double*)rhs, scale, x, r, p, dinv, w.partials, w.S, rtol * rtol);
+  else
+    k_cg_init<T, float><<<gv, kVecBlock, 0, ctx->stream>>>(n, (const float*)rhs, scale, x, r, p,
+                                                          dinv, w.partials, w.S, rtol * rtol);
+  ctx->launches++;
+  const int64_t* sptr = A->sell_ptr.as<int64_t>();
+  const int32_t* scol = A->sell_col.as<int32_t>();
+  int done_iters = 0;
+  for (;;) {
+    for (int k = 0; k < check_every; ++k) {
+      k_cg_spmv_dot<T><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, sptr, scol, sval, p, q,
+                                                           w.partials, w.S);
+      k_cg_update<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
+      k_cg_direction<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
+      ctx->launches += 3;
+    }
+    GFE_CUDA_TRY(cudaGetLastError());
+    GFE_TRY(read_state(ctx, w));
+    done_iters = w.hS->iter;
+    if (w.hS->done) break;
+  }
+  *iters = done_iters;
+  *converged = w.hS->converged;
+  return GFE_OK;
+}
+
+int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d_b,
+          double* d_x, gfe_solve_report* rep) {
+  if (A->nrows != A->ncols)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "solve: matrix is not square");
+  GFE_TRY(build_solver_plan(ctx, A));
+  const int64_t n = A->nrows;
+  const int check_every = o->check_every > 0 ? o->check_every : 25;
+  const int maxit = o->maxiter > 0 ? o->maxiter : 100000;
+  // work vectors: FP64 r, p, q (CG) or FP64 r + FP32 x, r, p, q (IR)
+  const size_t n8 = sizeof(double) * (size_t)(n > 0 ? n : 1);
+  GFE_TRY(ctx->scratch[SCR_SOLVER].reserve(n8 * 3 + 64));
+  GFE_TRY(ctx->scratch[SCR_SOLVER2].reserve(n8 * 2 + 64));
+  const size_t npart = (size_t)grid_for(n, kSpmvBlock) * 2 + (size_t)ctx->num_sms * 8 + 64;
+  GFE_TRY(ctx->scratch[SCR_REDUCE].reserve(sizeof(SolverState) + sizeof(double) * npart + 256));
+  SolverWork w;
+  w.S = ctx->scratch[SCR_REDUCE].as<SolverState>();
+  w.partials = (double*)((char*)ctx->scratch[SCR_REDUCE].ptr + 256);
+  w.hS = (SolverState*)ctx->h_pinned;
+  // The precondition switch: Jacobi uses 1/diag, none uses ones (same kernels).
+  const bool jac = o->precond == GFE_PC_JACOBI;
+  if (!jac && o->precond != GFE_PC_NONE)
+    return set_error(GFE_ERR_UNSUPPORTED, "solve: unknown preconditioner %d", o->precond);
+  double* v64 = ctx->scratch[SCR_SOLVER].as<double>();
+  const double* dinv64 = A->dinv64.as<double>();
+  const float* dinv32 = A->dinv32.as<float>();
+  DevBuf ones;
+  if (!jac) {
+    GFE_TRY(ones.reserve(n8 + sizeof(float) * n + 64));
+    std::vector<double> h1(n, 1.0);
+    std::vector<float> h1f(n, 1.0f);
+    GFE_CUDA_TRY(cudaMemcpyAsync(ones.ptr, h1.data(), n8, cudaMemcpyHostToDevice, ctx->stream));
+    GFE_CUDA_TRY(cudaMemcpyAsync((char*)ones.ptr + n8, h1f.data(), sizeof(float) * n,
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    dinv64 = ones.as<double>();
+    dinv32 = (const float*)((char*)ones.ptr + n8);
+  }
+  rep->iterations = 0;
+  rep->refinements = 0;
+  rep->converged = 0;
+  rep->status = GFE_OK;
+  rep->relres = 0.0;
+
+  if (o->method == GFE_SOLVER_CG) {
+    double* r = v64;
+    double* p = v64 + n;
+    double* q = v64 + 2 * n;
+    int it = 0, conv = 0;
+    GFE_TRY(run_pcg<double>(ctx, A, A->sell_val64.as<double>(), dinv64, d_b, true, 1.0, d_x, r,
+                            p, q, o->rtol, maxit, check_every, w, &it, &conv));
+    rep->iterations = it;
+  } else if (o->method == GFE_SOLVER_IR_CG) {
+    double* r64 = v64;  // FP64 residual
+    float* f = (float*)ctx->scratch[SCR_SOLVER2].ptr;
+    float* x32 = f;
+    float* r32 = f + n;
+    float* p32 = f + 2 * n;
+    float* q32 = f + 3 * n;
+    const unsigned gv = (unsigned)(ctx->num_sms * 4);
+    double* rr_dev = &w.S->rr;
+    // x = 0, r = b, ||b||^2
+    GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
+    GFE_CUDA_TRY(cudaMemcpyAsync(r64, d_b, n8, cudaMemcpyDeviceToDevice, ctx->stream));
+    GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
+    k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, rr_dev, &w.S->ticket[2]);
+    ctx->launches++;
+    GFE_TRY(read_state(ctx, w));
+    const double bb = w.hS->rr;
+    const double tol2 = o->rtol * o->rtol * bb;
+    double rr = bb;
+    const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
+    int total = 0, outer = 0;
+    while (rr > tol2 && total < maxit && bb > 0.0) {
+      const double s = 1.0 / std::sqrt(rr);
+      int it = 0, conv = 0;
+      GFE_TRY(run_pcg<float>(ctx, A, A->sell_val32.as<float>(), dinv32, r64, true, s, x32, r32,
+                             p32, q32, inner, maxit - total, check_every, w, &it, &conv));
+      total += it;
+      ++outer;
+      k_refine_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32, 1.0 / s);
+      k_residual64<<<grid_for(n, kSpmvBlock), kSpmvBlock, 0, ctx->stream>>>(
+          n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(),
+          d_x, d_b, r64, w.partials, rr_dev, &w.S->ticket[2]);
+      ctx->launches += 2;
+      GFE_CUDA_TRY(cudaGetLastError());
+      GFE_TRY(read_state(ctx, w));
+      rr = w.hS->rr;
+      if (!std::isfinite(rr)) break;
+      if (outer > 200) break;
+    }
+    rep->iterations = total;
+    rep->refinements = outer;
+  } else {
+    return set_error(GFE_ERR_UNSUPPORTED, "solve: unknown method %d", o->method);
+  }
+  // true FP64 residual of the returned x
+  {
+    double* r = v64;
+    const unsigned gs = grid_for(n, kSpmvBlock);
+    k_residual64<<<gs, kSpmvBlock, 0, ctx->stream>>>(
+        n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(), d_x,
+        d_b, r, w.partials, &w.S->rr, &w.S->ticket[2]);
+    const unsigned gv = (unsigned)(ctx->num_sms * 4);
+    k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb,
+                                                  &w.S->ticket[3]);
+    ctx->launches += 2;
+    GFE_CUDA_TRY(cudaGetLastError());
+    GFE_TRY(read_state(ctx, w));
+    const double bb = w.hS->bb;
+    rep->relres = bb > 0 ? std::sqrt(w.hS->rr / bb) : 0.0;
+    rep->converged = std::isfinite(rep->relres) && rep->relres <= o->rtol * (1.0 + 1e-6);
+    if (!std::isfinite(rep->relres)) rep->status = GFE_ERR_NONFINITE;
+  }
+  return GFE_OK;
+}
+
+}  // namespace gfe

@@ -1,0 +1,110 @@
+"""LinearSolver protocol (Algebra/LinearSolvers.jl:58-129,202-209) with GPU CG solvers.
+
+Gridap ships no Krylov solver; a user plugs one in through
+symbolic_setup -> numerical_setup -> solve!(x, ns, b). These classes are that plug-in:
+
+  - CGSolver(rtol, maxiter, precond="jacobi"): FP64 preconditioned CG;
+  - IRCGSolver(rtol, inner_rtol, ...): FP32 PCG inside FP64 iterative refinement: the outer
+    loop forms r = b - A x and updates x in FP64, the inner solves A d = r in FP32.
+
+Both stop on the FP64 relative residual ||b - A x|| <= rtol ||b|| and report it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .assembly import AffineFEOperator, DeviceMatrix
+from .fespaces import FEFunction
+
+
+class SolveReport:
+    def __init__(self, r: _lib.SolveReport):
+        self.iterations = r.iterations
+        self.refinements = r.refinements
+        self.converged = bool(r.converged)
+        self.status = r.status
+        self.relres = r.relres
+
+    def __repr__(self):
+        return (f"SolveReport(iterations={self.iterations}, refinements={self.refinements}, "
+                f"converged={self.converged}, relres={self.relres:.3e})")
+
+
+class LinearSolver:
+    method = _lib.GFE_SOLVER_CG
+
+    def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, precond: str = "jacobi",
+                 inner_rtol: float = 1e-4, check_every: int = 0):
+        self.rtol = rtol
+        self.maxiter = maxiter
+        self.precond = {"jacobi": _lib.GFE_PC_JACOBI, "none": _lib.GFE_PC_NONE}[precond]
+        self.inner_rtol = inner_rtol
+        self.check_every = check_every
+
+    def opts(self) -> _lib.SolverOpts:
+        return _lib.SolverOpts(self.method, self.precond, self.rtol, self.maxiter,
+                               self.inner_rtol, self.check_every)
+
+
+class CGSolver(LinearSolver):
+    method = _lib.GFE_SOLVER_CG
+
+
+class IRCGSolver(LinearSolver):
+    method = _lib.GFE_SOLVER_IR_CG
+
+
+class SymbolicSetup:
+    def __init__(self, solver: LinearSolver):
+        self.solver = solver
+
+
+class NumericalSetup:
+    def __init__(self, solver: LinearSolver, A: DeviceMatrix):
+        self.solver = solver
+        self.A = A
+        self.report: SolveReport | None = None
+
+
+def symbolic_setup(solver: LinearSolver, A: DeviceMatrix) -> SymbolicSetup:
+    return SymbolicSetup(solver)
+
+
+def numerical_setup(ss: SymbolicSetup, A: DeviceMatrix) -> NumericalSetup:
+    return NumericalSetup(ss.solver, A)
+
+
+def numerical_setup_(ns: NumericalSetup, A: DeviceMatrix) -> NumericalSetup:
+    ns.A = A
+    return ns
+
+
+def solve_(x, ns: NumericalSetup, b):
+    """solve!(x, ns, b): x (numpy or CUDA tensor) receives the solution."""
+    rep = _lib.SolveReport()
+    o = ns.solver.opts()
+    _lib.check(_lib.load().gfe_solve(ns.A.ctx.handle, ns.A.handle, C.byref(o), _lib.ptr(b),
+                                     _lib.ptr(x), C.byref(rep)))
+    ns.report = SolveReport(rep)
+    return x
+
+
+class LinearFESolver:
+    def __init__(self, ls: LinearSolver | None = None):
+        self.ls = ls or CGSolver()
+
+
+def solve(solver, op: AffineFEOperator):
+    """uh = solve(solver, op): an FEFunction of the trial space; the solver's report is
+    attached as `uh.report`."""
+    ls = solver.ls if isinstance(solver, LinearFESolver) else solver
+    A, b = op.get_matrix(), op.get_vector()
+    x = np.empty_like(b) if isinstance(b, np.ndarray) else b.new_empty(b.shape)
+    ns = numerical_setup(symbolic_setup(ls, A), A)
+    solve_(x, ns, b)
+    uh = FEFunction(op.get_trial(), x)
+    uh.report = ns.report
+    return uh

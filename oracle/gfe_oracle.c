@@ -1,0 +1,652 @@
+/*
+ * gfe_oracle.c -- TEST INFRASTRUCTURE ONLY (the oracle), not part of the product.
+ *
+ * CPU restatement of Gridap.jl v0.20.8's assembly and solve path. The functions follow the
+ * Gridap sources cited beside each one, step by step, including the order in which values
+ * are accumulated, so that the CUDA library can be checked against it entry by entry. The
+ * restatement is pinned by the known-answer values in Gridap's own test suite (see
+ * tests/golden/).
+ */
+#include "gfe_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ====================================================================================== */
+/* polytopes                                                                               */
+/* ====================================================================================== */
+
+/* Gridap enumerates the faces of an extrusion polytope recursively and then applies a
+ * sequence of stable sorts: by anchor[1..D], then extrusion[1..D], then face dimension
+ * (ReferenceFEs/ExtrusionPolytopes.jl:460-481). The last sort is the primary key, so the
+ * final order is: dimension, then extrusion read with its last component most significant,
+ * then anchor read the same way. Every (extrusion, anchor) pair is distinct, so that key
+ * fixes the order regardless of the recursion's initial order. */
+static int ncube_key(int D, const int32_t* ext, const int32_t* anc) {
+  int dim = 0, e = 0, a = 0;
+  for (int d = 0; d < D; ++d) {
+    dim += ext[d] != 0;
+    e |= (ext[d] != 0) << d;
+    a |= (anc[d] != 0) << d;
+  }
+  return (dim << 16) | (e << 8) | a;
+}
+
+int orc_ncube_faces(int D, int32_t* ext, int32_t* anchor) {
+  int n = 0;
+  int32_t e[3], a[3];
+  int keys[27];
+  int32_t tmp_e[27 * 3], tmp_a[27 * 3];
+  for (int em = 0; em < (1 << D); ++em)
+    for (int am = 0; am < (1 << D); ++am) {
+      if (am & em) continue; /* anchor is 0 along extruded directions */
+      for (int d = 0; d < D; ++d) {
+        e[d] = (em >> d) & 1;
+        a[d] = (am >> d) & 1;
+      }
+      memcpy(tmp_e + n * D, e, sizeof(int32_t) * D);
+      memcpy(tmp_a + n * D, a, sizeof(int32_t) * D);
+      keys[n] = ncube_key(D, e, a);
+      ++n;
+    }
+  /* selection by key */
+  int used[27] = {0};
+  for (int k = 0; k < n; ++k) {
+    int best = -1;
+    for (int i = 0; i < n; ++i)
+      if (!used[i] && (best < 0 || keys[i] < keys[best])) best = i;
+    used[best] = 1;
+    memcpy(ext + k * D, tmp_e + best * D, sizeof(int32_t) * D);
+    memcpy(anchor + k * D, tmp_a + best * D, sizeof(int32_t) * D);
+  }
+  return n;
+}
+
+/* ====================================================================================== */
+/* Cartesian model                                                                         */
+/* ====================================================================================== */
+
+/* Node coordinates: x0[d] + (I[d]-1)*dx[d], dx = (hi-lo)/n, nodes in column-major
+ * LinearIndices order (Geometry/CartesianGrids.jl:58-62,115-123). */
+void orc_cartesian_coords(int D, const int64_t* part, const double* domain, double* coords) {
+  int64_t np[3] = {1, 1, 1};
+  double x0[3], dx[3];
+  for (int d = 0; d < D; ++d) {
+    np[d] = part[d] + 1;
+    x0[d] = domain[2 * d];
+    dx[d] = (domain[2 * d + 1] - domain[2 * d]) / (double)part[d];
+  }
+  int64_t node = 0;
+  for (int64_t k = 0; k < np[2]; ++k)
+    for (int64_t j = 0; j < np[1]; ++j)
+      for (int64_t i = 0; i < np[0]; ++i, ++node) {
+        int64_t I[3] = {i, j, k};
+        for (int d = 0; d < D; ++d) coords[node * D + d] = x0[d] + (double)I[d] * dx[d];
+      }
+}
+
+/* Cell nodes: cell (i,j,k) gets nodes[(i,j,k) + lnode] for lnode in CartesianIndices of
+ * 2^D, first index fastest (Geometry/CartesianGrids.jl:152-161). Ids 1-based. */
+void orc_cartesian_cell_nodes(int D, const int64_t* part, int32_t* cell_nodes) {
+  int64_t n[3] = {1, 1, 1}, np[3] = {1, 1, 1};
+  for (int d = 0; d < D; ++d) {
+    n[d] = part[d];
+    np[d] = part[d] + 1;
+  }
+  int nv = 1 << D;
+  int64_t cell = 0;
+  for (int64_t k = 0; k < n[2]; ++k)
+    for (int64_t j = 0; j < n[1]; ++j)
+      for (int64_t i = 0; i < n[0]; ++i, ++cell)
+        for (int a = 0; a < nv; ++a) {
+          int64_t I[3] = {i + (a & 1), j + ((a >> 1) & 1), k + ((a >> 2) & 1)};
+          int64_t id = I[0] + np[0] * (I[1] + np[1] * I[2]);
+          cell_nodes[cell * nv + a] = (int32_t)(id + 1);
+        }
+}
+
+/* A vertex of the Cartesian mesh lies in the interior of exactly one face of the domain
+ * box: extruded along directions where it is strictly inside, anchored at 1 where it sits
+ * on the upper side. Its label is that face's 1-based id in the box polytope
+ * (Geometry/CartesianDiscreteModels.jl:133-189 assigns these entities). */
+void orc_cartesian_node_entity(int D, const int64_t* part, int32_t* node_entity) {
+  int32_t ext[27 * 3], anc[27 * 3];
+  int nf = orc_ncube_faces(D, ext, anc);
+  int64_t np[3] = {1, 1, 1};
+  for (int d = 0; d < D; ++d) np[d] = part[d] + 1;
+  int64_t node = 0;
+  for (int64_t k = 0; k < np[2]; ++k)
+    for (int64_t j = 0; j < np[1]; ++j)
+      for (int64_t i = 0; i < np[0]; ++i, ++node) {
+        int64_t I[3] = {i, j, k};
+        int32_t e[3] = {0, 0, 0}, a[3] = {0, 0, 0};
+        for (int d = 0; d < D; ++d) {
+          if (I[d] == 0) {
+            e[d] = 0; a[d] = 0;
+          } else if (I[d] == part[d]) {
+            e[d] = 0; a[d] = 1;
+          } else {
+            e[d] = 1; a[d] = 0;
+          }
+        }
+        int found = 0;
+        for (int f = 0; f < nf; ++f) {
+          int ok = 1;
+          for (int d = 0; d < D; ++d)
+            if (ext[f * D + d] != e[d] || anc[f * D + d] != a[d]) ok = 0;
+          if (ok) { found = f + 1; break; }
+        }
+        node_entity[node] = found;
+      }
+}
+
+/* get_face_tag_index: the first tag (in the given order) whose entity set contains the
+ * face's entity (Geometry/FaceLabelings.jl:411-427). */
+void orc_node_tag_index(int64_t nnodes, const int32_t* node_entity, int ntags,
+                        const int32_t* tag_ptrs, const int32_t* tag_entities,
+                        int8_t* node_to_tag) {
+  for (int64_t n = 0; n < nnodes; ++n) {
+    node_to_tag[n] = 0;
+    for (int t = 0; t < ntags; ++t) {
+      int hit = 0;
+      for (int32_t p = tag_ptrs[t]; p < tag_ptrs[t + 1]; ++p)
+        if (tag_entities[p] == node_entity[n]) { hit = 1; break; }
+      if (hit) { node_to_tag[n] = (int8_t)(t + 1); break; }
+    }
+  }
+}
+
+void orc_jitter_interior(int D, const int64_t* part, const double* jitter, double* coords) {
+  int64_t np[3] = {1, 1, 1};
+  for (int d = 0; d < D; ++d) np[d] = part[d] + 1;
+  int64_t node = 0;
+  for (int64_t k = 0; k < np[2]; ++k)
+    for (int64_t j = 0; j < np[1]; ++j)
+      for (int64_t i = 0; i < np[0]; ++i, ++node) {
+        int64_t I[3] = {i, j, k};
+        int interior = 1;
+        for (int d = 0; d < D; ++d)
+          if (I[d] == 0 || I[d] == part[d]) interior = 0;
+        if (interior)
+          for (int d = 0; d < D; ++d) coords[node * D + d] += jitter[node * D + d];
+      }
+}
+
+/* ====================================================================================== */
+/* CLagrangian numbering                                                                   */
+/* ====================================================================================== */
+
+/* _generate_node_to_dof_glue_component_major (FESpaces/CLagrangianFESpaces.jl:155-275):
+ * walk nodes in order; for each node walk components; a masked (node,comp) of a tagged
+ * node becomes the next Dirichlet dof (negative), every other one the next free dof.
+ * _fill_cell_dofs_clagrangian! (:356-380) then gathers cell dofs through the local
+ * (node,comp) -> local dof table. */
+void orc_clagrangian_numbering(int64_t nnodes, const int8_t* node_to_tag, int ncomp,
+                               const uint8_t* tag_masks, int64_t ncells, int nv,
+                               const int32_t* cell_nodes, const int32_t* lnode_comp_to_ldof,
+                               int32_t* node_comp_to_dof, int32_t* cell_dofs,
+                               int32_t* nfree, int32_t* ndiri) {
+  int32_t nf = 0, nd = 0;
+  for (int64_t n = 0; n < nnodes; ++n) {
+    int tag = node_to_tag[n];
+    for (int c = 0; c < ncomp; ++c) {
+      int diri = tag != 0 && tag_masks[(tag - 1) * ncomp + c];
+      if (diri)
+        node_comp_to_dof[n * ncomp + c] = -(++nd);
+      else
+        node_comp_to_dof[n * ncomp + c] = ++nf;
+    }
+  }
+  *nfree = nf;
+  *ndiri = nd;
+  int ndof_cell = nv * ncomp;
+  for (int64_t cell = 0; cell < ncells; ++cell)
+    for (int a = 0; a < nv; ++a) {
+      int64_t node = cell_nodes[cell * nv + a] - 1;
+      for (int c = 0; c < ncomp; ++c) {
+        int ldof = lnode_comp_to_ldof[a * ncomp + c];
+        cell_dofs[cell * ndof_cell + ldof - 1] = node_comp_to_dof[node * ncomp + c];
+      }
+    }
+}
+
+/* ====================================================================================== */
+/* quadrature                                                                              */
+/* ====================================================================================== */
+
+/* Gauss-Legendre nodes/weights on [-1,1] by Newton iteration on P_n (the Golub-Welsch
+ * rule gives the same unique nodes), mapped to [0,1] as x=(x+1)/2, w=w/2
+ * (ReferenceFEs/TensorProductQuadratures.jl:68-80). Nodes ascending. */
+void orc_gauss_legendre01(int n, double* x, double* w) {
+  /* evaluated in long double, then rounded: the weights come out within ~0.5 ulp */
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int i = 0; i < n; ++i) {
+    long double z = cosl(pi * (i + 0.75L) / (n + 0.5L));
+    long double p0 = 1.0L, p1 = z, dp = 1.0L;
+    for (int it = 0; it < 100; ++it) {
+      p0 = 1.0L;
+      p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        long double p2 = ((2.0L * k - 1.0L) * z * p1 - (k - 1.0L) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = (n == 1) ? 1.0L : n * (z * p1 - p0) / (z * z - 1.0L);
+      long double dz = p1 / dp;
+      z -= dz;
+      if (fabsl(dz) < 1e-30L) break;
+    }
+    p0 = 1.0L;
+    p1 = z;
+    for (int k = 2; k <= n; ++k) {
+      long double p2 = ((2.0L * k - 1.0L) * z * p1 - (k - 1.0L) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = (n == 1) ? 1.0L : n * (z * p1 - p0) / (z * z - 1.0L);
+    /* z decreases with i: store ascending */
+    x[n - 1 - i] = (double)((z + 1.0L) / 2.0L);
+    w[n - 1 - i] = (double)((2.0L / ((1.0L - z * z) * dp * dp)) / 2.0L);
+  }
+}
+
+/* npoints per direction = div(degree,2)+1 (Quadratures.jl:191); tensor product over
+ * CartesianIndices, first index fastest, w = prod of 1D weights (Quadratures.jl:193-227). */
+int orc_tensor_quadrature(int D, int degree, double* coords, double* weights) {
+  int n = degree / 2 + 1;
+  double x1[64], w1[64];
+  orc_gauss_legendre01(n, x1, w1);
+  int np = 1;
+  for (int d = 0; d < D; ++d) np *= n;
+  for (int k = 0; k < np; ++k) {
+    int r = k;
+    double w = 1.0;
+    for (int d = 0; d < D; ++d) {
+      int i = r % n;
+      r /= n;
+      coords[k * D + d] = x1[i];
+      w *= w1[i];
+    }
+    weights[k] = w;
+  }
+  return np;
+}
+
+/* ====================================================================================== */
+/* Q1 shape functions                                                                      */
+/* ====================================================================================== */
+
+/* Multilinear Lagrange basis on the lexicographically ordered vertices of [0,1]^D (the
+ * node order of Gridap's first-order LagrangianRefFE on QUAD/HEX,
+ * ReferenceFEs/CLagrangianRefFEs.jl:246-275). phi[p*nv+a], dphi[(p*nv+a)*D+k]. */
+void orc_q1_shapes(int D, int npts, const double* pts, double* phi, double* dphi) {
+  int nv = 1 << D;
+  for (int p = 0; p < npts; ++p)
+    for (int a = 0; a < nv; ++a) {
+      double f[3], g[3];
+      for (int d = 0; d < D; ++d) {
+        int b = (a >> d) & 1;
+        double xi = pts[p * D + d];
+        f[d] = b ? xi : 1.0 - xi;
+        g[d] = b ? 1.0 : -1.0;
+      }
+      double v = 1.0;
+      for (int d = 0; d < D; ++d) v *= f[d];
+      phi[p * nv + a] = v;
+      for (int k = 0; k < D; ++k) {
+        double dv = 1.0;
+        for (int d = 0; d < D; ++d) dv *= (d == k) ? g[d] : f[d];
+        dphi[(p * nv + a) * D + k] = dv;
+      }
+    }
+}
+
+/* ====================================================================================== */
+/* tensor algebra of TensorValues/Operations.jl:875-934,989                                */
+/* ====================================================================================== */
+
+/* A[k][l] stored as A[k*D+l]. */
+static double det_t(int D, const double* a) {
+  if (D == 1) return a[0];
+  if (D == 2) return a[0] * a[3] - a[1] * a[2];
+  double a11 = a[0], a12 = a[1], a13 = a[2], a21 = a[3], a22 = a[4], a23 = a[5], a31 = a[6],
+         a32 = a[7], a33 = a[8];
+  return a11 * a22 * a33 + a12 * a23 * a31 + a13 * a21 * a32 -
+         (a11 * a23 * a32 + a12 * a21 * a33 + a13 * a22 * a31);
+}
+
+static void inv_t(int D, const double* a, double* r) {
+  if (D == 1) {
+    r[0] = 1.0 / a[0];
+    return;
+  }
+  if (D == 2) {
+    double c = 1.0 / det_t(2, a);
+    r[0] = a[3] * c;
+    r[1] = -a[1] * c;
+    r[2] = -a[2] * c;
+    r[3] = a[0] * c;
+    return;
+  }
+  double a11 = a[0], a12 = a[1], a13 = a[2], a21 = a[3], a22 = a[4], a23 = a[5], a31 = a[6],
+         a32 = a[7], a33 = a[8];
+  double c = 1.0 / det_t(3, a);
+  r[0] = (a22 * a33 - a23 * a32) * c;
+  r[3] = -(a21 * a33 - a23 * a31) * c;
+  r[6] = (a21 * a32 - a22 * a31) * c;
+  r[1] = -(a12 * a33 - a13 * a32) * c;
+  r[4] = (a11 * a33 - a13 * a31) * c;
+  r[7] = -(a11 * a32 - a12 * a31) * c;
+  r[2] = (a12 * a23 - a13 * a22) * c;
+  r[5] = -(a11 * a23 - a13 * a21) * c;
+  r[8] = (a11 * a22 - a12 * a21) * c;
+}
+
+/* ====================================================================================== */
+/* cell integrals                                                                          */
+/* ====================================================================================== */
+
+void orc_q1_cell_qpoints(int D, int64_t ncells, const int32_t* cell_nodes, const double* coords,
+                         int nq, const double* qx, double* xq) {
+  int nv = 1 << D;
+  double* phi = (double*)malloc(sizeof(double) * nq * nv);
+  double* dphi = (double*)malloc(sizeof(double) * nq * nv * D);
+  orc_q1_shapes(D, nq, qx, phi, dphi);
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int q = 0; q < nq; ++q)
+      for (int l = 0; l < D; ++l) {
+        double s = 0.0;
+        for (int a = 0; a < nv; ++a)
+          s += phi[q * nv + a] * coords[(int64_t)(cell_nodes[c * nv + a] - 1) * D + l];
+        xq[(c * nq + q) * D + l] = s;
+      }
+  free(phi);
+  free(dphi);
+}
+
+int orc_q1_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_nodes,
+                                 const double* coords, int geom, const double* h,
+                                 const double* kappa_cell, int nq, const double* qx,
+                                 const double* qw, int fkind, const double* fdata,
+                                 double* cellmats, double* cellvecs) {
+  int nv = 1 << D;
+  double* phi = (double*)malloc(sizeof(double) * nq * nv);
+  double* dphi = (double*)malloc(sizeof(double) * nq * nv * D);
+  double* g = (double*)malloc(sizeof(double) * nv * D);
+  orc_q1_shapes(D, nq, qx, phi, dphi);
+  for (int64_t c = 0; c < ncells; ++c) {
+    const int32_t* nodes = cell_nodes + c * nv;
+    double* K = cellmats ? cellmats + c * nv * nv : NULL;
+    double* bv = cellvecs ? cellvecs + c * nv : NULL;
+    if (K) memset(K, 0, sizeof(double) * nv * nv);
+    if (bv) memset(bv, 0, sizeof(double) * nv);
+    double kap = kappa_cell ? kappa_cell[c] : 1.0;
+    for (int q = 0; q < nq; ++q) {
+      /* Jt at the quadrature point */
+      double Jt[9] = {0}, iJt[9];
+      if (geom == ORC_GEOM_CARTESIAN) {
+        for (int k = 0; k < D; ++k) Jt[k * D + k] = h[k];
+      } else {
+        for (int a = 0; a < nv; ++a) {
+          const double* xa = coords + (int64_t)(nodes[a] - 1) * D;
+          for (int k = 0; k < D; ++k)
+            for (int l = 0; l < D; ++l) Jt[k * D + l] += dphi[(q * nv + a) * D + k] * xa[l];
+        }
+      }
+      double dJ = det_t(D, Jt);
+      if (!(dJ > 0.0) && !(dJ < 0.0)) {
+        free(phi); free(dphi); free(g);
+        return -1; /* degenerate cell */
+      }
+      inv_t(D, Jt, iJt);
+      double dV = fabs(dJ) * qw[q];
+      /* physical gradients: invJt . grad phi_hat */
+      for (int a = 0; a < nv; ++a)
+        for (int k = 0; k < D; ++k) {
+          double s = 0.0;
+          for (int l = 0; l < D; ++l) s += iJt[k * D + l] * dphi[(q * nv + a) * D + l];
+          g[a * D + k] = s;
+        }
+      if (K) {
+        for (int j = 0; j < nv; ++j)
+          for (int i = 0; i < nv; ++i) {
+            double s = 0.0;
+            if (kappa_cell)
+              for (int k = 0; k < D; ++k) s += (kap * g[i * D + k]) * g[j * D + k];
+            else
+              for (int k = 0; k < D; ++k) s += g[i * D + k] * g[j * D + k];
+            K[i + j * nv] += s * dV;
+          }
+      }
+      if (bv && fkind != ORC_F_NONE) {
+        double fq;
+        if (fkind == ORC_F_CONST) {
+          fq = fdata[0];
+        } else if (fkind == ORC_F_NODAL) {
+          fq = 0.0;
+          for (int a = 0; a < nv; ++a) fq += fdata[nodes[a] - 1] * phi[q * nv + a];
+        } else {
+          fq = fdata[c * nq + q];
+        }
+        for (int i = 0; i < nv; ++i) bv[i] += (fq * phi[q * nv + i]) * dV;
+      }
+    }
+  }
+  free(phi);
+  free(dphi);
+  free(g);
+  return 0;
+}
+
+/* ====================================================================================== */
+/* assembly                                                                                */
+/* ====================================================================================== */
+
+/* lower bound of x in v[lo..hi] (inclusive), returns hi+1 if all smaller
+ * (Base.searchsortedfirst as used by Algebra/SparseMatrixCSC.jl:128). */
+static int64_t sorted_first(const int64_t* v, int64_t x, int64_t lo, int64_t hi) {
+  int64_t a = lo, b = hi + 1;
+  while (a < b) {
+    int64_t m = a + (b - a) / 2;
+    if (v[m] < x) a = m + 1; else b = m;
+  }
+  return a;
+}
+
+int orc_assemble_matrix_csc(int64_t ncells, int nd, const int32_t* cell_rows,
+                            const int32_t* cell_cols, const double* cellmats, int64_t nrows,
+                            int64_t ncols, orc_csc* out) {
+  /* symbolic loop: CounterCSC.colnnzmax[j] += 1 for every positive (i,j) touched
+   * (FESpaces/SparseMatrixAssemblers.jl:174-210, Algebra/SparseMatrixCSC.jl:72-89) */
+  int64_t* colnnz = (int64_t*)calloc(ncols + 1, sizeof(int64_t));
+  int64_t* colptr = (int64_t*)malloc(sizeof(int64_t) * (ncols + 1));
+  if (!colnnz || !colptr) return -1;
+  for (int64_t c = 0; c < ncells; ++c) {
+    const int32_t* rs = cell_rows + c * nd;
+    const int32_t* cs = cell_cols + c * nd;
+    for (int lj = 0; lj < nd; ++lj) {
+      if (cs[lj] <= 0) continue;
+      for (int li = 0; li < nd; ++li)
+        if (rs[li] > 0) colnnz[cs[lj] - 1] += 1;
+    }
+  }
+  /* nz_allocation (SparseMatrixCSC.jl:250-262): colptr from counts, colnnz reset */
+  colptr[0] = 1;
+  for (int64_t j = 0; j < ncols; ++j) colptr[j + 1] = colptr[j] + colnnz[j];
+  int64_t ndata = colptr[ncols] - 1;
+  int64_t* rowval = (int64_t*)malloc(sizeof(int64_t) * (ndata > 0 ? ndata : 1));
+  double* nzval = (double*)calloc(ndata > 0 ? ndata : 1, sizeof(double));
+  if (!rowval || !nzval) return -1;
+  memset(colnnz, 0, sizeof(int64_t) * (ncols + 1));
+  /* numeric loop: InserterCSC.add_entry! in cell order, cols outer, rows inner
+   * (SparseMatrixAssemblers.jl:214-248, AlgebraInterfaces.jl:176-187,
+   * SparseMatrixCSC.jl:124-150); arrays here are 0-based views of 1-based data. */
+  for (int64_t c = 0; c < ncells; ++c) {
+    const int32_t* rs = cell_rows + c * nd;
+    const int32_t* cs = cell_cols + c * nd;
+    const double* vs = cellmats ? cellmats + c * nd * nd : NULL;
+    for (int lj = 0; lj < nd; ++lj) {
+      int64_t j = cs[lj];
+      if (j <= 0) continue;
+      for (int li = 0; li < nd; ++li) {
+        int64_t i = rs[li];
+        if (i <= 0) continue;
+        double v = vs ? vs[li + lj * nd] : 0.0;
+        int64_t pini = colptr[j - 1] - 1;
+        int64_t pend = pini + colnnz[j - 1] - 1;
+        int64_t p = sorted_first(rowval, i, pini, pend);
+        if (p > pend) {
+          colnnz[j - 1] += 1;
+          rowval[p] = i;
+          nzval[p] = v;
+        } else if (rowval[p] != i) {
+          for (int64_t k = pend; k >= p; --k) {
+            rowval[k + 1] = rowval[k];
+            nzval[k + 1] = nzval[k];
+          }
+          colnnz[j - 1] += 1;
+          rowval[p] = i;
+          nzval[p] = v;
+        } else {
+          nzval[p] += v;
+        }
+      }
+    }
+  }
+  /* create_from_nz (SparseMatrixCSC.jl:264-283): compact columns in place */
+  int64_t k = 0;
+  for (int64_t j = 0; j < ncols; ++j) {
+    int64_t pini = colptr[j] - 1;
+    for (int64_t p = pini; p < pini + colnnz[j]; ++p, ++k) {
+      nzval[k] = nzval[p];
+      rowval[k] = rowval[p];
+    }
+  }
+  colptr[0] = 1;
+  for (int64_t j = 0; j < ncols; ++j) colptr[j + 1] = colptr[j] + colnnz[j];
+  free(colnnz);
+  out->nrows = nrows;
+  out->ncols = ncols;
+  out->nnz = colptr[ncols] - 1;
+  out->colptr = colptr;
+  out->rowval = rowval;
+  out->nzval = nzval;
+  return 0;
+}
+
+void orc_csc_free(orc_csc* a) {
+  free(a->colptr);
+  free(a->rowval);
+  free(a->nzval);
+  a->colptr = NULL;
+  a->rowval = NULL;
+  a->nzval = NULL;
+}
+
+/* Dense vector: b[i] += v for positive ids, cell order (SparseMatrixAssemblers.jl:287-316,
+ * AlgebraInterfaces.jl:200-207). */
+void orc_assemble_vector(int64_t ncells, int nd, const int32_t* cell_rows,
+                         const double* cellvecs, double* b) {
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int li = 0; li < nd; ++li) {
+      int32_t i = cell_rows[c * nd + li];
+      if (i > 0) b[i - 1] += cellvecs[c * nd + li];
+    }
+}
+
+/* ====================================================================================== */
+/* solver                                                                                  */
+/* ====================================================================================== */
+
+void orc_csc_mul(const orc_csc* A, const double* x, double* y) {
+  memset(y, 0, sizeof(double) * A->nrows);
+  for (int64_t j = 0; j < A->ncols; ++j) {
+    double xj = x[j];
+    for (int64_t p = A->colptr[j] - 1; p < A->colptr[j + 1] - 1; ++p)
+      y[A->rowval[p] - 1] += A->nzval[p] * xj;
+  }
+}
+
+/* symmetric matrix: row r = column r of the CSC */
+static void sym_mul(const orc_csc* A, const double* x, double* y, int nt) {
+  int64_t n = A->ncols;
+  (void)nt;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+  for (int64_t r = 0; r < n; ++r) {
+    double s = 0.0;
+    for (int64_t p = A->colptr[r] - 1; p < A->colptr[r + 1] - 1; ++p)
+      s += A->nzval[p] * x[A->rowval[p] - 1];
+    y[r] = s;
+  }
+}
+
+static double dotp(int64_t n, const double* a, const double* b, int nt) {
+  double s = 0.0;
+  (void)nt;
+#pragma omp parallel for schedule(static) reduction(+ : s) num_threads(nt) if (nt > 1)
+  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+/* Preconditioned conjugate gradients (Hestenes-Stiefel) with x0 = 0. This is the
+ * LinearSolver a Gridap user plugs in through solve!(x, ns, b)
+ * (Algebra/LinearSolvers.jl:58-129, 202-209): Gridap itself ships no Krylov method. */
+int orc_pcg(const orc_csc* A, const double* b, double* x, double rtol, int maxit, int precond,
+            int nthreads, double* relres) {
+  int64_t n = A->nrows;
+  int nt = nthreads > 0 ? nthreads : 1;
+  double* r = (double*)malloc(sizeof(double) * n);
+  double* z = (double*)malloc(sizeof(double) * n);
+  double* p = (double*)malloc(sizeof(double) * n);
+  double* q = (double*)malloc(sizeof(double) * n);
+  double* dinv = (double*)malloc(sizeof(double) * n);
+  if (!r || !z || !p || !q || !dinv) return -1;
+  for (int64_t i = 0; i < n; ++i) {
+    dinv[i] = 1.0;
+    if (precond)
+      for (int64_t k = A->colptr[i] - 1; k < A->colptr[i + 1] - 1; ++k)
+        if (A->rowval[k] - 1 == i) dinv[i] = 1.0 / A->nzval[k];
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    x[i] = 0.0;
+    r[i] = b[i];
+    z[i] = dinv[i] * r[i];
+    p[i] = z[i];
+  }
+  double bnorm = sqrt(dotp(n, b, b, nt));
+  double rz = dotp(n, r, z, nt);
+  double rn = bnorm;
+  int it = 0;
+  if (bnorm == 0.0) {
+    *relres = 0.0;
+    goto done;
+  }
+  while (it < maxit) {
+    sym_mul(A, p, q, nt);
+    double pq = dotp(n, p, q, nt);
+    double alpha = rz / pq;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+    for (int64_t i = 0; i < n; ++i) {
+      x[i] += alpha * p[i];
+      r[i] -= alpha * q[i];
+    }
+    ++it;
+    rn = sqrt(dotp(n, r, r, nt));
+    if (rn <= rtol * bnorm) break;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+    for (int64_t i = 0; i < n; ++i) z[i] = dinv[i] * r[i];
+    double rz1 = dotp(n, r, z, nt);
+    double beta = rz1 / rz;
+    rz = rz1;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+    for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+  }
+  *relres = rn / bnorm;
+done:
+  free(r); free(z); free(p); free(q); free(dinv);
+  return it;
+}

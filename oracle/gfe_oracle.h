@@ -1,0 +1,111 @@
+/*
+ * gfe_oracle.h -- TEST INFRASTRUCTURE ONLY (the oracle), not part of the product.
+ *
+ * A plain-C, CPU restatement of Gridap.jl v0.20.8's cell-wise finite-element assembly and
+ * linear solve, for the element/geometry/weak-form combinations the GPU library covers.
+ * Every function cites the Gridap source it follows (paths relative to the Gridap project).
+ *
+ * Only the test suite, the smoke check and the benchmark's CPU-baseline / reference legs may
+ * load this library, and only as the checker or the timed CPU baseline; the product path
+ * never calls it.
+ *
+ * Conventions (Gridap's):
+ *   - node, cell and dof ids are 1-based; Dirichlet dofs are negative (-1, -2, ...);
+ *   - cell arrays are column-major per cell (cellmat[c][i + j*nd], i = test/row, j = trial/col);
+ *   - the assembled matrix is a SparseMatrixCSC{Float64,Int64}: 1-based colptr/rowval.
+ */
+#ifndef GFE_ORACLE_H
+#define GFE_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- polytopes ---------------------------------------------------------------------- */
+/* Faces of the D-cube in Gridap's order (ReferenceFEs/ExtrusionPolytopes.jl:460-531).
+ * Writes 3^D faces as (extrusion[D], anchor[D]) pairs; returns the number of faces. */
+int orc_ncube_faces(int D, int32_t* ext, int32_t* anchor);
+
+/* ---- Cartesian model (Geometry/CartesianGrids.jl:108-171, CartesianDiscreteModels.jl) -- */
+void orc_cartesian_coords(int D, const int64_t* partition, const double* domain, double* coords);
+void orc_cartesian_cell_nodes(int D, const int64_t* partition, int32_t* cell_nodes);
+/* Box entity (1-based, n-cube face id) of every node: the labels Gridap's Cartesian face
+ * labeling gives the vertices (Geometry/CartesianDiscreteModels.jl:133-189). */
+void orc_cartesian_node_entity(int D, const int64_t* partition, int32_t* node_entity);
+/* get_face_tag_index for d=0 (Geometry/FaceLabelings.jl:411-427): tags given as entity
+ * lists tag_ptrs[ntags+1] (0-based offsets), tag_entities[]. UNSET = 0. */
+void orc_node_tag_index(int64_t nnodes, const int32_t* node_entity, int ntags,
+                        const int32_t* tag_ptrs, const int32_t* tag_entities, int8_t* node_to_tag);
+
+/* ---- jittered Cartesian nodes (synthetic geometry for distorted-cell configurations) ---- */
+/* coords += jitter on nodes that are not on the domain boundary (per node, D values). */
+void orc_jitter_interior(int D, const int64_t* partition, const double* jitter, double* coords);
+
+/* ---- CLagrangian dof numbering (FESpaces/CLagrangianFESpaces.jl:155-380) --------------- */
+/* node_to_tag[nnodes] (0 = UNSET), tag_masks[ntags*ncomp]; lnode_comp_to_ldof[nv*ncomp]
+ * (1-based local dof of (local node, comp)). Outputs node_comp_to_dof[nnodes*ncomp],
+ * cell_dofs[ncells*nv*ncomp]. */
+void orc_clagrangian_numbering(int64_t nnodes, const int8_t* node_to_tag, int ncomp,
+                               const uint8_t* tag_masks, int64_t ncells, int nv,
+                               const int32_t* cell_nodes, const int32_t* lnode_comp_to_ldof,
+                               int32_t* node_comp_to_dof, int32_t* cell_dofs,
+                               int32_t* nfree, int32_t* ndiri);
+
+/* ---- quadrature (ReferenceFEs/Quadratures.jl:191-227, TensorProductQuadratures.jl:68-80) */
+void orc_gauss_legendre01(int n, double* x, double* w);
+/* Tensor-product Gauss-Legendre of a degree on [0,1]^D; returns npoints. */
+int orc_tensor_quadrature(int D, int degree, double* coords, double* weights);
+
+/* ---- Q1 (lexicographic-node multilinear) shape functions ------------------------------- */
+void orc_q1_shapes(int D, int npts, const double* pts, double* phi, double* dphi);
+
+/* ---- cell integrals ------------------------------------------------------------------- */
+enum { ORC_F_NONE = 0, ORC_F_CONST = 1, ORC_F_NODAL = 2, ORC_F_QPOINT = 3 };
+enum { ORC_GEOM_CARTESIAN = 0, ORC_GEOM_NODAL = 1 };
+/* Physical coordinates of the quadrature points of every Q1 cell (ncells*nq*D). */
+void orc_q1_cell_qpoints(int D, int64_t ncells, const int32_t* cell_nodes, const double* coords,
+                         int nq, const double* qx, double* xq);
+/* Diffusion stiffness  K_ij = sum_q (kappa grad v_i) . grad u_j |det Jt_q| w_q  and source
+ * b_i = sum_q f(x_q) v_i |det Jt_q| w_q on Q1 cells (Fields/FieldsInterfaces.jl:708-720,
+ * Fields/ApplyOptimizations.jl:293-310, TensorValues/Operations.jl:875-934).
+ * geom = ORC_GEOM_CARTESIAN uses Jt = diag(h) (Geometry/CartesianGrids.jl:247-276);
+ * ORC_GEOM_NODAL uses Jt_q = sum_a x_a (x) grad phi_a(xi_q) (Geometry/Grids.jl:237-241).
+ * kappa_cell may be NULL (kappa = 1). cellmats/cellvecs may be NULL to skip. */
+int orc_q1_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_nodes,
+                                 const double* coords, int geom, const double* h,
+                                 const double* kappa_cell, int nq, const double* qx,
+                                 const double* qw, int fkind, const double* fdata,
+                                 double* cellmats, double* cellvecs);
+
+/* ---- assembly (FESpaces/SparseMatrixAssemblers.jl:174-316, Algebra/SparseMatrixCSC.jl) - */
+typedef struct {
+  int64_t nrows, ncols, nnz;
+  int64_t* colptr; /* ncols+1, 1-based */
+  int64_t* rowval; /* nnz, 1-based      */
+  double* nzval;   /* nnz               */
+} orc_csc;
+/* symbolic loop (CounterCSC) + nz_allocation + numeric loop (InserterCSC) + create_from_nz.
+ * cellmats may be NULL (pattern only, values 0). Returns 0 on success. */
+int orc_assemble_matrix_csc(int64_t ncells, int nd, const int32_t* cell_rows,
+                            const int32_t* cell_cols, const double* cellmats, int64_t nrows,
+                            int64_t ncols, orc_csc* out);
+void orc_csc_free(orc_csc* a);
+/* Dense vector assembly (SparseMatrixAssemblers.jl:287-316). b must be zeroed by caller. */
+void orc_assemble_vector(int64_t ncells, int nd, const int32_t* cell_rows,
+                         const double* cellvecs, double* b);
+
+/* ---- solver --------------------------------------------------------------------------- */
+/* Jacobi-preconditioned CG (precond=1) or plain CG (precond=0) on a symmetric CSC matrix,
+ * x0 = 0, stopping on ||r||_2 <= rtol ||b||_2. nthreads > 1 uses OpenMP row-parallel loops
+ * (symmetric matrix: column j of the CSC is row j). Returns the iteration count (<0 on
+ * error); *relres gets the final recursive relative residual. */
+int orc_pcg(const orc_csc* A, const double* b, double* x, double rtol, int maxit, int precond,
+            int nthreads, double* relres);
+/* y = A x for a CSC matrix (serial, column-oriented as SparseArrays' mul!). */
+void orc_csc_mul(const orc_csc* A, const double* x, double* y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,294 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes wrapper of the oracle (libgfe_oracle.so), the CPU
+restatement of Gridap.jl v0.20.8's assembly and solve path (gfe_oracle.c).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline / reference legs use it, as
+the checker or the timed CPU baseline. The product (gridap.jl_gb300/) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import pathlib
+import subprocess
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libgfe_oracle.so"
+
+F_NONE, F_CONST, F_NODAL, F_QPOINT = 0, 1, 2, 3
+GEOM_CARTESIAN, GEOM_NODAL = 0, 1
+
+_lib = None
+
+
+def build() -> pathlib.Path:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB_PATH
+
+
+class _CSC(C.Structure):
+    _fields_ = [("nrows", C.c_int64), ("ncols", C.c_int64), ("nnz", C.c_int64),
+                ("colptr", C.POINTER(C.c_int64)), ("rowval", C.POINTER(C.c_int64)),
+                ("nzval", C.POINTER(C.c_double))]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        L = C.CDLL(str(LIB_PATH))
+        P = C.c_void_p
+        L.orc_ncube_faces.argtypes = [C.c_int, P, P]
+        L.orc_cartesian_coords.argtypes = [C.c_int, P, P, P]
+        L.orc_cartesian_cell_nodes.argtypes = [C.c_int, P, P]
+        L.orc_cartesian_node_entity.argtypes = [C.c_int, P, P]
+        L.orc_node_tag_index.argtypes = [C.c_int64, P, C.c_int, P, P, P]
+        L.orc_jitter_interior.argtypes = [C.c_int, P, P, P]
+        L.orc_clagrangian_numbering.argtypes = [C.c_int64, P, C.c_int, P, C.c_int64, C.c_int, P,
+                                                P, P, P, P, P]
+        L.orc_gauss_legendre01.argtypes = [C.c_int, P, P]
+        L.orc_tensor_quadrature.argtypes = [C.c_int, C.c_int, P, P]
+        L.orc_q1_shapes.argtypes = [C.c_int, C.c_int, P, P, P]
+        L.orc_q1_cell_qpoints.argtypes = [C.c_int, C.c_int64, P, P, C.c_int, P, P]
+        L.orc_q1_cell_arrays_diffusion.argtypes = [C.c_int, C.c_int64, P, P, C.c_int, P, P,
+                                                   C.c_int, P, P, C.c_int, P, P, P]
+        L.orc_assemble_matrix_csc.argtypes = [C.c_int64, C.c_int, P, P, P, C.c_int64, C.c_int64,
+                                              C.POINTER(_CSC)]
+        L.orc_csc_free.argtypes = [C.POINTER(_CSC)]
+        L.orc_assemble_vector.argtypes = [C.c_int64, C.c_int, P, P, P]
+        L.orc_pcg.argtypes = [C.POINTER(_CSC), P, P, C.c_double, C.c_int, C.c_int, C.c_int, P]
+        L.orc_csc_mul.argtypes = [C.POINTER(_CSC), P, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data if a is not None else None
+
+
+# ---- geometry ----------------------------------------------------------------------------
+def ncube_faces(D):
+    ext = np.zeros((27, D), np.int32)
+    anc = np.zeros((27, D), np.int32)
+    n = lib().orc_ncube_faces(D, _p(ext), _p(anc))
+    return ext[:n], anc[:n]
+
+
+def cartesian_model(domain, partition):
+    D = len(partition)
+    part = np.asarray(partition, np.int64)
+    dom = np.asarray(domain, np.float64)
+    nn = int(np.prod(part + 1))
+    nc = int(np.prod(part))
+    coords = np.empty((nn, D))
+    cells = np.empty((nc, 2 ** D), np.int32)
+    ent = np.empty(nn, np.int32)
+    L = lib()
+    L.orc_cartesian_coords(D, _p(part), _p(dom), _p(coords))
+    L.orc_cartesian_cell_nodes(D, _p(part), _p(cells))
+    L.orc_cartesian_node_entity(D, _p(part), _p(ent))
+    return coords, cells, ent
+
+
+def jitter_interior(partition, coords, jitter):
+    D = len(partition)
+    part = np.asarray(partition, np.int64)
+    out = np.ascontiguousarray(coords.copy())
+    lib().orc_jitter_interior(D, _p(part), _p(np.ascontiguousarray(jitter, np.float64)), _p(out))
+    return out
+
+
+def cartesian_tags(D):
+    """Gridap's Cartesian tags: tag_<i> per boundary entity, 'interior', 'boundary'."""
+    interior = 3 ** D
+    width = math.ceil(math.log10(interior))
+    names, ents = [], []
+    for i in range(1, interior):
+        names.append(f"tag_{str(i).zfill(width)}")
+        ents.append([i])
+    names += ["interior", "boundary"]
+    ents += [[interior], list(range(1, interior))]
+    return names, ents
+
+
+def node_tag_index(D, node_entity, tags):
+    names, ents = cartesian_tags(D)
+    sel = []
+    for t in tags:
+        sel.append(ents[t - 1] if isinstance(t, (int, np.integer)) else ents[names.index(t)])
+    ptrs = np.zeros(len(sel) + 1, np.int32)
+    for i, e in enumerate(sel):
+        ptrs[i + 1] = ptrs[i] + len(e)
+    flat = np.asarray([x for e in sel for x in e] or [0], np.int32)
+    out = np.zeros(node_entity.shape[0], np.int8)
+    lib().orc_node_tag_index(node_entity.shape[0], _p(np.ascontiguousarray(node_entity)),
+                             len(sel), _p(ptrs), _p(flat), _p(out))
+    return out
+
+
+# ---- dofs -------------------------------------------------------------------------------
+def clagrangian(node_to_tag, cell_nodes, ncomp=1, masks=None, lmap=None):
+    nn = node_to_tag.shape[0]
+    nc, nv = cell_nodes.shape
+    ntags = max(int(node_to_tag.max(initial=0)), 1)
+    if masks is None:
+        masks = np.ones((ntags, ncomp), np.uint8)
+    masks = np.ascontiguousarray(masks, np.uint8)
+    if lmap is None:
+        lmap = np.array([[c * nv + a + 1 for c in range(ncomp)] for a in range(nv)], np.int32)
+    node_dof = np.empty((nn, ncomp), np.int32)
+    cell_dofs = np.empty((nc, nv * ncomp), np.int32)
+    nf = np.zeros(1, np.int32)
+    ndr = np.zeros(1, np.int32)
+    lib().orc_clagrangian_numbering(nn, _p(node_to_tag), ncomp, _p(masks), nc, nv,
+                                    _p(np.ascontiguousarray(cell_nodes)), _p(lmap), _p(node_dof),
+                                    _p(cell_dofs), _p(nf), _p(ndr))
+    return node_dof, cell_dofs, int(nf[0]), int(ndr[0])
+
+
+# ---- quadrature / shapes -------------------------------------------------------------------
+def gauss_legendre01(n):
+    x = np.empty(n)
+    w = np.empty(n)
+    lib().orc_gauss_legendre01(n, _p(x), _p(w))
+    return x, w
+
+
+def tensor_quadrature(D, degree):
+    n = (degree // 2 + 1) ** D
+    x = np.empty((n, D))
+    w = np.empty(n)
+    lib().orc_tensor_quadrature(D, degree, _p(x), _p(w))
+    return x, w
+
+
+def q1_shapes(D, pts):
+    pts = np.ascontiguousarray(pts, np.float64)
+    nv = 2 ** D
+    phi = np.empty((pts.shape[0], nv))
+    dphi = np.empty((pts.shape[0], nv, D))
+    lib().orc_q1_shapes(D, pts.shape[0], _p(pts), _p(phi), _p(dphi))
+    return phi, dphi
+
+
+# ---- cell arrays ---------------------------------------------------------------------------
+def qpoints(D, cell_nodes, coords, degree):
+    qx, _ = tensor_quadrature(D, degree)
+    nc = cell_nodes.shape[0]
+    xq = np.empty((nc, qx.shape[0], D))
+    lib().orc_q1_cell_qpoints(D, nc, _p(np.ascontiguousarray(cell_nodes)),
+                              _p(np.ascontiguousarray(coords)), qx.shape[0], _p(qx), _p(xq))
+    return xq
+
+
+def q1_cell_arrays(D, cell_nodes, coords, degree, geom=GEOM_CARTESIAN, h=None, kappa=None,
+                   fkind=F_NONE, fdata=None, want_mat=True, want_vec=True):
+    """Cell matrices (ncells, nd, nd)[c, i, j] and vectors (ncells, nd)."""
+    qx, qw = tensor_quadrature(D, degree)
+    nc, nv = cell_nodes.shape
+    mats = np.zeros((nc, nv, nv)) if want_mat else None  # filled col-major per cell
+    vecs = np.zeros((nc, nv)) if want_vec else None
+    hh = np.asarray(h if h is not None else [1.0] * D, np.float64)
+    kap = None if kappa is None else np.ascontiguousarray(kappa, np.float64)
+    fd = None if fdata is None else np.ascontiguousarray(fdata, np.float64)
+    st = lib().orc_q1_cell_arrays_diffusion(
+        D, nc, _p(np.ascontiguousarray(cell_nodes)), _p(np.ascontiguousarray(coords)), geom,
+        _p(hh), _p(kap), qx.shape[0], _p(qx), _p(qw), fkind, _p(fd), _p(mats), _p(vecs))
+    if st != 0:
+        raise RuntimeError("oracle: degenerate cell")
+    if mats is not None:
+        mats = np.ascontiguousarray(np.transpose(mats, (0, 2, 1)))  # col-major -> [c, i, j]
+    return mats, vecs
+
+
+# ---- assembly ------------------------------------------------------------------------------
+def assemble_csc(cell_rows, cell_cols, cellmats, nrows, ncols):
+    """Gridap's SparseMatrixCSC{Float64,Int}: returns (colptr, rowval, nzval), 1-based."""
+    cell_rows = np.ascontiguousarray(cell_rows, np.int32)
+    cell_cols = np.ascontiguousarray(cell_cols, np.int32)
+    nc, nd = cell_rows.shape
+    cm = None
+    if cellmats is not None:
+        cm = np.ascontiguousarray(np.transpose(cellmats, (0, 2, 1)), np.float64)  # col-major
+    out = _CSC()
+    st = lib().orc_assemble_matrix_csc(nc, nd, _p(cell_rows), _p(cell_cols), _p(cm), nrows,
+                                       ncols, C.byref(out))
+    if st != 0:
+        raise MemoryError("oracle assembly failed")
+    nnz = out.nnz
+    colptr = np.ctypeslib.as_array(out.colptr, (ncols + 1,)).copy()
+    rowval = np.ctypeslib.as_array(out.rowval, (max(nnz, 1),))[:nnz].copy()
+    nzval = np.ctypeslib.as_array(out.nzval, (max(nnz, 1),))[:nnz].copy()
+    lib().orc_csc_free(C.byref(out))
+    return colptr, rowval, nzval
+
+
+def to_scipy(colptr, rowval, nzval, nrows, ncols):
+    import scipy.sparse as sp
+    return sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=(nrows, ncols))
+
+
+def assemble_vector(cell_rows, cellvecs, nrows):
+    b = np.zeros(nrows)
+    cell_rows = np.ascontiguousarray(cell_rows, np.int32)
+    lib().orc_assemble_vector(cell_rows.shape[0], cell_rows.shape[1], _p(cell_rows),
+                              _p(np.ascontiguousarray(cellvecs, np.float64)), _p(b))
+    return b
+
+
+def _csc_struct(colptr, rowval, nzval, n):
+    s = _CSC()
+    s.nrows = n
+    s.ncols = n
+    s.nnz = nzval.shape[0]
+    s.colptr = colptr.ctypes.data_as(C.POINTER(C.c_int64))
+    s.rowval = rowval.ctypes.data_as(C.POINTER(C.c_int64))
+    s.nzval = nzval.ctypes.data_as(C.POINTER(C.c_double))
+    return s
+
+
+def pcg(colptr, rowval, nzval, b, rtol, maxit=100000, precond=1, nthreads=1):
+    n = b.shape[0]
+    s = _csc_struct(colptr, rowval, nzval, n)
+    x = np.zeros(n)
+    rr = np.zeros(1)
+    it = lib().orc_pcg(C.byref(s), _p(np.ascontiguousarray(b)), _p(x), rtol, maxit, precond,
+                       nthreads, _p(rr))
+    return x, it, float(rr[0])
+
+
+def csc_mul(colptr, rowval, nzval, x):
+    n = colptr.shape[0] - 1
+    s = _csc_struct(colptr, rowval, nzval, n)
+    y = np.zeros(n)
+    lib().orc_csc_mul(C.byref(s), _p(np.ascontiguousarray(x)), _p(y))
+    return y
+
+
+# ---- a whole Gridap-style problem ----------------------------------------------------------
+def poisson_q1(domain, partition, dirichlet_tags=("boundary",), kappa=None, fkind=F_NONE,
+               fdata=None, f_callable=None, degree=2, jitter=None, assemble=True):
+    """Everything Gridap computes for  a = ∫ κ ∇v⋅∇u dΩ,  l = ∫ f v dΩ  on a Q1 space:
+    returns a dict with model arrays, dofs, cell arrays, the CSC matrix (1-based) and b."""
+    D = len(partition)
+    coords, cells, ent = cartesian_model(domain, partition)
+    geom = GEOM_CARTESIAN
+    if jitter is not None:
+        coords = jitter_interior(partition, coords, jitter)
+        geom = GEOM_NODAL
+    h = [(domain[2 * d + 1] - domain[2 * d]) / partition[d] for d in range(D)]
+    ntt = node_tag_index(D, ent, list(dirichlet_tags))
+    node_dof, cell_dofs, nfree, ndiri = clagrangian(ntt, cells)
+    if f_callable is not None:
+        xq = qpoints(D, cells, coords, degree)
+        fkind = F_QPOINT
+        fdata = np.asarray(f_callable(xq.reshape(-1, D)), np.float64).reshape(-1)
+    mats, vecs = q1_cell_arrays(D, cells, coords, degree, geom, h, kappa, fkind, fdata)
+    out = dict(coords=coords, cells=cells, node_entity=ent, node_to_tag=ntt, node_dof=node_dof,
+               cell_dofs=cell_dofs, nfree=nfree, ndiri=ndiri, cellmats=mats, cellvecs=vecs)
+    if assemble:
+        out["csc"] = assemble_csc(cell_dofs, cell_dofs, mats, nfree, nfree)
+        out["b"] = assemble_vector(cell_dofs, vecs, nfree)
+    return out

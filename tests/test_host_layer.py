@@ -1,0 +1,105 @@
+"""CPU tests of the product's host layer: the C-ABI library loads and exports every symbol
+include/gfe.h declares, and its host-side set-up (Cartesian model arrays, face labels, dof
+numbering) equals the oracle's. No kernel is launched here (no GPU in this container)."""
+import ctypes
+import pathlib
+import re
+
+import numpy as np
+import pytest
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    src = (ROOT / "include" / "gfe.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(gfe_[a-z0-9_]+)\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol(gg):
+    lib = gg._lib.load()
+    names = declared_symbols()
+    assert len(names) >= 19
+    for n in names:
+        assert hasattr(lib, n), n
+    # the Python binding covers the whole header
+    assert sorted(gg._lib.SIGNATURES) == names
+
+
+def test_version_and_error_channel(gg):
+    lib = gg._lib.load()
+    assert b"sm_103a" in lib.gfe_version()
+    # a host-only call with bad arguments returns a status and a message
+    st = lib.gfe_cartesian_model(5, None, None, None, None, None)
+    assert st == gg._lib.GFE_ERR_INVALID_ARGUMENT
+    assert b"gfe_cartesian_model" in lib.gfe_last_error()
+
+
+@pytest.mark.parametrize("part", [(2, 2), (5, 3), (3, 4, 2), (1, 1, 1)])
+def test_cartesian_model_matches_oracle(gg, orc, part):
+    D = len(part)
+    dom = tuple(v for d in range(D) for v in (-0.5 + d, 1.25 + 2 * d))
+    m = gg.CartesianDiscreteModel(dom, part)
+    coords, cells, ent = orc.cartesian_model(dom, part)
+    assert np.array_equal(m.cell_node_ids, cells)
+    assert np.array_equal(m.labels.node_entity, ent)
+    assert np.array_equal(m.node_coords, coords)
+
+
+@pytest.mark.parametrize("tags", [["boundary"], [1, 2, 3, 4, 6, 5], ["tag_5", "tag_7"],
+                                  ["interior"], []])
+def test_clagrangian_scalar_matches_oracle(gg, orc, tags):
+    part = (6, 5)
+    m = gg.CartesianDiscreteModel((0, 1, 0, 1), part)
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags=tags)
+    coords, cells, ent = orc.cartesian_model((0, 1, 0, 1), part)
+    ntt = orc.node_tag_index(2, ent, tags) if tags else np.zeros(ent.shape[0], np.int8)
+    node_dof, cell_dofs, nfree, ndiri = orc.clagrangian(ntt, cells)
+    assert np.array_equal(V.cell_dof_ids, cell_dofs)
+    assert (V.nfree, V.ndiri) == (nfree, ndiri)
+
+
+def test_clagrangian_3d_boundary(gg, orc):
+    part = (4, 3, 5)
+    m = gg.CartesianDiscreteModel((0, 1, 0, 1, 0, 1), part)
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    assert V.nfree == 3 * 2 * 4
+    coords, cells, ent = orc.cartesian_model((0, 1, 0, 1, 0, 1), part)
+    ntt = orc.node_tag_index(3, ent, ["boundary"])
+    _, cell_dofs, nfree, _ = orc.clagrangian(ntt, cells)
+    assert np.array_equal(V.cell_dof_ids, cell_dofs)
+    # tag_25 is the x=0 face of the box
+    V25 = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="tag_25")
+    x0 = np.isclose(m.node_coords[:, 0], 0) & ~np.isclose(m.node_coords[:, 1], 0) & \
+        ~np.isclose(m.node_coords[:, 1], 1) & ~np.isclose(m.node_coords[:, 2], 0) & \
+        ~np.isclose(m.node_coords[:, 2], 1)
+    assert V25.ndiri == int(x0.sum())
+
+
+def test_clagrangian_masked_vector_kat(gg, kats):
+    k = kats["clagrangian_2x2"]
+    m = gg.CartesianDiscreteModel(tuple(k["domain"]), tuple(k["partition"]))
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, 2, 1), dirichlet_tags=k["tags"],
+                   dirichlet_masks=np.array(k["masks2"], np.uint8))
+    assert V.cell_dof_ids.tolist() == k["masked_vector_cell_dofs"]
+    assert V.node_comp_to_dof.tolist() == k["masked_vector_node_and_comp_to_dof"]
+    V1 = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags=k["tags"],
+                    dirichlet_masks=np.array(k["masks1"], np.uint8).reshape(-1, 1))
+    assert V1.cell_dof_ids.tolist() == k["masked_cell_dofs"]
+
+
+def test_weak_form_recognition(gg):
+    m = gg.CartesianDiscreteModel((0, 1, 0, 1), (2, 2))
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    u, v = gg.get_trial_fe_basis(V), gg.get_fe_basis(V)
+    from importlib import import_module
+    cd = import_module("gridap_gb300.celldata")
+    assert cd.classify_bilinear(gg.inner(gg.grad(v), gg.grad(u))) == ("diffusion", None)
+    k = gg.CellField(np.ones(4))
+    assert cd.classify_bilinear(k * gg.inner(gg.grad(v), gg.grad(u)))[1] is k
+    assert cd.classify_bilinear(gg.inner(k * gg.grad(v), gg.grad(u)))[1] is k
+    assert cd.classify_linear(3.0 * v) == ("source", 3.0)
+    with pytest.raises(NotImplementedError):
+        cd.classify_bilinear(gg.inner(gg.grad(v), gg.grad(v)))
+    with pytest.raises(NotImplementedError):
+        cd.classify_linear(gg.grad(v))

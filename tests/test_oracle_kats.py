@@ -1,0 +1,168 @@
+"""The oracle against Gridap's own known-answer tests (tests/golden/gridap_kats.json, extracted
+from Gridap's test files by tests/golden/extract_kats.py). These pin the CPU restatement
+before it is trusted as the checker of the GPU library."""
+import itertools
+
+import numpy as np
+import pytest
+
+
+def test_quad_faces_match_gridap(orc, kats):
+    ext, anc = orc.ncube_faces(2)
+    dims = ext.sum(axis=1).tolist()
+    assert dims == kats["quad_facedims"]["value"]
+    # vertices of each edge: the face's anchor plus its extrusion span, vertex id 1 + x + 2y
+    edges = []
+    for e, a in zip(ext, anc):
+        if e.sum() != 1:
+            continue
+        verts = []
+        for t in (0, 1):
+            p = a + t * e
+            verts.append(1 + int(p[0]) + 2 * int(p[1]))
+        edges.append(verts)
+    assert edges == kats["quad_edge_vertices"]["value"]
+
+
+def test_hex_faces_order():
+    # 8 vertices, 12 edges (x-, y-, z-extruded), 6 faces (z-normal, y-normal, x-normal), 1 cell
+    from oracle import oracle as orc
+    ext, anc = orc.ncube_faces(3)
+    assert ext.shape[0] == 27
+    assert ext.sum(axis=1).tolist() == [0] * 8 + [1] * 12 + [2] * 6 + [3]
+    faces = ext[20:26]
+    assert faces.tolist() == [[1, 1, 0]] * 2 + [[1, 0, 1]] * 2 + [[0, 1, 1]] * 2
+    assert anc[24].tolist() == [0, 0, 0] and anc[25].tolist() == [1, 0, 0]  # x=0 is tag 25
+
+
+def test_gauss_legendre_matches_numpy(orc):
+    for n in range(1, 12):
+        x, w = orc.gauss_legendre01(n)
+        xr, wr = np.polynomial.legendre.leggauss(n)
+        assert np.allclose(x, (xr + 1) / 2, rtol=0, atol=2e-16 * 4)
+        assert np.allclose(w, wr / 2, rtol=0, atol=4e-16 * 4)
+
+
+@pytest.mark.parametrize("D", [2, 3])
+def test_tensor_quadrature_exactness(orc, kats, D):
+    k = kats["tensor_quadrature_exactness"]
+    for degree in range(k["degrees"][0], k["degrees"][1] + 1):
+        x, w = orc.tensor_quadrature(D, degree)
+        assert abs(w.sum() - 1.0) < 1e-14
+        errs, exact = [], []
+        for expo in itertools.product(range(degree + 1), repeat=D):
+            q = float(np.sum(w * np.prod(x ** np.array(expo), axis=1)))
+            e = 1.0 / np.prod(np.array(expo) + 1.0)
+            errs.append(abs(q - e))
+            exact.append(abs(e))
+        assert max(errs) / max(exact) < k["max_rel_err"]
+
+
+def _clag(orc, kats, tags, ncomp, masks):
+    k = kats["clagrangian_2x2"]
+    coords, cells, ent = orc.cartesian_model(k["domain"], k["partition"])
+    ntt = orc.node_tag_index(2, ent, tags) if tags else np.zeros(9, np.int8)
+    return orc.clagrangian(ntt, cells, ncomp=ncomp, masks=masks)
+
+
+def test_clagrangian_scalar(orc, kats):
+    k = kats["clagrangian_2x2"]
+    coords, cells, ent = orc.cartesian_model(k["domain"], k["partition"])
+    node_dof, cell_dofs, nfree, ndiri = _clag(orc, kats, [], 1, None)
+    assert np.array_equal(cell_dofs, cells)  # get_cell_dof_ids(V) == cell node ids
+    assert nfree == 9 and ndiri == 0
+
+
+def test_clagrangian_vector(orc, kats):
+    k = kats["clagrangian_2x2"]
+    node_dof, cell_dofs, nfree, ndiri = _clag(orc, kats, [], 2, None)
+    assert cell_dofs.tolist() == k["vector_cell_dofs"]
+    assert node_dof.tolist() == k["vector_node_and_comp_to_dof"]
+
+
+def test_clagrangian_masked_scalar(orc, kats):
+    k = kats["clagrangian_2x2"]
+    masks = np.array(k["masks1"], np.uint8).reshape(-1, 1)
+    node_dof, cell_dofs, nfree, ndiri = _clag(orc, kats, k["tags"], 1, masks)
+    assert cell_dofs.tolist() == k["masked_cell_dofs"]
+    assert node_dof[:, 0].tolist() == k["masked_node_and_comp_to_dof"]
+    free_nodes = [i + 1 for i in range(9) if node_dof[i, 0] > 0]
+    diri_nodes = [i + 1 for i in range(9) if node_dof[i, 0] < 0]
+    assert free_nodes == k["masked_free_dof_to_node"]
+    assert diri_nodes == k["masked_dirichlet_dof_to_node"]
+
+
+def test_clagrangian_masked_vector(orc, kats):
+    k = kats["clagrangian_2x2"]
+    masks = np.array(k["masks2"], np.uint8)
+    node_dof, cell_dofs, nfree, ndiri = _clag(orc, kats, k["tags"], 2, masks)
+    assert cell_dofs.tolist() == k["masked_vector_cell_dofs"]
+    assert node_dof.tolist() == k["masked_vector_node_and_comp_to_dof"]
+
+
+def test_poisson_2x2_matrix_and_vector(orc, kats):
+    k = kats["poisson_2x2_q1"]
+    ref = orc.poisson_q1(k["domain"], k["partition"], k["dirichlet_tags"],
+                         f_callable=lambda x: x[:, 1], degree=k["degree"])
+    assert ref["nfree"] == 3
+    A = orc.to_scipy(*ref["csc"], 3, 3).toarray()
+    for i, j, v in k["mat_entries"]:
+        assert abs(A[i - 1, j - 1] - v) <= 1e-13 * max(1.0, abs(v))
+    assert np.allclose(ref["b"], k["vec"], rtol=1e-14, atol=1e-16)
+    # the matrix Gridap prints is symmetric and its stored pattern is full 3x3 tridiagonal
+    assert np.array_equal(A, A.T)
+
+
+def test_oracle_csc_semantics(orc):
+    """Pattern from InserterCSC equals the set of touched (row, col) pairs; values are the
+    cell-order sums, checked against a dense accumulation."""
+    rng = np.random.default_rng(0)
+    ref = orc.poisson_q1((0, 1, 0, 1, 0, 1), (3, 4, 2), ("boundary",),
+                         kappa=np.exp(rng.standard_normal(24)), fkind=orc.F_CONST,
+                         fdata=np.array([1.0]))
+    n = ref["nfree"]
+    dense = np.zeros((n, n))
+    touched = np.zeros((n, n), bool)
+    for c, dofs in enumerate(ref["cell_dofs"]):
+        for lj, j in enumerate(dofs):
+            for li, i in enumerate(dofs):
+                if i > 0 and j > 0:
+                    dense[i - 1, j - 1] += ref["cellmats"][c, li, lj]
+                    touched[i - 1, j - 1] = True
+    A = orc.to_scipy(*ref["csc"], n, n)
+    assert A.nnz == touched.sum()
+    Ad = A.toarray()
+    assert np.array_equal(Ad != 0, touched & (dense != 0))
+    assert np.allclose(Ad, dense, rtol=1e-15, atol=1e-15)
+    colptr, rowval, _ = ref["csc"]
+    for j in range(n):  # sorted unique rows per column
+        rows = rowval[colptr[j] - 1:colptr[j + 1] - 1]
+        assert np.all(np.diff(rows) > 0)
+
+
+def test_oracle_cg_matches_direct_solve(orc):
+    import scipy.sparse.linalg as spla
+    rng = np.random.default_rng(1)
+    part = (8, 7, 6)
+    nn = 9 * 8 * 7
+    ref = orc.poisson_q1((0, 1, 0, 1, 0, 1), part, ("boundary",),
+                         kappa=np.exp(rng.standard_normal(8 * 7 * 6)), fkind=orc.F_NODAL,
+                         fdata=rng.standard_normal(nn))
+    n = ref["nfree"]
+    A = orc.to_scipy(*ref["csc"], n, n).tocsc()
+    xd = spla.spsolve(A, ref["b"])
+    for nt in (1, 2):
+        x, it, rr = orc.pcg(*ref["csc"], ref["b"], 1e-12, nthreads=nt)
+        assert rr <= 1e-12
+        assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-9
+
+
+def test_manufactured_nodal_solution(orc):
+    """A discrete solution placed in the FE space is recovered exactly (to solver tolerance)."""
+    rng = np.random.default_rng(2)
+    ref = orc.poisson_q1((0, 2, 0, 1), (16, 9), ("boundary",), fkind=orc.F_NONE)
+    n = ref["nfree"]
+    u = rng.standard_normal(n)
+    b = orc.csc_mul(*ref["csc"], u)
+    x, it, rr = orc.pcg(*ref["csc"], b, 1e-13)
+    assert np.linalg.norm(x - u) / np.linalg.norm(u) < 1e-10

@@ -1,0 +1,394 @@
+"""Benchmark: DOF/s assembled + solved to 1e-8 FP64 relative residual on one GB300.
+
+Workload: 3-D lognormal diffusion, 128^3 Q1 hexahedra (2,048,383 free dofs), kappa a seeded
+lognormal Gaussian random field (correlation length 8h, contrast 1e4), f ~ N(0,1) per node,
+homogeneous Dirichlet on the boundary. One step = what AffineFEOperator + solve do:
+symbolic assembly (pattern on the device), numeric assembly of A and b (FP64), and the
+linear solve to ||b - A x|| <= 1e-8 ||b|| (FP64 residual).
+
+  value (headline arm)  mixed precision: FP32-inner PCG inside FP64 iterative refinement,
+                        inputs resident in HBM;
+  plain_fp64            FP64 assembly + FP64 Jacobi-PCG, same inputs (the spec base);
+  e2e                   the headline arm through the C ABI with pinned host buffers:
+                        cell ids, kappa and f copied in, x copied out, every step.
+
+`--impl reference` times the oracle (the CPU restatement of Gridap's algorithm) on the host
+cores on a bounded sample of the same workload.
+
+Multi-GPU: the path does not shard (one problem per GPU); N>1 runs N independent replicas
+and reports the DOF of all replicas over the slowest replica's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "DOF/s assembled+solved to 1e-8 rel. residual: mixed/learned vs plain FP64, 1 GB300"
+UNIT = "DOF/s"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def spmv_bytes(nnz, n, s):
+    """Algorithmic bytes of one CSR SpMV: values + column ids + row pointers + x + y."""
+    return nnz * (s + 4) + (n + 1) * 4 + n * 2 * s
+
+
+def profile_traffic(kind: str):
+    """Per-launch DRAM traffic of the dominant kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "cg_spmv_lognormal_3d.md"
+    if not p.exists():
+        return None
+    m = re.search(rf"traffic_bytes_per_launch_{kind}:\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+# ---- GPU arm ------------------------------------------------------------------------------
+def run_gpu(args):
+    import ctypes
+
+    import torch
+
+    import __graft_entry__ as ge
+    gg = ge.load_package()
+    from gridap_gb300 import _lib, workloads
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    ctx = gg.Context(local)
+    lib = _lib.load()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+
+    w = workloads.lognormal_3d(n=args.n)
+    V = w.space
+    nfree = V.num_free_dofs()
+    ids_h = V.cell_dof_ids
+    ncells, nd = ids_h.shape
+    # device-resident inputs
+    ids_d = torch.from_numpy(ids_h).to(dev)
+    kap_d = torch.from_numpy(w.kappa).to(dev)
+    f_d = torch.from_numpy(w.source.values).to(dev)
+    b_d = torch.zeros(nfree, dtype=torch.float64, device=dev)
+    x_d = torch.zeros(nfree, dtype=torch.float64, device=dev)
+    # pinned host inputs for the end-to-end arm
+    ids_p = torch.from_numpy(ids_h).pin_memory()
+    kap_p = torch.from_numpy(w.kappa).pin_memory()
+    f_p = torch.from_numpy(w.source.values).pin_memory()
+    x_p = torch.zeros(nfree, dtype=torch.float64).pin_memory()
+    b_scratch = torch.zeros(nfree, dtype=torch.float64, device=dev)
+
+    def problem(ids, kap, f):
+        prep = gg.prepare_problem(V, V, w.measure, gg.CellField(kap), gg.NodalField(f),
+                                  cell_dof_ids=ids)
+        return prep
+
+    def step(ids, kap, f, x, solver, b):
+        prep = problem(ids, kap, f)
+        h = ctypes.c_void_p()
+        _lib.check(lib.gfe_symbolic_loop_matrix(ctx.handle, ncells, nd, _lib.ptr(ids),
+                                                _lib.ptr(ids), nfree, nfree, ctypes.byref(h)))
+        try:
+            _lib.check(lib.gfe_assemble_matrix_and_vector(ctx.handle, ctypes.byref(prep.p), h,
+                                                          _lib.ptr(b)))
+            o = solver.opts()
+            rep = _lib.SolveReport()
+            _lib.check(lib.gfe_solve(ctx.handle, h, ctypes.byref(o), _lib.ptr(b), _lib.ptr(x),
+                                     ctypes.byref(rep)))
+        finally:
+            lib.gfe_matrix_destroy(h)
+        return rep
+
+    mixed = gg.IRCGSolver(rtol=w.rtol, inner_rtol=args.inner_rtol)
+    plain = gg.CGSolver(rtol=w.rtol)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        ctx.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed(label, fn, steps, warmup):
+        for _ in range(warmup):
+            rep = fn()
+        barrier()
+        ctx.set_timing(True)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        l0 = ctx.kernel_launches()
+        reps = []
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            reps.append(fn())
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+        kt = {k: ctx.kernel_time(k) for k in (_lib.GFE_KT_SPMV64, _lib.GFE_KT_SPMV32,
+                                              _lib.GFE_KT_ASSEMBLE, _lib.GFE_KT_RESIDUAL64)}
+        ctx.set_timing(False)
+        ms = e0.elapsed_time(e1) / steps
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return dict(ms=ms, wall_ms=1e3 * wall / steps, reps=reps, kt=kt,
+                    launches=ctx.kernel_launches() - l0)
+
+    mixed_dev = lambda: step(ids_d, kap_d, f_d, x_d, mixed, b_d)  # noqa: E731
+    plain_dev = lambda: step(ids_d, kap_d, f_d, x_d, plain, b_d)  # noqa: E731
+
+    def mixed_e2e():
+        rep = step(ids_p, kap_p, f_p, x_p, mixed, b_scratch)
+        return rep
+
+    with ClockSampler(local) as clk:
+        r_mixed = timed("mixed", mixed_dev, args.steps, args.warmup)
+    r_plain = timed("plain", plain_dev, args.steps, max(3, args.warmup))
+    x_plain = x_d.clone()
+    r_mixed_chk = mixed_dev()
+    x_mixed = x_d.clone()
+    err_vs_fp64 = float(torch.linalg.norm(x_mixed - x_plain) / torch.linalg.norm(x_plain))
+    r_e2e = timed("e2e", mixed_e2e, args.steps, max(3, args.warmup))
+
+    # dominant kernel: the CG SpMV, timed with CUDA events inside the timed regions
+    def avg_ms(r, k):
+        tot, n = r["kt"][k]
+        return tot / n if n else float("nan")
+    nnz_c = ctypes.c_int64()
+    hA = ctypes.c_void_p()
+    _lib.check(lib.gfe_symbolic_loop_matrix(ctx.handle, ncells, nd, _lib.ptr(ids_d),
+                                            _lib.ptr(ids_d), nfree, nfree, ctypes.byref(hA)))
+    lib.gfe_matrix_info(hA, None, None, ctypes.byref(nnz_c))
+    lib.gfe_matrix_destroy(hA)
+    prof = {"nnz": nnz_c.value, "fp32_ms": avg_ms(r_mixed, _lib.GFE_KT_SPMV32),
+            "fp64_ms": avg_ms(r_plain, _lib.GFE_KT_SPMV64),
+            "fp32_launches": r_mixed["kt"][_lib.GFE_KT_SPMV32][1],
+            "assemble_ms": avg_ms(r_plain, _lib.GFE_KT_ASSEMBLE)}
+    spmv_share = r_mixed["kt"][_lib.GFE_KT_SPMV32][0] / (r_mixed["ms"] * args.steps)
+
+    rep_m, rep_p = r_mixed["reps"][-1], r_plain["reps"][-1]
+    for rp in r_mixed["reps"] + r_plain["reps"] + r_e2e["reps"]:
+        if not rp.relres <= w.rtol * (1 + 1e-6):
+            raise RuntimeError(f"solve did not reach rtol: relres={rp.relres}")
+    value = world * nfree / (r_mixed["ms"] * 1e-3)
+    plain_value = world * nfree / (r_plain["ms"] * 1e-3)
+    e2e_value = world * nfree / (r_e2e["ms"] * 1e-3)
+    h2d = ids_h.nbytes + w.kappa.nbytes + w.source.values.nbytes
+    d2h = nfree * 8
+    peak, peak_kind = peaks()
+    nnz = prof["nnz"]
+    alg = spmv_bytes(nnz, nfree, 4)
+    achieved = alg / (prof["fp32_ms"] * 1e-3) / 1e9
+    alg64 = spmv_bytes(nnz, nfree, 8)
+    achieved64 = alg64 / (prof["fp64_ms"] * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r_mixed["ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-inner/f64-refinement",
+        "data": "synthetic (seeded lognormal GRF kappa, N(0,1) nodal f)",
+        "config": {"workload": f"lognormal_3d {args.n}^3 Q1 (BASELINE config 5 shape)",
+                   "free_dofs": nfree, "cells": ncells, "nnz": nnz, "rtol": w.rtol,
+                   "solver": f"IR-CG (FP32 Jacobi-PCG inner rtol {args.inner_rtol}, FP64 outer)",
+                   "assembly": "FP64 cell integrals, FP64 row-gather scatter",
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (matrix %.2f GB)" % (nnz * 12 / 1e9)},
+        "iterations": {"mixed_inner": rep_m.iterations, "mixed_refinements": rep_m.refinements,
+                       "plain_fp64": rep_p.iterations},
+        "plain_fp64": {"value": plain_value, "ms_per_step": r_plain["ms"],
+                       "solver": "FP64 Jacobi-PCG", "relres": rep_p.relres},
+        "mixed_over_plain": value / plain_value,
+        "error_vs_fp64": {"rel_l2_solution": err_vs_fp64, "relres_mixed": rep_m.relres},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": r_e2e["ms"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": profile_traffic("fp32"),
+                     "kernel": "k_cg_spmv_dot<float> (sliced-ELL SpMV + p.q)",
+                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes_per_launch": alg, "avg_launch_ms": prof["fp32_ms"],
+                     "launches_timed": prof["fp32_launches"],
+                     "share_of_step_time": spmv_share,
+                     "fp64_spmv": {"achieved": achieved64, "frac": achieved64 / peak,
+                                   "avg_launch_ms": prof["fp64_ms"],
+                                   "traffic": profile_traffic("fp64")}},
+        "assembly": {"row_gather_ms": prof["assemble_ms"]},
+        "gpu_launches": r_mixed["launches"],
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(args, w, quick=True)
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# ---- CPU baseline / reference arm ---------------------------------------------------------
+def cpu_baseline(args, w=None, quick=False):
+    """The oracle (CPU restatement of Gridap's algorithm) on the host cores: serial
+    assembly exactly like Gridap's numeric loop, then Jacobi-PCG with all host threads for a
+    bounded number of iterations; DOF/s extrapolates the per-iteration time to the
+    iteration count the FP64 solve needs."""
+    from oracle import oracle as orc
+    import __graft_entry__ as ge
+    ge.load_package()
+    from gridap_gb300 import workloads
+    if w is None:
+        w = workloads.lognormal_3d(n=args.n)
+    n = args.n
+    V = w.space
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref = orc.poisson_q1((0, 1, 0, 1, 0, 1), (n, n, n), ("boundary",), kappa=w.kappa,
+                         fkind=orc.F_NODAL, fdata=w.source.values)
+    t_asm = time.perf_counter() - t0
+    cp, rv, zv = ref["csc"]
+    iters_sample = 20 if quick else 60
+    t1 = time.perf_counter()
+    _, it, _ = orc.pcg(cp, rv, zv, ref["b"], 1e-30, maxit=iters_sample, nthreads=nthreads)
+    t_it = (time.perf_counter() - t1) / max(it, 1)
+    iters_needed = args.ref_iters
+    total = t_asm + t_it * iters_needed
+    return {"value": V.num_free_dofs() / total, "unit": UNIT, "cores": nthreads,
+            "kind": "port",
+            "sample": (f"oracle on {n}^3: full serial assembly ({t_asm:.2f} s, 1 thread, "
+                       f"Gridap's InserterCSC loop) + {it} Jacobi-PCG iterations on "
+                       f"{nthreads} threads ({1e3 * t_it:.2f} ms/iter), extrapolated to "
+                       f"{iters_needed} iterations (the FP64 GPU solve's count)"),
+            "assembly_s": t_asm, "ms_per_iteration": 1e3 * t_it}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import __graft_entry__ as ge
+    ge.load_package()
+    vals = []
+    cb = None
+    for k in range(args.warmup + args.steps):
+        cb = cpu_baseline(args)
+        if k >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.median(vals))
+    cb["value"] = v
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded lognormal GRF kappa, N(0,1) nodal f)",
+           "config": {"workload": f"lognormal_3d {args.n}^3 Q1 (BASELINE config 5 shape)"},
+           "cpu_baseline": cb,
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gfe", choices=["gfe", "reference"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--inner-rtol", type=float, default=1e-4)
+    ap.add_argument("--ref-iters", type=int, default=0,
+                    help="FP64 PCG iterations the CPU baseline extrapolates to "
+                         "(0: measured by the GPU FP64 solve, or 1500 without a GPU)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gfe":
+        args.warmup = 3
+    if args.ref_iters == 0:
+        args.ref_iters = 1500
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

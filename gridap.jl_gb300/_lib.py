@@ -32,6 +32,7 @@ GFE_SRC_NONE, GFE_SRC_CONST, GFE_SRC_NODAL, GFE_SRC_QPOINT, GFE_SRC_SINSUM = 0, 
 GFE_PREC_FP64, GFE_PREC_FP32 = 0, 1
 GFE_SOLVER_CG, GFE_SOLVER_IR_CG = 0, 1
 GFE_PC_NONE, GFE_PC_JACOBI = 0, 1
+GFE_KT_SPMV64, GFE_KT_SPMV32, GFE_KT_ASSEMBLE, GFE_KT_RESIDUAL64 = 0, 1, 2, 3
 
 
 class GfeError(RuntimeError):
@@ -77,6 +78,8 @@ SIGNATURES = {
     "gfe_ctx_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "gfe_ctx_synchronize": (C.c_int, [_P]),
     "gfe_ctx_kernel_launches": (C.c_int, [_P, _I64P]),
+    "gfe_ctx_set_timing": (C.c_int, [_P, C.c_int]),
+    "gfe_ctx_kernel_time": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), _I64P]),
     "gfe_cartesian_model": (C.c_int, [C.c_int, _P, _P, _P, _P, _P]),
     "gfe_clagrangian_dofs": (C.c_int, [C.c_int64, _P, C.c_int, _P, C.c_int64, C.c_int, _P, _P,
                                        _P, _P, _P, _P]),

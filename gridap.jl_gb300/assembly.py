@@ -44,6 +44,15 @@ class Context:
         _lib.check(_lib.load().gfe_ctx_kernel_launches(self.handle, C.byref(n)))
         return n.value
 
+    def set_timing(self, enable: bool) -> None:
+        _lib.check(_lib.load().gfe_ctx_set_timing(self.handle, int(enable)))
+
+    def kernel_time(self, kind: int) -> tuple[float, int]:
+        """(total milliseconds, launches) of a kernel class since timing was enabled."""
+        ms, n = C.c_double(), C.c_int64()
+        _lib.check(_lib.load().gfe_ctx_kernel_time(self.handle, kind, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
     def __del__(self):
         try:
             if self.handle:

@@ -57,6 +57,7 @@ extern "C" int gfe_ctx_destroy(gfe_ctx* c) {
   DeviceGuard g(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto& s : c->scratch) s.release();
+  timer_release(c);
   if (c->d_err) cudaFree(c->d_err);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -83,6 +84,30 @@ extern "C" int gfe_ctx_kernel_launches(gfe_ctx* c, int64_t* count) {
   clear_error();
   if (!c || !count) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_ctx_kernel_launches: NULL");
   *count = c->launches;
+  return GFE_OK;
+}
+
+extern "C" int gfe_ctx_set_timing(gfe_ctx* c, int enable) {
+  clear_error();
+  if (!c) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_ctx_set_timing: NULL");
+  DeviceGuard g(c->device);
+  GFE_TRY(timer_flush(c));
+  c->timer.enabled = enable != 0;
+  for (int k = 0; k < 8; ++k) {
+    c->timer.total_ms[k] = 0.0;
+    c->timer.count[k] = 0;
+  }
+  return GFE_OK;
+}
+
+extern "C" int gfe_ctx_kernel_time(gfe_ctx* c, int kernel, double* total_ms, int64_t* launches) {
+  clear_error();
+  if (!c || kernel < 0 || kernel >= 8 || !total_ms || !launches)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_ctx_kernel_time: bad arguments");
+  DeviceGuard g(c->device);
+  GFE_TRY(timer_flush(c));
+  *total_ms = c->timer.total_ms[kernel];
+  *launches = c->timer.count[kernel];
   return GFE_OK;
 }
 

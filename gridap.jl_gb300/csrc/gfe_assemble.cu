@@ -190,7 +190,9 @@ static int launch_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src) {
   if (smem > 48 * 1024)
     GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
+  timer_begin(ctx, GFE_KT_ASSEMBLE);
   kern<<<grid_for(a.nrows, R), R, smem, ctx->stream>>>(a, src);
+  timer_end(ctx);
   ctx->launches++;
   GFE_CUDA_TRY(cudaGetLastError());
   return GFE_OK;

@@ -107,6 +107,50 @@ int check_device_error(gfe_ctx* ctx, const char* where) {
   return GFE_OK;
 }
 
+// ---- kernel timing ------------------------------------------------------------------------
+void timer_begin(gfe_ctx* ctx, int kind) {
+  KernelTimer& t = ctx->timer;
+  if (!t.enabled) return;
+  while (t.pool.size() < t.used + 2) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return;
+    }
+    t.pool.push_back(e);
+  }
+  t.kinds.push_back(kind);
+  cudaEventRecord(t.pool[t.used++], ctx->stream);
+}
+
+void timer_end(gfe_ctx* ctx) {
+  KernelTimer& t = ctx->timer;
+  if (!t.enabled || t.used % 2 == 0) return;
+  cudaEventRecord(t.pool[t.used++], ctx->stream);
+}
+
+int timer_flush(gfe_ctx* ctx) {
+  KernelTimer& t = ctx->timer;
+  if (t.used == 0) return GFE_OK;
+  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  for (size_t i = 0; i + 1 < t.used; i += 2) {
+    float ms = 0.f;
+    GFE_CUDA_TRY(cudaEventElapsedTime(&ms, t.pool[i], t.pool[i + 1]));
+    const int k = t.kinds[i / 2];
+    t.total_ms[k] += ms;
+    t.count[k] += 1;
+  }
+  t.used = 0;
+  t.kinds.clear();
+  return GFE_OK;
+}
+
+void timer_release(gfe_ctx* ctx) {
+  for (auto e : ctx->timer.pool) cudaEventDestroy(e);
+  ctx->timer.pool.clear();
+  ctx->timer.used = 0;
+}
+
 // ---- quadrature ---------------------------------------------------------------------------
 // Gauss-Legendre rule with n points: Newton's method on the Legendre three-term recurrence
 // from the Tricomi initial guesses; nodes/weights mapped from [-1,1] to [0,1]. Tensor

@@ -57,6 +57,19 @@ struct ScratchSlot;
 
 }  // namespace gfe
 
+namespace gfe {
+// Optional per-kernel timing: CUDA events recorded on the context's stream around the
+// launches of a kernel class, summed when the stream is next synchronised by the library.
+struct KernelTimer {
+  bool enabled = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<int> kinds;  // kind of each (begin, end) pair in use
+  size_t used = 0;
+  double total_ms[8] = {0};
+  long long count[8] = {0};
+};
+}  // namespace gfe
+
 struct gfe_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -67,6 +80,7 @@ struct gfe_ctx {
   gfe::DevBuf scratch[16];
   // pinned staging for small device->host reads
   void* h_pinned = nullptr;
+  gfe::KernelTimer timer;
 };
 
 struct gfe_matrix {
@@ -146,6 +160,13 @@ int build_solver_plan(gfe_ctx* ctx, gfe_matrix* A);
 int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d_b,
           double* d_x, gfe_solve_report* rep);
 int spmv64(gfe_ctx* ctx, gfe_matrix* A, const double* d_x, double* d_y);
+
+// kernel timing (gfe_host.cpp): begin/end bracket one launch of kernel class `kind`;
+// flush folds finished pairs into the totals (call after a stream synchronisation).
+void timer_begin(gfe_ctx* ctx, int kind);
+void timer_end(gfe_ctx* ctx);
+int timer_flush(gfe_ctx* ctx);
+void timer_release(gfe_ctx* ctx);
 
 // host set-up (gfe_host.cpp)
 int tensor_quadrature(int D, int degree, std::vector<double>& x, std::vector<double>& w);

@@ -382,7 +382,7 @@ static int read_state(gfe_ctx* ctx, SolverWork& w) {
   GFE_CUDA_TRY(cudaMemcpyAsync(w.hS, w.S, sizeof(SolverState), cudaMemcpyDeviceToHost,
                                ctx->stream));
   GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  return GFE_OK;
+  return timer_flush(ctx);
 }
 
 // Runs PCG on A (values of type T) for rhs*scale from x=0 until done; returns iterations.
@@ -409,8 +409,10 @@ static int run_pcg(gfe_ctx* ctx, gfe_matrix* A, const T* sval, const T* dinv, co
   int done_iters = 0;
   for (;;) {
     for (int k = 0; k < check_every; ++k) {
+      timer_begin(ctx, sizeof(T) == 4 ? GFE_KT_SPMV32 : GFE_KT_SPMV64);
       k_cg_spmv_dot<T><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, sptr, scol, sval, p, q,
                                                            w.partials, w.S);
+      timer_end(ctx);
       k_cg_update<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
       k_cg_direction<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
       ctx->launches += 3;
@@ -505,9 +507,11 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
       total += it;
       ++outer;
       k_refine_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32, 1.0 / s);
+      timer_begin(ctx, GFE_KT_RESIDUAL64);
       k_residual64<<<grid_for(n, kSpmvBlock), kSpmvBlock, 0, ctx->stream>>>(
           n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(),
           d_x, d_b, r64, w.partials, rr_dev, &w.S->ticket[2]);
+      timer_end(ctx);
       ctx->launches += 2;
       GFE_CUDA_TRY(cudaGetLastError());
       GFE_TRY(read_state(ctx, w));

@@ -1,0 +1,77 @@
+"""Seeded synthetic problems with the shapes, sizes and value distributions of the
+benchmark configurations (no dataset is involved; every input is generated here).
+
+  - poisson_2d:      2-D Poisson on the unit square, 256 x 256 Q1 cells, quadrature degree
+                     2, f = sum of 8 sinusoids with amplitudes ~ N(0,1) and integer
+                     wavenumbers 1..8 (seed 1), homogeneous Dirichlet on "boundary".
+  - lognormal_3d:    3-D diffusion on 128^3 Q1 cells, kappa = exp(sigma g) with g a
+                     unit-variance Gaussian random field of correlation length 8h (FFT
+                     filtering of white noise on the cell grid), sigma set so that
+                     max(kappa)/min(kappa) = 1e4; f ~ N(0,1) per node; Dirichlet on
+                     "boundary".
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .celldata import CellField, NodalField, SinSum
+from .fespaces import FESpace, ReferenceFE, lagrangian
+from .geometry import CartesianDiscreteModel, Measure, Triangulation
+
+
+@dataclass
+class Workload:
+    name: str
+    model: CartesianDiscreteModel
+    space: FESpace
+    measure: Measure
+    kappa: np.ndarray | None  # per cell
+    source: object            # NodalField / SinSum / float
+    rtol: float
+
+
+def gaussian_random_field(shape, corr_cells: float, rng: np.random.Generator) -> np.ndarray:
+    """Unit-variance stationary Gaussian field on a periodic cell grid with a Gaussian
+    covariance of correlation length `corr_cells` cells (spectral filtering)."""
+    white = rng.standard_normal(shape)
+    k = [np.fft.fftfreq(n) * 2 * np.pi for n in shape]
+    kk = np.zeros(shape)
+    for d, kd in enumerate(k):
+        sh = [1] * len(shape)
+        sh[d] = shape[d]
+        kk = kk + (kd.reshape(sh)) ** 2
+    filt = np.exp(-0.25 * kk * corr_cells ** 2)
+    g = np.real(np.fft.ifftn(np.fft.fftn(white) * filt))
+    g -= g.mean()
+    g /= g.std()
+    return g
+
+
+def lognormal_3d(n: int = 128, seed: int = 5999, contrast: float = 1e4,
+                 corr_cells: float = 8.0) -> Workload:
+    model = CartesianDiscreteModel((0, 1, 0, 1, 0, 1), (n, n, n))
+    V = FESpace(model, ReferenceFE(lagrangian, float, 1), dirichlet_tags="boundary")
+    rng = np.random.default_rng(seed)
+    # cell grid in Gridap's cell order (x fastest): field indexed [k, j, i]
+    g = gaussian_random_field((n, n, n), corr_cells, rng)
+    sigma = np.log(contrast) / (g.max() - g.min())
+    kappa = np.exp(sigma * (g - g.mean())).reshape(-1)
+    f = rng.standard_normal(model.num_nodes())
+    return Workload("lognormal_3d", model, V, Measure(Triangulation(model), 2), kappa,
+                    NodalField(f), 1e-8)
+
+
+def poisson_2d(n: int = 256, seed: int = 1) -> Workload:
+    model = CartesianDiscreteModel((0, 1, 0, 1), (n, n))
+    V = FESpace(model, ReferenceFE(lagrangian, float, 1), dirichlet_tags="boundary")
+    rng = np.random.default_rng(seed)
+    terms = np.column_stack([rng.standard_normal(8), rng.integers(1, 9, 8),
+                             rng.integers(1, 9, 8)]).astype(np.float64)
+    return Workload("poisson_2d", model, V, Measure(Triangulation(model), 2), None,
+                    SinSum(terms), 1e-10)
+
+
+def coefficient(w: Workload):
+    return None if w.kappa is None else CellField(w.kappa)

@@ -58,6 +58,17 @@ int gfe_ctx_stream(gfe_ctx* ctx, void** stream);
 int gfe_ctx_synchronize(gfe_ctx* ctx);
 /* Number of kernels this context has launched so far (for launch accounting). */
 int gfe_ctx_kernel_launches(gfe_ctx* ctx, int64_t* count);
+/* Kernel timing: when enabled, CUDA events on the context's stream bracket every launch of
+ * the kernel classes below and their device times are summed. Enabling or disabling resets
+ * the totals. gfe_ctx_kernel_time returns the total milliseconds and launch count. */
+enum {
+  GFE_KT_SPMV64 = 0,     /* FP64 SpMV + dot of the CG iteration */
+  GFE_KT_SPMV32 = 1,     /* FP32 SpMV + dot of the inner CG iteration */
+  GFE_KT_ASSEMBLE = 2,   /* row-gather numeric assembly */
+  GFE_KT_RESIDUAL64 = 3  /* FP64 residual r = b - A x of iterative refinement */
+};
+int gfe_ctx_set_timing(gfe_ctx* ctx, int enable);
+int gfe_ctx_kernel_time(gfe_ctx* ctx, int kernel, double* total_ms, int64_t* launches);
 
 /* ---- FE space set-up (host) -------------------------------------------------------------- */
 /* CartesianDiscreteModel(domain, partition) arrays: node coordinates (nnodes*D, x fastest),

@@ -94,6 +94,9 @@ SIGNATURES = {
     "gfe_assemble_matrix_and_vector": (C.c_int, [_P, C.POINTER(Problem), _P, _P]),
     "gfe_solve": (C.c_int, [_P, _P, C.POINTER(SolverOpts), _P, _P, C.POINTER(SolveReport)]),
     "gfe_matrix_mul": (C.c_int, [_P, _P, _P, _P]),
+    "gfe_cg_solve_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, _P, _P, C.c_double,
+                                       C.c_int32, _P, C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_double)]),
 }
 
 _lib = None

@@ -207,6 +207,23 @@ int gfe_solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* opts, const do
 /* y = A x in FP64 (Gridap's mul!(y, A, x) on the assembled matrix; used for residuals). */
 int gfe_matrix_mul(gfe_ctx* ctx, gfe_matrix* A, const double* x, double* y);
 
+/* ---- allocation-free solve ----------------------------------------------------------------- */
+/* FP64 Jacobi-preconditioned CG (x0 = 0, stop on ||b - A x|| <= rtol ||b||) on a matrix the
+ * caller holds in device memory as 0-based CSR (rowptr[n+1], colval[nnz], val[nnz]), with b
+ * and x in device memory too. It allocates no device memory at all: for callers that cannot
+ * call cudaMalloc -- applications whose device memory is owned by their own pool or arena
+ * (e.g. a Julia CUDA.jl pool, or a code that allocates once at start-up and must not
+ * allocate while it runs). Its work vectors live in a fixed static device array sized for
+ * n <= 524,288 rows (about 16 MB held by every GPU that loads the library); larger n is
+ * rejected with GFE_ERR_INVALID_ARGUMENT. The first call on a device looks up that array's
+ * address (once per device); make it before any stream capture. All calls share the array:
+ * calls that overlap on the GPU race. Work is ordered on `stream` (a cudaStream_t, NULL for
+ * the default stream) and complete on return.
+ * No counterpart in Gridap: it is an extra entry point of this library. */
+int gfe_cg_solve_noalloc(const int32_t* rowptr, const int32_t* colval, const double* val,
+                         int64_t n, int64_t nnz, const double* b, double* x, double rtol,
+                         int32_t maxiter, void* stream, int32_t* iterations, double* relres);
+
 #ifdef __cplusplus
 }
 #endif

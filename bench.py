@@ -6,8 +6,8 @@ homogeneous Dirichlet on the boundary. One step = what AffineFEOperator + solve 
 symbolic assembly (pattern on the device), numeric assembly of A and b (FP64), and the
 linear solve to ||b - A x|| <= 1e-8 ||b|| (FP64 residual).
 
-  value (headline arm)  mixed precision: FP32-inner PCG inside FP64 iterative refinement,
-                        inputs resident in HBM;
+  value (headline arm)  mixed precision: FP32 Jacobi-PCG with FP64 reliable updates (x and
+                        the true residual in FP64), inputs resident in HBM;
   plain_fp64            FP64 assembly + FP64 Jacobi-PCG, same inputs (the north-star base);
   e2e                   the headline arm through the C ABI with pinned host buffers:
                         cell ids, kappa and f copied in, x copied out, every step.
@@ -112,12 +112,13 @@ def spmv_bytes(nnz, n, s):
 
 
 def profile_traffic(kind: str):
-    """Per-launch DRAM traffic of the dominant kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "cg_spmv_lognormal_3d.md"
-    if not p.exists():
-        return None
-    m = re.search(rf"traffic_bytes_per_launch_{kind}:\s*([0-9.eE+]+)", p.read_text())
-    return float(m.group(1)) if m else None
+    """Per-launch DRAM traffic of a kernel at the bench workload, from the committed ncu
+    summaries under profiles/ (a line `traffic_bytes_per_launch_<kind>: <bytes>`)."""
+    for p in sorted((ROOT / "profiles").glob("*.md")):
+        m = re.search(rf"traffic_bytes_per_launch_{kind}:\s*([0-9.eE+]+)", p.read_text())
+        if m:
+            return float(m.group(1))
+    return None
 
 
 # ---- GPU arm ------------------------------------------------------------------------------
@@ -179,7 +180,7 @@ def run_gpu(args):
             lib.gfe_matrix_destroy(h)
         return rep
 
-    mixed = gg.IRCGSolver(rtol=w.rtol, inner_rtol=args.inner_rtol)
+    mixed = gg.MixedCGSolver(rtol=w.rtol, inner_rtol=args.delta)
     plain = gg.CGSolver(rtol=w.rtol)
 
     def barrier():
@@ -262,7 +263,9 @@ def run_gpu(args):
     d2h = nfree * 8
     peak, peak_kind = peaks()
     nnz = prof["nnz"]
-    alg = spmv_bytes(nnz, nfree, 4)
+    dia = rep_m.operator_format == 1
+    # diagonal format: values + x + y (no column ids); sliced ELL: the CSR formula
+    alg = (nnz * 4 + nfree * 8) if dia else spmv_bytes(nnz, nfree, 4)
     achieved = alg / (prof["fp32_ms"] * 1e-3) / 1e9
     alg64 = spmv_bytes(nnz, nfree, 8)
     achieved64 = alg64 / (prof["fp64_ms"] * 1e-3) / 1e9
@@ -273,11 +276,12 @@ def run_gpu(args):
         "data": "synthetic (seeded lognormal GRF kappa, N(0,1) nodal f)",
         "config": {"workload": f"lognormal_3d {args.n}^3 Q1 (BASELINE config 5 shape)",
                    "free_dofs": nfree, "cells": ncells, "nnz": nnz, "rtol": w.rtol,
-                   "solver": f"IR-CG (FP32 Jacobi-PCG inner rtol {args.inner_rtol}, FP64 outer)",
+                   "solver": f"mixed CG: FP32 Jacobi-PCG with FP64 reliable updates "
+                             f"(delta {args.delta}), FP64 x and true residual",
                    "assembly": "FP64 cell integrals, FP64 row-gather scatter",
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (matrix %.2f GB)" % (nnz * 12 / 1e9)},
-        "iterations": {"mixed_inner": rep_m.iterations, "mixed_refinements": rep_m.refinements,
+        "iterations": {"mixed": rep_m.iterations, "mixed_reliable_updates": rep_m.refinements,
                        "plain_fp64": rep_p.iterations},
         "plain_fp64": {"value": plain_value, "ms_per_step": r_plain["ms"],
                        "solver": "FP64 Jacobi-PCG", "relres": rep_p.relres},
@@ -286,15 +290,18 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": r_e2e["ms"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": profile_traffic("fp32"),
-                     "kernel": "k_cg_spmv_dot<float> (sliced-ELL SpMV + p.q)",
+                     "frac": achieved / peak,
+                     "traffic": profile_traffic("fp32_dia" if dia else "fp32_sell"),
+                     "kernel": ("k_cg_spmv_dot<float, DiaOp<float>> (diagonal-format SpMV, "
+                                f"{rep_m.ndiag} diagonals, + p.q)") if dia else
+                               "k_cg_spmv_dot<float, SellOp<float>> (sliced-ELL SpMV + p.q)",
                      "peak_source": f"{peak_kind} hbm_gbs",
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": prof["fp32_ms"],
                      "launches_timed": prof["fp32_launches"],
                      "share_of_step_time": spmv_share,
                      "fp64_spmv": {"achieved": achieved64, "frac": achieved64 / peak,
                                    "avg_launch_ms": prof["fp64_ms"],
-                                   "traffic": profile_traffic("fp64")}},
+                                   "traffic": profile_traffic("fp64_sell")}},
         "assembly": {"row_gather_ms": prof["assemble_ms"]},
         "gpu_launches": r_mixed["launches"],
         "clocks": clk.summary(),
@@ -374,7 +381,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gfe", choices=["gfe", "reference"])
     ap.add_argument("--n", type=int, default=128)
-    ap.add_argument("--inner-rtol", type=float, default=1e-4)
+    ap.add_argument("--delta", type=float, default=0.1,
+                    help="residual reduction between FP64 reliable updates of the mixed CG")
     ap.add_argument("--ref-iters", type=int, default=0,
                     help="FP64 PCG iterations the CPU baseline extrapolates to "
                          "(0: measured by the GPU FP64 solve, or 1500 without a GPU)")

@@ -20,7 +20,8 @@ from .celldata import (CellField, DomainContribution, NodalField, SinSum, dot, g
 from .fespaces import (FEFunction, FESpace, ReferenceFE, TrialFESpace, get_cell_dof_ids,
                        lagrangian, num_free_dofs)
 from .geometry import CartesianDiscreteModel, FaceLabeling, Measure, Triangulation
-from .solvers import (CGSolver, IRCGSolver, LinearFESolver, LinearSolver, SolveReport, solve,
+from .solvers import (CGSolver, IRCGSolver, LinearFESolver, LinearSolver, MixedCGSolver,
+                      SolveReport, solve,
                       solve_, numerical_setup, numerical_setup_, symbolic_setup)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

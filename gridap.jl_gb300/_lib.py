@@ -24,15 +24,15 @@ GFE_ERR_TIMEOUT = 6
 GFE_ERR_UNSUPPORTED = 7
 GFE_ERR_NONFINITE = 8
 
-GFE_REFFE_Q1 = 1
+GFE_REFFE_Q1, GFE_REFFE_Q2 = 1, 2
 GFE_GEOM_CARTESIAN, GFE_GEOM_NODAL = 0, 1
 GFE_FORM_DIFFUSION = 1
 GFE_COEF_ONE, GFE_COEF_CONST, GFE_COEF_CELL = 0, 1, 2
 GFE_SRC_NONE, GFE_SRC_CONST, GFE_SRC_NODAL, GFE_SRC_QPOINT, GFE_SRC_SINSUM = 0, 1, 2, 3, 4
 GFE_PREC_FP64, GFE_PREC_FP32 = 0, 1
-GFE_SOLVER_CG, GFE_SOLVER_IR_CG = 0, 1
+GFE_SOLVER_CG, GFE_SOLVER_IR_CG, GFE_SOLVER_MIXED_CG = 0, 1, 2
 GFE_PC_NONE, GFE_PC_JACOBI = 0, 1
-GFE_KT_SPMV64, GFE_KT_SPMV32, GFE_KT_ASSEMBLE, GFE_KT_RESIDUAL64 = 0, 1, 2, 3
+GFE_KT_SPMV64, GFE_KT_SPMV32, GFE_KT_ASSEMBLE, GFE_KT_RESIDUAL64, GFE_KT_ELEMENT = 0, 1, 2, 3, 4
 
 
 class GfeError(RuntimeError):
@@ -63,7 +63,8 @@ class SolverOpts(C.Structure):
 
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("converged", C.c_int32),
-                ("status", C.c_int32), ("relres", C.c_double)]
+                ("status", C.c_int32), ("relres", C.c_double), ("operator_format", C.c_int32),
+                ("ndiag", C.c_int32)]
 
 
 _P = C.c_void_p
@@ -83,6 +84,8 @@ SIGNATURES = {
     "gfe_cartesian_model": (C.c_int, [C.c_int, _P, _P, _P, _P, _P]),
     "gfe_clagrangian_dofs": (C.c_int, [C.c_int64, _P, C.c_int, _P, C.c_int64, C.c_int, _P, _P,
                                        _P, _P, _P, _P]),
+    "gfe_cartesian_conforming_dofs": (C.c_int, [C.c_int, C.c_int, _P, C.c_int, _P, _P, _P, _P,
+                                                _P]),
     "gfe_symbolic_loop_matrix": (C.c_int, [_P, C.c_int64, C.c_int, _P, _P, C.c_int64,
                                            C.c_int64, C.POINTER(C.c_void_p)]),
     "gfe_matrix_destroy": (C.c_int, [_P]),

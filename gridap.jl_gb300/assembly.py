@@ -258,7 +258,9 @@ def prepare_problem(U, V, measure: Measure, coef=None, source=None, precision="f
     prep = _Prepared()
     p = prep.p
     D = model.dim
-    p.dim, p.reffe, p.ncomp, p.degree = D, _lib.GFE_REFFE_Q1, V.reffe.ncomp, measure.degree
+    q2 = V.reffe.order == 2
+    p.dim, p.ncomp, p.degree = D, V.reffe.ncomp, measure.degree
+    p.reffe = _lib.GFE_REFFE_Q2 if q2 else _lib.GFE_REFFE_Q1
     p.ncells = model.num_cells()
     p.nd = V.ndofs_per_cell()
     ids = V.cell_dof_ids if cell_dof_ids is None else cell_dof_ids
@@ -270,7 +272,7 @@ def prepare_problem(U, V, measure: Measure, coef=None, source=None, precision="f
         p.domain[2 * d] = model.domain[2 * d]
         p.domain[2 * d + 1] = model.domain[2 * d + 1]
     p.nnodes = model.num_nodes()
-    if model.cartesian:
+    if model.cartesian and not q2:
         p.geometry = _lib.GFE_GEOM_CARTESIAN
     else:
         p.geometry = _lib.GFE_GEOM_NODAL

@@ -39,6 +39,20 @@ extern "C" int gfe_ctx_create(int device, gfe_ctx** out) {
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount,
                                                    device);
+  if (e == cudaSuccess) {
+    // a private stream-ordered pool that keeps freed memory for reuse by later steps
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    e = cudaMemPoolCreate(&c->pool, &props);
+    if (e == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      e = cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
+  for (auto& s : c->scratch) s.owner = c;
   if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, sizeof(DevError));
   if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(DevError), c->stream);
   if (e == cudaSuccess) e = cudaMallocHost(&c->h_pinned, 4096);
@@ -58,6 +72,8 @@ extern "C" int gfe_ctx_destroy(gfe_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto& s : c->scratch) s.release();
   timer_release(c);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->pool) cudaMemPoolDestroy(c->pool);
   if (c->d_err) cudaFree(c->d_err);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -125,6 +141,10 @@ extern "C" int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd,
   DeviceGuard g(ctx->device);
   gfe_matrix* A = new gfe_matrix();
   A->ctx = ctx;
+  for (gfe::DevBuf* b : {&A->rowptr, &A->colval, &A->val, &A->cell_rows, &A->cell_cols,
+                         &A->ref_ptr, &A->refs, &A->refpos, &A->sell_ptr, &A->sell_col,
+                         &A->sell_val64, &A->sell_val32, &A->dinv64, &A->dinv32})
+    b->owner = ctx;
   A->nrows = nrows;
   A->ncols = ncols;
   A->nd = nd;
@@ -206,6 +226,7 @@ extern "C" int gfe_matrix_fillstored_zero(gfe_matrix* A) {
   if (A->nnz)
     GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * A->nnz, A->ctx->stream));
   A->plan_valid = false;
+  A->dia_checked = false;
   return GFE_OK;
 }
 
@@ -220,6 +241,7 @@ extern "C" int gfe_numeric_loop_matrix(gfe_ctx* ctx, gfe_matrix* A, const double
                       SCR_CELLMAT, &d));
   GFE_TRY(assemble_cellmats(ctx, A, (const double*)d));
   A->plan_valid = false;
+  A->dia_checked = false;
   return GFE_OK;
 }
 
@@ -267,7 +289,10 @@ extern "C" int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* p
     db = ctx->scratch[SCR_VEC_B].as<double>();
   }
   GFE_TRY(assemble_problem(ctx, p, A, db));
-  if (A) A->plan_valid = false;
+  if (A) {
+    A->plan_valid = false;
+    A->dia_checked = false;
+  }
   if (b && !bdev) GFE_TRY(copy_out(ctx, b, db, sizeof(double) * p->nfree));
   return GFE_OK;
 }

@@ -36,12 +36,28 @@ struct RowArgs {
   const int64_t* ref_ptr;
   const int32_t* refs;
   const int32_t* cell_cols;  // column ids per cell (Gridap convention)
+  const void* refpos;        // per (reference, local column) position in the row
   double* val;               // may be null (vector only)
   double* b;                 // may be null (matrix only)
   DevError* err;
 };
 
 // ---- cell value sources -------------------------------------------------------------------
+// FP32 stored cell arrays (the tensor-core element kernels' output), accumulated in FP64.
+struct StoredCellsF32 {
+  const float* mat;
+  const float* vec;
+  int64_t cs, es, vcs, ves;
+  int ntab;
+  __device__ void load_tables(double*) const {}
+  __device__ __forceinline__ double m(const double*, int64_t cell, int li, int lj, int nd) const {
+    return (double)__ldg(mat + cell * cs + (int64_t)(li + lj * nd) * es);
+  }
+  __device__ __forceinline__ double v(const double*, int64_t cell, int li) const {
+    return (double)__ldg(vec + cell * vcs + (int64_t)li * ves);
+  }
+};
+
 // Stored cell arrays. Entry (cell, li, lj) at mat[cell*cs + (li + lj*nd)*es].
 struct StoredCells {
   const double* mat;
@@ -116,7 +132,7 @@ struct CartesianDiffusionQ1 {
 };
 
 // ---- the row-gather kernel ----------------------------------------------------------------
-template <int MAXW, int R, class Src>
+template <int MAXW, int R, class Src, typename PosT>
 __global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
   extern __shared__ double smem[];
   double* acc = smem;                 // acc[k*R + t]
@@ -142,26 +158,21 @@ __global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
 
   double bacc = 0.0;
   if (r < a.nrows) {
-    const int32_t* cols = a.colval + start;
+    const PosT* refpos = static_cast<const PosT*>(a.refpos);
     for (int64_t q = a.ref_ptr[r]; q < a.ref_ptr[r + 1]; ++q) {
       const int32_t e = a.refs[q];
       const int64_t cell = e / a.nd;
       const int li = e - (int)(cell * a.nd);
       if (a.val) {
-        const int32_t* cc = a.cell_cols + cell * a.nd;
+        const PosT* pp = refpos + q * a.nd;
         for (int lj = 0; lj < a.nd; ++lj) {
-          const int32_t c = __ldg(cc + lj) - 1;
-          if (c < 0) continue;
-          int lo = 0, hi = n;
-          while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (__ldg(cols + mid) < c) lo = mid + 1; else hi = mid;
-          }
-          if (lo >= n || __ldg(cols + lo) != c) {
+          const PosT p = __ldg(pp + lj);
+          if (p == (PosT)~(PosT)0) continue;  // Dirichlet column
+          if (p >= n) {
             raise_err(a.err, GFE_ERR_INVALID_ARGUMENT, r);
             continue;
           }
-          acc[lo * R + t] += src.m(tab, cell, li, lj, a.nd);
+          acc[p * R + t] += src.m(tab, cell, li, lj, a.nd);
         }
       }
       if (a.b) bacc += src.v(tab, cell, li);
@@ -184,9 +195,10 @@ __global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
 }
 
 template <int MAXW, int R, class Src>
-static int launch_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src) {
+static int launch_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src, int pos_bytes) {
   const size_t smem = sizeof(double) * ((size_t)MAXW * R + (size_t)src.ntab);
-  auto kern = k_assemble_rows<MAXW, R, Src>;
+  auto kern = pos_bytes == 1 ? k_assemble_rows<MAXW, R, Src, uint8_t>
+                             : k_assemble_rows<MAXW, R, Src, uint16_t>;
   if (smem > 48 * 1024)
     GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
@@ -227,13 +239,14 @@ static int max_row_width(gfe_ctx* ctx, gfe_matrix* A, int* out) {
 }
 
 template <class Src>
-static int run_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src, int maxw) {
-  if (maxw <= 16) return launch_rows<16, 128>(ctx, a, src);
-  if (maxw <= 32) return launch_rows<32, 128>(ctx, a, src);
-  if (maxw <= 64) return launch_rows<64, 128>(ctx, a, src);
-  if (maxw <= 128) return launch_rows<128, 64>(ctx, a, src);
-  if (maxw <= 256) return launch_rows<256, 32>(ctx, a, src);
-  return set_error(GFE_ERR_ROW_TOO_WIDE, "assembly: row width %d exceeds 256", maxw);
+static int run_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src, int maxw, int pb) {
+  if (maxw <= 16) return launch_rows<16, 128>(ctx, a, src, pb);
+  if (maxw <= 32) return launch_rows<32, 128>(ctx, a, src, pb);
+  if (maxw <= 64) return launch_rows<64, 128>(ctx, a, src, pb);
+  if (maxw <= 128) return launch_rows<128, 64>(ctx, a, src, pb);
+  if (maxw <= 256) return launch_rows<256, 32>(ctx, a, src, pb);
+  if (maxw <= 512) return launch_rows<512, 16>(ctx, a, src, pb);
+  return set_error(GFE_ERR_ROW_TOO_WIDE, "assembly: row width %d exceeds 512", maxw);
 }
 
 static RowArgs row_args(gfe_ctx* ctx, gfe_matrix* A, double* b, bool with_matrix) {
@@ -245,6 +258,7 @@ static RowArgs row_args(gfe_ctx* ctx, gfe_matrix* A, double* b, bool with_matrix
   a.ref_ptr = A->ref_ptr.as<int64_t>();
   a.refs = A->refs.as<int32_t>();
   a.cell_cols = A->cell_cols.as<int32_t>();
+  a.refpos = A->refpos.ptr;
   a.val = with_matrix ? A->val.as<double>() : nullptr;
   a.b = b;
   a.err = ctx->d_err;
@@ -279,8 +293,7 @@ static int vector_only_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src) {
 
 // ---- caller-provided cell matrices (Gridap's numeric_loop_matrix!) -----------------------
 int assemble_cellmats(gfe_ctx* ctx, gfe_matrix* A, const double* d_cellmats) {
-  int maxw = 0;
-  GFE_TRY(max_row_width(ctx, A, &maxw));
+  const int maxw = A->max_width;
   StoredCells src{};
   src.mat = d_cellmats;
   src.vec = nullptr;
@@ -288,7 +301,7 @@ int assemble_cellmats(gfe_ctx* ctx, gfe_matrix* A, const double* d_cellmats) {
   src.es = 1;
   src.ntab = 0;
   RowArgs a = row_args(ctx, A, nullptr, true);
-  GFE_TRY(run_rows(ctx, a, src, maxw));
+  GFE_TRY(run_rows(ctx, a, src, maxw, A->pos_bytes));
   return check_device_error(ctx, "numeric_loop_matrix");
 }
 
@@ -299,6 +312,7 @@ int assemble_cellvecs(gfe_ctx* ctx, int64_t ncells, int nd, const int32_t* d_row
   // A temporary matrix object carries the references (no pattern needed).
   gfe_matrix T;
   T.ctx = ctx;
+  T.cell_rows.owner = T.ref_ptr.owner = T.refs.owner = ctx;
   T.nrows = nrows;
   T.ncols = nrows;
   T.nd = nd;
@@ -326,7 +340,6 @@ int assemble_cellvecs(gfe_ctx* ctx, int64_t ncells, int nd, const int32_t* d_row
   a.b = d_b;
   a.err = ctx->d_err;
   GFE_TRY((vector_only_rows<StoredCells, true>(ctx, a, src)));
-  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // T's buffers are freed at return
   return check_device_error(ctx, "numeric_loop_vector");
 }
 
@@ -550,14 +563,147 @@ static void cartesian_tables(int D, const double* h, int nq, const std::vector<d
   }
 }
 
+// ---- Q2 (27-node HEX, 9-node QUAD) cell integrals ----------------------------------------
+// The diffusion cell matrix on a cell with (multi)linear geometry is
+//     K = B^T D B,   B[(q,k), i] = d phi_hat_i / d xi_k (xi_q)   (same for every cell),
+//     D = blockdiag_q( G_q ),  G_q = kappa |det Jt_q| w_q  invJt_q^T invJt_q   (3x3 per q),
+// which is Gridap's sum over q of (kappa invJt grad phi_i).(invJt grad phi_j) |det Jt| w_q
+// (Fields/FieldsInterfaces.jl:708-720, Fields/ApplyOptimizations.jl:293-310) regrouped.
+// Jacobians, inverses and determinants are always FP64 (distorted cells).
+struct Q2Tables {
+  int D, nn, nq, nv;  // dims, nodes (27/9), q-points, geometry vertices (8/4)
+};
+
+// G_q for one cell into g[q*9] (FP64); returns false on a degenerate cell.
+template <int D>
+__device__ bool q2_metric(const double* __restrict__ xv, const double* __restrict__ dphi1,
+                          const double* __restrict__ w, int nq, double kap, double* g,
+                          double* dv) {
+  constexpr int NV = 1 << D;
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+    double Jt[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int a = 0; a < NV; ++a)
+      for (int k = 0; k < D; ++k) {
+        const double gk = dphi1[(q * NV + a) * D + k];
+        for (int l = 0; l < D; ++l) Jt[k][l] += gk * xv[a * D + l];
+      }
+    double det, iJ[3][3];
+    if (D == 2) {
+      det = Jt[0][0] * Jt[1][1] - Jt[0][1] * Jt[1][0];
+      const double c = 1.0 / det;
+      iJ[0][0] = Jt[1][1] * c;
+      iJ[0][1] = -Jt[0][1] * c;
+      iJ[1][0] = -Jt[1][0] * c;
+      iJ[1][1] = Jt[0][0] * c;
+    } else {
+      const double a11 = Jt[0][0], a12 = Jt[0][1], a13 = Jt[0][2];
+      const double a21 = Jt[1][0], a22 = Jt[1][1], a23 = Jt[1][2];
+      const double a31 = Jt[2][0], a32 = Jt[2][1], a33 = Jt[2][2];
+      det = a11 * a22 * a33 + a12 * a23 * a31 + a13 * a21 * a32 -
+            (a11 * a23 * a32 + a12 * a21 * a33 + a13 * a22 * a31);
+      const double c = 1.0 / det;
+      iJ[0][0] = (a22 * a33 - a23 * a32) * c;
+      iJ[1][0] = -(a21 * a33 - a23 * a31) * c;
+      iJ[2][0] = (a21 * a32 - a22 * a31) * c;
+      iJ[0][1] = -(a12 * a33 - a13 * a32) * c;
+      iJ[1][1] = (a11 * a33 - a13 * a31) * c;
+      iJ[2][1] = -(a11 * a32 - a12 * a31) * c;
+      iJ[0][2] = (a12 * a23 - a13 * a22) * c;
+      iJ[1][2] = -(a11 * a23 - a13 * a21) * c;
+      iJ[2][2] = (a11 * a22 - a12 * a21) * c;
+    }
+    if (!(det != 0.0) || !isfinite(det)) return false;
+    const double s = kap * fabs(det) * w[q];
+    dv[q] = fabs(det) * w[q];
+    // G = s * iJ^T iJ  (grad_i . grad_j = (iJ g_i).(iJ g_j) = g_i^T iJ^T iJ g_j)
+    for (int k = 0; k < D; ++k)
+      for (int l = 0; l < D; ++l) {
+        double t = 0.0;
+        for (int m = 0; m < D; ++m) t += iJ[m][k] * iJ[m][l];
+        g[q * 9 + k * 3 + l] = s * t;
+      }
+  }
+  return true;
+}
+
+// FP64 Q2 cell matrices: one block per cell (grid-stride over cells). Output entry-major:
+// K[(i + j*nn)*ncells + cell], b[i*ncells + cell].
+template <int D>
+__global__ void __launch_bounds__(256)
+    k_q2_cells_fp64(int64_t ncells, const int32_t* __restrict__ cell_vertices,
+                    const double* __restrict__ coords, const double* __restrict__ tabs, int nq,
+                    int coef_kind, const double* __restrict__ coef, int src_kind,
+                    const double* __restrict__ src, double* __restrict__ K,
+                    double* __restrict__ bvec, DevError* err) {
+  constexpr int NV = 1 << D, NN = D == 2 ? 9 : 27;
+  extern __shared__ double sm[];
+  // tables: w[nq] | phi2[nq*NN] | dphi1[nq*NV*D] | B[(q*D+k)*NN + i]
+  const int nB = nq * D * NN;
+  const int ntab = nq + nq * NN + nq * NV * D + nB;
+  double* w = sm;
+  double* phi2 = w + nq;
+  double* dphi1 = phi2 + nq * NN;
+  double* B = dphi1 + nq * NV * D;
+  double* G = sm + ntab;                // nq*9
+  double* dv = G + nq * 9;              // nq
+  double* C = dv + nq;                  // nB: C[(q*D+k)*NN + j]
+  double* xv = C + nB;                  // NV*D
+  for (int i = threadIdx.x; i < ntab; i += blockDim.x) sm[i] = tabs[i];
+  __syncthreads();
+  for (int64_t cell = blockIdx.x; cell < ncells; cell += gridDim.x) {
+    if (threadIdx.x < NV * D) {
+      const int a = threadIdx.x / D, d = threadIdx.x % D;
+      xv[threadIdx.x] = coords[((int64_t)cell_vertices[cell * NV + a] - 1) * D + d];
+    }
+    const double kap = coef_kind == GFE_COEF_CELL ? coef[cell]
+                       : coef_kind == GFE_COEF_CONST ? coef[0] : 1.0;
+    __syncthreads();
+    const bool ok = q2_metric<D>(xv, dphi1, w, nq, kap, G, dv);
+    if (!ok) raise_err(err, GFE_ERR_DEGENERATE_CELL, cell);
+    __syncthreads();
+    // C = D B
+    for (int idx = threadIdx.x; idx < nB; idx += blockDim.x) {
+      const int j = idx % NN, qk = idx / NN, q = qk / D, k = qk % D;
+      double s = 0.0;
+      for (int l = 0; l < D; ++l) s += G[q * 9 + k * 3 + l] * B[(q * D + l) * NN + j];
+      C[idx] = s;
+    }
+    __syncthreads();
+    // K = B^T C, upper triangle, mirrored
+    for (int idx = threadIdx.x; idx < NN * NN; idx += blockDim.x) {
+      const int i = idx % NN, j = idx / NN;
+      if (i > j) continue;
+      double s = 0.0;
+      for (int qk = 0; qk < nq * D; ++qk) s += B[qk * NN + i] * C[qk * NN + j];
+      K[(int64_t)(i + j * NN) * ncells + cell] = s;
+      K[(int64_t)(j + i * NN) * ncells + cell] = s;
+    }
+    if (bvec)
+      for (int i = threadIdx.x; i < NN; i += blockDim.x) {
+        double s = 0.0;
+        if (src_kind != GFE_SRC_NONE)
+          for (int q = 0; q < nq; ++q) {
+            const double fq = src_kind == GFE_SRC_CONST ? src[0] : src[cell * nq + q];
+            s += (fq * phi2[q * NN + i]) * dv[q];
+          }
+        bvec[(int64_t)i * ncells + cell] = s;
+      }
+    __syncthreads();
+  }
+}
+
+
 // ---- host: fused integrate + assemble -----------------------------------------------------
 int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* d_b) {
   const int D = p->dim;
-  if (p->reffe != GFE_REFFE_Q1 || p->ncomp != 1 || p->form != GFE_FORM_DIFFUSION)
-    return set_error(GFE_ERR_UNSUPPORTED, "assemble: only scalar Q1 diffusion is provided");
+  if ((p->reffe != GFE_REFFE_Q1 && p->reffe != GFE_REFFE_Q2) || p->ncomp != 1 ||
+      p->form != GFE_FORM_DIFFUSION)
+    return set_error(GFE_ERR_UNSUPPORTED, "assemble: scalar Q1/Q2 diffusion is provided");
   if (D != 2 && D != 3) return set_error(GFE_ERR_UNSUPPORTED, "assemble: dim must be 2 or 3");
   const int nv = 1 << D;
-  if (p->nd != nv) return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: nd != 2^dim for Q1");
+  const bool q2 = p->reffe == GFE_REFFE_Q2;
+  const int nn = q2 ? (D == 2 ? 9 : 27) : nv;
+  if (p->nd != nn) return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: nd does not match the element");
   if (A && (A->ncells != p->ncells || A->nd != p->nd))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: matrix pattern built for other cells");
   std::vector<double> qx, qw;
@@ -627,6 +773,7 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
   // rows of the assembly: the matrix's rows, or (vector only) the problem's cell ids
   gfe_matrix* R = A;
   gfe_matrix tmp;
+  tmp.cell_rows.owner = tmp.ref_ptr.owner = tmp.refs.owner = ctx;
   if (!R) {
     tmp.ctx = ctx;
     tmp.nrows = p->nfree;
@@ -642,10 +789,108 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
     GFE_TRY(build_refs(ctx, &tmp));
     R = &tmp;
   }
-  int maxw = 1;
-  if (A) GFE_TRY(max_row_width(ctx, A, &maxw));
+  const int maxw = A ? A->max_width : 1;
 
-  if (p->geometry == GFE_GEOM_CARTESIAN) {
+  if (q2) {
+    if (src_kind == GFE_SRC_NODAL)
+      return set_error(GFE_ERR_UNSUPPORTED, "assemble: nodal sources are Q1 only");
+    if (!p->node_coords || !p->cell_node_ids)
+      return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: Q2 needs node coordinates and "
+                                                 "cell vertex ids");
+    const void* vc;
+    const void* vn;
+    GFE_TRY(device_view(ctx, p->node_coords, sizeof(double) * (size_t)p->nnodes * D, SCR_COORDS,
+                        &vc));
+    GFE_TRY(device_view(ctx, p->cell_node_ids, sizeof(int32_t) * (size_t)ncells * nv,
+                        SCR_CELLNODES, &vn));
+    std::vector<double> phi1, dphi1, phi2, dphi2;
+    q1_shapes(D, nq, qx.data(), phi1, dphi1);
+    q2_shapes(D, nq, qx.data(), phi2, dphi2);
+    std::vector<double> tabs(qw);
+    tabs.insert(tabs.end(), phi2.begin(), phi2.end());
+    tabs.insert(tabs.end(), dphi1.begin(), dphi1.end());
+    for (int q = 0; q < nq; ++q)  // B[(q*D+k)*nn + i]
+      for (int k = 0; k < D; ++k)
+        for (int i = 0; i < nn; ++i) tabs.push_back(dphi2[((size_t)q * nn + i) * D + k]);
+    GFE_TRY(ctx->scratch[SCR_TMP1].reserve(sizeof(double) * tabs.size()));
+    GFE_CUDA_TRY(cudaMemcpyAsync(ctx->scratch[SCR_TMP1].ptr, tabs.data(),
+                                 sizeof(double) * tabs.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    GFE_TRY(ctx->scratch[SCR_CELLMAT].reserve(sizeof(double) * (size_t)ncells * nn * nn));
+    GFE_TRY(ctx->scratch[SCR_CELLVEC].reserve(sizeof(double) * (size_t)ncells * nn));
+    if (fp32) {
+      if (D != 3)
+        return set_error(GFE_ERR_UNSUPPORTED, "assemble: the tensor-core Q2 path is 3-D");
+      if (nq != 27)
+        return set_error(GFE_ERR_UNSUPPORTED, "assemble: the tensor-core Q2 path needs degree 4");
+      float* Kf = ctx->scratch[SCR_CELLMAT].as<float>();
+      float* bf = ctx->scratch[SCR_CELLVEC].as<float>();
+      if (src_kind == GFE_SRC_NONE)
+        GFE_CUDA_TRY(cudaMemsetAsync(bf, 0, sizeof(float) * (size_t)ncells * nn, ctx->stream));
+      timer_begin(ctx, GFE_KT_ELEMENT);
+      GFE_TRY(launch_q2_cells_tf32(ctx, ncells, (const int32_t*)vn, (const double*)vc,
+                                   ctx->scratch[SCR_TMP1].as<double>(), p->coef_kind, d_coef,
+                                   src_kind, d_src, Kf, bf));
+      timer_end(ctx);
+      GFE_TRY(check_device_error(ctx, "assemble (Q2 tensor-core cell integrals)"));
+      StoredCellsF32 s{};
+      s.mat = Kf;
+      s.vec = bf;
+      s.cs = (int64_t)nn * nn;
+      s.es = 1;
+      s.vcs = nn;
+      s.ves = 1;
+      s.ntab = 0;
+      RowArgs a = row_args(ctx, R, d_b, A != nullptr);
+      if (A) {
+        GFE_TRY(run_rows(ctx, a, s, maxw, A->pos_bytes));
+      } else {
+        GFE_TRY(vector_only_rows(ctx, a, s));
+      }
+      return check_device_error(ctx, "assemble_matrix_and_vector");
+    }
+    const size_t sm = sizeof(double) * (tabs.size() + (size_t)nq * 10 + (size_t)nq * D * nn +
+                                        (size_t)nv * D);
+    const unsigned grid = (unsigned)std::min<int64_t>(ncells, (int64_t)ctx->num_sms * 8);
+    timer_begin(ctx, GFE_KT_ELEMENT);
+    if (D == 2) {
+      auto kern = k_q2_cells_fp64<2>;
+      GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm));
+      kern<<<grid, 256, sm, ctx->stream>>>(ncells, (const int32_t*)vn, (const double*)vc,
+                                           ctx->scratch[SCR_TMP1].as<double>(), nq, p->coef_kind,
+                                           d_coef, src_kind, d_src,
+                                           ctx->scratch[SCR_CELLMAT].as<double>(),
+                                           ctx->scratch[SCR_CELLVEC].as<double>(), ctx->d_err);
+    } else {
+      auto kern = k_q2_cells_fp64<3>;
+      GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm));
+      kern<<<grid, 256, sm, ctx->stream>>>(ncells, (const int32_t*)vn, (const double*)vc,
+                                           ctx->scratch[SCR_TMP1].as<double>(), nq, p->coef_kind,
+                                           d_coef, src_kind, d_src,
+                                           ctx->scratch[SCR_CELLMAT].as<double>(),
+                                           ctx->scratch[SCR_CELLVEC].as<double>(), ctx->d_err);
+    }
+    timer_end(ctx);
+    ctx->launches++;
+    GFE_CUDA_TRY(cudaGetLastError());
+    GFE_TRY(check_device_error(ctx, "assemble (Q2 cell integrals)"));
+    StoredCells s{};
+    s.mat = ctx->scratch[SCR_CELLMAT].as<double>();
+    s.vec = ctx->scratch[SCR_CELLVEC].as<double>();
+    s.cs = 1;
+    s.es = ncells;
+    s.vcs = 1;
+    s.ves = ncells;
+    s.ntab = 0;
+    RowArgs a = row_args(ctx, R, d_b, A != nullptr);
+    if (A) {
+      GFE_TRY(run_rows(ctx, a, s, maxw, A->pos_bytes));
+    } else {
+      GFE_TRY(vector_only_rows(ctx, a, s));
+    }
+  } else if (p->geometry == GFE_GEOM_CARTESIAN) {
     double h[3] = {1, 1, 1};
     for (int d = 0; d < D; ++d)
       h[d] = (p->domain[2 * d + 1] - p->domain[2 * d]) / (double)p->partition[d];
@@ -678,7 +923,7 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
     s.cell_nodes = cn;                                                                  \
     s.ntab = (int)tabs.size();                                                          \
     if (A) {                                                                            \
-      GFE_TRY(run_rows(ctx, a, s, maxw));                                               \
+      GFE_TRY(run_rows(ctx, a, s, maxw, A->pos_bytes));                                 \
     } else {                                                                            \
       GFE_TRY(vector_only_rows(ctx, a, s));                                             \
     }                                                                                   \
@@ -747,13 +992,13 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
     s.ntab = 0;
     RowArgs a = row_args(ctx, R, d_b, A != nullptr);
     if (A) {
-      GFE_TRY(run_rows(ctx, a, s, maxw));
+      GFE_TRY(run_rows(ctx, a, s, maxw, A->pos_bytes));
     } else {
       GFE_TRY(vector_only_rows(ctx, a, s));
     }
   }
-  if (!A) GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // tmp freed at return
   return check_device_error(ctx, "assemble_matrix_and_vector");
 }
 
 }  // namespace gfe
+

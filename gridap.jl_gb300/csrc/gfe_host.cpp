@@ -32,7 +32,12 @@ const char* g_last_error_ptr() { return g_last_error.c_str(); }
 DevBuf::~DevBuf() { release(); }
 
 void DevBuf::release() {
-  if (ptr) cudaFree(ptr);
+  if (ptr) {
+    if (owner && owner->pool)
+      cudaFreeAsync(ptr, owner->stream);
+    else
+      cudaFree(ptr);
+  }
   ptr = nullptr;
   bytes = 0;
 }
@@ -41,7 +46,9 @@ int DevBuf::reserve(size_t nbytes) {
   if (nbytes <= bytes && ptr) return GFE_OK;
   release();
   size_t n = nbytes < 256 ? 256 : nbytes;
-  cudaError_t e = cudaMalloc(&ptr, n);
+  cudaError_t e = (owner && owner->pool)
+                      ? cudaMallocFromPoolAsync(&ptr, n, owner->pool, owner->stream)
+                      : cudaMalloc(&ptr, n);
   if (e != cudaSuccess) {
     ptr = nullptr;
     (void)cudaGetLastError();
@@ -321,3 +328,178 @@ extern "C" int gfe_clagrangian_dofs(int64_t nnodes, const int8_t* node_to_tag, i
   }
   return GFE_OK;
 }
+
+// ---- conforming Q2 numbering on Cartesian grids -------------------------------------------
+// Faces of the D-cube in Gridap's order: by dimension, extrusion mask, anchor mask.
+static int ncube_faces(int D, unsigned* ext, unsigned* anc) {
+  int n = 0;
+  for (int k = 0; k <= D; ++k)
+    for (unsigned e = 0; e < (1u << D); ++e) {
+      if (__builtin_popcount(e) != k) continue;
+      // anchors over the non-extruded directions, ascending as a compressed mask
+      const int free_dims = D - k;
+      for (unsigned m = 0; m < (1u << free_dims); ++m) {
+        unsigned a = 0;
+        int bit = 0;
+        for (int d = 0; d < D; ++d) {
+          if (e & (1u << d)) continue;
+          if (m & (1u << bit)) a |= 1u << d;
+          ++bit;
+        }
+        ext[n] = e;
+        anc[n] = a;
+        ++n;
+      }
+    }
+  return n;
+}
+
+extern "C" int gfe_cartesian_conforming_dofs(int dim, int order, const int64_t* partition,
+                                             int ncomp, const int8_t* entity_to_tag,
+                                             const uint8_t* tag_masks, int32_t* cell_dof_ids,
+                                             int32_t* nfree, int32_t* ndiri) {
+  clear_error();
+  if (dim < 2 || dim > 3 || order != 2 || !partition || ncomp < 1 || !entity_to_tag ||
+      !cell_dof_ids || !nfree || !ndiri)
+    return set_error(GFE_ERR_INVALID_ARGUMENT,
+                     "gfe_cartesian_conforming_dofs: dim 2/3, order 2 and outputs required");
+  int64_t n[3] = {1, 1, 1}, np[3] = {1, 1, 1};
+  for (int d = 0; d < dim; ++d) {
+    if (partition[d] < 1)
+      return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_cartesian_conforming_dofs: partition");
+    n[d] = partition[d];
+    np[d] = n[d] + 1;
+  }
+  unsigned fe[27], fa[27];
+  const int nlf = ncube_faces(dim, fe, fa);
+  const int64_t nlat = np[0] * np[1] * np[2];
+  const int64_t ncells = n[0] * n[1] * n[2];
+  // first-touch ids of the faces of dimension 1..D-1, keyed by (extrusion mask, lattice pos)
+  std::vector<int32_t> id((size_t)(1u << dim) * nlat, 0);
+  std::vector<std::vector<int64_t>> faces_of_dim(dim + 1);  // key of each id (1-based order)
+  auto key = [&](unsigned e, const int64_t* P) {
+    return (int64_t)e * nlat + P[0] + np[0] * (P[1] + np[1] * P[2]);
+  };
+  std::vector<int32_t> cell_face((size_t)ncells * nlf);
+  for (int64_t c = 0; c < ncells; ++c) {
+    const int64_t B[3] = {c % n[0], (c / n[0]) % n[1], c / (n[0] * n[1])};
+    for (int f = 0; f < nlf; ++f) {
+      const int k = __builtin_popcount(fe[f]);
+      int64_t P[3] = {B[0], B[1], B[2]};
+      for (int d = 0; d < dim; ++d)
+        if (fa[f] & (1u << d)) P[d] += 1;
+      if (k == 0) {
+        cell_face[c * nlf + f] = (int32_t)(P[0] + np[0] * (P[1] + np[1] * P[2]) + 1);
+      } else if (k == dim) {
+        cell_face[c * nlf + f] = (int32_t)(c + 1);
+      } else {
+        const int64_t kk = key(fe[f], P);
+        if (id[kk] == 0) {
+          faces_of_dim[k].push_back(kk);
+          id[kk] = (int32_t)faces_of_dim[k].size();
+        }
+        cell_face[c * nlf + f] = id[kk];
+      }
+    }
+  }
+  // label of a face with extrusion e at lattice position P: box-face classification
+  auto entity = [&](unsigned e, const int64_t* P) {
+    unsigned ext = 0, anc = 0;
+    for (int d = 0; d < dim; ++d) {
+      if ((e & (1u << d)) || (P[d] > 0 && P[d] < n[d])) ext |= 1u << d;
+      else if (P[d] == n[d]) anc |= 1u << d;
+    }
+    return box_entity(dim, ext, anc);
+  };
+  int64_t f = 0, g = 0;
+  std::vector<std::vector<int32_t>> dof(dim + 1);
+  auto assign = [&](int dd, int64_t count, auto pos_of) {
+    dof[dd].resize((size_t)(count + 1) * ncomp);
+    for (int64_t i = 1; i <= count; ++i) {
+      unsigned e;
+      int64_t P[3];
+      pos_of(i, &e, P);
+      const int tag = entity_to_tag[entity(e, P) - 1];
+      for (int comp = 0; comp < ncomp; ++comp) {
+        const bool diri = tag > 0 && tag_masks && tag_masks[(size_t)(tag - 1) * ncomp + comp];
+        dof[dd][i * ncomp + comp] = diri ? (int32_t)-(++g) : (int32_t)(++f);
+      }
+    }
+  };
+  assign(0, nlat, [&](int64_t i, unsigned* e, int64_t* P) {
+    *e = 0;
+    const int64_t v = i - 1;
+    P[0] = v % np[0];
+    P[1] = (v / np[0]) % np[1];
+    P[2] = v / (np[0] * np[1]);
+  });
+  for (int dd = 1; dd < dim; ++dd)
+    assign(dd, (int64_t)faces_of_dim[dd].size(), [&](int64_t i, unsigned* e, int64_t* P) {
+      const int64_t kk = faces_of_dim[dd][i - 1];
+      *e = (unsigned)(kk / nlat);
+      const int64_t v = kk % nlat;
+      P[0] = v % np[0];
+      P[1] = (v / np[0]) % np[1];
+      P[2] = v / (np[0] * np[1]);
+    });
+  assign(dim, ncells, [&](int64_t i, unsigned* e, int64_t* P) {
+    *e = (1u << dim) - 1;
+    const int64_t c = i - 1;
+    P[0] = c % n[0];
+    P[1] = (c / n[0]) % n[1];
+    P[2] = c / (n[0] * n[1]);
+  });
+  if (f > INT32_MAX || g > INT32_MAX)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_cartesian_conforming_dofs: too many dofs");
+  const int ndc = nlf * ncomp;
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int lf = 0; lf < nlf; ++lf) {
+      const int dd = __builtin_popcount(fe[lf]);
+      const int32_t fid = cell_face[c * nlf + lf];
+      for (int comp = 0; comp < ncomp; ++comp)
+        cell_dof_ids[c * ndc + comp * nlf + lf] = dof[dd][(size_t)fid * ncomp + comp];
+    }
+  *nfree = (int32_t)f;
+  *ndiri = (int32_t)g;
+  return GFE_OK;
+}
+
+namespace gfe {
+// Q2 Lagrange basis on the 3^D nodes of the n-cube in Gridap's local order (vertices, edges,
+// faces, interior; one node per face at its centre): node lattice index 0 / 1 / 2 per
+// direction (2*anchor along fixed directions, 1 along spanned ones), 1-D factors the
+// quadratic Lagrange polynomials on {0, 1/2, 1}.
+void q2_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
+               std::vector<double>& dphi) {
+  unsigned fe[27], fa[27];
+  const int nn = ncube_faces(D, fe, fa);
+  phi.assign((size_t)nq * nn, 0.0);
+  dphi.assign((size_t)nq * nn * D, 0.0);
+  for (int q = 0; q < nq; ++q)
+    for (int a = 0; a < nn; ++a) {
+      double L[3], dL[3];
+      for (int d = 0; d < D; ++d) {
+        const int idx = (fe[a] >> d) & 1 ? 1 : 2 * ((fa[a] >> d) & 1);
+        const double t = qx[(size_t)q * D + d];
+        if (idx == 0) {
+          L[d] = 2.0 * (t - 0.5) * (t - 1.0);
+          dL[d] = 4.0 * t - 3.0;
+        } else if (idx == 1) {
+          L[d] = 4.0 * t * (1.0 - t);
+          dL[d] = 4.0 - 8.0 * t;
+        } else {
+          L[d] = 2.0 * t * (t - 0.5);
+          dL[d] = 4.0 * t - 1.0;
+        }
+      }
+      double v = 1.0;
+      for (int d = 0; d < D; ++d) v *= L[d];
+      phi[(size_t)q * nn + a] = v;
+      for (int k = 0; k < D; ++k) {
+        double g = 1.0;
+        for (int d = 0; d < D; ++d) g *= (d == k) ? dL[d] : L[d];
+        dphi[((size_t)q * nn + a) * D + k] = g;
+      }
+    }
+}
+}  // namespace gfe

@@ -41,10 +41,17 @@ struct DevError {
 };
 
 // ---- device buffers -----------------------------------------------------------------------
-// A growable device allocation owned by a context or matrix.
+// A growable device allocation. With an owner context it comes from the context's
+// stream-ordered memory pool (cudaMallocAsync / cudaFreeAsync on the context's stream), so
+// buffers created and released every step are recycled without device synchronisation.
 struct DevBuf {
   void* ptr = nullptr;
   size_t bytes = 0;
+  gfe_ctx* owner = nullptr;
+  DevBuf() = default;
+  explicit DevBuf(gfe_ctx* o) : owner(o) {}
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf();
   int reserve(size_t nbytes);  // keeps contents only if no growth is needed
   void release();
@@ -73,6 +80,7 @@ struct KernelTimer {
 struct gfe_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;  // stream-ordered pool of this context's device buffers
   int num_sms = 0;
   long long launches = 0;
   gfe::DevError* d_err = nullptr;  // device error word
@@ -94,10 +102,21 @@ struct gfe_matrix {
   gfe::DevBuf cell_rows, cell_cols;
   // row -> (cell*nd + local) references, sorted by cell: the row-gather assembly lists
   gfe::DevBuf ref_ptr, refs;
+  // position of every (reference, local column) in its row's column list (uint8 when every
+  // row has <= 255 entries, else uint16); 0xff / 0xffff marks a skipped (negative) id
+  gfe::DevBuf refpos;
+  int pos_bytes = 1;
+  int max_width = 0;
+  int64_t nrefs = 0;
   // solver plan (sliced ELL copy with 32-row slices), built lazily
   bool plan_valid = false;
   int64_t nslices = 0, sell_nnz = 0;
   gfe::DevBuf sell_ptr, sell_col, sell_val64, sell_val32, dinv64, dinv32;
+  // diagonal (DIA) FP32 copy, built when all column offsets c - r fall in <= 32 values
+  bool dia_checked = false, dia_valid = false;
+  int dia_ndiag = 0;
+  int32_t dia_off[32] = {0};
+  gfe::DevBuf dia_val32;
 };
 
 namespace gfe {
@@ -155,8 +174,15 @@ int assemble_cellvecs(gfe_ctx* ctx, int64_t ncells, int nd, const int32_t* d_row
                       const double* d_cellvecs, int64_t nrows, double* d_b);
 int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* d_b);
 
+// tensor-core Q2 cell integrals (gfe_q2_tc.cu)
+int launch_q2_cells_tf32(gfe_ctx* ctx, int64_t ncells, const int32_t* cell_vertices,
+                         const double* coords, const double* tabs, int coef_kind,
+                         const double* coef, int src_kind, const double* src, float* K,
+                         float* bvec);
+
 // solver (gfe_solve.cu)
 int build_solver_plan(gfe_ctx* ctx, gfe_matrix* A);
+int build_dia(gfe_ctx* ctx, gfe_matrix* A);
 int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d_b,
           double* d_x, gfe_solve_report* rep);
 int spmv64(gfe_ctx* ctx, gfe_matrix* A, const double* d_x, double* d_y);
@@ -170,5 +196,7 @@ void timer_release(gfe_ctx* ctx);
 
 // host set-up (gfe_host.cpp)
 int tensor_quadrature(int D, int degree, std::vector<double>& x, std::vector<double>& w);
+void q2_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
+               std::vector<double>& dphi);
 
 }  // namespace gfe

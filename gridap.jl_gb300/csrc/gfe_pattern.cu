@@ -72,7 +72,7 @@ static int scan_impl(gfe_ctx* ctx, const TIn* in, int64_t* out, int64_t n, int d
   if (depth > 6) return set_error(GFE_ERR_INVALID_ARGUMENT, "scan: input too large");
   const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
   const int64_t nt = ntiles < 1 ? 1 : ntiles;
-  DevBuf sums;  // tile sums and their scan (small; allocated per level)
+  DevBuf sums(ctx);  // tile sums and their scan (small; stream-ordered, freed in order)
   GFE_TRY(sums.reserve(sizeof(int64_t) * (2 * nt + 2)));
   int64_t* tile_sums = sums.as<int64_t>();
   int64_t* tile_offs = tile_sums + nt;  // nt+1 entries
@@ -93,8 +93,6 @@ static int scan_impl(gfe_ctx* ctx, const TIn* in, int64_t* out, int64_t n, int d
     ctx->launches++;
   }
   GFE_CUDA_TRY(cudaGetLastError());
-  // `sums` is freed at scope exit: make sure the kernels reading it are done.
-  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return GFE_OK;
 }
 
@@ -182,12 +180,13 @@ __device__ __forceinline__ int insert_unique(int32_t* cols, int n, int32_t c) {
   return n + 1;
 }
 
-template <int MAXW, bool WRITE>
+template <int MAXW, bool WRITE, typename PosT>
 __global__ void k_row_pattern(int64_t nrows, int nd, const int64_t* __restrict__ ref_ptr,
                               const int32_t* __restrict__ refs,
                               const int32_t* __restrict__ cell_cols, int64_t ncols,
                               int64_t* __restrict__ width, const int64_t* __restrict__ rowptr,
-                              int32_t* __restrict__ colval, DevError* err) {
+                              int32_t* __restrict__ colval, PosT* __restrict__ refpos,
+                              DevError* err) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows) return;
   int32_t cols[MAXW];
@@ -212,9 +211,27 @@ __global__ void k_row_pattern(int64_t nrows, int nd, const int64_t* __restrict__
   }
   if (!WRITE) {
     width[r] = n;
-  } else {
-    const int64_t start = rowptr[r];
-    for (int k = 0; k < n; ++k) colval[start + k] = cols[k];
+    return;
+  }
+  const int64_t start = rowptr[r];
+  for (int k = 0; k < n; ++k) colval[start + k] = cols[k];
+  // positions of every (reference, local column) in this row's sorted column list
+  for (int64_t q = ref_ptr[r]; q < ref_ptr[r + 1]; ++q) {
+    const int32_t cell = refs[q] / nd;
+    const int32_t* cc = cell_cols + (int64_t)cell * nd;
+    for (int lj = 0; lj < nd; ++lj) {
+      const int32_t c = cc[lj] - 1;
+      PosT pos = (PosT)~(PosT)0;
+      if (c >= 0 && c < ncols) {
+        int lo = 0, hi = n;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (cols[mid] < c) lo = mid + 1; else hi = mid;
+        }
+        pos = (PosT)lo;
+      }
+      refpos[q * nd + lj] = pos;
+    }
   }
 }
 
@@ -223,13 +240,17 @@ static void launch_row_pattern(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cell_
                                bool write, int64_t* width, const int64_t* rowptr64) {
   const int64_t* ref_ptr = A->ref_ptr.as<int64_t>();
   if (!write)
-    k_row_pattern<MAXW, false><<<grid_for(A->nrows, 128), 128, 0, ctx->stream>>>(
+    k_row_pattern<MAXW, false, uint8_t><<<grid_for(A->nrows, 128), 128, 0, ctx->stream>>>(
         A->nrows, A->nd, ref_ptr, A->refs.as<int32_t>(), cell_cols, A->ncols, width, nullptr,
-        nullptr, ctx->d_err);
-  else
-    k_row_pattern<MAXW, true><<<grid_for(A->nrows, 128), 128, 0, ctx->stream>>>(
+        nullptr, nullptr, ctx->d_err);
+  else if (A->pos_bytes == 1)
+    k_row_pattern<MAXW, true, uint8_t><<<grid_for(A->nrows, 128), 128, 0, ctx->stream>>>(
         A->nrows, A->nd, ref_ptr, A->refs.as<int32_t>(), cell_cols, A->ncols, nullptr,
-        rowptr64, A->colval.as<int32_t>(), ctx->d_err);
+        rowptr64, A->colval.as<int32_t>(), A->refpos.as<uint8_t>(), ctx->d_err);
+  else
+    k_row_pattern<MAXW, true, uint16_t><<<grid_for(A->nrows, 128), 128, 0, ctx->stream>>>(
+        A->nrows, A->nd, ref_ptr, A->refs.as<int32_t>(), cell_cols, A->ncols, nullptr,
+        rowptr64, A->colval.as<int32_t>(), A->refpos.as<uint16_t>(), ctx->d_err);
   ctx->launches++;
 }
 
@@ -243,6 +264,18 @@ static void row_pattern(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cell_cols, b
     launch_row_pattern<128>(ctx, A, cell_cols, write, width, rowptr64);
   else
     launch_row_pattern<512>(ctx, A, cell_cols, write, width, rowptr64);
+}
+
+__global__ void k_max_i64(const int64_t* __restrict__ v, int64_t n, unsigned long long* out) {
+  long long m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    m = v[i] > m ? v[i] : m;
+  for (int off = 16; off > 0; off >>= 1) {
+    const long long o = __shfl_down_sync(0xffffffffu, m, off);
+    m = o > m ? o : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)m);
 }
 
 __global__ void k_max_i32(const int32_t* __restrict__ v, int64_t n, int32_t* out) {
@@ -278,6 +311,7 @@ int build_refs(gfe_ctx* ctx, gfe_matrix* A) {
   GFE_TRY(scan_exclusive_i32_to_i64(ctx, cnt, A->ref_ptr.as<int64_t>(), nrows));
   int64_t nrefs = 0;
   GFE_TRY(copy_out(ctx, &nrefs, A->ref_ptr.as<int64_t>() + nrows, sizeof(int64_t)));
+  A->nrefs = nrefs;
   GFE_TRY(A->refs.reserve(sizeof(int32_t) * (nrefs > 0 ? nrefs : 1)));
   GFE_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nrows + 1), ctx->stream));
   k_fill_refs<<<g, 256, 0, ctx->stream>>>(rows, n, nrows, A->ref_ptr.as<int64_t>(), cnt,
@@ -302,7 +336,7 @@ int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
   // wider than the largest bound raise GFE_ERR_ROW_TOO_WIDE.
   int maxw;
   {
-    DevBuf dmax;
+    DevBuf dmax(ctx);
     GFE_TRY(dmax.reserve(sizeof(int32_t)));
     GFE_CUDA_TRY(cudaMemsetAsync(dmax.ptr, 0, sizeof(int32_t), ctx->stream));
     k_max_i32<<<grid_for(nrows, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
@@ -314,15 +348,25 @@ int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
     if (bound > A->ncols) bound = A->ncols;
     maxw = bound < 1 ? 1 : (bound > 512 ? 512 : (int)bound);
   }
-  DevBuf width, rowptr64;
+  DevBuf width(ctx), rowptr64(ctx);
   GFE_TRY(width.reserve(sizeof(int64_t) * (nrows + 1)));
   GFE_TRY(rowptr64.reserve(sizeof(int64_t) * (nrows + 1)));
   row_pattern(ctx, A, cols, false, width.as<int64_t>(), nullptr, maxw);
   GFE_CUDA_TRY(cudaGetLastError());
   GFE_TRY(check_device_error(ctx, "symbolic_loop_matrix (column ids)"));
   GFE_TRY(scan_exclusive_i64(ctx, width.as<int64_t>(), rowptr64.as<int64_t>(), nrows));
-  int64_t nnz = 0;
+  DevBuf dwmax(ctx);
+  GFE_TRY(dwmax.reserve(sizeof(int64_t)));
+  GFE_CUDA_TRY(cudaMemsetAsync(dwmax.ptr, 0, sizeof(int64_t), ctx->stream));
+  k_max_i64<<<grid_for(nrows, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+      width.as<int64_t>(), nrows, dwmax.as<unsigned long long>());
+  ctx->launches++;
+  int64_t nnz = 0, wmax = 0;
+  GFE_CUDA_TRY(cudaMemcpyAsync(&wmax, dwmax.ptr, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                               ctx->stream));
   GFE_TRY(copy_out(ctx, &nnz, rowptr64.as<int64_t>() + nrows, sizeof(int64_t)));
+  A->max_width = (int)wmax;
+  A->pos_bytes = wmax <= 255 ? 1 : 2;
   if (nnz > (int64_t)INT32_MAX - 64)
     return set_error(GFE_ERR_UNSUPPORTED, "symbolic_loop_matrix: nnz %lld exceeds int32",
                      (long long)nnz);
@@ -330,6 +374,8 @@ int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
   GFE_TRY(A->rowptr.reserve(sizeof(int32_t) * (nrows + 1)));
   GFE_TRY(A->colval.reserve(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
   GFE_TRY(A->val.reserve(sizeof(double) * (nnz > 0 ? nnz : 1)));
+  GFE_TRY(A->refpos.reserve((size_t)A->pos_bytes * (size_t)(A->nrefs > 0 ? A->nrefs : 1) *
+                            A->nd));
   GFE_TRY(narrow_i64_to_i32(ctx, rowptr64.as<int64_t>(), A->rowptr.as<int32_t>(), nrows + 1));
   row_pattern(ctx, A, cols, true, nullptr, rowptr64.as<int64_t>(), maxw);
   GFE_CUDA_TRY(cudaGetLastError());

@@ -27,11 +27,15 @@ struct SolverState {
   double bb;      // ||b||^2 of the system being solved
   double tol2;    // rtol^2 * bb
   double rz;      // r.z
-  double rz_new;
+  double rz_prev; // r.z of the previous iteration (reliable updates)
   double rr;      // r.r
   double pq;      // p.Ap
   double alpha, beta;
+  double delta2;  // reliable-update threshold (squared); 0 disables
+  double rmax2;   // ||r||^2 at the last reliable update
+  double rr64;    // true FP64 ||b - A x||^2 at the last reliable update
   int iter, done, converged, maxit;
+  int need_update;
   unsigned ticket[4];
 };
 
@@ -132,7 +136,7 @@ int build_solver_plan(gfe_ctx* ctx, gfe_matrix* A) {
   if (A->plan_valid) return GFE_OK;
   const int64_t nrows = A->nrows;
   const int64_t nslices = (nrows + 31) / 32;
-  DevBuf w;
+  DevBuf w(ctx);
   GFE_TRY(w.reserve(sizeof(int64_t) * (nslices + 1)));
   GFE_TRY(A->sell_ptr.reserve(sizeof(int64_t) * (nslices + 1)));
   k_slice_widths<<<grid_for(nslices, 256), 256, 0, ctx->stream>>>(A->rowptr.as<int32_t>(), nrows,
@@ -154,8 +158,94 @@ int build_solver_plan(gfe_ctx* ctx, gfe_matrix* A) {
       A->sell_val32.as<float>(), A->dinv64.as<double>(), A->dinv32.as<float>());
   ctx->launches++;
   GFE_CUDA_TRY(cudaGetLastError());
-  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // w freed at return
   A->plan_valid = true;
+  return GFE_OK;
+}
+
+// ---- diagonal (DIA) FP32 copy ---------------------------------------------------------------
+__global__ void k_first_row_of_width(const int32_t* __restrict__ rowptr, int64_t n, int32_t w,
+                                     unsigned long long* out) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x)
+    if (rowptr[r + 1] - rowptr[r] == w) atomicMin(out, (unsigned long long)r);
+}
+
+struct DiagSet {
+  int32_t off[32];
+  int32_t nd;
+};
+
+__global__ void k_dia_check(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                            int64_t n, DiagSet o, int* bad) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x)
+    for (int32_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+      const int64_t off = (int64_t)col[k] - r;
+      bool found = false;
+      for (int d = 0; d < o.nd; ++d) found |= (o.off[d] == off);
+      if (!found) atomicExch(bad, 1);
+    }
+}
+
+// thread per row, one pass per diagonal (sorted columns and sorted offsets merge)
+__global__ void k_dia_fill(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                           const double* __restrict__ val, int64_t n, DiagSet o,
+                           float* __restrict__ dval) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  int32_t k = rowptr[r];
+  const int32_t e = rowptr[r + 1];
+  for (int d = 0; d < o.nd; ++d) {
+    const int64_t c = r + o.off[d];
+    float v = 0.f;
+    if (k < e && (int64_t)col[k] == c) v = (float)val[k++];
+    dval[(int64_t)d * n + r] = v;
+  }
+}
+
+int build_dia(gfe_ctx* ctx, gfe_matrix* A) {
+  if (A->dia_checked) return GFE_OK;
+  A->dia_checked = true;
+  A->dia_valid = false;
+  const int64_t n = A->nrows;
+  const int w = A->max_width;
+  if (n == 0 || w < 1 || w > 32 || A->nrows != A->ncols) return GFE_OK;
+  DevBuf tmp(ctx);
+  GFE_TRY(tmp.reserve(64 + sizeof(int32_t) * 64));
+  unsigned long long* drow = tmp.as<unsigned long long>();
+  int* dbad = (int*)((char*)tmp.ptr + 16);
+  int32_t* dcols = (int32_t*)((char*)tmp.ptr + 64);
+  const unsigned long long init = ~0ull;
+  GFE_CUDA_TRY(cudaMemcpyAsync(drow, &init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
+  GFE_CUDA_TRY(cudaMemsetAsync(dbad, 0, sizeof(int), ctx->stream));
+  k_first_row_of_width<<<grid_for(n, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+      A->rowptr.as<int32_t>(), n, w, drow);
+  ctx->launches++;
+  unsigned long long row = 0;
+  GFE_TRY(copy_out(ctx, &row, drow, sizeof(row)));
+  if (row >= (unsigned long long)n) return GFE_OK;
+  int32_t start = 0;
+  GFE_TRY(copy_out(ctx, &start, A->rowptr.as<int32_t>() + row, sizeof(int32_t)));
+  int32_t cols[32];
+  GFE_TRY(copy_out(ctx, cols, A->colval.as<int32_t>() + start, sizeof(int32_t) * w));
+  DiagSet o;
+  o.nd = w;
+  for (int d = 0; d < w; ++d) o.off[d] = cols[d] - (int32_t)row;
+  k_dia_check<<<grid_for(n, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+      A->rowptr.as<int32_t>(), A->colval.as<int32_t>(), n, o, dbad);
+  ctx->launches++;
+  int bad = 0;
+  GFE_TRY(copy_out(ctx, &bad, dbad, sizeof(int)));
+  if (bad) return GFE_OK;
+  GFE_TRY(A->dia_val32.reserve(sizeof(float) * (size_t)n * w));
+  k_dia_fill<<<grid_for(n, 256), 256, 0, ctx->stream>>>(
+      A->rowptr.as<int32_t>(), A->colval.as<int32_t>(), A->val.as<double>(), n, o,
+      A->dia_val32.as<float>());
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  A->dia_ndiag = w;
+  for (int d = 0; d < w; ++d) A->dia_off[d] = o.off[d];
+  A->dia_valid = true;
   return GFE_OK;
 }
 
@@ -189,6 +279,40 @@ __device__ __forceinline__ TV sell_row(int64_t r, const int64_t* __restrict__ sp
   return acc;
 }
 
+// SpMV operators (thread per row)
+template <typename T>
+struct SellOp {
+  const int64_t* sptr;
+  const int32_t* scol;
+  const T* sval;
+  __device__ __forceinline__ T row(int64_t r, const T* __restrict__ x) const {
+    return sell_row<T, T>(r, sptr, scol, sval, x);
+  }
+};
+
+struct DiagOffsets {
+  int32_t off[32];
+  int32_t nd;
+};
+
+// Diagonal storage: val[d*n + r] = A(r, r + off[d]) (0 where absent). Every load of values
+// and of x is a coalesced stream; no column ids are read.
+template <typename T>
+struct DiaOp {
+  const T* val;
+  int64_t n;
+  DiagOffsets o;
+  __device__ __forceinline__ T row(int64_t r, const T* __restrict__ x) const {
+    T acc = (T)0;
+#pragma unroll 9
+    for (int d = 0; d < o.nd; ++d) {
+      const int64_t c = r + o.off[d];
+      if ((uint64_t)c < (uint64_t)n) acc = fma(__ldcs(val + (int64_t)d * n + r), __ldg(x + c), acc);
+    }
+    return acc;
+  }
+};
+
 template <typename TV, typename TX, typename TY>
 __global__ void __launch_bounds__(kSpmvBlock)
     k_spmv(int64_t nrows, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
@@ -210,21 +334,20 @@ int spmv64(gfe_ctx* ctx, gfe_matrix* A, const double* d_x, double* d_y) {
 
 // ---- CG kernels (T: vector/matrix type; dot products accumulate in double) ----------------
 // q = A p and partial p.q; the last block computes alpha = rz / pq.
-template <typename T>
+template <typename T, class Op>
 __global__ void __launch_bounds__(kSpmvBlock)
-    k_cg_spmv_dot(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
-                  const T* __restrict__ sval, const T* __restrict__ p, T* __restrict__ q,
+    k_cg_spmv_dot(int64_t n, Op op, const T* __restrict__ p, T* __restrict__ q,
                   double* __restrict__ partials, SolverState* S) {
   __shared__ double sh[kSpmvBlock / 32];
   if (S->done) return;
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double d = 0.0;
+  T dt = (T)0;
   if (r < n) {
-    const T y = sell_row<T, T>(r, sptr, scol, sval, p);
+    const T y = op.row(r, p);
     q[r] = y;
-    d = (double)p[r] * (double)y;
+    dt = p[r] * y;
   }
-  d = block_sum<kSpmvBlock>(d, sh);
+  const double d = block_sum<kSpmvBlock>((double)dt, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = d;
   double tot[1];
   if (last_block_reduce<kSpmvBlock, 1>(&S->ticket[0], partials, gridDim.x, tot, sh) &&
@@ -243,17 +366,19 @@ __global__ void __launch_bounds__(kVecBlock)
   __shared__ double sh[kVecBlock / 32];
   if (S->done) return;
   const T alpha = (T)S->alpha;
-  double rz = 0.0, rr = 0.0;
+  // per-thread partial sums in T (a thread covers ~n / (grid*block) entries); FP64 from the
+  // block sum on, so FP32 vectors cost no FP64 issue slots per element
+  T rz_t = (T)0, rr_t = (T)0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     x[i] = fma(alpha, p[i], x[i]);
     const T ri = fma(-alpha, q[i], r[i]);
     r[i] = ri;
-    rz += (double)ri * (double)(dinv[i] * ri);
-    rr += (double)ri * (double)ri;
+    rz_t = fma(ri, dinv[i] * ri, rz_t);
+    rr_t = fma(ri, ri, rr_t);
   }
-  rz = block_sum<kVecBlock>(rz, sh);
-  rr = block_sum<kVecBlock>(rr, sh);
+  double rz = block_sum<kVecBlock>((double)rz_t, sh);
+  double rr = block_sum<kVecBlock>((double)rr_t, sh);
   if (threadIdx.x == 0) {
     partials[2 * blockIdx.x] = rz;
     partials[2 * blockIdx.x + 1] = rr;
@@ -271,8 +396,12 @@ __global__ void __launch_bounds__(kVecBlock)
       S->converged = 1;
     } else if (S->iter >= S->maxit) {
       S->done = 1;
+    } else if (S->delta2 > 0.0 && tot[1] < S->delta2 * S->rmax2) {
+      S->done = 1;  // hand over to the host for an FP64 reliable update
+      S->need_update = 1;
     }
     S->beta = S->rz != 0.0 ? tot[0] / S->rz : 0.0;
+    S->rz_prev = S->rz;
     S->rz = tot[0];
   }
 }
@@ -370,6 +499,77 @@ __global__ void k_dot_self(int64_t n, const double* __restrict__ v, double* __re
     *out = tot[0];
 }
 
+// ---- reliable updates of the mixed-precision CG ---------------------------------------------
+// x64 += x32; x32 = 0
+__global__ void k_merge(int64_t n, double* __restrict__ x64, float* __restrict__ x32) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x64[i] += (double)x32[i];
+    x32[i] = 0.f;
+  }
+}
+
+// After r64 = b - A64 x64: stop if converged; else r32 = r64, rz = r.Dr, rp = r.p, and the
+// last block sets c = rp/rz (to re-orthogonalise p against the new r) and beta = rz/rz_prev.
+__global__ void __launch_bounds__(kVecBlock)
+    k_restart32(int64_t n, const double* __restrict__ r64, float* __restrict__ r32,
+                const float* __restrict__ p, const float* __restrict__ dinv,
+                double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kVecBlock / 32];
+  if (S->rr64 <= S->tol2) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      S->converged = 1;
+      S->done = 1;
+      S->need_update = 0;
+    }
+    return;
+  }
+  double rz = 0.0, rp = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float ri = (float)r64[i];
+    r32[i] = ri;
+    rz += (double)ri * (double)(dinv[i] * ri);
+    rp += (double)ri * (double)p[i];
+  }
+  rz = block_sum<kVecBlock>(rz, sh);
+  rp = block_sum<kVecBlock>(rp, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = rz;
+    partials[2 * blockIdx.x + 1] = rp;
+  }
+  double tot[2];
+  if (last_block_reduce<kVecBlock, 2>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->alpha = tot[0] != 0.0 ? tot[1] / tot[0] : 0.0;  // c (reused field)
+    S->beta = S->rz_prev != 0.0 ? tot[0] / S->rz_prev : 0.0;
+    S->rz = tot[0];
+    S->rmax2 = S->rr64;
+    S->rr = S->rr64;
+    S->need_update = 0;
+    S->converged = 0;
+    S->done = (S->iter >= S->maxit || !isfinite(tot[0])) ? 1 : 0;
+  }
+}
+
+// p = beta (p - c z) + z with z = D r (c in S->alpha)
+__global__ void k_restart_dir(int64_t n, float* __restrict__ p, const float* __restrict__ r,
+                              const float* __restrict__ dinv, const SolverState* S) {
+  if (S->done) return;
+  const float c = (float)S->alpha, beta = (float)S->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float z = dinv[i] * r[i];
+    p[i] = fma(beta, p[i] - c * z, z);
+  }
+}
+
+__global__ void k_set_reliable(SolverState* S, double delta2) {
+  S->delta2 = delta2;
+  S->rmax2 = S->bb;
+  S->rr64 = S->bb;
+}
+
 // ---- host drivers -------------------------------------------------------------------------
 struct SolverWork {
   SolverState* S;      // device
@@ -386,13 +586,35 @@ static int read_state(gfe_ctx* ctx, SolverWork& w) {
 }
 
 // Runs PCG on A (values of type T) for rhs*scale from x=0 until done; returns iterations.
+// Launches chunks of CG iterations until the device sets `done`.
+template <typename T, class Op>
+static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* x, T* r, T* p,
+                   T* q, int check_every, SolverWork& w) {
+  const int64_t n = A->nrows;
+  const unsigned gv = (unsigned)(ctx->num_sms * 4);
+  const unsigned gs = grid_for(n, kSpmvBlock);
+  for (;;) {
+    for (int k = 0; k < check_every; ++k) {
+      timer_begin(ctx, sizeof(T) == 4 ? GFE_KT_SPMV32 : GFE_KT_SPMV64);
+      k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
+      timer_end(ctx);
+      k_cg_update<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
+      k_cg_direction<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
+      ctx->launches += 3;
+    }
+    GFE_CUDA_TRY(cudaGetLastError());
+    GFE_TRY(read_state(ctx, w));
+    if (w.hS->done) break;
+  }
+  return GFE_OK;
+}
+
 template <typename T>
 static int run_pcg(gfe_ctx* ctx, gfe_matrix* A, const T* sval, const T* dinv, const void* rhs,
                    bool rhs_is_double, double scale, T* x, T* r, T* p, T* q, double rtol,
                    int maxit, int check_every, SolverWork& w, int* iters, int* converged) {
   const int64_t n = A->nrows;
   const unsigned gv = (unsigned)(ctx->num_sms * 4);
-  const unsigned gs = grid_for(n, kSpmvBlock);
   GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
   int maxit_field = maxit;
   GFE_CUDA_TRY(cudaMemcpyAsync(&w.S->maxit, &maxit_field, sizeof(int), cudaMemcpyHostToDevice,
@@ -404,24 +626,9 @@ static int run_pcg(gfe_ctx* ctx, gfe_matrix* A, const T* sval, const T* dinv, co
     k_cg_init<T, float><<<gv, kVecBlock, 0, ctx->stream>>>(n, (const float*)rhs, scale, x, r, p,
                                                           dinv, w.partials, w.S, rtol * rtol);
   ctx->launches++;
-  const int64_t* sptr = A->sell_ptr.as<int64_t>();
-  const int32_t* scol = A->sell_col.as<int32_t>();
-  int done_iters = 0;
-  for (;;) {
-    for (int k = 0; k < check_every; ++k) {
-      timer_begin(ctx, sizeof(T) == 4 ? GFE_KT_SPMV32 : GFE_KT_SPMV64);
-      k_cg_spmv_dot<T><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, sptr, scol, sval, p, q,
-                                                           w.partials, w.S);
-      timer_end(ctx);
-      k_cg_update<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
-      k_cg_direction<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
-      ctx->launches += 3;
-    }
-    GFE_CUDA_TRY(cudaGetLastError());
-    GFE_TRY(read_state(ctx, w));
-    done_iters = w.hS->iter;
-    if (w.hS->done) break;
-  }
+  SellOp<T> op{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval};
+  GFE_TRY((iterate<T, SellOp<T>>(ctx, A, op, dinv, x, r, p, q, check_every, w)));
+  const int done_iters = w.hS->iter;
   *iters = done_iters;
   *converged = w.hS->converged;
   return GFE_OK;
@@ -452,7 +659,7 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
   double* v64 = ctx->scratch[SCR_SOLVER].as<double>();
   const double* dinv64 = A->dinv64.as<double>();
   const float* dinv32 = A->dinv32.as<float>();
-  DevBuf ones;
+  DevBuf ones(ctx);
   if (!jac) {
     GFE_TRY(ones.reserve(n8 + sizeof(float) * n + 64));
     std::vector<double> h1(n, 1.0);
@@ -478,6 +685,64 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
     GFE_TRY(run_pcg<double>(ctx, A, A->sell_val64.as<double>(), dinv64, d_b, true, 1.0, d_x, r,
                             p, q, o->rtol, maxit, check_every, w, &it, &conv));
     rep->iterations = it;
+  } else if (o->method == GFE_SOLVER_MIXED_CG) {
+    // FP32 PCG with FP64 reliable updates: whenever the FP32 recursive residual has dropped
+    // by delta since the last update (or meets rtol), x64 absorbs the FP32 correction, the
+    // true residual b - A x64 is formed in FP64 and replaces the FP32 one, and the search
+    // direction is re-orthogonalised against it and continued (no restart).
+    double* r64 = v64;
+    float* f = (float*)ctx->scratch[SCR_SOLVER2].ptr;
+    float* x32 = f;
+    float* r32 = f + n;
+    float* p32 = f + 2 * n;
+    float* q32 = f + 3 * n;
+    const unsigned gv = (unsigned)(ctx->num_sms * 4);
+    const double delta = o->inner_rtol > 0 ? o->inner_rtol : 0.1;
+    GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
+    GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
+    int maxit_field = maxit;
+    GFE_CUDA_TRY(cudaMemcpyAsync(&w.S->maxit, &maxit_field, sizeof(int), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    k_cg_init<float, double><<<gv, kVecBlock, 0, ctx->stream>>>(
+        n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
+    k_set_reliable<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta);
+    ctx->launches += 2;
+    int updates = 0;
+    GFE_TRY(build_dia(ctx, A));
+    for (;;) {
+      if (A->dia_valid) {
+        DiaOp<float> op{A->dia_val32.as<float>(), n, {}};
+        for (int d = 0; d < A->dia_ndiag; ++d) op.o.off[d] = A->dia_off[d];
+        op.o.nd = A->dia_ndiag;
+        GFE_TRY((iterate<float, DiaOp<float>>(ctx, A, op, dinv32, x32, r32, p32, q32,
+                                              check_every, w)));
+      } else {
+        SellOp<float> op{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(),
+                         A->sell_val32.as<float>()};
+        GFE_TRY((iterate<float, SellOp<float>>(ctx, A, op, dinv32, x32, r32, p32, q32,
+                                               check_every, w)));
+      }
+      if (w.hS->iter >= maxit || !std::isfinite(w.hS->rr)) break;
+      // reliable update
+      k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
+      timer_begin(ctx, GFE_KT_RESIDUAL64);
+      k_residual64<<<grid_for(n, kSpmvBlock), kSpmvBlock, 0, ctx->stream>>>(
+          n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(),
+          d_x, d_b, r64, w.partials, &w.S->rr64, &w.S->ticket[2]);
+      timer_end(ctx);
+      k_restart32<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, p32, dinv32, w.partials, w.S);
+      k_restart_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, r32, dinv32, w.S);
+      ctx->launches += 4;
+      ++updates;
+      GFE_CUDA_TRY(cudaGetLastError());
+      GFE_TRY(read_state(ctx, w));
+      if (w.hS->converged || w.hS->done) break;
+      if (updates > 1000) break;
+    }
+    rep->iterations = w.hS->iter;
+    rep->refinements = updates;
+    rep->operator_format = A->dia_valid ? 1 : 0;
+    rep->ndiag = A->dia_valid ? A->dia_ndiag : 0;
   } else if (o->method == GFE_SOLVER_IR_CG) {
     double* r64 = v64;  // FP64 residual
     float* f = (float*)ctx->scratch[SCR_SOLVER2].ptr;

@@ -30,8 +30,8 @@ class ReferenceFE:
 class FESpace:
     def __init__(self, model: CartesianDiscreteModel, reffe: ReferenceFE, dirichlet_tags=(),
                  dirichlet_masks=None):
-        if reffe.order != 1:
-            raise NotImplementedError("only first-order Lagrangian spaces are provided")
+        if reffe.order not in (1, 2):
+            raise NotImplementedError("Lagrangian spaces of order 1 and 2 are provided")
         lib = _lib.load()
         self.model = model
         self.reffe = reffe
@@ -39,6 +39,9 @@ class FESpace:
             dirichlet_tags = [dirichlet_tags]
         self.dirichlet_tags = list(dirichlet_tags)
         nc = reffe.ncomp
+        if reffe.order == 2:
+            self._conforming(lib, dirichlet_masks)
+            return
         node_to_tag = model.get_face_labeling().get_face_tag_index(self.dirichlet_tags, 0)
         ntags = max(len(self.dirichlet_tags), 1)
         if dirichlet_masks is None:
@@ -59,6 +62,33 @@ class FESpace:
             _lib.ptr(ndiri)))
         self.nfree = int(nfree[0])
         self.ndiri = int(ndiri[0])
+
+    def _conforming(self, lib, dirichlet_masks):
+        """Q2 numbering (ConformingFESpaces.jl:367-636) through gfe_cartesian_conforming_dofs."""
+        model, nc = self.model, self.reffe.ncomp
+        labels = model.get_face_labeling()
+        D = model.dim
+        ntags = max(len(self.dirichlet_tags), 1)
+        ent_to_tag = np.zeros(3 ** D, dtype=np.int8)
+        for e in range(1, 3 ** D + 1):
+            for k, t in enumerate(self.dirichlet_tags):
+                if e in labels.tag_entities[labels._tag_index(t)]:
+                    ent_to_tag[e - 1] = k + 1
+                    break
+        if dirichlet_masks is None:
+            masks = np.ones((ntags, nc), dtype=np.uint8)
+        else:
+            masks = np.asarray(dirichlet_masks, dtype=np.uint8).reshape(len(self.dirichlet_tags), nc)
+        part = np.asarray(model.partition, dtype=np.int64)
+        self.cell_dof_ids = np.empty((model.num_cells(), 3 ** D * nc), dtype=np.int32)
+        nfree = np.zeros(1, dtype=np.int32)
+        ndiri = np.zeros(1, dtype=np.int32)
+        _lib.check(lib.gfe_cartesian_conforming_dofs(
+            D, 2, _lib.ptr(part), nc, _lib.ptr(ent_to_tag), _lib.ptr(np.ascontiguousarray(masks)),
+            _lib.ptr(self.cell_dof_ids), _lib.ptr(nfree), _lib.ptr(ndiri)))
+        self.nfree = int(nfree[0])
+        self.ndiri = int(ndiri[0])
+        self.node_comp_to_dof = None
 
     def num_free_dofs(self) -> int:
         return self.nfree

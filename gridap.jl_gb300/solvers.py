@@ -5,7 +5,8 @@ symbolic_setup -> numerical_setup -> solve!(x, ns, b). These classes are that pl
 
   - CGSolver(rtol, maxiter, precond="jacobi"): FP64 preconditioned CG;
   - IRCGSolver(rtol, inner_rtol, ...): FP32 PCG inside FP64 iterative refinement: the outer
-    loop forms r = b - A x and updates x in FP64, the inner solves A d = r in FP32.
+    loop forms r = b - A x and updates x in FP64, the inner solves A d = r in FP32;
+  - MixedCGSolver(rtol, ...): FP32 PCG with FP64 reliable updates (no restarts).
 
 Both stop on the FP64 relative residual ||b - A x|| <= rtol ||b|| and report it.
 """
@@ -27,6 +28,8 @@ class SolveReport:
         self.converged = bool(r.converged)
         self.status = r.status
         self.relres = r.relres
+        self.operator_format = ("sliced-ELL", "diagonal")[r.operator_format]
+        self.ndiag = r.ndiag
 
     def __repr__(self):
         return (f"SolveReport(iterations={self.iterations}, refinements={self.refinements}, "
@@ -55,6 +58,17 @@ class CGSolver(LinearSolver):
 
 class IRCGSolver(LinearSolver):
     method = _lib.GFE_SOLVER_IR_CG
+
+
+class MixedCGSolver(LinearSolver):
+    """FP32 PCG with FP64 reliable updates: x accumulates in FP64 and the FP32 residual is
+    replaced by the FP64 true residual b - A x every time it has dropped by `inner_rtol`
+    (default 0.1); the search direction is re-orthogonalised and kept."""
+    method = _lib.GFE_SOLVER_MIXED_CG
+
+    def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, precond: str = "jacobi",
+                 inner_rtol: float = 0.1, check_every: int = 0):
+        super().__init__(rtol, maxiter, precond, inner_rtol, check_every)
 
 
 class SymbolicSetup:

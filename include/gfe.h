@@ -65,7 +65,8 @@ enum {
   GFE_KT_SPMV64 = 0,     /* FP64 SpMV + dot of the CG iteration */
   GFE_KT_SPMV32 = 1,     /* FP32 SpMV + dot of the inner CG iteration */
   GFE_KT_ASSEMBLE = 2,   /* row-gather numeric assembly */
-  GFE_KT_RESIDUAL64 = 3  /* FP64 residual r = b - A x of iterative refinement */
+  GFE_KT_RESIDUAL64 = 3, /* FP64 residual r = b - A x of iterative refinement */
+  GFE_KT_ELEMENT = 4     /* element (cell-integral) kernels */
 };
 int gfe_ctx_set_timing(gfe_ctx* ctx, int enable);
 int gfe_ctx_kernel_time(gfe_ctx* ctx, int kernel, double* total_ms, int64_t* launches);
@@ -88,6 +89,20 @@ int gfe_clagrangian_dofs(int64_t nnodes, const int8_t* node_to_tag, int ncomp,
                          const int32_t* cell_node_ids, const int32_t* lnode_comp_to_ldof,
                          int32_t* node_comp_to_dof, int32_t* cell_dof_ids, int32_t* nfree,
                          int32_t* ndiri);
+
+/* Conforming dof numbering of a Lagrangian space of order 2 (Q2: 9 nodes per QUAD, 27 per
+ * HEX) on a Cartesian grid: topology edges and faces numbered first-touch over cells and
+ * local faces, labels of every face from the domain box, dofs numbered dimension by dimension
+ * (vertices, edges, faces, cell interiors) in face order with the components of a node
+ * consecutive; Dirichlet dofs negative. entity_to_tag[3^dim] gives, per box entity, the
+ * 1-based position of the first Dirichlet tag containing it (0 = none), tag_masks[ntags*ncomp]
+ * the component masks. cell_dof_ids: ncells x (3^dim*ncomp), component-major over the nodes
+ * in Gridap's local order (vertices, edges, faces, interior).
+ * Replaces FESpaces/ConformingFESpaces.jl:367-636 with Geometry/GridTopologies.jl:1184-1250
+ * and Geometry/CartesianDiscreteModels.jl:133-260. */
+int gfe_cartesian_conforming_dofs(int dim, int order, const int64_t* partition, int ncomp,
+                                  const int8_t* entity_to_tag, const uint8_t* tag_masks,
+                                  int32_t* cell_dof_ids, int32_t* nfree, int32_t* ndiri);
 
 /* ---- assembly: symbolic ------------------------------------------------------------------ */
 /* Builds the sparsity pattern of the matrix that assembling cell matrices over
@@ -126,7 +141,11 @@ int gfe_numeric_loop_vector(gfe_ctx* ctx, int64_t ncells, int nd, const int32_t*
                             const double* cellvecs, int64_t nrows, double* b);
 
 /* ---- assembly: fused integrate + assemble for recognised weak forms ----------------------- */
-enum { GFE_REFFE_Q1 = 1 };                        /* lexicographic Lagrangian Q1 on QUAD/HEX */
+enum {
+  GFE_REFFE_Q1 = 1, /* Lagrangian Q1 on QUAD/HEX, lexicographic nodes */
+  GFE_REFFE_Q2 = 2  /* Lagrangian Q2 on QUAD/HEX (9/27 nodes: vertices, edges, faces, interior)
+                       on (multi)linear cells given by node_coords + cell_node_ids (vertices) */
+};
 enum { GFE_GEOM_CARTESIAN = 0, GFE_GEOM_NODAL = 1 };
 enum { GFE_FORM_DIFFUSION = 1 };                  /* a(u,v) = int kappa grad(v).grad(u) */
 enum { GFE_COEF_ONE = 0, GFE_COEF_CONST = 1, GFE_COEF_CELL = 2 };
@@ -162,7 +181,9 @@ typedef struct gfe_problem {
   int32_t source_kind;  /* GFE_SRC_* */
   const double* source;
   int64_t source_len;   /* number of doubles at `source` */
-  int32_t precision;    /* GFE_PREC_*: arithmetic of the cell integrals (scatter stays FP64) */
+  int32_t precision;    /* GFE_PREC_*: arithmetic of the cell integrals (scatter stays FP64);
+                           FP32 on Q2 uses the tensor cores (TF32 operands, FP32 accumulate,
+                           FP64 Jacobians) */
 } gfe_problem;
 
 /* Integrates the recognised bilinear and linear forms over every cell and assembles them
@@ -177,25 +198,30 @@ int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* problem, gfe
                                    double* b);
 
 /* ---- linear solve ------------------------------------------------------------------------ */
-enum { GFE_SOLVER_CG = 0, GFE_SOLVER_IR_CG = 1 };
+enum { GFE_SOLVER_CG = 0, GFE_SOLVER_IR_CG = 1, GFE_SOLVER_MIXED_CG = 2 };
 enum { GFE_PC_NONE = 0, GFE_PC_JACOBI = 1 };
 
 typedef struct gfe_solver_opts {
   int32_t method;       /* GFE_SOLVER_CG: FP64 PCG; GFE_SOLVER_IR_CG: FP32 inner PCG inside
-                           FP64 iterative refinement */
+                           FP64 iterative refinement (restarted per refinement step);
+                           GFE_SOLVER_MIXED_CG: FP32 PCG with FP64 reliable updates (x and the
+                           true residual in FP64, search direction kept) */
   int32_t precond;      /* GFE_PC_* */
   double rtol;          /* stop when ||b - A x||_2 <= rtol ||b||_2 (FP64 residual) */
   int32_t maxiter;      /* total inner iterations allowed */
-  double inner_rtol;    /* GFE_SOLVER_IR_CG: relative reduction per refinement step */
+  double inner_rtol;    /* IR_CG: relative reduction per refinement step; MIXED_CG: residual
+                           reduction between reliable updates (default 0.1) */
   int32_t check_every;  /* iterations between host convergence checks (0 = default) */
 } gfe_solver_opts;
 
 typedef struct gfe_solve_report {
   int32_t iterations;       /* inner (Krylov) iterations */
-  int32_t refinements;      /* outer FP64 refinement steps (IR-CG), 0 for CG */
+  int32_t refinements;      /* FP64 refinement steps (IR-CG) or reliable updates (MIXED_CG) */
   int32_t converged;        /* 1 when the FP64 residual met rtol */
   int32_t status;           /* GFE_OK or the code that stopped the solver */
   double relres;            /* final ||b - A x|| / ||b|| in FP64, recomputed after the solve */
+  int32_t operator_format;  /* SpMV format of the (inner) operator: 0 sliced ELL, 1 diagonal */
+  int32_t ndiag;            /* diagonals of the diagonal format (0 otherwise) */
 } gfe_solve_report;
 
 /* Solves A x = b. Replaces the LinearSolver protocol's numerical_setup + solve!

@@ -16,6 +16,9 @@
 #include <omp.h>
 #endif
 
+static double det_t(int D, const double* a);
+static void inv_t(int D, const double* a, double* r);
+
 /* ====================================================================================== */
 /* polytopes                                                                               */
 /* ====================================================================================== */
@@ -212,6 +215,283 @@ void orc_clagrangian_numbering(int64_t nnodes, const int8_t* node_to_tag, int nc
         cell_dofs[cell * ndof_cell + ldof - 1] = node_comp_to_dof[node * ncomp + c];
       }
     }
+}
+
+/* ====================================================================================== */
+/* conforming Q2 numbering on Cartesian grids                                              */
+/* ====================================================================================== */
+
+/* local vertices of each n-cube face (lexicographic in the face's own coordinates) */
+static int face_lvertices(int D, const int32_t* ext, const int32_t* anc, int32_t* lv) {
+  int nv = 0;
+  int span[3], ns = 0;
+  for (int d = 0; d < D; ++d)
+    if (ext[d]) span[ns++] = d;
+  for (int m = 0; m < (1 << ns); ++m) {
+    int v = 0;
+    for (int d = 0; d < D; ++d) {
+      int bit = anc[d];
+      for (int t = 0; t < ns; ++t)
+        if (span[t] == d) bit = (m >> t) & 1;
+      v |= bit << d;
+    }
+    lv[nv++] = v;
+  }
+  return nv;
+}
+
+static int cmp_i32(const void* a, const void* b) {
+  int32_t x = *(const int32_t*)a, y = *(const int32_t*)b;
+  return (x > y) - (x < y);
+}
+
+int orc_conforming_q2(int D, const int64_t* part, int ncomp, const int8_t* entity_to_tag,
+                      const uint8_t* tag_masks, int32_t* cell_dofs, int32_t* nfree,
+                      int32_t* ndiri) {
+  int32_t ext[27 * 3], anc[27 * 3];
+  const int nlf = orc_ncube_faces(D, ext, anc); /* 3^D local faces incl. the cell */
+  int32_t lf_dim[27], lf_nv[27], lf_v[27][8];
+  for (int f = 0; f < nlf; ++f) {
+    lf_dim[f] = 0;
+    for (int d = 0; d < D; ++d) lf_dim[f] += ext[f * D + d];
+    lf_nv[f] = face_lvertices(D, ext + f * D, anc + f * D, lf_v[f]);
+  }
+  int64_t n[3] = {1, 1, 1}, np[3] = {1, 1, 1};
+  for (int d = 0; d < D; ++d) {
+    n[d] = part[d];
+    np[d] = part[d] + 1;
+  }
+  const int64_t ncells = n[0] * n[1] * n[2];
+  const int64_t nverts = np[0] * np[1] * np[2];
+  const int nvc = 1 << D;
+  int32_t* cv = (int32_t*)malloc(sizeof(int32_t) * ncells * nvc);
+  orc_cartesian_cell_nodes(D, part, cv);
+  /* vertex -> cells */
+  int64_t* vptr = (int64_t*)calloc(nverts + 1, sizeof(int64_t));
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int a = 0; a < nvc; ++a) vptr[cv[c * nvc + a]] += 1;
+  for (int64_t v = 0; v < nverts; ++v) vptr[v + 1] += vptr[v];
+  int64_t* vfill = (int64_t*)calloc(nverts, sizeof(int64_t));
+  int32_t* vcells = (int32_t*)malloc(sizeof(int32_t) * vptr[nverts]);
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int a = 0; a < nvc; ++a) {
+      int64_t v = cv[c * nvc + a] - 1;
+      vcells[vptr[v] + vfill[v]++] = (int32_t)c; /* ascending cell order */
+    }
+  /* cell -> face ids per local face (vertices = node ids; cell interiors = cell ids); faces
+   * of each dimension numbered first-touch over (cell, local face) */
+  int32_t* cf = (int32_t*)malloc(sizeof(int32_t) * ncells * nlf);
+  for (int64_t i = 0; i < ncells * nlf; ++i) cf[i] = 0;
+  int32_t nface_d[4] = {0, 0, 0, 0};
+  for (int dd = 1; dd < D; ++dd) {
+    int32_t next = 0;
+    for (int64_t c = 0; c < ncells; ++c)
+      for (int f = 0; f < nlf; ++f) {
+        if (lf_dim[f] != dd || cf[c * nlf + f] != 0) continue;
+        int32_t fv[8];
+        for (int k = 0; k < lf_nv[f]; ++k) fv[k] = cv[c * nvc + lf_v[f][k]];
+        qsort(fv, lf_nv[f], sizeof(int32_t), cmp_i32);
+        ++next;
+        /* cells around all vertices of the face: intersect vertex -> cells lists */
+        int64_t v0 = fv[0] - 1;
+        for (int64_t p = vptr[v0]; p < vptr[v0 + 1]; ++p) {
+          int32_t c2 = vcells[p];
+          int ok = 1;
+          for (int k = 1; k < lf_nv[f] && ok; ++k) {
+            int64_t vk = fv[k] - 1, hit = 0;
+            for (int64_t q = vptr[vk]; q < vptr[vk + 1]; ++q)
+              if (vcells[q] == c2) hit = 1;
+            ok = (int)hit;
+          }
+          if (!ok) continue;
+          /* local face of c2 with the same vertex set */
+          for (int f2 = 0; f2 < nlf; ++f2) {
+            if (lf_dim[f2] != dd) continue;
+            int32_t gv[8];
+            for (int k = 0; k < lf_nv[f2]; ++k) gv[k] = cv[c2 * nvc + lf_v[f2][k]];
+            qsort(gv, lf_nv[f2], sizeof(int32_t), cmp_i32);
+            if (memcmp(gv, fv, sizeof(int32_t) * lf_nv[f]) == 0) cf[(int64_t)c2 * nlf + f2] = next;
+          }
+        }
+      }
+    nface_d[dd] = next;
+  }
+  nface_d[0] = (int32_t)nverts;
+  nface_d[D] = (int32_t)ncells;
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int f = 0; f < nlf; ++f) {
+      if (lf_dim[f] == 0) cf[c * nlf + f] = cv[c * nvc + lf_v[f][0]];
+      if (lf_dim[f] == D) cf[c * nlf + f] = (int32_t)(c + 1);
+    }
+  /* labels: a d-face with one cell around takes that cell's local face id; one with fewer
+   * than 2^(D-d) cells is "boundary" and takes the first non-interior, non-boundary label of
+   * a higher-dimensional face containing it (CartesianDiscreteModels.jl:195-260) */
+  int32_t* lab[4];
+  int32_t* ncell_around[4];
+  for (int dd = 0; dd <= D; ++dd) {
+    lab[dd] = (int32_t*)malloc(sizeof(int32_t) * (nface_d[dd] + 1));
+    ncell_around[dd] = (int32_t*)calloc(nface_d[dd] + 1, sizeof(int32_t));
+  }
+  const int32_t interior = nlf, boundary = -1;
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int f = 0; f < nlf; ++f) ncell_around[lf_dim[f]][cf[c * nlf + f]] += 1;
+  for (int dd = 0; dd <= D; ++dd)
+    for (int32_t i = 1; i <= nface_d[dd]; ++i) {
+      int32_t k = ncell_around[dd][i];
+      lab[dd][i] = interior;
+      if (dd < D && k != (1 << (D - dd)) && k != 1) lab[dd][i] = boundary;
+    }
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int f = 0; f < nlf; ++f) {
+      int dd = lf_dim[f];
+      int32_t i = cf[c * nlf + f];
+      if (dd < D && ncell_around[dd][i] == 1) lab[dd][i] = f + 1;
+    }
+  /* fix boundary labels from higher-dimensional faces, ascending dimension j > d; the
+   * d-face -> j-faces relation is taken from the cells' local faces */
+  for (int dd = 0; dd <= D - 2; ++dd)
+    for (int jj = dd + 1; jj <= D - 1; ++jj)
+      for (int64_t c = 0; c < ncells; ++c)
+        for (int f = 0; f < nlf; ++f) {
+          if (lf_dim[f] != dd) continue;
+          int32_t i = cf[c * nlf + f];
+          if (lab[dd][i] != boundary) continue;
+          /* j-faces of this cell that contain local face f, in local order */
+          for (int g = 0; g < nlf; ++g) {
+            if (lf_dim[g] != jj) continue;
+            int contains = 1;
+            for (int k = 0; k < lf_nv[f]; ++k) {
+              int in = 0;
+              for (int m = 0; m < lf_nv[g]; ++m) in |= lf_v[g][m] == lf_v[f][k];
+              contains &= in;
+            }
+            if (!contains) continue;
+            int32_t gl = lab[jj][cf[c * nlf + g]];
+            if (gl != interior && gl != boundary) {
+              lab[dd][i] = gl;
+              break;
+            }
+          }
+        }
+  /* dofs: dimension by dimension, face id order, one node per face, comps inside */
+  int32_t* fdof[4];
+  int32_t nf = 0, nd = 0;
+  for (int dd = 0; dd <= D; ++dd) {
+    fdof[dd] = (int32_t*)malloc(sizeof(int32_t) * (nface_d[dd] + 1) * ncomp);
+    for (int32_t i = 1; i <= nface_d[dd]; ++i) {
+      int32_t ent = lab[dd][i];
+      int tag = (ent >= 1 && ent <= nlf) ? entity_to_tag[ent - 1] : 0;
+      for (int k = 0; k < ncomp; ++k) {
+        int diri = tag > 0 && tag_masks[(tag - 1) * ncomp + k];
+        fdof[dd][i * ncomp + k] = diri ? -(++nd) : ++nf;
+      }
+    }
+  }
+  const int ndc = nlf * ncomp;
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int f = 0; f < nlf; ++f)
+      for (int k = 0; k < ncomp; ++k)
+        cell_dofs[c * ndc + k * nlf + f] = fdof[lf_dim[f]][cf[c * nlf + f] * ncomp + k];
+  *nfree = nf;
+  *ndiri = nd;
+  for (int dd = 0; dd <= D; ++dd) {
+    free(lab[dd]);
+    free(ncell_around[dd]);
+    free(fdof[dd]);
+  }
+  free(cv); free(vptr); free(vfill); free(vcells); free(cf);
+  return 0;
+}
+
+/* Q2 node of local face f: lattice index 2*anchor along fixed directions, 1 along spanned */
+void orc_q2_shapes(int D, int npts, const double* pts, double* phi, double* dphi) {
+  int32_t ext[27 * 3], anc[27 * 3];
+  const int nn = orc_ncube_faces(D, ext, anc);
+  for (int p = 0; p < npts; ++p)
+    for (int a = 0; a < nn; ++a) {
+      double L[3], dL[3];
+      for (int d = 0; d < D; ++d) {
+        const int idx = ext[a * D + d] ? 1 : 2 * anc[a * D + d];
+        const double t = pts[p * D + d];
+        if (idx == 0) {
+          L[d] = 2.0 * (t - 0.5) * (t - 1.0);
+          dL[d] = 4.0 * t - 3.0;
+        } else if (idx == 1) {
+          L[d] = 4.0 * t * (1.0 - t);
+          dL[d] = 4.0 - 8.0 * t;
+        } else {
+          L[d] = 2.0 * t * (t - 0.5);
+          dL[d] = 4.0 * t - 1.0;
+        }
+      }
+      double v = 1.0;
+      for (int d = 0; d < D; ++d) v *= L[d];
+      phi[p * nn + a] = v;
+      for (int k = 0; k < D; ++k) {
+        double g = 1.0;
+        for (int d = 0; d < D; ++d) g *= (d == k) ? dL[d] : L[d];
+        dphi[(p * nn + a) * D + k] = g;
+      }
+    }
+}
+
+int orc_q2_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_vertices,
+                                 const double* coords, const double* kappa_cell, int nq,
+                                 const double* qx, const double* qw, int fkind,
+                                 const double* fdata, double* cellmats, double* cellvecs) {
+  const int nv = 1 << D, nn = D == 2 ? 9 : 27;
+  double* phi1 = (double*)malloc(sizeof(double) * nq * nv);
+  double* dphi1 = (double*)malloc(sizeof(double) * nq * nv * D);
+  double* phi = (double*)malloc(sizeof(double) * nq * nn);
+  double* dphi = (double*)malloc(sizeof(double) * nq * nn * D);
+  double* g = (double*)malloc(sizeof(double) * nn * D);
+  orc_q1_shapes(D, nq, qx, phi1, dphi1);
+  orc_q2_shapes(D, nq, qx, phi, dphi);
+  for (int64_t c = 0; c < ncells; ++c) {
+    const int32_t* vs = cell_vertices + c * nv;
+    double* K = cellmats ? cellmats + c * nn * nn : NULL;
+    double* bv = cellvecs ? cellvecs + c * nn : NULL;
+    if (K) memset(K, 0, sizeof(double) * nn * nn);
+    if (bv) memset(bv, 0, sizeof(double) * nn);
+    const double kap = kappa_cell ? kappa_cell[c] : 1.0;
+    for (int q = 0; q < nq; ++q) {
+      double Jt[9] = {0}, iJt[9];
+      for (int a = 0; a < nv; ++a) {
+        const double* xa = coords + (int64_t)(vs[a] - 1) * D;
+        for (int k = 0; k < D; ++k)
+          for (int l = 0; l < D; ++l) Jt[k * D + l] += dphi1[(q * nv + a) * D + k] * xa[l];
+      }
+      const double dJ = det_t(D, Jt);
+      if (!(dJ > 0.0) && !(dJ < 0.0)) {
+        free(phi1); free(dphi1); free(phi); free(dphi); free(g);
+        return -1;
+      }
+      inv_t(D, Jt, iJt);
+      const double dV = fabs(dJ) * qw[q];
+      for (int a = 0; a < nn; ++a)
+        for (int k = 0; k < D; ++k) {
+          double s = 0.0;
+          for (int l = 0; l < D; ++l) s += iJt[k * D + l] * dphi[(q * nn + a) * D + l];
+          g[a * D + k] = s;
+        }
+      if (K)
+        for (int j = 0; j < nn; ++j)
+          for (int i = 0; i < nn; ++i) {
+            double s = 0.0;
+            if (kappa_cell)
+              for (int k = 0; k < D; ++k) s += (kap * g[i * D + k]) * g[j * D + k];
+            else
+              for (int k = 0; k < D; ++k) s += g[i * D + k] * g[j * D + k];
+            K[i + j * nn] += s * dV;
+          }
+      if (bv && fkind != ORC_F_NONE) {
+        double fq = fkind == ORC_F_CONST ? fdata[0] : fdata[c * nq + q];
+        for (int i = 0; i < nn; ++i) bv[i] += (fq * phi[q * nn + i]) * dV;
+      }
+    }
+  }
+  free(phi1); free(dphi1); free(phi); free(dphi); free(g);
+  return 0;
 }
 
 /* ====================================================================================== */

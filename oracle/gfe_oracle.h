@@ -52,6 +52,25 @@ void orc_clagrangian_numbering(int64_t nnodes, const int8_t* node_to_tag, int nc
                                int32_t* node_comp_to_dof, int32_t* cell_dofs,
                                int32_t* nfree, int32_t* ndiri);
 
+/* ---- conforming Q2 numbering on Cartesian grids (FESpaces/ConformingFESpaces.jl:367-636) --
+ * Topology faces numbered first-touch (Geometry/GridTopologies.jl:1184-1250), face labels by
+ * Gridap's Cartesian rule (Geometry/CartesianDiscreteModels.jl:133-260), dofs by dimension
+ * then face id, own dofs "for node, for comp". entity_to_tag[3^D] (0 = untagged, else a
+ * 1-based tag index), tag_masks[ntags*ncomp]. cell_dofs: ncells x (3^D * ncomp), local
+ * order comp-major over the 3^D nodes (vertices, edges, faces, interior in n-cube order). */
+int orc_conforming_q2(int D, const int64_t* partition, int ncomp, const int8_t* entity_to_tag,
+                      const uint8_t* tag_masks, int32_t* cell_dofs, int32_t* nfree,
+                      int32_t* ndiri);
+/* Q2 Lagrange shape functions on the 3^D nodes in Gridap's order (n-cube faces: vertices,
+ * edges, faces, interior; one node at each face centre). */
+void orc_q2_shapes(int D, int npts, const double* pts, double* phi, double* dphi);
+/* Diffusion cell arrays for Q2 on Q1 (trilinear) geometry: nodal geometry from the 2^D
+ * cell vertices. Same steps as orc_q1_cell_arrays_diffusion. */
+int orc_q2_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_vertices,
+                                 const double* coords, const double* kappa_cell, int nq,
+                                 const double* qx, const double* qw, int fkind,
+                                 const double* fdata, double* cellmats, double* cellvecs);
+
 /* ---- quadrature (ReferenceFEs/Quadratures.jl:191-227, TensorProductQuadratures.jl:68-80) */
 void orc_gauss_legendre01(int n, double* x, double* w);
 /* Tensor-product Gauss-Legendre of a degree on [0,1]^D; returns npoints. */

@@ -48,6 +48,10 @@ def lib():
         L.orc_jitter_interior.argtypes = [C.c_int, P, P, P]
         L.orc_clagrangian_numbering.argtypes = [C.c_int64, P, C.c_int, P, C.c_int64, C.c_int, P,
                                                 P, P, P, P, P]
+        L.orc_conforming_q2.argtypes = [C.c_int, P, C.c_int, P, P, P, P, P]
+        L.orc_q2_shapes.argtypes = [C.c_int, C.c_int, P, P, P]
+        L.orc_q2_cell_arrays_diffusion.argtypes = [C.c_int, C.c_int64, P, P, P, C.c_int, P, P,
+                                                   C.c_int, P, P, P]
         L.orc_gauss_legendre01.argtypes = [C.c_int, P, P]
         L.orc_tensor_quadrature.argtypes = [C.c_int, C.c_int, P, P]
         L.orc_q1_shapes.argtypes = [C.c_int, C.c_int, P, P, P]
@@ -146,6 +150,74 @@ def clagrangian(node_to_tag, cell_nodes, ncomp=1, masks=None, lmap=None):
                                     _p(np.ascontiguousarray(cell_nodes)), _p(lmap), _p(node_dof),
                                     _p(cell_dofs), _p(nf), _p(ndr))
     return node_dof, cell_dofs, int(nf[0]), int(ndr[0])
+
+
+def conforming_q2(partition, tags, ncomp=1, masks=None):
+    """Q2 conforming numbering: (cell_dofs, nfree, ndiri)."""
+    D = len(partition)
+    names, ents = cartesian_tags(D)
+    ent_to_tag = np.zeros(3 ** D, np.int8)
+    for e in range(1, 3 ** D + 1):
+        for k, t in enumerate(tags):
+            te = ents[t - 1] if isinstance(t, (int, np.integer)) else ents[names.index(t)]
+            if e in te:
+                ent_to_tag[e - 1] = k + 1
+                break
+    ntags = max(len(tags), 1)
+    if masks is None:
+        masks = np.ones((ntags, ncomp), np.uint8)
+    masks = np.ascontiguousarray(masks, np.uint8)
+    part = np.asarray(partition, np.int64)
+    nc = int(np.prod(part))
+    cd = np.empty((nc, 3 ** D * ncomp), np.int32)
+    nf = np.zeros(1, np.int32)
+    nd = np.zeros(1, np.int32)
+    lib().orc_conforming_q2(D, _p(part), ncomp, _p(ent_to_tag), _p(masks), _p(cd), _p(nf),
+                            _p(nd))
+    return cd, int(nf[0]), int(nd[0])
+
+
+def q2_shapes(D, pts):
+    pts = np.ascontiguousarray(pts, np.float64)
+    nn = 3 ** D
+    phi = np.empty((pts.shape[0], nn))
+    dphi = np.empty((pts.shape[0], nn, D))
+    lib().orc_q2_shapes(D, pts.shape[0], _p(pts), _p(phi), _p(dphi))
+    return phi, dphi
+
+
+def q2_cell_arrays(D, cell_vertices, coords, degree, kappa=None, fkind=F_NONE, fdata=None):
+    qx, qw = tensor_quadrature(D, degree)
+    nc = cell_vertices.shape[0]
+    nn = 3 ** D
+    mats = np.zeros((nc, nn, nn))
+    vecs = np.zeros((nc, nn))
+    kap = None if kappa is None else np.ascontiguousarray(kappa, np.float64)
+    fd = None if fdata is None else np.ascontiguousarray(fdata, np.float64)
+    st = lib().orc_q2_cell_arrays_diffusion(
+        D, nc, _p(np.ascontiguousarray(cell_vertices)), _p(np.ascontiguousarray(coords)),
+        _p(kap), qx.shape[0], _p(qx), _p(qw), fkind, _p(fd), _p(mats), _p(vecs))
+    if st != 0:
+        raise RuntimeError("oracle: degenerate cell")
+    return np.ascontiguousarray(np.transpose(mats, (0, 2, 1))), vecs
+
+
+def poisson_q2(domain, partition, dirichlet_tags=("boundary",), kappa=None, fconst=None,
+               degree=4, jitter=None):
+    """Gridap's Q2 problem: numbering, cell arrays, CSC matrix and vector."""
+    D = len(partition)
+    coords, cells, ent = cartesian_model(domain, partition)
+    if jitter is not None:
+        coords = jitter_interior(partition, coords, jitter)
+    cd, nfree, ndiri = conforming_q2(partition, list(dirichlet_tags))
+    fk = F_NONE if fconst is None else F_CONST
+    fd = None if fconst is None else np.array([float(fconst)])
+    mats, vecs = q2_cell_arrays(D, cells, coords, degree, kappa, fk, fd)
+    out = dict(coords=coords, cells=cells, cell_dofs=cd, nfree=nfree, ndiri=ndiri,
+               cellmats=mats, cellvecs=vecs)
+    out["csc"] = assemble_csc(cd, cd, mats, nfree, nfree)
+    out["b"] = assemble_vector(cd, vecs, nfree)
+    return out
 
 
 # ---- quadrature / shapes -------------------------------------------------------------------

@@ -225,6 +225,56 @@ def test_ir_cg_reaches_fp64_tolerance(gg, orc):
     assert np.linalg.norm(x - x64) / np.linalg.norm(x64) < 1e-5
 
 
+def test_mixed_cg_reaches_fp64_tolerance_without_restarts(gg):
+    """FP32 PCG with FP64 reliable updates meets the FP64 residual with close to the FP64
+    iteration count (the search direction survives each update)."""
+    rng = np.random.default_rng(32)
+    part = (28, 26, 24)
+    kappa = np.exp(1.5 * rng.standard_normal(int(np.prod(part))))
+    fnod = rng.standard_normal(int(np.prod(np.array(part) + 1)))
+    _, V, A, b = _problem(gg, (0, 1) * 3, part, ("boundary",), kappa, gg.NodalField(fnod))
+    x64 = np.empty_like(b)
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.CGSolver(rtol=1e-8), A), A)
+    gg.solve_(x64, ns, b)
+    x = np.empty_like(b)
+    ns2 = gg.numerical_setup(gg.symbolic_setup(gg.MixedCGSolver(rtol=1e-8), A), A)
+    gg.solve_(x, ns2, b)
+    assert ns2.report.converged and ns2.report.relres <= 1e-8
+    assert ns2.report.refinements >= 3
+    assert ns2.report.iterations <= 1.25 * ns.report.iterations + 10
+    r = b - A.to_scipy() @ x
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1e-8 * 1.01
+    assert np.linalg.norm(x - x64) / np.linalg.norm(x64) < 1e-5
+
+
+def test_mixed_cg_on_permuted_numbering(gg, orc):
+    """A random renumbering of the free dofs leaves no small set of diagonals, so the FP32
+    operator falls back from the diagonal copy to the sliced-ELL one; same answer."""
+    rng = np.random.default_rng(33)
+    part = (14, 13, 12)
+    kappa = np.exp(rng.standard_normal(int(np.prod(part))))
+    ref = orc.poisson_q1((0, 1) * 3, part, ("boundary",), kappa=kappa, fkind=orc.F_CONST,
+                         fdata=np.array([1.0]))
+    n = ref["nfree"]
+    perm = rng.permutation(n) + 1
+    ids = ref["cell_dofs"].copy()
+    m = ids > 0
+    ids[m] = perm[ids[m] - 1]
+    m3 = gg.CartesianDiscreteModel((0, 1) * 3, part)
+    V = gg.FESpace(m3, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    assem = gg.SparseMatrixAssembler(V, V)
+    A = gg.symbolic_loop_matrix(assem, (None, ids, ids))
+    gg.numeric_loop_matrix(A, assem, (ref["cellmats"], ids, ids))
+    b = np.zeros(n)
+    gg.numeric_loop_vector(b, assem, (ref["cellvecs"], ids))
+    x = np.empty(n)
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.MixedCGSolver(rtol=1e-9), A), A)
+    gg.solve_(x, ns, b)
+    assert ns.report.converged and ns.report.relres <= 1e-9
+    xo, _, _ = orc.pcg(*ref["csc"], ref["b"], 1e-13)
+    assert np.linalg.norm(x[perm - 1] - xo) / np.linalg.norm(xo) < 1e-6
+
+
 def test_fp32_cell_integrals_close_to_fp64(gg):
     rng = np.random.default_rng(41)
     dom, part = (0, 1, 0, 1, 0, 1), (9, 8, 7)
@@ -319,3 +369,59 @@ def test_c5_scale_pattern_properties(gg):
     assert np.abs(sums).max() <= 1e-12 * np.abs(nz[diag_idx]).max()
     S = A.to_scipy()
     assert abs(S - S.T).max() == 0.0
+
+
+# ---- Q2 (config 2 shape, small) -------------------------------------------------------------
+@pytest.mark.parametrize("part,jit", [((4, 3), False), ((3, 4, 2), False), ((4, 3, 3), True)])
+def test_q2_fp64_matches_oracle(gg, orc, part, jit):
+    rng = np.random.default_rng(61 + len(part))
+    D = len(part)
+    nn = int(np.prod(np.array(part) + 1))
+    h = 1.0 / np.array(part)
+    jitter = rng.uniform(-0.2, 0.2, (nn, D)) * h if jit else None
+    kappa = np.exp(rng.standard_normal(int(np.prod(part))))
+    model = gg.CartesianDiscreteModel((0, 1) * D, part, node_jitter=jitter)
+    V = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, float, 2), dirichlet_tags="boundary")
+    dO = gg.Measure(gg.Triangulation(model), 4)
+    kap = gg.CellField(kappa)
+    op = gg.AffineFEOperator(lambda u, v: gg.integrate(kap * gg.inner(gg.grad(v), gg.grad(u)), dO),
+                             lambda v: gg.integrate(1.0 * v, dO), V, V)
+    ref = orc.poisson_q2((0, 1) * D, part, ("boundary",), kappa=kappa, fconst=1.0, degree=4,
+                         jitter=jitter)
+    assert V.nfree == ref["nfree"]
+    rp, cv, nz = op.A.export_csr(1)
+    cp, rv, zv = ref["csc"]
+    assert np.array_equal(rp, cp) and np.array_equal(cv, rv)
+    assert _rowscaled_err(rp - 1, nz, zv) <= TOL_VAL
+    assert np.abs(op.b - ref["b"]).max() <= TOL_VAL * np.abs(ref["b"]).max()
+    uh = gg.solve(gg.LinearFESolver(gg.CGSolver(rtol=1e-10)), op)
+    xo, _, _ = orc.pcg(cp, rv, zv, ref["b"], 1e-13)
+    assert np.linalg.norm(uh.free_values - xo) / np.linalg.norm(xo) < 1e-7
+
+
+def test_q2_tensor_core_cells_close_to_fp64(gg, orc):
+    """TF32 tensor-core Q2 cell matrices (tcgen05, FP32 accumulate, FP64 Jacobians) against
+    the FP64 path on distorted cells: |A_tf32 - A_fp64| <= 2e-3 * row max (TF32 keeps 10
+    mantissa bits; the scatter-add is FP64 in both)."""
+    rng = np.random.default_rng(71)
+    part = (7, 6, 5)
+    nn = 8 * 7 * 6
+    jit = rng.uniform(-0.2, 0.2, (nn, 3)) * (1.0 / np.array(part))
+    kappa = np.exp(rng.standard_normal(int(np.prod(part))))
+    model = gg.CartesianDiscreteModel((0, 1) * 3, part, node_jitter=jit)
+    V = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, float, 2), dirichlet_tags="boundary")
+    dO = gg.Measure(gg.Triangulation(model), 4)
+    kap = gg.CellField(kappa)
+    a = lambda u, v: gg.integrate(kap * gg.inner(gg.grad(v), gg.grad(u)), dO)  # noqa: E731
+    l = lambda v: gg.integrate(1.0 * v, dO)  # noqa: E731
+    op64 = gg.AffineFEOperator(a, l, V, V, gg.SparseMatrixAssembler(V, V, precision="fp64"))
+    op32 = gg.AffineFEOperator(a, l, V, V, gg.SparseMatrixAssembler(V, V, precision="fp32"))
+    rp, cv, z64 = op64.A.export_csr(0)
+    rp2, cv2, z32 = op32.A.export_csr(0)
+    assert np.array_equal(rp, rp2) and np.array_equal(cv, cv2)
+    err = _rowscaled_err(rp, z32, z64)
+    assert err <= 2e-3, err
+    assert np.abs(op32.b - op64.b).max() <= 1e-5 * np.abs(op64.b).max()
+    # and the FP64 path itself matches the oracle
+    ref = orc.poisson_q2((0, 1) * 3, part, ("boundary",), kappa=kappa, fconst=1.0, jitter=jit)
+    assert _rowscaled_err(rp, z64, ref["csc"][2]) <= TOL_VAL

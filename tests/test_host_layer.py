@@ -103,3 +103,27 @@ def test_weak_form_recognition(gg):
         cd.classify_bilinear(gg.inner(gg.grad(v), gg.grad(v)))
     with pytest.raises(NotImplementedError):
         cd.classify_linear(gg.grad(v))
+
+
+@pytest.mark.parametrize("part,tags", [((3, 3), ["tag_1", "tag_6"]), ((4, 5), ["boundary"]),
+                                       ((3, 2, 4), ["boundary"]), ((2, 3, 2), ["tag_25", 7]),
+                                       ((4, 4, 4), []), ((1, 2, 1), ["tag_21"])])
+def test_conforming_q2_matches_oracle(gg, orc, part, tags):
+    D = len(part)
+    m = gg.CartesianDiscreteModel((0, 1) * D, part)
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 2), dirichlet_tags=tags)
+    cd, nfree, ndiri = orc.conforming_q2(part, tags)
+    assert np.array_equal(V.cell_dof_ids, cd)
+    assert (V.nfree, V.ndiri) == (nfree, ndiri)
+
+
+def test_conforming_q2_vector_components(gg, orc):
+    """Vector Q2 (3 components) with a component mask: product vs oracle."""
+    part = (2, 3, 2)
+    masks = np.array([[1, 0, 1]], np.uint8)
+    m = gg.CartesianDiscreteModel((0, 1) * 3, part)
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, 3, 2), dirichlet_tags=["tag_25"],
+                   dirichlet_masks=masks)
+    cd, nfree, ndiri = orc.conforming_q2(part, ["tag_25"], ncomp=3, masks=masks)
+    assert np.array_equal(V.cell_dof_ids, cd)
+    assert (V.nfree, V.ndiri) == (nfree, ndiri)

@@ -166,3 +166,23 @@ def test_manufactured_nodal_solution(orc):
     b = orc.csc_mul(*ref["csc"], u)
     x, it, rr = orc.pcg(*ref["csc"], b, 1e-13)
     assert np.linalg.norm(x - u) / np.linalg.norm(u) < 1e-10
+
+
+def test_conforming_q2_matches_gridap_kat(orc, kats):
+    k = kats["conforming_q2_3x3"]
+    cd, nfree, ndiri = orc.conforming_q2(tuple(k["partition"]), k["dirichlet_tags"])
+    assert cd.tolist() == k["cell_dofs"]
+    assert (nfree, ndiri) == (k["nfree"], k["ndiri"])
+
+
+def test_q2_shapes_partition_of_unity_and_nodality(orc):
+    for D in (2, 3):
+        # nodes at the face centres of the n-cube, in local order
+        ext, anc = orc.ncube_faces(D)
+        nodes = np.where(ext == 1, 0.5, anc.astype(float))
+        phi, dphi = orc.q2_shapes(D, nodes)
+        assert np.allclose(phi, np.eye(3 ** D), atol=1e-15)
+        x, _ = orc.tensor_quadrature(D, 4)
+        phi, dphi = orc.q2_shapes(D, x)
+        assert np.allclose(phi.sum(axis=1), 1.0, atol=1e-14)
+        assert np.allclose(dphi.sum(axis=1), 0.0, atol=1e-13)

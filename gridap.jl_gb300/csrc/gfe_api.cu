@@ -70,6 +70,8 @@ extern "C" int gfe_ctx_destroy(gfe_ctx* c) {
   if (!c) return GFE_OK;
   DeviceGuard g(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
+  for (auto e : c->cg_events) cudaEventDestroy(e);
   for (auto& s : c->scratch) s.release();
   timer_release(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
@@ -143,7 +145,8 @@ extern "C" int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd,
   A->ctx = ctx;
   for (gfe::DevBuf* b : {&A->rowptr, &A->colval, &A->val, &A->cell_rows, &A->cell_cols,
                          &A->ref_ptr, &A->refs, &A->refpos, &A->sell_ptr, &A->sell_col,
-                         &A->sell_val64, &A->sell_val32, &A->dinv64, &A->dinv32})
+                         &A->sell_val64, &A->sell_val32, &A->dinv64, &A->dinv32,
+                         &A->dia_val32})
     b->owner = ctx;
   A->nrows = nrows;
   A->ncols = ncols;
@@ -168,10 +171,11 @@ extern "C" int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd,
   return GFE_OK;
 }
 
+// The matrix's buffers return to the context's pool in stream order (no synchronisation).
+// Destroy matrices before their context.
 extern "C" int gfe_matrix_destroy(gfe_matrix* A) {
   if (!A) return GFE_OK;
   DeviceGuard g(A->ctx->device);
-  cudaStreamSynchronize(A->ctx->stream);
   delete A;
   return GFE_OK;
 }

@@ -136,6 +136,14 @@ void timer_end(gfe_ctx* ctx) {
   cudaEventRecord(t.pool[t.used++], ctx->stream);
 }
 
+void timer_drop_last(gfe_ctx* ctx, int n) {
+  KernelTimer& t = ctx->timer;
+  while (n-- > 0 && t.used >= 2) {
+    t.used -= 2;
+    t.kinds.pop_back();
+  }
+}
+
 int timer_flush(gfe_ctx* ctx) {
   KernelTimer& t = ctx->timer;
   if (t.used == 0) return GFE_OK;

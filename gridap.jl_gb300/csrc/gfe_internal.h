@@ -89,6 +89,10 @@ struct gfe_ctx {
   // pinned staging for small device->host reads
   void* h_pinned = nullptr;
   gfe::KernelTimer timer;
+  // CUDA graph of one chunk of CG iterations, reused while its launch parameters match
+  cudaGraphExec_t cg_exec = nullptr;
+  uint64_t cg_key = 0;
+  std::vector<cudaEvent_t> cg_events;  // event pairs captured into the graph (timing on)
 };
 
 struct gfe_matrix {
@@ -191,6 +195,8 @@ int spmv64(gfe_ctx* ctx, gfe_matrix* A, const double* d_x, double* d_y);
 // flush folds finished pairs into the totals (call after a stream synchronisation).
 void timer_begin(gfe_ctx* ctx, int kind);
 void timer_end(gfe_ctx* ctx);
+// drops the last n (begin, end) pairs (launches that turned out to be no-ops)
+void timer_drop_last(gfe_ctx* ctx, int n);
 int timer_flush(gfe_ctx* ctx);
 void timer_release(gfe_ctx* ctx);
 

@@ -578,11 +578,11 @@ struct SolverWork {
   unsigned* tickets;   // device (inside S)
 };
 
-static int read_state(gfe_ctx* ctx, SolverWork& w) {
+static int read_state(gfe_ctx* ctx, SolverWork& w, bool flush = true) {
   GFE_CUDA_TRY(cudaMemcpyAsync(w.hS, w.S, sizeof(SolverState), cudaMemcpyDeviceToHost,
                                ctx->stream));
   GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  return timer_flush(ctx);
+  return flush ? timer_flush(ctx) : GFE_OK;
 }
 
 // Runs PCG on A (values of type T) for rhs*scale from x=0 until done; returns iterations.
@@ -593,20 +593,84 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
   const int64_t n = A->nrows;
   const unsigned gv = (unsigned)(ctx->num_sms * 4);
   const unsigned gs = grid_for(n, kSpmvBlock);
-  for (;;) {
+  // A chunk of iterations is captured once into a CUDA graph and replayed. With kernel timing
+  // on, CUDA event records around every SpMV are captured into the graph too; each replay
+  // re-records them, and after the chunk's synchronisation the pairs of the iterations that
+  // actually ran are folded into the totals.
+  const bool timing = ctx->timer.enabled;
+  const int kind = sizeof(T) == 4 ? GFE_KT_SPMV32 : GFE_KT_SPMV64;
+  uint64_t key = 1469598103934665603ull;  // FNV-1a over what the captured launches depend on
+  auto mix = [&key](const void* ptr, size_t nb) {
+    const unsigned char* c = static_cast<const unsigned char*>(ptr);
+    for (size_t i = 0; i < nb; ++i) key = (key ^ c[i]) * 1099511628211ull;
+  };
+  const void* ptrs[] = {x, r, p, q, dinv, w.partials, w.S};
+  mix(ptrs, sizeof(ptrs));
+  mix(&op, sizeof(Op));
+  mix(&n, sizeof(n));
+  mix(&check_every, sizeof(check_every));
+  const int flags[2] = {(int)sizeof(T), timing ? 1 : 0};
+  mix(flags, sizeof(flags));
+  cudaGraphExec_t exec = (ctx->cg_exec && ctx->cg_key == key) ? ctx->cg_exec : nullptr;
+  if (!exec) {
+    if (ctx->cg_exec) {
+      cudaGraphExecDestroy(ctx->cg_exec);
+      ctx->cg_exec = nullptr;
+    }
+    if (timing)
+      while ((int)ctx->cg_events.size() < 2 * check_every) {
+        cudaEvent_t e;
+        GFE_CUDA_TRY(cudaEventCreate(&e));
+        ctx->cg_events.push_back(e);
+      }
+    cudaGraph_t graph = nullptr;
+    GFE_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < check_every; ++k) {
-      timer_begin(ctx, sizeof(T) == 4 ? GFE_KT_SPMV32 : GFE_KT_SPMV64);
+      if (timing) cudaEventRecord(ctx->cg_events[2 * k], ctx->stream);
       k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
-      timer_end(ctx);
+      if (timing) cudaEventRecord(ctx->cg_events[2 * k + 1], ctx->stream);
       k_cg_update<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
       k_cg_direction<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
-      ctx->launches += 3;
     }
-    GFE_CUDA_TRY(cudaGetLastError());
-    GFE_TRY(read_state(ctx, w));
+    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+    if (ce != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return set_error(GFE_ERR_CUDA, "solve: graph capture failed: %s", cudaGetErrorString(ce));
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess)
+      return set_error(GFE_ERR_CUDA, "solve: graph instantiate failed: %s",
+                       cudaGetErrorString(ie));
+    ctx->cg_exec = exec;
+    ctx->cg_key = key;
+  }
+  int st = GFE_OK;
+  for (;;) {
+    const int iter0 = w.hS->iter;
+    const cudaError_t le = cudaGraphLaunch(exec, ctx->stream);
+    if (le != cudaSuccess) {
+      st = set_error(GFE_ERR_CUDA, "solve: graph launch: %s", cudaGetErrorString(le));
+      break;
+    }
+    ctx->launches += 3 * check_every;
+    st = read_state(ctx, w);
+    if (st != GFE_OK) break;
+    if (timing) {
+      // iterations after convergence returned at once: keep them out of the timing
+      const int executed = w.hS->iter - iter0;
+      for (int k = 0; k < executed && k < check_every; ++k) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ctx->cg_events[2 * k], ctx->cg_events[2 * k + 1]) ==
+            cudaSuccess) {
+          ctx->timer.total_ms[kind] += ms;
+          ctx->timer.count[kind] += 1;
+        }
+      }
+    }
     if (w.hS->done) break;
   }
-  return GFE_OK;
+  return st;
 }
 
 template <typename T>
@@ -626,6 +690,7 @@ static int run_pcg(gfe_ctx* ctx, gfe_matrix* A, const T* sval, const T* dinv, co
     k_cg_init<T, float><<<gv, kVecBlock, 0, ctx->stream>>>(n, (const float*)rhs, scale, x, r, p,
                                                           dinv, w.partials, w.S, rtol * rtol);
   ctx->launches++;
+  w.hS->iter = 0;
   SellOp<T> op{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval};
   GFE_TRY((iterate<T, SellOp<T>>(ctx, A, op, dinv, x, r, p, q, check_every, w)));
   const int done_iters = w.hS->iter;
@@ -707,6 +772,7 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
         n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
     k_set_reliable<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta);
     ctx->launches += 2;
+    w.hS->iter = 0;
     int updates = 0;
     GFE_TRY(build_dia(ctx, A));
     for (;;) {

@@ -115,6 +115,8 @@ int gfe_cartesian_conforming_dofs(int dim, int order, const int64_t* partition, 
 int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd, const int32_t* cell_rows,
                              const int32_t* cell_cols, int64_t nrows, int64_t ncols,
                              gfe_matrix** A);
+/* Releases the matrix (stream-ordered; no device synchronisation). Destroy every matrix of a
+ * context before the context itself. */
 int gfe_matrix_destroy(gfe_matrix* A);
 int gfe_matrix_info(gfe_matrix* A, int64_t* nrows, int64_t* ncols, int64_t* nnz);
 /* Copies the CSR arrays out (rowptr[nrows+1], colval[nnz], nzval[nnz]); index_base 0 or 1;

@@ -26,13 +26,15 @@ GFE_ERR_NONFINITE = 8
 
 GFE_REFFE_Q1, GFE_REFFE_Q2 = 1, 2
 GFE_GEOM_CARTESIAN, GFE_GEOM_NODAL = 0, 1
-GFE_FORM_DIFFUSION = 1
+GFE_FORM_DIFFUSION, GFE_FORM_ELASTICITY = 1, 2
+GFE_REFFE_Q1, GFE_REFFE_Q2, GFE_REFFE_P2_TET = 1, 2, 3
 GFE_COEF_ONE, GFE_COEF_CONST, GFE_COEF_CELL = 0, 1, 2
 GFE_SRC_NONE, GFE_SRC_CONST, GFE_SRC_NODAL, GFE_SRC_QPOINT, GFE_SRC_SINSUM = 0, 1, 2, 3, 4
 GFE_PREC_FP64, GFE_PREC_FP32 = 0, 1
 GFE_SOLVER_CG, GFE_SOLVER_IR_CG, GFE_SOLVER_MIXED_CG = 0, 1, 2
 GFE_PC_NONE, GFE_PC_JACOBI = 0, 1
 GFE_KT_SPMV64, GFE_KT_SPMV32, GFE_KT_ASSEMBLE, GFE_KT_RESIDUAL64, GFE_KT_ELEMENT = 0, 1, 2, 3, 4
+GFE_KT_PRECOND = 5
 
 
 class GfeError(RuntimeError):
@@ -64,7 +66,7 @@ class SolverOpts(C.Structure):
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("converged", C.c_int32),
                 ("status", C.c_int32), ("relres", C.c_double), ("operator_format", C.c_int32),
-                ("ndiag", C.c_int32)]
+                ("ndiag", C.c_int32), ("fallback", C.c_int32)]
 
 
 _P = C.c_void_p
@@ -97,6 +99,24 @@ SIGNATURES = {
     "gfe_assemble_matrix_and_vector": (C.c_int, [_P, C.POINTER(Problem), _P, _P]),
     "gfe_solve": (C.c_int, [_P, _P, C.POINTER(SolverOpts), _P, _P, C.POINTER(SolveReport)]),
     "gfe_matrix_mul": (C.c_int, [_P, _P, _P, _P]),
+    "gfe_learned_pc_create": (C.c_int, [_P, _P, _P, _P, C.c_int64, _P, C.POINTER(C.c_void_p)]),
+    "gfe_learned_pc_destroy": (C.c_int, [_P]),
+    "gfe_learned_pc_num_params": (C.c_int, []),
+    "gfe_learned_pc_set_weights": (C.c_int, [_P, _P]),
+    "gfe_learned_pc_get_weights": (C.c_int, [_P, _P]),
+    "gfe_learned_pc_apply": (C.c_int, [_P, _P, _P]),
+    "gfe_learned_pc_samples": (C.c_int, [_P, _P, _P, C.c_int64, _P, _P, _P]),
+    "gfe_learned_pc_train": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, C.c_int32, C.c_float,
+                                       C.c_uint64, C.POINTER(C.c_float)]),
+    "gfe_solve_fcg": (C.c_int, [_P, _P, _P, C.POINTER(SolverOpts), _P, _P,
+                                C.POINTER(SolveReport)]),
+    "gfe_simplex_model": (C.c_int, [_P, _P]),
+    "gfe_simplex_p2_dofs": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P, _P]),
+    "gfe_batch_create": (C.c_int, [_P, C.c_int32, _P, _P, C.POINTER(C.c_void_p)]),
+    "gfe_batch_destroy": (C.c_int, [_P]),
+    "gfe_batch_info": (C.c_int, [_P, _I64P, _I64P, _I64P]),
+    "gfe_batch_assemble_solve": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32, _P, _P,
+                                           C.POINTER(C.c_int32)]),
     "gfe_cg_solve_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, _P, _P, C.c_double,
                                        C.c_int32, _P, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_double)]),

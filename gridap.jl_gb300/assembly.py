@@ -16,7 +16,7 @@ import numpy as np
 from . import _lib
 from .celldata import CellField, NodalField, SinSum, classify_bilinear, classify_linear
 from .fespaces import FESpace, TrialFESpace, _space
-from .geometry import Measure
+from .geometry import Measure, SimplexDiscreteModel
 
 _CTX = {}
 
@@ -250,11 +250,74 @@ def _source_to_problem(prep: _Prepared, f, model, measure):
         raise NotImplementedError(f"source of type {type(f)}")
 
 
+def _lame_to_problem(prep: _Prepared, lame, ncells):
+    """(λ, μ), each a number or a per-cell CellField -> interleaved (λ, μ) array."""
+    p = prep.p
+    if lame is None:
+        p.coef_kind = _lib.GFE_COEF_ONE
+        return
+    lam, mu = lame
+    if all(isinstance(c, (int, float)) for c in (lam, mu)):
+        arr = np.array([float(lam), float(mu)])
+        p.coef_kind = _lib.GFE_COEF_CONST
+    else:
+        cols = []
+        for c in (lam, mu):
+            vals = c.values if isinstance(c, CellField) else c
+            if isinstance(vals, (int, float)):
+                vals = np.full(ncells, float(vals))
+            vals = np.asarray(vals.cpu() if hasattr(vals, "cpu") else vals, np.float64)
+            if vals.shape != (ncells,):
+                raise ValueError("per-cell Lamé coefficient has the wrong length")
+            cols.append(vals)
+        arr = np.ascontiguousarray(np.stack(cols, axis=1).reshape(-1))
+        p.coef_kind = _lib.GFE_COEF_CELL
+    prep.keep.append(arr)
+    p.coef = _lib.ptr(arr)
+
+
+def _prepare_elasticity(V, measure, lame, force, precision, cell_dof_ids, geometry):
+    model = V.model
+    prep = _Prepared()
+    p = prep.p
+    p.dim, p.ncomp, p.degree = 3, V.reffe.ncomp, measure.degree
+    p.reffe = _lib.GFE_REFFE_P2_TET
+    p.ncells = model.num_cells()
+    p.nd = V.ndofs_per_cell()
+    ids = V.cell_dof_ids if cell_dof_ids is None else cell_dof_ids
+    prep.keep.append(ids)
+    p.cell_dof_ids = _lib.ptr(ids)
+    p.nfree = V.num_free_dofs()
+    for d in range(3):
+        p.partition[d] = model.partition[d]
+        p.domain[2 * d] = model.domain[2 * d]
+        p.domain[2 * d + 1] = model.domain[2 * d + 1]
+    p.nnodes = model.num_nodes()
+    prep.keep += [model.node_coords, model.cell_node_ids]
+    p.node_coords = _lib.ptr(model.node_coords)
+    p.cell_node_ids = _lib.ptr(model.cell_node_ids)
+    p.geometry = _lib.GFE_GEOM_NODAL if geometry == "nodal" else _lib.GFE_GEOM_CARTESIAN
+    p.form = _lib.GFE_FORM_ELASTICITY
+    _lame_to_problem(prep, lame, p.ncells)
+    if force is None:
+        p.source_kind = _lib.GFE_SRC_NONE
+    else:
+        fv = np.ascontiguousarray(force, np.float64).reshape(3)
+        prep.keep.append(fv)
+        p.source_kind, p.source, p.source_len = _lib.GFE_SRC_CONST, _lib.ptr(fv), 3
+    p.precision = _lib.GFE_PREC_FP32 if precision == "fp32" else _lib.GFE_PREC_FP64
+    return prep
+
+
 def prepare_problem(U, V, measure: Measure, coef=None, source=None, precision="fp64",
-                    cell_dof_ids=None) -> _Prepared:
-    """The gfe_problem for ∫ coef ∇v⋅∇u dΩ and ∫ source v dΩ on V (U == V for square)."""
+                    cell_dof_ids=None, geometry=None) -> _Prepared:
+    """The gfe_problem for ∫ coef ∇v⋅∇u dΩ and ∫ source v dΩ on V (U == V for square); on a
+    simplexified model, for ∫ ε(v) ⊙ σ(ε(u)) dΩ with coef = (λ, μ) and ∫ f⋅v dΩ with
+    source = f. geometry="nodal" forces the general (node-coordinate) element path."""
     V = _space(V)
     model = V.model
+    if isinstance(model, SimplexDiscreteModel):
+        return _prepare_elasticity(V, measure, coef, source, precision, cell_dof_ids, geometry)
     prep = _Prepared()
     p = prep.p
     D = model.dim

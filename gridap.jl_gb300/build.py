@@ -23,7 +23,7 @@ def _sources():
 
 def _compile(src: pathlib.Path) -> pathlib.Path:
     obj = OUT / (src.stem + ".o")
-    deps = [src] + list(CSRC.glob("*.h")) + [HERE.parent / "include" / "gfe.h"]
+    deps = [src] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "gfe.h"]
     if obj.exists() and all(obj.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return obj
     cmd = [NVCC, *ARCH, *COMMON, "-c", str(src), "-o", str(obj)]

@@ -7,7 +7,10 @@ arbitrary Julia code to the GPU, so it recognises the integrands it provides and
 enum plus coefficient arrays across the C ABI:
 
   - bilinear  `κ * inner(grad(v), grad(u))`  (κ: number, per-cell CellField, or absent);
-  - linear    `f * v`  (f: number, NodalField, SinSum, or a Python callable of x).
+  - linear    `f * v`  (f: number, NodalField, SinSum, or a Python callable of x);
+  - bilinear  `inner(ε(v), σ(ε(u)))` with σ = isotropic_stress(λ, μ), i.e.
+              ε(v) ⊙ (λ tr(ε(u)) I + 2μ ε(u))  (λ, μ: numbers or per-cell CellFields);
+  - linear    `inner(f, v)` with f a constant 3-vector (body force).
 
 Anything else raises NotImplementedError; in Gridap that integrand would stay on Gridap's
 own CPU path.
@@ -82,6 +85,31 @@ class _Scaled(_Expr):
         self.expr = expr
 
 
+class _Eps(_Expr):
+    def __init__(self, arg):
+        self.arg = arg
+
+
+class _Stress(_Expr):
+    def __init__(self, lam, mu, eps):
+        self.lam = lam
+        self.mu = mu
+        self.eps = eps
+
+
+def symmetric_gradient(a):
+    """ε(a) = (∇a + ∇aᵀ)/2 (Fields/DiffOperators.jl:48)."""
+    return _Eps(a)
+
+
+ε = symmetric_gradient
+
+
+def isotropic_stress(lam, mu):
+    """σ(ε) = λ tr(ε) I + 2μ ε, as a function of ε."""
+    return lambda e: _Stress(lam, mu, e)
+
+
 def get_trial_fe_basis(U) -> _Basis:
     return _Basis(U, True)
 
@@ -125,9 +153,26 @@ def _strip_scale(e):
     return coef, e
 
 
+def _elasticity(e):
+    if not isinstance(e, _Inner):
+        return None
+    for x, s in ((e.a, e.b), (e.b, e.a)):
+        if isinstance(x, _Eps) and isinstance(s, _Stress) and isinstance(s.eps, _Eps) \
+                and isinstance(x.arg, _Basis) and isinstance(s.eps.arg, _Basis) \
+                and x.arg.trial != s.eps.arg.trial:
+            return s.lam, s.mu
+    return None
+
+
 def classify_bilinear(expr):
-    """Returns ("diffusion", coef) for κ ∇v⋅∇u forms."""
+    """Returns ("diffusion", coef) for κ ∇v⋅∇u forms and ("elasticity", (λ, μ)) for
+    ε(v) ⊙ σ(ε(u)) forms."""
     coef, e = _strip_scale(expr)
+    lm = _elasticity(e)
+    if lm is not None:
+        if coef is not None:
+            raise NotImplementedError("scale λ and μ instead of the elasticity form")
+        return "elasticity", lm
     if isinstance(e, _Inner):
         ca, a = _strip_scale(e.a)
         cb, b = _strip_scale(e.b)
@@ -141,7 +186,15 @@ def classify_bilinear(expr):
 
 
 def classify_linear(expr):
-    """Returns ("source", f) for f*v forms."""
+    """Returns ("source", f) for f*v forms and ("body_force", f) for inner(f, v) with a
+    constant vector f."""
+    if isinstance(expr, _Inner):
+        for f, v in ((expr.a, expr.b), (expr.b, expr.a)):
+            if isinstance(v, _Basis) and not v.trial and not isinstance(f, _Expr):
+                fv = np.asarray(f, dtype=np.float64).reshape(-1)
+                if fv.size != 3:
+                    raise NotImplementedError("body forces are constant 3-vectors")
+                return "body_force", fv
     coef, e = _strip_scale(expr)
     if isinstance(e, _Basis) and not e.trial:
         return "source", (1.0 if coef is None else coef)

@@ -71,7 +71,6 @@ extern "C" int gfe_ctx_destroy(gfe_ctx* c) {
   DeviceGuard g(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
-  for (auto e : c->cg_events) cudaEventDestroy(e);
   for (auto& s : c->scratch) s.release();
   timer_release(c);
   if (c->stream) cudaStreamSynchronize(c->stream);

@@ -92,7 +92,6 @@ struct gfe_ctx {
   // CUDA graph of one chunk of CG iterations, reused while its launch parameters match
   cudaGraphExec_t cg_exec = nullptr;
   uint64_t cg_key = 0;
-  std::vector<cudaEvent_t> cg_events;  // event pairs captured into the graph (timing on)
 };
 
 struct gfe_matrix {
@@ -184,6 +183,13 @@ int launch_q2_cells_tf32(gfe_ctx* ctx, int64_t ncells, const int32_t* cell_verti
                          const double* coef, int src_kind, const double* src, float* K,
                          float* bvec);
 
+// learned block preconditioner (gfe_learned.cu); `skip` (device int, may be null) makes the
+// kernels return at once when non-zero
+int learned_apply(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, float* d_z,
+                  const int* skip = nullptr);
+int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_opts* o,
+              const double* d_b, double* d_x, gfe_solve_report* rep);
+
 // solver (gfe_solve.cu)
 int build_solver_plan(gfe_ctx* ctx, gfe_matrix* A);
 int build_dia(gfe_ctx* ctx, gfe_matrix* A);
@@ -204,5 +210,14 @@ void timer_release(gfe_ctx* ctx);
 int tensor_quadrature(int D, int degree, std::vector<double>& x, std::vector<double>& w);
 void q2_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
                std::vector<double>& dphi);
+// simplexified boxes and P2 tets (gfe_simplex.cpp)
+extern const int kHexTets[6][4];
+extern const int kTetEdges[6][2];
+int tet_quadrature(int degree, std::vector<double>& x, std::vector<double>& w);
+void p2tet_shapes(int nq, const double* qx, double* phi, double* dphi);
+int elasticity_p2_tables(const double* h, int degree, std::vector<double>& tab);
+int p2tet_reference_integrals(int degree, std::vector<double>& G, std::vector<double>& m);
+// P2 tet elasticity assembly (gfe_elasticity.cu)
+int assemble_p2_elasticity(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* d_b);
 
 }  // namespace gfe

@@ -1,0 +1,226 @@
+// gfe_rows.cuh -- the row-gather assembly kernel shared by the element families.
+//
+// Every matrix row is owned by one thread, which walks the row's cell references (sorted by
+// cell) and accumulates each contribution at its precomputed position in the row, so each
+// stored value receives Gridap's additions in Gridap's order (ascending cells), with no
+// atomics and no colouring. A block of R rows then writes its contiguous CSR slice with
+// coalesced stores. Cell values come from a source functor with
+//   load_tables(smem), m(tables, cell, li, lj, nd), v(tables, cell, li)  and  ntab.
+#pragma once
+#include "gfe_internal.h"
+
+namespace gfe {
+namespace {
+__device__ __forceinline__ void raise_err(DevError* err, int code, long long index) {
+  if (atomicCAS(&err->code, 0, code) == 0) err->index = index;
+}
+
+struct RowArgs {
+  int64_t nrows;
+  int nd;
+  const int32_t* rowptr;
+  const int32_t* colval;
+  const int64_t* ref_ptr;
+  const int32_t* refs;
+  const int32_t* cell_cols;  // column ids per cell (Gridap convention)
+  const void* refpos;        // per (reference, local column) position in the row
+  double* val;               // may be null (vector only)
+  double* b;                 // may be null (matrix only)
+  DevError* err;
+};
+
+// ---- cell value sources -------------------------------------------------------------------
+// FP32 stored cell arrays (the tensor-core element kernels' output), accumulated in FP64.
+struct StoredCellsF32 {
+  const float* mat;
+  const float* vec;
+  int64_t cs, es, vcs, ves;
+  int ntab;
+  __device__ void load_tables(double*) const {}
+  __device__ __forceinline__ double m(const double*, int64_t cell, int li, int lj, int nd) const {
+    return (double)__ldg(mat + cell * cs + (int64_t)(li + lj * nd) * es);
+  }
+  __device__ __forceinline__ double v(const double*, int64_t cell, int li) const {
+    return (double)__ldg(vec + cell * vcs + (int64_t)li * ves);
+  }
+};
+
+// Stored cell arrays. Entry (cell, li, lj) at mat[cell*cs + (li + lj*nd)*es].
+struct StoredCells {
+  const double* mat;
+  const double* vec;
+  int64_t cs, es;    // cell stride, entry stride of mat
+  int64_t vcs, ves;  // same for vec
+  int ntab;          // no tables
+  __device__ void load_tables(double*) const {}
+  __device__ __forceinline__ double m(const double*, int64_t cell, int li, int lj, int nd) const {
+    return __ldg(mat + cell * cs + (int64_t)(li + lj * nd) * es);
+  }
+  __device__ __forceinline__ double v(const double*, int64_t cell, int li) const {
+    return __ldg(vec + cell * vcs + (int64_t)li * ves);
+  }
+};
+
+
+// ---- the row-gather kernel ----------------------------------------------------------------
+template <int MAXW, int R, class Src, typename PosT>
+__global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
+  extern __shared__ double smem[];
+  double* acc = smem;                 // acc[k*R + t]
+  double* tab = smem + MAXW * R;      // source tables
+  __shared__ int32_t lrp[R + 1];      // block-relative row starts
+  const int t = threadIdx.x;
+  const int64_t r0 = (int64_t)blockIdx.x * R;
+  const int64_t r = r0 + t;
+  src.load_tables(tab);
+
+  int32_t start = 0, n = 0;
+  if (r < a.nrows) {
+    start = a.rowptr[r];
+    n = a.rowptr[r + 1] - start;
+  }
+  const int64_t rend = (r0 + R < a.nrows) ? r0 + R : a.nrows;
+  const int32_t bstart = a.rowptr[r0 < a.nrows ? r0 : a.nrows];
+  lrp[t] = (r < a.nrows ? start : a.rowptr[rend]) - bstart;
+  if (t == 0) lrp[R] = a.rowptr[rend] - bstart;
+  if (a.val)
+    for (int k = 0; k < n; ++k) acc[k * R + t] = 0.0;
+  __syncthreads();
+
+  double bacc = 0.0;
+  if (r < a.nrows) {
+    const PosT* refpos = static_cast<const PosT*>(a.refpos);
+    for (int64_t q = a.ref_ptr[r]; q < a.ref_ptr[r + 1]; ++q) {
+      const int32_t e = a.refs[q];
+      const int64_t cell = e / a.nd;
+      const int li = e - (int)(cell * a.nd);
+      if (a.val) {
+        const PosT* pp = refpos + q * a.nd;
+        for (int lj = 0; lj < a.nd; ++lj) {
+          const PosT p = __ldg(pp + lj);
+          if (p == (PosT)~(PosT)0) continue;  // Dirichlet column
+          if (p >= n) {
+            raise_err(a.err, GFE_ERR_INVALID_ARGUMENT, r);
+            continue;
+          }
+          acc[p * R + t] += src.m(tab, cell, li, lj, a.nd);
+        }
+      }
+      if (a.b) bacc += src.v(tab, cell, li);
+    }
+    if (a.b) a.b[r] = bacc;
+  }
+  if (!a.val) return;
+  __syncthreads();
+  // coalesced write-out of the block's CSR slice
+  const int32_t total = lrp[R];
+  double* out = a.val + bstart;
+  for (int32_t l = t; l < total; l += R) {
+    int lo = 0, hi = R;  // largest row t' with lrp[t'] <= l
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (lrp[mid] <= l) lo = mid; else hi = mid;
+    }
+    out[l] = acc[(l - lrp[lo]) * R + lo];
+  }
+}
+
+template <int MAXW, int R, class Src>
+static int launch_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src, int pos_bytes) {
+  const size_t smem = sizeof(double) * ((size_t)MAXW * R + (size_t)src.ntab);
+  auto kern = pos_bytes == 1 ? k_assemble_rows<MAXW, R, Src, uint8_t>
+                             : k_assemble_rows<MAXW, R, Src, uint16_t>;
+  if (smem > 48 * 1024)
+    GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  timer_begin(ctx, GFE_KT_ASSEMBLE);
+  kern<<<grid_for(a.nrows, R), R, smem, ctx->stream>>>(a, src);
+  timer_end(ctx);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+// Maximum row width of a matrix (device reduction over rowptr differences).
+__global__ void k_max_width(const int32_t* __restrict__ rowptr, int64_t n, int32_t* out) {
+  int32_t m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t w = rowptr[i + 1] - rowptr[i];
+    m = w > m ? w : m;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const int32_t o = __shfl_down_sync(0xffffffffu, m, off);
+    m = o > m ? o : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+static int max_row_width(gfe_ctx* ctx, gfe_matrix* A, int* out) {
+  GFE_TRY(ctx->scratch[SCR_REDUCE].reserve(256));
+  int32_t* d = ctx->scratch[SCR_REDUCE].as<int32_t>();
+  GFE_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(int32_t), ctx->stream));
+  k_max_width<<<grid_for(A->nrows, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+      A->rowptr.as<int32_t>(), A->nrows, d);
+  ctx->launches++;
+  int32_t h = 0;
+  GFE_TRY(copy_out(ctx, &h, d, sizeof(int32_t)));
+  *out = h;
+  return GFE_OK;
+}
+
+template <class Src>
+static int run_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src, int maxw, int pb) {
+  if (maxw <= 16) return launch_rows<16, 128>(ctx, a, src, pb);
+  if (maxw <= 32) return launch_rows<32, 128>(ctx, a, src, pb);
+  if (maxw <= 64) return launch_rows<64, 128>(ctx, a, src, pb);
+  if (maxw <= 128) return launch_rows<128, 64>(ctx, a, src, pb);
+  if (maxw <= 256) return launch_rows<256, 32>(ctx, a, src, pb);
+  if (maxw <= 512) return launch_rows<512, 16>(ctx, a, src, pb);
+  return set_error(GFE_ERR_ROW_TOO_WIDE, "assembly: row width %d exceeds 512", maxw);
+}
+
+static RowArgs row_args(gfe_ctx* ctx, gfe_matrix* A, double* b, bool with_matrix) {
+  RowArgs a;
+  a.nrows = A->nrows;
+  a.nd = A->nd;
+  a.rowptr = A->rowptr.as<int32_t>();
+  a.colval = A->colval.as<int32_t>();
+  a.ref_ptr = A->ref_ptr.as<int64_t>();
+  a.refs = A->refs.as<int32_t>();
+  a.cell_cols = A->cell_cols.as<int32_t>();
+  a.refpos = A->refpos.ptr;
+  a.val = with_matrix ? A->val.as<double>() : nullptr;
+  a.b = b;
+  a.err = ctx->d_err;
+  return a;
+}
+
+// Vector-only gather: b[r] (+)= the row's cell contributions in cell order.
+template <class Src, bool ADD>
+__global__ void k_vector_rows(RowArgs a, Src src) {
+  extern __shared__ double tab[];
+  src.load_tables(tab);
+  __syncthreads();
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.nrows) return;
+  double acc = 0.0;
+  for (int64_t q = a.ref_ptr[r]; q < a.ref_ptr[r + 1]; ++q) {
+    const int32_t e = a.refs[q];
+    const int64_t cell = e / a.nd;
+    acc += src.v(tab, cell, e - (int)(cell * a.nd));
+  }
+  if (ADD) a.b[r] += acc; else a.b[r] = acc;
+}
+
+template <class Src, bool ADD = false>
+static int vector_only_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src) {
+  k_vector_rows<Src, ADD><<<grid_for(a.nrows, 256), 256, sizeof(double) * src.ntab,
+                            ctx->stream>>>(a, src);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+}  // namespace
+}  // namespace gfe

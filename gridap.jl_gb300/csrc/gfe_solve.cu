@@ -570,6 +570,133 @@ __global__ void k_set_reliable(SolverState* S, double delta2) {
   S->rr64 = S->bb;
 }
 
+// ---- flexible CG (FCG(1)) with a variable preconditioner --------------------------------------
+//   x += a p; r -= a q; z = M(r); beta = -(z.q)/(p.q); p = z + beta p; q = A p; a = (p.r)/(p.q)
+// (Notay's truncated flexible CG with one previous direction). FP32 vectors; x and the true
+// residual in FP64 through reliable updates, as the mixed CG.
+__global__ void __launch_bounds__(kVecBlock)
+    k_fcg_update(int64_t n, float* __restrict__ x, float* __restrict__ r,
+                 const float* __restrict__ p, const float* __restrict__ q,
+                 double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kVecBlock / 32];
+  if (S->done) return;
+  const float a = (float)S->alpha;
+  float rr_t = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = fmaf(a, p[i], x[i]);
+    const float ri = fmaf(-a, q[i], r[i]);
+    r[i] = ri;
+    rr_t = fmaf(ri, ri, rr_t);
+  }
+  const double rr = block_sum<kVecBlock>((double)rr_t, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = rr;
+  double tot[1];
+  if (last_block_reduce<kVecBlock, 1>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->iter += 1;
+    S->rr = tot[0];
+    if (!isfinite(tot[0])) {
+      S->done = 1;
+    } else if (tot[0] <= S->tol2) {
+      S->done = 1;
+      S->converged = 1;
+    } else if (S->iter >= S->maxit) {
+      S->done = 1;
+    } else if (S->delta2 > 0.0 && tot[0] < S->delta2 * S->rmax2) {
+      S->done = 1;
+      S->need_update = 1;
+    }
+  }
+}
+
+__global__ void k_jacobi_apply(int64_t n, const float* __restrict__ r,
+                               const float* __restrict__ dinv, float* __restrict__ z,
+                               const SolverState* S) {
+  if (S && S->done) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = dinv[i] * r[i];
+}
+
+// beta = -(z.q) / (p.q)
+__global__ void __launch_bounds__(kVecBlock)
+    k_fcg_beta(int64_t n, const float* __restrict__ z, const float* __restrict__ q,
+               double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kVecBlock / 32];
+  if (S->done) return;
+  float t = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    t = fmaf(z[i], q[i], t);
+  const double d = block_sum<kVecBlock>((double)t, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = d;
+  double tot[1];
+  if (last_block_reduce<kVecBlock, 1>(&S->ticket[3], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0)
+    S->beta = S->pq != 0.0 ? -tot[0] / S->pq : 0.0;
+}
+
+__global__ void k_fcg_dir(int64_t n, float* __restrict__ p, const float* __restrict__ z,
+                          const SolverState* S) {
+  if (S->done) return;
+  const float beta = (float)S->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = fmaf(beta, p[i], z[i]);
+}
+
+// q = A p, partials of p.q and p.r; alpha = (p.r)/(p.q)
+template <class Op>
+__global__ void __launch_bounds__(kSpmvBlock)
+    k_fcg_spmv(int64_t n, Op op, const float* __restrict__ p, float* __restrict__ q,
+               const float* __restrict__ r, double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kSpmvBlock / 32];
+  if (S->done) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float pq = 0.f, pr = 0.f;
+  if (i < n) {
+    const float y = op.row(i, p);
+    q[i] = y;
+    pq = p[i] * y;
+    pr = p[i] * r[i];
+  }
+  const double dpq = block_sum<kSpmvBlock>((double)pq, sh);
+  const double dpr = block_sum<kSpmvBlock>((double)pr, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = dpq;
+    partials[2 * blockIdx.x + 1] = dpr;
+  }
+  double tot[2];
+  if (last_block_reduce<kSpmvBlock, 2>(&S->ticket[0], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->pq = tot[0];
+    S->alpha = tot[0] != 0.0 ? tot[1] / tot[0] : 0.0;
+  }
+}
+
+// r32 = (float) r64 after a reliable update (no orthogonalisation needed: FCG takes alpha from
+// p.r and beta from z.q with the current vectors); stop when the FP64 residual meets rtol.
+__global__ void k_fcg_restart(int64_t n, const double* __restrict__ r64, float* __restrict__ r32,
+                              SolverState* S) {
+  const bool conv = S->rr64 <= S->tol2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n && !conv;
+       i += (int64_t)gridDim.x * blockDim.x)
+    r32[i] = (float)r64[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    S->need_update = 0;
+    if (conv) {
+      S->converged = 1;
+      S->done = 1;
+    } else {
+      S->rmax2 = S->rr64;
+      S->rr = S->rr64;
+      S->converged = 0;
+      S->done = S->iter >= S->maxit ? 1 : 0;
+    }
+  }
+}
+
 // ---- host drivers -------------------------------------------------------------------------
 struct SolverWork {
   SolverState* S;      // device
@@ -593,82 +720,84 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
   const int64_t n = A->nrows;
   const unsigned gv = (unsigned)(ctx->num_sms * 4);
   const unsigned gs = grid_for(n, kSpmvBlock);
-  // A chunk of iterations is captured once into a CUDA graph and replayed. With kernel timing
-  // on, CUDA event records around every SpMV are captured into the graph too; each replay
-  // re-records them, and after the chunk's synchronisation the pairs of the iterations that
-  // actually ran are folded into the totals.
+  // Without kernel timing a chunk of iterations is captured once into a CUDA graph (cached in
+  // the context while its launch parameters match) and replayed. With timing on, every
+  // iteration is launched directly with CUDA events around the SpMV; launches after the
+  // converged iteration (they return at once) are dropped from the timing.
   const bool timing = ctx->timer.enabled;
   const int kind = sizeof(T) == 4 ? GFE_KT_SPMV32 : GFE_KT_SPMV64;
-  uint64_t key = 1469598103934665603ull;  // FNV-1a over what the captured launches depend on
-  auto mix = [&key](const void* ptr, size_t nb) {
-    const unsigned char* c = static_cast<const unsigned char*>(ptr);
-    for (size_t i = 0; i < nb; ++i) key = (key ^ c[i]) * 1099511628211ull;
-  };
-  const void* ptrs[] = {x, r, p, q, dinv, w.partials, w.S};
-  mix(ptrs, sizeof(ptrs));
-  mix(&op, sizeof(Op));
-  mix(&n, sizeof(n));
-  mix(&check_every, sizeof(check_every));
-  const int flags[2] = {(int)sizeof(T), timing ? 1 : 0};
-  mix(flags, sizeof(flags));
-  cudaGraphExec_t exec = (ctx->cg_exec && ctx->cg_key == key) ? ctx->cg_exec : nullptr;
-  if (!exec) {
-    if (ctx->cg_exec) {
-      cudaGraphExecDestroy(ctx->cg_exec);
-      ctx->cg_exec = nullptr;
-    }
-    if (timing)
-      while ((int)ctx->cg_events.size() < 2 * check_every) {
-        cudaEvent_t e;
-        GFE_CUDA_TRY(cudaEventCreate(&e));
-        ctx->cg_events.push_back(e);
+  cudaGraphExec_t exec = nullptr;
+  if (!timing) {
+    uint64_t key = 1469598103934665603ull;  // FNV-1a over what the launches depend on
+    auto mix = [&key](const void* ptr, size_t nb) {
+      const unsigned char* c = static_cast<const unsigned char*>(ptr);
+      for (size_t i = 0; i < nb; ++i) key = (key ^ c[i]) * 1099511628211ull;
+    };
+    const void* ptrs[] = {x, r, p, q, dinv, w.partials, w.S};
+    mix(ptrs, sizeof(ptrs));
+    mix(&op, sizeof(Op));
+    mix(&n, sizeof(n));
+    mix(&check_every, sizeof(check_every));
+    const int tsize = (int)sizeof(T);
+    mix(&tsize, sizeof(tsize));
+    if (ctx->cg_exec && ctx->cg_key == key) exec = ctx->cg_exec;
+    if (!exec) {
+      if (ctx->cg_exec) {
+        cudaGraphExecDestroy(ctx->cg_exec);
+        ctx->cg_exec = nullptr;
       }
-    cudaGraph_t graph = nullptr;
-    GFE_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < check_every; ++k) {
-      if (timing) cudaEventRecord(ctx->cg_events[2 * k], ctx->stream);
-      k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
-      if (timing) cudaEventRecord(ctx->cg_events[2 * k + 1], ctx->stream);
-      k_cg_update<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
-      k_cg_direction<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
+      cudaGraph_t graph = nullptr;
+      GFE_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < check_every; ++k) {
+        k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
+        k_cg_update<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
+        k_cg_direction<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
+      }
+      const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+      if (ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return set_error(GFE_ERR_CUDA, "solve: graph capture failed: %s",
+                         cudaGetErrorString(ce));
+      }
+      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ie != cudaSuccess)
+        return set_error(GFE_ERR_CUDA, "solve: graph instantiate failed: %s",
+                         cudaGetErrorString(ie));
+      ctx->cg_exec = exec;
+      ctx->cg_key = key;
     }
-    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
-    if (ce != cudaSuccess) {
-      if (graph) cudaGraphDestroy(graph);
-      return set_error(GFE_ERR_CUDA, "solve: graph capture failed: %s", cudaGetErrorString(ce));
-    }
-    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ie != cudaSuccess)
-      return set_error(GFE_ERR_CUDA, "solve: graph instantiate failed: %s",
-                       cudaGetErrorString(ie));
-    ctx->cg_exec = exec;
-    ctx->cg_key = key;
   }
   int st = GFE_OK;
   for (;;) {
     const int iter0 = w.hS->iter;
-    const cudaError_t le = cudaGraphLaunch(exec, ctx->stream);
-    if (le != cudaSuccess) {
-      st = set_error(GFE_ERR_CUDA, "solve: graph launch: %s", cudaGetErrorString(le));
-      break;
-    }
-    ctx->launches += 3 * check_every;
-    st = read_state(ctx, w);
-    if (st != GFE_OK) break;
-    if (timing) {
-      // iterations after convergence returned at once: keep them out of the timing
-      const int executed = w.hS->iter - iter0;
-      for (int k = 0; k < executed && k < check_every; ++k) {
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, ctx->cg_events[2 * k], ctx->cg_events[2 * k + 1]) ==
-            cudaSuccess) {
-          ctx->timer.total_ms[kind] += ms;
-          ctx->timer.count[kind] += 1;
-        }
+    if (exec) {
+      const cudaError_t le = cudaGraphLaunch(exec, ctx->stream);
+      if (le != cudaSuccess) {
+        st = set_error(GFE_ERR_CUDA, "solve: graph launch: %s", cudaGetErrorString(le));
+        break;
+      }
+      ctx->launches += 3 * check_every;
+    } else {
+      for (int k = 0; k < check_every; ++k) {
+        timer_begin(ctx, kind);
+        k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
+        timer_end(ctx);
+        k_cg_update<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
+        k_cg_direction<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
+        ctx->launches += 3;
+      }
+      const cudaError_t le = cudaGetLastError();
+      if (le != cudaSuccess) {
+        st = set_error(GFE_ERR_CUDA, "solve: launch: %s", cudaGetErrorString(le));
+        break;
       }
     }
-    if (w.hS->done) break;
+    st = read_state(ctx, w, false);
+    if (st != GFE_OK) break;
+    if (timing) timer_drop_last(ctx, check_every - (w.hS->iter - iter0));
+    st = timer_flush(ctx);
+    if (st != GFE_OK || w.hS->done) break;
   }
   return st;
 }
@@ -873,6 +1002,141 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
     rep->converged = std::isfinite(rep->relres) && rep->relres <= o->rtol * (1.0 + 1e-6);
     if (!std::isfinite(rep->relres)) rep->status = GFE_ERR_NONFINITE;
   }
+  return GFE_OK;
+}
+
+
+// Flexible CG with the learned block preconditioner (pc != nullptr) or Jacobi, FP32 vectors
+// with FP64 reliable updates. Falls back to Jacobi when the learned preconditioner stagnates
+// (the FP32 residual fails to halve over `check_every` iterations twice in a row).
+int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_opts* o,
+              const double* d_b, double* d_x, gfe_solve_report* rep) {
+  if (A->nrows != A->ncols) return set_error(GFE_ERR_INVALID_ARGUMENT, "fcg: not square");
+  GFE_TRY(build_solver_plan(ctx, A));
+  GFE_TRY(build_dia(ctx, A));
+  const int64_t n = A->nrows;
+  const int check_every = o->check_every > 0 ? o->check_every : 10;
+  const int maxit = o->maxiter > 0 ? o->maxiter : 100000;
+  const size_t n8 = sizeof(double) * (size_t)(n > 0 ? n : 1);
+  GFE_TRY(ctx->scratch[SCR_SOLVER].reserve(n8 * 3 + 64));
+  GFE_TRY(ctx->scratch[SCR_SOLVER2].reserve(sizeof(float) * (size_t)(n > 0 ? n : 1) * 5 + 64));
+  const size_t npart = (size_t)grid_for(n, kSpmvBlock) * 2 + (size_t)ctx->num_sms * 8 + 64;
+  GFE_TRY(ctx->scratch[SCR_REDUCE].reserve(sizeof(SolverState) + sizeof(double) * npart + 256));
+  SolverWork w;
+  w.S = ctx->scratch[SCR_REDUCE].as<SolverState>();
+  w.partials = (double*)((char*)ctx->scratch[SCR_REDUCE].ptr + 256);
+  w.hS = (SolverState*)ctx->h_pinned;
+  double* r64 = ctx->scratch[SCR_SOLVER].as<double>();
+  float* f = (float*)ctx->scratch[SCR_SOLVER2].ptr;
+  float *x32 = f, *r32 = f + n, *p32 = f + 2 * n, *q32 = f + 3 * n, *z32 = f + 4 * n;
+  const float* dinv32 = A->dinv32.as<float>();
+  const unsigned gv = (unsigned)(ctx->num_sms * 4), gs = grid_for(n, kSpmvBlock);
+  const double delta = o->inner_rtol > 0 ? o->inner_rtol : 0.1;
+  bool learned = pc != nullptr;
+  DiaOp<float> dop{A->dia_val32.as<float>(), n, {}};
+  for (int d = 0; d < A->dia_ndiag; ++d) dop.o.off[d] = A->dia_off[d];
+  dop.o.nd = A->dia_ndiag;
+  SellOp<float> sop{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(),
+                    A->sell_val32.as<float>()};
+  auto spmv = [&]() {
+    timer_begin(ctx, GFE_KT_SPMV32);
+    if (A->dia_valid)
+      k_fcg_spmv<DiaOp<float>><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, dop, p32, q32, r32,
+                                                                  w.partials, w.S);
+    else
+      k_fcg_spmv<SellOp<float>><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, sop, p32, q32, r32,
+                                                                   w.partials, w.S);
+    timer_end(ctx);
+    ctx->launches++;
+  };
+  auto precond = [&]() -> int {
+    if (learned) return learned_apply(ctx, pc, r32, z32, &w.S->done);
+    k_jacobi_apply<<<gv, kVecBlock, 0, ctx->stream>>>(n, r32, dinv32, z32, w.S);
+    ctx->launches++;
+    return GFE_OK;
+  };
+  // start: x = 0, r = b, z = M r, p = z, q = A p, alpha
+  GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
+  GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
+  int maxit_field = maxit;
+  GFE_CUDA_TRY(cudaMemcpyAsync(&w.S->maxit, &maxit_field, sizeof(int), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  k_cg_init<float, double><<<gv, kVecBlock, 0, ctx->stream>>>(
+      n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
+  k_set_reliable<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta);
+  ctx->launches += 2;
+  GFE_TRY(precond());
+  GFE_CUDA_TRY(cudaMemcpyAsync(p32, z32, sizeof(float) * n, cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+  spmv();
+  GFE_TRY(read_state(ctx, w));
+  int updates = 0, slow = 0, fallback = 0;
+  double rr_chunk = w.hS->rr;
+  while (!w.hS->done) {
+    for (int k = 0; k < check_every; ++k) {
+      k_fcg_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S);
+      ctx->launches++;
+      GFE_TRY(precond());
+      k_fcg_beta<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
+      k_fcg_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
+      ctx->launches += 2;
+      spmv();
+    }
+    GFE_CUDA_TRY(cudaGetLastError());
+    GFE_TRY(read_state(ctx, w));
+    if (w.hS->done && (w.hS->need_update || w.hS->converged)) {
+      // reliable update: x64 += x32, r64 = b - A64 x64, r32 = r64 (or stop)
+      k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
+      timer_begin(ctx, GFE_KT_RESIDUAL64);
+      k_residual64<<<gs, kSpmvBlock, 0, ctx->stream>>>(
+          n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(),
+          d_x, d_b, r64, w.partials, &w.S->rr64, &w.S->ticket[2]);
+      timer_end(ctx);
+      k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, w.S);
+      ctx->launches += 3;
+      ++updates;
+      GFE_TRY(read_state(ctx, w));
+      if (w.hS->converged || w.hS->done) break;
+      // z, p restart from the new residual direction (keeps FCG's beta well defined)
+      GFE_TRY(precond());
+      k_fcg_beta<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
+      k_fcg_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
+      ctx->launches += 2;
+      spmv();
+      rr_chunk = w.hS->rr;
+      continue;
+    }
+    if (w.hS->done) break;
+    // stagnation check of the learned preconditioner
+    if (learned) {
+      slow = (w.hS->rr > 0.25 * rr_chunk) ? slow + 1 : 0;
+      if (slow >= 2) {
+        learned = false;  // Jacobi from here on
+        fallback = 1;
+      }
+    }
+    rr_chunk = w.hS->rr;
+  }
+  // any FP32 correction not yet absorbed
+  k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
+  ctx->launches++;
+  rep->iterations = w.hS->iter;
+  rep->refinements = updates;
+  rep->operator_format = A->dia_valid ? 1 : 0;
+  rep->ndiag = A->dia_valid ? A->dia_ndiag : 0;
+  rep->fallback = fallback;
+  // true FP64 residual
+  k_residual64<<<gs, kSpmvBlock, 0, ctx->stream>>>(
+      n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(), d_x,
+      d_b, r64, w.partials, &w.S->rr, &w.S->ticket[2]);
+  k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb, &w.S->ticket[1]);
+  ctx->launches += 2;
+  GFE_CUDA_TRY(cudaGetLastError());
+  GFE_TRY(read_state(ctx, w));
+  const double bb = w.hS->bb;
+  rep->relres = bb > 0 ? std::sqrt(w.hS->rr / bb) : 0.0;
+  rep->converged = std::isfinite(rep->relres) && rep->relres <= o->rtol * (1.0 + 1e-6);
+  rep->status = std::isfinite(rep->relres) ? GFE_OK : GFE_ERR_NONFINITE;
   return GFE_OK;
 }
 

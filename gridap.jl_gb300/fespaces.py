@@ -11,7 +11,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _lib
-from .geometry import CartesianDiscreteModel
+from .geometry import CartesianDiscreteModel, SimplexDiscreteModel
 
 lagrangian = "lagrangian"
 
@@ -39,6 +39,9 @@ class FESpace:
             dirichlet_tags = [dirichlet_tags]
         self.dirichlet_tags = list(dirichlet_tags)
         nc = reffe.ncomp
+        if isinstance(model, SimplexDiscreteModel):
+            self._simplex_p2(lib, dirichlet_masks)
+            return
         if reffe.order == 2:
             self._conforming(lib, dirichlet_masks)
             return
@@ -86,6 +89,36 @@ class FESpace:
         _lib.check(lib.gfe_cartesian_conforming_dofs(
             D, 2, _lib.ptr(part), nc, _lib.ptr(ent_to_tag), _lib.ptr(np.ascontiguousarray(masks)),
             _lib.ptr(self.cell_dof_ids), _lib.ptr(nfree), _lib.ptr(ndiri)))
+        self.nfree = int(nfree[0])
+        self.ndiri = int(ndiri[0])
+        self.node_comp_to_dof = None
+
+    def _simplex_p2(self, lib, dirichlet_masks):
+        """P2 on a simplexified box (ConformingFESpaces.jl:367-636) via gfe_simplex_p2_dofs.
+        dirichlet_tags name vertex-filter tags of the model; with several tags they must share
+        one component mask."""
+        model, nc = self.model, self.reffe.ncomp
+        if self.reffe.order != 2:
+            raise NotImplementedError("simplexified models carry P2 spaces")
+        vmask = np.zeros(model.num_nodes(), dtype=np.uint8)
+        for t in self.dirichlet_tags:
+            if t not in model.vertex_tags:
+                raise ValueError(f"unknown tag {t!r} (add it with add_tag_from_vertex_filter)")
+            vmask |= model.vertex_tags[t].astype(np.uint8)
+        if dirichlet_masks is None:
+            cmask = np.ones(nc, dtype=np.uint8)
+        else:
+            m = np.asarray(dirichlet_masks, dtype=np.uint8).reshape(-1, nc)
+            if (m != m[0]).any():
+                raise NotImplementedError("one component mask for all Dirichlet tags")
+            cmask = np.ascontiguousarray(m[0])
+        part = np.asarray(model.partition, dtype=np.int64)
+        self.cell_dof_ids = np.empty((model.num_cells(), 10 * nc), dtype=np.int32)
+        nfree = np.zeros(1, dtype=np.int32)
+        ndiri = np.zeros(1, dtype=np.int32)
+        _lib.check(lib.gfe_simplex_p2_dofs(_lib.ptr(part), nc, _lib.ptr(vmask), _lib.ptr(cmask),
+                                           _lib.ptr(self.cell_dof_ids), _lib.ptr(nfree),
+                                           _lib.ptr(ndiri)))
         self.nfree = int(nfree[0])
         self.ndiri = int(ndiri[0])
         self.node_comp_to_dof = None

@@ -113,6 +113,57 @@ class CartesianDiscreteModel:
                      for d in range(self.dim))
 
 
+class SimplexDiscreteModel:
+    """simplexify(CartesianDiscreteModel(domain, partition)) in 3-D: every hexahedron c is
+    split into the 6 tets of the oriented 3-cube simplexification, tet 6c+t
+    (Geometry/Grids.jl:487-558, Geometry/UnstructuredDiscreteModels.jl:85-200). The vertices
+    (and their coordinates) are the Cartesian model's nodes. Dirichlet regions are tags made
+    with `add_tag_from_vertex_filter` (face_labeling_from_vertex_filter: a vertex, edge, face
+    or tet carries the tag when all its vertices pass the filter)."""
+
+    def __init__(self, cart: CartesianDiscreteModel):
+        if cart.dim != 3 or not cart.cartesian:
+            raise NotImplementedError("simplexify is provided for 3-D Cartesian models")
+        self.cart = cart
+        self.dim = 3
+        self.partition = cart.partition
+        self.domain = cart.domain
+        self.node_coords = cart.node_coords
+        self.cartesian = True
+        part = np.asarray(self.partition, dtype=np.int64)
+        self.cell_node_ids = np.empty((int(np.prod(part)) * 6, 4), dtype=np.int32)
+        _lib.check(_lib.load().gfe_simplex_model(_lib.ptr(part), _lib.ptr(self.cell_node_ids)))
+        self.vertex_tags: dict[str, np.ndarray] = {}
+
+    def add_tag_from_vertex_filter(self, name: str, filt):
+        """filt(coords[nverts, 3]) -> bool mask, or a per-vertex callable."""
+        x = self.node_coords
+        try:
+            m = np.asarray(filt(x), dtype=bool)
+            if m.shape != (x.shape[0],):
+                raise ValueError
+        except (ValueError, TypeError, IndexError):
+            m = np.array([bool(filt(xi)) for xi in x])
+        self.vertex_tags[name] = m
+        return self
+
+    def num_cells(self) -> int:
+        return self.cell_node_ids.shape[0]
+
+    def num_nodes(self) -> int:
+        return self.node_coords.shape[0]
+
+    def get_node_coordinates(self) -> np.ndarray:
+        return self.node_coords
+
+    def get_cell_node_ids(self) -> np.ndarray:
+        return self.cell_node_ids
+
+
+def simplexify(model: CartesianDiscreteModel) -> SimplexDiscreteModel:
+    return SimplexDiscreteModel(model)
+
+
 class Triangulation:
     def __init__(self, model: CartesianDiscreteModel):
         self.model = model
@@ -130,4 +181,8 @@ class Measure:
         self.degree = int(degree)
 
     def num_points(self) -> int:
+        if isinstance(self.trian.model, SimplexDiscreteModel):
+            if self.degree not in (4, 5):
+                raise NotImplementedError("tet quadrature of degree 4 or 5 is provided")
+            return 14  # Witherden-Vincent degree 4/5 (ReferenceFEs/WitherdenVincentQuadratures.jl)
         return (self.degree // 2 + 1) ** self.trian.model.dim

@@ -30,6 +30,7 @@ class SolveReport:
         self.relres = r.relres
         self.operator_format = ("sliced-ELL", "diagonal")[r.operator_format]
         self.ndiag = r.ndiag
+        self.fallback = bool(r.fallback)
 
     def __repr__(self):
         return (f"SolveReport(iterations={self.iterations}, refinements={self.refinements}, "
@@ -71,6 +72,17 @@ class MixedCGSolver(LinearSolver):
         super().__init__(rtol, maxiter, precond, inner_rtol, check_every)
 
 
+class FCGSolver(LinearSolver):
+    """Flexible CG with FP32 vectors and FP64 reliable updates, preconditioned by a
+    LearnedBlockPreconditioner (`pc`) or by Jacobi (pc=None); a stagnating learned
+    preconditioner hands over to Jacobi (report.fallback)."""
+
+    def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, pc=None,
+                 inner_rtol: float = 0.1, check_every: int = 0):
+        super().__init__(rtol, maxiter, "jacobi", inner_rtol, check_every)
+        self.pc = pc
+
+
 class SymbolicSetup:
     def __init__(self, solver: LinearSolver):
         self.solver = solver
@@ -100,8 +112,13 @@ def solve_(x, ns: NumericalSetup, b):
     """solve!(x, ns, b): x (numpy or CUDA tensor) receives the solution."""
     rep = _lib.SolveReport()
     o = ns.solver.opts()
-    _lib.check(_lib.load().gfe_solve(ns.A.ctx.handle, ns.A.handle, C.byref(o), _lib.ptr(b),
-                                     _lib.ptr(x), C.byref(rep)))
+    if isinstance(ns.solver, FCGSolver):
+        pc = ns.solver.pc.handle if ns.solver.pc is not None else None
+        _lib.check(_lib.load().gfe_solve_fcg(ns.A.ctx.handle, ns.A.handle, pc, C.byref(o),
+                                             _lib.ptr(b), _lib.ptr(x), C.byref(rep)))
+    else:
+        _lib.check(_lib.load().gfe_solve(ns.A.ctx.handle, ns.A.handle, C.byref(o), _lib.ptr(b),
+                                         _lib.ptr(x), C.byref(rep)))
     ns.report = SolveReport(rep)
     return x
 

@@ -66,7 +66,8 @@ enum {
   GFE_KT_SPMV32 = 1,     /* FP32 SpMV + dot of the inner CG iteration */
   GFE_KT_ASSEMBLE = 2,   /* row-gather numeric assembly */
   GFE_KT_RESIDUAL64 = 3, /* FP64 residual r = b - A x of iterative refinement */
-  GFE_KT_ELEMENT = 4     /* element (cell-integral) kernels */
+  GFE_KT_ELEMENT = 4,    /* element (cell-integral) kernels */
+  GFE_KT_PRECOND = 5     /* learned block preconditioner (MLP on tensor cores + gather) */
 };
 int gfe_ctx_set_timing(gfe_ctx* ctx, int enable);
 int gfe_ctx_kernel_time(gfe_ctx* ctx, int kernel, double* total_ms, int64_t* launches);
@@ -103,6 +104,22 @@ int gfe_clagrangian_dofs(int64_t nnodes, const int8_t* node_to_tag, int ncomp,
 int gfe_cartesian_conforming_dofs(int dim, int order, const int64_t* partition, int ncomp,
                                   const int8_t* entity_to_tag, const uint8_t* tag_masks,
                                   int32_t* cell_dof_ids, int32_t* nfree, int32_t* ndiri);
+
+/* simplexify(CartesianDiscreteModel((0,1)^3-like box, partition)) connectivity: tet 6c+t of
+ * hexahedron c has the hexahedron's nodes at the t-th local tet of the oriented 3-cube
+ * simplexification (1-based node ids, ntets*4).
+ * Replaces Geometry/Grids.jl:487-558 with ReferenceFEs/ExtrusionPolytopes.jl:290-299. */
+int gfe_simplex_model(const int64_t* partition, int32_t* tet_vertex_ids);
+/* Conforming P2 dof numbering on that simplexified box: vertices first (vertex order), then
+ * edges in first-touch order over (tet, local edge), the components of a node consecutive;
+ * a vertex or edge is Dirichlet for the components in comp_mask[ncomp] when all its
+ * vertices carry vertex_mask (the labeling face_labeling_from_vertex_filter builds).
+ * cell_dof_ids: ntets x (10*ncomp), component-major over the 10 local nodes.
+ * Replaces FESpaces/ConformingFESpaces.jl:367-636 with Geometry/GridTopologies.jl:1184-1250,
+ * Geometry/UnstructuredDiscreteModels.jl:85-200 and Geometry/FaceLabelings.jl:590-611. */
+int gfe_simplex_p2_dofs(const int64_t* partition, int32_t ncomp, const uint8_t* vertex_mask,
+                        const uint8_t* comp_mask, int32_t* cell_dof_ids, int32_t* nfree,
+                        int32_t* ndiri);
 
 /* ---- assembly: symbolic ------------------------------------------------------------------ */
 /* Builds the sparsity pattern of the matrix that assembling cell matrices over
@@ -145,11 +162,21 @@ int gfe_numeric_loop_vector(gfe_ctx* ctx, int64_t ncells, int nd, const int32_t*
 /* ---- assembly: fused integrate + assemble for recognised weak forms ----------------------- */
 enum {
   GFE_REFFE_Q1 = 1, /* Lagrangian Q1 on QUAD/HEX, lexicographic nodes */
-  GFE_REFFE_Q2 = 2  /* Lagrangian Q2 on QUAD/HEX (9/27 nodes: vertices, edges, faces, interior)
+  GFE_REFFE_Q2 = 2, /* Lagrangian Q2 on QUAD/HEX (9/27 nodes: vertices, edges, faces, interior)
                        on (multi)linear cells given by node_coords + cell_node_ids (vertices) */
+  GFE_REFFE_P2_TET = 3 /* Lagrangian P2 on TET (10 nodes: vertices, then the midpoints of the
+                          TET edges 12, 13, 23, 14, 24, 34), vector-valued (ncomp 3, local dofs
+                          component-major); cells are the tets of simplexify(Cartesian box)
+                          (GFE_GEOM_CARTESIAN: tet 6c+t of hexahedron c) or affine tets given
+                          by node_coords + cell_node_ids (4 vertices, GFE_GEOM_NODAL) */
 };
 enum { GFE_GEOM_CARTESIAN = 0, GFE_GEOM_NODAL = 1 };
-enum { GFE_FORM_DIFFUSION = 1 };                  /* a(u,v) = int kappa grad(v).grad(u) */
+enum {
+  GFE_FORM_DIFFUSION = 1,  /* a(u,v) = int kappa grad(v).grad(u),  l(v) = int f v */
+  GFE_FORM_ELASTICITY = 2  /* a(u,v) = int eps(v) : (lambda tr(eps(u)) I + 2 mu eps(u)),
+                              l(v) = int f . v; coef = (lambda, mu) once (CONST) or per cell
+                              (CELL, 2 values per cell); source CONST with 3 values (f) */
+};
 enum { GFE_COEF_ONE = 0, GFE_COEF_CONST = 1, GFE_COEF_CELL = 2 };
 enum {
   GFE_SRC_NONE = 0,
@@ -163,7 +190,7 @@ enum { GFE_PREC_FP64 = 0, GFE_PREC_FP32 = 1 };
 typedef struct gfe_problem {
   int32_t dim;          /* 2 or 3 */
   int32_t reffe;        /* GFE_REFFE_* */
-  int32_t ncomp;        /* 1 (scalar) */
+  int32_t ncomp;        /* 1 (scalar); 3 for GFE_FORM_ELASTICITY */
   int32_t degree;       /* quadrature degree (Measure(trian, degree)) */
   int64_t ncells;
   int32_t nd;           /* dofs per cell */
@@ -179,7 +206,7 @@ typedef struct gfe_problem {
   /* weak form */
   int32_t form;         /* GFE_FORM_* */
   int32_t coef_kind;    /* GFE_COEF_* */
-  const double* coef;   /* kappa (1 value or ncells values) */
+  const double* coef;   /* kappa (1 value or ncells values); (lambda, mu) for elasticity */
   int32_t source_kind;  /* GFE_SRC_* */
   const double* source;
   int64_t source_len;   /* number of doubles at `source` */
@@ -224,6 +251,7 @@ typedef struct gfe_solve_report {
   double relres;            /* final ||b - A x|| / ||b|| in FP64, recomputed after the solve */
   int32_t operator_format;  /* SpMV format of the (inner) operator: 0 sliced ELL, 1 diagonal */
   int32_t ndiag;            /* diagonals of the diagonal format (0 otherwise) */
+  int32_t fallback;         /* 1 when a learned preconditioner stagnated and Jacobi took over */
 } gfe_solve_report;
 
 /* Solves A x = b. Replaces the LinearSolver protocol's numerical_setup + solve!
@@ -234,6 +262,58 @@ int gfe_solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* opts, const do
 
 /* y = A x in FP64 (Gridap's mul!(y, A, x) on the assembled matrix; used for residuals). */
 int gfe_matrix_mul(gfe_ctx* ctx, gfe_matrix* A, const double* x, double* y);
+
+/* ---- batched problems -------------------------------------------------------------------- */
+/* Many independent scalar Q1 diffusion problems -div(kappa grad u) = f on unit cubes with
+ * their own partitions (partitions[3*p..3*p+2], equal entries: cubic cells), per-cell kappa (concatenated in problem and
+ * Gridap cell order), homogeneous Dirichlet on the boundary, assembled and solved together:
+ * one block-diagonal system with every problem's rows padded to 256, one symbolic and one
+ * numeric assembly, and a batched Jacobi-PCG with per-problem scalars, convergence and early
+ * exit, replayed in chunks from a CUDA graph with an autotuned launch shape.
+ * No counterpart in Gridap (which solves one operator at a time). */
+typedef struct gfe_batch gfe_batch;
+int gfe_batch_create(gfe_ctx* ctx, int32_t nproblems, const int64_t* partitions,
+                     const double* kappa, gfe_batch** batch);
+int gfe_batch_destroy(gfe_batch* batch);
+int gfe_batch_info(gfe_batch* batch, int64_t* nrows, int64_t* nfree, int64_t* ncells);
+/* x receives the problems' free-dof solutions one after the other (sum of nfree entries). */
+int gfe_batch_assemble_solve(gfe_batch* batch, double source, double rtol, int32_t maxiter,
+                             double* x, int32_t* iterations, int32_t* nconverged);
+
+/* ---- learned block preconditioner + flexible CG -------------------------------------------- */
+/* A preconditioner for 3-D Q1 problems on Cartesian grids: the cells are grouped in 2x2x2
+ * blocks (27 nodes, neighbouring blocks share face nodes) and a small MLP (35 -> 64 -> 64 ->
+ * 27, BF16 weights, FP32 accumulation on the tensor cores) maps each block's residual patch
+ * (RMS-normalised) and its log-kappa pattern to an approximation of the block's local solve;
+ * the block results are averaged at shared nodes. node_to_dof[nnodes] is the Q1 space's node
+ * numbering (Gridap convention), kappa_cell[ncells] the cell coefficients.
+ * No counterpart in Gridap: a LinearSolver preconditioner that a user plugs in. */
+typedef struct gfe_learned_pc gfe_learned_pc;
+int gfe_learned_pc_create(gfe_ctx* ctx, const int64_t* partition, const double* domain,
+                          const int32_t* node_to_dof, int64_t nfree, const double* kappa_cell,
+                          gfe_learned_pc** pc);
+int gfe_learned_pc_destroy(gfe_learned_pc* pc);
+/* Number of FP32 parameters: W1[48][64] | b1[64] | W2[64][64] | b2[64] | W3[64][32] | b3[32]. */
+int gfe_learned_pc_num_params(void);
+int gfe_learned_pc_set_weights(gfe_learned_pc* pc, const float* params);
+int gfe_learned_pc_get_weights(gfe_learned_pc* pc, float* params);
+/* z = M(r) for FP32 device vectors (for tests and custom solvers). */
+int gfe_learned_pc_apply(gfe_learned_pc* pc, const float* r, float* z);
+/* Training samples from an FP64 residual r (host or device) of A: for each listed block, the
+ * network input (48 floats) and the target (32 floats): the block's local solve
+ * A_b^{-1} r_b in FP64, in the network's normalised units. X and T are device arrays. */
+int gfe_learned_pc_samples(gfe_learned_pc* pc, gfe_matrix* A, const double* r,
+                           int64_t nsamples, const int64_t* block_ids, float* X, float* T);
+/* Adam on the mean squared error over (X, T) (device, n rows), `epochs` passes of minibatches
+ * of `batch` rows; initialises the weights when the pc has none. *loss = last epoch's mean. */
+int gfe_learned_pc_train(gfe_learned_pc* pc, const float* X, const float* T, int64_t n,
+                         int32_t epochs, int32_t batch, float lr, uint64_t seed, float* loss);
+/* Flexible CG (FCG(1)) with FP32 vectors and FP64 reliable updates, preconditioned by the
+ * learned block preconditioner (pc != NULL) or by Jacobi (pc == NULL); stagnation of the
+ * learned preconditioner switches to Jacobi (report->fallback = 1). opts->inner_rtol is the
+ * residual reduction between reliable updates; stops on the FP64 relative residual. */
+int gfe_solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_opts* opts,
+                  const double* b, double* x, gfe_solve_report* report);
 
 /* ---- allocation-free solve ----------------------------------------------------------------- */
 /* FP64 Jacobi-preconditioned CG (x0 = 0, stop on ||b - A x|| <= rtol ||b||) on a matrix the

@@ -930,3 +930,331 @@ done:
   free(r); free(z); free(p); free(q); free(dinv);
   return it;
 }
+
+/* ====================================================================================== */
+/* simplexified Cartesian meshes, P2 tetrahedra, Witherden-Vincent quadrature, elasticity */
+/* ====================================================================================== */
+
+/* Local tets of a HEX (1-based local vertices, x fastest), the oriented simplexification of
+ * the 3-cube (ReferenceFEs/ExtrusionPolytopes.jl:290-299). */
+static const int ORC_HEX_TETS[6][4] = {{1, 2, 3, 7}, {1, 2, 5, 7}, {2, 3, 4, 7},
+                                       {2, 4, 7, 8}, {2, 5, 6, 7}, {2, 6, 7, 8}};
+/* TET edges as vertex pairs, in the order of Gridap's extrusion-polytope face generation
+ * (ReferenceFEs/ExtrusionPolytopes.jl:460-531 applied to the (TET, TET, TET) extrusion). */
+static const int ORC_TET_EDGES[6][2] = {{1, 2}, {1, 3}, {2, 3}, {1, 4}, {2, 4}, {3, 4}};
+
+/* simplexify_connectivity (Geometry/Grids.jl:518-558): tet 6c+t of hex c has the hex's
+ * nodes at ORC_HEX_TETS[t]. */
+void orc_simplex_cells(const int64_t* part, int32_t* tet_vertices) {
+  const int64_t nc = part[0] * part[1] * part[2];
+  int32_t* hex = (int32_t*)malloc(sizeof(int32_t) * nc * 8);
+  orc_cartesian_cell_nodes(3, part, hex);
+  for (int64_t c = 0; c < nc; ++c)
+    for (int t = 0; t < 6; ++t)
+      for (int a = 0; a < 4; ++a)
+        tet_vertices[(c * 6 + t) * 4 + a] = hex[c * 8 + ORC_HEX_TETS[t][a] - 1];
+  free(hex);
+}
+
+/* Conforming P2 numbering on the simplexified box: tet edges numbered first-touch over
+ * (tet, local edge) with the cells-around-vertices search of
+ * Geometry/GridTopologies.jl:1184-1250; a face is Dirichlet when every one of its vertices
+ * is (the labeling of Geometry/FaceLabelings.jl:590-611, face_labeling_from_vertex_filter);
+ * dofs numbered vertices first, then edges, in face id order with the components of a face
+ * consecutive (FESpaces/ConformingFESpaces.jl:543-636). cell_dofs: ntets x (10*ncomp),
+ * comp-major over the 10 nodes (4 vertices, 6 edge midpoints in TET edge order). */
+int orc_simplex_p2_numbering(const int64_t* part, int ncomp, const uint8_t* vertex_mask,
+                             const uint8_t* comp_mask, int32_t* cell_dofs, int32_t* nfree,
+                             int32_t* ndiri) {
+  const int64_t ncells = part[0] * part[1] * part[2] * 6;
+  const int64_t nverts = (part[0] + 1) * (part[1] + 1) * (part[2] + 1);
+  int32_t* tv = (int32_t*)malloc(sizeof(int32_t) * ncells * 4);
+  orc_simplex_cells(part, tv);
+  int64_t* vptr = (int64_t*)calloc(nverts + 1, sizeof(int64_t));
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int a = 0; a < 4; ++a) vptr[tv[c * 4 + a]] += 1;
+  for (int64_t v = 0; v < nverts; ++v) vptr[v + 1] += vptr[v];
+  int64_t* vfill = (int64_t*)calloc(nverts, sizeof(int64_t));
+  int32_t* vcells = (int32_t*)malloc(sizeof(int32_t) * vptr[nverts]);
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int a = 0; a < 4; ++a) {
+      int64_t v = tv[c * 4 + a] - 1;
+      vcells[vptr[v] + vfill[v]++] = (int32_t)c;
+    }
+  int32_t* ce = (int32_t*)calloc(ncells * 6, sizeof(int32_t));
+  int32_t nedges = 0;
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int e = 0; e < 6; ++e) {
+      if (ce[c * 6 + e]) continue;
+      const int32_t va = tv[c * 4 + ORC_TET_EDGES[e][0] - 1];
+      const int32_t vb = tv[c * 4 + ORC_TET_EDGES[e][1] - 1];
+      ++nedges;
+      for (int64_t p = vptr[va - 1]; p < vptr[va]; ++p) {
+        const int32_t c2 = vcells[p];
+        int hit = 0;
+        for (int a = 0; a < 4; ++a) hit |= tv[(int64_t)c2 * 4 + a] == vb;
+        if (!hit) continue;
+        for (int e2 = 0; e2 < 6; ++e2) {
+          const int32_t wa = tv[(int64_t)c2 * 4 + ORC_TET_EDGES[e2][0] - 1];
+          const int32_t wb = tv[(int64_t)c2 * 4 + ORC_TET_EDGES[e2][1] - 1];
+          if ((wa == va && wb == vb) || (wa == vb && wb == va)) ce[(int64_t)c2 * 6 + e2] = nedges;
+        }
+      }
+    }
+  /* edge endpoints */
+  int32_t* ev = (int32_t*)malloc(sizeof(int32_t) * 2 * (nedges + 1));
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int e = 0; e < 6; ++e) {
+      ev[2 * ce[c * 6 + e]] = tv[c * 4 + ORC_TET_EDGES[e][0] - 1];
+      ev[2 * ce[c * 6 + e] + 1] = tv[c * 4 + ORC_TET_EDGES[e][1] - 1];
+    }
+  int32_t* vdof = (int32_t*)malloc(sizeof(int32_t) * (nverts + 1) * ncomp);
+  int32_t* edof = (int32_t*)malloc(sizeof(int32_t) * (nedges + 1) * ncomp);
+  int32_t nf = 0, nd = 0;
+  for (int64_t v = 1; v <= nverts; ++v)
+    for (int k = 0; k < ncomp; ++k) {
+      const int diri = vertex_mask[v - 1] && comp_mask[k];
+      vdof[v * ncomp + k] = diri ? -(++nd) : ++nf;
+    }
+  for (int32_t e = 1; e <= nedges; ++e)
+    for (int k = 0; k < ncomp; ++k) {
+      const int tagged = vertex_mask[ev[2 * e] - 1] && vertex_mask[ev[2 * e + 1] - 1];
+      const int diri = tagged && comp_mask[k];
+      edof[e * ncomp + k] = diri ? -(++nd) : ++nf;
+    }
+  const int ndc = 10 * ncomp;
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int k = 0; k < ncomp; ++k) {
+      for (int a = 0; a < 4; ++a) cell_dofs[c * ndc + k * 10 + a] = vdof[tv[c * 4 + a] * ncomp + k];
+      for (int e = 0; e < 6; ++e)
+        cell_dofs[c * ndc + k * 10 + 4 + e] = edof[ce[c * 6 + e] * ncomp + k];
+    }
+  *nfree = nf;
+  *ndiri = nd;
+  free(tv); free(vptr); free(vfill); free(vcells); free(ce); free(ev); free(vdof); free(edof);
+  return 0;
+}
+
+/* P2 Lagrange basis on the unit tet at Gridap's nodes: vertices (0,0,0), (1,0,0), (0,1,0),
+ * (0,0,1), then the midpoints of the TET edges (ReferenceFEs/CLagrangianRefFEs.jl:493-547).
+ * With barycentrics l0 = 1-x-y-z, l1 = x, l2 = y, l3 = z the nodal basis is l_a (2 l_a - 1)
+ * at vertex a and 4 l_a l_b at edge (a, b). phi[npts*10], dphi[npts*10*3]. */
+void orc_p2tet_shapes(int npts, const double* pts, double* phi, double* dphi) {
+  static const double G[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int q = 0; q < npts; ++q) {
+    const double x = pts[q * 3], y = pts[q * 3 + 1], z = pts[q * 3 + 2];
+    const double l[4] = {1.0 - x - y - z, x, y, z};
+    for (int a = 0; a < 4; ++a) {
+      if (phi) phi[q * 10 + a] = l[a] * (2.0 * l[a] - 1.0);
+      if (dphi)
+        for (int d = 0; d < 3; ++d) dphi[(q * 10 + a) * 3 + d] = (4.0 * l[a] - 1.0) * G[a][d];
+    }
+    for (int e = 0; e < 6; ++e) {
+      const int a = ORC_TET_EDGES[e][0] - 1, b = ORC_TET_EDGES[e][1] - 1;
+      if (phi) phi[q * 10 + 4 + e] = 4.0 * l[a] * l[b];
+      if (dphi)
+        for (int d = 0; d < 3; ++d)
+          dphi[(q * 10 + 4 + e) * 3 + d] = 4.0 * (G[a][d] * l[b] + l[a] * G[b][d]);
+    }
+  }
+}
+
+/* The 14-point degree-5 symmetric rule of Witherden & Vincent (2015) on the unit tet, which
+ * Gridap uses for degrees 4 and 5 (ReferenceFEs/WitherdenVincentQuadratures.jl:367-520,
+ * Quadratures.jl:157-182): two S31 orbits (barycentrics (a,a,a,1-3a) and permutations) and
+ * one S22 orbit ((b,b,1/2-b,1/2-b) and permutations). The orbit parameters and weights are
+ * the solution of the degree-5 moment equations, found here by Gauss-Newton in extended
+ * precision from a start near the published values; points are listed in Gridap's orbit
+ * expansion order and the weights sum to 1/6. pts[14*3], w[14]. Returns the residual. */
+static void wv_points(const long double* u, long double P[14][3], long double W[14],
+                      long double dP[14][3][6], long double dW[14][6]) {
+  int r = 0;
+  memset(dP, 0, sizeof(long double) * 14 * 3 * 6);
+  memset(dW, 0, sizeof(long double) * 14 * 6);
+  for (int o = 0; o < 2; ++o) {
+    const long double a = u[o], c = 1.0L - 3.0L * a;
+    /* [-1,1] pattern (s,s,t), (s,t,s), (t,s,s), (s,s,s): s <-> a, t <-> c */
+    const int pat[4][3] = {{0, 0, 1}, {0, 1, 0}, {1, 0, 0}, {0, 0, 0}};
+    for (int k = 0; k < 4; ++k, ++r) {
+      for (int d = 0; d < 3; ++d) {
+        P[r][d] = pat[k][d] ? c : a;
+        dP[r][d][o] = pat[k][d] ? -3.0L : 1.0L;
+      }
+      W[r] = u[3 + o];
+      dW[r][3 + o] = 1.0L;
+    }
+  }
+  {
+    const long double b = u[2], e = 0.5L - b;
+    /* (s,t,t), (t,s,t), (s,s,t), (s,t,s), (t,s,s), (t,t,s): s <-> b, t <-> 1/2-b */
+    const int pat[6][3] = {{0, 1, 1}, {1, 0, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}, {1, 1, 0}};
+    for (int k = 0; k < 6; ++k, ++r) {
+      for (int d = 0; d < 3; ++d) {
+        P[r][d] = pat[k][d] ? e : b;
+        dP[r][d][2] = pat[k][d] ? -1.0L : 1.0L;
+      }
+      W[r] = u[5];
+      dW[r][5] = 1.0L;
+    }
+  }
+}
+
+static long double lpow(long double x, int n) {
+  long double r = 1.0L;
+  for (int i = 0; i < n; ++i) r *= x;
+  return r;
+}
+
+static long double lfact(int n) {
+  long double r = 1.0L;
+  for (int i = 2; i <= n; ++i) r *= i;
+  return r;
+}
+
+double orc_wv_tet_degree5(double* pts, double* w) {
+  long double u[6] = {0.31L, 0.09L, 0.045L, 0.0188L, 0.0122L, 0.0071L};
+  long double P[14][3], W[14], dP[14][3][6], dW[14][6];
+  long double res = 0.0L;
+  for (int it = 0; it < 60; ++it) {
+    wv_points(u, P, W, dP, dW);
+    long double JtJ[6][6] = {{0}}, Jtr[6] = {0};
+    res = 0.0L;
+    for (int p = 0; p <= 5; ++p)
+      for (int q = 0; p + q <= 5; ++q)
+        for (int s = 0; p + q + s <= 5; ++s) {
+          const long double exact = lfact(p) * lfact(q) * lfact(s) / lfact(p + q + s + 3);
+          long double f = -exact, g[6] = {0};
+          for (int k = 0; k < 14; ++k) {
+            const long double m = lpow(P[k][0], p) * lpow(P[k][1], q) * lpow(P[k][2], s);
+            f += W[k] * m;
+            const long double dm[3] = {
+                p ? p * lpow(P[k][0], p - 1) * lpow(P[k][1], q) * lpow(P[k][2], s) : 0.0L,
+                q ? q * lpow(P[k][0], p) * lpow(P[k][1], q - 1) * lpow(P[k][2], s) : 0.0L,
+                s ? s * lpow(P[k][0], p) * lpow(P[k][1], q) * lpow(P[k][2], s - 1) : 0.0L};
+            for (int j = 0; j < 6; ++j)
+              g[j] += dW[k][j] * m +
+                      W[k] * (dm[0] * dP[k][0][j] + dm[1] * dP[k][1][j] + dm[2] * dP[k][2][j]);
+          }
+          res += f * f;
+          for (int i = 0; i < 6; ++i) {
+            Jtr[i] += g[i] * f;
+            for (int j = 0; j < 6; ++j) JtJ[i][j] += g[i] * g[j];
+          }
+        }
+    /* solve JtJ d = -Jtr (Gaussian elimination with partial pivoting) */
+    long double M[6][7];
+    for (int i = 0; i < 6; ++i) {
+      for (int j = 0; j < 6; ++j) M[i][j] = JtJ[i][j];
+      M[i][6] = -Jtr[i];
+    }
+    for (int c = 0; c < 6; ++c) {
+      int piv = c;
+      for (int i = c + 1; i < 6; ++i)
+        if (fabsl(M[i][c]) > fabsl(M[piv][c])) piv = i;
+      for (int j = 0; j < 7; ++j) {
+        long double t = M[c][j];
+        M[c][j] = M[piv][j];
+        M[piv][j] = t;
+      }
+      for (int i = c + 1; i < 6; ++i) {
+        const long double f = M[i][c] / M[c][c];
+        for (int j = c; j < 7; ++j) M[i][j] -= f * M[c][j];
+      }
+    }
+    long double d[6];
+    for (int i = 5; i >= 0; --i) {
+      long double s = M[i][6];
+      for (int j = i + 1; j < 6; ++j) s -= M[i][j] * d[j];
+      d[i] = s / M[i][i];
+    }
+    long double dn = 0.0L;
+    for (int i = 0; i < 6; ++i) {
+      u[i] += d[i];
+      dn += fabsl(d[i]);
+    }
+    if (dn < 1e-30L) break;
+  }
+  wv_points(u, P, W, dP, dW);
+  for (int k = 0; k < 14; ++k) {
+    for (int d = 0; d < 3; ++d) pts[k * 3 + d] = (double)P[k][d];
+    w[k] = (double)W[k];
+  }
+  return (double)sqrtl(res);
+}
+
+/* Isotropic linear elasticity on P2 tets with affine (P1) geometry, following Gridap's
+ * per-quadrature-point steps: Jt = sum_a grad phi1_a (x) x_a over the 4 vertices
+ * (Geometry/Grids.jl:237-241), grad phi = inv(Jt) . grad phi_hat (Fields/FieldsInterfaces.jl
+ * :98-106), eps(u) = symmetric part of grad u for u = phi e_comp (Fields/DiffOperators.jl:48),
+ * sigma = lambda tr(eps) I + 2 mu eps, a = eps(v) : sigma(u), K_ij += a |det Jt| w_q
+ * (Fields/FieldsInterfaces.jl:708-720); b_i += (f . v_i) |det Jt| w_q. Local dofs are
+ * comp-major: dof k*10 + n is node n, component k. lame[2*ncells] = (lambda, mu) per cell;
+ * f[3] constant body force. cellmats[ncells*900] column-major, cellvecs[ncells*30]. */
+int orc_p2tet_cell_arrays_elasticity(int64_t ncells, const int32_t* tet_vertices,
+                                     const double* coords, const double* lame, int nq,
+                                     const double* qx, const double* qw, const double* f,
+                                     double* cellmats, double* cellvecs) {
+  double* phi = (double*)malloc(sizeof(double) * nq * 10);
+  double* dphi = (double*)malloc(sizeof(double) * nq * 10 * 3);
+  orc_p2tet_shapes(nq, qx, phi, dphi);
+  static const double G1[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int64_t c = 0; c < ncells; ++c) {
+    double Jt[9] = {0}, iJt[9];
+    for (int a = 0; a < 4; ++a) {
+      const double* xa = coords + (int64_t)(tet_vertices[c * 4 + a] - 1) * 3;
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) Jt[k * 3 + l] += G1[a][k] * xa[l];
+    }
+    const double dJ = det_t(3, Jt);
+    if (!(dJ > 0.0) && !(dJ < 0.0)) {
+      free(phi);
+      free(dphi);
+      return -1;
+    }
+    inv_t(3, Jt, iJt);
+    const double lam = lame[2 * c], mu = lame[2 * c + 1];
+    double* K = cellmats ? cellmats + c * 900 : NULL;
+    double* bv = cellvecs ? cellvecs + c * 30 : NULL;
+    if (K) memset(K, 0, sizeof(double) * 900);
+    if (bv) memset(bv, 0, sizeof(double) * 30);
+    for (int q = 0; q < nq; ++q) {
+      const double dV = fabs(dJ) * qw[q];
+      double g[10][3];
+      for (int n = 0; n < 10; ++n)
+        for (int k = 0; k < 3; ++k) {
+          double s = 0.0;
+          for (int l = 0; l < 3; ++l) s += iJt[k * 3 + l] * dphi[(q * 10 + n) * 3 + l];
+          g[n][k] = s;
+        }
+      if (K) {
+        for (int j = 0; j < 30; ++j) {
+          const int cj = j / 10, nj = j % 10;
+          /* grad u: (grad u)_{ab} = d_a phi delta_{cj b}; eps = sym; sigma */
+          double eu[3][3], su[3][3];
+          for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+              eu[a][b] = 0.5 * ((b == cj ? g[nj][a] : 0.0) + (a == cj ? g[nj][b] : 0.0));
+          const double tr = eu[0][0] + eu[1][1] + eu[2][2];
+          for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) su[a][b] = (a == b ? lam * tr : 0.0) + 2.0 * mu * eu[a][b];
+          for (int i = 0; i < 30; ++i) {
+            const int ci = i / 10, ni = i % 10;
+            double s = 0.0;
+            for (int a = 0; a < 3; ++a)
+              for (int b = 0; b < 3; ++b) {
+                const double ev =
+                    0.5 * ((b == ci ? g[ni][a] : 0.0) + (a == ci ? g[ni][b] : 0.0));
+                s += ev * su[a][b];
+              }
+            K[i + j * 30] += s * dV;
+          }
+        }
+      }
+      if (bv && f)
+        for (int i = 0; i < 30; ++i) bv[i] += (f[i / 10] * phi[q * 10 + i % 10]) * dV;
+    }
+  }
+  free(phi);
+  free(dphi);
+  return 0;
+}

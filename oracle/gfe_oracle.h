@@ -71,6 +71,23 @@ int orc_q2_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_vert
                                  const double* qx, const double* qw, int fkind,
                                  const double* fdata, double* cellmats, double* cellvecs);
 
+/* ---- simplexified Cartesian boxes, P2 tets, elasticity ---------------------------------- */
+/* Tet 6c+t of hex c: the hex's nodes at its t-th local tet (Geometry/Grids.jl:487-558,
+ * ReferenceFEs/ExtrusionPolytopes.jl:290-299). tet_vertices[ntets*4], 1-based node ids. */
+void orc_simplex_cells(const int64_t* partition, int32_t* tet_vertices);
+/* Conforming P2 dofs on the simplexified box; vertex_mask[nverts] marks the vertices of the
+ * Dirichlet vertex filter, comp_mask[ncomp] the constrained components. */
+int orc_simplex_p2_numbering(const int64_t* partition, int ncomp, const uint8_t* vertex_mask,
+                             const uint8_t* comp_mask, int32_t* cell_dofs, int32_t* nfree,
+                             int32_t* ndiri);
+void orc_p2tet_shapes(int npts, const double* pts, double* phi, double* dphi);
+/* 14-point degree-5 Witherden-Vincent tet rule (Gridap's rule for degrees 4 and 5). */
+double orc_wv_tet_degree5(double* pts, double* w);
+int orc_p2tet_cell_arrays_elasticity(int64_t ncells, const int32_t* tet_vertices,
+                                     const double* coords, const double* lame, int nq,
+                                     const double* qx, const double* qw, const double* f,
+                                     double* cellmats, double* cellvecs);
+
 /* ---- quadrature (ReferenceFEs/Quadratures.jl:191-227, TensorProductQuadratures.jl:68-80) */
 void orc_gauss_legendre01(int n, double* x, double* w);
 /* Tensor-product Gauss-Legendre of a degree on [0,1]^D; returns npoints. */

@@ -64,6 +64,13 @@ def lib():
         L.orc_assemble_vector.argtypes = [C.c_int64, C.c_int, P, P, P]
         L.orc_pcg.argtypes = [C.POINTER(_CSC), P, P, C.c_double, C.c_int, C.c_int, C.c_int, P]
         L.orc_csc_mul.argtypes = [C.POINTER(_CSC), P, P]
+        L.orc_simplex_cells.argtypes = [P, P]
+        L.orc_simplex_p2_numbering.argtypes = [P, C.c_int, P, P, P, P, P]
+        L.orc_p2tet_shapes.argtypes = [C.c_int, P, P, P]
+        L.orc_wv_tet_degree5.argtypes = [P, P]
+        L.orc_wv_tet_degree5.restype = C.c_double
+        L.orc_p2tet_cell_arrays_elasticity.argtypes = [C.c_int64, P, P, P, C.c_int, P, P, P,
+                                                       P, P]
         _lib = L
     return _lib
 
@@ -363,4 +370,109 @@ def poisson_q1(domain, partition, dirichlet_tags=("boundary",), kappa=None, fkin
     if assemble:
         out["csc"] = assemble_csc(cell_dofs, cell_dofs, mats, nfree, nfree)
         out["b"] = assemble_vector(cell_dofs, vecs, nfree)
+    return out
+
+
+# ---- simplexified boxes, P2 tets, elasticity ------------------------------------------------
+def simplex_cells(partition):
+    part = np.ascontiguousarray(partition, np.int64)
+    tv = np.empty((int(np.prod(part)) * 6, 4), np.int32)
+    lib().orc_simplex_cells(_p(part), _p(tv))
+    return tv
+
+
+def simplex_p2_numbering(partition, vertex_mask, ncomp=3, comp_mask=None):
+    part = np.ascontiguousarray(partition, np.int64)
+    vm = np.ascontiguousarray(vertex_mask, np.uint8)
+    cm = np.ascontiguousarray(np.ones(ncomp) if comp_mask is None else comp_mask, np.uint8)
+    cd = np.empty((int(np.prod(part)) * 6, 10 * ncomp), np.int32)
+    nf = np.zeros(1, np.int32)
+    nd = np.zeros(1, np.int32)
+    lib().orc_simplex_p2_numbering(_p(part), ncomp, _p(vm), _p(cm), _p(cd), _p(nf), _p(nd))
+    return cd, int(nf[0]), int(nd[0])
+
+
+def p2tet_shapes(pts):
+    pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+    phi = np.empty((pts.shape[0], 10))
+    dphi = np.empty((pts.shape[0], 10, 3))
+    lib().orc_p2tet_shapes(pts.shape[0], _p(pts), _p(phi), _p(dphi))
+    return phi, dphi
+
+
+def wv_tet_degree5():
+    x = np.empty((14, 3))
+    w = np.empty(14)
+    res = lib().orc_wv_tet_degree5(_p(x), _p(w))
+    return x, w, res
+
+
+def elasticity_p2(domain, partition, lame, f=(0.0, 0.0, -1.0), clamp_x0=True, assemble=True):
+    """Everything Gridap computes for a(u,v) = int eps(v) : (lambda tr eps(u) I + 2 mu eps(u)),
+    l(v) = int f . v on vector P2 over simplexify(CartesianDiscreteModel(domain, partition))
+    with the x = x0 face clamped (all components)."""
+    part = np.asarray(partition, np.int64)
+    coords, _, _ = cartesian_model(domain, partition)
+    tv = simplex_cells(part)
+    vmask = (np.abs(coords[:, 0] - domain[0]) < 1e-12) if clamp_x0 else np.zeros(len(coords), bool)
+    cd, nfree, ndiri = simplex_p2_numbering(part, vmask)
+    x, w, _ = wv_tet_degree5()
+    lame = np.ascontiguousarray(lame, np.float64).reshape(-1)
+    fv = np.ascontiguousarray(f, np.float64)
+    nc = tv.shape[0]
+    mats = np.empty((nc, 30, 30))  # filled col-major per cell
+    vecs = np.empty((nc, 30))
+    rc = lib().orc_p2tet_cell_arrays_elasticity(nc, _p(tv), _p(np.ascontiguousarray(coords)),
+                                                _p(lame), 14, _p(x), _p(w), _p(fv), _p(mats),
+                                                _p(vecs))
+    if rc != 0:
+        raise RuntimeError("degenerate tet")
+    mats = np.ascontiguousarray(np.transpose(mats, (0, 2, 1)))  # col-major -> [c, i, j]
+    out = dict(coords=coords, tet_vertices=tv, cell_dofs=cd, nfree=nfree, ndiri=ndiri,
+               cellmats=mats, cellvecs=vecs, qx=x, qw=w)
+    if assemble:
+        out["csc"] = assemble_csc(cd, cd, mats, nfree, nfree)
+        out["b"] = assemble_vector(cd, vecs, nfree)
+    return out
+
+
+def extrusion_faces(extrusion):
+    """Faces of an extrusion polytope as 1-based vertex lists per dimension, by the
+    generation and ordering rules of ReferenceFEs/ExtrusionPolytopes.jl:460-531
+    (_polytopenfaces / _nfaceboundary!; HEX_AXIS = 1, TET_AXIS = 2)."""
+    D = len(extrusion)
+
+    def boundary(anchor, ext, extend, isanchor, lst):
+        lst.append((anchor, ext))
+        newext = extend
+        for i in range(D):
+            curex = newext[i]
+            if curex > 0:
+                newext = tuple(0 if j == i else newext[j] for j in range(D))
+                edim = tuple(1 if j == i else 0 for j in range(D))
+                tetp = tuple(anchor[j] if j >= i else 0 for j in range(D))
+                if curex == 1:
+                    boundary(tuple(a + e for a, e in zip(anchor, edim)), ext, newext, False, lst)
+                elif isanchor:
+                    boundary(tuple(a + e for a, e in zip(tetp, edim)), ext, newext, False, lst)
+                boundary(anchor, tuple(x + e * curex for x, e in zip(ext, edim)), newext, False,
+                         lst)
+        return lst
+
+    def nfaces(anchor, ext):
+        lst = boundary(anchor, (0,) * D, ext, True, [])
+        for i in range(D):
+            lst.sort(key=lambda f: f[0][i])  # stable sorts, as Julia's sort!
+        for i in range(D):
+            lst.sort(key=lambda f: f[1][i])
+        lst.sort(key=lambda f: sum(1 for x in f[1] if x))
+        return lst
+
+    dim = lambda f: sum(1 for x in f[1] if x)  # noqa: E731
+    allf = nfaces((0,) * D, tuple(extrusion))
+    ids = {f: k + 1 for k, f in enumerate(allf)}
+    out = []
+    for d in range(D + 1):
+        out.append([[ids[s] for s in nfaces(f[0], f[1]) if dim(s) == 0]
+                    for f in allf if dim(f) == d])
     return out

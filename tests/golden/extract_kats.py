@@ -152,6 +152,49 @@ def main(ref: pathlib.Path):
                                  "partition": [3, 3], "order": 2, "dirichlet_tags": dtags,
                                  "cell_dofs": r_q2, "nfree": nfree, "ndiri": ndiri}
 
+    # ---- simplexify(HEX) local tets (ExtrusionPolytopes.jl source) -------------------------
+    f = "src/ReferenceFEs/ExtrusionPolytopes.jl"
+    L = (ref / f).read_text().splitlines()
+    i = find(L, r"^function oriented_simplexify_hypercube")
+    i = find(L, r"elseif dim == 3", i)
+    txt, j = collect_bracketed(L, i + 1, "[")
+    kats["hex_simplexify"] = {"source": f"{f}:{i + 2}-{j + 1}", "tets": julia_array(txt)}
+    f = "test/ReferenceFEsTests/ExtrusionPolytopesTests.jl"
+    L = (ref / f).read_text().splitlines()
+    i = find(L, r"p = Polytope\(TET_AXIS, TET_AXIS, TET_AXIS\)")
+    i = find(L, r"^x = Point\{3,Float64\}\[", i)
+    kats["tet_vertex_coordinates"] = {"source": f"{f}:{i + 1}",
+                                      "value": julia_array(rhs_after(L[i], "="))}
+
+    # ---- Witherden-Vincent tet rule for degrees 4 and 5 (source tables) --------------------
+    f = "src/ReferenceFEs/WitherdenVincentQuadratures.jl"
+    L = (ref / f).read_text().splitlines()
+    i0 = find(L, r"^function _witherdenvincent_quad_tet")
+    i = find(L, r"elseif degree in \(4, 5\)", i0)
+    tx2, j2 = collect_bracketed(L, find(L, r"data2 = \[", i), "[")
+    tx3, j3 = collect_bracketed(L, find(L, r"data3 = \[", i), "[")
+    d2 = julia_array(tx2)
+    d3 = julia_array(tx3)
+    # expansion and mapping to the unit tet as Gridap does it (lines around the tables)
+    wx = []
+    for w, s, t in d2:
+        for x, y, z in ((s, s, t), (s, t, s), (t, s, s), (s, s, s)):
+            wx.append([w, x, y, z])
+    for w, s, t in d3:
+        for x, y, z in ((s, t, t), (t, s, t), (s, s, t), (s, t, s), (t, s, s), (t, t, s)):
+            wx.append([w, x, y, z])
+    for r in wx:
+        r[0] /= 2
+        for d in (1, 2, 3):
+            r[d] = (r[d] + 1) / 2
+    tot = sum(r[0] for r in wx)
+    scale = (1 / 6) / tot
+    kats["wv_tet_degree4"] = {
+        "source": f"{f}:{i + 1}-{j3 + 1}", "npoints": len(wx),
+        "points": [r[1:] for r in wx], "weights": [r[0] * scale for r in wx],
+        "note": "orbit tables expanded, mapped from [-1,1] to the unit tet, weights scaled "
+                "to the tet measure 1/6 (Quadratures.jl _weightcoords_to_coord_weights)"}
+
     out = HERE / "gridap_kats.json"
     out.write_text(json.dumps(kats, indent=1) + "\n")
     print(f"wrote {out}")

@@ -1,0 +1,116 @@
+"""GPU parity of vector P2 elasticity on simplexified Cartesian boxes (the configuration of
+3-D linear elasticity with per-cell Lamé coefficients, body force (0, 0, -1) and the x = 0
+face clamped).
+
+Against the oracle (a literal restatement of Gridap's per-quadrature-point arithmetic and
+InserterCSC assembly): the CSR pattern bit-exact, FP64 values within 1e-12 of each row's
+largest entry, the load vector within 1e-12 of its largest entry. FP32 cell matrices
+(scatter still FP64) within 1e-5 of the row maximum (FP32 keeps 24 bits; the tables and
+Jacobians are formed in FP64 and rounded once, plus FP32 products).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_VAL = 1e-12
+
+
+def _rowscaled_err(rp, nz, ref_nz):
+    err = 0.0
+    for r in range(rp.shape[0] - 1):
+        a, b = rp[r], rp[r + 1]
+        if b > a:
+            s = np.abs(ref_nz[a:b]).max()
+            err = max(err, np.abs(nz[a:b] - ref_nz[a:b]).max() / max(s, 1e-300))
+    return err
+
+
+def _space(gg, part):
+    m = gg.simplexify(gg.CartesianDiscreteModel((0, 1) * 3, part))
+    m.add_tag_from_vertex_filter("x0", lambda x: np.abs(x[:, 0]) < 1e-12)
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, 3, 2), dirichlet_tags="x0")
+    return m, V
+
+
+def _assemble(gg, V, m, lame, precision="fp64", geometry=None):
+    import ctypes as C
+    from gridap_gb300 import _lib
+    dO = gg.Measure(gg.Triangulation(m), 4)
+    lam, mu = gg.CellField(lame[:, 0]), gg.CellField(lame[:, 1])
+    prep = gg.prepare_problem(V, V, dO, (lam, mu), np.array([0.0, 0.0, -1.0]),
+                              precision=precision, geometry=geometry)
+    assem = gg.SparseMatrixAssembler(V, V)
+    A = gg.symbolic_loop_matrix(assem, (None, V.cell_dof_ids, V.cell_dof_ids))
+    b = np.zeros(V.nfree)
+    _lib.check(_lib.load().gfe_assemble_matrix_and_vector(
+        assem.ctx.handle, C.byref(prep.p), A.handle, _lib.ptr(b)))
+    return A, b
+
+
+@pytest.mark.parametrize("part", [(2, 2, 2), (4, 3, 5)])
+@pytest.mark.parametrize("geometry", [None, "nodal"])
+def test_p2_elasticity_fp64_matches_oracle(gg, orc, part, geometry):
+    rng = np.random.default_rng(80 + part[2])
+    m, V = _space(gg, part)
+    lame = np.exp(rng.standard_normal((m.num_cells(), 2)))
+    ref = orc.elasticity_p2((0, 1) * 3, part, lame)
+    assert V.nfree == ref["nfree"]
+    A, b = _assemble(gg, V, m, lame, geometry=geometry)
+    rp, cv, nz = A.export_csr(1)
+    cp, rv, zv = ref["csc"]
+    assert np.array_equal(rp, cp) and np.array_equal(cv, rv)  # symmetric: CSR == CSC
+    assert _rowscaled_err(rp - 1, nz, zv) <= TOL_VAL
+    assert np.abs(b - ref["b"]).max() <= TOL_VAL * np.abs(ref["b"]).max()
+
+
+def test_p2_elasticity_fp32_cells_close(gg, orc):
+    rng = np.random.default_rng(91)
+    part = (3, 4, 3)
+    m, V = _space(gg, part)
+    lame = np.exp(rng.standard_normal((m.num_cells(), 2)))
+    ref = orc.elasticity_p2((0, 1) * 3, part, lame)
+    for geometry in (None, "nodal"):
+        A, b = _assemble(gg, V, m, lame, precision="fp32", geometry=geometry)
+        rp, cv, nz = A.export_csr(1)
+        assert np.array_equal(cv, ref["csc"][1])
+        assert _rowscaled_err(rp - 1, nz, ref["csc"][2]) <= 1e-5
+        assert np.abs(b - ref["b"]).max() <= 1e-12 * np.abs(ref["b"]).max()
+
+
+def test_p2_elasticity_affine_op_and_fcg_solve(gg, orc):
+    """AffineFEOperator through the recognised weak form, then FCG (Jacobi) to 1e-8 against
+    the oracle's own solve of its matrix."""
+    rng = np.random.default_rng(92)
+    part = (4, 4, 4)
+    m, V = _space(gg, part)
+    lame = np.exp(rng.standard_normal((m.num_cells(), 2)))
+    dO = gg.Measure(gg.Triangulation(m), 4)
+    sigma = gg.isotropic_stress(gg.CellField(lame[:, 0]), gg.CellField(lame[:, 1]))
+    op = gg.AffineFEOperator(lambda u, v: gg.integrate(gg.inner(gg.ε(v), sigma(gg.ε(u))), dO),
+                             lambda v: gg.integrate(gg.inner((0.0, 0.0, -1.0), v), dO), V, V)
+    ref = orc.elasticity_p2((0, 1) * 3, part, lame)
+    rp, cv, nz = op.A.export_csr(1)
+    assert np.array_equal(cv, ref["csc"][1])
+    assert _rowscaled_err(rp - 1, nz, ref["csc"][2]) <= TOL_VAL
+    x = np.empty(V.nfree)
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.FCGSolver(rtol=1e-8), op.A), op.A)
+    gg.solve_(x, ns, op.b)
+    assert ns.report.converged and ns.report.relres <= 1e-8
+    S = orc.to_scipy(*ref["csc"], V.nfree, V.nfree)
+    r = ref["b"] - S @ x
+    assert np.linalg.norm(r) / np.linalg.norm(ref["b"]) <= 1.01e-8
+    import scipy.sparse.linalg as sl
+    xs = sl.spsolve(S.tocsc(), ref["b"])
+    assert np.linalg.norm(x - xs) <= 1e-5 * np.linalg.norm(xs)
+
+
+def test_p2_elasticity_vector_only(gg, orc):
+    rng = np.random.default_rng(93)
+    part = (2, 3, 2)
+    m, V = _space(gg, part)
+    lame = np.exp(rng.standard_normal((m.num_cells(), 2)))
+    ref = orc.elasticity_p2((0, 1) * 3, part, lame)
+    dO = gg.Measure(gg.Triangulation(m), 4)
+    b = gg.assemble_vector(lambda v: gg.integrate(gg.inner((0.0, 0.0, -1.0), v), dO), V)
+    assert np.abs(b - ref["b"]).max() <= TOL_VAL * np.abs(ref["b"]).max()

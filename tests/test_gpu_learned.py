@@ -1,0 +1,160 @@
+"""GPU tests of the learned block preconditioner (tcgen05 BF16 MLP, training kernels) and of
+flexible CG.
+
+Tolerances: the MLP output against a numpy evaluation with the same BF16 roundings (inputs,
+weights, hidden activations) within 2e-2 relative to the output scale (FP32 accumulation
+order differs); FCG solutions meet the FP64 relative residual they were asked for.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16(a):
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def _space(gg, n):
+    m = gg.CartesianDiscreteModel((0, 1) * 3, (n, n, n))
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    return m, V
+
+
+def _blocks(V, n):
+    """Block -> 27 dofs (0-based, -1 absent) in the library's order."""
+    nb = (n + 1) // 2
+    n2d = V.node_comp_to_dof[:, 0]
+    out = -np.ones((nb ** 3, 27), np.int64)
+    for b in range(nb ** 3):
+        i0, j0, k0 = 2 * (b % nb), 2 * ((b // nb) % nb), 2 * (b // nb ** 2)
+        for s in range(27):
+            i, j, k = i0 + s % 3, j0 + (s // 3) % 3, k0 + s // 9
+            if i <= n and j <= n and k <= n:
+                d = n2d[i + (n + 1) * (j + (n + 1) * k)]
+                if d > 0:
+                    out[b, s] = d - 1
+    return out
+
+
+def _reference_apply(params, V, n, kappa, r):
+    P = params
+    W1 = P[:48 * 64].reshape(48, 64)
+    b1 = P[3072:3136]
+    W2 = P[3136:3136 + 4096].reshape(64, 64)
+    b2 = P[7232:7296]
+    W3 = P[7296:7296 + 2048].reshape(64, 32)
+    b3 = P[9344:9376]
+    blocks = _blocks(V, n)
+    nb = (n + 1) // 2
+    h = 1.0 / n
+    kap = kappa.reshape(n, n, n)  # [k][j][i]
+    z = np.zeros(V.nfree)
+    cnt = np.zeros(V.nfree)
+    for b in range(blocks.shape[0]):
+        i0, j0, k0 = 2 * (b % nb), 2 * ((b // nb) % nb), 2 * (b // nb ** 2)
+        ids = blocks[b]
+        v = np.where(ids >= 0, r[np.maximum(ids, 0)], 0.0).astype(np.float32)
+        s = np.float32(np.sqrt(np.mean(v * v)))
+        lk = np.array([np.log(kap[min(k0 + (c >> 2), n - 1), min(j0 + ((c >> 1) & 1), n - 1),
+                                 min(i0 + (c & 1), n - 1)]) for c in range(8)])
+        x = np.zeros(48, np.float32)
+        x[:27] = v / s if s > 0 else 0.0
+        x[27:35] = lk - lk.mean()
+        h1 = bf16(np.maximum(bf16(x) @ bf16(W1) + b1, 0))
+        h2 = bf16(np.maximum(h1 @ bf16(W2) + b2, 0))
+        y = h2 @ bf16(W3) + b3
+        scale = s / (np.exp(lk.mean()) * h)
+        for t in range(27):
+            if ids[t] >= 0:
+                z[ids[t]] += y[t] * scale
+                cnt[ids[t]] += 1
+    return z / np.maximum(cnt, 1)
+
+
+def test_mlp_block_apply_matches_bf16_reference(gg):
+    torch = pytest.importorskip("torch")
+    n = 6
+    m, V = _space(gg, n)
+    rng = np.random.default_rng(3)
+    kappa = np.exp(rng.standard_normal(n ** 3))
+    pc = gg.LearnedBlockPreconditioner(V, kappa)
+    P = (rng.standard_normal(pc.num_params()) * 0.2).astype(np.float32)
+    pc.set_weights(P)
+    assert np.array_equal(pc.get_weights(), P)
+    r = rng.standard_normal(V.nfree)
+    dev = torch.device("cuda:0")
+    rd = torch.tensor(r, dtype=torch.float32, device=dev)
+    zd = torch.zeros_like(rd)
+    pc.apply(rd, zd)
+    z = zd.cpu().numpy()
+    zr = _reference_apply(P, V, n, kappa, r.astype(np.float32))
+    assert np.abs(z - zr).max() <= 2e-2 * np.abs(zr).max()
+
+
+def test_training_reduces_loss_and_targets_are_local_solves(gg):
+    torch = pytest.importorskip("torch")
+    n = 8
+    m, V = _space(gg, n)
+    rng = np.random.default_rng(4)
+    kappa = np.exp(rng.standard_normal(n ** 3))
+    dO = gg.Measure(gg.Triangulation(m), 2)
+    kap = gg.CellField(kappa)
+    A, b = gg.assemble_matrix_and_vector(
+        lambda u, v: gg.integrate(kap * gg.inner(gg.grad(v), gg.grad(u)), dO),
+        lambda v: gg.integrate(1.0 * v, dO), V, V)
+    pc = gg.LearnedBlockPreconditioner(V, kappa)
+    dev = torch.device("cuda:0")
+    nsamp = 4096
+    X = torch.empty((nsamp, 48), dtype=torch.float32, device=dev)
+    T = torch.empty((nsamp, 32), dtype=torch.float32, device=dev)
+    ids = rng.integers(0, pc.nblocks, nsamp)
+    r = rng.standard_normal(V.nfree)
+    pc.samples(A, r, ids, X, T)
+    # target of one block = local solve A_b^{-1} r_b in normalised units
+    S = A.to_scipy().toarray()
+    blocks = _blocks(V, n)
+    b0 = ids[0]
+    dofs = blocks[b0]
+    live = dofs >= 0
+    Ab = S[np.ix_(dofs[live], dofs[live])]
+    y = np.linalg.solve(Ab, r[dofs[live]])
+    rb = np.where(live, r[np.maximum(dofs, 0)], 0.0)
+    s = np.sqrt(np.mean(rb ** 2))
+    nb = (n + 1) // 2
+    i0, j0, k0 = 2 * (b0 % nb), 2 * ((b0 // nb) % nb), 2 * (b0 // nb ** 2)
+    kap3 = kappa.reshape(n, n, n)
+    lk = [np.log(kap3[min(k0 + (c >> 2), n - 1), min(j0 + ((c >> 1) & 1), n - 1),
+                      min(i0 + (c & 1), n - 1)]) for c in range(8)]
+    scale = s / (np.exp(np.mean(lk)) / n)
+    t = T[0].cpu().numpy()[:27][live] * scale
+    assert np.allclose(t, y, rtol=1e-4, atol=1e-6 * np.abs(y).max())
+    l1 = pc.fit(X, T, epochs=1, batch=512, lr=1e-3)
+    l2 = pc.fit(X, T, epochs=20, batch=512, lr=1e-3)
+    assert np.isfinite(l1) and l2 < l1
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_fcg_reaches_fp64_tolerance(gg, learned):
+    n = 24
+    m, V = _space(gg, n)
+    rng = np.random.default_rng(5)
+    kappa = np.exp(rng.standard_normal(n ** 3))
+    dO = gg.Measure(gg.Triangulation(m), 2)
+    kap = gg.CellField(kappa)
+    f = gg.NodalField(rng.standard_normal(m.num_nodes()))
+    A, b = gg.assemble_matrix_and_vector(
+        lambda u, v: gg.integrate(kap * gg.inner(gg.grad(v), gg.grad(u)), dO),
+        lambda v: gg.integrate(f * v, dO), V, V)
+    pc = None
+    if learned:
+        pc = gg.LearnedBlockPreconditioner(V, kappa)
+        pc.set_weights((rng.standard_normal(pc.num_params()) * 0.05).astype(np.float32))
+    x = np.empty_like(b)
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.FCGSolver(rtol=1e-8, pc=pc), A), A)
+    gg.solve_(x, ns, b)
+    assert ns.report.converged and ns.report.relres <= 1e-8
+    r = b - A.to_scipy() @ x
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.01e-8

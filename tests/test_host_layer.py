@@ -127,3 +127,58 @@ def test_conforming_q2_vector_components(gg, orc):
     cd, nfree, ndiri = orc.conforming_q2(part, ["tag_25"], ncomp=3, masks=masks)
     assert np.array_equal(V.cell_dof_ids, cd)
     assert (V.nfree, V.ndiri) == (nfree, ndiri)
+
+
+def test_box_cell_dofs_matches_fespace(gg):
+    from gridap_gb300 import workloads
+    for n in (2, 3, 5):
+        m = gg.CartesianDiscreteModel((0, 1) * 3, (n, n, n))
+        V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+        assert np.array_equal(workloads.box_cell_dofs(n), np.asarray(V.cell_dof_ids))
+
+
+def test_batched_workload_sizes():
+    import __graft_entry__ as ge
+    ge.load_package()
+    from gridap_gb300 import workloads
+    sizes, kappas = workloads.batched_diffusion(256)
+    assert len(sizes) == 256 and min(sizes) >= 16 and max(sizes) <= 64
+    assert all(k.size == n ** 3 for n, k in zip(sizes, kappas))
+
+
+@pytest.mark.parametrize("part,face", [((1, 1, 1), 0), ((2, 3, 2), 0), ((3, 2, 4), 1),
+                                       ((4, 4, 4), None)])
+def test_simplex_p2_numbering_matches_oracle(gg, orc, part, face):
+    m = gg.simplexify(gg.CartesianDiscreteModel((0, 1) * 3, part))
+    assert np.array_equal(m.cell_node_ids, orc.simplex_cells(part))
+    coords, _, _ = orc.cartesian_model((0, 1) * 3, part)
+    if face is None:
+        vm = np.zeros(coords.shape[0], bool)
+        tags = ()
+    else:
+        vm = np.abs(coords[:, face] - (0.0 if face == 0 else 1.0)) < 1e-12
+        m.add_tag_from_vertex_filter("clamp", lambda x: np.abs(x[:, face] - (0.0 if face == 0
+                                                                              else 1.0)) < 1e-12)
+        tags = "clamp"
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, 3, 2), dirichlet_tags=tags)
+    cd, nf, nd = orc.simplex_p2_numbering(part, vm)
+    assert (V.nfree, V.ndiri) == (nf, nd)
+    assert np.array_equal(V.cell_dof_ids, cd)
+    # component mask: only z clamped
+    if face is not None:
+        V2 = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, 3, 2), dirichlet_tags=tags,
+                        dirichlet_masks=[[0, 0, 1]])
+        cd2, nf2, nd2 = orc.simplex_p2_numbering(part, vm, comp_mask=[0, 0, 1])
+        assert np.array_equal(V2.cell_dof_ids, cd2) and (V2.nfree, V2.ndiri) == (nf2, nd2)
+
+
+def test_elasticity_form_recognition(gg):
+    from gridap_gb300.celldata import classify_bilinear, classify_linear
+    u, v = gg.get_trial_fe_basis(None), gg.get_fe_basis(None)
+    sigma = gg.isotropic_stress(2.0, 0.5)
+    kind, lm = classify_bilinear(gg.inner(gg.ε(v), sigma(gg.ε(u))))
+    assert kind == "elasticity" and lm == (2.0, 0.5)
+    kind, f = classify_linear(gg.inner((0.0, 0.0, -1.0), v))
+    assert kind == "body_force" and np.array_equal(f, [0, 0, -1])
+    with pytest.raises(NotImplementedError):
+        classify_bilinear(gg.inner(gg.ε(v), gg.ε(u)))

@@ -186,3 +186,101 @@ def test_q2_shapes_partition_of_unity_and_nodality(orc):
         phi, dphi = orc.q2_shapes(D, x)
         assert np.allclose(phi.sum(axis=1), 1.0, atol=1e-14)
         assert np.allclose(dphi.sum(axis=1), 0.0, atol=1e-13)
+
+
+# ---- simplexified boxes, P2 tets, Witherden-Vincent, elasticity ----------------------------
+def test_extrusion_faces_restatement(orc, kats):
+    quad = orc.extrusion_faces((1, 1))
+    assert quad[1] == kats["quad_edge_vertices"]["value"]
+    tet = orc.extrusion_faces((2, 2, 2))
+    assert tet[1] == [[1, 2], [1, 3], [2, 3], [1, 4], [2, 4], [3, 4]]
+    assert len(sum(tet, [])) == 15
+
+
+def test_simplexify_matches_gridap_table(orc, kats):
+    tv = orc.simplex_cells((1, 1, 1))
+    assert tv.tolist() == kats["hex_simplexify"]["tets"]
+
+
+def test_wv_tet_rule_matches_gridap_tables(orc, kats):
+    x, w, res = orc.wv_tet_degree5()
+    g = kats["wv_tet_degree4"]
+    assert res < 1e-18
+    assert np.abs(x - np.array(g["points"])).max() < 2e-16
+    assert np.abs(w - np.array(g["weights"])).max() < 1e-17
+
+
+def test_p2tet_nodal_basis(orc, kats):
+    V = np.array(kats["tet_vertex_coordinates"]["value"], float)
+    edges = orc.extrusion_faces((2, 2, 2))[1]
+    nodes = np.vstack([V] + [(V[a - 1] + V[b - 1]) / 2 for a, b in edges])
+    phi, dphi = orc.p2tet_shapes(nodes)
+    assert np.abs(phi - np.eye(10)).max() < 1e-15
+    # partition of unity and exact gradients of a quadratic
+    x, w, _ = orc.wv_tet_degree5()
+    phi, dphi = orc.p2tet_shapes(x)
+    assert np.abs(phi.sum(1) - 1).max() < 1e-15
+    f = lambda p: p[..., 0] ** 2 + 3 * p[..., 1] * p[..., 2] - p[..., 2]  # noqa: E731
+    gx = np.stack([2 * x[:, 0], 3 * x[:, 2], 3 * x[:, 1] - 1], 1)
+    assert np.abs(np.einsum("qn,n->q", phi, f(nodes)) - f(x)).max() < 1e-14
+    assert np.abs(np.einsum("qnd,n->qd", dphi, f(nodes)) - gx).max() < 1e-13
+
+
+def test_simplex_p2_numbering_counts(orc):
+    for part in [(1, 1, 1), (2, 3, 2), (3, 3, 3)]:
+        coords, _, _ = orc.cartesian_model((0, 1) * 3, part)
+        vm = coords[:, 0] == 0.0
+        cd, nf, nd = orc.simplex_p2_numbering(part, vm)
+        nodes = np.prod([2 * n + 1 for n in part])
+        assert nf + nd == 3 * nodes
+        assert nd == 3 * (2 * part[1] + 1) * (2 * part[2] + 1)
+        ids = cd.ravel()
+        assert set(ids[ids > 0]) == set(range(1, nf + 1))
+        assert set(-ids[ids < 0]) == set(range(1, nd + 1))
+        # vertices are numbered before edges
+        nv = int(np.prod([n + 1 for n in part]))
+        vert = np.abs(cd[:, :4]).max()
+        edge = np.abs(cd[:, 4:10][cd[:, 4:10] > 0]).min()
+        assert vert <= 3 * nv and edge > 0
+
+
+def test_elasticity_p2_invariants(orc):
+    part = (2, 2, 2)
+    rng = np.random.default_rng(0)
+    lame = np.exp(rng.standard_normal((48, 2)))
+    P = orc.elasticity_p2((0, 1) * 3, part, lame, clamp_x0=False)
+    A = orc.to_scipy(*P["csc"], P["nfree"], P["nfree"])
+    assert abs(A - A.T).max() <= 1e-15 * abs(A).max()
+    cd = P["cell_dofs"]
+    coords, _, _ = orc.cartesian_model((0, 1) * 3, part)
+    # every dof's node position: vertices and edge midpoints
+    tv = P["tet_vertices"]
+    X = np.zeros((P["nfree"], 3))
+    comp = np.zeros(P["nfree"], int)
+    edges = orc.extrusion_faces((2, 2, 2))[1]
+    for c in range(cd.shape[0]):
+        xv = coords[tv[c] - 1]
+        xn = np.vstack([xv] + [(xv[a - 1] + xv[b - 1]) / 2 for a, b in edges])
+        for k in range(3):
+            X[cd[c, k * 10:(k + 1) * 10] - 1] = xn
+            comp[cd[c, k * 10:(k + 1) * 10] - 1] = k
+    # rigid body modes are in the kernel
+    for m in range(6):
+        u = np.zeros(P["nfree"])
+        if m < 3:
+            u[comp == m] = 1.0
+        else:
+            a, b = [(1, 2), (2, 0), (0, 1)][m - 3]
+            u[comp == a] = -X[comp == a, b]
+            u[comp == b] = X[comp == b, a]
+        assert np.abs(A @ u).max() < 1e-13 * abs(A).max()
+    # energy of a linear field u = G x with constant lambda, mu
+    P1 = orc.elasticity_p2((0, 1) * 3, part, np.tile([2.0, 0.5], 48), clamp_x0=False)
+    A1 = orc.to_scipy(*P1["csc"], P1["nfree"], P1["nfree"])
+    G = rng.standard_normal((3, 3))
+    u = np.array([G[comp[i]] @ X[i] for i in range(P1["nfree"])])
+    eps = 0.5 * (G + G.T)
+    energy = 2.0 * np.trace(eps) ** 2 + 2 * 0.5 * np.sum(eps * eps)
+    assert abs(u @ (A1 @ u) - energy) < 1e-12 * energy
+    # body force: total load = int f over the box
+    assert abs(P1["b"].reshape(-1)[comp == 2].sum() + 1.0) < 1e-14

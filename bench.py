@@ -210,7 +210,8 @@ def run_gpu(args):
         wall = time.perf_counter() - t0
         kt = {k: ctx.kernel_time(k) for k in (_lib.GFE_KT_SPMV64, _lib.GFE_KT_SPMV32,
                                               _lib.GFE_KT_ASSEMBLE, _lib.GFE_KT_RESIDUAL64,
-                                              _lib.GFE_KT_PRECOND)}
+                                              _lib.GFE_KT_PRECOND, _lib.GFE_KT_VECTOR,
+                                              _lib.GFE_KT_ELEMENT)}
         ctx.set_timing(False)
         ms = e0.elapsed_time(e1) / steps
         if world > 1:
@@ -299,7 +300,6 @@ def run_gpu(args):
             "fp64_ms": avg_ms(r_plain_kt, _lib.GFE_KT_SPMV64),
             "fp32_launches": r_mixed_kt["kt"][_lib.GFE_KT_SPMV32][1],
             "assemble_ms": avg_ms(r_plain_kt, _lib.GFE_KT_ASSEMBLE)}
-    spmv_share = r_mixed_kt["kt"][_lib.GFE_KT_SPMV32][0] / (r_mixed_kt["ms"] * args.steps)
 
     rep_m, rep_p = r_mixed["reps"][-1], r_plain["reps"][-1]
     for rp in r_mixed["reps"] + r_plain["reps"] + r_e2e["reps"]:
@@ -312,10 +312,38 @@ def run_gpu(args):
     d2h = nfree * 8
     peak, peak_kind = peaks()
     nnz = prof["nnz"]
-    dia = rep_m.operator_format == 1
-    # diagonal format: values + x + y (no column ids); sliced ELL: the CSR formula
-    alg = (nnz * 4 + nfree * 8) if dia else spmv_bytes(nnz, nfree, 4)
-    achieved = alg / (prof["fp32_ms"] * 1e-3) / 1e9
+    fmt = rep_m.operator_format
+    # algorithmic bytes of one launch of each timed kernel class (FP32 inner iteration)
+    #   matrix-free lattice SpMV: kappa per cell + p read + q written
+    #   diagonal format: values + p + q (no column ids); sliced ELL: the CSR formula
+    #   vector updates (update + direction): x, r, p, q, dinv read + x, r written, then
+    #   p, r, dinv read + p written = 44 B per row
+    if fmt == 2:
+        alg, kname = ncells * 4 + nfree * 8, ("k_cg_spmv_dot<float, LatticeQ1Op> (matrix-free "
+                                              "FP32 Q1 operator + p.q)")
+    elif fmt == 1:
+        alg, kname = nnz * 4 + nfree * 8, (f"k_cg_spmv_dot<float, DiaOp<float>> (diagonal "
+                                           f"format, {rep_m.ndiag} diagonals, + p.q)")
+    else:
+        alg, kname = spmv_bytes(nnz, nfree, 4), "k_cg_spmv_dot<float, SellOp<float>>"
+    kinds = {
+        "spmv32": dict(kernel=kname, alg=alg, kt=r_mixed_kt["kt"][_lib.GFE_KT_SPMV32],
+                       traffic=profile_traffic({2: "fp32_lattice", 1: "fp32_dia"}.get(
+                           fmt, "fp32_sell"))),
+        "vector32": dict(kernel="k_cg_update4 + k_cg_direction4 (FP32 CG vector updates)",
+                         alg=44 * nfree, kt=r_mixed_kt["kt"][_lib.GFE_KT_VECTOR],
+                         traffic=profile_traffic("fp32_vector")),
+    }
+    table = {}
+    for k, d in kinds.items():
+        tot, cnt = d["kt"]
+        ms_avg = tot / cnt if cnt else float("nan")
+        ach = d["alg"] / (ms_avg * 1e-3) / 1e9 if cnt else float("nan")
+        table[k] = {"kernel": d["kernel"], "algorithmic_bytes_per_launch": d["alg"],
+                    "avg_launch_ms": ms_avg, "launches_timed": cnt, "achieved": ach,
+                    "frac": ach / peak, "traffic": d["traffic"],
+                    "share_of_step_time": tot / (r_mixed_kt["ms"] * args.steps)}
+    dom = max(table, key=lambda k: table[k]["share_of_step_time"])
     alg64 = spmv_bytes(nnz, nfree, 8)
     achieved64 = alg64 / (prof["fp64_ms"] * 1e-3) / 1e9
     out = {
@@ -326,7 +354,8 @@ def run_gpu(args):
         "config": {"workload": f"lognormal_3d {args.n}^3 Q1 diffusion",
                    "free_dofs": nfree, "cells": ncells, "nnz": nnz, "rtol": w.rtol,
                    "solver": f"mixed CG: FP32 Jacobi-PCG with FP64 reliable updates "
-                             f"(delta {args.delta}), FP64 x and true residual",
+                             f"(delta {args.delta}), FP64 x and true residual; inner "
+                             f"operator {rep_m.operator_format}",
                    "assembly": "FP64 cell integrals, FP64 row-gather scatter",
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (matrix %.2f GB)" % (nnz * 12 / 1e9)},
@@ -338,20 +367,21 @@ def run_gpu(args):
         "error_vs_fp64": {"rel_l2_solution": err_vs_fp64, "relres_mixed": rep_m.relres},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": r_e2e["ms"]},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak,
-                     "traffic": profile_traffic("fp32_dia" if dia else "fp32_sell"),
-                     "kernel": ("k_cg_spmv_dot<float, DiaOp<float>> (diagonal-format SpMV, "
-                                f"{rep_m.ndiag} diagonals, + p.q)") if dia else
-                               "k_cg_spmv_dot<float, SellOp<float>> (sliced-ELL SpMV + p.q)",
+        "roofline": {"bound": "hbm", "achieved": table[dom]["achieved"], "peak": peak,
+                     "unit": "GB/s", "frac": table[dom]["frac"],
+                     "traffic": table[dom]["traffic"], "kernel": table[dom]["kernel"],
                      "peak_source": f"{peak_kind} hbm_gbs",
-                     "algorithmic_bytes_per_launch": alg, "avg_launch_ms": prof["fp32_ms"],
-                     "launches_timed": prof["fp32_launches"],
-                     "share_of_step_time": spmv_share,
-                     "timed_in": "instrumented repeat of the timed steps (events around "
-                                 "each SpMV launch on the library's stream), "
+                     "algorithmic_bytes_per_launch": table[dom]["algorithmic_bytes_per_launch"],
+                     "avg_launch_ms": table[dom]["avg_launch_ms"],
+                     "launches_timed": table[dom]["launches_timed"],
+                     "share_of_step_time": table[dom]["share_of_step_time"],
+                     "timed_in": "instrumented repeat of the timed steps (CUDA events around "
+                                 "each launch on the library's stream), "
                                  f"{r_mixed_kt['ms']:.2f} ms/step",
-                     "fp64_spmv": {"achieved": achieved64, "frac": achieved64 / peak,
+                     "kernels": table,
+                     "fp64_spmv": {"kernel": "k_cg_spmv_dot<double, SellOp<double>> (plain path)",
+                                   "achieved": achieved64, "frac": achieved64 / peak,
+                                   "algorithmic_bytes_per_launch": alg64,
                                    "avg_launch_ms": prof["fp64_ms"],
                                    "traffic": profile_traffic("fp64_sell")}},
         "assembly": {"row_gather_ms": prof["assemble_ms"]},
@@ -379,8 +409,9 @@ def bench_batched(args, gg, ctx, lib, barrier):
     n uniform in 16..64, per-cell lognormal kappa (sigma 1.5), u = 0 on the boundary: one
     batched assemble+solve call against the same problems solved one after the other through
     the single-problem path (symbolic + numeric assembly + FP64 Jacobi-PCG per problem)."""
+    import ctypes
     import torch
-    from gridap_gb300 import workloads
+    from gridap_gb300 import _lib, workloads
     sizes, kappas = workloads.batched_diffusion(args.batch_problems)
     rtol = 1e-8
     B = gg.BatchedPoissonProblems(sizes, kappas, ctx)
@@ -467,7 +498,7 @@ def bench_elasticity(args, gg, ctx, lib, timed):
     FP64 and with FP32 cell matrices (FP64 scatter)."""
     import ctypes
     import torch
-    from gridap_gb300 import workloads
+    from gridap_gb300 import _lib, workloads
     model, V, dO, lame, force = workloads.elasticity_3d(args.elast_n)
     nfree = V.num_free_dofs()
     dev = torch.device("cuda", ctx.device)

@@ -34,7 +34,7 @@ GFE_PREC_FP64, GFE_PREC_FP32 = 0, 1
 GFE_SOLVER_CG, GFE_SOLVER_IR_CG, GFE_SOLVER_MIXED_CG = 0, 1, 2
 GFE_PC_NONE, GFE_PC_JACOBI = 0, 1
 GFE_KT_SPMV64, GFE_KT_SPMV32, GFE_KT_ASSEMBLE, GFE_KT_RESIDUAL64, GFE_KT_ELEMENT = 0, 1, 2, 3, 4
-GFE_KT_PRECOND = 5
+GFE_KT_PRECOND, GFE_KT_VECTOR = 5, 6
 
 
 class GfeError(RuntimeError):

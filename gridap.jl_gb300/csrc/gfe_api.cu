@@ -145,7 +145,7 @@ extern "C" int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd,
   for (gfe::DevBuf* b : {&A->rowptr, &A->colval, &A->val, &A->cell_rows, &A->cell_cols,
                          &A->ref_ptr, &A->refs, &A->refpos, &A->sell_ptr, &A->sell_col,
                          &A->sell_val64, &A->sell_val32, &A->dinv64, &A->dinv32,
-                         &A->dia_val32})
+                         &A->dia_val32, &A->mf_kap32, &A->mf_flag})
     b->owner = ctx;
   A->nrows = nrows;
   A->ncols = ncols;
@@ -230,6 +230,7 @@ extern "C" int gfe_matrix_fillstored_zero(gfe_matrix* A) {
     GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * A->nnz, A->ctx->stream));
   A->plan_valid = false;
   A->dia_checked = false;
+  A->mf_state = 0;
   return GFE_OK;
 }
 
@@ -242,6 +243,7 @@ extern "C" int gfe_numeric_loop_matrix(gfe_ctx* ctx, gfe_matrix* A, const double
   const void* d;
   GFE_TRY(device_view(ctx, cellmats, sizeof(double) * (size_t)A->ncells * A->nd * A->nd,
                       SCR_CELLMAT, &d));
+  A->mf_state = 0;
   GFE_TRY(assemble_cellmats(ctx, A, (const double*)d));
   A->plan_valid = false;
   A->dia_checked = false;
@@ -291,6 +293,7 @@ extern "C" int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* p
     GFE_TRY(ctx->scratch[SCR_VEC_B].reserve(sizeof(double) * (p->nfree > 0 ? p->nfree : 1)));
     db = ctx->scratch[SCR_VEC_B].as<double>();
   }
+  if (A) A->mf_state = 0;
   GFE_TRY(assemble_problem(ctx, p, A, db));
   if (A) {
     A->plan_valid = false;

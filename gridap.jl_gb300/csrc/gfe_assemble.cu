@@ -726,6 +726,7 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
     else if (!fp32) GFE_CART(3, false)
     else GFE_CART(3, true)
 #undef GFE_CART
+    if (A && D == 3) GFE_TRY(attach_lattice_operator(ctx, A, p, d_coef, tabs.data()));
   } else {
     // nodal geometry: element kernel into entry-major scratch, then the row gather
     if (!p->node_coords || !p->cell_node_ids)

@@ -487,8 +487,9 @@ extern "C" int gfe_batch_assemble_solve(gfe_batch* B, double source, double rtol
   k_b_init<1><<<g, kRows, 0, ctx->stream>>>(a, B->b.as<double>(), xd, r, p, rtol * rtol);
   ctx->launches++;
   GFE_CUDA_TRY(cudaGetLastError());
-  // autotune once: rows per thread 1 or 2 (256 or 128 threads per block), timed on one
-  // iteration each of the live system (iterations are real CG steps, not discarded)
+  // autotune once: rows per thread 1 or 2 (256 or 128 threads per block), timed on two
+  // iterations each of the live system; the solve then restarts from x = 0, so every call
+  // runs the same arithmetic (repeated calls give identical results)
   int* hdone = (int*)ctx->h_pinned;
   if (B->rpt == 0) {
     cudaEvent_t e0, e1, e2;
@@ -508,6 +509,11 @@ extern "C" int gfe_batch_assemble_solve(gfe_batch* B, double source, double rtol
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaEventDestroy(e2);
+    GFE_CUDA_TRY(cudaMemsetAsync(B->state.ptr, 0, sizeof(PState) * B->nproblems, ctx->stream));
+    GFE_CUDA_TRY(cudaMemsetAsync(B->ndone.ptr, 0, sizeof(int) * 4, ctx->stream));
+    k_b_init<1><<<g, kRows, 0, ctx->stream>>>(a, B->b.as<double>(), xd, r, p, rtol * rtol);
+    ctx->launches++;
+    GFE_CUDA_TRY(cudaGetLastError());
   }
   // chunks of iterations captured once into a CUDA graph and replayed
   const int chunk = 20;

@@ -120,6 +120,14 @@ struct gfe_matrix {
   int dia_ndiag = 0;
   int32_t dia_off[32] = {0};
   gfe::DevBuf dia_val32;
+  // matrix-free FP32 form of a uniform Cartesian Q1 diffusion matrix (3-D) whose rows are the
+  // interior nodes in node order: per-cell kappa in FP32 plus the reference stiffness. The
+  // fused assembly attaches it and checks the row numbering on the device (mf_flag); any
+  // other change of the values drops it. 0 none, 1 numbering check pending, 2 valid.
+  int mf_state = 0;
+  int64_t mf_n[3] = {0, 0, 0};
+  float mf_K[64] = {0};
+  gfe::DevBuf mf_kap32, mf_flag;
 };
 
 namespace gfe {
@@ -217,6 +225,9 @@ int tet_quadrature(int degree, std::vector<double>& x, std::vector<double>& w);
 void p2tet_shapes(int nq, const double* qx, double* phi, double* dphi);
 int elasticity_p2_tables(const double* h, int degree, std::vector<double>& tab);
 int p2tet_reference_integrals(int degree, std::vector<double>& G, std::vector<double>& m);
+// matrix-free FP32 operator attached by the Cartesian Q1 assembly (gfe_solve.cu)
+int attach_lattice_operator(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p,
+                            const double* d_coef, const double* Kref);
 // P2 tet elasticity assembly (gfe_elasticity.cu)
 int assemble_p2_elasticity(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* d_b);
 

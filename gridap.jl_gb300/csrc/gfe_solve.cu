@@ -14,7 +14,9 @@
 // the partials in a fixed order and computes the scalar (alpha, beta) on the device. A done
 // flag set on the device makes later kernels return immediately, so the host launches
 // chunks of iterations and checks convergence once per chunk.
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 
 #include "gfe_internal.h"
 
@@ -249,6 +251,72 @@ int build_dia(gfe_ctx* ctx, gfe_matrix* A) {
   return GFE_OK;
 }
 
+// ---- matrix-free lattice operator: attach (at assembly) and validate -------------------------
+// Checks that the matrix rows are the interior nodes of the (n0, n1, n2) box in node order:
+// every interior corner of every cell carries dof 1 + its interior lattice index, every
+// boundary corner a Dirichlet (negative) id.
+__global__ void k_lattice_check(const int32_t* __restrict__ ids, int64_t n0, int64_t n1,
+                                int64_t n2, int* bad) {
+  const int64_t ncells = n0 * n1 * n2;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncells;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ci = c % n0, t = c / n0, cj = t % n1, ck = t / n1;
+    for (int a = 0; a < 8; ++a) {
+      const int64_t i = ci + (a & 1), j = cj + ((a >> 1) & 1), k = ck + (a >> 2);
+      const bool interior = i > 0 && j > 0 && k > 0 && i < n0 && j < n1 && k < n2;
+      const int32_t id = ids[c * 8 + a];
+      const int64_t want = 1 + (i - 1) + (n0 - 1) * ((j - 1) + (n1 - 1) * (k - 1));
+      if (interior ? (int64_t)id != want : id >= 0) atomicExch(bad, 1);
+    }
+  }
+}
+
+__global__ void k_coef_to_f32(const double* __restrict__ c, int kind, int64_t n,
+                              float* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = kind == GFE_COEF_CELL ? (float)c[i] : kind == GFE_COEF_CONST ? (float)c[0] : 1.f;
+}
+
+int attach_lattice_operator(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p,
+                            const double* d_coef, const double* Kref) {
+  A->mf_state = 0;
+  const int64_t n0 = p->partition[0], n1 = p->partition[1], n2 = p->partition[2];
+  if (p->dim != 3 || n0 < 2 || n1 < 2 || n2 < 2 || A->nd != 8 || A->ncells != n0 * n1 * n2 ||
+      A->nrows != (n0 - 1) * (n1 - 1) * (n2 - 1) || A->nrows != A->ncols)
+    return GFE_OK;
+  const int64_t nc = A->ncells;
+  A->mf_kap32.owner = A->mf_flag.owner = ctx;
+  GFE_TRY(A->mf_kap32.reserve(sizeof(float) * (size_t)nc));
+  GFE_TRY(A->mf_flag.reserve(sizeof(int) * 4));
+  GFE_CUDA_TRY(cudaMemsetAsync(A->mf_flag.ptr, 0, sizeof(int), ctx->stream));
+  const unsigned g = grid_for(nc, 256, (int64_t)ctx->num_sms * 8);
+  k_coef_to_f32<<<g, 256, 0, ctx->stream>>>(d_coef, d_coef ? p->coef_kind : GFE_COEF_ONE, nc,
+                                            A->mf_kap32.as<float>());
+  k_lattice_check<<<g, 256, 0, ctx->stream>>>(A->cell_rows.as<int32_t>(), n0, n1, n2,
+                                              A->mf_flag.as<int>());
+  ctx->launches += 2;
+  GFE_CUDA_TRY(cudaGetLastError());
+  for (int e = 0; e < 64; ++e) A->mf_K[e] = (float)Kref[e];
+  A->mf_n[0] = n0;
+  A->mf_n[1] = n1;
+  A->mf_n[2] = n2;
+  A->mf_state = 1;
+  return GFE_OK;
+}
+
+// Resolves a pending numbering check (one small device read); true when the lattice
+// operator may replace the FP32 matrix.
+static int lattice_ready(gfe_ctx* ctx, gfe_matrix* A, bool* ok) {
+  if (A->mf_state == 1) {
+    int bad = 1;
+    GFE_TRY(copy_out(ctx, &bad, A->mf_flag.ptr, sizeof(int)));
+    A->mf_state = bad ? 0 : 2;
+  }
+  *ok = A->mf_state == 2;
+  return GFE_OK;
+}
+
 // ---- SpMV ---------------------------------------------------------------------------------
 // y = A x on the sliced-ELL copy; thread per row, FMA chain in the accumulation type of TV.
 template <typename TV, typename TX>
@@ -279,7 +347,12 @@ __device__ __forceinline__ TV sell_row(int64_t r, const int64_t* __restrict__ sp
   return acc;
 }
 
-// SpMV operators (thread per row)
+// SpMV operators (thread per row). row_index() is the row of the calling thread (or -1) and
+// blocks() the grid that covers all rows with kSpmvBlock threads per block.
+__device__ __forceinline__ int64_t linear_row() {
+  return (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+}
+
 template <typename T>
 struct SellOp {
   const int64_t* sptr;
@@ -288,6 +361,8 @@ struct SellOp {
   __device__ __forceinline__ T row(int64_t r, const T* __restrict__ x) const {
     return sell_row<T, T>(r, sptr, scol, sval, x);
   }
+  __device__ __forceinline__ int64_t row_index() const { return linear_row(); }
+  unsigned blocks(int64_t n) const { return grid_for(n, kSpmvBlock); }
 };
 
 struct DiagOffsets {
@@ -311,6 +386,73 @@ struct DiaOp {
     }
     return acc;
   }
+  __device__ __forceinline__ int64_t row_index() const { return linear_row(); }
+  unsigned blocks(int64_t nr) const { return grid_for(nr, kSpmvBlock); }
+};
+
+// Matrix-free FP32 operator of uniform Cartesian Q1 diffusion on (n0, n1, n2) cells with rows
+// = interior nodes in node order (the CLagrangian numbering with every boundary node
+// Dirichlet): (A x)_r = sum over the 8 cells K around node r of kappa_K sum_c Kref[l_r, c]
+// x[node(K, c)], boundary nodes contributing 0 -- the cell-wise sum the assembled matrix
+// stores, applied with FP32 element matrices (kappa_K Kref). Reads kappa (4 B per cell) and
+// x instead of 27 values per row. Threads cover 32 x 8 tiles of one k-plane, so the x
+// neighbours along i and j are shared through L1.
+struct LatticeQ1Op {
+  const float* kap;
+  int n0, n1, n2;  // cells per direction
+  float K[64];     // Kref[li + 8 lj], symmetric
+  __device__ __forceinline__ int64_t row_index() const {
+    const int m0 = n0 - 1, m1 = n1 - 1;
+    const int ti = (m0 + 31) >> 5, tj = (m1 + 7) >> 3;
+    const int b = (int)blockIdx.x;
+    const int i = ((b % ti) << 5) + (int)(threadIdx.x & 31);
+    const int j = (((b / ti) % tj) << 3) + (int)(threadIdx.x >> 5);
+    const int k = b / (ti * tj);
+    if (i >= m0 || j >= m1 || k >= n2 - 1) return -1;
+    return (int64_t)i + (int64_t)m0 * ((int64_t)j + (int64_t)m1 * k);
+  }
+  unsigned blocks(int64_t) const {
+    const int64_t m0 = n0 - 1, m1 = n1 - 1, m2 = n2 - 1;
+    return (unsigned)(((m0 + 31) / 32) * ((m1 + 7) / 8) * m2);
+  }
+  __device__ __forceinline__ float row(int64_t r, const float* __restrict__ x) const {
+    const int m0 = n0 - 1, m1 = n1 - 1, m2 = n2 - 1;
+    const int i = (int)(r % m0);
+    const int64_t t = r / m0;
+    const int j = (int)(t % m1), k = (int)(t / m1);
+    // x at the 27 nodes around (i, j, k) (0-based interior coordinates); outside = 0
+    float xs[27];
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          const bool in = (unsigned)(i + dx) < (unsigned)m0 && (unsigned)(j + dy) < (unsigned)m1 &&
+                          (unsigned)(k + dz) < (unsigned)m2;
+          xs[(dx + 1) + 3 * ((dy + 1) + 3 * (dz + 1))] =
+              in ? __ldg(x + r + dx + (int64_t)m0 * (dy + (int64_t)m1 * dz)) : 0.f;
+        }
+    float acc = 0.f;
+#pragma unroll
+    for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+      for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+        for (int cx = 0; cx < 2; ++cx) {
+          // cell (i + cx, j + cy, k + cz) in cell coordinates; the node is its corner lr
+          const float kc =
+              __ldg(kap + (i + cx) + (int64_t)n0 * ((j + cy) + (int64_t)n1 * (k + cz)));
+          const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
+          float s = 0.f;
+#pragma unroll
+          for (int lc = 0; lc < 8; ++lc)
+            s = fmaf(K[lr + 8 * lc],
+                     xs[(cx + (lc & 1)) + 3 * ((cy + ((lc >> 1) & 1)) + 3 * (cz + (lc >> 2)))], s);
+          acc = fmaf(kc, s, acc);
+        }
+    return acc;
+  }
 };
 
 template <typename TV, typename TX, typename TY>
@@ -332,6 +474,16 @@ int spmv64(gfe_ctx* ctx, gfe_matrix* A, const double* d_x, double* d_y) {
   return GFE_OK;
 }
 
+static LatticeQ1Op lattice_op(const gfe_matrix* A) {
+  LatticeQ1Op op;
+  op.kap = A->mf_kap32.as<float>();
+  op.n0 = (int)A->mf_n[0];
+  op.n1 = (int)A->mf_n[1];
+  op.n2 = (int)A->mf_n[2];
+  for (int e = 0; e < 64; ++e) op.K[e] = A->mf_K[e];
+  return op;
+}
+
 // ---- CG kernels (T: vector/matrix type; dot products accumulate in double) ----------------
 // q = A p and partial p.q; the last block computes alpha = rz / pq.
 template <typename T, class Op>
@@ -340,9 +492,9 @@ __global__ void __launch_bounds__(kSpmvBlock)
                   double* __restrict__ partials, SolverState* S) {
   __shared__ double sh[kSpmvBlock / 32];
   if (S->done) return;
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t r = op.row_index();
   T dt = (T)0;
-  if (r < n) {
+  if (r >= 0 && r < n) {
     const T y = op.row(r, p);
     q[r] = y;
     dt = p[r] * y;
@@ -415,6 +567,91 @@ __global__ void __launch_bounds__(kVecBlock)
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     p[i] = fma(beta, p[i], dinv[i] * r[i]);
+}
+
+// FP32 update / direction with 16-byte vector accesses (all bases 16-byte aligned); the
+// scalar tail covers n % 4 entries. Same arithmetic per entry as the scalar kernels.
+__device__ __forceinline__ void upd1(float alpha, float& x, float& r, float p, float q, float d,
+                                     float& rz, float& rr) {
+  x = fmaf(alpha, p, x);
+  r = fmaf(-alpha, q, r);
+  rz = fmaf(r, d * r, rz);
+  rr = fmaf(r, r, rr);
+}
+
+__global__ void __launch_bounds__(kVecBlock)
+    k_cg_update4(int64_t n, float* __restrict__ x, float* __restrict__ r,
+                 const float* __restrict__ p, const float* __restrict__ q,
+                 const float* __restrict__ dinv, double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kVecBlock / 32];
+  if (S->done) return;
+  const float alpha = (float)S->alpha;
+  float rz_t = 0.f, rr_t = 0.f;
+  const int64_t n4 = n >> 2;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = tid; i < n4; i += nth) {
+    float4 xv = reinterpret_cast<float4*>(x)[i];
+    float4 rv = reinterpret_cast<float4*>(r)[i];
+    const float4 pv = __ldcs(reinterpret_cast<const float4*>(p) + i);
+    const float4 qv = __ldcs(reinterpret_cast<const float4*>(q) + i);
+    const float4 dv = __ldg(reinterpret_cast<const float4*>(dinv) + i);
+    upd1(alpha, xv.x, rv.x, pv.x, qv.x, dv.x, rz_t, rr_t);
+    upd1(alpha, xv.y, rv.y, pv.y, qv.y, dv.y, rz_t, rr_t);
+    upd1(alpha, xv.z, rv.z, pv.z, qv.z, dv.z, rz_t, rr_t);
+    upd1(alpha, xv.w, rv.w, pv.w, qv.w, dv.w, rz_t, rr_t);
+    reinterpret_cast<float4*>(x)[i] = xv;
+    reinterpret_cast<float4*>(r)[i] = rv;
+  }
+  for (int64_t i = 4 * n4 + tid; i < n; i += nth) upd1(alpha, x[i], r[i], p[i], q[i], dinv[i], rz_t, rr_t);
+  double rz = block_sum<kVecBlock>((double)rz_t, sh);
+  double rr = block_sum<kVecBlock>((double)rr_t, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = rz;
+    partials[2 * blockIdx.x + 1] = rr;
+  }
+  double tot[2];
+  if (last_block_reduce<kVecBlock, 2>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->iter += 1;
+    S->rr = tot[1];
+    if (!isfinite(tot[1]) || !isfinite(tot[0])) {
+      S->done = 1;
+      S->converged = 0;
+    } else if (tot[1] <= S->tol2) {
+      S->done = 1;
+      S->converged = 1;
+    } else if (S->iter >= S->maxit) {
+      S->done = 1;
+    } else if (S->delta2 > 0.0 && tot[1] < S->delta2 * S->rmax2) {
+      S->done = 1;
+      S->need_update = 1;
+    }
+    S->beta = S->rz != 0.0 ? tot[0] / S->rz : 0.0;
+    S->rz_prev = S->rz;
+    S->rz = tot[0];
+  }
+}
+
+__global__ void __launch_bounds__(kVecBlock)
+    k_cg_direction4(int64_t n, float* __restrict__ p, const float* __restrict__ r,
+                    const float* __restrict__ dinv, const SolverState* S) {
+  if (S->done) return;
+  const float beta = (float)S->beta;
+  const int64_t n4 = n >> 2;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = tid; i < n4; i += nth) {
+    float4 pv = reinterpret_cast<float4*>(p)[i];
+    const float4 rv = __ldcs(reinterpret_cast<const float4*>(r) + i);
+    const float4 dv = __ldg(reinterpret_cast<const float4*>(dinv) + i);
+    pv.x = fmaf(beta, pv.x, dv.x * rv.x);
+    pv.y = fmaf(beta, pv.y, dv.y * rv.y);
+    pv.z = fmaf(beta, pv.z, dv.z * rv.z);
+    pv.w = fmaf(beta, pv.w, dv.w * rv.w);
+    reinterpret_cast<float4*>(p)[i] = pv;
+  }
+  for (int64_t i = 4 * n4 + tid; i < n; i += nth) p[i] = fmaf(beta, p[i], dinv[i] * r[i]);
 }
 
 // CG start from x = 0: r = s*rhs (T), z = dinv r, p = z; partials of r.z and r.r.
@@ -653,9 +890,9 @@ __global__ void __launch_bounds__(kSpmvBlock)
                const float* __restrict__ r, double* __restrict__ partials, SolverState* S) {
   __shared__ double sh[kSpmvBlock / 32];
   if (S->done) return;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = op.row_index();
   float pq = 0.f, pr = 0.f;
-  if (i < n) {
+  if (i >= 0 && i < n) {
     const float y = op.row(i, p);
     q[i] = y;
     pq = p[i] * y;
@@ -718,12 +955,33 @@ template <typename T, class Op>
 static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* x, T* r, T* p,
                    T* q, int check_every, SolverWork& w) {
   const int64_t n = A->nrows;
-  const unsigned gv = (unsigned)(ctx->num_sms * 4);
-  const unsigned gs = grid_for(n, kSpmvBlock);
+  const unsigned gs = op.blocks(n);
+  // FP32 vectors with 16-byte aligned bases take the 4-wide update kernels, with a grid of
+  // up to 8 blocks per SM (enough bytes in flight to stream at HBM rate)
+  bool vec4 = false;
+  if constexpr (sizeof(T) == 4) {
+    vec4 = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(r) |
+             reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(q) |
+             reinterpret_cast<uintptr_t>(dinv)) & 15) == 0;
+  }
+  const unsigned gv = vec4 ? (unsigned)std::max<int64_t>(
+                                 1, std::min<int64_t>((n + 1023) / 1024, ctx->num_sms * 8))
+                           : (unsigned)(ctx->num_sms * 4);
   // Without kernel timing a chunk of iterations is captured once into a CUDA graph (cached in
   // the context while its launch parameters match) and replayed. With timing on, every
   // iteration is launched directly with CUDA events around the SpMV; launches after the
   // converged iteration (they return at once) are dropped from the timing.
+  auto launch_vec = [&](unsigned g) {
+    if constexpr (sizeof(T) == 4) {
+      if (vec4) {
+        k_cg_update4<<<g, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
+        k_cg_direction4<<<g, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
+        return;
+      }
+    }
+    k_cg_update<T><<<g, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
+    k_cg_direction<T><<<g, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
+  };
   const bool timing = ctx->timer.enabled;
   const int kind = sizeof(T) == 4 ? GFE_KT_SPMV32 : GFE_KT_SPMV64;
   cudaGraphExec_t exec = nullptr;
@@ -738,6 +996,8 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
     mix(&op, sizeof(Op));
     mix(&n, sizeof(n));
     mix(&check_every, sizeof(check_every));
+    mix(&gv, sizeof(gv));
+    mix(&vec4, sizeof(vec4));
     const int tsize = (int)sizeof(T);
     mix(&tsize, sizeof(tsize));
     if (ctx->cg_exec && ctx->cg_key == key) exec = ctx->cg_exec;
@@ -750,8 +1010,7 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
       GFE_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
       for (int k = 0; k < check_every; ++k) {
         k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
-        k_cg_update<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
-        k_cg_direction<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
+        launch_vec(gv);
       }
       const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
       if (ce != cudaSuccess) {
@@ -783,8 +1042,9 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
         timer_begin(ctx, kind);
         k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
         timer_end(ctx);
-        k_cg_update<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, x, r, p, q, dinv, w.partials, w.S);
-        k_cg_direction<T><<<gv, kVecBlock, 0, ctx->stream>>>(n, p, r, dinv, w.S);
+        timer_begin(ctx, GFE_KT_VECTOR);
+        launch_vec(gv);
+        timer_end(ctx);
         ctx->launches += 3;
       }
       const cudaError_t le = cudaGetLastError();
@@ -795,7 +1055,7 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
     }
     st = read_state(ctx, w, false);
     if (st != GFE_OK) break;
-    if (timing) timer_drop_last(ctx, check_every - (w.hS->iter - iter0));
+    if (timing) timer_drop_last(ctx, 2 * (check_every - (w.hS->iter - iter0)));
     st = timer_flush(ctx);
     if (st != GFE_OK || w.hS->done) break;
   }
@@ -838,9 +1098,16 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
   const int maxit = o->maxiter > 0 ? o->maxiter : 100000;
   // work vectors: FP64 r, p, q (CG) or FP64 r + FP32 x, r, p, q (IR)
   const size_t n8 = sizeof(double) * (size_t)(n > 0 ? n : 1);
+  // FP32 vectors at a stride padded to 64 entries: every base 16-byte aligned (4-wide kernels)
+  const int64_t npad = (n + 63) & ~(int64_t)63;
   GFE_TRY(ctx->scratch[SCR_SOLVER].reserve(n8 * 3 + 64));
-  GFE_TRY(ctx->scratch[SCR_SOLVER2].reserve(n8 * 2 + 64));
-  const size_t npart = (size_t)grid_for(n, kSpmvBlock) * 2 + (size_t)ctx->num_sms * 8 + 64;
+  GFE_TRY(ctx->scratch[SCR_SOLVER2].reserve(sizeof(float) * (size_t)(npad > 0 ? npad : 64) * 4 +
+                                            256));
+  bool lattice = false;
+  GFE_TRY(lattice_ready(ctx, A, &lattice));
+  size_t nblk = grid_for(n, kSpmvBlock);
+  if (lattice) nblk = std::max<size_t>(nblk, lattice_op(A).blocks(n));
+  const size_t npart = nblk * 2 + (size_t)ctx->num_sms * 16 + 64;
   GFE_TRY(ctx->scratch[SCR_REDUCE].reserve(sizeof(SolverState) + sizeof(double) * npart + 256));
   SolverWork w;
   w.S = ctx->scratch[SCR_REDUCE].as<SolverState>();
@@ -887,9 +1154,9 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
     double* r64 = v64;
     float* f = (float*)ctx->scratch[SCR_SOLVER2].ptr;
     float* x32 = f;
-    float* r32 = f + n;
-    float* p32 = f + 2 * n;
-    float* q32 = f + 3 * n;
+    float* r32 = f + npad;
+    float* p32 = f + 2 * npad;
+    float* q32 = f + 3 * npad;
     const unsigned gv = (unsigned)(ctx->num_sms * 4);
     const double delta = o->inner_rtol > 0 ? o->inner_rtol : 0.1;
     GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
@@ -903,9 +1170,13 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
     ctx->launches += 2;
     w.hS->iter = 0;
     int updates = 0;
-    GFE_TRY(build_dia(ctx, A));
+    if (!lattice) GFE_TRY(build_dia(ctx, A));
     for (;;) {
-      if (A->dia_valid) {
+      if (lattice) {
+        const LatticeQ1Op op = lattice_op(A);
+        GFE_TRY((iterate<float, LatticeQ1Op>(ctx, A, op, dinv32, x32, r32, p32, q32,
+                                             check_every, w)));
+      } else if (A->dia_valid) {
         DiaOp<float> op{A->dia_val32.as<float>(), n, {}};
         for (int d = 0; d < A->dia_ndiag; ++d) op.o.off[d] = A->dia_off[d];
         op.o.nd = A->dia_ndiag;
@@ -936,15 +1207,15 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
     }
     rep->iterations = w.hS->iter;
     rep->refinements = updates;
-    rep->operator_format = A->dia_valid ? 1 : 0;
-    rep->ndiag = A->dia_valid ? A->dia_ndiag : 0;
+    rep->operator_format = lattice ? 2 : A->dia_valid ? 1 : 0;
+    rep->ndiag = lattice ? 27 : A->dia_valid ? A->dia_ndiag : 0;
   } else if (o->method == GFE_SOLVER_IR_CG) {
     double* r64 = v64;  // FP64 residual
     float* f = (float*)ctx->scratch[SCR_SOLVER2].ptr;
     float* x32 = f;
-    float* r32 = f + n;
-    float* p32 = f + 2 * n;
-    float* q32 = f + 3 * n;
+    float* r32 = f + npad;
+    float* p32 = f + 2 * npad;
+    float* q32 = f + 3 * npad;
     const unsigned gv = (unsigned)(ctx->num_sms * 4);
     double* rr_dev = &w.S->rr;
     // x = 0, r = b, ||b||^2
@@ -1013,14 +1284,20 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
               const double* d_b, double* d_x, gfe_solve_report* rep) {
   if (A->nrows != A->ncols) return set_error(GFE_ERR_INVALID_ARGUMENT, "fcg: not square");
   GFE_TRY(build_solver_plan(ctx, A));
-  GFE_TRY(build_dia(ctx, A));
   const int64_t n = A->nrows;
   const int check_every = o->check_every > 0 ? o->check_every : 10;
   const int maxit = o->maxiter > 0 ? o->maxiter : 100000;
   const size_t n8 = sizeof(double) * (size_t)(n > 0 ? n : 1);
+  const int64_t npad = (n + 63) & ~(int64_t)63;
   GFE_TRY(ctx->scratch[SCR_SOLVER].reserve(n8 * 3 + 64));
-  GFE_TRY(ctx->scratch[SCR_SOLVER2].reserve(sizeof(float) * (size_t)(n > 0 ? n : 1) * 5 + 64));
-  const size_t npart = (size_t)grid_for(n, kSpmvBlock) * 2 + (size_t)ctx->num_sms * 8 + 64;
+  GFE_TRY(ctx->scratch[SCR_SOLVER2].reserve(sizeof(float) * (size_t)(npad > 0 ? npad : 64) * 5 +
+                                            256));
+  bool lattice = false;
+  GFE_TRY(lattice_ready(ctx, A, &lattice));
+  if (!lattice) GFE_TRY(build_dia(ctx, A));
+  size_t nblk = grid_for(n, kSpmvBlock);
+  if (lattice) nblk = std::max<size_t>(nblk, lattice_op(A).blocks(n));
+  const size_t npart = nblk * 2 + (size_t)ctx->num_sms * 16 + 64;
   GFE_TRY(ctx->scratch[SCR_REDUCE].reserve(sizeof(SolverState) + sizeof(double) * npart + 256));
   SolverWork w;
   w.S = ctx->scratch[SCR_REDUCE].as<SolverState>();
@@ -1028,7 +1305,8 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   w.hS = (SolverState*)ctx->h_pinned;
   double* r64 = ctx->scratch[SCR_SOLVER].as<double>();
   float* f = (float*)ctx->scratch[SCR_SOLVER2].ptr;
-  float *x32 = f, *r32 = f + n, *p32 = f + 2 * n, *q32 = f + 3 * n, *z32 = f + 4 * n;
+  float *x32 = f, *r32 = f + npad, *p32 = f + 2 * npad, *q32 = f + 3 * npad,
+        *z32 = f + 4 * npad;
   const float* dinv32 = A->dinv32.as<float>();
   const unsigned gv = (unsigned)(ctx->num_sms * 4), gs = grid_for(n, kSpmvBlock);
   const double delta = o->inner_rtol > 0 ? o->inner_rtol : 0.1;
@@ -1038,9 +1316,13 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   dop.o.nd = A->dia_ndiag;
   SellOp<float> sop{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(),
                     A->sell_val32.as<float>()};
+  const LatticeQ1Op lop = lattice ? lattice_op(A) : LatticeQ1Op{};
   auto spmv = [&]() {
     timer_begin(ctx, GFE_KT_SPMV32);
-    if (A->dia_valid)
+    if (lattice)
+      k_fcg_spmv<LatticeQ1Op><<<lop.blocks(n), kSpmvBlock, 0, ctx->stream>>>(
+          n, lop, p32, q32, r32, w.partials, w.S);
+    else if (A->dia_valid)
       k_fcg_spmv<DiaOp<float>><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, dop, p32, q32, r32,
                                                                   w.partials, w.S);
     else

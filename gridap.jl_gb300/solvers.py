@@ -28,7 +28,8 @@ class SolveReport:
         self.converged = bool(r.converged)
         self.status = r.status
         self.relres = r.relres
-        self.operator_format = ("sliced-ELL", "diagonal")[r.operator_format]
+        self.operator_format = ("sliced-ELL", "diagonal", "matrix-free lattice")[
+            r.operator_format]
         self.ndiag = r.ndiag
         self.fallback = bool(r.fallback)
 

@@ -67,7 +67,8 @@ enum {
   GFE_KT_ASSEMBLE = 2,   /* row-gather numeric assembly */
   GFE_KT_RESIDUAL64 = 3, /* FP64 residual r = b - A x of iterative refinement */
   GFE_KT_ELEMENT = 4,    /* element (cell-integral) kernels */
-  GFE_KT_PRECOND = 5     /* learned block preconditioner (MLP on tensor cores + gather) */
+  GFE_KT_PRECOND = 5,    /* learned block preconditioner (MLP on tensor cores + gather) */
+  GFE_KT_VECTOR = 6      /* CG vector updates of one iteration (update + direction kernels) */
 };
 int gfe_ctx_set_timing(gfe_ctx* ctx, int enable);
 int gfe_ctx_kernel_time(gfe_ctx* ctx, int kernel, double* total_ms, int64_t* launches);
@@ -249,8 +250,11 @@ typedef struct gfe_solve_report {
   int32_t converged;        /* 1 when the FP64 residual met rtol */
   int32_t status;           /* GFE_OK or the code that stopped the solver */
   double relres;            /* final ||b - A x|| / ||b|| in FP64, recomputed after the solve */
-  int32_t operator_format;  /* SpMV format of the (inner) operator: 0 sliced ELL, 1 diagonal */
-  int32_t ndiag;            /* diagonals of the diagonal format (0 otherwise) */
+  int32_t operator_format;  /* SpMV format of the (inner FP32) operator: 0 sliced ELL,
+                               1 diagonal, 2 matrix-free (uniform Cartesian Q1 diffusion with
+                               rows = interior nodes in node order: per-cell kappa times the
+                               reference stiffness, applied cell-wise in FP32) */
+  int32_t ndiag;            /* diagonals of the diagonal format, 27 for matrix-free, else 0 */
   int32_t fallback;         /* 1 when a learned preconditioner stagnated and Jacobi took over */
 } gfe_solve_report;
 

@@ -242,9 +242,53 @@ def test_mixed_cg_reaches_fp64_tolerance_without_restarts(gg):
     assert ns2.report.converged and ns2.report.relres <= 1e-8
     assert ns2.report.refinements >= 3
     assert ns2.report.iterations <= 1.25 * ns.report.iterations + 10
+    # all-boundary Dirichlet on a uniform box: the inner operator is the matrix-free one
+    assert ns2.report.operator_format == "matrix-free lattice"
     r = b - A.to_scipy() @ x
     assert np.linalg.norm(r) / np.linalg.norm(b) <= 1e-8 * 1.01
     assert np.linalg.norm(x - x64) / np.linalg.norm(x64) < 1e-5
+
+
+def test_matrix_free_inner_operator_matches_assembled_fp32(gg, orc):
+    """The matrix-free FP32 operator and the assembled matrix's FP32 diagonal copy drive the
+    same mixed CG: re-assembling the same cell matrices through numeric_loop_matrix drops the
+    matrix-free form; both runs meet the FP64 tolerance with iteration counts within a few
+    percent and agree to the solver tolerance. A Dirichlet set that is not the whole boundary
+    (different numbering) never gets the matrix-free form."""
+    rng = np.random.default_rng(34)
+    part = (20, 17, 15)
+    kappa = np.exp(rng.standard_normal(int(np.prod(part))))
+    fnod = rng.standard_normal(int(np.prod(np.array(part) + 1)))
+    _, V, A, b = _problem(gg, (0, 1) * 3, part, ("boundary",), kappa, gg.NodalField(fnod))
+    x1 = np.empty_like(b)
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.MixedCGSolver(rtol=1e-9), A), A)
+    gg.solve_(x1, ns, b)
+    assert ns.report.operator_format == "matrix-free lattice" and ns.report.converged
+    it1 = ns.report.iterations
+    ref = orc.poisson_q1((0, 1) * 3, part, ("boundary",), kappa=kappa, fkind=orc.F_NODAL,
+                         fdata=fnod)
+    assem = gg.SparseMatrixAssembler(V, V)
+    gg.numeric_loop_matrix(A, assem, (ref["cellmats"], V.cell_dof_ids, V.cell_dof_ids))
+    x2 = np.empty_like(b)
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.MixedCGSolver(rtol=1e-9), A), A)
+    gg.solve_(x2, ns, b)
+    assert ns.report.operator_format == "diagonal" and ns.report.converged
+    assert abs(ns.report.iterations - it1) <= 0.05 * it1 + 3
+    assert np.linalg.norm(x1 - x2) <= 1e-7 * np.linalg.norm(x2)
+    # FCG on the lattice form too
+    _, V3, A3, b3 = _problem(gg, (0, 1) * 3, part, ("boundary",), kappa, gg.NodalField(fnod))
+    x3 = np.empty_like(b3)
+    ns3 = gg.numerical_setup(gg.symbolic_setup(gg.FCGSolver(rtol=1e-9), A3), A3)
+    gg.solve_(x3, ns3, b3)
+    assert ns3.report.converged and ns3.report.relres <= 1e-9
+    assert np.linalg.norm(x3 - x2) <= 1e-7 * np.linalg.norm(x2)
+    # Dirichlet on part of the boundary only: other numbering, assembled operator
+    _, V4, A4, b4 = _problem(gg, (0, 1) * 3, part, ("tag_21", "tag_22"), kappa,
+                             gg.NodalField(fnod))
+    x4 = np.empty_like(b4)
+    ns4 = gg.numerical_setup(gg.symbolic_setup(gg.MixedCGSolver(rtol=1e-8), A4), A4)
+    gg.solve_(x4, ns4, b4)
+    assert ns4.report.operator_format != "matrix-free lattice" and ns4.report.converged
 
 
 def test_mixed_cg_on_permuted_numbering(gg, orc):

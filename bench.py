@@ -393,6 +393,10 @@ def run_gpu(args):
         out["batched"] = bench_batched(args, gg, ctx, lib, barrier)
     if not args.no_elasticity:
         out["elasticity_p2"] = bench_elasticity(args, gg, ctx, lib, timed)
+    if not args.no_q2:
+        out["q2_tensor_cores"] = bench_q2(args, gg, ctx, lib, timed)
+    if not args.no_poisson2d:
+        out["poisson_2d"] = bench_poisson2d(args, gg, ctx, lib, timed)
     if rank == 0:
         if not args.no_cpu_baseline:
             args.ref_iters = rep_p.iterations
@@ -551,6 +555,129 @@ def bench_elasticity(args, gg, ctx, lib, timed):
     return out
 
 
+# ---- Q2 on jittered hexahedra: FP64 cells vs TF32 tensor-core cells -------------------------
+def bench_q2(args, gg, ctx, lib, timed):
+    """64^3 Q2 Poisson on jittered hexahedra (2,048,383 free dofs): symbolic + numeric
+    assembly + mixed CG (FP32 inner, FP64 reliable updates) to 1e-8, once with FP64 cell
+    matrices and once with TF32 tensor-core cell matrices (tcgen05, FP32 accumulation, FP64
+    Jacobians), FP64 scatter in both. Reports the element kernel's rate against the dense
+    bf16/tf32 tensor peak it runs on, and the TF32 result's error against FP64."""
+    import ctypes
+    import torch
+    from gridap_gb300 import _lib, workloads
+    model, V, dO = workloads.jittered_q2_3d(args.q2_n)
+    nfree = V.num_free_dofs()
+    ncells, nd = V.cell_dof_ids.shape
+    dev = torch.device("cuda", ctx.device)
+    ids_d = torch.from_numpy(V.cell_dof_ids).to(dev)
+    b = torch.zeros(nfree, dtype=torch.float64, device=dev)
+    x = torch.zeros(nfree, dtype=torch.float64, device=dev)
+    solver = gg.MixedCGSolver(rtol=1e-8)
+    preps = {p: gg.prepare_problem(V, V, dO, 1.0, 1.0, precision=p) for p in ("fp64", "fp32")}
+    vals = {}
+
+    def step(prec, keep=False):
+        h = ctypes.c_void_p()
+        _lib.check(lib.gfe_symbolic_loop_matrix(ctx.handle, ncells, nd, _lib.ptr(ids_d),
+                                                _lib.ptr(ids_d), nfree, nfree, ctypes.byref(h)))
+        try:
+            _lib.check(lib.gfe_assemble_matrix_and_vector(
+                ctx.handle, ctypes.byref(preps[prec].p), h, _lib.ptr(b)))
+            if keep:
+                nnz = ctypes.c_int64()
+                lib.gfe_matrix_info(h, None, None, ctypes.byref(nnz))
+                z = np.empty(nnz.value)
+                rp = np.empty(nfree + 1, np.int64)
+                _lib.check(lib.gfe_matrix_export_csr(h, 0, _lib.ptr(rp), None, _lib.ptr(z)))
+                vals[prec] = (rp, z)
+            o = solver.opts()
+            rep = _lib.SolveReport()
+            _lib.check(lib.gfe_solve(ctx.handle, h, ctypes.byref(o), _lib.ptr(b), _lib.ptr(x),
+                                     ctypes.byref(rep)))
+        finally:
+            lib.gfe_matrix_destroy(h)
+        return rep
+
+    out = {"workload": f"{args.q2_n}^3 Q2 Poisson, jittered nodes (+-0.2h), degree 4",
+           "free_dofs": nfree, "cells": ncells,
+           "solver": "mixed CG (FP32 inner, FP64 reliable updates), Jacobi, 1e-8"}
+    sols = {}
+    peak_tf = None
+    try:
+        mp = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        peak_tf = mp.get("bf16_tflops")
+    except (OSError, ValueError):
+        pass
+    flops = 34.4e9 * ncells / 262144  # Q2 per-cell contraction count (27 q x (push-forward +
+    # 27^2 x 3 x 2 products)) at 64^3
+    for prec in ("fp64", "fp32"):
+        step(prec, keep=True)
+        r = timed("q2_" + prec, lambda: step(prec), 1, 1)
+        rep = r["reps"][-1]
+        if not rep.relres <= 1e-8 * (1 + 1e-6):
+            raise RuntimeError(f"Q2 solve did not reach 1e-8: {rep.relres}")
+        el_tot, el_n = r["kt"][_lib.GFE_KT_ELEMENT]
+        el_ms = el_tot / el_n if el_n else float("nan")
+        out[prec] = {"value": nfree / (r["ms"] * 1e-3), "unit": "DOF/s", "ms_per_step": r["ms"],
+                     "iterations": rep.iterations, "relres": rep.relres,
+                     "element_kernel_ms": el_ms,
+                     "element_tflops": flops / (el_ms * 1e-3) / 1e12 if el_n else None,
+                     "assembly_ms_per_launch": (r["kt"][_lib.GFE_KT_ASSEMBLE][0] /
+                                                max(r["kt"][_lib.GFE_KT_ASSEMBLE][1], 1))}
+        sols[prec] = x.clone()
+    out["fp32"]["element_kernel"] = "tcgen05 kind::tf32 (M=128, N=32, K=88), FP32 accumulate"
+    if peak_tf and out["fp32"]["element_tflops"]:
+        out["fp32"]["element_frac_of_bf16_dense_peak"] = out["fp32"]["element_tflops"] / peak_tf
+    rp, z64 = vals["fp64"]
+    _, z32 = vals["fp32"]
+    rowmax = np.maximum.reduceat(np.abs(z64), rp[:-1])
+    out["tf32_cells_matrix_err_rowscaled"] = float(
+        np.max(np.abs(z32 - z64) / np.repeat(rowmax, np.diff(rp))))
+    out["tf32_cells_solution_rel_l2_vs_fp64"] = float(
+        torch.linalg.norm(sols["fp32"] - sols["fp64"]) / torch.linalg.norm(sols["fp64"]))
+    return out
+
+
+# ---- 2-D Poisson, the configuration Gridap runs on CPU -------------------------------------
+def bench_poisson2d(args, gg, ctx, lib, timed):
+    """256^2 Q1 Poisson, f = sum of 8 seeded sinusoids, CG (FP64, Jacobi) to 1e-10, against
+    the oracle (Gridap's algorithm on the host) for the same problem."""
+    import ctypes
+    import torch
+    from gridap_gb300 import _lib, workloads
+    w = workloads.poisson_2d(256)
+    V = w.space
+    nfree = V.num_free_dofs()
+    ncells, nd = V.cell_dof_ids.shape
+    dev = torch.device("cuda", ctx.device)
+    ids_d = torch.from_numpy(V.cell_dof_ids).to(dev)
+    b = torch.zeros(nfree, dtype=torch.float64, device=dev)
+    x = torch.zeros(nfree, dtype=torch.float64, device=dev)
+    prep = gg.prepare_problem(V, V, w.measure, None, w.source)
+    solver = gg.CGSolver(rtol=w.rtol)
+
+    def step():
+        h = ctypes.c_void_p()
+        _lib.check(lib.gfe_symbolic_loop_matrix(ctx.handle, ncells, nd, _lib.ptr(ids_d),
+                                                _lib.ptr(ids_d), nfree, nfree, ctypes.byref(h)))
+        try:
+            _lib.check(lib.gfe_assemble_matrix_and_vector(ctx.handle, ctypes.byref(prep.p), h,
+                                                          _lib.ptr(b)))
+            o = solver.opts()
+            rep = _lib.SolveReport()
+            _lib.check(lib.gfe_solve(ctx.handle, h, ctypes.byref(o), _lib.ptr(b), _lib.ptr(x),
+                                     ctypes.byref(rep)))
+        finally:
+            lib.gfe_matrix_destroy(h)
+        return rep
+
+    r = timed("poisson2d", step, 5, 3, kernel_timing=False)
+    rep = r["reps"][-1]
+    return {"workload": "256^2 Q1 Poisson, sinusoid-sum source, CG 1e-10", "free_dofs": nfree,
+            "value": nfree / (r["ms"] * 1e-3), "unit": "DOF/s", "ms_per_step": r["ms"],
+            "iterations": rep.iterations, "relres": rep.relres}
+
+
 # ---- CPU baseline / reference arm ---------------------------------------------------------
 def cpu_baseline(args, w=None, quick=False):
     """The oracle (CPU restatement of Gridap's algorithm) on the host cores: serial
@@ -627,6 +754,9 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-elasticity", action="store_true")
     ap.add_argument("--elast-n", type=int, default=48)
+    ap.add_argument("--no-q2", action="store_true")
+    ap.add_argument("--q2-n", type=int, default=64)
+    ap.add_argument("--no-poisson2d", action="store_true")
     ap.add_argument("--batch-problems", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gfe":

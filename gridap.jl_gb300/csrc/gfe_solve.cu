@@ -59,6 +59,34 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return s;
 }
 
+// Block sum of FP32 values: FP32 within each warp (shuffles), FP64 across the block's warps
+// in warp order. Deterministic; avoids FP64 shuffles, which cost a full warp instruction on
+// the FP64 pipe each.
+template <int NT>
+__device__ __forceinline__ double block_sum_f(float v, double* sh) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = (double)v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NT / 32; ++i) s += sh[i];
+  __syncthreads();
+  return s;
+}
+
+template <int NT, typename T>
+__device__ __forceinline__ double block_sum_t(T v, double* sh) {
+  if constexpr (sizeof(T) == 4) return block_sum_f<NT>(v, sh);
+  else return block_sum<NT>((double)v, sh);
+}
+
+// Linear block id and block count of 1-, 2- or 3-D grids.
+__device__ __forceinline__ unsigned block_linear() {
+  return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+}
+__device__ __forceinline__ unsigned grid_blocks() { return gridDim.x * gridDim.y * gridDim.z; }
+
 // Called by every block after writing its partial(s). Returns true in the last block, with
 // the partial sums of all blocks reduced in block order into out[0..nv).
 template <int NT, int NV>
@@ -66,7 +94,7 @@ __device__ bool last_block_reduce(unsigned* ticket, const double* partials, int 
                                   double* out, double* sh) {
   __shared__ bool last;
   __threadfence();
-  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == (unsigned)nblocks - 1);
   __syncthreads();
   if (!last) return false;
   __threadfence();
@@ -285,6 +313,9 @@ int attach_lattice_operator(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p,
   if (p->dim != 3 || n0 < 2 || n1 < 2 || n2 < 2 || A->nd != 8 || A->ncells != n0 * n1 * n2 ||
       A->nrows != (n0 - 1) * (n1 - 1) * (n2 - 1) || A->nrows != A->ncols)
     return GFE_OK;
+  // the operator's 32-bit strides and its (i-tiles, j-tiles, k) grid
+  if (n0 * n1 >= ((int64_t)1 << 31) || n2 - 1 > 65535 || (n1 - 1 + 7) / 8 > 65535)
+    return GFE_OK;
   const int64_t nc = A->ncells;
   A->mf_kap32.owner = A->mf_flag.owner = ctx;
   GFE_TRY(A->mf_kap32.reserve(sizeof(float) * (size_t)nc));
@@ -363,6 +394,7 @@ struct SellOp {
   }
   __device__ __forceinline__ int64_t row_index() const { return linear_row(); }
   unsigned blocks(int64_t n) const { return grid_for(n, kSpmvBlock); }
+  dim3 grid(int64_t n) const { return dim3(blocks(n)); }
 };
 
 struct DiagOffsets {
@@ -388,6 +420,7 @@ struct DiaOp {
   }
   __device__ __forceinline__ int64_t row_index() const { return linear_row(); }
   unsigned blocks(int64_t nr) const { return grid_for(nr, kSpmvBlock); }
+  dim3 grid(int64_t nr) const { return dim3(blocks(nr)); }
 };
 
 // Matrix-free FP32 operator of uniform Cartesian Q1 diffusion on (n0, n1, n2) cells with rows
@@ -399,40 +432,44 @@ struct DiaOp {
 // neighbours along i and j are shared through L1.
 struct LatticeQ1Op {
   const float* kap;
-  int n0, n1, n2;  // cells per direction
-  float K[64];     // Kref[li + 8 lj], symmetric
+  int n0, n1, n2;   // cells per direction
+  int s1, s2;       // row strides of j and k: m0 and m0*m1 (m = n - 1 interior nodes)
+  int c1, c2;       // cell strides of j and k: n0 and n0*n1
+  float K[64];      // Kref[li + 8 lj], symmetric
+  // grid: x = 32-wide tiles along i, y = 8-wide tiles along j, z = k
+  dim3 grid(int64_t) const {
+    return dim3((unsigned)((n0 - 1 + 31) / 32), (unsigned)((n1 - 1 + 7) / 8), (unsigned)(n2 - 1));
+  }
+  unsigned blocks(int64_t n) const {
+    const dim3 g = grid(n);
+    return g.x * g.y * g.z;
+  }
+  __device__ __forceinline__ int ti() const { return (int)(blockIdx.x * 32 + (threadIdx.x & 31)); }
+  __device__ __forceinline__ int tj() const { return (int)(blockIdx.y * 8 + (threadIdx.x >> 5)); }
   __device__ __forceinline__ int64_t row_index() const {
-    const int m0 = n0 - 1, m1 = n1 - 1;
-    const int ti = (m0 + 31) >> 5, tj = (m1 + 7) >> 3;
-    const int b = (int)blockIdx.x;
-    const int i = ((b % ti) << 5) + (int)(threadIdx.x & 31);
-    const int j = (((b / ti) % tj) << 3) + (int)(threadIdx.x >> 5);
-    const int k = b / (ti * tj);
-    if (i >= m0 || j >= m1 || k >= n2 - 1) return -1;
-    return (int64_t)i + (int64_t)m0 * ((int64_t)j + (int64_t)m1 * k);
+    const int i = ti(), j = tj(), k = (int)blockIdx.z;
+    if (i >= n0 - 1 || j >= n1 - 1) return -1;
+    return (int64_t)i + (int64_t)s1 * j + (int64_t)s2 * k;
   }
-  unsigned blocks(int64_t) const {
-    const int64_t m0 = n0 - 1, m1 = n1 - 1, m2 = n2 - 1;
-    return (unsigned)(((m0 + 31) / 32) * ((m1 + 7) / 8) * m2);
-  }
+  // Valid only for r == row_index() of the calling thread: the node comes from the thread.
   __device__ __forceinline__ float row(int64_t r, const float* __restrict__ x) const {
-    const int m0 = n0 - 1, m1 = n1 - 1, m2 = n2 - 1;
-    const int i = (int)(r % m0);
-    const int64_t t = r / m0;
-    const int j = (int)(t % m1), k = (int)(t / m1);
-    // x at the 27 nodes around (i, j, k) (0-based interior coordinates); outside = 0
+    const int i = ti(), j = tj(), k = (int)blockIdx.z;
+    const bool ok[3][3] = {{i > 0, true, i < n0 - 2}, {j > 0, true, j < n1 - 2},
+                           {k > 0, true, k < n2 - 2}};
+    const float* xr = x + r;
+    // x at the 27 nodes around (i, j, k) (interior coordinates); outside the interior = 0
     float xs[27];
 #pragma unroll
     for (int dz = -1; dz <= 1; ++dz)
 #pragma unroll
       for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
-        for (int dx = -1; dx <= 1; ++dx) {
-          const bool in = (unsigned)(i + dx) < (unsigned)m0 && (unsigned)(j + dy) < (unsigned)m1 &&
-                          (unsigned)(k + dz) < (unsigned)m2;
+        for (int dx = -1; dx <= 1; ++dx)
           xs[(dx + 1) + 3 * ((dy + 1) + 3 * (dz + 1))] =
-              in ? __ldg(x + r + dx + (int64_t)m0 * (dy + (int64_t)m1 * dz)) : 0.f;
-        }
+              (ok[0][dx + 1] && ok[1][dy + 1] && ok[2][dz + 1]) ? __ldg(xr + dx + s1 * dy + s2 * dz)
+                                                               : 0.f;
+    // cell (i + cx, j + cy, k + cz) in cell coordinates; the node is its local corner lr
+    const float* kp = kap + ((int64_t)i + (int64_t)c1 * j + (int64_t)c2 * k);
     float acc = 0.f;
 #pragma unroll
     for (int cz = 0; cz < 2; ++cz)
@@ -440,9 +477,7 @@ struct LatticeQ1Op {
       for (int cy = 0; cy < 2; ++cy)
 #pragma unroll
         for (int cx = 0; cx < 2; ++cx) {
-          // cell (i + cx, j + cy, k + cz) in cell coordinates; the node is its corner lr
-          const float kc =
-              __ldg(kap + (i + cx) + (int64_t)n0 * ((j + cy) + (int64_t)n1 * (k + cz)));
+          const float kc = __ldg(kp + cx + c1 * cy + c2 * cz);
           const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
           float s = 0.f;
 #pragma unroll
@@ -480,6 +515,10 @@ static LatticeQ1Op lattice_op(const gfe_matrix* A) {
   op.n0 = (int)A->mf_n[0];
   op.n1 = (int)A->mf_n[1];
   op.n2 = (int)A->mf_n[2];
+  op.s1 = op.n0 - 1;
+  op.s2 = (op.n0 - 1) * (op.n1 - 1);
+  op.c1 = op.n0;
+  op.c2 = op.n0 * op.n1;
   for (int e = 0; e < 64; ++e) op.K[e] = A->mf_K[e];
   return op;
 }
@@ -499,10 +538,10 @@ __global__ void __launch_bounds__(kSpmvBlock)
     q[r] = y;
     dt = p[r] * y;
   }
-  const double d = block_sum<kSpmvBlock>((double)dt, sh);
-  if (threadIdx.x == 0) partials[blockIdx.x] = d;
+  const double d = block_sum_t<kSpmvBlock, T>(dt, sh);
+  if (threadIdx.x == 0) partials[block_linear()] = d;
   double tot[1];
-  if (last_block_reduce<kSpmvBlock, 1>(&S->ticket[0], partials, gridDim.x, tot, sh) &&
+  if (last_block_reduce<kSpmvBlock, 1>(&S->ticket[0], partials, grid_blocks(), tot, sh) &&
       threadIdx.x == 0) {
     S->pq = tot[0];
     S->alpha = tot[0] != 0.0 ? S->rz / tot[0] : 0.0;
@@ -590,22 +629,36 @@ __global__ void __launch_bounds__(kVecBlock)
   const int64_t n4 = n >> 2;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nth = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = tid; i < n4; i += nth) {
-    float4 xv = reinterpret_cast<float4*>(x)[i];
-    float4 rv = reinterpret_cast<float4*>(r)[i];
-    const float4 pv = __ldcs(reinterpret_cast<const float4*>(p) + i);
-    const float4 qv = __ldcs(reinterpret_cast<const float4*>(q) + i);
-    const float4 dv = __ldg(reinterpret_cast<const float4*>(dinv) + i);
-    upd1(alpha, xv.x, rv.x, pv.x, qv.x, dv.x, rz_t, rr_t);
-    upd1(alpha, xv.y, rv.y, pv.y, qv.y, dv.y, rz_t, rr_t);
-    upd1(alpha, xv.z, rv.z, pv.z, qv.z, dv.z, rz_t, rr_t);
-    upd1(alpha, xv.w, rv.w, pv.w, qv.w, dv.w, rz_t, rr_t);
-    reinterpret_cast<float4*>(x)[i] = xv;
-    reinterpret_cast<float4*>(r)[i] = rv;
+  // two float4 groups per trip so that ten 16-byte loads are in flight per thread
+  for (int64_t i0 = tid; i0 < n4; i0 += 2 * nth) {
+    float4 xv[2], rv[2], pv[2], qv[2], dv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t i = i0 + u * nth;
+      if (i < n4) {
+        xv[u] = reinterpret_cast<float4*>(x)[i];
+        rv[u] = reinterpret_cast<float4*>(r)[i];
+        pv[u] = __ldcs(reinterpret_cast<const float4*>(p) + i);
+        qv[u] = __ldcs(reinterpret_cast<const float4*>(q) + i);
+        dv[u] = __ldg(reinterpret_cast<const float4*>(dinv) + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t i = i0 + u * nth;
+      if (i < n4) {
+        upd1(alpha, xv[u].x, rv[u].x, pv[u].x, qv[u].x, dv[u].x, rz_t, rr_t);
+        upd1(alpha, xv[u].y, rv[u].y, pv[u].y, qv[u].y, dv[u].y, rz_t, rr_t);
+        upd1(alpha, xv[u].z, rv[u].z, pv[u].z, qv[u].z, dv[u].z, rz_t, rr_t);
+        upd1(alpha, xv[u].w, rv[u].w, pv[u].w, qv[u].w, dv[u].w, rz_t, rr_t);
+        reinterpret_cast<float4*>(x)[i] = xv[u];
+        reinterpret_cast<float4*>(r)[i] = rv[u];
+      }
+    }
   }
   for (int64_t i = 4 * n4 + tid; i < n; i += nth) upd1(alpha, x[i], r[i], p[i], q[i], dinv[i], rz_t, rr_t);
-  double rz = block_sum<kVecBlock>((double)rz_t, sh);
-  double rr = block_sum<kVecBlock>((double)rr_t, sh);
+  double rz = block_sum_f<kVecBlock>(rz_t, sh);
+  double rr = block_sum_f<kVecBlock>(rr_t, sh);
   if (threadIdx.x == 0) {
     partials[2 * blockIdx.x] = rz;
     partials[2 * blockIdx.x + 1] = rr;
@@ -898,14 +951,14 @@ __global__ void __launch_bounds__(kSpmvBlock)
     pq = p[i] * y;
     pr = p[i] * r[i];
   }
-  const double dpq = block_sum<kSpmvBlock>((double)pq, sh);
-  const double dpr = block_sum<kSpmvBlock>((double)pr, sh);
+  const double dpq = block_sum_f<kSpmvBlock>(pq, sh);
+  const double dpr = block_sum_f<kSpmvBlock>(pr, sh);
   if (threadIdx.x == 0) {
-    partials[2 * blockIdx.x] = dpq;
-    partials[2 * blockIdx.x + 1] = dpr;
+    partials[2 * block_linear()] = dpq;
+    partials[2 * block_linear() + 1] = dpr;
   }
   double tot[2];
-  if (last_block_reduce<kSpmvBlock, 2>(&S->ticket[0], partials, gridDim.x, tot, sh) &&
+  if (last_block_reduce<kSpmvBlock, 2>(&S->ticket[0], partials, grid_blocks(), tot, sh) &&
       threadIdx.x == 0) {
     S->pq = tot[0];
     S->alpha = tot[0] != 0.0 ? tot[1] / tot[0] : 0.0;
@@ -955,7 +1008,7 @@ template <typename T, class Op>
 static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* x, T* r, T* p,
                    T* q, int check_every, SolverWork& w) {
   const int64_t n = A->nrows;
-  const unsigned gs = op.blocks(n);
+  const dim3 gs = op.grid(n);
   // FP32 vectors with 16-byte aligned bases take the 4-wide update kernels, with a grid of
   // up to 8 blocks per SM (enough bytes in flight to stream at HBM rate)
   bool vec4 = false;
@@ -1320,7 +1373,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   auto spmv = [&]() {
     timer_begin(ctx, GFE_KT_SPMV32);
     if (lattice)
-      k_fcg_spmv<LatticeQ1Op><<<lop.blocks(n), kSpmvBlock, 0, ctx->stream>>>(
+      k_fcg_spmv<LatticeQ1Op><<<lop.grid(n), kSpmvBlock, 0, ctx->stream>>>(
           n, lop, p32, q32, r32, w.partials, w.S);
     else if (A->dia_valid)
       k_fcg_spmv<DiaOp<float>><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, dop, p32, q32, r32,

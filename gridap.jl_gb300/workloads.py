@@ -121,3 +121,15 @@ def elasticity_3d(n: int = 48, seed: int = 3):
     lame = np.exp(rng.standard_normal((model.num_cells(), 2)))
     lame /= lame.mean(axis=0)
     return model, V, Measure(Triangulation(model), 4), lame, np.array([0.0, 0.0, -1.0])
+
+
+def jittered_q2_3d(n: int = 64, seed: int = 2, amplitude: float = 0.2):
+    """3-D Poisson on (0,1)^3 with n^3 hexahedra whose interior nodes are moved by a seeded
+    uniform jitter in (-amplitude h, amplitude h)^3, Lagrangian Q2 with homogeneous Dirichlet
+    data on the boundary, kappa = 1, f = 1, quadrature degree 4. Returns (model, V, measure)."""
+    nn = (n + 1) ** 3
+    rng = np.random.default_rng(seed)
+    jit = rng.uniform(-amplitude, amplitude, (nn, 3)) / n
+    model = CartesianDiscreteModel((0, 1, 0, 1, 0, 1), (n, n, n), node_jitter=jit)
+    V = FESpace(model, ReferenceFE(lagrangian, float, 2), dirichlet_tags="boundary")
+    return model, V, Measure(Triangulation(model), 4)

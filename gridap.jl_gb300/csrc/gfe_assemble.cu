@@ -51,11 +51,12 @@ struct CartesianDiffusionQ1 {
     if (coef_kind == GFE_COEF_CONST) return __ldg(coef);
     return 1.0;
   }
-  __device__ __forceinline__ double m(const double* s, int64_t cell, int li, int lj, int) const {
+  __device__ __forceinline__ double cell(int64_t c) const { return kappa(c); }
+  __device__ __forceinline__ double m(const double* s, double kap, int li, int lj, int) const {
     const double k = s[li + lj * NV];
     if (coef_kind == GFE_COEF_ONE) return k;
-    if (FP32) return (double)((float)kappa(cell) * (float)k);
-    return kappa(cell) * k;
+    if (FP32) return (double)((float)kap * (float)k);
+    return kap * k;
   }
   __device__ __forceinline__ int64_t node(int64_t cell, int a) const {
     if (cell_nodes) return (int64_t)__ldg(cell_nodes + cell * NV + a) - 1;

@@ -56,15 +56,23 @@ struct CartesianElasticityP2 {
   const double* coef;
   const double* f;  // body force (3 values) or null
   int ntab;
-  __device__ void load_tables(double*) const {}
-  __device__ __forceinline__ double m(const double*, int64_t cell, int li, int lj, int) const {
-    const int e = (int)(cell % 6) * 900 + li + lj * 30;
+  struct Cell {
+    int t;  // local tet 0..5 of its hexahedron
     double lam, mu;
-    lame_of(coef_kind, coef, cell, lam, mu);
+  };
+  __device__ void load_tables(double*) const {}
+  __device__ __forceinline__ Cell cell(int64_t c) const {
+    Cell k;
+    k.t = (int)(c % 6);
+    lame_of(coef_kind, coef, c, k.lam, k.mu);
+    return k;
+  }
+  __device__ __forceinline__ double m(const double*, const Cell& k, int li, int lj, int) const {
+    const int e = k.t * 900 + li + lj * 30;
     if (FP32)
-      return (double)fmaf((float)lam, (float)__ldg(tables + e),
-                          (float)mu * (float)__ldg(tables + 5400 + e));
-    return fma(lam, __ldg(tables + e), mu * __ldg(tables + 5400 + e));
+      return (double)fmaf((float)k.lam, (float)__ldg(tables + e),
+                          (float)k.mu * (float)__ldg(tables + 5400 + e));
+    return fma(k.lam, __ldg(tables + e), k.mu * __ldg(tables + 5400 + e));
   }
   __device__ __forceinline__ double v(const double*, int64_t cell, int li) const {
     if (!f) return 0.0;

@@ -37,6 +37,7 @@ struct StoredCellsF32 {
   int64_t cs, es, vcs, ves;
   int ntab;
   __device__ void load_tables(double*) const {}
+  __device__ __forceinline__ int64_t cell(int64_t c) const { return c; }
   __device__ __forceinline__ double m(const double*, int64_t cell, int li, int lj, int nd) const {
     return (double)__ldg(mat + cell * cs + (int64_t)(li + lj * nd) * es);
   }
@@ -53,6 +54,7 @@ struct StoredCells {
   int64_t vcs, ves;  // same for vec
   int ntab;          // no tables
   __device__ void load_tables(double*) const {}
+  __device__ __forceinline__ int64_t cell(int64_t c) const { return c; }
   __device__ __forceinline__ double m(const double*, int64_t cell, int li, int lj, int nd) const {
     return __ldg(mat + cell * cs + (int64_t)(li + lj * nd) * es);
   }
@@ -95,6 +97,7 @@ __global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
       const int64_t cell = e / a.nd;
       const int li = e - (int)(cell * a.nd);
       if (a.val) {
+        const auto cc = src.cell(cell);  // per-cell data (coefficients) loaded once per ref
         const PosT* pp = refpos + q * a.nd;
         for (int lj = 0; lj < a.nd; ++lj) {
           const PosT p = __ldg(pp + lj);
@@ -103,7 +106,7 @@ __global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
             raise_err(a.err, GFE_ERR_INVALID_ARGUMENT, r);
             continue;
           }
-          acc[p * R + t] += src.m(tab, cell, li, lj, a.nd);
+          acc[p * R + t] += src.m(tab, cc, li, lj, a.nd);
         }
       }
       if (a.b) bacc += src.v(tab, cell, li);
@@ -169,8 +172,85 @@ static int max_row_width(gfe_ctx* ctx, gfe_matrix* A, int* out) {
   return GFE_OK;
 }
 
+// Warp-per-row variant for elements with many dofs per cell (nd >= 16: Q2, P2, vector
+// spaces). A warp owns one row; its lanes take the local columns of one reference at a time
+// (lane lj, then lj + 32, ...), so the references -- and hence the additions into every
+// stored value -- are still processed in ascending cell order, exactly as in the
+// thread-per-row kernel. Distinct local columns of one cell land on distinct positions, so
+// the lanes of a step never collide. Each warp keeps its row in MAXW doubles of shared
+// memory; 8 warps per block.
+constexpr int kRowWarps = 8;
+
+template <int MAXW, class Src, typename PosT>
+__global__ void __launch_bounds__(32 * kRowWarps)
+    k_assemble_rows_warp(RowArgs a, Src src) {
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double* acc = smem + wib * MAXW;
+  double* tab = smem + kRowWarps * MAXW;
+  src.load_tables(tab);
+  __syncthreads();
+  const int64_t r = (int64_t)blockIdx.x * kRowWarps + wib;
+  if (r >= a.nrows) return;
+  int32_t start = 0, n = 0;
+  if (a.val) {
+    start = a.rowptr[r];
+    n = a.rowptr[r + 1] - start;
+    for (int k = lane; k < n; k += 32) acc[k] = 0.0;
+    __syncwarp();
+  }
+  const PosT* refpos = static_cast<const PosT*>(a.refpos);
+  double bacc = 0.0;
+  for (int64_t q = a.ref_ptr[r]; q < a.ref_ptr[r + 1]; ++q) {
+    const int32_t e = a.refs[q];
+    const int64_t cell = e / a.nd;
+    const int li = e - (int)(cell * a.nd);
+    if (a.val) {
+      const auto cc = src.cell(cell);
+      for (int lj = lane; lj < a.nd; lj += 32) {
+        const PosT pp = __ldg(refpos + q * a.nd + lj);
+        if (pp == (PosT)~(PosT)0) continue;  // Dirichlet column
+        if (pp >= n) {
+          raise_err(a.err, GFE_ERR_INVALID_ARGUMENT, r);
+          continue;
+        }
+        acc[pp] += src.m(tab, cc, li, lj, a.nd);
+      }
+      __syncwarp();
+    }
+    if (a.b && lane == 0) bacc += src.v(tab, cell, li);
+  }
+  if (a.b && lane == 0) a.b[r] = bacc;
+  if (!a.val) return;
+  double* out = a.val + start;
+  for (int k = lane; k < n; k += 32) out[k] = acc[k];
+}
+
+template <int MAXW, class Src>
+static int launch_rows_warp(gfe_ctx* ctx, const RowArgs& a, const Src& src, int pos_bytes) {
+  const size_t smem = sizeof(double) * ((size_t)MAXW * kRowWarps + (size_t)src.ntab);
+  auto kern = pos_bytes == 1 ? k_assemble_rows_warp<MAXW, Src, uint8_t>
+                             : k_assemble_rows_warp<MAXW, Src, uint16_t>;
+  if (smem > 48 * 1024)
+    GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  timer_begin(ctx, GFE_KT_ASSEMBLE);
+  kern<<<grid_for(a.nrows, kRowWarps), 32 * kRowWarps, smem, ctx->stream>>>(a, src);
+  timer_end(ctx);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
 template <class Src>
 static int run_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src, int maxw, int pb) {
+  if (a.nd >= 16 && a.val) {
+    if (maxw <= 128) return launch_rows_warp<128>(ctx, a, src, pb);
+    if (maxw <= 256) return launch_rows_warp<256>(ctx, a, src, pb);
+    if (maxw <= 512) return launch_rows_warp<512>(ctx, a, src, pb);
+    if (maxw <= 1024) return launch_rows_warp<1024>(ctx, a, src, pb);
+    return set_error(GFE_ERR_ROW_TOO_WIDE, "assembly: row width %d exceeds 1024", maxw);
+  }
   if (maxw <= 16) return launch_rows<16, 128>(ctx, a, src, pb);
   if (maxw <= 32) return launch_rows<32, 128>(ctx, a, src, pb);
   if (maxw <= 64) return launch_rows<64, 128>(ctx, a, src, pb);

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 
 #include "gfe_internal.h"
 
@@ -427,66 +428,26 @@ struct DiaOp {
 // = interior nodes in node order (the CLagrangian numbering with every boundary node
 // Dirichlet): (A x)_r = sum over the 8 cells K around node r of kappa_K sum_c Kref[l_r, c]
 // x[node(K, c)], boundary nodes contributing 0 -- the cell-wise sum the assembled matrix
-// stores, applied with FP32 element matrices (kappa_K Kref). Reads kappa (4 B per cell) and
-// x instead of 27 values per row. Threads cover 32 x 8 tiles of one k-plane, so the x
-// neighbours along i and j are shared through L1.
+// stores, applied with FP32 element matrices (kappa_K Kref). It reads kappa (4 B per cell)
+// and x instead of 27 values per row. Applied by k_lattice_spmv: a block covers a 32 x 8 tile
+// of (i, j) and kLatK consecutive k-planes; each thread marches up its k-column keeping the
+// three x-planes and two kappa-planes around its node in registers, so a row costs 9 x and 4
+// kappa loads.
+constexpr int kLatK = 4;
+
 struct LatticeQ1Op {
   const float* kap;
   int n0, n1, n2;   // cells per direction
   int s1, s2;       // row strides of j and k: m0 and m0*m1 (m = n - 1 interior nodes)
   int c1, c2;       // cell strides of j and k: n0 and n0*n1
   float K[64];      // Kref[li + 8 lj], symmetric
-  // grid: x = 32-wide tiles along i, y = 8-wide tiles along j, z = k
   dim3 grid(int64_t) const {
-    return dim3((unsigned)((n0 - 1 + 31) / 32), (unsigned)((n1 - 1 + 7) / 8), (unsigned)(n2 - 1));
+    return dim3((unsigned)((n0 - 1 + 31) / 32), (unsigned)((n1 - 1 + 7) / 8),
+                (unsigned)((n2 - 1 + kLatK - 1) / kLatK));
   }
   unsigned blocks(int64_t n) const {
     const dim3 g = grid(n);
     return g.x * g.y * g.z;
-  }
-  __device__ __forceinline__ int ti() const { return (int)(blockIdx.x * 32 + (threadIdx.x & 31)); }
-  __device__ __forceinline__ int tj() const { return (int)(blockIdx.y * 8 + (threadIdx.x >> 5)); }
-  __device__ __forceinline__ int64_t row_index() const {
-    const int i = ti(), j = tj(), k = (int)blockIdx.z;
-    if (i >= n0 - 1 || j >= n1 - 1) return -1;
-    return (int64_t)i + (int64_t)s1 * j + (int64_t)s2 * k;
-  }
-  // Valid only for r == row_index() of the calling thread: the node comes from the thread.
-  __device__ __forceinline__ float row(int64_t r, const float* __restrict__ x) const {
-    const int i = ti(), j = tj(), k = (int)blockIdx.z;
-    const bool ok[3][3] = {{i > 0, true, i < n0 - 2}, {j > 0, true, j < n1 - 2},
-                           {k > 0, true, k < n2 - 2}};
-    const float* xr = x + r;
-    // x at the 27 nodes around (i, j, k) (interior coordinates); outside the interior = 0
-    float xs[27];
-#pragma unroll
-    for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-      for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-        for (int dx = -1; dx <= 1; ++dx)
-          xs[(dx + 1) + 3 * ((dy + 1) + 3 * (dz + 1))] =
-              (ok[0][dx + 1] && ok[1][dy + 1] && ok[2][dz + 1]) ? __ldg(xr + dx + s1 * dy + s2 * dz)
-                                                               : 0.f;
-    // cell (i + cx, j + cy, k + cz) in cell coordinates; the node is its local corner lr
-    const float* kp = kap + ((int64_t)i + (int64_t)c1 * j + (int64_t)c2 * k);
-    float acc = 0.f;
-#pragma unroll
-    for (int cz = 0; cz < 2; ++cz)
-#pragma unroll
-      for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-        for (int cx = 0; cx < 2; ++cx) {
-          const float kc = __ldg(kp + cx + c1 * cy + c2 * cz);
-          const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
-          float s = 0.f;
-#pragma unroll
-          for (int lc = 0; lc < 8; ++lc)
-            s = fmaf(K[lr + 8 * lc],
-                     xs[(cx + (lc & 1)) + 3 * ((cy + ((lc >> 1) & 1)) + 3 * (cz + (lc >> 2)))], s);
-          acc = fmaf(kc, s, acc);
-        }
-    return acc;
   }
 };
 
@@ -507,6 +468,112 @@ int spmv64(gfe_ctx* ctx, gfe_matrix* A, const double* d_x, double* d_y) {
   ctx->launches++;
   GFE_CUDA_TRY(cudaGetLastError());
   return GFE_OK;
+}
+
+// q = A p with the lattice operator; partial p.q (and p.r for flexible CG), last-block alpha.
+template <bool FCG>
+__global__ void __launch_bounds__(kSpmvBlock)
+    k_lattice_spmv(LatticeQ1Op op, const float* __restrict__ p, float* __restrict__ q,
+                   const float* __restrict__ rr, double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kSpmvBlock / 32];
+  if (S->done) return;
+  const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
+  const int i = (int)(blockIdx.x * 32 + (threadIdx.x & 31));
+  const int j = (int)(blockIdx.y * 8 + (threadIdx.x >> 5));
+  const int k0 = (int)blockIdx.z * kLatK;
+  float d1 = 0.f, d2 = 0.f;
+  if (i < m0 && j < m1) {
+    const bool okx[3] = {i > 0, true, i < m0 - 1};
+    const bool oky[3] = {j > 0, true, j < m1 - 1};
+    const int64_t col = (int64_t)i + (int64_t)op.s1 * j;  // row of (i, j, 0)
+    const float* kcol = op.kap + ((int64_t)i + (int64_t)op.c1 * j);
+    // x-plane kk (9 values around (i, j)); 0 outside the interior
+    auto xplane = [&](int kk, float* v) {
+      const bool okz = kk >= 0 && kk < m2;
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          float t = 0.f;
+          if (okz && okx[dx + 1] && oky[dy + 1])
+            t = __ldg(p + col + (int64_t)op.s2 * kk + dx + op.s1 * dy);
+          v[(dx + 1) + 3 * (dy + 1)] = t;
+        }
+    };
+    // kappa-plane of cell layer kk: cells (i + cx, j + cy, kk)
+    auto kplane = [&](int kk, float* v) {
+#pragma unroll
+      for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+        for (int cx = 0; cx < 2; ++cx)
+          v[cx + 2 * cy] = __ldg(kcol + (int64_t)op.c2 * kk + cx + op.c1 * cy);
+    };
+    float xa[9], xb[9], xc[9], ka[4], kb[4];
+    xplane(k0 - 1, xa);
+    xplane(k0, xb);
+    kplane(k0, ka);
+#pragma unroll
+    for (int t = 0; t < kLatK; ++t) {
+      const int k = k0 + t;
+      if (k < m2) {
+        xplane(k + 1, xc);
+        kplane(k + 1, kb);
+        float acc = 0.f;
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+          for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+            for (int cx = 0; cx < 2; ++cx) {
+              const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
+              float s = 0.f;
+#pragma unroll
+              for (int lc = 0; lc < 8; ++lc) {
+                const int ix = cx + (lc & 1), iy = cy + ((lc >> 1) & 1), iz = cz + (lc >> 2);
+                const float xv = iz == 0 ? xa[ix + 3 * iy] : iz == 1 ? xb[ix + 3 * iy]
+                                                                     : xc[ix + 3 * iy];
+                s = fmaf(op.K[lr + 8 * lc], xv, s);
+              }
+              acc = fmaf(cz == 0 ? ka[cx + 2 * cy] : kb[cx + 2 * cy], s, acc);
+            }
+        const int64_t row = col + (int64_t)op.s2 * k;
+        q[row] = acc;
+        d1 = fmaf(xb[4], acc, d1);
+        if (FCG) d2 = fmaf(xb[4], __ldg(rr + row), d2);
+      }
+#pragma unroll
+      for (int e = 0; e < 9; ++e) {
+        xa[e] = xb[e];
+        xb[e] = xc[e];
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) ka[e] = kb[e];
+    }
+  }
+  const double s1 = block_sum_f<kSpmvBlock>(d1, sh);
+  double s2 = 0.0;
+  if (FCG) s2 = block_sum_f<kSpmvBlock>(d2, sh);
+  const unsigned bl = block_linear();
+  if (threadIdx.x == 0) {
+    if (FCG) {
+      partials[2 * bl] = s1;
+      partials[2 * bl + 1] = s2;
+    } else {
+      partials[bl] = s1;
+    }
+  }
+  double tot[2];
+  if (FCG) {
+    if (last_block_reduce<kSpmvBlock, 2>(&S->ticket[0], partials, grid_blocks(), tot, sh) &&
+        threadIdx.x == 0) {
+      S->pq = tot[0];
+      S->alpha = tot[0] != 0.0 ? tot[1] / tot[0] : 0.0;
+    }
+  } else if (last_block_reduce<kSpmvBlock, 1>(&S->ticket[0], partials, grid_blocks(), tot, sh) &&
+             threadIdx.x == 0) {
+    S->pq = tot[0];
+    S->alpha = tot[0] != 0.0 ? S->rz / tot[0] : 0.0;
+  }
 }
 
 static LatticeQ1Op lattice_op(const gfe_matrix* A) {
@@ -1009,8 +1076,9 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
                    T* q, int check_every, SolverWork& w) {
   const int64_t n = A->nrows;
   const dim3 gs = op.grid(n);
-  // FP32 vectors with 16-byte aligned bases take the 4-wide update kernels, with a grid of
-  // up to 8 blocks per SM (enough bytes in flight to stream at HBM rate)
+  // FP32 vectors with 16-byte aligned bases take the 4-wide update kernels. Two blocks per SM
+  // with two 16-byte groups in flight per thread keep enough bytes in flight to stream at
+  // HBM rate, while the per-block reduction cost (barriers, fence, ticket) stays small.
   bool vec4 = false;
   if constexpr (sizeof(T) == 4) {
     vec4 = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(r) |
@@ -1018,12 +1086,19 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
              reinterpret_cast<uintptr_t>(dinv)) & 15) == 0;
   }
   const unsigned gv = vec4 ? (unsigned)std::max<int64_t>(
-                                 1, std::min<int64_t>((n + 1023) / 1024, ctx->num_sms * 8))
+                                 1, std::min<int64_t>((n + 1023) / 1024, ctx->num_sms * 2))
                            : (unsigned)(ctx->num_sms * 4);
   // Without kernel timing a chunk of iterations is captured once into a CUDA graph (cached in
   // the context while its launch parameters match) and replayed. With timing on, every
   // iteration is launched directly with CUDA events around the SpMV; launches after the
   // converged iteration (they return at once) are dropped from the timing.
+  auto launch_spmv = [&]() {
+    if constexpr (std::is_same<Op, LatticeQ1Op>::value)
+      k_lattice_spmv<false><<<gs, kSpmvBlock, 0, ctx->stream>>>(op, p, q, nullptr, w.partials,
+                                                                w.S);
+    else
+      k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
+  };
   auto launch_vec = [&](unsigned g) {
     if constexpr (sizeof(T) == 4) {
       if (vec4) {
@@ -1062,7 +1137,7 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
       cudaGraph_t graph = nullptr;
       GFE_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
       for (int k = 0; k < check_every; ++k) {
-        k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
+        launch_spmv();
         launch_vec(gv);
       }
       const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
@@ -1093,7 +1168,7 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
     } else {
       for (int k = 0; k < check_every; ++k) {
         timer_begin(ctx, kind);
-        k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
+        launch_spmv();
         timer_end(ctx);
         timer_begin(ctx, GFE_KT_VECTOR);
         launch_vec(gv);
@@ -1373,8 +1448,8 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   auto spmv = [&]() {
     timer_begin(ctx, GFE_KT_SPMV32);
     if (lattice)
-      k_fcg_spmv<LatticeQ1Op><<<lop.grid(n), kSpmvBlock, 0, ctx->stream>>>(
-          n, lop, p32, q32, r32, w.partials, w.S);
+      k_lattice_spmv<true><<<lop.grid(n), kSpmvBlock, 0, ctx->stream>>>(lop, p32, q32, r32,
+                                                                      w.partials, w.S);
     else if (A->dia_valid)
       k_fcg_spmv<DiaOp<float>><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, dop, p32, q32, r32,
                                                                   w.partials, w.S);

@@ -114,3 +114,26 @@ def test_p2_elasticity_vector_only(gg, orc):
     dO = gg.Measure(gg.Triangulation(m), 4)
     b = gg.assemble_vector(lambda v: gg.integrate(gg.inner((0.0, 0.0, -1.0), v), dO), V)
     assert np.abs(b - ref["b"]).max() <= TOL_VAL * np.abs(ref["b"]).max()
+
+
+def test_generic_numeric_loop_bit_exact_wide_cells(gg, orc):
+    """Caller cell matrices with 30 dofs per cell (the warp-per-row gather) give exactly the
+    oracle's InserterCSC sums: the same additions in the same cell order."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(94)
+    part = (3, 3, 2)
+    m, V = _space(gg, part)
+    lame = np.exp(rng.standard_normal((m.num_cells(), 2)))
+    ref = orc.elasticity_p2((0, 1) * 3, part, lame)
+    cm = ref["cellmats"] * (1 + 1e-3 * rng.standard_normal(ref["cellmats"].shape))
+    ids = ref["cell_dofs"]
+    n = ref["nfree"]
+    csc = orc.assemble_csc(ids, ids, cm, n, n)
+    assem = gg.SparseMatrixAssembler(V, V)
+    A = gg.symbolic_loop_matrix(assem, (None, ids, ids))
+    gg.numeric_loop_matrix(A, assem, (cm, ids, ids))
+    S = sp.csc_matrix((csc[2], csc[1] - 1, csc[0] - 1), shape=(n, n)).tocsr()
+    S.sort_indices()
+    rp, col, nz = A.export_csr(0)
+    assert np.array_equal(rp, S.indptr) and np.array_equal(col, S.indices)
+    assert np.array_equal(nz, S.data)

@@ -46,6 +46,21 @@ def dist_env():
     return rank, world, local
 
 
+def replica_step_ms(ms: float, device) -> float:
+    """Step time of a replicas-only run: every rank solves its own problem, the slowest rank
+    sets the time (max over ranks). No other data crosses ranks."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(nfree_per_rank: int, world: int, step_ms: float) -> float:
+    """Whole-job DOF/s: all ranks' free dofs over the max-over-ranks step time."""
+    return world * nfree_per_rank / (step_ms * 1e-3)
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -215,10 +230,7 @@ def run_gpu(args):
         ctx.set_timing(False)
         ms = e0.elapsed_time(e1) / steps
         if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([ms], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+            ms = replica_step_ms(ms, dev)
         return dict(ms=ms, wall_ms=1e3 * wall / steps, reps=reps, kt=kt,
                     launches=ctx.kernel_launches() - l0)
 
@@ -305,9 +317,9 @@ def run_gpu(args):
     for rp in r_mixed["reps"] + r_plain["reps"] + r_e2e["reps"]:
         if not rp.relres <= w.rtol * (1 + 1e-6):
             raise RuntimeError(f"solve did not reach rtol: relres={rp.relres}")
-    value = world * nfree / (r_mixed["ms"] * 1e-3)
-    plain_value = world * nfree / (r_plain["ms"] * 1e-3)
-    e2e_value = world * nfree / (r_e2e["ms"] * 1e-3)
+    value = replica_value(nfree, world, r_mixed["ms"])
+    plain_value = replica_value(nfree, world, r_plain["ms"])
+    e2e_value = replica_value(nfree, world, r_e2e["ms"])
     h2d = ids_h.nbytes + w.kappa.nbytes + w.source.values.nbytes
     d2h = nfree * 8
     peak, peak_kind = peaks()

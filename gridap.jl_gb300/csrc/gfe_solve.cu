@@ -440,7 +440,13 @@ struct LatticeQ1Op {
   int n0, n1, n2;   // cells per direction
   int s1, s2;       // row strides of j and k: m0 and m0*m1 (m = n - 1 interior nodes)
   int c1, c2;       // cell strides of j and k: n0 and n0*n1
+  int p1, p2;       // strides of the zero-halo padded layout: m0 + 2 and (m0 + 2)(m1 + 2)
   float K[64];      // Kref[li + 8 lj], symmetric
+  // padded index of interior node (i, j, k): halo of one zero entry on every side
+  __host__ __device__ int64_t pad_index(int i, int j, int k) const {
+    return (int64_t)(i + 1) + (int64_t)p1 * (j + 1) + (int64_t)p2 * (k + 1);
+  }
+  int64_t padded_size() const { return (int64_t)p2 * (n2 + 1); }
   dim3 grid(int64_t) const {
     return dim3((unsigned)((n0 - 1 + 31) / 32), (unsigned)((n1 - 1 + 7) / 8),
                 (unsigned)((n2 - 1 + kLatK - 1) / kLatK));
@@ -471,7 +477,10 @@ int spmv64(gfe_ctx* ctx, gfe_matrix* A, const double* d_x, double* d_y) {
 }
 
 // q = A p with the lattice operator; partial p.q (and p.r for flexible CG), last-block alpha.
-template <bool FCG>
+// PAD: p, q (and r) in the zero-halo padded layout (LatticeQ1Op::pad_index): every
+// neighbour load is unconditional and q is written at the padded index. Otherwise the rows
+// are the dof numbering and neighbours outside the interior read as 0.
+template <bool FCG, bool PAD>
 __global__ void __launch_bounds__(kSpmvBlock)
     k_lattice_spmv(LatticeQ1Op op, const float* __restrict__ p, float* __restrict__ q,
                    const float* __restrict__ rr, double* __restrict__ partials, SolverState* S) {
@@ -485,18 +494,20 @@ __global__ void __launch_bounds__(kSpmvBlock)
   if (i < m0 && j < m1) {
     const bool okx[3] = {i > 0, true, i < m0 - 1};
     const bool oky[3] = {j > 0, true, j < m1 - 1};
-    const int64_t col = (int64_t)i + (int64_t)op.s1 * j;  // row of (i, j, 0)
+    // row (or padded index) of (i, j, 0) and the strides between neighbours
+    const int64_t col = PAD ? op.pad_index(i, j, 0) : (int64_t)i + (int64_t)op.s1 * j;
+    const int sy = PAD ? op.p1 : op.s1, sz = PAD ? op.p2 : op.s2;
     const float* kcol = op.kap + ((int64_t)i + (int64_t)op.c1 * j);
     // x-plane kk (9 values around (i, j)); 0 outside the interior
     auto xplane = [&](int kk, float* v) {
-      const bool okz = kk >= 0 && kk < m2;
+      const bool okz = PAD || (kk >= 0 && kk < m2);
 #pragma unroll
       for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
         for (int dx = -1; dx <= 1; ++dx) {
           float t = 0.f;
-          if (okz && okx[dx + 1] && oky[dy + 1])
-            t = __ldg(p + col + (int64_t)op.s2 * kk + dx + op.s1 * dy);
+          if (PAD || (okz && okx[dx + 1] && oky[dy + 1]))
+            t = __ldg(p + col + (int64_t)sz * kk + dx + sy * dy);
           v[(dx + 1) + 3 * (dy + 1)] = t;
         }
     };
@@ -536,7 +547,7 @@ __global__ void __launch_bounds__(kSpmvBlock)
               }
               acc = fmaf(cz == 0 ? ka[cx + 2 * cy] : kb[cx + 2 * cy], s, acc);
             }
-        const int64_t row = col + (int64_t)op.s2 * k;
+        const int64_t row = col + (int64_t)sz * k;
         q[row] = acc;
         d1 = fmaf(xb[4], acc, d1);
         if (FCG) d2 = fmaf(xb[4], __ldg(rr + row), d2);
@@ -586,8 +597,74 @@ static LatticeQ1Op lattice_op(const gfe_matrix* A) {
   op.s2 = (op.n0 - 1) * (op.n1 - 1);
   op.c1 = op.n0;
   op.c2 = op.n0 * op.n1;
+  op.p1 = op.n0 + 1;
+  op.p2 = (op.n0 + 1) * (op.n1 + 1);
   for (int e = 0; e < 64; ++e) op.K[e] = A->mf_K[e];
   return op;
+}
+
+// ---- dof layout <-> zero-halo padded lattice layout (mixed CG with the lattice operator) ----
+__device__ __forceinline__ int64_t dof_to_pad(const LatticeQ1Op& op, int64_t r) {
+  const unsigned m0 = (unsigned)(op.n0 - 1), m1 = (unsigned)(op.n1 - 1);
+  const unsigned ru = (unsigned)r;
+  const unsigned i = ru % m0, t = ru / m0;
+  return op.pad_index((int)i, (int)(t % m1), (int)(t / m1));
+}
+
+// out[pad(r)] = in[r] (FP32), halo untouched (zero)
+__global__ void k_to_pad(LatticeQ1Op op, int64_t n, const float* __restrict__ in,
+                         float* __restrict__ out) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x)
+    out[dof_to_pad(op, r)] = in[r];
+}
+
+// CG start from x = 0 in the padded layout: r = rhs, p = D r; partials of r.z, r.r
+__global__ void __launch_bounds__(kVecBlock)
+    k_cg_init_pad(LatticeQ1Op op, int64_t n, const double* __restrict__ rhs,
+                  float* __restrict__ r, float* __restrict__ p, const float* __restrict__ dinv,
+                  double* __restrict__ partials, SolverState* S, double rtol2) {
+  __shared__ double sh[kVecBlock / 32];
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = dof_to_pad(op, i);
+    const float ri = (float)rhs[i];
+    r[j] = ri;
+    const float zi = dinv[j] * ri;
+    p[j] = zi;
+    rz += (double)ri * (double)zi;
+    rr += (double)ri * (double)ri;
+  }
+  rz = block_sum<kVecBlock>(rz, sh);
+  rr = block_sum<kVecBlock>(rr, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = rz;
+    partials[2 * blockIdx.x + 1] = rr;
+  }
+  double tot[2];
+  if (last_block_reduce<kVecBlock, 2>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->rz = tot[0];
+    S->rr = tot[1];
+    S->bb = tot[1];
+    S->tol2 = rtol2 * tot[1];
+    S->iter = 0;
+    S->converged = 0;
+    S->done = (tot[1] == 0.0) ? 1 : 0;
+    if (tot[1] == 0.0) S->converged = 1;
+  }
+}
+
+// x64 += x32 (padded), x32 = 0
+__global__ void k_merge_pad(LatticeQ1Op op, int64_t n, double* __restrict__ x64,
+                            float* __restrict__ x32) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = dof_to_pad(op, i);
+    x64[i] += (double)x32[j];
+    x32[j] = 0.f;
+  }
 }
 
 // ---- CG kernels (T: vector/matrix type; dot products accumulate in double) ----------------
@@ -909,6 +986,50 @@ __global__ void __launch_bounds__(kVecBlock)
   }
 }
 
+// k_restart32 for the padded layout: r32[pad(i)] = r64[i], dots r.Dr and r.p over the rows
+__global__ void __launch_bounds__(kVecBlock)
+    k_restart32_pad(LatticeQ1Op op, int64_t n, const double* __restrict__ r64,
+                    float* __restrict__ r32, const float* __restrict__ p,
+                    const float* __restrict__ dinv, double* __restrict__ partials,
+                    SolverState* S) {
+  __shared__ double sh[kVecBlock / 32];
+  if (S->rr64 <= S->tol2) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      S->converged = 1;
+      S->done = 1;
+      S->need_update = 0;
+    }
+    return;
+  }
+  double rz = 0.0, rp = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = dof_to_pad(op, i);
+    const float ri = (float)r64[i];
+    r32[j] = ri;
+    rz += (double)ri * (double)(dinv[j] * ri);
+    rp += (double)ri * (double)p[j];
+  }
+  rz = block_sum<kVecBlock>(rz, sh);
+  rp = block_sum<kVecBlock>(rp, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = rz;
+    partials[2 * blockIdx.x + 1] = rp;
+  }
+  double tot[2];
+  if (last_block_reduce<kVecBlock, 2>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->alpha = tot[0] != 0.0 ? tot[1] / tot[0] : 0.0;  // c (reused field)
+    S->beta = S->rz_prev != 0.0 ? tot[0] / S->rz_prev : 0.0;
+    S->rz = tot[0];
+    S->rmax2 = S->rr64;
+    S->rr = S->rr64;
+    S->need_update = 0;
+    S->converged = 0;
+    S->done = (S->iter >= S->maxit || !isfinite(tot[0])) ? 1 : 0;
+  }
+}
+
 // p = beta (p - c z) + z with z = D r (c in S->alpha)
 __global__ void k_restart_dir(int64_t n, float* __restrict__ p, const float* __restrict__ r,
                               const float* __restrict__ dinv, const SolverState* S) {
@@ -1073,11 +1194,12 @@ static int read_state(gfe_ctx* ctx, SolverWork& w, bool flush = true) {
 // Launches chunks of CG iterations until the device sets `done`.
 template <typename T, class Op>
 static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* x, T* r, T* p,
-                   T* q, int check_every, SolverWork& w) {
-  const int64_t n = A->nrows;
+                   T* q, int check_every, SolverWork& w, int64_t nvec = -1) {
+  // n: length of the vectors (the rows, or the padded lattice size)
+  const int64_t n = nvec >= 0 ? nvec : A->nrows;
   const dim3 gs = op.grid(n);
-  // FP32 vectors with 16-byte aligned bases take the 4-wide update kernels. Two blocks per SM
-  // with two 16-byte groups in flight per thread keep enough bytes in flight to stream at
+  // FP32 vectors with 16-byte aligned bases take the 4-wide update kernels. Four blocks per
+  // SM with two 16-byte groups in flight per thread keep enough bytes in flight to stream at
   // HBM rate, while the per-block reduction cost (barriers, fence, ticket) stays small.
   bool vec4 = false;
   if constexpr (sizeof(T) == 4) {
@@ -1086,7 +1208,7 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
              reinterpret_cast<uintptr_t>(dinv)) & 15) == 0;
   }
   const unsigned gv = vec4 ? (unsigned)std::max<int64_t>(
-                                 1, std::min<int64_t>((n + 1023) / 1024, ctx->num_sms * 2))
+                                 1, std::min<int64_t>((n + 1023) / 1024, ctx->num_sms * 4))
                            : (unsigned)(ctx->num_sms * 4);
   // Without kernel timing a chunk of iterations is captured once into a CUDA graph (cached in
   // the context while its launch parameters match) and replayed. With timing on, every
@@ -1094,8 +1216,8 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
   // converged iteration (they return at once) are dropped from the timing.
   auto launch_spmv = [&]() {
     if constexpr (std::is_same<Op, LatticeQ1Op>::value)
-      k_lattice_spmv<false><<<gs, kSpmvBlock, 0, ctx->stream>>>(op, p, q, nullptr, w.partials,
-                                                                w.S);
+      k_lattice_spmv<false, true><<<gs, kSpmvBlock, 0, ctx->stream>>>(op, p, q, nullptr,
+                                                                      w.partials, w.S);
     else
       k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
   };
@@ -1234,6 +1356,12 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
   bool lattice = false;
   GFE_TRY(lattice_ready(ctx, A, &lattice));
   size_t nblk = grid_for(n, kSpmvBlock);
+  // mixed CG on the lattice operator keeps its FP32 vectors (and D^-1) in the zero-halo padded
+  // lattice layout, stride nlat
+  const bool pad_layout = lattice && o->method == GFE_SOLVER_MIXED_CG;
+  const int64_t nlat = pad_layout ? ((lattice_op(A).padded_size() + 63) & ~(int64_t)63) : 0;
+  if (pad_layout)
+    GFE_TRY(ctx->scratch[SCR_SOLVER2].reserve(sizeof(float) * (size_t)nlat * 5 + 256));
   if (lattice) nblk = std::max<size_t>(nblk, lattice_op(A).blocks(n));
   const size_t npart = nblk * 2 + (size_t)ctx->num_sms * 16 + 64;
   GFE_TRY(ctx->scratch[SCR_REDUCE].reserve(sizeof(SolverState) + sizeof(double) * npart + 256));
@@ -1280,11 +1408,14 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
     // true residual b - A x64 is formed in FP64 and replaces the FP32 one, and the search
     // direction is re-orthogonalised against it and continued (no restart).
     double* r64 = v64;
+    const LatticeQ1Op lop = lattice ? lattice_op(A) : LatticeQ1Op{};
+    const int64_t nv = pad_layout ? nlat : npad;  // FP32 vector stride
     float* f = (float*)ctx->scratch[SCR_SOLVER2].ptr;
     float* x32 = f;
-    float* r32 = f + npad;
-    float* p32 = f + 2 * npad;
-    float* q32 = f + 3 * npad;
+    float* r32 = f + nv;
+    float* p32 = f + 2 * nv;
+    float* q32 = f + 3 * nv;
+    const float* dinv_in = dinv32;  // D^-1 in the layout of the FP32 vectors
     const unsigned gv = (unsigned)(ctx->num_sms * 4);
     const double delta = o->inner_rtol > 0 ? o->inner_rtol : 0.1;
     GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
@@ -1292,18 +1423,36 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
     int maxit_field = maxit;
     GFE_CUDA_TRY(cudaMemcpyAsync(&w.S->maxit, &maxit_field, sizeof(int), cudaMemcpyHostToDevice,
                                  ctx->stream));
-    k_cg_init<float, double><<<gv, kVecBlock, 0, ctx->stream>>>(
-        n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
+    if (pad_layout) {
+      // zero halo (x, r, p, q, D^-1), D^-1 scattered to the padded layout
+      float* dpad = f + 4 * nv;
+      GFE_CUDA_TRY(cudaMemsetAsync(f, 0, sizeof(float) * (size_t)nv * 5, ctx->stream));
+      k_to_pad<<<gv, kVecBlock, 0, ctx->stream>>>(lop, n, dinv32, dpad);
+      k_cg_init_pad<<<gv, kVecBlock, 0, ctx->stream>>>(lop, n, d_b, r32, p32, dpad, w.partials,
+                                                       w.S, o->rtol * o->rtol);
+      dinv_in = dpad;
+      ctx->launches += 2;
+    } else {
+      k_cg_init<float, double><<<gv, kVecBlock, 0, ctx->stream>>>(
+          n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
+      ctx->launches++;
+    }
     k_set_reliable<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta);
-    ctx->launches += 2;
+    ctx->launches++;
     w.hS->iter = 0;
     int updates = 0;
     if (!lattice) GFE_TRY(build_dia(ctx, A));
+    auto merge = [&]() {
+      if (pad_layout)
+        k_merge_pad<<<gv, kVecBlock, 0, ctx->stream>>>(lop, n, d_x, x32);
+      else
+        k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
+      ctx->launches++;
+    };
     for (;;) {
-      if (lattice) {
-        const LatticeQ1Op op = lattice_op(A);
-        GFE_TRY((iterate<float, LatticeQ1Op>(ctx, A, op, dinv32, x32, r32, p32, q32,
-                                             check_every, w)));
+      if (pad_layout) {
+        GFE_TRY((iterate<float, LatticeQ1Op>(ctx, A, lop, dinv_in, x32, r32, p32, q32,
+                                             check_every, w, nv)));
       } else if (A->dia_valid) {
         DiaOp<float> op{A->dia_val32.as<float>(), n, {}};
         for (int d = 0; d < A->dia_ndiag; ++d) op.o.off[d] = A->dia_off[d];
@@ -1316,17 +1465,26 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
         GFE_TRY((iterate<float, SellOp<float>>(ctx, A, op, dinv32, x32, r32, p32, q32,
                                                check_every, w)));
       }
-      if (w.hS->iter >= maxit || !std::isfinite(w.hS->rr)) break;
+      if (w.hS->iter >= maxit || !std::isfinite(w.hS->rr)) {
+        if (std::isfinite(w.hS->rr)) merge();  // keep the FP32 correction made so far
+        break;
+      }
       // reliable update
-      k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
+      merge();
       timer_begin(ctx, GFE_KT_RESIDUAL64);
       k_residual64<<<grid_for(n, kSpmvBlock), kSpmvBlock, 0, ctx->stream>>>(
           n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(),
           d_x, d_b, r64, w.partials, &w.S->rr64, &w.S->ticket[2]);
       timer_end(ctx);
-      k_restart32<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, p32, dinv32, w.partials, w.S);
-      k_restart_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, r32, dinv32, w.S);
-      ctx->launches += 4;
+      if (pad_layout)
+        k_restart32_pad<<<gv, kVecBlock, 0, ctx->stream>>>(lop, n, r64, r32, p32, dinv_in,
+                                                           w.partials, w.S);
+      else
+        k_restart32<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, p32, dinv32, w.partials,
+                                                       w.S);
+      k_restart_dir<<<gv, kVecBlock, 0, ctx->stream>>>(pad_layout ? nv : n, p32, r32, dinv_in,
+                                                       w.S);
+      ctx->launches += 3;
       ++updates;
       GFE_CUDA_TRY(cudaGetLastError());
       GFE_TRY(read_state(ctx, w));
@@ -1448,8 +1606,8 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   auto spmv = [&]() {
     timer_begin(ctx, GFE_KT_SPMV32);
     if (lattice)
-      k_lattice_spmv<true><<<lop.grid(n), kSpmvBlock, 0, ctx->stream>>>(lop, p32, q32, r32,
-                                                                      w.partials, w.S);
+      k_lattice_spmv<true, false><<<lop.grid(n), kSpmvBlock, 0, ctx->stream>>>(
+          lop, p32, q32, r32, w.partials, w.S);
     else if (A->dia_valid)
       k_fcg_spmv<DiaOp<float>><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, dop, p32, q32, r32,
                                                                   w.partials, w.S);

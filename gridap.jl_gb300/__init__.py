@@ -12,7 +12,8 @@ The directory name is not a Python identifier; load it with `load_package()` fro
 from . import _lib
 from ._lib import GfeError
 from .assembly import (AffineFEOperator, Context, DeviceMatrix, SparseMatrixAssembler,
-                       assemble_matrix, assemble_matrix_and_vector, assemble_vector,
+                       assemble_matrix, assemble_matrix_, assemble_matrix_and_vector,
+                       assemble_matrix_and_vector_, assemble_vector, assemble_vector_,
                        default_context, numeric_loop_matrix, numeric_loop_vector,
                        prepare_problem, symbolic_loop_matrix)
 from .celldata import (CellField, DomainContribution, NodalField, SinSum, dot, get_fe_basis,
@@ -24,8 +25,8 @@ from .geometry import (CartesianDiscreteModel, FaceLabeling, Measure, SimplexDis
                        Triangulation, simplexify)
 from .batch import BatchedPoissonProblems
 from .learned import LearnedBlockPreconditioner
-from .solvers import (CGSolver, FCGSolver, IRCGSolver, LinearFESolver, LinearSolver,
-                      MixedCGSolver,
+from .solvers import (AffineOperator, CGSolver, FCGSolver, IRCGSolver, LinearFESolver,
+                      LinearSolver, MixedCGSolver, solve_matrix_,
                       SolveReport, solve,
                       solve_, numerical_setup, numerical_setup_, symbolic_setup)
 

@@ -394,6 +394,34 @@ def assemble_matrix_and_vector(a, l, U, V, assem: SparseMatrixAssembler | None =
     return A, b
 
 
+def assemble_matrix_and_vector_(a, l, A: DeviceMatrix, b, U, V,
+                                assem: SparseMatrixAssembler | None = None):
+    """assemble_matrix_and_vector!(a, l, A, b, U, V): re-assembles into A's existing pattern
+    (fillstored!(A, 0) then the numeric loop, FESpaces/SparseMatrixAssemblers.jl:60-68) and
+    overwrites b."""
+    assem = assem or SparseMatrixAssembler(U, V)
+    meas, coef, source = _forms(a, l, U, V)
+    prep = prepare_problem(U, V, meas, coef, source if l is not None else None, assem.precision)
+    if A is not None:
+        A.fillstored_zero()
+    if b is not None:
+        b[...] = 0
+    _lib.check(_lib.load().gfe_assemble_matrix_and_vector(
+        A.ctx.handle if A is not None else assem.ctx.handle, C.byref(prep.p),
+        A.handle if A is not None else None, _lib.ptr(b) if b is not None else None))
+    return A, b
+
+
+def assemble_matrix_(a, A: DeviceMatrix, U, V, assem: SparseMatrixAssembler | None = None):
+    """assemble_matrix!(a, A, U, V)."""
+    return assemble_matrix_and_vector_(a, None, A, None, U, V, assem)[0]
+
+
+def assemble_vector_(l, b, V, assem: SparseMatrixAssembler | None = None):
+    """assemble_vector!(l, b, V)."""
+    return assemble_matrix_and_vector_(None, l, None, b, V, V, assem)[1]
+
+
 def assemble_matrix(a, U, V, assem: SparseMatrixAssembler | None = None) -> DeviceMatrix:
     return assemble_matrix_and_vector(a, None, U, V, assem)[0]
 

@@ -215,10 +215,13 @@ __global__ void k_row_pattern(int64_t nrows, int nd, const int64_t* __restrict__
   }
   const int64_t start = rowptr[r];
   for (int k = 0; k < n; ++k) colval[start + k] = cols[k];
-  // positions of every (reference, local column) in this row's sorted column list
+  // positions of every (reference, local column) in this row's sorted column list; byte
+  // positions are packed and stored four at a time when nd is a multiple of 4
+  const bool packed = sizeof(PosT) == 1 && (nd & 3) == 0;
   for (int64_t q = ref_ptr[r]; q < ref_ptr[r + 1]; ++q) {
     const int32_t cell = refs[q] / nd;
     const int32_t* cc = cell_cols + (int64_t)cell * nd;
+    uint32_t word = 0;
     for (int lj = 0; lj < nd; ++lj) {
       const int32_t c = cc[lj] - 1;
       PosT pos = (PosT)~(PosT)0;
@@ -230,7 +233,15 @@ __global__ void k_row_pattern(int64_t nrows, int nd, const int64_t* __restrict__
         }
         pos = (PosT)lo;
       }
-      refpos[q * nd + lj] = pos;
+      if (packed) {
+        word |= (uint32_t)(uint8_t)pos << (8 * (lj & 3));
+        if ((lj & 3) == 3) {
+          reinterpret_cast<uint32_t*>(refpos + q * nd)[lj >> 2] = word;
+          word = 0;
+        }
+      } else {
+        refpos[q * nd + lj] = pos;
+      }
     }
   }
 }

@@ -99,14 +99,24 @@ __global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
       if (a.val) {
         const auto cc = src.cell(cell);  // per-cell data (coefficients) loaded once per ref
         const PosT* pp = refpos + q * a.nd;
-        for (int lj = 0; lj < a.nd; ++lj) {
-          const PosT p = __ldg(pp + lj);
-          if (p == (PosT)~(PosT)0) continue;  // Dirichlet column
+        auto add = [&](int lj, PosT p) {
+          if (p == (PosT)~(PosT)0) return;  // Dirichlet column
           if (p >= n) {
             raise_err(a.err, GFE_ERR_INVALID_ARGUMENT, r);
-            continue;
+            return;
           }
           acc[p * R + t] += src.m(tab, cc, li, lj, a.nd);
+        };
+        if (sizeof(PosT) == 1 && (a.nd & 3) == 0) {
+          // byte positions four at a time (the reference's row of the table is 4-aligned)
+          const uint32_t* pw = reinterpret_cast<const uint32_t*>(pp);
+          for (int w4 = 0; w4 < (a.nd >> 2); ++w4) {
+            const uint32_t word = __ldg(pw + w4);
+#pragma unroll
+            for (int bb = 0; bb < 4; ++bb) add(4 * w4 + bb, (PosT)((word >> (8 * bb)) & 0xffu));
+          }
+        } else {
+          for (int lj = 0; lj < a.nd; ++lj) add(lj, __ldg(pp + lj));
         }
       }
       if (a.b) bacc += src.v(tab, cell, li);

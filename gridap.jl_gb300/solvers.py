@@ -124,15 +124,44 @@ def solve_(x, ns: NumericalSetup, b):
     return x
 
 
+class AffineOperator:
+    """AffineOperator(A, b): the algebraic operator x -> A x - b (Algebra/LinearSolvers.jl:8-33)."""
+
+    def __init__(self, A: DeviceMatrix, b):
+        self.matrix = A
+        self.vector = b
+
+    def get_matrix(self) -> DeviceMatrix:
+        return self.matrix
+
+    def get_vector(self):
+        return self.vector
+
+    def residual(self, x):
+        """A x - b (host arrays)."""
+        return self.matrix.matvec(x) - np.asarray(self.vector)
+
+
+def solve_matrix_(x, ls: LinearSolver, A: DeviceMatrix, b):
+    """solve!(x, ls, A, b) (Algebra/LinearSolvers.jl:202-209): one-shot setup and solve."""
+    return solve_(x, numerical_setup(symbolic_setup(ls, A), A), b)
+
+
 class LinearFESolver:
     def __init__(self, ls: LinearSolver | None = None):
         self.ls = ls or CGSolver()
 
 
-def solve(solver, op: AffineFEOperator):
-    """uh = solve(solver, op): an FEFunction of the trial space; the solver's report is
-    attached as `uh.report`."""
+def solve(solver, op, b=None):
+    """solve(solver, op) with op an AffineFEOperator returns an FEFunction of the trial space
+    (the solver's report attached as `uh.report`); solve(ls, op) with an AffineOperator and
+    solve(ls, A, b) with a matrix return the solution vector (Algebra/LinearSolvers.jl)."""
     ls = solver.ls if isinstance(solver, LinearFESolver) else solver
+    if b is not None or isinstance(op, AffineOperator):
+        A = op.get_matrix() if isinstance(op, AffineOperator) else op
+        rhs = op.get_vector() if isinstance(op, AffineOperator) else b
+        x = np.empty_like(rhs) if isinstance(rhs, np.ndarray) else rhs.new_empty(rhs.shape)
+        return solve_matrix_(x, ls, A, rhs)
     A, b = op.get_matrix(), op.get_vector()
     x = np.empty_like(b) if isinstance(b, np.ndarray) else b.new_empty(b.shape)
     ns = numerical_setup(symbolic_setup(ls, A), A)

@@ -462,10 +462,14 @@ __global__ void __launch_bounds__(256)
       C[idx] = s;
     }
     __syncthreads();
-    // K = B^T C, upper triangle, mirrored
-    for (int idx = threadIdx.x; idx < NN * NN; idx += blockDim.x) {
-      const int i = idx % NN, j = idx / NN;
-      if (i > j) continue;
+    // K = B^T C over the upper triangle only (i <= j), mirrored. The triangle is enumerated
+    // directly -- column j holds rows 0..j, so entry t lies in column j with
+    // j(j+1)/2 <= t < (j+1)(j+2)/2 -- so that no lane of an FP64 warp instruction idles.
+    for (int t = threadIdx.x; t < NN * (NN + 1) / 2; t += blockDim.x) {
+      int j = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+      while (j * (j + 1) / 2 > t) --j;
+      while ((j + 1) * (j + 2) / 2 <= t) ++j;
+      const int i = t - j * (j + 1) / 2;
       double s = 0.0;
       for (int qk = 0; qk < nq * D; ++qk) s += B[qk * NN + i] * C[qk * NN + j];
       K[(int64_t)(i + j * NN) * ncells + cell] = s;

@@ -433,7 +433,7 @@ struct DiaOp {
 // of (i, j) and kLatK consecutive k-planes; each thread marches up its k-column keeping the
 // three x-planes and two kappa-planes around its node in registers, so a row costs 9 x and 4
 // kappa loads.
-constexpr int kLatK = 4;
+constexpr int kLatK = 8;
 
 struct LatticeQ1Op {
   const float* kap;
@@ -782,8 +782,8 @@ __global__ void __launch_bounds__(kVecBlock)
       if (i < n4) {
         xv[u] = reinterpret_cast<float4*>(x)[i];
         rv[u] = reinterpret_cast<float4*>(r)[i];
-        pv[u] = __ldcs(reinterpret_cast<const float4*>(p) + i);
-        qv[u] = __ldcs(reinterpret_cast<const float4*>(q) + i);
+        pv[u] = __ldg(reinterpret_cast<const float4*>(p) + i);  // p, r, x stay L2-resident
+        qv[u] = __ldcs(reinterpret_cast<const float4*>(q) + i);  // q is rewritten next
         dv[u] = __ldg(reinterpret_cast<const float4*>(dinv) + i);
       }
     }
@@ -840,7 +840,7 @@ __global__ void __launch_bounds__(kVecBlock)
   const int64_t nth = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = tid; i < n4; i += nth) {
     float4 pv = reinterpret_cast<float4*>(p)[i];
-    const float4 rv = __ldcs(reinterpret_cast<const float4*>(r) + i);
+    const float4 rv = __ldg(reinterpret_cast<const float4*>(r) + i);
     const float4 dv = __ldg(reinterpret_cast<const float4*>(dinv) + i);
     pv.x = fmaf(beta, pv.x, dv.x * rv.x);
     pv.y = fmaf(beta, pv.y, dv.y * rv.y);

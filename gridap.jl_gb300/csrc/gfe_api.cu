@@ -132,6 +132,7 @@ extern "C" int gfe_ctx_kernel_time(gfe_ctx* c, int kernel, double* total_ms, int
 extern "C" int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd,
                                         const int32_t* cell_rows, const int32_t* cell_cols,
                                         int64_t nrows, int64_t ncols, gfe_matrix** out) {
+  gfe::NvtxRange nvtx_range("gfe_symbolic_loop_matrix");
   clear_error();
   if (!ctx || !out || nd < 1 || ncells < 0 || nrows < 0 || ncols < 0 ||
       (ncells > 0 && (!cell_rows || !cell_cols)))
@@ -236,6 +237,7 @@ extern "C" int gfe_matrix_fillstored_zero(gfe_matrix* A) {
 
 // ---- numeric, caller-provided cell arrays -------------------------------------------------
 extern "C" int gfe_numeric_loop_matrix(gfe_ctx* ctx, gfe_matrix* A, const double* cellmats) {
+  gfe::NvtxRange nvtx_range("gfe_numeric_loop_matrix");
   clear_error();
   if (!ctx || !A || (A->ncells > 0 && !cellmats) || A->ctx != ctx)
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_numeric_loop_matrix: bad arguments");
@@ -253,6 +255,7 @@ extern "C" int gfe_numeric_loop_matrix(gfe_ctx* ctx, gfe_matrix* A, const double
 extern "C" int gfe_numeric_loop_vector(gfe_ctx* ctx, int64_t ncells, int nd,
                                        const int32_t* cell_rows, const double* cellvecs,
                                        int64_t nrows, double* b) {
+  gfe::NvtxRange nvtx_range("gfe_numeric_loop_vector");
   clear_error();
   if (!ctx || nd < 1 || ncells < 0 || nrows < 0 || !b ||
       (ncells > 0 && (!cell_rows || !cellvecs)))
@@ -278,6 +281,7 @@ extern "C" int gfe_numeric_loop_vector(gfe_ctx* ctx, int64_t ncells, int nd,
 // ---- fused --------------------------------------------------------------------------------
 extern "C" int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* p,
                                               gfe_matrix* A, double* b) {
+  gfe::NvtxRange nvtx_range("gfe_assemble_matrix_and_vector");
   clear_error();
   if (!ctx || !p || (!A && !b) || p->ncells < 0 || (p->ncells > 0 && !p->cell_dof_ids))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_assemble_matrix_and_vector: bad arguments");
@@ -306,6 +310,7 @@ extern "C" int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* p
 // ---- solve --------------------------------------------------------------------------------
 extern "C" int gfe_solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* opts,
                          const double* b, double* x, gfe_solve_report* report) {
+  gfe::NvtxRange nvtx_range("gfe_solve");
   clear_error();
   if (!ctx || !A || !opts || !b || !x || A->ctx != ctx)
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_solve: bad arguments");
@@ -330,6 +335,7 @@ extern "C" int gfe_solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* opt
 }
 
 extern "C" int gfe_matrix_mul(gfe_ctx* ctx, gfe_matrix* A, const double* x, double* y) {
+  gfe::NvtxRange nvtx_range("gfe_matrix_mul");
   clear_error();
   if (!ctx || !A || !x || !y || A->ctx != ctx)
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_matrix_mul: bad arguments");

@@ -421,6 +421,7 @@ extern "C" int gfe_batch_info(gfe_batch* B, int64_t* nrows, int64_t* nfree, int6
 extern "C" int gfe_batch_assemble_solve(gfe_batch* B, double source, double rtol,
                                         int32_t maxiter, double* x, int32_t* iterations,
                                         int32_t* nconverged) {
+  gfe::NvtxRange nvtx_range("gfe_batch_assemble_solve");
   clear_error();
   if (!B || !x || !(rtol > 0.0))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_batch_assemble_solve: bad arguments");

@@ -10,7 +10,17 @@
 
 #include "../../include/gfe.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace gfe {
+
+// NVTX range over one ABI call (visible in nsys / ncu range filters; no cost without a tool)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ---- errors -------------------------------------------------------------------------------
 int set_error(int code, const char* fmt, ...);

@@ -655,6 +655,7 @@ extern "C" int gfe_learned_pc_get_weights(gfe_learned_pc* pc, float* params) {
 extern "C" int gfe_learned_pc_num_params(void) { return kNParams; }
 
 extern "C" int gfe_learned_pc_apply(gfe_learned_pc* pc, const float* r, float* z) {
+  gfe::NvtxRange nvtx_range("gfe_learned_pc_apply");
   clear_error();
   if (!pc || !r || !z || !is_device_ptr(r) || !is_device_ptr(z))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_learned_pc_apply: device vectors needed");
@@ -665,6 +666,7 @@ extern "C" int gfe_learned_pc_apply(gfe_learned_pc* pc, const float* r, float* z
 extern "C" int gfe_solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc,
                              const gfe_solver_opts* opts, const double* b, double* x,
                              gfe_solve_report* report) {
+  gfe::NvtxRange nvtx_range("gfe_solve_fcg");
   clear_error();
   if (!ctx || !A || !opts || !b || !x || A->ctx != ctx || (pc && pc->ndofs != A->nrows))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_solve_fcg: bad arguments");
@@ -714,6 +716,7 @@ extern "C" int gfe_learned_pc_samples(gfe_learned_pc* pc, gfe_matrix* A, const d
 extern "C" int gfe_learned_pc_train(gfe_learned_pc* pc, const float* X, const float* T,
                                     int64_t n, int32_t epochs, int32_t batch, float lr,
                                     uint64_t seed, float* loss) {
+  gfe::NvtxRange nvtx_range("gfe_learned_pc_train");
   clear_error();
   if (!pc || !X || !T || n < 1 || epochs < 1 || batch < 1 || !is_device_ptr(X) ||
       !is_device_ptr(T))

@@ -60,7 +60,8 @@ class Problem(C.Structure):
 
 class SolverOpts(C.Structure):
     _fields_ = [("method", C.c_int32), ("precond", C.c_int32), ("rtol", C.c_double),
-                ("maxiter", C.c_int32), ("inner_rtol", C.c_double), ("check_every", C.c_int32)]
+                ("maxiter", C.c_int32), ("inner_rtol", C.c_double), ("check_every", C.c_int32),
+                ("initial_guess", C.c_int32)]
 
 
 class SolveReport(C.Structure):

@@ -325,6 +325,8 @@ extern "C" int gfe_solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* opt
   if (!xdev) {
     GFE_TRY(ctx->scratch[SCR_VEC_X].reserve(n8 + 8));
     dx = ctx->scratch[SCR_VEC_X].as<double>();
+    if (opts->initial_guess)  // the guess lives in the caller's host array
+      GFE_CUDA_TRY(cudaMemcpyAsync(dx, x, n8, cudaMemcpyHostToDevice, ctx->stream));
   }
   gfe_solve_report rep;
   memset(&rep, 0, sizeof(rep));

@@ -1338,10 +1338,75 @@ static int run_pcg(gfe_ctx* ctx, gfe_matrix* A, const T* sval, const T* dinv, co
   return GFE_OK;
 }
 
+__global__ void k_axpy64(int64_t n, double* __restrict__ x, const double* __restrict__ d) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += d[i];
+}
+
+struct GuessStats {
+  double rr, bb;
+  unsigned ticket[2];
+};
+
+// Solve from the values in d_x (a restart): r0 = b - A x0 in FP64, the chosen solver runs on
+// A d = r0 from d = 0 with its tolerance scaled so that ||r0 - A d|| <= rtol ||b||, then
+// x = x0 + d and the report's relative residual is recomputed on x against b.
+static int solve_from_guess(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, bool fcg,
+                            const gfe_solver_opts* o, const double* d_b, double* d_x,
+                            gfe_solve_report* rep) {
+  GFE_TRY(build_solver_plan(ctx, A));
+  const int64_t n = A->nrows;
+  const unsigned gs = grid_for(n, kSpmvBlock);
+  const unsigned gv = (unsigned)(ctx->num_sms * 4);
+  const size_t n8 = sizeof(double) * (size_t)(n > 0 ? n : 1);
+  DevBuf tmp(ctx);
+  const size_t np = (size_t)std::max<unsigned>(gs, gv) + 64;
+  GFE_TRY(tmp.reserve(2 * n8 + sizeof(double) * np + 256));
+  double* r0 = tmp.as<double>();
+  double* d = r0 + (n > 0 ? n : 1);
+  double* partials = d + (n > 0 ? n : 1);
+  GuessStats* st = reinterpret_cast<GuessStats*>(partials + np);
+  GuessStats h;
+  auto residual = [&](const double* x) -> int {
+    GFE_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(GuessStats), ctx->stream));
+    k_residual64<<<gs, kSpmvBlock, 0, ctx->stream>>>(
+        n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(), x,
+        d_b, r0, partials, &st->rr, &st->ticket[0]);
+    k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, partials, &st->bb, &st->ticket[1]);
+    ctx->launches += 2;
+    GFE_CUDA_TRY(cudaGetLastError());
+    return copy_out(ctx, &h, st, sizeof(GuessStats));
+  };
+  GFE_TRY(residual(d_x));
+  memset(rep, 0, sizeof(*rep));
+  if (!std::isfinite(h.rr)) {
+    rep->status = GFE_ERR_NONFINITE;
+    return set_error(GFE_ERR_NONFINITE, "solve: the initial guess gives a non-finite residual");
+  }
+  if (h.bb == 0.0 || h.rr <= o->rtol * o->rtol * h.bb) {
+    if (h.bb == 0.0) GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
+    rep->converged = 1;
+    rep->relres = h.bb > 0.0 ? std::sqrt(h.rr / h.bb) : 0.0;
+    return GFE_OK;
+  }
+  gfe_solver_opts o2 = *o;
+  o2.initial_guess = 0;
+  o2.rtol = o->rtol * std::sqrt(h.bb / h.rr);
+  GFE_TRY(fcg ? solve_fcg(ctx, A, pc, &o2, r0, d, rep) : solve(ctx, A, &o2, r0, d, rep));
+  k_axpy64<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, d);
+  ctx->launches++;
+  GFE_TRY(residual(d_x));
+  rep->relres = std::sqrt(h.rr / h.bb);
+  rep->converged = std::isfinite(rep->relres) && rep->relres <= o->rtol * (1.0 + 1e-6);
+  return GFE_OK;
+}
+
 int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d_b,
           double* d_x, gfe_solve_report* rep) {
   if (A->nrows != A->ncols)
     return set_error(GFE_ERR_INVALID_ARGUMENT, "solve: matrix is not square");
+  if (o->initial_guess) return solve_from_guess(ctx, A, nullptr, false, o, d_b, d_x, rep);
   GFE_TRY(build_solver_plan(ctx, A));
   const int64_t n = A->nrows;
   const int check_every = o->check_every > 0 ? o->check_every : 25;
@@ -1569,6 +1634,7 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
 int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_opts* o,
               const double* d_b, double* d_x, gfe_solve_report* rep) {
   if (A->nrows != A->ncols) return set_error(GFE_ERR_INVALID_ARGUMENT, "fcg: not square");
+  if (o->initial_guess) return solve_from_guess(ctx, A, pc, true, o, d_b, d_x, rep);
   GFE_TRY(build_solver_plan(ctx, A));
   const int64_t n = A->nrows;
   const int check_every = o->check_every > 0 ? o->check_every : 10;

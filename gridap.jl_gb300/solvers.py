@@ -42,16 +42,18 @@ class LinearSolver:
     method = _lib.GFE_SOLVER_CG
 
     def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, precond: str = "jacobi",
-                 inner_rtol: float = 1e-4, check_every: int = 0):
+                 inner_rtol: float = 1e-4, check_every: int = 0, initial_guess: bool = False):
         self.rtol = rtol
         self.maxiter = maxiter
         self.precond = {"jacobi": _lib.GFE_PC_JACOBI, "none": _lib.GFE_PC_NONE}[precond]
         self.inner_rtol = inner_rtol
         self.check_every = check_every
+        # True: solve!(x, ns, b) starts from the values in x (restart from a saved solution)
+        self.initial_guess = initial_guess
 
     def opts(self) -> _lib.SolverOpts:
         return _lib.SolverOpts(self.method, self.precond, self.rtol, self.maxiter,
-                               self.inner_rtol, self.check_every)
+                               self.inner_rtol, self.check_every, int(self.initial_guess))
 
 
 class CGSolver(LinearSolver):
@@ -69,8 +71,8 @@ class MixedCGSolver(LinearSolver):
     method = _lib.GFE_SOLVER_MIXED_CG
 
     def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, precond: str = "jacobi",
-                 inner_rtol: float = 0.1, check_every: int = 0):
-        super().__init__(rtol, maxiter, precond, inner_rtol, check_every)
+                 inner_rtol: float = 0.1, check_every: int = 0, initial_guess: bool = False):
+        super().__init__(rtol, maxiter, precond, inner_rtol, check_every, initial_guess)
 
 
 class FCGSolver(LinearSolver):
@@ -79,8 +81,8 @@ class FCGSolver(LinearSolver):
     preconditioner hands over to Jacobi (report.fallback)."""
 
     def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, pc=None,
-                 inner_rtol: float = 0.1, check_every: int = 0):
-        super().__init__(rtol, maxiter, "jacobi", inner_rtol, check_every)
+                 inner_rtol: float = 0.1, check_every: int = 0, initial_guess: bool = False):
+        super().__init__(rtol, maxiter, "jacobi", inner_rtol, check_every, initial_guess)
         self.pc = pc
 
 

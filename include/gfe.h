@@ -242,6 +242,9 @@ typedef struct gfe_solver_opts {
   double inner_rtol;    /* IR_CG: relative reduction per refinement step; MIXED_CG: residual
                            reduction between reliable updates (default 0.1) */
   int32_t check_every;  /* iterations between host convergence checks (0 = default) */
+  int32_t initial_guess;/* 0: start from x = 0; 1: start from the values in x (a restart from a
+                           saved solution): the solver runs on A d = b - A x0 with its tolerance
+                           scaled to ||b||, then x = x0 + d */
 } gfe_solver_opts;
 
 typedef struct gfe_solve_report {

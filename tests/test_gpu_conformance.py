@@ -118,3 +118,32 @@ def test_q2_manufactured_solution_is_exact(gg):
     X = _q2_node_coords(D, part, V)
     u = np.prod(X * (1 - X), axis=1)
     assert np.abs(uh.free_values - u).max() <= 1e-10 * np.abs(u).max()
+
+
+@pytest.mark.parametrize("kind", ["cg", "mixed", "fcg"])
+def test_restart_from_saved_solution(gg, tmp_path, kind):
+    """Checkpoint/restart: a solve stopped early is saved, reloaded and continued from that x
+    (initial_guess); the continued solve meets the tolerance, needs fewer iterations than a
+    cold start, and a converged guess returns at once."""
+    _, V, a, l = _system(gg, seed=42)
+    A, b = gg.assemble_matrix_and_vector(a, l, V, V)
+    cls = {"cg": gg.CGSolver, "mixed": gg.MixedCGSolver, "fcg": gg.FCGSolver}[kind]
+    cold = np.zeros_like(b)
+    ns = gg.numerical_setup(gg.symbolic_setup(cls(rtol=1e-10), A), A)
+    gg.solve_(cold, ns, b)
+    cold_it = ns.report.iterations
+    part = np.zeros_like(b)
+    ns = gg.numerical_setup(gg.symbolic_setup(cls(rtol=1e-4), A), A)
+    gg.solve_(part, ns, b)
+    np.save(tmp_path / "x.npy", part)
+    x = np.load(tmp_path / "x.npy")
+    ns = gg.numerical_setup(gg.symbolic_setup(cls(rtol=1e-10, initial_guess=True), A), A)
+    gg.solve_(x, ns, b)
+    assert ns.report.converged and ns.report.relres <= 1e-10
+    assert ns.report.iterations < cold_it
+    r = b - A.to_scipy() @ x
+    assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
+    ns = gg.numerical_setup(gg.symbolic_setup(cls(rtol=1e-6, initial_guess=True), A), A)
+    y = x.copy()
+    gg.solve_(y, ns, b)
+    assert ns.report.converged and ns.report.iterations == 0 and np.array_equal(y, x)

@@ -21,6 +21,7 @@ and reports the DOF of all replicas over the slowest replica's time.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import os
 import pathlib
@@ -70,7 +71,8 @@ def peaks():
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+    """Samples nvidia-smi clocks and throttle reasons (every 50 ms) around the timed regions;
+    `window()` marks a timed region and the summary keeps only samples taken inside one."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -78,24 +80,39 @@ class ClockSampler:
 
     def __init__(self, index: int):
         self.index = index
-        self.rows = []
+        self.rows = []      # (host time, fields)
+        self.windows = []   # (t0, t1) of the timed regions
         self.proc = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.perf_counter()
+            while not self.rows and time.perf_counter() - t0 < 5.0:  # sampler running
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
+
+    def window(self):
+        sampler = self
+
+        class _W:
+            def __enter__(self):
+                self.t0 = time.perf_counter()
+
+            def __exit__(self, *a):
+                sampler.windows.append((self.t0, time.perf_counter()))
+        return _W()
 
     def __exit__(self, *a):
         if self.proc:
@@ -106,19 +123,21 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if not self.rows:
+        rows = [r for t, r in self.rows
+                if not self.windows or any(a <= t <= b for a, b in self.windows)]
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = set()
-        for r in self.rows:
+        for r in rows:
             for k, nm in enumerate(names):
                 if len(r) > 4 + k and r[4 + k].lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
-                "samples": len(self.rows)}
+                "samples": len(rows), "period_ms": 50}
 
 
 def spmv_bytes(nnz, n, s):
@@ -205,6 +224,8 @@ def run_gpu(args):
             import torch.distributed as dist
             dist.barrier()
 
+    clocks = []  # the clock sampler while the headline arms run
+
     def timed(label, fn, steps, warmup, kernel_timing=True):
         for _ in range(warmup):
             fn()
@@ -214,15 +235,16 @@ def run_gpu(args):
         e1 = torch.cuda.Event(enable_timing=True)
         l0 = ctx.kernel_launches()
         reps = []
-        with torch.cuda.stream(stream):
-            e0.record(stream)
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            reps.append(fn())
-        with torch.cuda.stream(stream):
-            e1.record(stream)
-        barrier()
-        wall = time.perf_counter() - t0
+        with clocks[0].window() if clocks else contextlib.nullcontext():
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                reps.append(fn())
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            barrier()
+            wall = time.perf_counter() - t0
         kt = {k: ctx.kernel_time(k) for k in (_lib.GFE_KT_SPMV64, _lib.GFE_KT_SPMV32,
                                               _lib.GFE_KT_ASSEMBLE, _lib.GFE_KT_RESIDUAL64,
                                               _lib.GFE_KT_PRECOND, _lib.GFE_KT_VECTOR,
@@ -246,15 +268,18 @@ def run_gpu(args):
     # only on its direct-launch path, so the same steps are then repeated with kernel timing
     # on; the roofline comes from that instrumented repeat (its ms_per_step is reported too).
     with ClockSampler(local) as clk:
+        clocks.append(clk)
         r_mixed = timed("mixed", mixed_dev, args.steps, args.warmup, kernel_timing=False)
         r_mixed_kt = timed("mixed_kt", mixed_dev, args.steps, 1)
-    r_plain = timed("plain", plain_dev, args.steps, max(3, args.warmup), kernel_timing=False)
-    r_plain_kt = timed("plain_kt", plain_dev, args.steps, 1)
-    x_plain = x_d.clone()
-    r_mixed_chk = mixed_dev()
-    x_mixed = x_d.clone()
-    err_vs_fp64 = float(torch.linalg.norm(x_mixed - x_plain) / torch.linalg.norm(x_plain))
-    r_e2e = timed("e2e", mixed_e2e, args.steps, max(3, args.warmup), kernel_timing=False)
+        r_plain = timed("plain", plain_dev, args.steps, max(3, args.warmup),
+                        kernel_timing=False)
+        r_plain_kt = timed("plain_kt", plain_dev, args.steps, 1)
+        x_plain = x_d.clone()
+        mixed_dev()
+        x_mixed = x_d.clone()
+        err_vs_fp64 = float(torch.linalg.norm(x_mixed - x_plain) / torch.linalg.norm(x_plain))
+        r_e2e = timed("e2e", mixed_e2e, args.steps, max(3, args.warmup), kernel_timing=False)
+        clocks.clear()
 
     # learned arm: FCG with the learned block preconditioner (weights trained offline on
     # 64^3 draws), and FCG with Jacobi on the same vectors for comparison

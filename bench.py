@@ -777,7 +777,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gfe", choices=["gfe", "reference"])
     ap.add_argument("--n", type=int, default=128)
-    ap.add_argument("--delta", type=float, default=0.1,
+    ap.add_argument("--delta", type=float, default=0.01,
                     help="residual reduction between FP64 reliable updates of the mixed CG")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")

@@ -1482,7 +1482,7 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
     float* q32 = f + 3 * nv;
     const float* dinv_in = dinv32;  // D^-1 in the layout of the FP32 vectors
     const unsigned gv = (unsigned)(ctx->num_sms * 4);
-    const double delta = o->inner_rtol > 0 ? o->inner_rtol : 0.1;
+    const double delta = o->inner_rtol > 0 ? o->inner_rtol : 0.01;
     GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
     GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
     int maxit_field = maxit;

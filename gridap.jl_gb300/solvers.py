@@ -67,11 +67,11 @@ class IRCGSolver(LinearSolver):
 class MixedCGSolver(LinearSolver):
     """FP32 PCG with FP64 reliable updates: x accumulates in FP64 and the FP32 residual is
     replaced by the FP64 true residual b - A x every time it has dropped by `inner_rtol`
-    (default 0.1); the search direction is re-orthogonalised and kept."""
+    (default 0.01); the search direction is re-orthogonalised and kept."""
     method = _lib.GFE_SOLVER_MIXED_CG
 
     def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, precond: str = "jacobi",
-                 inner_rtol: float = 0.1, check_every: int = 0, initial_guess: bool = False):
+                 inner_rtol: float = 0.01, check_every: int = 0, initial_guess: bool = False):
         super().__init__(rtol, maxiter, precond, inner_rtol, check_every, initial_guess)
 
 

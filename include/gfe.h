@@ -240,7 +240,8 @@ typedef struct gfe_solver_opts {
   double rtol;          /* stop when ||b - A x||_2 <= rtol ||b||_2 (FP64 residual) */
   int32_t maxiter;      /* total inner iterations allowed */
   double inner_rtol;    /* IR_CG: relative reduction per refinement step; MIXED_CG: residual
-                           reduction between reliable updates (default 0.1) */
+                           reduction between reliable updates (default 0.01); FCG: the same
+                           (default 0.1) */
   int32_t check_every;  /* iterations between host convergence checks (0 = default) */
   int32_t initial_guess;/* 0: start from x = 0; 1: start from the values in x (a restart from a
                            saved solution): the solver runs on A d = b - A x0 with its tolerance

@@ -17,12 +17,12 @@ from .assembly import (AffineFEOperator, Context, DeviceMatrix, SparseMatrixAsse
                        default_context, numeric_loop_matrix, numeric_loop_vector,
                        prepare_problem, symbolic_loop_matrix)
 from .celldata import (CellField, DomainContribution, NodalField, SinSum, dot, get_fe_basis,
-                       get_trial_fe_basis, grad, gradient, inner, integrate, isotropic_stress,
-                       symmetric_gradient, ε)
+                       get_normal_vector, get_trial_fe_basis, grad, gradient, inner, integrate,
+                       isotropic_stress, symmetric_gradient, ε)
 from .fespaces import (FEFunction, FESpace, ReferenceFE, TrialFESpace, get_cell_dof_ids,
                        lagrangian, num_free_dofs)
-from .geometry import (CartesianDiscreteModel, FaceLabeling, Measure, SimplexDiscreteModel,
-                       Triangulation, simplexify)
+from .geometry import (Boundary, BoundaryTriangulation, CartesianDiscreteModel, FaceLabeling,
+                       Measure, SimplexDiscreteModel, Triangulation, simplexify)
 from .batch import BatchedPoissonProblems
 from .learned import LearnedBlockPreconditioner
 from .solvers import (AffineOperator, CGSolver, FCGSolver, IRCGSolver, LinearFESolver,

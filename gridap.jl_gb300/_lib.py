@@ -30,6 +30,7 @@ GFE_FORM_DIFFUSION, GFE_FORM_ELASTICITY = 1, 2
 GFE_REFFE_Q1, GFE_REFFE_Q2, GFE_REFFE_P2_TET = 1, 2, 3
 GFE_COEF_ONE, GFE_COEF_CONST, GFE_COEF_CELL = 0, 1, 2
 GFE_SRC_NONE, GFE_SRC_CONST, GFE_SRC_NODAL, GFE_SRC_QPOINT, GFE_SRC_SINSUM = 0, 1, 2, 3, 4
+GFE_BOP_VALUE, GFE_BOP_NORMAL_GRAD = 0, 1
 GFE_PREC_FP64, GFE_PREC_FP32 = 0, 1
 GFE_SOLVER_CG, GFE_SOLVER_IR_CG, GFE_SOLVER_MIXED_CG = 0, 1, 2
 GFE_PC_NONE, GFE_PC_JACOBI = 0, 1
@@ -54,7 +55,7 @@ class Problem(C.Structure):
         ("nnodes", C.c_int64), ("node_coords", C.c_void_p), ("cell_node_ids", C.c_void_p),
         ("form", C.c_int32), ("coef_kind", C.c_int32), ("coef", C.c_void_p),
         ("source_kind", C.c_int32), ("source", C.c_void_p), ("source_len", C.c_int64),
-        ("precision", C.c_int32),
+        ("precision", C.c_int32), ("dirichlet_values", C.c_void_p), ("ndirichlet", C.c_int64),
     ]
 
 
@@ -112,6 +113,11 @@ SIGNATURES = {
     "gfe_solve_fcg": (C.c_int, [_P, _P, _P, C.POINTER(SolverOpts), _P, _P,
                                 C.POINTER(SolveReport)]),
     "gfe_simplex_model": (C.c_int, [_P, _P]),
+    "gfe_assemble_boundary_vector": (C.c_int, [_P, C.POINTER(Problem), C.c_int64, _P, _P,
+                                               C.c_int32, C.c_int32, C.c_int32, _P, C.c_int64,
+                                               _P]),
+    "gfe_assemble_boundary_matrix": (C.c_int, [_P, C.POINTER(Problem), _P, _P, C.c_int64, _P,
+                                               _P, C.c_int32, _P]),
     "gfe_simplex_p2_dofs": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P, _P]),
     "gfe_batch_create": (C.c_int, [_P, C.c_int32, _P, _P, C.POINTER(C.c_void_p)]),
     "gfe_batch_destroy": (C.c_int, [_P]),

@@ -14,9 +14,10 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .celldata import CellField, NodalField, SinSum, classify_bilinear, classify_linear
+from .celldata import (CellField, NodalField, SinSum, classify_bilinear,
+                       classify_boundary_bilinear, classify_boundary_linear, classify_linear)
 from .fespaces import FESpace, TrialFESpace, _space
-from .geometry import Measure, SimplexDiscreteModel
+from .geometry import BoundaryTriangulation, Measure, SimplexDiscreteModel, Triangulation
 
 _CTX = {}
 
@@ -314,10 +315,13 @@ def prepare_problem(U, V, measure: Measure, coef=None, source=None, precision="f
     """The gfe_problem for ∫ coef ∇v⋅∇u dΩ and ∫ source v dΩ on V (U == V for square); on a
     simplexified model, for ∫ ε(v) ⊙ σ(ε(u)) dΩ with coef = (λ, μ) and ∫ f⋅v dΩ with
     source = f. geometry="nodal" forces the general (node-coordinate) element path."""
+    uD = U.dirichlet_values if isinstance(U, TrialFESpace) else None
     V = _space(V)
     model = V.model
     if isinstance(model, SimplexDiscreteModel):
-        return _prepare_elasticity(V, measure, coef, source, precision, cell_dof_ids, geometry)
+        prep = _prepare_elasticity(V, measure, coef, source, precision, cell_dof_ids, geometry)
+        _dirichlet_to_problem(prep, uD)
+        return prep
     prep = _Prepared()
     p = prep.p
     D = model.dim
@@ -347,40 +351,143 @@ def prepare_problem(U, V, measure: Measure, coef=None, source=None, precision="f
     _coef_to_problem(prep, coef, p.ncells)
     _source_to_problem(prep, source, model, measure)
     p.precision = _lib.GFE_PREC_FP32 if precision == "fp32" else _lib.GFE_PREC_FP64
+    _dirichlet_to_problem(prep, uD)
     return prep
 
 
-def _forms(a, l, U, V):
-    """Evaluates user forms a(u,v), l(v) into (measure, coef, source)."""
+def _dirichlet_to_problem(prep: _Prepared, uD) -> None:
+    if uD is None:
+        return
+    uD = np.ascontiguousarray(uD, np.float64)
+    prep.keep.append(uD)
+    prep.p.dirichlet_values, prep.p.ndirichlet = _lib.ptr(uD), uD.size
+
+
+class _Forms:
+    """User forms evaluated into the volume measure, coefficient and source, plus the
+    boundary terms: bilinear [(measure, (c0, c1, c2, c3))] and linear
+    [(measure, [(test_op, scale, data)])] on BoundaryTriangulation measures."""
+
+    def __init__(self, meas, coef, source, boundary, boundary_mat):
+        self.meas, self.coef, self.source = meas, coef, source
+        self.boundary, self.boundary_mat = boundary, boundary_mat
+
+    def __iter__(self):
+        return iter((self.meas, self.coef, self.source))
+
+
+def _forms(a, l, U, V) -> _Forms:
+    """Evaluates user forms a(u,v), l(v): one volume term in each, and any number of terms on
+    BoundaryTriangulation measures (Neumann, Nitsche and Robin terms)."""
     from .celldata import get_fe_basis, get_trial_fe_basis
     u, v = get_trial_fe_basis(U), get_fe_basis(V)
     coef = source = None
     meas = None
+    boundary, boundary_mat = [], []
     if a is not None:
         dc = a(u, v)
-        if len(dc.terms) != 1:
-            raise NotImplementedError("one bilinear term is provided")
-        expr, meas = dc.terms[0]
+        vol = [(e, m) for e, m in dc.terms if not m.on_boundary]
+        boundary_mat = [(m, classify_boundary_bilinear(e)) for e, m in dc.terms if m.on_boundary]
+        if len(vol) != 1:
+            raise NotImplementedError("one bilinear term over the cells is provided")
+        expr, meas = vol[0]
         _, coef = classify_bilinear(expr)
     if l is not None:
         dc = l(v)
-        if len(dc.terms) != 1:
-            raise NotImplementedError("one linear term is provided")
-        expr, m2 = dc.terms[0]
-        if meas is not None and m2.degree != meas.degree:
-            raise NotImplementedError("bilinear and linear forms on different measures")
-        meas = m2
-        _, source = classify_linear(expr)
-    return meas, coef, source
+        vol = [(e, m) for e, m in dc.terms if not m.on_boundary]
+        boundary = [(m, classify_boundary_linear(e)) for e, m in dc.terms if m.on_boundary]
+        if len(vol) > 1:
+            raise NotImplementedError("one linear term over the cells is provided")
+        if vol:
+            expr, m2 = vol[0]
+            if meas is not None and m2.degree != meas.degree:
+                raise NotImplementedError("bilinear and linear forms on different measures")
+            meas = m2
+            _, source = classify_linear(expr)
+    if meas is None:
+        # boundary terms only: the volume pass assembles no source
+        meas = Measure(Triangulation(_space(V).model), 2)
+    return _Forms(meas, coef, source, boundary, boundary_mat)
+
+
+def _facet_qpoints(trian: BoundaryTriangulation, degree: int) -> np.ndarray:
+    """Physical Gauss points of every facet (tensor Gauss-Legendre of `degree`, first facet
+    coordinate fastest): host glue for Python-callable boundary data."""
+    D = trian.model.dim
+    n = degree // 2 + 1
+    x1, _ = np.polynomial.legendre.leggauss(n)
+    x1 = (x1 + 1) / 2
+    k = np.arange(n ** (D - 1))
+    s = np.stack([x1[(k // n ** d) % n] for d in range(D - 1)], axis=1)
+    return trian.facet_points(s)[1]
+
+
+def _facet_data(trian: BoundaryTriangulation, degree: int, terms):
+    """Sum of scale * data over terms at every facet Gauss point: (kind, values)."""
+    if all(d is None for _, _, d in terms):
+        return _lib.GFE_SRC_CONST, np.array([sum(c for _, c, _ in terms)])
+    xq = _facet_qpoints(trian, degree)
+    nf, nq, D = xq.shape
+    x = xq.reshape(-1, D)
+    tot = np.zeros(nf * nq)
+    for _, c, d in terms:
+        if d is None:
+            tot += c
+        elif isinstance(d, tuple):  # n . G(x)
+            G = np.asarray(d[1](x), np.float64)
+            if G.shape != (x.shape[0], D):
+                G = np.array([np.asarray(d[1](xi), np.float64) for xi in x])
+            n = np.repeat(trian.get_facet_normal(), nq, axis=0)
+            tot += c * np.einsum("pd,pd->p", n, G)
+        else:
+            g = np.asarray(d(x), np.float64)
+            if g.shape != (x.shape[0],):
+                g = np.array([float(d(xi)) for xi in x])
+            tot += c * g
+    return _lib.GFE_SRC_QPOINT, np.ascontiguousarray(tot)
+
+
+def _assemble_boundary(ctx, prep: _Prepared, forms: _Forms, A, b) -> None:
+    """A += the facet matrices of the bilinear boundary terms (with their Dirichlet lift into
+    b) and b += the linear boundary terms: gfe_assemble_boundary_matrix / _vector."""
+    if not forms.boundary and not forms.boundary_mat:
+        return
+    p = prep.p
+    if p.reffe not in (_lib.GFE_REFFE_Q1, _lib.GFE_REFFE_Q2) or p.ncomp != 1:
+        raise NotImplementedError("boundary terms are provided for scalar Q1/Q2 spaces")
+    L = _lib.load()
+    if A is not None:
+        for meas, coefs in forms.boundary_mat:
+            G = meas.trian
+            cf = np.array(coefs, np.float64)
+            _lib.check(L.gfe_assemble_boundary_matrix(
+                ctx.handle, C.byref(p), A.handle, _lib.ptr(b) if b is not None else None,
+                G.num_cells(), _lib.ptr(G.facet_cells), _lib.ptr(G.facet_lfaces), meas.degree,
+                _lib.ptr(cf)))
+    if b is None:
+        return
+    for meas, terms in forms.boundary:
+        G = meas.trian
+        for op in (_lib.GFE_BOP_VALUE, _lib.GFE_BOP_NORMAL_GRAD):
+            sel = [t for t in terms if t[0] == op]
+            if not sel:
+                continue
+            kind, vals = _facet_data(G, meas.degree, sel)
+            _lib.check(L.gfe_assemble_boundary_vector(
+                ctx.handle, C.byref(p), G.num_cells(), _lib.ptr(G.facet_cells),
+                _lib.ptr(G.facet_lfaces), meas.degree, op, kind, _lib.ptr(vals), vals.size,
+                _lib.ptr(b)))
 
 
 def assemble_matrix_and_vector(a, l, U, V, assem: SparseMatrixAssembler | None = None,
                                b_out=None):
     """(A, b) for the weak forms a(u,v), l(v) (FESpaces/Assemblers.jl:372-400)."""
     assem = assem or SparseMatrixAssembler(U, V)
-    meas, coef, source = _forms(a, l, U, V)
+    forms = _forms(a, l, U, V)
+    meas, coef, source = forms
     Vs = _space(V)
     prep = prepare_problem(U, V, meas, coef, source if l is not None else None, assem.precision)
+    prep.model = Vs.model
     A = None
     if a is not None:
         ids = Vs.cell_dof_ids
@@ -391,6 +498,7 @@ def assemble_matrix_and_vector(a, l, U, V, assem: SparseMatrixAssembler | None =
     _lib.check(_lib.load().gfe_assemble_matrix_and_vector(
         assem.ctx.handle, C.byref(prep.p), A.handle if A is not None else None,
         _lib.ptr(b) if b is not None else None))
+    _assemble_boundary(assem.ctx, prep, forms, A, b)
     return A, b
 
 
@@ -400,15 +508,19 @@ def assemble_matrix_and_vector_(a, l, A: DeviceMatrix, b, U, V,
     (fillstored!(A, 0) then the numeric loop, FESpaces/SparseMatrixAssemblers.jl:60-68) and
     overwrites b."""
     assem = assem or SparseMatrixAssembler(U, V)
-    meas, coef, source = _forms(a, l, U, V)
+    forms = _forms(a, l, U, V)
+    meas, coef, source = forms
     prep = prepare_problem(U, V, meas, coef, source if l is not None else None, assem.precision)
+    prep.model = _space(V).model
     if A is not None:
         A.fillstored_zero()
     if b is not None:
         b[...] = 0
+    ctx = A.ctx if A is not None else assem.ctx
     _lib.check(_lib.load().gfe_assemble_matrix_and_vector(
-        A.ctx.handle if A is not None else assem.ctx.handle, C.byref(prep.p),
+        ctx.handle, C.byref(prep.p),
         A.handle if A is not None else None, _lib.ptr(b) if b is not None else None))
+    _assemble_boundary(ctx, prep, forms, A, b)
     return A, b
 
 

@@ -10,7 +10,11 @@ enum plus coefficient arrays across the C ABI:
   - linear    `f * v`  (f: number, NodalField, SinSum, or a Python callable of x);
   - bilinear  `inner(ε(v), σ(ε(u)))` with σ = isotropic_stress(λ, μ), i.e.
               ε(v) ⊙ (λ tr(ε(u)) I + 2μ ε(u))  (λ, μ: numbers or per-cell CellFields);
-  - linear    `inner(f, v)` with f a constant 3-vector (body force).
+  - linear    `inner(f, v)` with f a constant 3-vector (body force);
+  - on a BoundaryTriangulation measure: sums of  c v u,  c v (n⋅∇u),  c (n⋅∇v) u,
+    c (n⋅∇v)(n⋅∇u)  (c constant; Nitsche and Robin terms) in bilinear forms and of
+    g v,  g (n⋅∇v)  in linear forms (g a number, a callable of x, or n⋅G with G a callable
+    returning vectors, e.g. the gradient of an exact solution).
 
 Anything else raises NotImplementedError; in Gridap that integrand would stay on Gridap's
 own CPU path.
@@ -56,10 +60,55 @@ class SinSum:
 
 class _Expr:
     def __mul__(self, other):
+        if isinstance(other, _Expr):
+            return _Prod(self, other)
         return _Scaled(other, self)
 
     def __rmul__(self, other):
         return _Scaled(other, self)
+
+    def __add__(self, other):
+        return _Sum([(1.0, self), (1.0, other)])
+
+    def __sub__(self, other):
+        return _Sum([(1.0, self), (-1.0, other)])
+
+    def __neg__(self):
+        return _Scaled(-1.0, self)
+
+    def __truediv__(self, other):
+        if isinstance(other, _Expr):
+            return NotImplemented
+        return _Scaled(1.0 / other, self)
+
+
+class _Prod(_Expr):
+    def __init__(self, a, b):
+        self.a = a
+        self.b = b
+
+
+class _Sum(_Expr):
+    """sum of sign * term"""
+
+    def __init__(self, terms):
+        self.terms = []
+        for s, t in terms:
+            if isinstance(t, _Sum):
+                self.terms += [(s * s2, t2) for s2, t2 in t.terms]
+            else:
+                self.terms.append((s, t))
+
+
+class _Normal(_Expr):
+    """get_normal_vector(Γ): the outward unit normal of a BoundaryTriangulation's facets."""
+
+    def __init__(self, trian):
+        self.trian = trian
+
+
+def get_normal_vector(trian) -> _Normal:
+    return _Normal(trian)
 
 
 class _Basis(_Expr):
@@ -199,3 +248,95 @@ def classify_linear(expr):
     if isinstance(e, _Basis) and not e.trial:
         return "source", (1.0 if coef is None else coef)
     raise NotImplementedError("linear form not recognised (provided: f*v)")
+
+
+# ---- boundary integrands --------------------------------------------------------------------
+BOP_VALUE, BOP_NORMAL_GRAD = 0, 1
+
+
+def _monomials(e):
+    """Expands an integrand into [(factors)]: products of leaves (numbers, callables, bases,
+    n⋅∇(basis), n⋅G data) with the signs and constant scales as number factors."""
+    if isinstance(e, _Sum):
+        out = []
+        for s, t in e.terms:
+            out += [[s] + m for m in _monomials(t)]
+        return out
+    if isinstance(e, _Scaled):
+        return [[e.coef] + m for m in _monomials(e.expr)]
+    if isinstance(e, _Prod):
+        return [ma + mb for ma in _monomials(e.a) for mb in _monomials(e.b)]
+    return [[e]]
+
+
+def _normal_grad_of(f):
+    """n⋅∇(basis) -> the basis; n⋅G with G a callable -> ('data', G); else None."""
+    if not isinstance(f, _Inner):
+        return None
+    for n, g in ((f.a, f.b), (f.b, f.a)):
+        if isinstance(n, _Normal):
+            if isinstance(g, _Grad) and isinstance(g.arg, _Basis):
+                return g.arg
+            if callable(g) and not isinstance(g, _Expr):
+                return ("data", g)
+    return None
+
+
+def _split_factor(f):
+    """('test'|'trial', op) for a basis factor, ('num', c), ('data', g) or ('ndata', G)."""
+    if isinstance(f, _Basis):
+        return ("trial" if f.trial else "test", BOP_VALUE)
+    ng = _normal_grad_of(f)
+    if isinstance(ng, _Basis):
+        return ("trial" if ng.trial else "test", BOP_NORMAL_GRAD)
+    if isinstance(ng, tuple):
+        return ("ndata", ng[1])
+    if isinstance(f, (int, float, np.floating, np.integer)):
+        return ("num", float(f))
+    if callable(f) and not isinstance(f, _Expr):
+        return ("data", f)
+    raise NotImplementedError(f"boundary integrand factor {type(f).__name__} not recognised")
+
+
+def classify_boundary_bilinear(expr):
+    """Coefficients (c0, c1, c2, c3) of ∫ c0 v u + c1 v (n⋅∇u) + c2 (n⋅∇v) u
+    + c3 (n⋅∇v)(n⋅∇u) dΓ."""
+    coefs = [0.0, 0.0, 0.0, 0.0]
+    for mono in _monomials(expr):
+        c, test, trial = 1.0, None, None
+        for f in mono:
+            kind, val = _split_factor(f)
+            if kind == "num":
+                c *= val
+            elif kind == "test" and test is None:
+                test = val
+            elif kind == "trial" and trial is None:
+                trial = val
+            else:
+                raise NotImplementedError("boundary bilinear terms carry constant coefficients")
+        if test is None or trial is None:
+            raise NotImplementedError("each boundary bilinear term needs u and v")
+        coefs[2 * test + trial] += c
+    return tuple(coefs)
+
+
+def classify_boundary_linear(expr):
+    """[(test_op, scale, data)] of the terms scale * data * op(v): data None (constant), a
+    callable g(x), or ('n', G) for n⋅G(x)."""
+    out = []
+    for mono in _monomials(expr):
+        c, test, data = 1.0, None, None
+        for f in mono:
+            kind, val = _split_factor(f)
+            if kind == "num":
+                c *= val
+            elif kind == "test" and test is None:
+                test = val
+            elif kind in ("data", "ndata") and data is None:
+                data = val if kind == "data" else ("n", val)
+            else:
+                raise NotImplementedError("boundary linear term not recognised (g v, g n⋅∇v)")
+        if test is None:
+            raise NotImplementedError("each boundary linear term needs v")
+        out.append((test, c, data))
+    return out

@@ -8,16 +8,7 @@ using namespace gfe;
 
 namespace {
 
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    if (prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    if (prev >= 0) cudaSetDevice(prev);
-  }
-};
+
 
 }  // namespace
 
@@ -298,6 +289,21 @@ extern "C" int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* p
     db = ctx->scratch[SCR_VEC_B].as<double>();
   }
   if (A) A->mf_state = 0;
+  struct LiftReset {
+    gfe_ctx* c;
+    ~LiftReset() {
+      c->lift_uD = nullptr;
+      c->lift_ndiri = 0;
+    }
+  } lift_reset{ctx};
+  if (A && b && p->dirichlet_values && p->ndirichlet > 0) {
+    // nonzero Dirichlet data: the lift needs the matrix entries, so it comes with A and b
+    const void* v;
+    GFE_TRY(device_view(ctx, p->dirichlet_values, sizeof(double) * (size_t)p->ndirichlet,
+                        SCR_DIRI, &v));
+    ctx->lift_uD = static_cast<const double*>(v);
+    ctx->lift_ndiri = p->ndirichlet;
+  }
   GFE_TRY(assemble_problem(ctx, p, A, db));
   if (A) {
     A->plan_valid = false;

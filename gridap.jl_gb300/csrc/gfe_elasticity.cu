@@ -297,26 +297,7 @@ int assemble_p2_elasticity(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, do
     ctx->launches++;
   }
   GFE_CUDA_TRY(cudaGetLastError());
-  RowArgs am = a;  // matrix pass; the vector goes through its own gather below
-  am.b = nullptr;
-  if (fp32) {
-    StoredCellsF32 src{};
-    src.mat = A ? ctx->scratch[SCR_CELLMAT].as<float>() : nullptr;
-    src.cs = 1;
-    src.es = ncells;
-    src.vec = nullptr;
-    src.ntab = 0;
-    if (A) GFE_TRY(run_rows(ctx, am, src, maxw, A->pos_bytes));
-  } else {
-    StoredCells src{};
-    src.mat = A ? ctx->scratch[SCR_CELLMAT].as<double>() : nullptr;
-    src.cs = 1;
-    src.es = ncells;
-    src.vec = nullptr;
-    src.ntab = 0;
-    if (A) GFE_TRY(run_rows(ctx, am, src, maxw, A->pos_bytes));
-  }
-  if (bv) {
+  if (bv) {  // the vector through its own gather, before the matrix pass and its lift
     StoredCells vs{};
     vs.mat = nullptr;
     vs.vec = bv;
@@ -326,6 +307,28 @@ int assemble_p2_elasticity(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, do
     RowArgs av = a;
     av.val = nullptr;
     GFE_TRY(vector_only_rows(ctx, av, vs));
+  }
+  RowArgs am = a;  // matrix pass
+  am.b = nullptr;
+  const bool lift = A && bv && a.uD;
+  if (fp32) {
+    StoredCellsF32 src{};
+    src.mat = A ? ctx->scratch[SCR_CELLMAT].as<float>() : nullptr;
+    src.cs = 1;
+    src.es = ncells;
+    src.vec = nullptr;
+    src.ntab = 0;
+    if (A) GFE_TRY(run_rows(ctx, am, src, maxw, A->pos_bytes));
+    if (lift) GFE_TRY(dirichlet_lift(ctx, a, src));
+  } else {
+    StoredCells src{};
+    src.mat = A ? ctx->scratch[SCR_CELLMAT].as<double>() : nullptr;
+    src.cs = 1;
+    src.es = ncells;
+    src.vec = nullptr;
+    src.ntab = 0;
+    if (A) GFE_TRY(run_rows(ctx, am, src, maxw, A->pos_bytes));
+    if (lift) GFE_TRY(dirichlet_lift(ctx, a, src));
   }
   return check_device_error(ctx, "assemble (P2 elasticity)");
 }

@@ -14,6 +14,18 @@
 
 namespace gfe {
 
+// Makes ctx's device current for one ABI call and restores the caller's device after it.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
 // NVTX range over one ABI call (visible in nsys / ncu range filters; no cost without a tool)
 struct NvtxRange {
   explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
@@ -95,7 +107,11 @@ struct gfe_ctx {
   long long launches = 0;
   gfe::DevError* d_err = nullptr;  // device error word
   // named scratch buffers reused across calls
-  gfe::DevBuf scratch[16];
+  gfe::DevBuf scratch[18];
+  // Dirichlet values (device) of the assembly call in progress; the row gathers of a
+  // matrix-and-vector assembly add the lift b_i -= K_ij u_D_j when set
+  const double* lift_uD = nullptr;
+  int64_t lift_ndiri = 0;
   // pinned staging for small device->host reads
   void* h_pinned = nullptr;
   gfe::KernelTimer timer;
@@ -159,8 +175,11 @@ enum ScratchId {
   SCR_VEC_X,
   SCR_SOLVER,
   SCR_SOLVER2,
-  SCR_REDUCE
+  SCR_REDUCE,
+  SCR_DIRI,
+  SCR_COUNT
 };
+static_assert(SCR_COUNT <= 18, "scratch slots");
 
 // pointer classification
 bool is_device_ptr(const void* p);

@@ -27,6 +27,8 @@ struct RowArgs {
   double* val;               // may be null (vector only)
   double* b;                 // may be null (matrix only)
   DevError* err;
+  const double* uD = nullptr;  // Dirichlet values for the lift (null: u_D = 0)
+  int64_t ndiri = 0;
 };
 
 // ---- cell value sources -------------------------------------------------------------------
@@ -252,8 +254,67 @@ static int launch_rows_warp(gfe_ctx* ctx, const RowArgs& a, const Src& src, int 
   return GFE_OK;
 }
 
+// Dirichlet lift (AttachDirichletMap, CellData/AttachDirichlet.jl:59-110): every cell's
+// vector entry li receives -sum_j K_cell[li][j] u_D[j] over the cell's Dirichlet columns j;
+// b[r] += those contributions of the row's references, in cell order.
+template <class Src>
+__global__ void k_dirichlet_lift(RowArgs a, Src src) {
+  extern __shared__ double tab[];
+  src.load_tables(tab);
+  __syncthreads();
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.nrows) return;
+  double acc = 0.0;
+  bool any = false;
+  for (int64_t q = a.ref_ptr[r]; q < a.ref_ptr[r + 1]; ++q) {
+    const int32_t e = a.refs[q];
+    const int64_t cell = e / a.nd;
+    const int li = e - (int)(cell * a.nd);
+    const int32_t* ids = a.cell_cols + cell * a.nd;
+    double l = 0.0;
+    bool has = false;
+    const auto cc = src.cell(cell);
+    for (int lj = 0; lj < a.nd; ++lj) {
+      const int32_t col = __ldg(ids + lj);
+      if (col >= 0) continue;
+      const int64_t k = -(int64_t)col - 1;
+      if (k >= a.ndiri) {
+        raise_err(a.err, GFE_ERR_INVALID_ARGUMENT, r);
+        continue;
+      }
+      has = true;
+      l -= src.m(tab, cc, li, lj, a.nd) * __ldg(a.uD + k);
+    }
+    if (has) {
+      acc += l;
+      any = true;
+    }
+  }
+  if (any) a.b[r] += acc;
+}
+
+template <class Src>
+static int dirichlet_lift(gfe_ctx* ctx, const RowArgs& a, const Src& src) {
+  k_dirichlet_lift<Src><<<grid_for(a.nrows, 128), 128, sizeof(double) * src.ntab,
+                          ctx->stream>>>(a, src);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+template <class Src>
+static int run_rows_main(gfe_ctx* ctx, const RowArgs& a, const Src& src, int maxw, int pb);
+
+// The row gather, followed by the Dirichlet lift when the call carries Dirichlet values.
 template <class Src>
 static int run_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src, int maxw, int pb) {
+  GFE_TRY(run_rows_main(ctx, a, src, maxw, pb));
+  if (a.uD && a.b && a.val && a.cell_cols) GFE_TRY(dirichlet_lift(ctx, a, src));
+  return GFE_OK;
+}
+
+template <class Src>
+static int run_rows_main(gfe_ctx* ctx, const RowArgs& a, const Src& src, int maxw, int pb) {
   if (a.nd >= 16 && a.val) {
     if (maxw <= 128) return launch_rows_warp<128>(ctx, a, src, pb);
     if (maxw <= 256) return launch_rows_warp<256>(ctx, a, src, pb);
@@ -283,6 +344,8 @@ static RowArgs row_args(gfe_ctx* ctx, gfe_matrix* A, double* b, bool with_matrix
   a.val = with_matrix ? A->val.as<double>() : nullptr;
   a.b = b;
   a.err = ctx->d_err;
+  a.uD = ctx->lift_uD;
+  a.ndiri = ctx->lift_ndiri;
   return a;
 }
 

@@ -172,15 +172,111 @@ class Triangulation:
         return self.model.num_cells()
 
 
+def facet_axis(D: int, lf: int) -> tuple[int, int]:
+    """Normal axis and side (0 lower, 1 upper) of local facet lf of the D-cube in Gridap's
+    face order: the facets come by normal axis from the last to the first, lower side first
+    (3-D: z-, z+, y-, y+, x-, x+; 2-D: y-, y+, x-, x+)."""
+    return D - 1 - lf // 2, lf & 1
+
+
+class BoundaryTriangulation:
+    """BoundaryTriangulation(model; tags) (Geometry/BoundaryTriangulations.jl:174-208): the
+    boundary facets of a Cartesian model whose entity one of `tags` lists (None: all boundary
+    facets), in ascending facet id. Facet ids are numbered first-touch over the cells
+    (Geometry/GridTopologies.jl:1184-1240), so a boundary facet, which has one cell, comes in
+    (owner cell, local facet) order; its entity is the local facet's position in the n-cube
+    face list (Geometry/CartesianDiscreteModels.jl:215-240).
+
+    facet_cells: owner cell of each facet (0-based); facet_lfaces: its local facet (0-based)."""
+
+    def __init__(self, model: CartesianDiscreteModel, tags=None):
+        if isinstance(model, SimplexDiscreteModel):
+            raise NotImplementedError("boundary terms are provided on hexahedral Cartesian models")
+        self.model = model
+        D = model.dim
+        part = np.asarray(model.partition, np.int64)
+        nc = int(np.prod(part))
+        c = np.arange(nc, dtype=np.int64)
+        stride = np.concatenate([[1], np.cumprod(part)[:-1]])
+        idx = (c[:, None] // stride[None, :]) % part[None, :]
+        offset = 4 if D == 2 else 20  # faces of lower dimension in the n-cube face list
+        labels = model.get_face_labeling()
+        if tags is None:
+            sel = set(labels.tag_entities[labels._tag_index("boundary")])
+        else:
+            sel = set()
+            for t in ([tags] if isinstance(tags, (str, int, np.integer)) else tags):
+                sel |= set(labels.tag_entities[labels._tag_index(t)])
+        mask = np.zeros((nc, 2 * D), dtype=bool)
+        for lf in range(2 * D):
+            ax, side = facet_axis(D, lf)
+            if offset + lf + 1 in sel:
+                mask[:, lf] = idx[:, ax] == (0 if side == 0 else part[ax] - 1)
+        cells, lfaces = np.nonzero(mask)  # row-major: (cell, local facet) order
+        self.facet_cells = np.ascontiguousarray(cells, dtype=np.int32)
+        self.facet_lfaces = np.ascontiguousarray(lfaces, dtype=np.int32)
+
+    def num_cells(self) -> int:
+        return int(self.facet_cells.shape[0])
+
+    def facet_points(self, s: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """Facet points s (npoints x D-1, facet reference coordinates) in every facet's owner
+        cell: reference-cell coordinates (nfacets x npoints x D; the facet's spanned axes in
+        increasing order carry s, the normal axis is fixed at the facet's side) and physical
+        coordinates through the owner cell's Q1 map (glue.tface_to_mface_map and
+        get_cell_map of Geometry/BoundaryTriangulations.jl)."""
+        model = self.model
+        D = model.dim
+        s = np.asarray(s, np.float64).reshape(-1, D - 1)
+        nv = 2 ** D
+        ref = np.empty((self.num_cells(), s.shape[0], D))
+        phys = np.empty_like(ref)
+        X = model.node_coords[model.cell_node_ids[self.facet_cells] - 1]  # (nf, nv, D)
+        for lf in range(2 * D):
+            ax, side = facet_axis(D, lf)
+            xi = np.empty((s.shape[0], D))
+            xi[:, ax] = side
+            xi[:, [d for d in range(D) if d != ax]] = s
+            phi = np.ones((xi.shape[0], nv))
+            for a in range(nv):
+                for d in range(D):
+                    phi[:, a] *= xi[:, d] if (a >> d) & 1 else 1 - xi[:, d]
+            sel = self.facet_lfaces == lf
+            ref[sel] = xi
+            phys[sel] = np.einsum("qa,fad->fqd", phi, X[sel])
+        return ref, phys
+
+    def get_facet_normal(self) -> np.ndarray:
+        """Outward unit normal of every facet (nfacets x D); the box's facets are flat."""
+        D = self.model.dim
+        n = np.zeros((self.num_cells(), D))
+        for lf in range(2 * D):
+            ax, side = facet_axis(D, lf)
+            n[self.facet_lfaces == lf, ax] = 1.0 if side else -1.0
+        return n
+
+    get_normal_vector = get_facet_normal
+
+
+Boundary = BoundaryTriangulation
+
+
 class Measure:
     """Measure(trian, degree): tensor-product Gauss-Legendre of the given degree
-    (ReferenceFEs/Quadratures.jl:157-182)."""
+    (ReferenceFEs/Quadratures.jl:157-182), on the cells of a Triangulation or on the facets of
+    a BoundaryTriangulation."""
 
-    def __init__(self, trian: Triangulation, degree: int):
+    def __init__(self, trian, degree: int):
         self.trian = trian
         self.degree = int(degree)
 
+    @property
+    def on_boundary(self) -> bool:
+        return isinstance(self.trian, BoundaryTriangulation)
+
     def num_points(self) -> int:
+        if self.on_boundary:
+            return (self.degree // 2 + 1) ** (self.trian.model.dim - 1)
         if isinstance(self.trian.model, SimplexDiscreteModel):
             if self.degree not in (4, 5):
                 raise NotImplementedError("tet quadrature of degree 4 or 5 is provided")

@@ -214,18 +214,63 @@ typedef struct gfe_problem {
   int32_t precision;    /* GFE_PREC_*: arithmetic of the cell integrals (scatter stays FP64);
                            FP32 on Q2 uses the tensor cores (TF32 operands, FP32 accumulate,
                            FP64 Jacobians) */
+  /* Dirichlet data of the trial space (TrialFESpace(V, u_D)): the value of Dirichlet dof -k
+     at dirichlet_values[k-1], host or device; NULL (or ndirichlet = 0) for u_D = 0. With it,
+     every cell (and facet) vector receives the lift  b_i -= sum_j A_ij u_D_j  over the cell's
+     Dirichlet columns j before it is added (AttachDirichletMap, CellData/AttachDirichlet.jl:
+     59-110, applied per triangulation in FESpaces/Assemblers.jl:525-542). */
+  const double* dirichlet_values;
+  int64_t ndirichlet;
 } gfe_problem;
 
 /* Integrates the recognised bilinear and linear forms over every cell and assembles them
  * into A (pattern from gfe_symbolic_loop_matrix over problem->cell_dof_ids) and b (nfree
- * entries, overwritten). A or b may be NULL to skip one. Dirichlet values are zero, so the
- * lift of AttachDirichlet leaves b unchanged.
+ * entries, overwritten). A or b may be NULL to skip one. With problem->dirichlet_values the
+ * cell vectors carry the Dirichlet lift (b_i -= sum_j K_ij u_D_j); without, u_D = 0 and the
+ * lift leaves b unchanged.
  * Replaces the cell-array evaluation that Gridap's numeric loops trigger
  * (CellData/CellQuadratures.jl:138-170, Fields/FieldsInterfaces.jl:708-720,
  * Fields/ApplyOptimizations.jl:293-310) together with numeric_loop_matrix_and_vector!
  * (FESpaces/SparseMatrixAssemblers.jl:365-405). */
 int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* problem, gfe_matrix* A,
                                    double* b);
+
+/* ---- assembly: boundary terms (Neumann, Nitsche, Robin) ---------------------------------- */
+/* Boundary integrals over facets of a Cartesian box, scalar Q1/Q2 (problem: dim, reffe,
+ * partition, domain, cell_dof_ids, nd, nfree). The facets lie on the box `domain` with the
+ * partition's spacing (also for a Cartesian model whose interior nodes are jittered, as
+ * boundary nodes stay in place). Facet f belongs to cell facet_cells[f] (0-based) as its
+ * local facet facet_lfaces[f] (0-based, Gridap's face order of the D-cube: z-, z+, y-, y+,
+ * x-, x+ in 3-D; y-, y+, x-, x+ in 2-D); facets are added in the given order, each with its
+ * owner cell's dof ids (Gridap's BoundaryTriangulation order is ascending facet id). The
+ * facet rule is the tensor Gauss rule of `degree` on the facet, n the outward unit normal.
+ * Replace the cell arrays of a BoundaryTriangulation measure
+ * (Geometry/BoundaryTriangulations.jl:13-35,150-205, CellData/CellQuadratures.jl:138-170)
+ * and their numeric loops (FESpaces/SparseMatrixAssemblers.jl:214-316). */
+enum {
+  GFE_BOP_VALUE = 0,       /* test function v */
+  GFE_BOP_NORMAL_GRAD = 1  /* n . grad(v) */
+};
+
+/* b += int_Gamma g op(v) dGamma. g is constant (GFE_SRC_CONST, 1 value) or given at the
+ * facet's Gauss points (GFE_SRC_QPOINT, nfacets * npoints values, facet by facet; facet
+ * coordinates = the spanned axes in increasing order, the first fastest). test_op is a
+ * GFE_BOP_*. b (nfree entries, host or device) is added to. */
+int gfe_assemble_boundary_vector(gfe_ctx* ctx, const gfe_problem* problem, int64_t nfacets,
+                                 const int32_t* facet_cells, const int32_t* facet_lfaces,
+                                 int32_t degree, int32_t test_op, int32_t source_kind,
+                                 const double* source, int64_t source_len, double* b);
+
+/* A += int_Gamma c0 v u + c1 v (n.grad u) + c2 (n.grad v) u + c3 (n.grad v)(n.grad u) dGamma,
+ * coefs = (c0, c1, c2, c3) constants (Nitsche: (gamma/h, -1, -1, 0); Robin: (alpha, 0, 0, 0)).
+ * A is an assembled matrix whose pattern covers the owner cells' dof pairs (the volume
+ * pattern does); its values are added to in facet order per entry. With
+ * problem->dirichlet_values and b (nfree entries, host or device, may be NULL), b receives
+ * the facets' Dirichlet lift b_i -= sum_j M_ij u_D_j. */
+int gfe_assemble_boundary_matrix(gfe_ctx* ctx, const gfe_problem* problem, gfe_matrix* A,
+                                 double* b, int64_t nfacets, const int32_t* facet_cells,
+                                 const int32_t* facet_lfaces, int32_t degree,
+                                 const double* coefs);
 
 /* ---- linear solve ------------------------------------------------------------------------ */
 enum { GFE_SOLVER_CG = 0, GFE_SOLVER_IR_CG = 1, GFE_SOLVER_MIXED_CG = 2 };

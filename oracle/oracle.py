@@ -476,3 +476,160 @@ def extrusion_faces(extrusion):
         out.append([[ids[s] for s in nfaces(f[0], f[1]) if dim(s) == 0]
                     for f in allf if dim(f) == d])
     return out
+
+
+# ---- boundary (Neumann) terms --------------------------------------------------------------
+def boundary_facets(partition, tags=None):
+    """(owner cell, local facet) of the boundary facets of a Cartesian model selected by
+    `tags` (None: every boundary facet), in Gridap's BoundaryTriangulation order.
+
+    Facet ids come from the first-touch numbering of the grid topology: cells in order, the
+    local faces of each cell in n-cube order, a new id for every face not met before
+    (Geometry/GridTopologies.jl:1184-1240); a boundary facet has one cell around, so its id
+    order is the (cell, local facet) order. BoundaryTriangulation keeps findall(mask), i.e.
+    ascending ids (Geometry/BoundaryTriangulations.jl:174-203). The entity of a boundary
+    facet is its local facet's position in the n-cube face list
+    (Geometry/CartesianDiscreteModels.jl:215-240), and a tag selects the facets whose entity it
+    lists. Normal axis and side are read off the n-cube faces: the axis the face does not
+    extend along, and the anchor's coordinate on it."""
+    D = len(partition)
+    ext, anc = ncube_faces(D)
+    fids = [k for k in range(ext.shape[0]) if int(ext[k].sum()) == D - 1]
+    names, ents = cartesian_tags(D)
+    if tags is None:
+        sel = set(ents[names.index("boundary")])
+    else:
+        sel = set()
+        for t in ([tags] if isinstance(tags, (str, int)) else tags):
+            sel |= set(ents[t - 1] if isinstance(t, int) else ents[names.index(t)])
+    axes = [(int(np.nonzero(ext[k] == 0)[0][0]), int(anc[k][np.nonzero(ext[k] == 0)[0][0]]))
+            for k in fids]
+    cells, lfaces = [], []
+    nc = int(np.prod(partition))
+    stride = [int(np.prod(partition[:d])) for d in range(D)]
+    for c in range(nc):
+        idx = [(c // stride[d]) % partition[d] for d in range(D)]
+        for lf, k in enumerate(fids):
+            ax, side = axes[lf]
+            if idx[ax] == (0 if side == 0 else partition[ax] - 1) and (k + 1) in sel:
+                cells.append(c)
+                lfaces.append(lf)
+    return np.array(cells, np.int32), np.array(lfaces, np.int32)
+
+
+def facet_arrays(coords, cell_nodes, order, facet_cells, facet_lfaces, degree):
+    """Per facet, at the Gauss points of the facet polytope (Quadrature(QUAD/SEGMENT,
+    degree)): the owner cell's shape values phi (nq, nn), their outward normal derivatives
+    dn (nq, nn), the integration factors w_q |J_q| (nq), the physical points (nq, D) and
+    the unit normals (nq, D).
+
+    The facet points are mapped into the owner cell through the facet's vertex list (the
+    n-cube face-to-vertex table; the reference face map interpolates those vertices'
+    reference coordinates). |J| = sqrt(det(JᵀJ)) with J the facet map's Jacobian from the
+    facet's physical vertices. Gradients are pushed forward with the owner cell's Q1 map
+    (∇φ = J_c⁻ᵀ ∇_ξ φ) and the normal is the unit vector orthogonal to the facet's tangents,
+    pointing away from the cell's centre (get_facet_normal)."""
+    D = coords.shape[1]
+    fverts = extrusion_faces((1,) * D)[D - 1]
+    refv = np.array([[(v >> d) & 1 for d in range(D)] for v in range(2 ** D)], np.float64)
+    sx, sw = tensor_quadrature(D - 1, degree)
+    sphi, sdphi = q1_shapes(D - 1, sx)
+    out = []
+    for f in range(facet_cells.shape[0]):
+        c, lf = int(facet_cells[f]), int(facet_lfaces[f])
+        vs = [v - 1 for v in fverts[lf]]
+        cellpts = sphi @ refv[vs]
+        Xc = coords[cell_nodes[c] - 1]  # owner cell vertices
+        X = Xc[vs]
+        xq = sphi @ X
+        if order == 1:
+            phi, dphi = q1_shapes(D, cellpts)
+        else:
+            phi, dphi = q2_shapes(D, cellpts)
+        _, gdphi = q1_shapes(D, cellpts)  # geometry map
+        centre = Xc.mean(axis=0)
+        dn = np.zeros_like(phi)
+        wm = np.zeros(sw.shape[0])
+        nrm = np.zeros((sw.shape[0], D))
+        for q in range(sw.shape[0]):
+            T = sdphi[q].T @ X  # (D-1, D) tangents
+            wm[q] = sw[q] * math.sqrt(np.linalg.det(T @ T.T))
+            if D == 2:
+                n = np.array([T[0, 1], -T[0, 0]])
+            else:
+                n = np.cross(T[0], T[1])
+            n /= np.linalg.norm(n)
+            if np.dot(n, xq[q] - centre) < 0:
+                n = -n
+            nrm[q] = n
+            Jc = gdphi[q].T @ Xc  # (D, D): Jc[k, l] = d x_l / d xi_k
+            grad = np.linalg.solve(Jc, dphi[q].T)  # (D, nn) physical gradients
+            dn[q] = n @ grad
+        out.append((phi, dn, wm, xq, nrm))
+    return out
+
+
+def boundary_vector(partition, coords, cell_nodes, cell_dofs, order, facet_cells,
+                    facet_lfaces, degree, g, nfree, test_op=0):
+    """Gridap's assemble_vector of ∫ g v dΓ (test_op 0) or ∫ g (n⋅∇v) dΓ (test_op 1) on a
+    BoundaryTriangulation: the facet vector r_i = Σ_q g_q op(φ_i)(q) w_q |J_q| in the order of
+    Fields/FieldsInterfaces.jl:660-670, added with the owner cell's dof ids in facet order
+    (FESpaces/SparseMatrixAssemblers.jl:287-316). g: a number or a callable on physical
+    points (npoints, D); returns (b, g values at the points, facet by facet)."""
+    arrs = facet_arrays(coords, cell_nodes, order, facet_cells, facet_lfaces, degree)
+    nf = facet_cells.shape[0]
+    vecs = np.zeros((nf, cell_dofs.shape[1]))
+    nq = arrs[0][2].shape[0] if nf else 0
+    gvals = np.zeros((nf, nq))
+    for f, (phi, dn, wm, xq, _) in enumerate(arrs):
+        op = phi if test_op == 0 else dn
+        gq = (np.full(nq, float(g)) if not callable(g)
+              else np.asarray(g(xq), np.float64).reshape(-1))
+        gvals[f] = gq
+        for q in range(nq):
+            for i in range(op.shape[1]):
+                vecs[f, i] += gq[q] * op[q, i] * wm[q]
+    b = assemble_vector(cell_dofs[facet_cells], vecs, nfree)
+    return b, gvals
+
+
+def boundary_matrix(coords, cell_nodes, cell_dofs, order, facet_cells, facet_lfaces, degree,
+                    coefs, nfree, uD=None):
+    """Dense sum of the facet matrices of ∫ c0 v u + c1 v (n⋅∇u) + c2 (n⋅∇v) u
+    + c3 (n⋅∇v)(n⋅∇u) dΓ over the free rows and columns, and the Dirichlet lift
+    -Σ_j M_ij u_D_j of the Dirichlet columns (AttachDirichletMap, CellData/AttachDirichlet.jl)."""
+    arrs = facet_arrays(coords, cell_nodes, order, facet_cells, facet_lfaces, degree)
+    K = np.zeros((nfree, nfree))
+    lift = np.zeros(nfree)
+    c0, c1, c2, c3 = coefs
+    for f, (phi, dn, wm, _, _) in enumerate(arrs):
+        M = np.zeros((phi.shape[1], phi.shape[1]))
+        for q in range(wm.shape[0]):
+            M += (c0 * np.outer(phi[q], phi[q]) + c1 * np.outer(phi[q], dn[q])
+                  + c2 * np.outer(dn[q], phi[q]) + c3 * np.outer(dn[q], dn[q])) * wm[q]
+        ids = cell_dofs[facet_cells[f]]
+        for i, r in enumerate(ids):
+            if r <= 0:
+                continue
+            for j, s in enumerate(ids):
+                if s > 0:
+                    K[r - 1, s - 1] += M[i, j]
+                elif uD is not None:
+                    lift[r - 1] -= M[i, j] * uD[-s - 1]
+    return K, lift
+
+
+def dirichlet_lift(cell_dofs, cellmats, uD, nfree):
+    """-Σ_j K_ij u_D_j over every cell's Dirichlet columns, added by row (the vector part of
+    AttachDirichletMap, CellData/AttachDirichlet.jl:59-110). cellmats[c][i][j]: i test row."""
+    b = np.zeros(nfree)
+    for c in range(cell_dofs.shape[0]):
+        ids = cell_dofs[c]
+        neg = ids < 0
+        if not neg.any():
+            continue
+        lv = -(cellmats[c][:, neg] @ uD[-ids[neg] - 1])
+        for i, r in enumerate(ids):
+            if r > 0:
+                b[r - 1] += lv[i]
+    return b

@@ -195,6 +195,23 @@ def main(ref: pathlib.Path):
         "note": "orbit tables expanded, mapped from [-1,1] to the unit tet, weights scaled "
                 "to the tet measure 1/6 (Quadratures.jl _weightcoords_to_coord_weights)"}
 
+    # ---- boundary facets of a 2x2 Cartesian model: order, facet-to-cell map, physical
+    # points and normals at the facet points s = 0.25, 0.75 -----------------------------------
+    f = "test/GeometryTests/BoundaryTriangulationsTests.jl"
+    L = (ref / f).read_text().splitlines()
+    i = find(L, r"^model = CartesianDiscreteModel\(domain,partition\)")
+    i = find(L, r"^btrian = BoundaryTriangulation\(model\)$", i)
+    vals = []
+    k = i
+    for _ in range(3):
+        k = find(L, r"^r = Vector\{Point\{2,Float64\}\}\[", k + 1)
+        txt, j = collect_bracketed(L, k, "V")
+        vals.append((k, j, julia_array(txt)))
+    kats["boundary_facets_2x2"] = {
+        "source": f"{f}:{vals[0][0] + 1}-{vals[2][1] + 1}", "domain": [0, 4, 0, 4],
+        "partition": [2, 2], "s": [0.25, 0.75], "cell_points": vals[0][2],
+        "physical_points": vals[1][2], "normals": vals[2][2]}
+
     out = HERE / "gridap_kats.json"
     out.write_text(json.dumps(kats, indent=1) + "\n")
     print(f"wrote {out}")

@@ -182,3 +182,60 @@ def test_elasticity_form_recognition(gg):
     assert kind == "body_force" and np.array_equal(f, [0, 0, -1])
     with pytest.raises(NotImplementedError):
         classify_bilinear(gg.inner(gg.ε(v), gg.ε(u)))
+
+
+def test_boundary_facets_kat_and_order(gg, orc, kats):
+    """The product's BoundaryTriangulation reproduces Gridap's 2x2 facet KAT and the oracle's
+    facet order for tag selections in 2-D and 3-D."""
+    k = kats["boundary_facets_2x2"]
+    m = gg.CartesianDiscreteModel(k["domain"], k["partition"])
+    G = gg.BoundaryTriangulation(m)
+    ref, phys = G.facet_points(np.array(k["s"])[:, None])
+    np.testing.assert_array_equal(ref, k["cell_points"])
+    np.testing.assert_allclose(phys, k["physical_points"], atol=1e-15)
+    np.testing.assert_array_equal(G.get_facet_normal() + 0.0, np.array(k["normals"])[:, 0] + 0.0)
+    for part, tags in (((3, 2), None), ((3, 2), "tag_7"), ((4, 3), ["tag_5", 8]),
+                       ((2, 3, 2), None), ((2, 3, 2), ["tag_21", "tag_24", "tag_26"]),
+                       ((3, 1, 2), "boundary"), ((2, 2, 2), "interior")):
+        m = gg.CartesianDiscreteModel((0, 1) * len(part), part)
+        G = gg.BoundaryTriangulation(m, tags=tags)
+        c, l = orc.boundary_facets(part, tags)
+        assert np.array_equal(G.facet_cells, c) and np.array_equal(G.facet_lfaces, l)
+
+
+def test_boundary_forms_and_facet_points(gg, orc):
+    """Linear forms split into the volume source and the ∫ g v dΓ terms; the facet Gauss
+    points handed to a callable g come in the oracle's order (facet by facet, first facet
+    coordinate fastest), on a jittered model too."""
+    from importlib import import_module
+    A = import_module(gg.__name__ + ".assembly")
+    part = (3, 2, 2)
+    nn = int(np.prod(np.array(part) + 1))
+    jit = 0.05 * np.random.default_rng(2).standard_normal((nn, 3))
+    m = gg.CartesianDiscreteModel((0, 1, 0, 2, 0, 1), part, node_jitter=jit)
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="tag_01")
+    dO = gg.Measure(gg.Triangulation(m), 2)
+    G = gg.BoundaryTriangulation(m, tags=["tag_23", "tag_26"])
+    dG = gg.Measure(G, 4)
+    fo = A._forms(None, lambda v: gg.integrate(2.0 * v, dO) + gg.integrate(3.0 * v, dG), V, V)
+    assert fo.source == 2.0 and fo.boundary == [(dG, [(0, 3.0, None)])]
+    fo = A._forms(None, lambda v: gg.integrate(3.0 * v, dG), V, V)
+    assert fo.source is None and len(fo.boundary) == 1
+    # Nitsche terms: (γ/h) v u - v (n⋅∇u) - (n⋅∇v) u and (γ/h) v g - (n⋅∇v) g
+    n = gg.get_normal_vector(G)
+    g = lambda x: x[:, 0]  # noqa: E731
+    fo = A._forms(lambda u, v: gg.integrate(gg.inner(gg.grad(v), gg.grad(u)), dO)
+                  + gg.integrate(40.0 * v * u - v * gg.inner(n, gg.grad(u))
+                                 - gg.inner(n, gg.grad(v)) * u, dG),
+                  lambda v: gg.integrate(40.0 * v * g - gg.inner(n, gg.grad(v)) * g, dG), V, V)
+    assert fo.boundary_mat == [(dG, (40.0, -1.0, -1.0, 0.0))]
+    assert fo.boundary == [(dG, [(0, 40.0, g), (1, -1.0, g)])]
+    with pytest.raises(NotImplementedError):  # a gradient term that is not along n
+        A._forms(lambda u, v: gg.integrate(gg.inner(gg.grad(v), gg.grad(u)), dO)
+                 + gg.integrate(gg.inner(gg.grad(v), gg.grad(u)), dG), None, V, V)
+    g = lambda x: x[:, 0] + 10 * x[:, 1] + 100 * x[:, 2]  # noqa: E731
+    xq = A._facet_qpoints(G, 4)
+    assert xq.shape == (G.num_cells(), dG.num_points(), 3)
+    _, gvals = orc.boundary_vector(part, m.node_coords, m.cell_node_ids, V.cell_dof_ids, 1,
+                                   G.facet_cells, G.facet_lfaces, 4, g, V.num_free_dofs())
+    np.testing.assert_allclose(g(xq.reshape(-1, 3)), gvals.reshape(-1), rtol=1e-14, atol=1e-14)

@@ -284,3 +284,64 @@ def test_elasticity_p2_invariants(orc):
     assert abs(u @ (A1 @ u) - energy) < 1e-12 * energy
     # body force: total load = int f over the box
     assert abs(P1["b"].reshape(-1)[comp == 2].sum() + 1.0) < 1e-14
+
+
+def test_boundary_facets_2x2_kat(orc, kats):
+    """Gridap's BoundaryTriangulation(model) on a 2x2 model of (0,4)^2: facet order, facet
+    points in the owner cell and physical points at s = 0.25, 0.75
+    (test/GeometryTests/BoundaryTriangulationsTests.jl)."""
+    k = kats["boundary_facets_2x2"]
+    part = tuple(k["partition"])
+    cells, lfaces = orc.boundary_facets(part)
+    coords, cell_nodes, _ = orc.cartesian_model(k["domain"], part)
+    fverts = orc.extrusion_faces((1, 1))[1]
+    refv = np.array([[(v >> d) & 1 for d in range(2)] for v in range(4)], np.float64)
+    s = np.array(k["s"])[:, None]
+    sphi, _ = orc.q1_shapes(1, s)
+    assert len(cells) == len(k["cell_points"]) == 8
+    for f in range(8):
+        vs = [v - 1 for v in fverts[lfaces[f]]]
+        np.testing.assert_allclose(sphi @ refv[vs], k["cell_points"][f], atol=0)
+        X = coords[cell_nodes[cells[f], vs] - 1]
+        np.testing.assert_allclose(sphi @ X, k["physical_points"][f], atol=1e-15)
+    arrs = orc.facet_arrays(coords, cell_nodes, 1, cells, lfaces, 2)
+    for f in range(8):
+        np.testing.assert_allclose(arrs[f][4], k["normals"][f], atol=1e-15)
+
+
+def test_facet_normal_derivatives(orc):
+    """n⋅∇φ from the oracle's facet arrays equals the analytic outward derivative of the Q1
+    and Q2 shape functions on an undistorted box (sum over the dofs of n⋅∇φ is 0, and for
+    φ = 1 - x on the x = 0 facet, n⋅∇φ = +1/h)."""
+    part, dom = (3, 2), (0, 3, 0, 1)
+    coords, cell_nodes, _ = orc.cartesian_model(dom, part)
+    cells, lfaces = orc.boundary_facets(part)
+    for order in (1, 2):
+        arrs = orc.facet_arrays(coords, cell_nodes, order, cells, lfaces, 4)
+        for phi, dn, wm, xq, n in arrs:
+            np.testing.assert_allclose(dn.sum(axis=1), 0.0, atol=1e-12)
+            np.testing.assert_allclose(phi.sum(axis=1), 1.0, atol=1e-14)
+    arrs = orc.facet_arrays(coords, cell_nodes, 1, cells, lfaces, 2)
+    f = [i for i in range(len(cells)) if cells[i] == 0 and lfaces[i] == 2][0]  # x- of cell 0
+    np.testing.assert_allclose(arrs[f][1][:, 0] + arrs[f][1][:, 2], 1.0, atol=1e-14)
+
+
+def test_boundary_vector_measures(orc):
+    """∫ 1 v dΓ summed over the dofs is the measure of Γ; the facet sizes of a jittered model
+    are those of the box (its boundary nodes stay in place)."""
+    for part, dom in (((3, 2), (0, 2, 0, 1)), ((2, 3, 2), (0, 1, 0, 2, 0, 3))):
+        D = len(part)
+        coords, cell_nodes, _ = orc.cartesian_model(dom, part)
+        rng = np.random.default_rng(3)
+        coords = orc.jitter_interior(part, coords, 0.05 * rng.standard_normal(coords.shape))
+        ids = np.arange(cell_nodes.size, dtype=np.int32).reshape(cell_nodes.shape) + 1
+        for tags, meas in ((None, None), ("tag_26" if D == 3 else "tag_8", None)):
+            fc, fl = orc.boundary_facets(part, tags)
+            b, _ = orc.boundary_vector(part, coords, cell_nodes, ids, 1, fc, fl, 2, 1.0,
+                                       ids.size)
+            L = [dom[2 * d + 1] - dom[2 * d] for d in range(D)]
+            if tags is None:
+                want = 2 * sum(np.prod([L[e] for e in range(D) if e != d]) for d in range(D))
+            else:
+                want = np.prod(L[1:])
+            assert abs(b.sum() - want) <= 1e-13 * want

@@ -18,14 +18,18 @@ from .assembly import (AffineFEOperator, Context, DeviceMatrix, SparseMatrixAsse
                        prepare_problem, symbolic_loop_matrix)
 from .celldata import (CellField, DomainContribution, NodalField, SinSum, dot, get_fe_basis,
                        get_normal_vector, get_trial_fe_basis, grad, gradient, inner, integrate,
-                       isotropic_stress, symmetric_gradient, ε)
+                       isotropic_stress, PolynomialCoefficient, PowerLawFlux,
+                       symmetric_gradient, ε)
 from .fespaces import (FEFunction, FESpace, ReferenceFE, TrialFESpace, get_cell_dof_ids,
                        lagrangian, num_free_dofs)
 from .geometry import (Boundary, BoundaryTriangulation, CartesianDiscreteModel, FaceLabeling,
                        Measure, SimplexDiscreteModel, Triangulation, simplexify)
 from .batch import BatchedPoissonProblems
+from .nonlinear import (FEOperator, NewtonRaphsonSolver, NLSolver, NonlinearFESolver,
+                        solve_nonlinear_)
 from .learned import LearnedBlockPreconditioner
-from .solvers import (AffineOperator, CGSolver, FCGSolver, IRCGSolver, LinearFESolver,
+from .solvers import (AffineOperator, BiCGStabSolver, CGSolver, FCGSolver, IRCGSolver,
+                      LinearFESolver,
                       LinearSolver, MixedCGSolver, solve_matrix_,
                       SolveReport, solve,
                       solve_, numerical_setup, numerical_setup_, symbolic_setup)

@@ -26,13 +26,14 @@ GFE_ERR_NONFINITE = 8
 
 GFE_REFFE_Q1, GFE_REFFE_Q2 = 1, 2
 GFE_GEOM_CARTESIAN, GFE_GEOM_NODAL = 0, 1
-GFE_FORM_DIFFUSION, GFE_FORM_ELASTICITY = 1, 2
+GFE_FORM_DIFFUSION, GFE_FORM_ELASTICITY, GFE_FORM_QUASILINEAR = 1, 2, 3
 GFE_REFFE_Q1, GFE_REFFE_Q2, GFE_REFFE_P2_TET = 1, 2, 3
 GFE_COEF_ONE, GFE_COEF_CONST, GFE_COEF_CELL = 0, 1, 2
 GFE_SRC_NONE, GFE_SRC_CONST, GFE_SRC_NODAL, GFE_SRC_QPOINT, GFE_SRC_SINSUM = 0, 1, 2, 3, 4
 GFE_BOP_VALUE, GFE_BOP_NORMAL_GRAD = 0, 1
+GFE_LAW_POLY, GFE_LAW_POWER = 0, 1
 GFE_PREC_FP64, GFE_PREC_FP32 = 0, 1
-GFE_SOLVER_CG, GFE_SOLVER_IR_CG, GFE_SOLVER_MIXED_CG = 0, 1, 2
+GFE_SOLVER_CG, GFE_SOLVER_IR_CG, GFE_SOLVER_MIXED_CG, GFE_SOLVER_BICGSTAB = 0, 1, 2, 3
 GFE_PC_NONE, GFE_PC_JACOBI = 0, 1
 GFE_KT_SPMV64, GFE_KT_SPMV32, GFE_KT_ASSEMBLE, GFE_KT_RESIDUAL64, GFE_KT_ELEMENT = 0, 1, 2, 3, 4
 GFE_KT_PRECOND, GFE_KT_VECTOR = 5, 6
@@ -56,6 +57,7 @@ class Problem(C.Structure):
         ("form", C.c_int32), ("coef_kind", C.c_int32), ("coef", C.c_void_p),
         ("source_kind", C.c_int32), ("source", C.c_void_p), ("source_len", C.c_int64),
         ("precision", C.c_int32), ("dirichlet_values", C.c_void_p), ("ndirichlet", C.c_int64),
+        ("state", C.c_void_p), ("law", C.c_int32), ("law_params", C.c_double * 4),
     ]
 
 

@@ -340,3 +340,175 @@ def classify_boundary_linear(expr):
             raise NotImplementedError("each boundary linear term needs v")
         out.append((test, c, data))
     return out
+
+
+# ---- quasilinear (nonlinear) integrands ------------------------------------------------------
+class _FEState(_Expr):
+    """The FE function u a residual or Jacobian is evaluated at (FEOperator's uh)."""
+
+    def __init__(self, fun):
+        self.fun = fun
+
+
+class PowerLawFlux:
+    """flux(∇u) = (eps2 + |∇u|²)^((p-2)/2) ∇u — the p-Laplacian flux |∇u|^(p-2) ∇u for
+    eps2 = 0 (test/GridapTests/PLaplacianTests.jl). flux(grad(u)) builds the residual's
+    integrand factor, flux.derivative(grad(du), grad(u)) the Jacobian's (Gridap's dflux)."""
+
+    def __init__(self, p: float, eps2: float = 0.0):
+        self.p = float(p)
+        self.eps2 = float(eps2)
+
+    def __call__(self, gradu):
+        return _Flux(self, gradu)
+
+    def derivative(self, graddu, gradu):
+        return _DFlux(self, graddu, gradu)
+
+
+class PolynomialCoefficient:
+    """α(u) = c0 + c1 u + c2 u² for quasilinear diffusion ∫ α(u) ∇v⋅∇u; α.derivative(u) is
+    α'(u) for the Jacobian term ∫ α'(u) du ∇v⋅∇u."""
+
+    def __init__(self, c0: float, c1: float = 0.0, c2: float = 0.0):
+        self.c = (float(c0), float(c1), float(c2))
+
+    def __call__(self, u):
+        return _Coef(self, u)
+
+    def derivative(self, u):
+        return _DCoef(self, u)
+
+
+class _Flux(_Expr):
+    def __init__(self, law, gradu):
+        self.law, self.gradu = law, gradu
+
+
+class _DFlux(_Expr):
+    def __init__(self, law, graddu, gradu):
+        self.law, self.graddu, self.gradu = law, graddu, gradu
+
+
+class _Coef(_Expr):
+    def __init__(self, law, u):
+        self.law, self.u = law, u
+
+
+class _DCoef(_Expr):
+    def __init__(self, law, u):
+        self.law, self.u = law, u
+
+
+def _is_grad_of(e, pred):
+    return isinstance(e, _Grad) and pred(e.arg)
+
+
+def _is_state(e):
+    return isinstance(e, _FEState)
+
+
+def _is_test(e):
+    return isinstance(e, _Basis) and not e.trial
+
+
+def _is_trial(e):
+    return isinstance(e, _Basis) and e.trial
+
+
+def _inner_pair(e, pa, pb):
+    """inner(a, b) with pa(a) and pb(b) in either order."""
+    if not isinstance(e, _Inner):
+        return False
+    return (pa(e.a) and pb(e.b)) or (pa(e.b) and pb(e.a))
+
+
+def _scale_and_rest(mono):
+    """Splits a monomial into its numeric scale, per-cell CellFields and other factors."""
+    s, cells, rest = 1.0, [], []
+    for f in mono:
+        if isinstance(f, (int, float, np.floating, np.integer)):
+            s *= float(f)
+        elif isinstance(f, CellField):
+            cells.append(f)
+        else:
+            rest.append(f)
+    return s, cells, rest
+
+
+class QuasilinearForm:
+    """A recognised residual  ∫ κ α(u, ∇u) ∇v⋅∇u - f v  (law, κ, f)."""
+
+    def __init__(self, law, scale, cells, source):
+        self.law, self.scale, self.cells, self.source = law, scale, cells, source
+
+
+def classify_residual(expr) -> QuasilinearForm:
+    """Recognises  κ ∇v⋅flux(∇u)  or  κ α(u) ∇v⋅∇u  plus an optional  -f v  term."""
+    law = None
+    scale, cells, source = 1.0, [], None
+    grad_state = lambda e: _is_grad_of(e, _is_state)  # noqa: E731
+    grad_test = lambda e: _is_grad_of(e, _is_test)  # noqa: E731
+    for mono in _monomials(expr):
+        s, cf, rest = _scale_and_rest(mono)
+        if len(rest) == 1 and _inner_pair(rest[0], grad_test,
+                                          lambda e: isinstance(e, _Flux) and grad_state(e.gradu)):
+            lw = rest[0].a.law if isinstance(rest[0].a, _Flux) else rest[0].b.law
+        elif len(rest) == 2 and any(isinstance(f, _Coef) and _is_state(f.u) for f in rest) and \
+                any(_inner_pair(f, grad_test, grad_state) for f in rest):
+            lw = [f for f in rest if isinstance(f, _Coef)][0].law
+        elif any(_is_test(f) for f in rest) and not cf:
+            data = [f for f in rest if not _is_test(f)]
+            if len(rest) - len(data) != 1 or len(data) > 1 or source is not None:
+                raise NotImplementedError("one source term f*v is provided in a residual")
+            d = data[0] if data else 1.0
+            if isinstance(d, _Expr):
+                raise NotImplementedError("residual source term not recognised")
+            source = (-s, d)  # residual holds -f v: f = -s d
+            continue
+        else:
+            raise NotImplementedError("residual term not recognised (κ ∇v⋅flux(∇u), "
+                                      "κ α(u) ∇v⋅∇u, f v)")
+        if law is not None:
+            raise NotImplementedError("one nonlinear diffusion term is provided")
+        law, scale, cells = lw, s, cf
+    if law is None:
+        raise NotImplementedError("the residual has no nonlinear diffusion term")
+    if len(cells) > 1:
+        raise NotImplementedError("one per-cell coefficient is provided")
+    return QuasilinearForm(law, scale, cells, source)
+
+
+def check_jacobian(expr, form: QuasilinearForm) -> None:
+    """Checks that a user Jacobian is the derivative of the recognised residual's law (the
+    device evaluates that derivative exactly); raises NotImplementedError otherwise."""
+    grad_state = lambda e: _is_grad_of(e, _is_state)  # noqa: E731
+    grad_test = lambda e: _is_grad_of(e, _is_test)  # noqa: E731
+    grad_trial = lambda e: _is_grad_of(e, _is_trial)  # noqa: E731
+    seen = set()
+    for mono in _monomials(expr):
+        s, cf, rest = _scale_and_rest(mono)
+        same = s == form.scale and [c is k for c, k in zip(cf, form.cells)] == [True] * len(cf) \
+            and len(cf) == len(form.cells)
+        law = form.law
+        if isinstance(law, PowerLawFlux) and len(rest) == 1 and _inner_pair(
+                rest[0], grad_test, lambda e: isinstance(e, _DFlux) and e.law is law
+                and grad_trial(e.graddu) and grad_state(e.gradu)) and same:
+            seen.add("dflux")
+        elif isinstance(law, PolynomialCoefficient) and len(rest) == 2 and same and any(
+                isinstance(f, _Coef) and f.law is law and _is_state(f.u) for f in rest) and any(
+                _inner_pair(f, grad_test, grad_trial) for f in rest):
+            seen.add("coef")
+        elif isinstance(law, PolynomialCoefficient) and len(rest) == 3 and same and any(
+                isinstance(f, _DCoef) and f.law is law and _is_state(f.u) for f in rest) and any(
+                _is_trial(f) for f in rest) and any(
+                _inner_pair(f, grad_test, grad_state) for f in rest):
+            seen.add("dcoef")
+        else:
+            raise NotImplementedError("the Jacobian is not the derivative of the residual's law")
+    need = {"dflux"} if isinstance(form.law, PowerLawFlux) else {"coef", "dcoef"}
+    if isinstance(form.law, PolynomialCoefficient) and form.law.c[1] == 0 and \
+            form.law.c[2] == 0:
+        need = {"coef"}
+    if not need <= seen:
+        raise NotImplementedError("the Jacobian misses terms of the residual's derivative")

@@ -296,7 +296,7 @@ extern "C" int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* p
       c->lift_ndiri = 0;
     }
   } lift_reset{ctx};
-  if (A && b && p->dirichlet_values && p->ndirichlet > 0) {
+  if (A && b && p->dirichlet_values && p->ndirichlet > 0 && p->form != GFE_FORM_QUASILINEAR) {
     // nonzero Dirichlet data: the lift needs the matrix entries, so it comes with A and b
     const void* v;
     GFE_TRY(device_view(ctx, p->dirichlet_values, sizeof(double) * (size_t)p->ndirichlet,

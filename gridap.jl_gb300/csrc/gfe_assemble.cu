@@ -299,30 +299,6 @@ __global__ void k_check_finite(const double* __restrict__ v, int64_t n, DevError
 }
 
 // ---- host: reference tables ---------------------------------------------------------------
-static void q1_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
-                      std::vector<double>& dphi) {
-  const int nv = 1 << D;
-  phi.assign((size_t)nq * nv, 0.0);
-  dphi.assign((size_t)nq * nv * D, 0.0);
-  for (int q = 0; q < nq; ++q)
-    for (int a = 0; a < nv; ++a) {
-      double f[3], g[3];
-      for (int d = 0; d < D; ++d) {
-        const bool hi = (a >> d) & 1;
-        f[d] = hi ? qx[q * D + d] : 1.0 - qx[q * D + d];
-        g[d] = hi ? 1.0 : -1.0;
-      }
-      double v = 1.0;
-      for (int d = 0; d < D; ++d) v *= f[d];
-      phi[(size_t)q * nv + a] = v;
-      for (int k = 0; k < D; ++k) {
-        double dv = 1.0;
-        for (int d = 0; d < D; ++d) dv *= (d == k) ? g[d] : f[d];
-        dphi[((size_t)q * nv + a) * D + k] = dv;
-      }
-    }
-}
-
 // Reference tables of a uniform Cartesian cell with sizes h (FP64, same steps as the
 // per-cell integral with Jt = diag(h)).
 static void cartesian_tables(int D, const double* h, int nq, const std::vector<double>& qx,
@@ -493,6 +469,7 @@ __global__ void __launch_bounds__(256)
 // ---- host: fused integrate + assemble -----------------------------------------------------
 int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* d_b) {
   if (p->reffe == GFE_REFFE_P2_TET) return assemble_p2_elasticity(ctx, p, A, d_b);
+  if (p->form == GFE_FORM_QUASILINEAR) return assemble_quasilinear(ctx, p, A, d_b);
   const int D = p->dim;
   if ((p->reffe != GFE_REFFE_Q1 && p->reffe != GFE_REFFE_Q2) || p->ncomp != 1 ||
       p->form != GFE_FORM_DIFFUSION)

@@ -203,6 +203,32 @@ static void gauss01(int n, double* x, double* w) {
   }
 }
 
+// Q1 shape values phi[q][a] and reference gradients dphi[q][a][k] at the points qx[q][D];
+// vertex a has coordinate bit d = (a >> d) & 1.
+void q1_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
+                      std::vector<double>& dphi) {
+  const int nv = 1 << D;
+  phi.assign((size_t)nq * nv, 0.0);
+  dphi.assign((size_t)nq * nv * D, 0.0);
+  for (int q = 0; q < nq; ++q)
+    for (int a = 0; a < nv; ++a) {
+      double f[3], g[3];
+      for (int d = 0; d < D; ++d) {
+        const bool hi = (a >> d) & 1;
+        f[d] = hi ? qx[q * D + d] : 1.0 - qx[q * D + d];
+        g[d] = hi ? 1.0 : -1.0;
+      }
+      double v = 1.0;
+      for (int d = 0; d < D; ++d) v *= f[d];
+      phi[(size_t)q * nv + a] = v;
+      for (int k = 0; k < D; ++k) {
+        double dv = 1.0;
+        for (int d = 0; d < D; ++d) dv *= (d == k) ? g[d] : f[d];
+        dphi[((size_t)q * nv + a) * D + k] = dv;
+      }
+    }
+}
+
 int tensor_quadrature(int D, int degree, std::vector<double>& x, std::vector<double>& w) {
   if (D < 1 || D > 3 || degree < 0 || degree > 60)
     return set_error(GFE_ERR_INVALID_ARGUMENT, "quadrature: bad dim %d / degree %d", D, degree);

@@ -245,8 +245,15 @@ void timer_release(gfe_ctx* ctx);
 
 // host set-up (gfe_host.cpp)
 int tensor_quadrature(int D, int degree, std::vector<double>& x, std::vector<double>& w);
+void q1_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
+               std::vector<double>& dphi);
 void q2_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
                std::vector<double>& dphi);
+// Jacobi-preconditioned FP64 BiCGStab from x = 0 (gfe_bicgstab.cu)
+int bicgstab(gfe_ctx* ctx, gfe_matrix* A, const double* dinv, const double* d_b, double* d_x,
+             double rtol, int maxit, int* iterations);
+// quasilinear diffusion residual + Jacobian (gfe_nonlinear.cu)
+int assemble_quasilinear(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* d_b);
 // simplexified boxes and P2 tets (gfe_simplex.cpp)
 extern const int kHexTets[6][4];
 extern const int kTetEdges[6][2];

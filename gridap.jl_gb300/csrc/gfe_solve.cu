@@ -1603,6 +1603,10 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
     }
     rep->iterations = total;
     rep->refinements = outer;
+  } else if (o->method == GFE_SOLVER_BICGSTAB) {
+    int it = 0;
+    GFE_TRY(bicgstab(ctx, A, dinv64, d_b, d_x, o->rtol, maxit, &it));
+    rep->iterations = it;
   } else {
     return set_error(GFE_ERR_UNSUPPORTED, "solve: unknown method %d", o->method);
   }

@@ -6,7 +6,8 @@ symbolic_setup -> numerical_setup -> solve!(x, ns, b). These classes are that pl
   - CGSolver(rtol, maxiter, precond="jacobi"): FP64 preconditioned CG;
   - IRCGSolver(rtol, inner_rtol, ...): FP32 PCG inside FP64 iterative refinement: the outer
     loop forms r = b - A x and updates x in FP64, the inner solves A d = r in FP32;
-  - MixedCGSolver(rtol, ...): FP32 PCG with FP64 reliable updates (no restarts).
+  - MixedCGSolver(rtol, ...): FP32 PCG with FP64 reliable updates (no restarts);
+  - BiCGStabSolver(rtol, ...): FP64 Jacobi-preconditioned BiCGStab (non-symmetric matrices).
 
 Both stop on the FP64 relative residual ||b - A x|| <= rtol ||b|| and report it.
 """
@@ -73,6 +74,12 @@ class MixedCGSolver(LinearSolver):
     def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, precond: str = "jacobi",
                  inner_rtol: float = 0.01, check_every: int = 0, initial_guess: bool = False):
         super().__init__(rtol, maxiter, precond, inner_rtol, check_every, initial_guess)
+
+
+class BiCGStabSolver(LinearSolver):
+    """FP64 BiCGStab with a Jacobi (right) preconditioner, for non-symmetric matrices such as
+    the Jacobians of quasilinear forms whose coefficient depends on u."""
+    method = _lib.GFE_SOLVER_BICGSTAB
 
 
 class FCGSolver(LinearSolver):
@@ -158,6 +165,9 @@ def solve(solver, op, b=None):
     """solve(solver, op) with op an AffineFEOperator returns an FEFunction of the trial space
     (the solver's report attached as `uh.report`); solve(ls, op) with an AffineOperator and
     solve(ls, A, b) with a matrix return the solution vector (Algebra/LinearSolvers.jl)."""
+    if getattr(op, "is_nonlinear", False):
+        from .nonlinear import solve_nonlinear
+        return solve_nonlinear(solver, op)
     ls = solver.ls if isinstance(solver, LinearFESolver) else solver
     if b is not None or isinstance(op, AffineOperator):
         A = op.get_matrix() if isinstance(op, AffineOperator) else op

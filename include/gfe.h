@@ -174,9 +174,20 @@ enum {
 enum { GFE_GEOM_CARTESIAN = 0, GFE_GEOM_NODAL = 1 };
 enum {
   GFE_FORM_DIFFUSION = 1,  /* a(u,v) = int kappa grad(v).grad(u),  l(v) = int f v */
-  GFE_FORM_ELASTICITY = 2  /* a(u,v) = int eps(v) : (lambda tr(eps(u)) I + 2 mu eps(u)),
+  GFE_FORM_ELASTICITY = 2, /* a(u,v) = int eps(v) : (lambda tr(eps(u)) I + 2 mu eps(u)),
                               l(v) = int f . v; coef = (lambda, mu) once (CONST) or per cell
                               (CELL, 2 values per cell); source CONST with 3 values (f) */
+  GFE_FORM_QUASILINEAR = 3 /* residual r(u; v) = int kappa alpha(u, grad u) grad u . grad v
+                              - f v and its Jacobian at the state u (problem->state plus the
+                              Dirichlet values): A receives the Jacobian, b the residual.
+                              alpha is problem->law (GFE_LAW_*) with problem->law_params;
+                              kappa = coef (ONE, CONST or CELL); f = source (NONE, CONST,
+                              QPOINT). Scalar Q1/Q2, node coordinates required. */
+};
+enum {
+  GFE_LAW_POLY = 0,  /* alpha = c0 + c1 u + c2 u^2 (law_params c0, c1, c2) */
+  GFE_LAW_POWER = 1  /* alpha = (eps2 + |grad u|^2)^((p-2)/2) (law_params p, eps2): the
+                        p-Laplacian flux |grad u|^(p-2) grad u for eps2 = 0 */
 };
 enum { GFE_COEF_ONE = 0, GFE_COEF_CONST = 1, GFE_COEF_CELL = 2 };
 enum {
@@ -221,6 +232,11 @@ typedef struct gfe_problem {
      59-110, applied per triangulation in FESpaces/Assemblers.jl:525-542). */
   const double* dirichlet_values;
   int64_t ndirichlet;
+  /* GFE_FORM_QUASILINEAR: the free values of the state u (nfree entries, host or device),
+     the law and its parameters */
+  const double* state;
+  int32_t law;
+  double law_params[4];
 } gfe_problem;
 
 /* Integrates the recognised bilinear and linear forms over every cell and assembles them
@@ -273,7 +289,12 @@ int gfe_assemble_boundary_matrix(gfe_ctx* ctx, const gfe_problem* problem, gfe_m
                                  const double* coefs);
 
 /* ---- linear solve ------------------------------------------------------------------------ */
-enum { GFE_SOLVER_CG = 0, GFE_SOLVER_IR_CG = 1, GFE_SOLVER_MIXED_CG = 2 };
+enum {
+  GFE_SOLVER_CG = 0,
+  GFE_SOLVER_IR_CG = 1,
+  GFE_SOLVER_MIXED_CG = 2,
+  GFE_SOLVER_BICGSTAB = 3  /* FP64 BiCGStab, Jacobi (right) preconditioner: non-symmetric A */
+};
 enum { GFE_PC_NONE = 0, GFE_PC_JACOBI = 1 };
 
 typedef struct gfe_solver_opts {

@@ -633,3 +633,54 @@ def dirichlet_lift(cell_dofs, cellmats, uD, nfree):
             if r > 0:
                 b[r - 1] += lv[i]
     return b
+
+
+# ---- quasilinear diffusion (nonlinear FEOperator) --------------------------------------------
+LAW_POLY, LAW_POWER = 0, 1
+
+
+def quasilinear_cell_arrays(coords, cell_nodes, cell_dofs, order, degree, state, uD, law,
+                            params, kappa=None, f=None):
+    """Cell residuals and Jacobians of  r(u; v) = ∫ κ α(u, ∇u) ∇u⋅∇v - f v  at the FE function
+    u (free values `state`, Dirichlet values `uD`), by Gridap's per-point evaluation of
+    res(uh, v) and jac(uh, du, v) (CellData/CellQuadratures.jl:138-170): geometry from the cell's
+    Q1 map, ∇φ = J⁻ᵀ ∇ξφ, u_q = Σ u_i φ_i, ∇u_q = Σ u_i ∇φ_i, then
+      r_i  += κ α ∇u⋅∇φ_i dV - f φ_i dV,
+      J_ij += κ (α ∇φ_j⋅∇φ_i + α_u φ_j ∇u⋅∇φ_i + γ (∇u⋅∇φ_j)(∇u⋅∇φ_i)) dV
+    with the laws POLY α = c0 + c1 u + c2 u² (α_u = c1 + 2 c2 u, γ = 0) and POWER
+    α = (e + |∇u|²)^((p-2)/2), γ = (p-2)(e + |∇u|²)^((p-4)/2) (params p, e): the derivative of
+    the p-Laplacian flux (test/GridapTests/PLaplacianTests.jl dflux). f: a number or a
+    callable of the points. Returns (mats [c, i, j] (i test), vecs)."""
+    D = coords.shape[1]
+    qx, qw = tensor_quadrature(D, degree)
+    phi1, dphi1 = q1_shapes(D, qx)
+    phi, dref = (phi1, dphi1) if order == 1 else q2_shapes(D, qx)
+    nc, nn = cell_dofs.shape
+    mats = np.zeros((nc, nn, nn))
+    vecs = np.zeros((nc, nn))
+    for c in range(nc):
+        X = coords[cell_nodes[c] - 1]
+        ids = cell_dofs[c]
+        uc = np.array([state[i - 1] if i > 0 else (uD[-i - 1] if uD is not None else 0.0)
+                       for i in ids])
+        kap = 1.0 if kappa is None else (float(kappa) if np.ndim(kappa) == 0 else kappa[c])
+        for q in range(qw.shape[0]):
+            Jt = dphi1[q].T @ X
+            dV = qw[q] * abs(np.linalg.det(Jt))
+            g = np.linalg.solve(Jt, dref[q].T).T  # (nn, D)
+            u = phi[q] @ uc
+            gu = g.T @ uc
+            n2 = gu @ gu
+            if law == LAW_POLY:
+                c0, c1, c2 = params[:3]
+                al, be, ga = c0 + c1 * u + c2 * u * u, c1 + 2 * c2 * u, 0.0
+            else:
+                p, e = params[:2]
+                al, be, ga = (e + n2) ** ((p - 2) / 2), 0.0, (p - 2) * (e + n2) ** ((p - 4) / 2)
+            xq = phi1[q] @ X
+            fq = 0.0 if f is None else (float(f(xq[None, :])[0]) if callable(f) else float(f))
+            a = g @ gu
+            vecs[c] += kap * al * a * dV - fq * phi[q] * dV
+            mats[c] += kap * (al * (g @ g.T) + be * np.outer(a, phi[q])
+                              + ga * np.outer(a, a)) * dV
+    return mats, vecs

@@ -239,3 +239,27 @@ def test_boundary_forms_and_facet_points(gg, orc):
     _, gvals = orc.boundary_vector(part, m.node_coords, m.cell_node_ids, V.cell_dof_ids, 1,
                                    G.facet_cells, G.facet_lfaces, 4, g, V.num_free_dofs())
     np.testing.assert_allclose(g(xq.reshape(-1, 3)), gvals.reshape(-1), rtol=1e-14, atol=1e-14)
+
+
+def test_quasilinear_forms_are_recognised(gg):
+    """Residuals κ ∇v⋅flux(∇u) - f v and κ α(u) ∇v⋅∇u - f v are recognised, a matching
+    Jacobian is accepted and one that drops a derivative term is refused."""
+    from importlib import import_module
+    cd = import_module(gg.__name__ + ".celldata")
+    m = gg.CartesianDiscreteModel((0, 1, 0, 1), (3, 3))
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 2))
+    u, v, du = cd._FEState(None), cd.get_fe_basis(V), cd.get_trial_fe_basis(V)
+    k = gg.CellField(np.ones(9))
+    f = lambda x: x[:, 0]  # noqa: E731
+    flux, alpha = gg.PowerLawFlux(3.0, 0.1), gg.PolynomialCoefficient(1.0, 0.5, 1.0)
+    F = cd.classify_residual(k * gg.inner(gg.grad(v), flux(gg.grad(u))) - f * v)
+    assert F.law is flux and F.cells == [k] and F.source == (1.0, f)
+    cd.check_jacobian(k * gg.inner(gg.grad(v), flux.derivative(gg.grad(du), gg.grad(u))), F)
+    F = cd.classify_residual(2.0 * alpha(u) * gg.inner(gg.grad(v), gg.grad(u)))
+    assert F.law is alpha and F.scale == 2.0 and F.source is None
+    cd.check_jacobian(2.0 * alpha(u) * gg.inner(gg.grad(v), gg.grad(du))
+                      + 2.0 * alpha.derivative(u) * du * gg.inner(gg.grad(v), gg.grad(u)), F)
+    with pytest.raises(NotImplementedError):
+        cd.check_jacobian(2.0 * alpha(u) * gg.inner(gg.grad(v), gg.grad(du)), F)
+    with pytest.raises(NotImplementedError):
+        cd.classify_residual(gg.inner(gg.grad(v), gg.grad(u)) * u)

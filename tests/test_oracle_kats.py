@@ -345,3 +345,30 @@ def test_boundary_vector_measures(orc):
             else:
                 want = np.prod(L[1:])
             assert abs(b.sum() - want) <= 1e-13 * want
+
+
+@pytest.mark.parametrize("law,params", [(0, (1.0, 0.5, 1.0)), (1, (3.0, 0.1)), (1, (4.0, 0.0))])
+def test_quasilinear_jacobian_is_the_residual_derivative(orc, law, params):
+    """The oracle's quasilinear Jacobian equals central differences of its residual (both on
+    a jittered Q2 grid and a Q1 grid), so the law derivatives it restates are consistent."""
+    rng = np.random.default_rng(11)
+    for order, part in ((1, (3, 3)), (2, (2, 2))):
+        coords, cells, _ = orc.cartesian_model((0, 1, 0, 1), part)
+        coords = orc.jitter_interior(part, coords, 0.05 * rng.standard_normal(coords.shape))
+        if order == 1:
+            ids = np.arange(cells.size, dtype=np.int32).reshape(cells.shape) + 1
+        else:
+            ids, _, _ = orc.conforming_q2(part, [])
+            ids = np.asarray(ids, np.int32)
+        x = rng.random(int(ids.max()))
+        f = lambda p: p[:, 0]  # noqa: E731
+        M, _ = orc.quasilinear_cell_arrays(coords, cells, ids, order, 4, x, None, law, params,
+                                           f=f)
+        d = rng.standard_normal(x.size)
+        eps = 1e-6
+        _, vp = orc.quasilinear_cell_arrays(coords, cells, ids, order, 4, x + eps * d, None,
+                                            law, params, f=f)
+        _, vm = orc.quasilinear_cell_arrays(coords, cells, ids, order, 4, x - eps * d, None,
+                                            law, params, f=f)
+        jd = np.einsum("cij,cj->ci", M, d[ids - 1])
+        assert np.abs((vp - vm) / (2 * eps) - jd).max() <= 1e-7 * np.abs(jd).max()

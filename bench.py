@@ -434,6 +434,8 @@ def run_gpu(args):
         out["q2_tensor_cores"] = bench_q2(args, gg, ctx, lib, timed)
     if not args.no_poisson2d:
         out["poisson_2d"] = bench_poisson2d(args, gg, ctx, lib, timed)
+    if not args.no_nonlinear:
+        out["nonlinear_plaplacian"] = bench_nonlinear(args, gg, ctx, lib, timed)
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args, w)
@@ -714,6 +716,57 @@ def bench_poisson2d(args, gg, ctx, lib, timed):
             "iterations": rep.iterations, "relres": rep.relres}
 
 
+def bench_nonlinear(args, gg, ctx, lib, timed):
+    """Newton on the 3-D p-Laplacian (p = 3, eps2 = 1e-2): n^3 Q1 cells, u = x + y + z on the
+    boundary, f = 1, degree 4 (8 points). Timed: the residual + Jacobian re-assembly into the
+    fixed pattern (what every Newton step repeats) and a whole Newton solve (NLSolver, CG
+    1e-10 on the SPD Jacobian) from a seeded random start; vectors stay on the device."""
+    import torch
+    n = args.nl_n
+    m = gg.CartesianDiscreteModel((0, 1, 0, 1, 0, 1), (n, n, n))
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    U = gg.TrialFESpace(V, lambda x: x[:, 0] + x[:, 1] + x[:, 2])
+    dO = gg.Measure(gg.Triangulation(m), 4)
+    flux = gg.PowerLawFlux(3.0, 1e-2)
+    op = gg.FEOperator(lambda u, v: gg.integrate(gg.inner(gg.grad(v), flux(gg.grad(u)))
+                                                 - 1.0 * v, dO), U, V,
+                       assem=gg.SparseMatrixAssembler(U, V, ctx=ctx))
+    nfree = V.num_free_dofs()
+    dev = torch.device("cuda", ctx.device)
+    gen = torch.Generator(device="cpu").manual_seed(17)
+    x0 = torch.rand(nfree, generator=gen, dtype=torch.float64).to(dev)
+    x = x0.clone()
+    b = torch.empty(nfree, dtype=torch.float64, device=dev)
+    A = op.allocate_jacobian()
+    r = timed("nl_reassembly", lambda: op.residual_and_jacobian_(b, A, x), args.steps,
+              max(3, args.warmup))
+    el_ms, el_n = r["kt"][_lib_const(lib, "GFE_KT_ELEMENT")]
+    asm_ms, asm_n = r["kt"][_lib_const(lib, "GFE_KT_ASSEMBLE")]
+    nls = gg.NLSolver(gg.CGSolver(rtol=1e-10), method="newton", ftol=1e-9)
+
+    def newton():
+        x.copy_(x0)
+        nls.solve_(x, op.get_algebraic_operator())
+        return nls.iterations
+
+    rs = timed("nl_newton", newton, 1, 1, kernel_timing=False)
+    its = rs["reps"][-1]
+    return {"workload": f"{n}^3 Q1 p-Laplacian (p=3, eps2=1e-2), Newton (NLSolver), CG 1e-10",
+            "free_dofs": nfree, "cells": m.num_cells(),
+            "reassembly": {"ms_per_call": r["ms"], "dof_per_s": nfree / (r["ms"] * 1e-3),
+                           "element_ms": el_ms / max(el_n, 1), "row_gather_ms":
+                           asm_ms / max(asm_n, 1),
+                           "what": "residual + Jacobian at the state: element kernel "
+                                   "(k_quasilinear_cells) + row gather into the fixed pattern"},
+            "newton": {"ms": rs["ms"], "iterations": its, "ms_per_newton_step": rs["ms"] / its,
+                       "final_residual_inf": nls.residual_norm}}
+
+
+def _lib_const(lib, name):
+    from gridap_gb300 import _lib
+    return getattr(_lib, name)
+
+
 # ---- CPU baseline / reference arm ---------------------------------------------------------
 def cpu_baseline(args, w=None, quick=False):
     """The oracle (CPU restatement of Gridap's algorithm) on the host cores, the whole
@@ -787,6 +840,8 @@ def main():
     ap.add_argument("--no-q2", action="store_true")
     ap.add_argument("--q2-n", type=int, default=64)
     ap.add_argument("--no-poisson2d", action="store_true")
+    ap.add_argument("--no-nonlinear", action="store_true")
+    ap.add_argument("--nl-n", type=int, default=64)
     ap.add_argument("--batch-problems", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gfe":

@@ -26,6 +26,34 @@
 namespace gfe {
 namespace {
 
+// alpha, d alpha / d u and gamma at a point (u, |grad u|^2). p = 3 (the p-Laplacian of the
+// reference tests) and p = 4 use sqrt / plain products instead of pow.
+__device__ __forceinline__ void law_values(int law, double c0, double c1, double c2, double u,
+                                           double n2, double* al, double* be, double* ga) {
+  if (law == GFE_LAW_POLY) {
+    *al = c0 + c1 * u + c2 * u * u;
+    *be = c1 + 2.0 * c2 * u;
+    *ga = 0.0;
+    return;
+  }
+  const double s = c1 + n2;  // eps2 + |grad u|^2
+  *be = 0.0;
+  if (c0 == 3.0) {
+    const double r = sqrt(s);
+    *al = r;
+    *ga = 1.0 / r;
+  } else if (c0 == 4.0) {
+    *al = s;
+    *ga = 2.0;
+  } else if (c0 == 2.0) {
+    *al = 1.0;
+    *ga = 0.0;
+  } else {
+    *al = pow(s, 0.5 * (c0 - 2.0));
+    *ga = (c0 - 2.0) * pow(s, 0.5 * (c0 - 4.0));
+  }
+}
+
 template <int D, int NN>
 __global__ void k_quasilinear_cells(int64_t ncells, const int32_t* __restrict__ cell_vertices,
                                     const double* __restrict__ coords,
@@ -133,16 +161,7 @@ __global__ void k_quasilinear_cells(int64_t ncells, const int32_t* __restrict__ 
         n2 += gq[k] * gq[k];
       }
       double al, be, ga;
-      if (law == GFE_LAW_POLY) {
-        al = c0 + c1 * u + c2 * u * u;
-        be = c1 + 2.0 * c2 * u;
-        ga = 0.0;
-      } else {
-        const double s = c1 + n2;  // eps2 + |grad u|^2
-        al = pow(s, 0.5 * (c0 - 2.0));
-        be = 0.0;
-        ga = (c0 - 2.0) * pow(s, 0.5 * (c0 - 4.0));
-      }
+      law_values(law, c0, c1, c2, u, n2, &al, &be, &ga);
       const double kd = kap * dv[q];
       cq[q * 3 + 0] = kd * al;
       cq[q * 3 + 1] = kd * be;
@@ -184,6 +203,303 @@ __global__ void k_quasilinear_cells(int64_t ncells, const int32_t* __restrict__ 
   }
 }
 
+// Q1 cells: one thread per cell with the cell arrays in registers (2^D nodes), the same
+// per-point steps as the block-per-cell kernel.
+template <int D>
+__global__ void __launch_bounds__(128)
+    k_quasilinear_q1(int64_t ncells, const int32_t* __restrict__ cell_vertices,
+                     const double* __restrict__ coords, const int32_t* __restrict__ cell_ids,
+                     const double* __restrict__ state, int64_t nfree,
+                     const double* __restrict__ uD, int64_t ndiri,
+                     const double* __restrict__ tabs, int nq, int coef_kind,
+                     const double* __restrict__ coef, int src_kind,
+                     const double* __restrict__ src, int law, double c0, double c1, double c2,
+                     double* __restrict__ K, double* __restrict__ bvec, DevError* err) {
+  constexpr int NV = 1 << D;
+  extern __shared__ double st[];  // w[nq] | phi[nq*NV] | dref[nq*NV*D] (| dphi1 = dref)
+  const int ntab = nq * (1 + NV + NV * D);
+  for (int i = threadIdx.x; i < ntab; i += blockDim.x) st[i] = tabs[i];
+  __syncthreads();
+  const double* w = st;
+  const double* phi = w + nq;
+  const double* dref = phi + nq * NV;
+  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncells) return;
+  double x[NV][D], uc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const int64_t nid = (int64_t)__ldg(cell_vertices + cell * NV + v) - 1;
+#pragma unroll
+    for (int d = 0; d < D; ++d) x[v][d] = __ldg(coords + nid * D + d);
+    const int32_t id = __ldg(cell_ids + cell * NV + v);
+    double u = 0.0;
+    if (id > 0 && id <= nfree) {
+      u = __ldg(state + id - 1);
+    } else if (id < 0 && -(int64_t)id <= ndiri) {
+      u = __ldg(uD - (int64_t)id - 1);
+    } else if (id != 0 && !(id < 0 && ndiri == 0)) {
+      raise_err(err, GFE_ERR_INVALID_ARGUMENT, cell);
+    }
+    uc[v] = u;
+  }
+  const double kap = coef_kind == GFE_COEF_CELL ? __ldg(coef + cell)
+                     : coef_kind == GFE_COEF_CONST ? __ldg(coef) : 1.0;
+  double Ke[NV][NV], be[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    be[i] = 0.0;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) Ke[i][j] = 0.0;
+  }
+  for (int q = 0; q < nq; ++q) {
+    double Jt[D][D];
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+#pragma unroll
+      for (int l = 0; l < D; ++l) Jt[k][l] = 0.0;
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        const double gr = dref[(q * NV + v) * D + k];
+#pragma unroll
+        for (int l = 0; l < D; ++l) Jt[k][l] += gr * x[v][l];
+      }
+    double det, iJ[D][D];
+    if (D == 2) {
+      det = Jt[0][0] * Jt[1][1] - Jt[0][1] * Jt[1][0];
+      iJ[0][0] = Jt[1][1] / det;
+      iJ[0][1] = -Jt[0][1] / det;
+      iJ[1][0] = -Jt[1][0] / det;
+      iJ[1][1] = Jt[0][0] / det;
+    } else {
+      const double c00 = Jt[1][1] * Jt[2][2] - Jt[1][2] * Jt[2][1];
+      const double c01 = Jt[1][2] * Jt[2][0] - Jt[1][0] * Jt[2][2];
+      const double c02 = Jt[1][0] * Jt[2][1] - Jt[1][1] * Jt[2][0];
+      det = Jt[0][0] * c00 + Jt[0][1] * c01 + Jt[0][2] * c02;
+      iJ[0][0] = c00 / det;
+      iJ[0][1] = (Jt[0][2] * Jt[2][1] - Jt[0][1] * Jt[2][2]) / det;
+      iJ[0][2] = (Jt[0][1] * Jt[1][2] - Jt[0][2] * Jt[1][1]) / det;
+      iJ[1][0] = c01 / det;
+      iJ[1][1] = (Jt[0][0] * Jt[2][2] - Jt[0][2] * Jt[2][0]) / det;
+      iJ[1][2] = (Jt[0][2] * Jt[1][0] - Jt[0][0] * Jt[1][2]) / det;
+      iJ[2][0] = c02 / det;
+      iJ[2][1] = (Jt[0][1] * Jt[2][0] - Jt[0][0] * Jt[2][1]) / det;
+      iJ[2][2] = (Jt[0][0] * Jt[1][1] - Jt[0][1] * Jt[1][0]) / det;
+    }
+    if (!(det != 0.0) || !isfinite(det)) raise_err(err, GFE_ERR_DEGENERATE_CELL, cell);
+    const double dV = w[q] * fabs(det);
+    double g[NV][D], u = 0.0, gu[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) gu[k] = 0.0;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      u += phi[q * NV + v] * uc[v];
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        double s = 0.0;
+#pragma unroll
+        for (int l = 0; l < D; ++l) s += iJ[k][l] * dref[(q * NV + v) * D + l];
+        g[v][k] = s;
+        gu[k] += s * uc[v];
+      }
+    }
+    double n2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) n2 += gu[k] * gu[k];
+    double al, be_, ga;
+    law_values(law, c0, c1, c2, u, n2, &al, &be_, &ga);
+    const double kd = kap * dV;
+    const double ca = kd * al, cb = kd * be_, cg = kd * ga;
+    if (!isfinite(ca) || !isfinite(cb) || !isfinite(cg)) raise_err(err, GFE_ERR_NONFINITE, cell);
+    double f = 0.0;
+    if (src_kind == GFE_SRC_CONST) f = __ldg(src);
+    else if (src_kind == GFE_SRC_QPOINT) f = __ldg(src + cell * nq + q);
+    const double fd = f * dV;
+    double a[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s += gu[k] * g[v][k];
+      a[v] = s;
+    }
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      be[i] += ca * a[i] - fd * phi[q * NV + i];
+#pragma unroll
+      for (int j = 0; j < NV; ++j) {
+        double gg = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) gg += g[i][k] * g[j][k];
+        Ke[i][j] += ca * gg + cb * a[i] * phi[q * NV + j] + cg * a[i] * a[j];
+      }
+    }
+  }
+  if (K)
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+#pragma unroll
+      for (int j = 0; j < NV; ++j) K[(int64_t)(i + j * NV) * ncells + cell] = Ke[i][j];
+  if (bvec)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) bvec[(int64_t)i * ncells + cell] = be[i];
+}
+
+// Uniform Cartesian Q1 cells: the physical gradients g, their products G[q][i][j] = g_i.g_j
+// and dV are the same in every cell (host tables), so a cell costs the state-dependent part
+// only. SYM (no d alpha/d u term): the Jacobian is symmetric and only j >= i is formed.
+template <int D, bool SYM>
+__global__ void __launch_bounds__(128)
+    k_quasilinear_q1_cart(int64_t ncells, const int32_t* __restrict__ cell_ids,
+                          const double* __restrict__ state, int64_t nfree,
+                          const double* __restrict__ uD, int64_t ndiri,
+                          const double* __restrict__ tabs, int nq, int coef_kind,
+                          const double* __restrict__ coef, int src_kind,
+                          const double* __restrict__ src, int law, double c0, double c1,
+                          double c2, double* __restrict__ K, double* __restrict__ bvec,
+                          DevError* err) {
+  constexpr int NV = 1 << D;
+  extern __shared__ double st[];  // dV[nq] | phi[nq*NV] | g[nq*NV*D] | G[nq*NV*NV]
+  const int ntab = nq * (1 + NV + NV * D + NV * NV);
+  for (int i = threadIdx.x; i < ntab; i += blockDim.x) st[i] = tabs[i];
+  __syncthreads();
+  const double* dVq = st;
+  const double* phi = dVq + nq;
+  const double* gt = phi + nq * NV;
+  const double* GG = gt + nq * NV * D;
+  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncells) return;
+  double uc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const int32_t id = __ldg(cell_ids + cell * NV + v);
+    double u = 0.0;
+    if (id > 0 && id <= nfree) {
+      u = __ldg(state + id - 1);
+    } else if (id < 0 && -(int64_t)id <= ndiri) {
+      u = __ldg(uD - (int64_t)id - 1);
+    } else if (id != 0 && !(id < 0 && ndiri == 0)) {
+      raise_err(err, GFE_ERR_INVALID_ARGUMENT, cell);
+    }
+    uc[v] = u;
+  }
+  const double kap = coef_kind == GFE_COEF_CELL ? __ldg(coef + cell)
+                     : coef_kind == GFE_COEF_CONST ? __ldg(coef) : 1.0;
+  double Ke[NV][NV], be[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    be[i] = 0.0;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) Ke[i][j] = 0.0;
+  }
+  for (int q = 0; q < nq; ++q) {
+    double u = 0.0, gu[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) gu[k] = 0.0;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      u += phi[q * NV + v] * uc[v];
+#pragma unroll
+      for (int k = 0; k < D; ++k) gu[k] += gt[(q * NV + v) * D + k] * uc[v];
+    }
+    double n2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) n2 += gu[k] * gu[k];
+    double al, be_, ga;
+    law_values(law, c0, c1, c2, u, n2, &al, &be_, &ga);
+    const double kd = kap * dVq[q];
+    const double ca = kd * al, cb = kd * be_, cg = kd * ga;
+    if (!isfinite(ca) || !isfinite(cb) || !isfinite(cg)) raise_err(err, GFE_ERR_NONFINITE, cell);
+    double f = 0.0;
+    if (src_kind == GFE_SRC_CONST) f = __ldg(src);
+    else if (src_kind == GFE_SRC_QPOINT) f = __ldg(src + cell * nq + q);
+    const double fd = f * dVq[q];
+    double a[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s += gu[k] * gt[(q * NV + v) * D + k];
+      a[v] = s;
+    }
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      be[i] += ca * a[i] - fd * phi[q * NV + i];
+      if (K) {
+        const double cga = cg * a[i];
+#pragma unroll
+        for (int j = SYM ? i : 0; j < NV; ++j) {
+          double t = ca * GG[(q * NV + i) * NV + j] + cga * a[j];
+          if (!SYM) t += cb * a[i] * phi[q * NV + j];
+          Ke[i][j] += t;
+        }
+      }
+    }
+  }
+  if (K)
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+#pragma unroll
+      for (int j = 0; j < NV; ++j)
+        K[(int64_t)(i + j * NV) * ncells + cell] = (SYM && j < i) ? Ke[j][i] : Ke[i][j];
+  if (bvec)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) bvec[(int64_t)i * ncells + cell] = be[i];
+}
+
+template <int D>
+int launch_quasilinear_cart(gfe_ctx* ctx, const gfe_problem* p, int64_t ncells,
+                            const int32_t* ids, const double* st, int64_t nfree,
+                            const double* uD, int64_t ndiri, const std::vector<double>& qw,
+                            const std::vector<double>& phi1, const std::vector<double>& dphi1,
+                            const double* coef, const double* src, double* K, double* bv) {
+  constexpr int NV = 1 << D;
+  const int nq = (int)qw.size();
+  double h[3], vol = 1.0;
+  for (int d = 0; d < D; ++d) {
+    h[d] = (p->domain[2 * d + 1] - p->domain[2 * d]) / (double)p->partition[d];
+    vol *= h[d];
+  }
+  std::vector<double> t;
+  for (int q = 0; q < nq; ++q) t.push_back(qw[q] * vol);
+  t.insert(t.end(), phi1.begin(), phi1.end());
+  std::vector<double> g((size_t)nq * NV * D);
+  for (int q = 0; q < nq; ++q)
+    for (int v = 0; v < NV; ++v)
+      for (int k = 0; k < D; ++k)
+        g[((size_t)q * NV + v) * D + k] = dphi1[((size_t)q * NV + v) * D + k] / h[k];
+  t.insert(t.end(), g.begin(), g.end());
+  for (int q = 0; q < nq; ++q)
+    for (int i = 0; i < NV; ++i)
+      for (int j = 0; j < NV; ++j) {
+        double s = 0.0;
+        for (int k = 0; k < D; ++k)
+          s += g[((size_t)q * NV + i) * D + k] * g[((size_t)q * NV + j) * D + k];
+        t.push_back(s);
+      }
+  GFE_TRY(ctx->scratch[SCR_TMP0].reserve(sizeof(double) * t.size()));
+  double* dt = ctx->scratch[SCR_TMP0].as<double>();
+  GFE_CUDA_TRY(cudaMemcpyAsync(dt, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  const size_t sm = sizeof(double) * t.size();
+  const bool sym =
+      p->law == GFE_LAW_POWER || (p->law_params[1] == 0.0 && p->law_params[2] == 0.0);
+  auto kern = sym ? k_quasilinear_q1_cart<D, true> : k_quasilinear_q1_cart<D, false>;
+  if (sm > 48 * 1024)
+    GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  timer_begin(ctx, GFE_KT_ELEMENT);
+  kern<<<grid_for(ncells, 128), 128, sm, ctx->stream>>>(
+      ncells, ids, st, nfree, uD, ndiri, dt, nq, p->coef_kind, coef, p->source_kind, src, p->law,
+      p->law_params[0], p->law_params[1], p->law_params[2], K, bv, ctx->d_err);
+  timer_end(ctx);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  // the host table must outlive its copy
+  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return GFE_OK;
+}
+
 template <int D, int NN>
 int launch_quasilinear(gfe_ctx* ctx, int64_t ncells, const int32_t* vn, const double* vc,
                        const int32_t* ids, const double* st, int64_t nfree, const double* uD,
@@ -196,6 +512,21 @@ int launch_quasilinear(gfe_ctx* ctx, int64_t ncells, const int32_t* vn, const do
                                       (size_t)nq * D + nq);
   if (sm > 227 * 1024)
     return set_error(GFE_ERR_UNSUPPORTED, "quasilinear: quadrature too large (%d points)", nq);
+  if (NN == NV) {  // Q1: thread per cell, tables only in shared memory
+    const size_t smq = sizeof(double) * (size_t)nq * (1 + NV + NV * D);
+    auto kq = k_quasilinear_q1<D>;
+    if (smq > 48 * 1024)
+      GFE_CUDA_TRY(cudaFuncSetAttribute(kq, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smq));
+    timer_begin(ctx, GFE_KT_ELEMENT);
+    kq<<<grid_for(ncells, 128), 128, smq, ctx->stream>>>(
+        ncells, vn, vc, ids, st, nfree, uD, ndiri, tabs, nq, coef_kind, coef, src_kind, src,
+        p->law, p->law_params[0], p->law_params[1], p->law_params[2], K, bv, ctx->d_err);
+    timer_end(ctx);
+    ctx->launches++;
+    GFE_CUDA_TRY(cudaGetLastError());
+    return GFE_OK;
+  }
   auto kern = k_quasilinear_cells<D, NN>;
   GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   const unsigned grid = (unsigned)std::min<int64_t>(ncells, (int64_t)ctx->num_sms * 8);
@@ -300,7 +631,14 @@ int assemble_quasilinear(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, doub
   const double* ud = (const double*)vd;
   const double* kc = (const double*)vk;
   const double* fs = (const double*)vf;
-  if (D == 2 && !q2)
+  if (!q2 && p->geometry == GFE_GEOM_CARTESIAN) {
+    if (D == 2)
+      GFE_TRY(launch_quasilinear_cart<2>(ctx, p, ncells, ids, st, p->nfree, ud, ndiri, qw, phi1,
+                                         dphi1, kc, fs, K, bv));
+    else
+      GFE_TRY(launch_quasilinear_cart<3>(ctx, p, ncells, ids, st, p->nfree, ud, ndiri, qw, phi1,
+                                         dphi1, kc, fs, K, bv));
+  } else if (D == 2 && !q2)
     GFE_TRY((launch_quasilinear<2, 4>(ctx, ncells, cv, xc, ids, st, p->nfree, ud, ndiri, dt, ntab,
                                       nq, p->coef_kind, kc, p->source_kind, fs, p, K, bv)));
   else if (D == 2)

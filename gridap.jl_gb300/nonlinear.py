@@ -101,7 +101,9 @@ class FEOperator:
             p.domain[2 * d] = model.domain[2 * d]
             p.domain[2 * d + 1] = model.domain[2 * d + 1]
         p.nnodes = model.num_nodes()
-        p.geometry = _lib.GFE_GEOM_NODAL
+        # undistorted Cartesian Q1 cells take the table-driven kernel; coordinates go along
+        p.geometry = (_lib.GFE_GEOM_CARTESIAN if model.cartesian and V.reffe.order == 1
+                      else _lib.GFE_GEOM_NODAL)
         p.node_coords = _lib.ptr(model.node_coords)
         p.cell_node_ids = _lib.ptr(model.cell_node_ids)
         p.form = _lib.GFE_FORM_QUASILINEAR
@@ -151,9 +153,14 @@ class FEOperator:
         self._assemble(uh, None, b)
         return b
 
+    def _new_vector(self, like):
+        n = _space(self.test).num_free_dofs()
+        if hasattr(like, "free_values"):
+            like = like.free_values
+        return np.empty(n) if isinstance(like, np.ndarray) else like.new_empty((n,))
+
     def residual(self, uh):
-        b = np.empty(_space(self.test).num_free_dofs())
-        return self.residual_(b, uh)
+        return self.residual_(self._new_vector(uh), uh)
 
     def jacobian_(self, A, uh):
         """jacobian!(A, op, uh): re-assembly into A's pattern."""
@@ -170,8 +177,7 @@ class FEOperator:
         return b, A
 
     def residual_and_jacobian(self, uh):
-        b = np.empty(_space(self.test).num_free_dofs())
-        return self.residual_and_jacobian_(b, self.allocate_jacobian(), uh)
+        return self.residual_and_jacobian_(self._new_vector(uh), self.allocate_jacobian(), uh)
 
     def get_algebraic_operator(self) -> "AlgebraicOpFromFEOp":
         return AlgebraicOpFromFEOp(self)
@@ -198,8 +204,15 @@ class AlgebraicOpFromFEOp:
     def zero_initial_guess(self):
         return np.zeros(_space(self.feop.test).num_free_dofs())
 
+    def allocate_jacobian(self):
+        return self.feop.allocate_jacobian()
+
 
 # ---- Newton solvers ----------------------------------------------------------------------------
+def _empty_like(b):
+    return np.empty_like(b) if isinstance(b, np.ndarray) else b.new_empty(b.shape)
+
+
 def _maxabs(b) -> float:
     return float(b.abs().max()) if hasattr(b, "abs") and not isinstance(b, np.ndarray) \
         else float(np.max(np.abs(b))) if len(b) else 0.0
@@ -219,7 +232,7 @@ class NewtonRaphsonSolver:
         if cache is None:
             b = op.residual(x)
             A = op.jacobian(x)
-            dx = np.empty_like(b)
+            dx = _empty_like(b)
             ns = numerical_setup(symbolic_setup(self.ls, A), A)
         else:
             A, b, dx, ns = cache
@@ -275,7 +288,7 @@ class NLSolver:
         else:
             A, F, ns = cache
             op.residual_(F, x)
-        p = np.empty_like(F)
+        p = _empty_like(F)
         self.iterations = 0
         fnorm = _maxabs(F)
         converged = fnorm <= self.ftol

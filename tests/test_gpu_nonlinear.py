@@ -63,13 +63,15 @@ def _operator(gg, m, order, law_kind, kappa=None, f=None, uD=None):
     return gg.FEOperator(res, jac, U, V), V, U, law, params, 2 * order + 2
 
 
-@pytest.mark.parametrize("part,order,law_kind", [
-    ((5, 4), 1, "power"), ((5, 4), 1, "poly"), ((3, 4), 2, "power"), ((3, 3), 2, "poly"),
-    ((3, 3, 2), 1, "poly"), ((2, 2, 2), 2, "power"),
+@pytest.mark.parametrize("part,order,law_kind,jitter", [
+    ((5, 4), 1, "power", 0.15), ((5, 4), 1, "poly", 0.15), ((3, 4), 2, "power", 0.15),
+    ((3, 3), 2, "poly", 0.15), ((3, 3, 2), 1, "poly", 0.15), ((2, 2, 2), 2, "power", 0.15),
+    # undistorted Q1 cells: the table-driven Cartesian kernel (symmetric and general)
+    ((6, 5), 1, "power", 0.0), ((4, 3, 5), 1, "poly", 0.0), ((4, 3, 3), 1, "power", 0.0),
 ])
-def test_residual_and_jacobian_match_oracle(gg, orc, part, order, law_kind):
+def test_residual_and_jacobian_match_oracle(gg, orc, part, order, law_kind, jitter):
     rng = np.random.default_rng(sum(part) + order)
-    m = _model(gg, part, jitter=0.15)
+    m = _model(gg, part, jitter=jitter)
     kappa = np.exp(0.3 * rng.standard_normal(m.num_cells()))
     f = lambda x: 1.0 + x[:, 0] * x[:, 1]  # noqa: E731
     uD = lambda x: 0.5 - x[:, 0]  # noqa: E731

@@ -25,6 +25,7 @@ from .fespaces import (FEFunction, FESpace, ReferenceFE, TrialFESpace, get_cell_
 from .geometry import (Boundary, BoundaryTriangulation, CartesianDiscreteModel, FaceLabeling,
                        Measure, SimplexDiscreteModel, Triangulation, simplexify)
 from .batch import BatchedPoissonProblems
+from .reindexing import compute_dof_permutation, reindex_free_dof_ids
 from .nonlinear import (FEOperator, NewtonRaphsonSolver, NLSolver, NonlinearFESolver,
                         solve_nonlinear_)
 from .learned import LearnedBlockPreconditioner

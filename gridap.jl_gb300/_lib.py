@@ -32,6 +32,7 @@ GFE_COEF_ONE, GFE_COEF_CONST, GFE_COEF_CELL = 0, 1, 2
 GFE_SRC_NONE, GFE_SRC_CONST, GFE_SRC_NODAL, GFE_SRC_QPOINT, GFE_SRC_SINSUM = 0, 1, 2, 3, 4
 GFE_BOP_VALUE, GFE_BOP_NORMAL_GRAD = 0, 1
 GFE_LAW_POLY, GFE_LAW_POWER = 0, 1
+GFE_REORDER_RCM, GFE_REORDER_SLOAN = 0, 1
 GFE_PREC_FP64, GFE_PREC_FP32 = 0, 1
 GFE_SOLVER_CG, GFE_SOLVER_IR_CG, GFE_SOLVER_MIXED_CG, GFE_SOLVER_BICGSTAB = 0, 1, 2, 3
 GFE_PC_NONE, GFE_PC_JACOBI = 0, 1
@@ -118,6 +119,8 @@ SIGNATURES = {
     "gfe_assemble_boundary_vector": (C.c_int, [_P, C.POINTER(Problem), C.c_int64, _P, _P,
                                                C.c_int32, C.c_int32, C.c_int32, _P, C.c_int64,
                                                _P]),
+    "gfe_dof_permutation": (C.c_int, [_P, C.c_int64, C.c_int32, _P, C.c_int64, C.c_int32,
+                                      C.c_int32, C.c_int32, _P]),
     "gfe_assemble_boundary_matrix": (C.c_int, [_P, C.POINTER(Problem), _P, _P, C.c_int64, _P,
                                                _P, C.c_int32, _P]),
     "gfe_simplex_p2_dofs": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P, _P]),

@@ -288,6 +288,17 @@ int gfe_assemble_boundary_matrix(gfe_ctx* ctx, const gfe_problem* problem, gfe_m
                                  const int32_t* facet_lfaces, int32_t degree,
                                  const double* coefs);
 
+/* ---- free-dof reordering ------------------------------------------------------------------ */
+/* iperm[old-1] = new (1-based) for the free dofs of cell_dof_ids (Gridap convention, host or
+ * device), as compute_dof_permutation (FESpaces/FESpaceReindexing.jl:264-300) returns it:
+ * GFE_REORDER_RCM, Reverse Cuthill-McKee with George-Liu pseudo-peripheral nodes; or
+ * GFE_REORDER_SLOAN with weights w1, w2 (Gridap's defaults 1, 2). iperm is host memory.
+ * Applying it: new cell ids = iperm[id-1] for id > 0 (reindex_free_dof_ids). */
+enum { GFE_REORDER_RCM = 0, GFE_REORDER_SLOAN = 1 };
+int gfe_dof_permutation(gfe_ctx* ctx, int64_t ncells, int32_t nd, const int32_t* cell_dof_ids,
+                        int64_t nfree, int32_t algorithm, int32_t w1, int32_t w2,
+                        int64_t* iperm);
+
 /* ---- linear solve ------------------------------------------------------------------------ */
 enum {
   GFE_SOLVER_CG = 0,

@@ -141,6 +141,17 @@ int orc_pcg(const orc_csc* A, const double* b, double* x, double rtol, int maxit
 /* y = A x for a CSC matrix (serial, column-oriented as SparseArrays' mul!). */
 void orc_csc_mul(const orc_csc* A, const double* x, double* y);
 
+/* ---- free-dof reordering (gfe_oracle_reorder.c) --------------------------------------- */
+/* compute_adjacency (Arrays/Tables.jl:1053-1107): 1-based ptrs (nfree+1) and data, malloc'd
+ * (release with orc_free). */
+int orc_compute_adjacency(int64_t ncells, int nd, const int32_t* cell_dofs, int64_t nfree,
+                          int64_t** ptrs, int32_t** data);
+void orc_free(void* p);
+/* Reverse Cuthill-McKee / Sloan permutations (FESpaceReindexing.jl): iperm[old-1] = new. */
+int orc_rcm_perm(int64_t nfree, const int64_t* ptrs, const int32_t* adj, int64_t* iperm);
+int orc_sloan_perm(int64_t nfree, const int64_t* ptrs, const int32_t* adj, int64_t w1,
+                   int64_t w2, int64_t* iperm);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,12 @@ def lib():
         L.orc_wv_tet_degree5.restype = C.c_double
         L.orc_p2tet_cell_arrays_elasticity.argtypes = [C.c_int64, P, P, P, C.c_int, P, P, P,
                                                        P, P]
+        L.orc_compute_adjacency.argtypes = [C.c_int64, C.c_int, P, C.c_int64,
+                                            C.POINTER(C.POINTER(C.c_int64)),
+                                            C.POINTER(C.POINTER(C.c_int32))]
+        L.orc_free.argtypes = [P]
+        L.orc_rcm_perm.argtypes = [C.c_int64, P, P, P]
+        L.orc_sloan_perm.argtypes = [C.c_int64, P, P, C.c_int64, C.c_int64, P]
         _lib = L
     return _lib
 
@@ -684,3 +690,54 @@ def quasilinear_cell_arrays(coords, cell_nodes, cell_dofs, order, degree, state,
             mats[c] += kap * (al * (g @ g.T) + be * np.outer(a, phi[q])
                               + ga * np.outer(a, a)) * dV
     return mats, vecs
+
+
+# ---- free-dof reordering ---------------------------------------------------------------------
+def compute_adjacency(cell_dofs, nfree):
+    """Gridap's compute_adjacency: (ptrs (nfree+1), data), 1-based like its Table."""
+    cd = np.ascontiguousarray(cell_dofs, np.int32)
+    pp = C.POINTER(C.c_int64)()
+    dp = C.POINTER(C.c_int32)()
+    L = lib()
+    if L.orc_compute_adjacency(C.c_int64(cd.shape[0]), cd.shape[1], _p(cd), C.c_int64(nfree),
+                               C.byref(pp), C.byref(dp)) != 0:
+        raise MemoryError("oracle adjacency")
+    ptrs = np.ctypeslib.as_array(pp, (nfree + 1,)).copy()
+    nnz = int(ptrs[-1] - 1)
+    data = np.ctypeslib.as_array(dp, (max(nnz, 1),))[:nnz].copy()
+    L.orc_free(C.cast(pp, C.c_void_p))
+    L.orc_free(C.cast(dp, C.c_void_p))
+    return ptrs, data
+
+
+def dof_permutation(cell_dofs, nfree, algorithm="rcm", w1=1, w2=2, coords=None):
+    """compute_dof_permutation (FESpaceReindexing.jl:264-300): iperm[old-1] = new (1-based).
+    'coordinates' sorts the free dofs' points lexicographically (stable sortperm by Tuple)."""
+    if algorithm == "coordinates":
+        X = np.asarray(coords, np.float64)
+        order = np.lexsort(tuple(X[:, d] for d in range(X.shape[1] - 1, -1, -1)))
+        iperm = np.empty(nfree, np.int64)
+        iperm[order] = np.arange(1, nfree + 1)
+        return iperm
+    ptrs, data = compute_adjacency(cell_dofs, nfree)
+    iperm = np.empty(nfree, np.int64)
+    L = lib()
+    if algorithm == "rcm":
+        st = L.orc_rcm_perm(C.c_int64(nfree), _p(ptrs), _p(data), _p(iperm))
+    elif algorithm == "sloan":
+        st = L.orc_sloan_perm(C.c_int64(nfree), _p(ptrs), _p(data), C.c_int64(w1),
+                              C.c_int64(w2), _p(iperm))
+    else:
+        raise ValueError(algorithm)
+    if st != 0:
+        raise MemoryError("oracle permutation")
+    return iperm
+
+
+def reindex_cell_dofs(cell_dofs, iperm):
+    """PosNegReindex of free ids (Dirichlet ids unchanged)."""
+    cd = np.asarray(cell_dofs)
+    out = cd.copy()
+    m = cd > 0
+    out[m] = iperm[cd[m] - 1]
+    return out.astype(np.int32)

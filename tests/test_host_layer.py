@@ -263,3 +263,21 @@ def test_quasilinear_forms_are_recognised(gg):
         cd.check_jacobian(2.0 * alpha(u) * gg.inner(gg.grad(v), gg.grad(du)), F)
     with pytest.raises(NotImplementedError):
         cd.classify_residual(gg.inner(gg.grad(v), gg.grad(u)) * u)
+
+
+def test_coordinate_reordering_matches_oracle(gg, orc):
+    """reindex_free_dof_ids(V, "coordinates") sorts free dofs by their nodes' coordinates
+    (lexicographic, stable), as the oracle's restatement of _coordinates_perm does."""
+    for order, part in ((1, (4, 3)), (2, (3, 2, 2))):
+        m = gg.CartesianDiscreteModel((0, 1) * len(part), part)
+        V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, order), dirichlet_tags="tag_1"
+                       if len(part) == 2 else "tag_01")
+        ip = gg.compute_dof_permutation(V, "coordinates")
+        fx, _, _, _ = V.dof_points()
+        assert np.array_equal(ip, orc.dof_permutation(V.cell_dof_ids, V.num_free_dofs(),
+                                                      "coordinates", coords=fx))
+        W = gg.reindex_free_dof_ids(V, ip)
+        assert W.num_free_dofs() == V.num_free_dofs()
+        assert W.num_dirichlet_dofs() == V.num_dirichlet_dofs()
+        fw, _, _, _ = W.dof_points()
+        assert np.array_equal(fw[ip - 1], fx)

@@ -372,3 +372,30 @@ def test_quasilinear_jacobian_is_the_residual_derivative(orc, law, params):
                                             law, params, f=f)
         jd = np.einsum("cij,cj->ci", M, d[ids - 1])
         assert np.abs((vp - vm) / (2 * eps) - jd).max() <= 1e-7 * np.abs(jd).max()
+
+
+def test_reindexing_oracle_on_gridaps_case(orc):
+    """test/FESpacesTests/FESpaceReindexingTests.jl: Q2 on a 4x4 box with Dirichlet
+    boundary; every algorithm gives a permutation of the free dofs, RCM reduces the
+    matrix bandwidth. A path graph is numbered end to end."""
+    cd, nf, nd = orc.conforming_q2((4, 4), ["boundary"])
+
+    def bw(c):
+        m = 0
+        for row in c:
+            r = row[row > 0]
+            if r.size:
+                m = max(m, int(r.max() - r.min()))
+        return m
+
+    for alg in ("rcm", "sloan"):
+        ip = orc.dof_permutation(cd, nf, alg)
+        assert np.array_equal(np.sort(ip), np.arange(1, nf + 1))
+    assert bw(orc.reindex_cell_dofs(cd, orc.dof_permutation(cd, nf, "rcm"))) < bw(cd)
+    chain = np.array([[i + 1, i + 2] for i in range(5)], np.int32)
+    for alg in ("rcm", "sloan"):
+        ip = orc.dof_permutation(chain, 6, alg)
+        assert list(ip) in ([6, 5, 4, 3, 2, 1], [1, 2, 3, 4, 5, 6])
+    ptrs, data = orc.compute_adjacency(chain, 6)
+    assert list(ptrs) == [1, 2, 4, 6, 8, 10, 11]
+    assert list(data) == [2, 1, 3, 2, 4, 3, 5, 4, 6, 5]

@@ -436,6 +436,8 @@ def run_gpu(args):
         out["poisson_2d"] = bench_poisson2d(args, gg, ctx, lib, timed)
     if not args.no_nonlinear:
         out["nonlinear_plaplacian"] = bench_nonlinear(args, gg, ctx, lib, timed)
+    if not args.no_reordering:
+        out["reordering_rcm"] = bench_reordering(args, gg, ctx, lib, timed)
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args, w)
@@ -762,6 +764,52 @@ def bench_nonlinear(args, gg, ctx, lib, timed):
                        "final_residual_inf": nls.residual_norm}}
 
 
+def bench_reordering(args, gg, ctx, lib, timed):
+    """Free-dof RCM on the jittered Q2 space (n^3 cells, Gridap's first-touch numbering):
+    the device permutation against the oracle's sequential restatement on one host core
+    (same permutation), and FP64 CG iterations on the matrix before and after reordering
+    (100 iterations each, same arithmetic up to the permutation)."""
+    import ctypes
+    import torch
+    from gridap_gb300 import _lib, workloads
+    from gridap_gb300.reindexing import bandwidth
+    model, V, dO = workloads.jittered_q2_3d(args.ro_n)
+    nfree = V.num_free_dofs()
+    ids = np.ascontiguousarray(V.cell_dof_ids, np.int32)
+    iperm = np.empty(nfree, np.int64)
+
+    def rcm():
+        _lib.check(lib.gfe_dof_permutation(ctx.handle, ids.shape[0], ids.shape[1],
+                                           _lib.ptr(ids), nfree, _lib.GFE_REORDER_RCM, 1, 2,
+                                           _lib.ptr(iperm)))
+
+    r = timed("rcm", rcm, 1, 1, kernel_timing=False)
+    W = gg.reindex_free_dof_ids(V, iperm.copy())
+    dev = torch.device("cuda", ctx.device)
+    out = {"workload": f"{args.ro_n}^3 Q2 jittered, free dofs {nfree}",
+           "rcm_gpu_ms": r["ms"]}
+    cg = gg.CGSolver(rtol=1e-30, maxiter=100)
+    for name, S in (("natural", V), ("rcm", W)):
+        prep = gg.prepare_problem(S, S, dO, None, 1.0)
+        A = gg.symbolic_loop_matrix(gg.SparseMatrixAssembler(S, S, ctx=ctx),
+                                    (None, S.cell_dof_ids, S.cell_dof_ids))
+        b = torch.zeros(nfree, dtype=torch.float64, device=dev)
+        x = torch.zeros(nfree, dtype=torch.float64, device=dev)
+        _lib.check(lib.gfe_assemble_matrix_and_vector(ctx.handle, ctypes.byref(prep.p), A.handle,
+                                                      _lib.ptr(b)))
+        ns = gg.numerical_setup(gg.symbolic_setup(cg, A), A)
+        rs = timed("cg_" + name, lambda: gg.solve_(x, ns, b), 3, 2, kernel_timing=False)
+        out[name] = {"bandwidth": bandwidth(A), "ms_per_cg_iteration": rs["ms"] / 100}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        t0 = time.perf_counter()
+        want = orc.dof_permutation(ids, nfree, "rcm")
+        out["rcm_cpu_oracle_s"] = time.perf_counter() - t0
+        out["rcm_cpu_cores"] = 1
+        out["same_permutation_as_oracle"] = bool(np.array_equal(want, iperm))
+    return out
+
+
 def _lib_const(lib, name):
     from gridap_gb300 import _lib
     return getattr(_lib, name)
@@ -842,6 +890,8 @@ def main():
     ap.add_argument("--no-poisson2d", action="store_true")
     ap.add_argument("--no-nonlinear", action="store_true")
     ap.add_argument("--nl-n", type=int, default=64)
+    ap.add_argument("--no-reordering", action="store_true")
+    ap.add_argument("--ro-n", type=int, default=48)
     ap.add_argument("--batch-problems", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gfe":

@@ -447,7 +447,7 @@ struct LatticeQ1Op {
     return (int64_t)(i + 1) + (int64_t)p1 * (j + 1) + (int64_t)p2 * (k + 1);
   }
   int64_t padded_size() const { return (int64_t)p2 * (n2 + 1); }
-  dim3 grid(int64_t) const {
+  __host__ __device__ dim3 grid(int64_t) const {
     return dim3((unsigned)((n0 - 1 + 31) / 32), (unsigned)((n1 - 1 + 7) / 8),
                 (unsigned)((n2 - 1 + kLatK - 1) / kLatK));
   }
@@ -480,17 +480,17 @@ int spmv64(gfe_ctx* ctx, gfe_matrix* A, const double* d_x, double* d_y) {
 // PAD: p, q (and r) in the zero-halo padded layout (LatticeQ1Op::pad_index): every
 // neighbour load is unconditional and q is written at the padded index. Otherwise the rows
 // are the dof numbering and neighbours outside the interior read as 0.
+// The rows of one tile: (i, j) = (32 bx + lane, 8 by + warp), k-planes kLatK bz .. + kLatK.
+// Adds p.q (and p.r for flexible CG) of the thread's rows to d1 (d2).
 template <bool FCG, bool PAD>
-__global__ void __launch_bounds__(kSpmvBlock)
-    k_lattice_spmv(LatticeQ1Op op, const float* __restrict__ p, float* __restrict__ q,
-                   const float* __restrict__ rr, double* __restrict__ partials, SolverState* S) {
-  __shared__ double sh[kSpmvBlock / 32];
-  if (S->done) return;
+__device__ __forceinline__ void lattice_tile(const LatticeQ1Op& op, int bx, int by, int bz,
+                                             const float* __restrict__ p, float* __restrict__ q,
+                                             const float* __restrict__ rr, float& d1,
+                                             float& d2) {
   const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
-  const int i = (int)(blockIdx.x * 32 + (threadIdx.x & 31));
-  const int j = (int)(blockIdx.y * 8 + (threadIdx.x >> 5));
-  const int k0 = (int)blockIdx.z * kLatK;
-  float d1 = 0.f, d2 = 0.f;
+  const int i = bx * 32 + (int)(threadIdx.x & 31);
+  const int j = by * 8 + (int)(threadIdx.x >> 5);
+  const int k0 = bz * kLatK;
   if (i < m0 && j < m1) {
     const bool okx[3] = {i > 0, true, i < m0 - 1};
     const bool oky[3] = {j > 0, true, j < m1 - 1};
@@ -561,6 +561,17 @@ __global__ void __launch_bounds__(kSpmvBlock)
       for (int e = 0; e < 4; ++e) ka[e] = kb[e];
     }
   }
+}
+
+template <bool FCG, bool PAD>
+__global__ void __launch_bounds__(kSpmvBlock)
+    k_lattice_spmv(LatticeQ1Op op, const float* __restrict__ p, float* __restrict__ q,
+                   const float* __restrict__ rr, double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kSpmvBlock / 32];
+  if (S->done) return;
+  float d1 = 0.f, d2 = 0.f;
+  lattice_tile<FCG, PAD>(op, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, p, q, rr, d1,
+                         d2);
   const double s1 = block_sum_f<kSpmvBlock>(d1, sh);
   double s2 = 0.0;
   if (FCG) s2 = block_sum_f<kSpmvBlock>(d2, sh);

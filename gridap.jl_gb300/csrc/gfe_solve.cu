@@ -19,6 +19,8 @@
 #include <cstdint>
 #include <type_traits>
 
+#include <cuda.h>  // CUtensorMap (the encoder is looked up at run time)
+
 #include "gfe_internal.h"
 
 namespace gfe {
@@ -300,11 +302,14 @@ __global__ void k_lattice_check(const int32_t* __restrict__ ids, int64_t n0, int
   }
 }
 
-__global__ void k_coef_to_f32(const double* __restrict__ c, int kind, int64_t n,
-                              float* __restrict__ out) {
+// kappa in FP32 at the lattice operator's cell layout: rows of n0 cells padded to a
+// multiple of 4 (16-byte row strides, as the tensor-map copies of the operator require)
+__global__ void k_coef_to_f32(const double* __restrict__ c, int kind, int64_t n0, int64_t c1,
+                              int64_t n, float* __restrict__ out) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = kind == GFE_COEF_CELL ? (float)c[i] : kind == GFE_COEF_CONST ? (float)c[0] : 1.f;
+    out[(i % n0) + c1 * (i / n0)] =
+        kind == GFE_COEF_CELL ? (float)c[i] : kind == GFE_COEF_CONST ? (float)c[0] : 1.f;
 }
 
 int attach_lattice_operator(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p,
@@ -318,13 +323,16 @@ int attach_lattice_operator(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p,
   if (n0 * n1 >= ((int64_t)1 << 31) || n2 - 1 > 65535 || (n1 - 1 + 7) / 8 > 65535)
     return GFE_OK;
   const int64_t nc = A->ncells;
+  const int64_t c1 = (n0 + 3) & ~(int64_t)3;
   A->mf_kap32.owner = A->mf_flag.owner = ctx;
-  GFE_TRY(A->mf_kap32.reserve(sizeof(float) * (size_t)nc));
+  GFE_TRY(A->mf_kap32.reserve(sizeof(float) * (size_t)(c1 * n1 * n2)));
+  GFE_CUDA_TRY(cudaMemsetAsync(A->mf_kap32.ptr, 0, sizeof(float) * (size_t)(c1 * n1 * n2),
+                               ctx->stream));
   GFE_TRY(A->mf_flag.reserve(sizeof(int) * 4));
   GFE_CUDA_TRY(cudaMemsetAsync(A->mf_flag.ptr, 0, sizeof(int), ctx->stream));
   const unsigned g = grid_for(nc, 256, (int64_t)ctx->num_sms * 8);
-  k_coef_to_f32<<<g, 256, 0, ctx->stream>>>(d_coef, d_coef ? p->coef_kind : GFE_COEF_ONE, nc,
-                                            A->mf_kap32.as<float>());
+  k_coef_to_f32<<<g, 256, 0, ctx->stream>>>(d_coef, d_coef ? p->coef_kind : GFE_COEF_ONE, n0,
+                                            c1, nc, A->mf_kap32.as<float>());
   k_lattice_check<<<g, 256, 0, ctx->stream>>>(A->cell_rows.as<int32_t>(), n0, n1, n2,
                                               A->mf_flag.as<int>());
   ctx->launches += 2;
@@ -439,8 +447,8 @@ struct LatticeQ1Op {
   const float* kap;
   int n0, n1, n2;   // cells per direction
   int s1, s2;       // row strides of j and k: m0 and m0*m1 (m = n - 1 interior nodes)
-  int c1, c2;       // cell strides of j and k: n0 and n0*n1
-  int p1, p2;       // strides of the zero-halo padded layout: m0 + 2 and (m0 + 2)(m1 + 2)
+  int c1, c2;       // cell strides of j and k: n0 rounded up to 4, and c1*n1
+  int p1, p2;       // strides of the zero-halo padded layout: m0 + 2 rounded up to 4, p1*(m1+2)
   float K[64];      // Kref[li + 8 lj], symmetric
   // padded index of interior node (i, j, k): halo of one zero entry on every side
   __host__ __device__ int64_t pad_index(int i, int j, int k) const {
@@ -451,9 +459,14 @@ struct LatticeQ1Op {
     return dim3((unsigned)((n0 - 1 + 31) / 32), (unsigned)((n1 - 1 + 7) / 8),
                 (unsigned)((n2 - 1 + kLatK - 1) / kLatK));
   }
-  unsigned blocks(int64_t n) const {
+  // grid of the tensor-map kernel: k-tiles of kz planes
+  dim3 grid_k(int kz) const {
+    return dim3((unsigned)((n0 - 1 + 31) / 32), (unsigned)((n1 - 1 + 7) / 8),
+                (unsigned)((n2 - 1 + kz - 1) / kz));
+  }
+  unsigned blocks(int64_t n) const {  // covers both grids (partials are sized from it)
     const dim3 g = grid(n);
-    return g.x * g.y * g.z;
+    return g.x * g.y * g.z * (kLatK / 2);
   }
 };
 
@@ -598,6 +611,209 @@ __global__ void __launch_bounds__(kSpmvBlock)
   }
 }
 
+// ---- lattice SpMV with the tile staged by the tensor-memory accelerator ---------------------
+// The same rows and arithmetic as k_lattice_spmv<false, true>, but the block's halo of p
+// (34 x 10 x (kLatK + 2) padded nodes) and of kappa (33 x 9 x (kLatK + 1) cells) arrive in
+// shared memory through two cp.async.bulk.tensor copies issued by one thread, completing on
+// an mbarrier; the k-march then reads its planes from shared memory instead of waiting on L1/L2
+// for 13 loads per row. Boxes are 36 floats wide (16-byte rows); their x origin, 32 bx, is a
+// multiple of 4 floats. Boxes past the arrays' ends read zeros.
+// The TMA tiles march over kTmaK planes: smaller tiles than the register kernel's, so that
+// the 128^3 grid (2048 blocks) spreads evenly over the SMs at six resident blocks each.
+constexpr int kTmaK = 4;
+constexpr int kTmaX = 36, kTmaPY = 10, kTmaPZ = kTmaK + 2, kTmaKY = 9, kTmaKZ = kTmaK + 1;
+constexpr unsigned long long kTmaWaitNs = 1000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long gtimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// bounded wait on phase `phase` of an mbarrier (false after kTmaWaitNs)
+__device__ __forceinline__ bool tma_bar_wait(uint32_t bar, uint32_t phase) {
+  const unsigned long long t0 = gtimer_ns();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (done) return true;
+    if (gtimer_ns() - t0 > kTmaWaitNs) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];"
+      :
+      : "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kSpmvBlock, 6)
+    k_lattice_spmv_tma(const __grid_constant__ CUtensorMap tmap_p,
+                       const __grid_constant__ CUtensorMap tmap_k, LatticeQ1Op op,
+                       float* __restrict__ q, double* __restrict__ partials, SolverState* S,
+                       DevError* err) {
+  __shared__ alignas(128) float sp[kTmaPZ][kTmaPY][kTmaX];
+  __shared__ alignas(128) float sk[kTmaKZ][kTmaKY][kTmaX];
+  __shared__ alignas(8) uint64_t bar;
+  __shared__ double sh[kSpmvBlock / 32];
+  if (S->done) return;
+  const int bx = (int)blockIdx.x, by = (int)blockIdx.y, k0 = (int)blockIdx.z * kTmaK;
+  const uint32_t b = smem_u32(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b),
+                 "r"((uint32_t)(sizeof(sp) + sizeof(sk)))
+                 : "memory");
+    tma_load_3d(smem_u32(&sp[0][0][0]), &tmap_p, 32 * bx, 8 * by, k0, b);
+    tma_load_3d(smem_u32(&sk[0][0][0]), &tmap_k, 32 * bx, 8 * by, k0, b);
+  }
+  // one thread polls the barrier (the others wait at bar.sync without taking issue slots)
+  __shared__ int landed;
+  if (threadIdx.x == 0) {
+    landed = tma_bar_wait(b, 0) ? 1 : 0;
+    if (!landed) {  // the copies did not land in time: report, wait once more, skip the tile
+      raise_e(err, GFE_ERR_TIMEOUT, (long long)block_linear());
+      tma_bar_wait(b, 0);
+      S->done = 1;
+    }
+  }
+  __syncthreads();
+  float d1 = 0.f;
+  if (landed) {
+    const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
+    const int lane = (int)(threadIdx.x & 31), wy = (int)(threadIdx.x >> 5);
+    const int i = 32 * bx + lane, j = 8 * by + wy;
+    if (i < m0 && j < m1) {
+      float xa[9], xb[9], xc[9], ka[4], kb[4];
+      auto xplane = [&](int t, float* xv) {  // plane k0 + t - 1 (t = 0 .. kTmaK + 1)
+#pragma unroll
+        for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+          for (int dx = 0; dx < 3; ++dx) xv[dx + 3 * dy] = sp[t][wy + dy][lane + dx];
+      };
+      auto kplane = [&](int t, float* kv) {  // cell layer k0 + t
+#pragma unroll
+        for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+          for (int cx = 0; cx < 2; ++cx) kv[cx + 2 * cy] = sk[t][wy + cy][lane + cx];
+      };
+      xplane(0, xa);
+      xplane(1, xb);
+      kplane(0, ka);
+      const int64_t col = op.pad_index(i, j, 0);
+#pragma unroll
+      for (int t = 0; t < kTmaK; ++t) {
+        const int k = k0 + t;
+        if (k < m2) {
+          xplane(t + 2, xc);
+          kplane(t + 1, kb);
+          float acc = 0.f;
+#pragma unroll
+          for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+            for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+              for (int cx = 0; cx < 2; ++cx) {
+                const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
+                float s = 0.f;
+#pragma unroll
+                for (int lc = 0; lc < 8; ++lc) {
+                  const int ix = cx + (lc & 1), iy = cy + ((lc >> 1) & 1), iz = cz + (lc >> 2);
+                  const float xv = iz == 0 ? xa[ix + 3 * iy] : iz == 1 ? xb[ix + 3 * iy]
+                                                                       : xc[ix + 3 * iy];
+                  s = fmaf(op.K[lr + 8 * lc], xv, s);
+                }
+                acc = fmaf(cz == 0 ? ka[cx + 2 * cy] : kb[cx + 2 * cy], s, acc);
+              }
+          q[col + (int64_t)op.p2 * k] = acc;
+          d1 = fmaf(xb[4], acc, d1);
+        }
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+          xa[e] = xb[e];
+          xb[e] = xc[e];
+        }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) ka[e] = kb[e];
+      }
+    }
+  }
+  const double s1 = block_sum_f<kSpmvBlock>(d1, sh);
+  if (threadIdx.x == 0) partials[block_linear()] = s1;
+  double tot[1];
+  if (last_block_reduce<kSpmvBlock, 1>(&S->ticket[0], partials, grid_blocks(), tot, sh) &&
+      threadIdx.x == 0) {
+    S->pq = tot[0];
+    S->alpha = tot[0] != 0.0 ? S->rz / tot[0] : 0.0;
+  }
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once (no link-time dependency).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn tensor_map_encoder() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult qr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &qr) == cudaSuccess &&
+        qr == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+    else
+      (void)cudaGetLastError();
+  }
+  return fn;
+}
+
+// Tensor maps of the padded p vector (p1, m1 + 2, m2 + 2) and of kappa (c1, n1, n2) with the
+// boxes of k_lattice_spmv_tma. False when the encoder is unavailable or refuses.
+static bool lattice_tensor_maps(const LatticeQ1Op& op, const float* p, CUtensorMap* tp,
+                                CUtensorMap* tk) {
+  EncodeTiledFn enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(p) & 15) || (reinterpret_cast<uintptr_t>(op.kap) & 15))
+    return false;
+  const cuuint32_t ones[3] = {1, 1, 1};
+  const cuuint64_t pd[3] = {(cuuint64_t)op.p1, (cuuint64_t)op.n1 + 1, (cuuint64_t)op.n2 + 1};
+  const cuuint64_t ps[2] = {(cuuint64_t)op.p1 * 4, (cuuint64_t)op.p2 * 4};
+  const cuuint32_t pb[3] = {kTmaX, kTmaPY, kTmaPZ};
+  const cuuint64_t kd[3] = {(cuuint64_t)op.c1, (cuuint64_t)op.n1, (cuuint64_t)op.n2};
+  const cuuint64_t ks[2] = {(cuuint64_t)op.c1 * 4, (cuuint64_t)op.c2 * 4};
+  const cuuint32_t kb[3] = {kTmaX, kTmaKY, kTmaKZ};
+  if (enc(tp, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(p), pd, ps, pb, ones,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  if (enc(tk, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(op.kap), kd, ks, kb, ones,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  return true;
+}
+
 static LatticeQ1Op lattice_op(const gfe_matrix* A) {
   LatticeQ1Op op;
   op.kap = A->mf_kap32.as<float>();
@@ -606,10 +822,10 @@ static LatticeQ1Op lattice_op(const gfe_matrix* A) {
   op.n2 = (int)A->mf_n[2];
   op.s1 = op.n0 - 1;
   op.s2 = (op.n0 - 1) * (op.n1 - 1);
-  op.c1 = op.n0;
-  op.c2 = op.n0 * op.n1;
-  op.p1 = op.n0 + 1;
-  op.p2 = (op.n0 + 1) * (op.n1 + 1);
+  op.c1 = (op.n0 + 3) & ~3;  // 16-byte row strides (tensor-map copies)
+  op.c2 = op.c1 * op.n1;
+  op.p1 = (op.n0 + 1 + 3) & ~3;
+  op.p2 = op.p1 * (op.n1 + 1);
   for (int e = 0; e < 64; ++e) op.K[e] = A->mf_K[e];
   return op;
 }
@@ -1225,11 +1441,26 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
   // the context while its launch parameters match) and replayed. With timing on, every
   // iteration is launched directly with CUDA events around the SpMV; launches after the
   // converged iteration (they return at once) are dropped from the timing.
+  // the lattice operator's halos arrive by tensor-map copies where the encoder is available
+  CUtensorMap tmap_p, tmap_k;
+  bool tma = false;
+  if constexpr (std::is_same<Op, LatticeQ1Op>::value) {
+    tma = lattice_tensor_maps(op, reinterpret_cast<const float*>(p), &tmap_p, &tmap_k);
+    // six resident blocks of 15 KB each: prefer shared memory over L1 for this kernel
+    if (tma)
+      GFE_CUDA_TRY(cudaFuncSetAttribute(k_lattice_spmv_tma,
+                                        cudaFuncAttributePreferredSharedMemoryCarveout,
+                                        (int)cudaSharedmemCarveoutMaxShared));
+  }
   auto launch_spmv = [&]() {
-    if constexpr (std::is_same<Op, LatticeQ1Op>::value)
-      k_lattice_spmv<false, true><<<gs, kSpmvBlock, 0, ctx->stream>>>(op, p, q, nullptr,
-                                                                      w.partials, w.S);
-    else
+    if constexpr (std::is_same<Op, LatticeQ1Op>::value) {
+      if (tma)
+        k_lattice_spmv_tma<<<op.grid_k(kTmaK), kSpmvBlock, 0, ctx->stream>>>(
+            tmap_p, tmap_k, op, q, w.partials, w.S, ctx->d_err);
+      else
+        k_lattice_spmv<false, true><<<gs, kSpmvBlock, 0, ctx->stream>>>(op, p, q, nullptr,
+                                                                        w.partials, w.S);
+    } else
       k_cg_spmv_dot<T, Op><<<gs, kSpmvBlock, 0, ctx->stream>>>(n, op, p, q, w.partials, w.S);
   };
   auto launch_vec = [&](unsigned g) {
@@ -1259,6 +1490,7 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
     mix(&check_every, sizeof(check_every));
     mix(&gv, sizeof(gv));
     mix(&vec4, sizeof(vec4));
+    mix(&tma, sizeof(tma));
     const int tsize = (int)sizeof(T);
     mix(&tsize, sizeof(tsize));
     if (ctx->cg_exec && ctx->cg_key == key) exec = ctx->cg_exec;

@@ -140,6 +140,37 @@ class ClockSampler:
                 "samples": len(rows), "period_ms": 50}
 
 
+def mg_levels(n):
+    """Cell counts per direction of the multigrid levels (halved while even and >= 8)."""
+    lv = [n]
+    while lv[-1] % 2 == 0 and lv[-1] >= 8:
+        lv.append(lv[-1] // 2)
+    return lv
+
+
+def vcycle_bytes(n):
+    """Algorithmic bytes of one V-cycle (FP32): per level with R rows, C cells and Rc coarse
+    rows, the first sweep (b, D read, x written: 12 R), each further sweep and the residual a
+    lattice apply (kappa 4 C, x read and t written 8 R) and an update (b, t, D, x read, x
+    written: 20 R), restriction (b, t read 8 R, 4 Rc written), prolongation (4 Rc read, x
+    read and written 8 R): 16 C + 120 R + 8 Rc per level; the coarsest level eight sweeps."""
+    lv = mg_levels(n)
+    tot = 0
+    for i, m in enumerate(lv):
+        R, C = (m - 1) ** 3, m ** 3
+        if i + 1 < len(lv):
+            tot += 16 * C + 120 * R + 8 * (lv[i + 1] - 1) ** 3
+        else:
+            tot += 12 * R + 7 * (4 * C + 28 * R)
+    return tot
+
+
+def assembly_bytes(nnz, n, ncells):
+    """Row-gather numeric loop of Q1 diffusion: per cell reference its id (4 B), the 8-byte
+    position table row and kappa (8 B); every stored value and b written (8 B)."""
+    return ncells * 8 * (4 + 8 + 8) + nnz * 8 + n * 8
+
+
 def spmv_bytes(nnz, n, s):
     """Algorithmic bytes of one CSR SpMV: values + column ids + row pointers + x + y."""
     return nnz * (s + 4) + (n + 1) * 4 + n * 2 * s
@@ -208,13 +239,20 @@ def run_gpu(args):
                                                           _lib.ptr(b)))
             o = solver.opts()
             rep = _lib.SolveReport()
-            _lib.check(lib.gfe_solve(ctx.handle, h, ctypes.byref(o), _lib.ptr(b), _lib.ptr(x),
-                                     ctypes.byref(rep)))
+            if isinstance(solver, gg.FCGSolver):
+                _lib.check(lib.gfe_solve_fcg(ctx.handle, h, None, ctypes.byref(o), _lib.ptr(b),
+                                             _lib.ptr(x), ctypes.byref(rep)))
+            else:
+                _lib.check(lib.gfe_solve(ctx.handle, h, ctypes.byref(o), _lib.ptr(b),
+                                         _lib.ptr(x), ctypes.byref(rep)))
         finally:
             lib.gfe_matrix_destroy(h)
         return rep
 
-    mixed = gg.MixedCGSolver(rtol=w.rtol, inner_rtol=args.delta)
+    # headline: flexible CG (FP32, FP64 reliable updates) with the multigrid V-cycle; the
+    # Jacobi mixed CG of the same precision scheme and the plain FP64 CG are measured beside
+    mixed_cg = gg.MixedCGSolver(rtol=w.rtol, inner_rtol=args.delta)
+    mixed = gg.FCGSolver(rtol=w.rtol, pc="mg") if args.solver == "mg" else mixed_cg
     plain = gg.CGSolver(rtol=w.rtol)
 
     def barrier():
@@ -279,6 +317,8 @@ def run_gpu(args):
         x_mixed = x_d.clone()
         err_vs_fp64 = float(torch.linalg.norm(x_mixed - x_plain) / torch.linalg.norm(x_plain))
         r_e2e = timed("e2e", mixed_e2e, args.steps, max(3, args.warmup), kernel_timing=False)
+        r_mcg = (timed("mixed_cg", lambda: step(ids_d, kap_d, f_d, x_d, mixed_cg, b_d),
+                       args.steps, 3, kernel_timing=False) if mixed is not mixed_cg else r_mixed)
         clocks.clear()
 
     # learned arm: FCG with the learned block preconditioner (weights trained offline on
@@ -309,6 +349,9 @@ def run_gpu(args):
                 lib.gfe_matrix_destroy(h)
             return rep
 
+        fcg_mg = gg.FCGSolver(rtol=w.rtol, pc="mg")
+        r_mg = timed("mg_fcg", lambda: fcg_step(fcg_mg), args.steps, 3, kernel_timing=False)
+        rmg = r_mg["reps"][-1]
         r_l = timed("learned", lambda: fcg_step(fcg_l), args.steps, 3)
         r_j = timed("fcg_jacobi", lambda: fcg_step(fcg_j), args.steps, 3)
         rl, rj = r_l["reps"][-1], r_j["reps"][-1]
@@ -320,6 +363,11 @@ def run_gpu(args):
                                      max(r_l["kt"][_lib.GFE_KT_PRECOND][1], 1)),
             "fcg_jacobi": {"value": world * nfree / (r_j["ms"] * 1e-3), "ms_per_step": r_j["ms"],
                            "iterations": rj.iterations, "relres": rj.relres},
+            "fcg_multigrid": {"value": world * nfree / (r_mg["ms"] * 1e-3),
+                              "ms_per_step": r_mg["ms"], "iterations": rmg.iterations,
+                              "relres": rmg.relres,
+                              "preconditioner": "geometric multigrid V-cycle on the lattice "
+                                                "operator (FP32, 2+2 damped Jacobi sweeps)"},
             "training": "residual/local-solve pairs from FP64 Jacobi-PCG solves of 200 "
                         "independent 64^3 kappa draws (seeds 5000..5199)"}
 
@@ -339,7 +387,7 @@ def run_gpu(args):
             "assemble_ms": avg_ms(r_plain_kt, _lib.GFE_KT_ASSEMBLE)}
 
     rep_m, rep_p = r_mixed["reps"][-1], r_plain["reps"][-1]
-    for rp in r_mixed["reps"] + r_plain["reps"] + r_e2e["reps"]:
+    for rp in r_mixed["reps"] + r_plain["reps"] + r_e2e["reps"] + r_mcg["reps"]:
         if not rp.relres <= w.rtol * (1 + 1e-6):
             raise RuntimeError(f"solve did not reach rtol: relres={rp.relres}")
     value = replica_value(nfree, world, r_mixed["ms"])
@@ -370,7 +418,25 @@ def run_gpu(args):
         "vector32": dict(kernel="k_cg_update4 + k_cg_direction4 (FP32 CG vector updates)",
                          alg=44 * nfree, kt=r_mixed_kt["kt"][_lib.GFE_KT_VECTOR],
                          traffic=profile_traffic("fp32_vector")),
+        "assembly": dict(kernel="k_assemble_rows (row-gather numeric loop, FP64 cell "
+                                "integrals fused)",
+                         alg=assembly_bytes(nnz, nfree, ncells), traffic=None,
+                         kt=r_mixed_kt["kt"][_lib.GFE_KT_ASSEMBLE]),
     }
+    if isinstance(mixed, gg.FCGSolver):
+        # FCG: the lattice SpMV also reads r (p.r), its vector kernels move x, r, p, q (update)
+        # and z, q, p (beta + direction) in two timed pairs per iteration; the V-cycle is one
+        # graph launch timed as a whole
+        kinds["spmv32"].update(kernel="k_lattice_spmv<true, false> (matrix-free FP32 Q1 "
+                                      "operator + p.q, p.r)", alg=ncells * 4 + nfree * 12,
+                               traffic=None)
+        kinds["vector32"].update(kernel="k_fcg_update; k_fcg_beta + k_fcg_dir (FP32 FCG "
+                                        "vector updates)", alg=22 * nfree, traffic=None)
+        kinds["vcycle"] = dict(kernel="multigrid V-cycle (CUDA graph: k_mg_apply, k_mg_jacobi, "
+                                      "k_mg_restrict, k_mg_prolong over %d levels)"
+                                      % len(mg_levels(args.n)),
+                               alg=vcycle_bytes(args.n), traffic=None,
+                               kt=r_mixed_kt["kt"][_lib.GFE_KT_PRECOND])
     table = {}
     for k, d in kinds.items():
         tot, cnt = d["kt"]
@@ -390,9 +456,14 @@ def run_gpu(args):
         "data": "synthetic (seeded lognormal GRF kappa, N(0,1) nodal f)",
         "config": {"workload": f"lognormal_3d {args.n}^3 Q1 diffusion",
                    "free_dofs": nfree, "cells": ncells, "nnz": nnz, "rtol": w.rtol,
-                   "solver": f"mixed CG: FP32 Jacobi-PCG with FP64 reliable updates "
-                             f"(delta {args.delta}), FP64 x and true residual; inner "
-                             f"operator {rep_m.operator_format}",
+                   "solver": (f"flexible CG, FP32 vectors with FP64 reliable updates, "
+                              f"preconditioned by a geometric multigrid V-cycle on the "
+                              f"matrix-free lattice operator ({len(mg_levels(args.n))} levels, "
+                              f"2+2 damped Jacobi sweeps); FP64 x and true residual"
+                              if isinstance(mixed, gg.FCGSolver) else
+                              f"mixed CG: FP32 Jacobi-PCG with FP64 reliable updates "
+                              f"(delta {args.delta}), FP64 x and true residual; inner "
+                              f"operator {rep_m.operator_format}"),
                    "assembly": "FP64 cell integrals, FP64 row-gather scatter",
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (matrix %.2f GB)" % (nnz * 12 / 1e9)},
@@ -401,6 +472,12 @@ def run_gpu(args):
         "plain_fp64": {"value": plain_value, "ms_per_step": r_plain["ms"],
                        "solver": "FP64 Jacobi-PCG", "relres": rep_p.relres},
         "mixed_over_plain": value / plain_value,
+        "mixed_cg_jacobi": {"value": replica_value(nfree, world, r_mcg["ms"]),
+                            "ms_per_step": r_mcg["ms"],
+                            "iterations": r_mcg["reps"][-1].iterations,
+                            "relres": r_mcg["reps"][-1].relres,
+                            "solver": f"FP32 Jacobi-PCG with FP64 reliable updates (delta "
+                                      f"{args.delta}) on the matrix-free lattice operator"},
         "error_vs_fp64": {"rel_l2_solution": err_vs_fp64, "relres_mixed": rep_m.relres},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": r_e2e["ms"]},
@@ -878,6 +955,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gfe", choices=["gfe", "reference"])
     ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--solver", default="mg", choices=["mg", "mixed"],
+                    help="headline solver: multigrid-preconditioned flexible CG or Jacobi mixed CG")
     ap.add_argument("--delta", type=float, default=0.01,
                     help="residual reduction between FP64 reliable updates of the mixed CG")
     ap.add_argument("--no-cpu-baseline", action="store_true")

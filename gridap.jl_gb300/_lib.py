@@ -35,7 +35,7 @@ GFE_LAW_POLY, GFE_LAW_POWER = 0, 1
 GFE_REORDER_RCM, GFE_REORDER_SLOAN = 0, 1
 GFE_PREC_FP64, GFE_PREC_FP32 = 0, 1
 GFE_SOLVER_CG, GFE_SOLVER_IR_CG, GFE_SOLVER_MIXED_CG, GFE_SOLVER_BICGSTAB = 0, 1, 2, 3
-GFE_PC_NONE, GFE_PC_JACOBI = 0, 1
+GFE_PC_NONE, GFE_PC_JACOBI, GFE_PC_MG = 0, 1, 2
 GFE_KT_SPMV64, GFE_KT_SPMV32, GFE_KT_ASSEMBLE, GFE_KT_RESIDUAL64, GFE_KT_ELEMENT = 0, 1, 2, 3, 4
 GFE_KT_PRECOND, GFE_KT_VECTOR = 5, 6
 

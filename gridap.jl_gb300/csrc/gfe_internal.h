@@ -249,6 +249,12 @@ void q1_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
                std::vector<double>& dphi);
 void q2_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
                std::vector<double>& dphi);
+// geometric multigrid V-cycle on the lattice operator (gfe_mg.cu)
+struct LatticeQ1Op;
+struct LatticeMG;
+int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out);
+int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done);
+void mg_destroy(LatticeMG* mg);
 // Jacobi-preconditioned FP64 BiCGStab from x = 0 (gfe_bicgstab.cu)
 int bicgstab(gfe_ctx* ctx, gfe_matrix* A, const double* dinv, const double* d_b, double* d_x,
              double rtol, int maxit, int* iterations);

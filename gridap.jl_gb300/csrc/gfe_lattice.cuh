@@ -1,0 +1,126 @@
+// gfe_lattice.cuh -- the matrix-free FP32 operator of uniform Cartesian Q1 diffusion (the
+// lattice operator) and its row kernel, shared by the CG solvers (gfe_solve.cu) and the
+// geometric multigrid preconditioner (gfe_mg.cu). Included inside namespace gfe.
+#pragma once
+
+// Matrix-free FP32 operator of uniform Cartesian Q1 diffusion on (n0, n1, n2) cells with rows
+// = interior nodes in node order (the CLagrangian numbering with every boundary node
+// Dirichlet): (A x)_r = sum over the 8 cells K around node r of kappa_K sum_c Kref[l_r, c]
+// x[node(K, c)], boundary nodes contributing 0 -- the cell-wise sum the assembled matrix
+// stores, applied with FP32 element matrices (kappa_K Kref). It reads kappa (4 B per cell)
+// and x instead of 27 values per row. Applied by k_lattice_spmv: a block covers a 32 x 8 tile
+// of (i, j) and kLatK consecutive k-planes; each thread marches up its k-column keeping the
+// three x-planes and two kappa-planes around its node in registers, so a row costs 9 x and 4
+// kappa loads.
+constexpr int kLatK = 8;
+
+struct LatticeQ1Op {
+  const float* kap;
+  int n0, n1, n2;   // cells per direction
+  int s1, s2;       // row strides of j and k: m0 and m0*m1 (m = n - 1 interior nodes)
+  int c1, c2;       // cell strides of j and k: n0 rounded up to 4, and c1*n1
+  int p1, p2;       // strides of the zero-halo padded layout: m0 + 2 rounded up to 4, p1*(m1+2)
+  float K[64];      // Kref[li + 8 lj], symmetric
+  // padded index of interior node (i, j, k): halo of one zero entry on every side
+  __host__ __device__ int64_t pad_index(int i, int j, int k) const {
+    return (int64_t)(i + 1) + (int64_t)p1 * (j + 1) + (int64_t)p2 * (k + 1);
+  }
+  int64_t padded_size() const { return (int64_t)p2 * (n2 + 1); }
+  __host__ __device__ dim3 grid(int64_t) const {
+    return dim3((unsigned)((n0 - 1 + 31) / 32), (unsigned)((n1 - 1 + 7) / 8),
+                (unsigned)((n2 - 1 + kLatK - 1) / kLatK));
+  }
+  // grid of the tensor-map kernel: k-tiles of kz planes
+  dim3 grid_k(int kz) const {
+    return dim3((unsigned)((n0 - 1 + 31) / 32), (unsigned)((n1 - 1 + 7) / 8),
+                (unsigned)((n2 - 1 + kz - 1) / kz));
+  }
+  unsigned blocks(int64_t n) const {  // covers both grids (partials are sized from it)
+    const dim3 g = grid(n);
+    return g.x * g.y * g.z * (kLatK / 2);
+  }
+};
+
+// The rows of one tile: (i, j) = (32 bx + lane, 8 by + warp), k-planes kLatK bz .. + kLatK.
+// Adds p.q (and p.r for flexible CG) of the thread's rows to d1 (d2).
+template <bool FCG, bool PAD>
+__device__ __forceinline__ void lattice_tile(const LatticeQ1Op& op, int bx, int by, int bz,
+                                             const float* __restrict__ p, float* __restrict__ q,
+                                             const float* __restrict__ rr, float& d1,
+                                             float& d2) {
+  const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
+  const int i = bx * 32 + (int)(threadIdx.x & 31);
+  const int j = by * 8 + (int)(threadIdx.x >> 5);
+  const int k0 = bz * kLatK;
+  if (i < m0 && j < m1) {
+    const bool okx[3] = {i > 0, true, i < m0 - 1};
+    const bool oky[3] = {j > 0, true, j < m1 - 1};
+    // row (or padded index) of (i, j, 0) and the strides between neighbours
+    const int64_t col = PAD ? op.pad_index(i, j, 0) : (int64_t)i + (int64_t)op.s1 * j;
+    const int sy = PAD ? op.p1 : op.s1, sz = PAD ? op.p2 : op.s2;
+    const float* kcol = op.kap + ((int64_t)i + (int64_t)op.c1 * j);
+    // x-plane kk (9 values around (i, j)); 0 outside the interior
+    auto xplane = [&](int kk, float* v) {
+      const bool okz = PAD || (kk >= 0 && kk < m2);
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          float t = 0.f;
+          if (PAD || (okz && okx[dx + 1] && oky[dy + 1]))
+            t = __ldg(p + col + (int64_t)sz * kk + dx + sy * dy);
+          v[(dx + 1) + 3 * (dy + 1)] = t;
+        }
+    };
+    // kappa-plane of cell layer kk: cells (i + cx, j + cy, kk)
+    auto kplane = [&](int kk, float* v) {
+#pragma unroll
+      for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+        for (int cx = 0; cx < 2; ++cx)
+          v[cx + 2 * cy] = __ldg(kcol + (int64_t)op.c2 * kk + cx + op.c1 * cy);
+    };
+    float xa[9], xb[9], xc[9], ka[4], kb[4];
+    xplane(k0 - 1, xa);
+    xplane(k0, xb);
+    kplane(k0, ka);
+#pragma unroll
+    for (int t = 0; t < kLatK; ++t) {
+      const int k = k0 + t;
+      if (k < m2) {
+        xplane(k + 1, xc);
+        kplane(k + 1, kb);
+        float acc = 0.f;
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+          for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+            for (int cx = 0; cx < 2; ++cx) {
+              const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
+              float s = 0.f;
+#pragma unroll
+              for (int lc = 0; lc < 8; ++lc) {
+                const int ix = cx + (lc & 1), iy = cy + ((lc >> 1) & 1), iz = cz + (lc >> 2);
+                const float xv = iz == 0 ? xa[ix + 3 * iy] : iz == 1 ? xb[ix + 3 * iy]
+                                                                     : xc[ix + 3 * iy];
+                s = fmaf(op.K[lr + 8 * lc], xv, s);
+              }
+              acc = fmaf(cz == 0 ? ka[cx + 2 * cy] : kb[cx + 2 * cy], s, acc);
+            }
+        const int64_t row = col + (int64_t)sz * k;
+        q[row] = acc;
+        d1 = fmaf(xb[4], acc, d1);
+        if (FCG) d2 = fmaf(xb[4], __ldg(rr + row), d2);
+      }
+#pragma unroll
+      for (int e = 0; e < 9; ++e) {
+        xa[e] = xb[e];
+        xb[e] = xc[e];
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) ka[e] = kb[e];
+    }
+  }
+}
+

@@ -1,0 +1,342 @@
+// gfe_mg.cu -- geometric multigrid V-cycle on the lattice operator, a preconditioner for the
+// flexible CG (gfe_solve_fcg with GFE_PC_MG). Gridap has no multigrid; this is the GPU
+// counterpart of a LinearSolver plug-in preconditioner for the uniform Cartesian Q1 problems
+// the lattice operator covers.
+//
+// Levels halve the cell counts while they stay even (at least 4 cells per direction). Each
+// level is again a lattice operator: kappa of a coarse cell is the mean of its 8 children and
+// the reference stiffness doubles (a Q1 stiffness on a box of sizes 2h is twice the one on h,
+// in 3-D), which for piecewise-constant kappa equals the Galerkin product P^T A P of the
+// nested Q1 spaces. Transfers are trilinear interpolation P and its transpose R = P^T (full
+// weighting 1, 1/2, 1/4, 1/8). Smoothing is damped Jacobi (omega 0.8, two sweeps before and
+// after, the first from zero), the coarsest level takes eight sweeps. All vectors are FP32 in
+// the lattice row order; every kernel returns at once when the solver's done flag is set.
+#include <vector>
+
+#include "gfe_internal.h"
+
+namespace gfe {
+#include "gfe_lattice.cuh"
+
+namespace {
+
+constexpr int kMgBlock = 256;
+constexpr float kOmega = 0.8f;
+constexpr int kPreSweeps = 2, kCoarseSweeps = 8;
+
+__device__ __forceinline__ bool stop(const int* done) { return done && *done; }
+
+__global__ void __launch_bounds__(kMgBlock)
+    k_mg_apply(LatticeQ1Op op, const float* __restrict__ x, float* __restrict__ y,
+               const int* done) {
+  if (stop(done)) return;
+  float d1 = 0.f, d2 = 0.f;
+  lattice_tile<false, false>(op, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, x, y,
+                             nullptr, d1, d2);
+}
+
+// x = omega D^-1 b  (first sweep from zero)
+__global__ void k_mg_jacobi0(int64_t n, const float* __restrict__ b,
+                             const float* __restrict__ dinv, float* __restrict__ x,
+                             const int* done) {
+  if (stop(done)) return;
+  for (int64_t i = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kMgBlock)
+    x[i] = kOmega * dinv[i] * b[i];
+}
+
+// x += omega D^-1 (b - t), t = A x
+__global__ void k_mg_jacobi(int64_t n, const float* __restrict__ b, const float* __restrict__ t,
+                            const float* __restrict__ dinv, float* __restrict__ x,
+                            const int* done) {
+  if (stop(done)) return;
+  for (int64_t i = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kMgBlock)
+    x[i] = fmaf(kOmega * dinv[i], b[i] - t[i], x[i]);
+}
+
+// b_c = R (b_f - t_f): coarse interior node (I, J, K) sits on fine interior node
+// (2I+1, 2J+1, 2K+1); weights prod_d (1 - |delta_d| / 2) over the 27 fine neighbours
+__global__ void k_mg_restrict(int mf0, int mf1, int mc0, int mc1, int mc2,
+                              const float* __restrict__ bf, const float* __restrict__ tf,
+                              float* __restrict__ bc, const int* done) {
+  if (stop(done)) return;
+  const int64_t nc = (int64_t)mc0 * mc1 * mc2;
+  for (int64_t c = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; c < nc;
+       c += (int64_t)gridDim.x * kMgBlock) {
+    const int I = (int)(c % mc0);
+    const int64_t rest = c / mc0;
+    const int J = (int)(rest % mc1), K = (int)(rest / mc1);
+    float s = 0.f;
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          const float w = (dx ? 0.5f : 1.f) * (dy ? 0.5f : 1.f) * (dz ? 0.5f : 1.f);
+          const int64_t f = (int64_t)(2 * I + 1 + dx) +
+                            (int64_t)mf0 * ((2 * J + 1 + dy) + (int64_t)mf1 * (2 * K + 1 + dz));
+          s = fmaf(w, bf[f] - tf[f], s);
+        }
+    bc[c] = s;
+  }
+}
+
+// x_f += P x_c (trilinear; coarse boundary nodes are zero)
+__global__ void k_mg_prolong(int mf0, int mf1, int mf2, int mc0, int mc1, int mc2,
+                             const float* __restrict__ xc, float* __restrict__ xf,
+                             const int* done) {
+  if (stop(done)) return;
+  const int64_t nf = (int64_t)mf0 * mf1 * mf2;
+  for (int64_t f = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; f < nf;
+       f += (int64_t)gridDim.x * kMgBlock) {
+    const int i = (int)(f % mf0);
+    const int64_t rest = f / mf0;
+    const int j = (int)(rest % mf1), k = (int)(rest / mf1);
+    // lattice positions i+1 etc.; coarse lattice position p/2 (even) or between (odd)
+    int ci[2], cj[2], ck[2];
+    float wi[2], wj[2], wk[2];
+    auto axis = [](int p, int mc, int* cc, float* ww) {  // p = lattice position (1-based)
+      if ((p & 1) == 0) {
+        cc[0] = p / 2 - 1;
+        ww[0] = 1.f;
+        cc[1] = -1;
+        ww[1] = 0.f;
+      } else {
+        cc[0] = p / 2 - 1;  // coarse interior index of lattice p/2 (-1: boundary)
+        cc[1] = p / 2;      // of lattice p/2 + 1 (mc: boundary)
+        ww[0] = ww[1] = 0.5f;
+        if (cc[1] >= mc) cc[1] = -1;
+      }
+    };
+    axis(i + 1, mc0, ci, wi);
+    axis(j + 1, mc1, cj, wj);
+    axis(k + 1, mc2, ck, wk);
+    float s = 0.f;
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+        for (int cc = 0; cc < 2; ++cc) {
+          if (ci[a] < 0 || cj[bb] < 0 || ck[cc] < 0) continue;
+          const float w = wi[a] * wj[bb] * wk[cc];
+          if (w == 0.f) continue;
+          s = fmaf(w, xc[(int64_t)ci[a] + (int64_t)mc0 * (cj[bb] + (int64_t)mc1 * ck[cc])], s);
+        }
+    xf[f] += s;
+  }
+}
+
+// coarse kappa = mean of the 8 children (padded row strides cf1, cc1)
+__global__ void k_mg_kappa(int nc0, int nc1, int nc2, int cf1, int nf1, int cc1,
+                           const float* __restrict__ kf, float* __restrict__ kc) {
+  const int64_t n = (int64_t)nc0 * nc1 * nc2;
+  for (int64_t c = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * kMgBlock) {
+    const int I = (int)(c % nc0);
+    const int64_t rest = c / nc0;
+    const int J = (int)(rest % nc1), K = (int)(rest / nc1);
+    float s = 0.f;
+    for (int e = 0; e < 8; ++e) {
+      const int i = 2 * I + (e & 1), j = 2 * J + ((e >> 1) & 1), k = 2 * K + (e >> 2);
+      s += kf[(int64_t)i + (int64_t)cf1 * (j + (int64_t)nf1 * k)];
+    }
+    kc[(int64_t)I + (int64_t)cc1 * (J + (int64_t)nc1 * K)] = 0.125f * s;
+  }
+}
+
+// D^-1 of a lattice operator: D_r = sum of kappa_K Kref[l_r, l_r] over the 8 cells around r
+__global__ void k_mg_diag(LatticeQ1Op op, float* __restrict__ dinv) {
+  const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
+  const int64_t n = (int64_t)m0 * m1 * m2;
+  for (int64_t r = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * kMgBlock) {
+    const int i = (int)(r % m0);
+    const int64_t rest = r / m0;
+    const int j = (int)(rest % m1), k = (int)(rest / m1);
+    float d = 0.f;
+    for (int e = 0; e < 8; ++e) {
+      const int cx = e & 1, cy = (e >> 1) & 1, cz = e >> 2;
+      const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
+      d += op.kap[(int64_t)(i + cx) + (int64_t)op.c1 * (j + cy) + (int64_t)op.c2 * (k + cz)] *
+           op.K[lr + 8 * lr];
+    }
+    dinv[r] = d > 0.f ? 1.f / d : 0.f;
+  }
+}
+
+}  // namespace
+
+struct LatticeMG {
+  struct Level {
+    LatticeQ1Op op;
+    int m0, m1, m2;
+    int64_t n;
+    float *x, *b, *t, *dinv;
+  };
+  gfe_ctx* ctx;
+  std::vector<Level> lv;
+  DevBuf buf;
+  // the V-cycle's launches, captured once per (r, z, done) and replayed
+  cudaGraphExec_t exec = nullptr;
+  const float* cap_r = nullptr;
+  float* cap_z = nullptr;
+  const int* cap_done = nullptr;
+  long long nodes = 0;
+  explicit LatticeMG(gfe_ctx* c) : ctx(c), buf(c) {}
+  ~LatticeMG() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+namespace {
+
+unsigned vgrid(gfe_ctx* ctx, int64_t n) {
+  return (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>((n + kMgBlock - 1) / kMgBlock, (int64_t)ctx->num_sms * 8));
+}
+
+int vcycle(LatticeMG* mg, size_t l, const int* done) {
+  gfe_ctx* ctx = mg->ctx;
+  LatticeMG::Level& L = mg->lv[l];
+  const unsigned g = vgrid(ctx, L.n);
+  const dim3 ga = L.op.grid(L.n);
+  const bool coarsest = l + 1 == mg->lv.size();
+  const int pre = coarsest ? kCoarseSweeps : kPreSweeps;
+  k_mg_jacobi0<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.dinv, L.x, done);
+  ctx->launches++;
+  for (int s = 1; s < pre; ++s) {
+    k_mg_apply<<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.t, done);
+    k_mg_jacobi<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.t, L.dinv, L.x, done);
+    ctx->launches += 2;
+  }
+  if (coarsest) return GFE_OK;
+  LatticeMG::Level& C = mg->lv[l + 1];
+  k_mg_apply<<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.t, done);
+  k_mg_restrict<<<vgrid(ctx, C.n), kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, C.m0, C.m1, C.m2,
+                                                               L.b, L.t, C.b, done);
+  ctx->launches += 2;
+  GFE_TRY(vcycle(mg, l + 1, done));
+  k_mg_prolong<<<g, kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, L.m2, C.m0, C.m1, C.m2, C.x, L.x,
+                                                done);
+  ctx->launches++;
+  for (int s = 0; s < kPreSweeps; ++s) {
+    k_mg_apply<<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.t, done);
+    k_mg_jacobi<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.t, L.dinv, L.x, done);
+    ctx->launches += 2;
+  }
+  return GFE_OK;
+}
+
+}  // namespace
+
+// Levels below the fine lattice operator; the fine level's b and x are set per apply.
+int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out) {
+  LatticeMG* mg = new LatticeMG(ctx);
+  *out = mg;
+  std::vector<LatticeQ1Op> ops{fine};
+  while (ops.size() < 12) {
+    const LatticeQ1Op& f = ops.back();
+    if ((f.n0 & 1) || (f.n1 & 1) || (f.n2 & 1) || f.n0 < 8 || f.n1 < 8 || f.n2 < 8) break;
+    LatticeQ1Op c = f;
+    c.n0 = f.n0 / 2;
+    c.n1 = f.n1 / 2;
+    c.n2 = f.n2 / 2;
+    c.s1 = c.n0 - 1;
+    c.s2 = (c.n0 - 1) * (c.n1 - 1);
+    c.c1 = (c.n0 + 3) & ~3;
+    c.c2 = c.c1 * c.n1;
+    c.p1 = (c.n0 + 1 + 3) & ~3;
+    c.p2 = c.p1 * (c.n1 + 1);
+    for (int e = 0; e < 64; ++e) c.K[e] = 2.f * f.K[e];
+    c.kap = nullptr;
+    ops.push_back(c);
+  }
+  // one buffer: per level x, b, t, dinv (+ kappa below the fine level), 256-byte aligned
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t total = 0;
+  for (size_t l = 0; l < ops.size(); ++l) {
+    const int64_t n = (int64_t)(ops[l].n0 - 1) * (ops[l].n1 - 1) * (ops[l].n2 - 1);
+    total += 4 * al(sizeof(float) * n);
+    if (l) total += al(sizeof(float) * (size_t)ops[l].c2 * ops[l].n2);
+  }
+  GFE_TRY(mg->buf.reserve(total));
+  char* p = (char*)mg->buf.ptr;
+  for (size_t l = 0; l < ops.size(); ++l) {
+    LatticeMG::Level L;
+    L.op = ops[l];
+    L.m0 = L.op.n0 - 1;
+    L.m1 = L.op.n1 - 1;
+    L.m2 = L.op.n2 - 1;
+    L.n = (int64_t)L.m0 * L.m1 * L.m2;
+    const size_t vb = al(sizeof(float) * L.n);
+    L.x = (float*)p;
+    L.b = (float*)(p + vb);
+    L.t = (float*)(p + 2 * vb);
+    L.dinv = (float*)(p + 3 * vb);
+    p += 4 * vb;
+    if (l) {
+      float* kc = (float*)p;
+      p += al(sizeof(float) * (size_t)L.op.c2 * L.op.n2);
+      const LatticeQ1Op& f = mg->lv.back().op;
+      GFE_CUDA_TRY(cudaMemsetAsync(kc, 0, sizeof(float) * (size_t)L.op.c2 * L.op.n2,
+                                   ctx->stream));
+      k_mg_kappa<<<vgrid(ctx, (int64_t)L.op.n0 * L.op.n1 * L.op.n2), kMgBlock, 0,
+                   ctx->stream>>>(L.op.n0, L.op.n1, L.op.n2, f.c1, f.n1, L.op.c1, f.kap, kc);
+      ctx->launches++;
+      L.op.kap = kc;
+    }
+    k_mg_diag<<<vgrid(ctx, L.n), kMgBlock, 0, ctx->stream>>>(L.op, L.dinv);
+    ctx->launches++;
+    mg->lv.push_back(L);
+  }
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+// z = V-cycle(r) on the fine lattice rows
+int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done) {
+  gfe_ctx* ctx = mg->ctx;
+  if (!mg->exec || mg->cap_r != r || mg->cap_z != z || mg->cap_done != done) {
+    if (mg->exec) {
+      cudaGraphExecDestroy(mg->exec);
+      mg->exec = nullptr;
+    }
+    mg->lv[0].b = const_cast<float*>(r);
+    mg->lv[0].x = z;
+    const long long l0 = ctx->launches;
+    cudaGraph_t graph = nullptr;
+    GFE_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int st = vcycle(mg, 0, done);
+    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+    ctx->launches = l0;  // counted when replayed
+    if (st != GFE_OK || ce != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return st != GFE_OK ? st
+                          : set_error(GFE_ERR_CUDA, "multigrid: graph capture failed: %s",
+                                      cudaGetErrorString(ce));
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&mg->exec, graph, 0);
+    size_t nodes = 0;
+    cudaGraphGetNodes(graph, nullptr, &nodes);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess)
+      return set_error(GFE_ERR_CUDA, "multigrid: graph instantiate failed: %s",
+                       cudaGetErrorString(ie));
+    mg->cap_r = r;
+    mg->cap_z = z;
+    mg->cap_done = done;
+    mg->nodes = (long long)nodes;
+  }
+  timer_begin(ctx, GFE_KT_PRECOND);
+  GFE_CUDA_TRY(cudaGraphLaunch(mg->exec, ctx->stream));
+  timer_end(ctx);
+  ctx->launches += mg->nodes;
+  return GFE_OK;
+}
+
+void mg_destroy(LatticeMG* mg) { delete mg; }
+
+}  // namespace gfe

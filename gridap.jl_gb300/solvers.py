@@ -84,12 +84,18 @@ class BiCGStabSolver(LinearSolver):
 
 class FCGSolver(LinearSolver):
     """Flexible CG with FP32 vectors and FP64 reliable updates, preconditioned by a
-    LearnedBlockPreconditioner (`pc`) or by Jacobi (pc=None); a stagnating learned
-    preconditioner hands over to Jacobi (report.fallback)."""
+    LearnedBlockPreconditioner (`pc`), by a geometric multigrid V-cycle on the lattice
+    operator (pc="mg"; uniform Cartesian Q1 in 3-D) or by Jacobi (pc=None); a stagnating
+    learned preconditioner hands over to Jacobi (report.fallback)."""
 
     def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, pc=None,
-                 inner_rtol: float = 0.1, check_every: int = 0, initial_guess: bool = False):
+                 inner_rtol: float = 0.0, check_every: int = 0, initial_guess: bool = False):
+        # inner_rtol 0: the library's reliable-update threshold (0.1; 1e-3 with pc="mg")
         super().__init__(rtol, maxiter, "jacobi", inner_rtol, check_every, initial_guess)
+        if isinstance(pc, str):
+            if pc != "mg":
+                raise ValueError(f"unknown preconditioner {pc!r}")
+            self.precond, pc = _lib.GFE_PC_MG, None
         self.pc = pc
 
 

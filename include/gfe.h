@@ -306,7 +306,13 @@ enum {
   GFE_SOLVER_MIXED_CG = 2,
   GFE_SOLVER_BICGSTAB = 3  /* FP64 BiCGStab, Jacobi (right) preconditioner: non-symmetric A */
 };
-enum { GFE_PC_NONE = 0, GFE_PC_JACOBI = 1 };
+enum {
+  GFE_PC_NONE = 0,
+  GFE_PC_JACOBI = 1,
+  GFE_PC_MG = 2  /* gfe_solve_fcg without a learned pc: geometric multigrid V-cycle on the
+                    lattice operator (uniform Cartesian Q1 in 3-D; FP32, damped Jacobi
+                    smoothing, trilinear transfers, kappa averaged to coarse cells) */
+};
 
 typedef struct gfe_solver_opts {
   int32_t method;       /* GFE_SOLVER_CG: FP64 PCG; GFE_SOLVER_IR_CG: FP32 inner PCG inside
@@ -318,7 +324,7 @@ typedef struct gfe_solver_opts {
   int32_t maxiter;      /* total inner iterations allowed */
   double inner_rtol;    /* IR_CG: relative reduction per refinement step; MIXED_CG: residual
                            reduction between reliable updates (default 0.01); FCG: the same
-                           (default 0.1) */
+                           (default 0.1, 1e-3 with GFE_PC_MG) */
   int32_t check_every;  /* iterations between host convergence checks (0 = default) */
   int32_t initial_guess;/* 0: start from x = 0; 1: start from the values in x (a restart from a
                            saved solution): the solver runs on A d = b - A x0 with its tolerance
@@ -394,9 +400,11 @@ int gfe_learned_pc_samples(gfe_learned_pc* pc, gfe_matrix* A, const double* r,
 int gfe_learned_pc_train(gfe_learned_pc* pc, const float* X, const float* T, int64_t n,
                          int32_t epochs, int32_t batch, float lr, uint64_t seed, float* loss);
 /* Flexible CG (FCG(1)) with FP32 vectors and FP64 reliable updates, preconditioned by the
- * learned block preconditioner (pc != NULL) or by Jacobi (pc == NULL); stagnation of the
- * learned preconditioner switches to Jacobi (report->fallback = 1). opts->inner_rtol is the
- * residual reduction between reliable updates; stops on the FP64 relative residual. */
+ * learned block preconditioner (pc != NULL), by the geometric multigrid V-cycle on the lattice
+ * operator (pc == NULL, opts->precond == GFE_PC_MG; GFE_ERR_UNSUPPORTED without the lattice
+ * form) or by Jacobi; stagnation of the learned preconditioner switches to Jacobi
+ * (report->fallback = 1). opts->inner_rtol is the residual reduction between reliable
+ * updates; stops on the FP64 relative residual. */
 int gfe_solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_opts* opts,
                   const double* b, double* x, gfe_solve_report* report);
 

@@ -1,0 +1,54 @@
+"""Geometric multigrid on the lattice operator as the preconditioner of the flexible CG
+(FCGSolver(pc="mg")): every solve must meet the FP64 relative residual (the report's relres
+is b - A x in FP64) and agree with the FP64 Jacobi-CG solution to the solver tolerance; the
+V-cycle must cut the iteration count far below Jacobi's on rough coefficients; odd cell
+counts (fewer levels, down to smoothing only) still converge; a matrix without the lattice
+form is refused.
+"""
+import numpy as np
+import pytest
+
+from test_gpu_q1 import _problem
+
+pytestmark = pytest.mark.gpu
+
+
+def _solve(gg, A, b, solver):
+    x = np.empty_like(b)
+    ns = gg.numerical_setup(gg.symbolic_setup(solver, A), A)
+    gg.solve_(x, ns, b)
+    return x, ns.report
+
+
+@pytest.mark.parametrize("part,sigma", [((32, 32, 32), 1.5), ((48, 40, 32), 2.5),
+                                        ((30, 28, 26), 1.0), ((21, 18, 16), 1.0)])
+def test_mg_fcg_meets_fp64_tolerance(gg, part, sigma):
+    rng = np.random.default_rng(sum(part))
+    kappa = np.exp(sigma * rng.standard_normal(int(np.prod(part))))
+    fnod = rng.standard_normal(int(np.prod(np.array(part) + 1)))
+    _, V, A, b = _problem(gg, (0, 1) * 3, part, ("boundary",), kappa, gg.NodalField(fnod))
+    x64, r64 = _solve(gg, A, b, gg.CGSolver(rtol=1e-10))
+    x, rep = _solve(gg, A, b, gg.FCGSolver(rtol=1e-8, pc="mg"))
+    assert rep.converged and rep.relres <= 1e-8
+    r = b - A.to_scipy() @ x
+    assert np.linalg.norm(r) <= 1.01e-8 * np.linalg.norm(b)
+    assert np.linalg.norm(x - x64) <= 1e-5 * np.linalg.norm(x64)
+    if part[0] % 4 == 0:  # at least three levels
+        assert rep.iterations < 0.25 * r64.iterations
+
+
+def test_mg_on_smooth_coefficient_converges_in_few_iterations(gg):
+    part = (64, 64, 64)
+    kappa = np.ones(int(np.prod(part)))
+    fnod = np.random.default_rng(3).standard_normal(int(np.prod(np.array(part) + 1)))
+    _, V, A, b = _problem(gg, (0, 1) * 3, part, ("boundary",), kappa, gg.NodalField(fnod))
+    x, rep = _solve(gg, A, b, gg.FCGSolver(rtol=1e-8, pc="mg"))
+    assert rep.converged and rep.relres <= 1e-8 and rep.iterations <= 30
+
+
+def test_mg_without_lattice_form_is_refused(gg):
+    part = (8, 8, 8)
+    kappa = np.ones(int(np.prod(part)))
+    _, V, A, b = _problem(gg, (0, 1) * 3, part, ("tag_21",), kappa, 1.0)
+    with pytest.raises(gg._lib.GfeError):
+        _solve(gg, A, b, gg.FCGSolver(rtol=1e-8, pc="mg"))

@@ -515,6 +515,8 @@ def run_gpu(args):
         out["nonlinear_plaplacian"] = bench_nonlinear(args, gg, ctx, lib, timed)
     if not args.no_reordering:
         out["reordering_rcm"] = bench_reordering(args, gg, ctx, lib, timed)
+    if not args.no_multifield:
+        out["multifield_stokes"] = bench_multifield(args, gg, ctx, lib, timed)
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args, w)
@@ -887,6 +889,69 @@ def bench_reordering(args, gg, ctx, lib, timed):
     return out
 
 
+def bench_multifield(args, gg, ctx, lib, timed):
+    """Stokes Taylor-Hood assembly (StokesTaylorHoodTests.jl's form: vector Q2 velocity, Q1
+    pressure, a = ∫ ∇v⊙∇u - (∇⋅v)p + q(∇⋅u), l = ∫ v⋅f + q g, u = u_exact on the boundary)
+    on n^3 cells, consecutive (one matrix) and block (2 x 2 grid) layouts. Timed: the whole
+    AffineFEOperator assembly call (host form classification and tables, device geometry and
+    cell integrals, symbolic and numeric loops, vector with the Dirichlet lift)."""
+    n = args.mf_n
+    m = gg.CartesianDiscreteModel((0, 1, 0, 1, 0, 1), (n, n, n))
+    u = lambda x: np.stack([x[:, 1] ** 2, x[:, 2] ** 2 + x[:, 0], x[:, 0] * x[:, 1]], 1)  # noqa
+    f = lambda x: np.tile([-2.0, -2.0, 0.0], (x.shape[0], 1))  # noqa: E731
+    V = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, 3, 2), dirichlet_tags="boundary")
+    Q = gg.FESpace(m, gg.ReferenceFE(gg.lagrangian, float, 1))
+    U, P = gg.TrialFESpace(V, u), gg.TrialFESpace(Q)
+    dO = gg.Measure(gg.Triangulation(m), 4)
+    a = lambda x, y: gg.integrate(gg.inner(gg.grad(y[0]), gg.grad(x[0]))  # noqa: E731
+                                  - gg.div(y[0]) * x[1] + y[1] * gg.div(x[0]), dO)
+    l = lambda y: gg.integrate(gg.inner(y[0], f), dO)  # noqa: E731
+    assem = gg.SparseMatrixAssembler(gg.MultiFieldFESpace([U, P]), gg.MultiFieldFESpace([V, Q]),
+                                     ctx=ctx)
+    out = {"workload": f"{n}^3 Stokes Taylor-Hood (vector Q2 / Q1), degree 4 (27 points)"}
+    for name, style in (("consecutive", None), ("block", gg.BlockMultiFieldStyle())):
+        X = gg.MultiFieldFESpace([U, P], style=style)
+        Y = gg.MultiFieldFESpace([V, Q], style=style)
+        steps = max(1, args.steps // 2)
+        r = timed("mf_" + name, lambda: gg.assemble_matrix_and_vector(a, l, X, Y, assem),
+                  steps, max(3, args.warmup))
+        el_ms, el_n = r["kt"][_lib_const(lib, "GFE_KT_ELEMENT")]
+        asm_ms, asm_n = r["kt"][_lib_const(lib, "GFE_KT_ASSEMBLE")]
+        nd = X.num_free_dofs()
+        out[name] = {"ms_per_assembly": r["ms"], "dof_per_s": nd / (r["ms"] * 1e-3),
+                     "cell_integral_ms": el_ms / steps, "row_gather_ms": asm_ms / steps,
+                     "kernel_launches_per_assembly": {"cell_integrals": el_n // steps,
+                                                      "row_gather": asm_n // steps}}
+    out["free_dofs"] = X.num_free_dofs()
+    out["cells"] = m.num_cells()
+    if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        ns = 8
+        ms = gg.CartesianDiscreteModel((0, 1, 0, 1, 0, 1), (ns, ns, ns))
+        Vs = gg.FESpace(ms, gg.ReferenceFE(gg.lagrangian, 3, 2), dirichlet_tags="boundary")
+        Qs = gg.FESpace(ms, gg.ReferenceFE(gg.lagrangian, float, 1))
+        Us = gg.TrialFESpace(Vs, u)
+        t0 = time.perf_counter()
+        xq = orc.qpoints(3, ms.cell_node_ids, ms.node_coords, 4)
+        fq = f(xq.reshape(-1, 3)).reshape(xq.shape[0], xq.shape[1], 3)
+        terms = [(0, 1, 0, 1, 1.0, None, None), (0, 2, 1, 0, -1.0, None, None),
+                 (1, 0, 0, 2, 1.0, None, None), (0, 0, None, None, 1.0, None, fq)]
+        K, F = orc.multifield_cell_arrays(3, ms.node_coords, ms.cell_node_ids, [(2, 3), (1, 1)],
+                                          terms, 4)
+        nu = Vs.num_free_dofs()
+        ip = Qs.get_cell_dof_ids()
+        orc.multifield_assemble([Vs.get_cell_dof_ids(), np.where(ip > 0, ip + nu, ip)],
+                                [nu, Qs.num_free_dofs()], K, F,
+                                [Us.get_dirichlet_dof_values(), None])
+        t = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "kind": "port", "cores": 1,
+            "sample": f"oracle (numpy cell integrals + serial CSC assembly) on {ns}^3 cells, "
+                      f"{t:.2f} s, scaled per cell",
+            "ms_per_assembly_scaled": 1e3 * t * m.num_cells() / ms.num_cells()}
+    return out
+
+
 def _lib_const(lib, name):
     from gridap_gb300 import _lib
     return getattr(_lib, name)
@@ -971,6 +1036,8 @@ def main():
     ap.add_argument("--nl-n", type=int, default=64)
     ap.add_argument("--no-reordering", action="store_true")
     ap.add_argument("--ro-n", type=int, default=48)
+    ap.add_argument("--no-multifield", action="store_true")
+    ap.add_argument("--mf-n", type=int, default=24)
     ap.add_argument("--batch-problems", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gfe":

@@ -16,15 +16,18 @@ from .assembly import (AffineFEOperator, Context, DeviceMatrix, SparseMatrixAsse
                        assemble_matrix_and_vector_, assemble_vector, assemble_vector_,
                        default_context, numeric_loop_matrix, numeric_loop_vector,
                        prepare_problem, symbolic_loop_matrix)
-from .celldata import (CellField, DomainContribution, NodalField, SinSum, dot, get_fe_basis,
-                       get_normal_vector, get_trial_fe_basis, grad, gradient, inner, integrate,
-                       isotropic_stress, PolynomialCoefficient, PowerLawFlux,
+from .celldata import (CellField, DomainContribution, NodalField, SinSum, div, divergence, dot,
+                       get_fe_basis, get_normal_vector, get_trial_fe_basis, grad, gradient,
+                       inner, integrate, isotropic_stress, PolynomialCoefficient, PowerLawFlux,
                        symmetric_gradient, ε)
 from .fespaces import (FEFunction, FESpace, ReferenceFE, TrialFESpace, get_cell_dof_ids,
                        lagrangian, num_free_dofs)
 from .geometry import (Boundary, BoundaryTriangulation, CartesianDiscreteModel, FaceLabeling,
                        Measure, SimplexDiscreteModel, Triangulation, simplexify)
 from .batch import BatchedPoissonProblems
+from .multifield import (BlockDeviceMatrix, BlockMultiFieldStyle, ConsecutiveMultiFieldStyle,
+                         MultiFieldFEFunction, MultiFieldFESpace, compute_field_offsets,
+                         num_fields)
 from .reindexing import compute_dof_permutation, reindex_free_dof_ids
 from .nonlinear import (FEOperator, NewtonRaphsonSolver, NLSolver, NonlinearFESolver,
                         solve_nonlinear_)

@@ -36,6 +36,7 @@ GFE_REORDER_RCM, GFE_REORDER_SLOAN = 0, 1
 GFE_PREC_FP64, GFE_PREC_FP32 = 0, 1
 GFE_SOLVER_CG, GFE_SOLVER_IR_CG, GFE_SOLVER_MIXED_CG, GFE_SOLVER_BICGSTAB = 0, 1, 2, 3
 GFE_PC_NONE, GFE_PC_JACOBI, GFE_PC_MG = 0, 1, 2
+GFE_MOP_VALUE, GFE_MOP_GRAD, GFE_MOP_DIV = 0, 1, 2
 GFE_KT_SPMV64, GFE_KT_SPMV32, GFE_KT_ASSEMBLE, GFE_KT_RESIDUAL64, GFE_KT_ELEMENT = 0, 1, 2, 3, 4
 GFE_KT_PRECOND, GFE_KT_VECTOR = 5, 6
 
@@ -60,6 +61,27 @@ class Problem(C.Structure):
         ("precision", C.c_int32), ("dirichlet_values", C.c_void_p), ("ndirichlet", C.c_int64),
         ("state", C.c_void_p), ("law", C.c_int32), ("law_params", C.c_double * 4),
     ]
+
+
+class MfField(C.Structure):
+    """gfe_mf_field."""
+    _fields_ = [("ncomp", C.c_int32), ("nnodes", C.c_int32), ("shapes", C.c_void_p),
+                ("grads", C.c_void_p)]
+
+
+class MfTerm(C.Structure):
+    """gfe_mf_term."""
+    _fields_ = [("test_field", C.c_int32), ("trial_field", C.c_int32),
+                ("test_op", C.c_int32), ("trial_op", C.c_int32), ("coef", C.c_double),
+                ("cell_coef", C.c_void_p), ("qdata", C.c_void_p), ("qdata_ncomp", C.c_int32)]
+
+
+class MfProblem(C.Structure):
+    """gfe_mf_problem."""
+    _fields_ = [("dim", C.c_int32), ("ncells", C.c_int64), ("nnodes", C.c_int64),
+                ("node_coords", C.c_void_p), ("cell_node_ids", C.c_void_p), ("nq", C.c_int32),
+                ("qweights", C.c_void_p), ("geo_grads", C.c_void_p), ("nfields", C.c_int32),
+                ("fields", C.c_void_p), ("nterms", C.c_int32), ("terms", C.c_void_p)]
 
 
 class SolverOpts(C.Structure):
@@ -95,6 +117,13 @@ SIGNATURES = {
                                                 _P]),
     "gfe_symbolic_loop_matrix": (C.c_int, [_P, C.c_int64, C.c_int, _P, _P, C.c_int64,
                                            C.c_int64, C.POINTER(C.c_void_p)]),
+    "gfe_symbolic_loop_matrix_rect": (C.c_int, [_P, C.c_int64, C.c_int, C.c_int, _P, _P,
+                                                C.c_int64, C.c_int64, C.POINTER(C.c_void_p)]),
+    "gfe_symbolic_loop_matrix_masked": (C.c_int, [_P, C.c_int64, C.c_int, C.c_int, _P, _P, _P,
+                                                  C.c_int64, C.c_int64,
+                                                  C.POINTER(C.c_void_p)]),
+    "gfe_multifield_assemble": (C.c_int, [_P, _P, C.c_int32, _P, C.c_int32, _P, _P, _P, _P,
+                                          C.c_int64, _P, C.c_int64, _P]),
     "gfe_matrix_destroy": (C.c_int, [_P]),
     "gfe_matrix_info": (C.c_int, [_P, _I64P, _I64P, _I64P]),
     "gfe_matrix_export_csr": (C.c_int, [_P, C.c_int, _P, _P, _P]),

@@ -10,6 +10,7 @@ CUDA tensors (device), whichever the caller passes.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -31,6 +32,19 @@ class Context:
         _lib.check(lib.gfe_ctx_create(device, C.byref(h)))
         self.handle = h
         self.device = device
+        self._children = weakref.WeakSet()
+
+    def _own(self, obj) -> None:
+        """Registers an object holding a handle of this context (matrix, batch, learned
+        preconditioner); close() releases it before the context itself."""
+        self._children.add(obj)
+
+    def close(self) -> None:
+        for obj in list(self._children):
+            obj._release()
+        if self.handle:
+            h, self.handle = self.handle, None
+            _lib.load().gfe_ctx_destroy(h)
 
     def stream(self) -> int:
         s = C.c_void_p()
@@ -56,8 +70,7 @@ class Context:
 
     def __del__(self):
         try:
-            if self.handle:
-                _lib.load().gfe_ctx_destroy(self.handle)
+            self.close()
         except Exception:
             pass
 
@@ -74,6 +87,7 @@ class DeviceMatrix:
     def __init__(self, handle, ctx: Context):
         self.handle = handle
         self.ctx = ctx
+        ctx._own(self)
         r, c, z = C.c_int64(), C.c_int64(), C.c_int64()
         _lib.check(_lib.load().gfe_matrix_info(handle, C.byref(r), C.byref(c), C.byref(z)))
         self.shape = (r.value, c.value)
@@ -103,10 +117,16 @@ class DeviceMatrix:
     def fillstored_zero(self):
         _lib.check(_lib.load().gfe_matrix_fillstored_zero(self.handle))
 
+    def _release(self):
+        # a context already closed (garbage cycles finalise in any order) took the matrix's
+        # device memory with it: only the handle is dropped then
+        h, self.handle = self.handle, None
+        if h and self.ctx.handle:
+            _lib.load().gfe_matrix_destroy(h)
+
     def __del__(self):
         try:
-            if self.handle:
-                _lib.load().gfe_matrix_destroy(self.handle)
+            self._release()
         except Exception:
             pass
 
@@ -133,14 +153,23 @@ class SparseMatrixAssembler:
 
 # ---- protocol-level entry points (FESpaces/SparseMatrixAssemblers.jl:174-316) ------------
 def symbolic_loop_matrix(assem: SparseMatrixAssembler, matdata) -> DeviceMatrix:
-    """Pattern of assembling matdata = (cellmats, cell_rows, cell_cols) (cellmats unused)."""
+    """Pattern of assembling matdata = (cellmats, cell_rows, cell_cols) (cellmats unused).
+    cell_rows and cell_cols may have different widths (a rectangular block)."""
     _, rows, cols = matdata
     rows = _as_ids(rows)
     cols = _as_ids(cols)
+    if rows.shape[0] != cols.shape[0]:
+        raise ValueError("cell_rows and cell_cols cover different numbers of cells")
     h = C.c_void_p()
-    _lib.check(_lib.load().gfe_symbolic_loop_matrix(
-        assem.ctx.handle, rows.shape[0], rows.shape[1], _lib.ptr(rows), _lib.ptr(cols),
-        assem.get_rows(), assem.get_cols(), C.byref(h)))
+    lib = _lib.load()
+    if rows.shape[1] == cols.shape[1]:
+        _lib.check(lib.gfe_symbolic_loop_matrix(
+            assem.ctx.handle, rows.shape[0], rows.shape[1], _lib.ptr(rows), _lib.ptr(cols),
+            assem.get_rows(), assem.get_cols(), C.byref(h)))
+    else:
+        _lib.check(lib.gfe_symbolic_loop_matrix_rect(
+            assem.ctx.handle, rows.shape[0], rows.shape[1], cols.shape[1], _lib.ptr(rows),
+            _lib.ptr(cols), assem.get_rows(), assem.get_cols(), C.byref(h)))
     return DeviceMatrix(h, assem.ctx)
 
 
@@ -482,6 +511,10 @@ def _assemble_boundary(ctx, prep: _Prepared, forms: _Forms, A, b) -> None:
 def assemble_matrix_and_vector(a, l, U, V, assem: SparseMatrixAssembler | None = None,
                                b_out=None):
     """(A, b) for the weak forms a(u,v), l(v) (FESpaces/Assemblers.jl:372-400)."""
+    from .multifield import MultiFieldFESpace
+    if isinstance(U, MultiFieldFESpace) or isinstance(V, MultiFieldFESpace):
+        from . import multifield
+        return multifield.assemble_matrix_and_vector(a, l, U, V, assem)
     assem = assem or SparseMatrixAssembler(U, V)
     forms = _forms(a, l, U, V)
     meas, coef, source = forms

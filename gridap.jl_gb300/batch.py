@@ -36,6 +36,7 @@ class BatchedPoissonProblems:
         _lib.check(lib.gfe_batch_create(self.ctx.handle, len(self.sizes), _lib.ptr(parts),
                                         _lib.ptr(kap), C.byref(h)))
         self.handle = h
+        self.ctx._own(self)
         nrows, nfree, ncells = C.c_int64(), C.c_int64(), C.c_int64()
         _lib.check(lib.gfe_batch_info(h, C.byref(nrows), C.byref(nfree), C.byref(ncells)))
         self.nrows, self.nfree, self.ncells = nrows.value, nfree.value, ncells.value
@@ -56,9 +57,13 @@ class BatchedPoissonProblems:
     def split(self, x):
         return [x[self.offsets[i]:self.offsets[i + 1]] for i in range(len(self.sizes))]
 
+    def _release(self):
+        h, self.handle = self.handle, None
+        if h and self.ctx.handle:
+            _lib.load().gfe_batch_destroy(h)
+
     def __del__(self):
         try:
-            if self.handle:
-                _lib.load().gfe_batch_destroy(self.handle)
+            self._release()
         except Exception:
             pass

@@ -112,9 +112,15 @@ def get_normal_vector(trian) -> _Normal:
 
 
 class _Basis(_Expr):
-    def __init__(self, space, trial: bool):
+    def __init__(self, space, trial: bool, field=None):
         self.space = space
         self.trial = trial
+        self.field = field  # position in a MultiFieldFESpace (None: single field)
+
+
+class _Div(_Expr):
+    def __init__(self, arg):
+        self.arg = arg
 
 
 class _Grad(_Expr):
@@ -159,12 +165,31 @@ def isotropic_stress(lam, mu):
     return lambda e: _Stress(lam, mu, e)
 
 
-def get_trial_fe_basis(U) -> _Basis:
+def _multifield(X):
+    from .multifield import MultiFieldFESpace
+    return isinstance(X, MultiFieldFESpace)
+
+
+def get_trial_fe_basis(U):
+    """The trial basis; on a MultiFieldFESpace one basis per field (a tuple to unpack, as
+    Gridap's MultiFieldFEBasis)."""
+    if _multifield(U):
+        return tuple(_Basis(Ui, True, i) for i, Ui in enumerate(U.spaces))
     return _Basis(U, True)
 
 
-def get_fe_basis(V) -> _Basis:
+def get_fe_basis(V):
+    if _multifield(V):
+        return tuple(_Basis(Vi, False, i) for i, Vi in enumerate(V.spaces))
     return _Basis(V, False)
+
+
+def divergence(a):
+    """∇⋅a of a vector-valued basis (Fields/DiffOperators.jl:7, tr(∇(a)))."""
+    return _Div(a)
+
+
+div = divergence
 
 
 def gradient(a):
@@ -512,3 +537,83 @@ def check_jacobian(expr, form: QuasilinearForm) -> None:
         need = {"coef"}
     if not need <= seen:
         raise NotImplementedError("the Jacobian misses terms of the residual's derivative")
+
+
+# ---- multi-field integrands -----------------------------------------------------------------
+MOP_VALUE, MOP_GRAD, MOP_DIV = 0, 1, 2
+
+
+class MfTerm:
+    """One product term of a multi-field integrand: coef * cell_coef * op_test(v_i) .
+    op_trial(u_j) (bilinear) or coef * cell_coef * op_test(v_i) . data (linear, trial_field
+    None); data is None (1), a constant (number or sequence) or a callable of x."""
+
+    def __init__(self, test_field, test_op, trial_field, trial_op, coef, cell_coef, data):
+        self.test_field, self.test_op = test_field, test_op
+        self.trial_field, self.trial_op = trial_field, trial_op
+        self.coef, self.cell_coef, self.data = coef, cell_coef, data
+
+
+def _mf_operand(e):
+    """(basis, op) for v, ∇(v) or ∇⋅v; None otherwise."""
+    if isinstance(e, _Basis):
+        return e, MOP_VALUE
+    if isinstance(e, _Grad) and isinstance(e.arg, _Basis):
+        return e.arg, MOP_GRAD
+    if isinstance(e, _Div) and isinstance(e.arg, _Basis):
+        return e.arg, MOP_DIV
+    return None
+
+
+def _mf_expand(e):
+    """[(coef, factors)]: the integrand as a sum of products of basis operands, CellFields
+    and data, with the numeric scales collected in coef."""
+    if isinstance(e, _Sum):
+        return [(s * c, f) for s, t in e.terms for c, f in _mf_expand(t)]
+    if isinstance(e, _Scaled):
+        inner_terms = _mf_expand(e.expr)
+        if isinstance(e.coef, (int, float, np.floating, np.integer)):
+            return [(float(e.coef) * c, f) for c, f in inner_terms]
+        return [(c, [_mf_leaf(e.coef)] + f) for c, f in inner_terms]
+    if isinstance(e, (_Prod, _Inner)):
+        return [(ca * cb, fa + fb) for ca, fa in _mf_expand(e.a) for cb, fb in _mf_expand(e.b)]
+    op = _mf_operand(e)
+    if op is not None:
+        return [(1.0, [op])]
+    if isinstance(e, (int, float, np.floating, np.integer)):
+        return [(float(e), [])]
+    return [(1.0, [_mf_leaf(e)])]
+
+
+def _mf_leaf(x):
+    if isinstance(x, CellField):
+        return x
+    if isinstance(x, _Expr):
+        raise NotImplementedError(f"multi-field integrand factor {type(x).__name__}")
+    if callable(x) or isinstance(x, (tuple, list, np.ndarray)):
+        return ("data", x)
+    raise NotImplementedError(f"multi-field integrand factor {type(x).__name__}")
+
+
+def classify_multifield(expr, bilinear: bool):
+    """Splits a multi-field integrand into MfTerm products, one test operand each (and one
+    trial operand for a bilinear form)."""
+    terms = []
+    for coef, factors in _mf_expand(expr):
+        ops = [f for f in factors if isinstance(f, tuple) and isinstance(f[0], _Basis)]
+        cells = [f for f in factors if isinstance(f, CellField)]
+        data = [f[1] for f in factors if isinstance(f, tuple) and f[0] == "data"]
+        tests = [o for o in ops if not o[0].trial]
+        trials = [o for o in ops if o[0].trial]
+        if len(tests) != 1 or len(trials) != (1 if bilinear else 0) or len(cells) > 1 \
+                or len(data) > (0 if bilinear else 1):
+            raise NotImplementedError(
+                "each term of a multi-field form is a product of one test operand"
+                + (", one trial operand" if bilinear else ", at most one data factor")
+                + " and at most one CellField coefficient")
+        (vb, vop), = tests
+        ub, uop = trials[0] if bilinear else (None, None)
+        cell = np.ascontiguousarray(cells[0].values, np.float64) if cells else None
+        terms.append(MfTerm(vb.field or 0, vop, None if ub is None else (ub.field or 0), uop,
+                            coef, cell, data[0] if data else None))
+    return terms

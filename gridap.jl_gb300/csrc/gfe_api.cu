@@ -120,16 +120,17 @@ extern "C" int gfe_ctx_kernel_time(gfe_ctx* c, int kernel, double* total_ms, int
 }
 
 // ---- symbolic -----------------------------------------------------------------------------
-extern "C" int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd,
-                                        const int32_t* cell_rows, const int32_t* cell_cols,
-                                        int64_t nrows, int64_t ncols, gfe_matrix** out) {
-  gfe::NvtxRange nvtx_range("gfe_symbolic_loop_matrix");
+static int symbolic_loop(gfe_ctx* ctx, int64_t ncells, int ndr, int ndc,
+                         const int32_t* cell_rows, const int32_t* cell_cols,
+                         const uint8_t* local_mask, int64_t nrows, int64_t ncols,
+                         gfe_matrix** out, const char* who) {
+  gfe::NvtxRange nvtx_range(who);
   clear_error();
-  if (!ctx || !out || nd < 1 || ncells < 0 || nrows < 0 || ncols < 0 ||
+  if (!ctx || !out || ndr < 1 || ndc < 1 || ncells < 0 || nrows < 0 || ncols < 0 ||
       (ncells > 0 && (!cell_rows || !cell_cols)))
-    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_symbolic_loop_matrix: bad arguments");
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "%s: bad arguments", who);
   if (nrows > INT32_MAX || ncols > INT32_MAX)
-    return set_error(GFE_ERR_UNSUPPORTED, "gfe_symbolic_loop_matrix: more than 2^31 rows");
+    return set_error(GFE_ERR_UNSUPPORTED, "%s: more than 2^31 rows", who);
   *out = nullptr;
   DeviceGuard g(ctx->device);
   gfe_matrix* A = new gfe_matrix();
@@ -137,21 +138,33 @@ extern "C" int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd,
   for (gfe::DevBuf* b : {&A->rowptr, &A->colval, &A->val, &A->cell_rows, &A->cell_cols,
                          &A->ref_ptr, &A->refs, &A->refpos, &A->sell_ptr, &A->sell_col,
                          &A->sell_val64, &A->sell_val32, &A->dinv64, &A->dinv32,
-                         &A->dia_val32, &A->mf_kap32, &A->mf_flag})
+                         &A->dia_val32, &A->mf_kap32, &A->mf_flag, &A->lmask})
     b->owner = ctx;
   A->nrows = nrows;
   A->ncols = ncols;
-  A->nd = nd;
+  A->nd = ndr;
+  A->ndc = ndc == ndr ? 0 : ndc;
   A->ncells = ncells;
-  const size_t idsz = sizeof(int32_t) * (size_t)ncells * nd;
-  int s = A->cell_rows.reserve(idsz);
-  if (s == GFE_OK) s = A->cell_cols.reserve(idsz);
-  if (s == GFE_OK && idsz) {
-    cudaError_t e = cudaMemcpyAsync(A->cell_rows.ptr, cell_rows, idsz, cudaMemcpyDefault,
+  const size_t rsz = sizeof(int32_t) * (size_t)ncells * ndr;
+  const size_t csz = sizeof(int32_t) * (size_t)ncells * ndc;
+  int s = A->cell_rows.reserve(rsz);
+  if (s == GFE_OK) s = A->cell_cols.reserve(csz);
+  if (s == GFE_OK && rsz) {
+    cudaError_t e = cudaMemcpyAsync(A->cell_rows.ptr, cell_rows, rsz, cudaMemcpyDefault,
                                     ctx->stream);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(A->cell_cols.ptr, cell_cols, idsz, cudaMemcpyDefault, ctx->stream);
+      e = cudaMemcpyAsync(A->cell_cols.ptr, cell_cols, csz, cudaMemcpyDefault, ctx->stream);
     if (e != cudaSuccess) s = set_error(GFE_ERR_CUDA, "copy cell ids: %s", cudaGetErrorString(e));
+  }
+  if (s == GFE_OK && local_mask) {
+    const size_t msz = (size_t)ndr * ndc;
+    s = A->lmask.reserve(msz);
+    if (s == GFE_OK) {
+      cudaError_t e = cudaMemcpyAsync(A->lmask.ptr, local_mask, msz, cudaMemcpyDefault,
+                                      ctx->stream);
+      if (e != cudaSuccess) s = set_error(GFE_ERR_CUDA, "copy mask: %s", cudaGetErrorString(e));
+      A->has_lmask = true;
+    }
   }
   if (s == GFE_OK) s = build_pattern(ctx, A);
   if (s != GFE_OK) {
@@ -160,6 +173,32 @@ extern "C" int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd,
   }
   *out = A;
   return GFE_OK;
+}
+
+extern "C" int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd,
+                                        const int32_t* cell_rows, const int32_t* cell_cols,
+                                        int64_t nrows, int64_t ncols, gfe_matrix** out) {
+  return symbolic_loop(ctx, ncells, nd, nd, cell_rows, cell_cols, nullptr, nrows, ncols, out,
+                       "gfe_symbolic_loop_matrix");
+}
+
+extern "C" int gfe_symbolic_loop_matrix_rect(gfe_ctx* ctx, int64_t ncells, int nd_rows,
+                                             int nd_cols, const int32_t* cell_rows,
+                                             const int32_t* cell_cols, int64_t nrows,
+                                             int64_t ncols, gfe_matrix** out) {
+  return symbolic_loop(ctx, ncells, nd_rows, nd_cols, cell_rows, cell_cols, nullptr, nrows,
+                       ncols, out, "gfe_symbolic_loop_matrix_rect");
+}
+
+extern "C" int gfe_symbolic_loop_matrix_masked(gfe_ctx* ctx, int64_t ncells, int nd_rows,
+                                               int nd_cols, const int32_t* cell_rows,
+                                               const int32_t* cell_cols,
+                                               const uint8_t* local_mask, int64_t nrows,
+                                               int64_t ncols, gfe_matrix** out) {
+  if (!local_mask)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_symbolic_loop_matrix_masked: no mask");
+  return symbolic_loop(ctx, ncells, nd_rows, nd_cols, cell_rows, cell_cols, local_mask, nrows,
+                       ncols, out, "gfe_symbolic_loop_matrix_masked");
 }
 
 // The matrix's buffers return to the context's pool in stream order (no synchronisation).
@@ -234,7 +273,7 @@ extern "C" int gfe_numeric_loop_matrix(gfe_ctx* ctx, gfe_matrix* A, const double
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_numeric_loop_matrix: bad arguments");
   DeviceGuard g(ctx->device);
   const void* d;
-  GFE_TRY(device_view(ctx, cellmats, sizeof(double) * (size_t)A->ncells * A->nd * A->nd,
+  GFE_TRY(device_view(ctx, cellmats, sizeof(double) * (size_t)A->ncells * A->nd * A->cols_per_cell(),
                       SCR_CELLMAT, &d));
   A->mf_state = 0;
   GFE_TRY(assemble_cellmats(ctx, A, (const double*)d));

@@ -90,7 +90,7 @@ int assemble_cellmats(gfe_ctx* ctx, gfe_matrix* A, const double* d_cellmats) {
   StoredCells src{};
   src.mat = d_cellmats;
   src.vec = nullptr;
-  src.cs = (int64_t)A->nd * A->nd;
+  src.cs = (int64_t)A->nd * A->cols_per_cell();
   src.es = 1;
   src.ntab = 0;
   RowArgs a = row_args(ctx, A, nullptr, true);
@@ -479,7 +479,8 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
   const bool q2 = p->reffe == GFE_REFFE_Q2;
   const int nn = q2 ? (D == 2 ? 9 : 27) : nv;
   if (p->nd != nn) return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: nd does not match the element");
-  if (A && (A->ncells != p->ncells || A->nd != p->nd))
+  if (A && (A->ncells != p->ncells || A->nd != p->nd ||
+            A->cols_per_cell() != p->nd))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: matrix pattern built for other cells");
   std::vector<double> qx, qw;
   GFE_TRY(tensor_quadrature(D, p->degree, qx, qw));

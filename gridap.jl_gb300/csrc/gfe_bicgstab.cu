@@ -191,18 +191,29 @@ int bicgstab(gfe_ctx* ctx, gfe_matrix* A, const double* dinv, const double* d_b,
         break;
       }
       alpha = rho1 / rv;
+      if (!std::isfinite(alpha)) {
+        breakdown = true;
+        break;
+      }
       k_bicg_half<<<grid, kBlk, 0, ctx->stream>>>(n, alpha, r, v, dinv, s, z);
       ctx->launches++;
       GFE_TRY(spmv64(ctx, A, z, t));
       GFE_TRY(dots.run(3, t, s, t, t, s, s));
-      const double ts = dots.h[0], tt = dots.h[1];
-      omega = tt > 0.0 ? ts / tt : 0.0;
+      const double ts = dots.h[0], tt = dots.h[1], ss = dots.h[2];
+      if (!std::isfinite(ts) || !std::isfinite(tt) || !std::isfinite(ss))
+        return set_error(GFE_ERR_NONFINITE, "bicgstab: half-step residual not finite");
+      // the half step already converged (s = r - alpha v small): x += alpha y and stop, before
+      // t = A z ~ 0 makes omega = t.s / t.t meaningless
+      const bool half_done = ss <= tol2;
+      omega = (half_done || !(tt > 0.0)) ? 0.0 : ts / tt;
+      if (!std::isfinite(omega)) omega = 0.0;
       k_bicg_update<<<grid, kBlk, 0, ctx->stream>>>(n, alpha, omega, y, z, s, t, d_x, r);
       ctx->launches++;
       GFE_CUDA_TRY(cudaGetLastError());
       ++it;
       rho = rho1;
       first = false;
+      if (half_done) break;  // the restart loop confirms with the true residual
       if (omega == 0.0) {
         breakdown = true;
         break;

@@ -330,7 +330,8 @@ extern "C" int gfe_assemble_boundary_matrix(gfe_ctx* ctx, const gfe_problem* p, 
       (nfacets > 0 && (!facet_cells || !facet_lfaces)))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "%s: bad arguments", who);
   GFE_TRY(check_boundary_problem(p, who));
-  if (A->nrows != p->nfree || A->nd != p->nd)
+  if (A->nrows != p->nfree || A->nd != p->nd ||
+      A->cols_per_cell() != p->nd)
     return set_error(GFE_ERR_INVALID_ARGUMENT, "%s: matrix does not match the problem", who);
   for (int k = 0; k < 4; ++k)
     if (!std::isfinite(coefs[k]))

@@ -166,7 +166,8 @@ int assemble_p2_elasticity(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, do
   if (p->dim != 3 || p->ncomp != 3 || p->nd != 30 || p->form != GFE_FORM_ELASTICITY)
     return set_error(GFE_ERR_UNSUPPORTED,
                      "assemble: P2 tets are provided for 3-D vector elasticity (nd 30)");
-  if (A && (A->ncells != p->ncells || A->nd != p->nd))
+  if (A && (A->ncells != p->ncells || A->nd != p->nd ||
+            A->cols_per_cell() != p->nd))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "assemble: matrix pattern built for other cells");
   const int64_t ncells = p->ncells;
   const bool fp32 = p->precision == GFE_PREC_FP32;

@@ -123,16 +123,23 @@ struct gfe_ctx {
 struct gfe_matrix {
   gfe_ctx* ctx = nullptr;
   int64_t nrows = 0, ncols = 0, nnz = 0;
-  int32_t nd = 0;
+  int32_t nd = 0;   // local rows per cell
+  int32_t ndc = 0;  // local columns per cell (rectangular blocks); 0 means nd
   int64_t ncells = 0;
+  int cols_per_cell() const { return ndc > 0 ? ndc : nd; }
+  // optional local coupling mask (nd x cols_per_cell(), column-major, nonzero keeps): the
+  // (local row, local column) pairs a multi-field weak form leaves untouched get no entry
+  gfe::DevBuf lmask;
+  bool has_lmask = false;
   // CSR pattern and values (0-based, int32 indices)
   gfe::DevBuf rowptr, colval, val;
   // cell ids the pattern was built from (device copies)
   gfe::DevBuf cell_rows, cell_cols;
-  // row -> (cell*nd + local) references, sorted by cell: the row-gather assembly lists
+  // row -> (cell*nd + local row) references, sorted by cell: the row-gather assembly lists
   gfe::DevBuf ref_ptr, refs;
-  // position of every (reference, local column) in its row's column list (uint8 when every
-  // row has <= 255 entries, else uint16); 0xff / 0xffff marks a skipped (negative) id
+  // position of every (reference, local column) in its row's column list, cols_per_cell()
+  // entries per reference (uint8 when every row has <= 255 entries, else uint16); 0xff /
+  // 0xffff marks a skipped (negative) id
   gfe::DevBuf refpos;
   int pos_bytes = 1;
   int max_width = 0;

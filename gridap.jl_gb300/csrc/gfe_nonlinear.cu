@@ -563,7 +563,8 @@ int assemble_quasilinear(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, doub
   const bool q2 = p->reffe == GFE_REFFE_Q2;
   const int nn = q2 ? (D == 2 ? 9 : 27) : nv;
   if (p->nd != nn) return set_error(GFE_ERR_INVALID_ARGUMENT, "quasilinear: nd mismatch");
-  if (A && (A->ncells != p->ncells || A->nd != p->nd))
+  if (A && (A->ncells != p->ncells || A->nd != p->nd ||
+            A->cols_per_cell() != p->nd))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "quasilinear: matrix built for other cells");
   std::vector<double> qx, qw;
   GFE_TRY(tensor_quadrature(D, p->degree, qx, qw));

@@ -9,8 +9,11 @@
 //   1. refs:   for every row r, the flattened positions e = cell*nd + li with
 //              cell_rows[e] == r+1, in ascending order (so cells in ascending order);
 //   2. widths: thread per row, the union of the positive column ids of the cells in its
-//              ref list, kept sorted and unique in registers/local memory;
-//   3. scan of widths -> rowptr; second pass writes colval.
+//              ref list, kept sorted and unique in shared memory (rows of up to 128
+//              columns; wider rows in local memory); the same pass stores each reference's
+//              column positions in the row;
+//   3. scan of widths -> rowptr; colval scattered from those positions (wider rows: a
+//      second pass over the local list).
 //
 // Both the pattern and the ref lists are reused by every numeric assembly afterwards.
 #include "gfe_internal.h"
@@ -181,7 +184,9 @@ __device__ __forceinline__ int insert_unique(int32_t* cols, int n, int32_t c) {
 }
 
 template <int MAXW, bool WRITE, typename PosT>
-__global__ void k_row_pattern(int64_t nrows, int nd, const int64_t* __restrict__ ref_ptr,
+__global__ void k_row_pattern(int64_t nrows, int ndr, int nd,
+                              const int64_t* __restrict__ ref_ptr,
+                              const uint8_t* __restrict__ lmask,
                               const int32_t* __restrict__ refs,
                               const int32_t* __restrict__ cell_cols, int64_t ncols,
                               int64_t* __restrict__ width, const int64_t* __restrict__ rowptr,
@@ -193,11 +198,12 @@ __global__ void k_row_pattern(int64_t nrows, int nd, const int64_t* __restrict__
   int n = 0;
   for (int64_t q = ref_ptr[r]; q < ref_ptr[r + 1]; ++q) {
     const int32_t e = refs[q];
-    const int32_t cell = e / nd;
+    const int32_t cell = e / ndr;
     const int32_t* cc = cell_cols + (int64_t)cell * nd;
+    const uint8_t* km = lmask ? lmask + (e - cell * ndr) : nullptr;
     for (int lj = 0; lj < nd; ++lj) {
       const int32_t c = cc[lj];
-      if (c <= 0) continue;
+      if (c <= 0 || (km && !km[lj * ndr])) continue;
       if (c > ncols) {
         raise(err, GFE_ERR_INVALID_ARGUMENT, (long long)cell * nd + lj);
         continue;
@@ -219,13 +225,14 @@ __global__ void k_row_pattern(int64_t nrows, int nd, const int64_t* __restrict__
   // positions are packed and stored four at a time when nd is a multiple of 4
   const bool packed = sizeof(PosT) == 1 && (nd & 3) == 0;
   for (int64_t q = ref_ptr[r]; q < ref_ptr[r + 1]; ++q) {
-    const int32_t cell = refs[q] / nd;
+    const int32_t cell = refs[q] / ndr;
     const int32_t* cc = cell_cols + (int64_t)cell * nd;
+    const uint8_t* km = lmask ? lmask + (refs[q] - cell * ndr) : nullptr;
     uint32_t word = 0;
     for (int lj = 0; lj < nd; ++lj) {
       const int32_t c = cc[lj] - 1;
       PosT pos = (PosT)~(PosT)0;
-      if (c >= 0 && c < ncols) {
+      if (c >= 0 && c < ncols && !(km && !km[lj * ndr])) {
         int lo = 0, hi = n;
         while (lo < hi) {
           const int mid = (lo + hi) >> 1;
@@ -246,21 +253,156 @@ __global__ void k_row_pattern(int64_t nrows, int nd, const int64_t* __restrict__
   }
 }
 
+// Single-pass variant for rows of at most MAXW (<= 128) columns: the row's sorted unique
+// list lives in shared memory (slot k of thread t at k*BLOCK + t, so a warp's accesses never
+// share a bank), and one pass writes both the width and the byte positions of every
+// (reference, local column); the column ids themselves are scattered afterwards from those
+// positions (k_scatter_cols), once rowptr is known. A row with more than MAXW columns writes
+// width MAXW+1 (its positions are then garbage); the host then takes the general two-pass
+// kernel above. (Staging the positions in shared memory for coalesced stores was measured
+// slower: the extra shared memory halves the resident blocks of this issue-bound kernel.)
+template <int MAXW, int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+    k_row_width_pos(int64_t nrows, int ndr, int ndc, const int64_t* __restrict__ ref_ptr,
+                    const uint8_t* __restrict__ lmask, const int32_t* __restrict__ refs,
+                    const int32_t* __restrict__ cell_cols,
+                    int64_t ncols, int64_t* __restrict__ width, uint8_t* __restrict__ refpos,
+                    DevError* err) {
+  static_assert(MAXW <= 255, "byte positions");
+  __shared__ int32_t list[MAXW * BLOCK];
+  const int64_t r = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  int32_t* L = list + threadIdx.x;
+  if (r >= nrows) return;
+  {
+    const int64_t q0 = ref_ptr[r], q1 = ref_ptr[r + 1];
+    int n = 0;
+    bool overflow = false;
+    for (int64_t q = q0; q < q1 && !overflow; ++q) {
+      const int64_t cell = refs[q] / ndr;
+      const int32_t* cc = cell_cols + cell * ndc;
+      const uint8_t* km = lmask ? lmask + (refs[q] - cell * ndr) : nullptr;
+      for (int lj = 0; lj < ndc; ++lj) {
+        const int32_t c1 = cc[lj];
+        if (c1 <= 0 || (km && !km[lj * ndr])) continue;
+        if (c1 > ncols) {
+          raise(err, GFE_ERR_INVALID_ARGUMENT, (long long)cell * ndc + lj);
+          continue;
+        }
+        const int32_t c = c1 - 1;
+        int lo;
+        const int32_t last = n > 0 ? L[(n - 1) * BLOCK] : -1;
+        if (last == c) continue;
+        if (last < c) {
+          lo = n;  // ascending arrivals append
+        } else {
+          lo = 0;
+          int hi = n - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (L[mid * BLOCK] < c) lo = mid + 1; else hi = mid;
+          }
+          if (L[lo * BLOCK] == c) continue;
+        }
+        if (n == MAXW) {
+          overflow = true;
+          break;
+        }
+        for (int k = n; k > lo; --k) L[k * BLOCK] = L[(k - 1) * BLOCK];
+        L[lo * BLOCK] = c;
+        ++n;
+      }
+    }
+    width[r] = overflow ? MAXW + 1 : n;
+    const bool packed = (ndc & 3) == 0;
+    for (int64_t q = q0; q < q1 && !overflow; ++q) {
+      const int64_t cell = refs[q] / ndr;
+      const int32_t* cc = cell_cols + cell * ndc;
+      const uint8_t* km = lmask ? lmask + (refs[q] - cell * ndr) : nullptr;
+      uint32_t word = 0;
+      for (int lj = 0; lj < ndc; ++lj) {
+        const int32_t c = cc[lj] - 1;
+        uint32_t pos = 0xFFu;
+        if (c >= 0 && c < ncols && !(km && !km[lj * ndr])) {
+          int lo = 0, hi = n;
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (L[mid * BLOCK] < c) lo = mid + 1; else hi = mid;
+          }
+          pos = (uint32_t)lo;
+        }
+        if (packed) {
+          word |= pos << (8 * (lj & 3));
+          if ((lj & 3) == 3) {
+            reinterpret_cast<uint32_t*>(refpos + q * ndc)[lj >> 2] = word;
+            word = 0;
+          }
+        } else {
+          refpos[q * ndc + lj] = (uint8_t)pos;
+        }
+      }
+    }
+  }
+}
+
+// colval[rowptr[r] + pos] = column for every (reference, local column) of row r: every slot
+// of the row is hit at least once (each unique column came from some reference), and every
+// write to a slot carries the same column id. The block's rows form one contiguous colval
+// range: it is put together in shared memory, then stored coalesced.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+    k_scatter_cols(int64_t nrows, int ndr, int ndc, const int64_t* __restrict__ ref_ptr,
+                   const int32_t* __restrict__ refs, const int32_t* __restrict__ cell_cols,
+                   const uint8_t* __restrict__ refpos, const int64_t* __restrict__ rowptr,
+                   int32_t* __restrict__ colval) {
+  extern __shared__ int32_t stage_cols[];
+  const int64_t r0 = (int64_t)blockIdx.x * BLOCK;
+  const int64_t r = r0 + threadIdx.x;
+  const int64_t r1 = r0 + BLOCK < nrows ? r0 + BLOCK : nrows;
+  const int64_t base = rowptr[r0];
+  if (r < nrows) {
+    int32_t* row = stage_cols + (rowptr[r] - base);
+    for (int64_t q = ref_ptr[r]; q < ref_ptr[r + 1]; ++q) {
+      const int32_t* cc = cell_cols + (int64_t)(refs[q] / ndr) * ndc;
+      const uint8_t* pp = refpos + q * ndc;
+      if ((ndc & 3) == 0) {
+        for (int w4 = 0; w4 < (ndc >> 2); ++w4) {
+          const uint32_t word = reinterpret_cast<const uint32_t*>(pp)[w4];
+#pragma unroll
+          for (int bb = 0; bb < 4; ++bb) {
+            const uint32_t pos = (word >> (8 * bb)) & 0xFFu;
+            if (pos != 0xFFu) row[pos] = cc[4 * w4 + bb] - 1;
+          }
+        }
+      } else {
+        for (int lj = 0; lj < ndc; ++lj) {
+          const uint8_t pos = pp[lj];
+          if (pos != 0xFF) row[pos] = cc[lj] - 1;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  const int64_t len = rowptr[r1] - base;
+  for (int64_t i = threadIdx.x; i < len; i += BLOCK) colval[base + i] = stage_cols[i];
+}
+
 template <int MAXW>
 static void launch_row_pattern(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cell_cols,
                                bool write, int64_t* width, const int64_t* rowptr64) {
   const int64_t* ref_ptr = A->ref_ptr.as<int64_t>();
+  const int ndr = A->nd, ndc = A->cols_per_cell();
+  const uint8_t* lm = A->has_lmask ? A->lmask.as<uint8_t>() : nullptr;
   if (!write)
     k_row_pattern<MAXW, false, uint8_t><<<grid_for(A->nrows, 128), 128, 0, ctx->stream>>>(
-        A->nrows, A->nd, ref_ptr, A->refs.as<int32_t>(), cell_cols, A->ncols, width, nullptr,
-        nullptr, nullptr, ctx->d_err);
+        A->nrows, ndr, ndc, ref_ptr, lm, A->refs.as<int32_t>(), cell_cols, A->ncols, width,
+        nullptr, nullptr, nullptr, ctx->d_err);
   else if (A->pos_bytes == 1)
     k_row_pattern<MAXW, true, uint8_t><<<grid_for(A->nrows, 128), 128, 0, ctx->stream>>>(
-        A->nrows, A->nd, ref_ptr, A->refs.as<int32_t>(), cell_cols, A->ncols, nullptr,
+        A->nrows, ndr, ndc, ref_ptr, lm, A->refs.as<int32_t>(), cell_cols, A->ncols, nullptr,
         rowptr64, A->colval.as<int32_t>(), A->refpos.as<uint8_t>(), ctx->d_err);
   else
     k_row_pattern<MAXW, true, uint16_t><<<grid_for(A->nrows, 128), 128, 0, ctx->stream>>>(
-        A->nrows, A->nd, ref_ptr, A->refs.as<int32_t>(), cell_cols, A->ncols, nullptr,
+        A->nrows, ndr, ndc, ref_ptr, lm, A->refs.as<int32_t>(), cell_cols, A->ncols, nullptr,
         rowptr64, A->colval.as<int32_t>(), A->refpos.as<uint16_t>(), ctx->d_err);
   ctx->launches++;
 }
@@ -275,6 +417,34 @@ static void row_pattern(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cell_cols, b
     launch_row_pattern<128>(ctx, A, cell_cols, write, width, rowptr64);
   else
     launch_row_pattern<512>(ctx, A, cell_cols, write, width, rowptr64);
+}
+
+// Widths and positions with the shared-memory list of MAXW columns.
+template <int MAXW, int BLOCK>
+static int launch_width_pos(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cols, int64_t* width) {
+  const uint8_t* lm = A->has_lmask ? A->lmask.as<uint8_t>() : nullptr;
+  k_row_width_pos<MAXW, BLOCK><<<grid_for(A->nrows, BLOCK), BLOCK, 0, ctx->stream>>>(
+      A->nrows, A->nd, A->cols_per_cell(), A->ref_ptr.as<int64_t>(), lm, A->refs.as<int32_t>(),
+      cols, A->ncols, width, A->refpos.as<uint8_t>(), ctx->d_err);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+// colval from the positions, a block of 128 rows (at most 128 columns each) at a time
+static int scatter_cols(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cols, int64_t wmax,
+                        const int64_t* rowptr64) {
+  constexpr int kBlock = 128;
+  const size_t smem = sizeof(int32_t) * kBlock * (size_t)(wmax > 0 ? wmax : 1);
+  if (smem > 48 * 1024)
+    GFE_CUDA_TRY(cudaFuncSetAttribute(k_scatter_cols<kBlock>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_scatter_cols<kBlock><<<grid_for(A->nrows, kBlock), kBlock, smem, ctx->stream>>>(
+      A->nrows, A->nd, A->cols_per_cell(), A->ref_ptr.as<int64_t>(), A->refs.as<int32_t>(),
+      cols, A->refpos.as<uint8_t>(), rowptr64, A->colval.as<int32_t>());
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
 }
 
 __global__ void k_max_i64(const int64_t* __restrict__ v, int64_t n, unsigned long long* out) {
@@ -355,26 +525,51 @@ int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
     ctx->launches++;
     int32_t hmax = 0;
     GFE_TRY(copy_out(ctx, &hmax, dmax.ptr, sizeof(int32_t)));
-    int64_t bound = (int64_t)hmax * A->nd;
+    int64_t bound = (int64_t)hmax * A->cols_per_cell();
     if (bound > A->ncols) bound = A->ncols;
     maxw = bound < 1 ? 1 : (bound > 512 ? 512 : (int)bound);
   }
-  DevBuf width(ctx), rowptr64(ctx);
+  DevBuf width(ctx), rowptr64(ctx), dwmax(ctx);
   GFE_TRY(width.reserve(sizeof(int64_t) * (nrows + 1)));
   GFE_TRY(rowptr64.reserve(sizeof(int64_t) * (nrows + 1)));
-  row_pattern(ctx, A, cols, false, width.as<int64_t>(), nullptr, maxw);
-  GFE_CUDA_TRY(cudaGetLastError());
-  GFE_TRY(check_device_error(ctx, "symbolic_loop_matrix (column ids)"));
-  GFE_TRY(scan_exclusive_i64(ctx, width.as<int64_t>(), rowptr64.as<int64_t>(), nrows));
-  DevBuf dwmax(ctx);
   GFE_TRY(dwmax.reserve(sizeof(int64_t)));
-  GFE_CUDA_TRY(cudaMemsetAsync(dwmax.ptr, 0, sizeof(int64_t), ctx->stream));
-  k_max_i64<<<grid_for(nrows, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
-      width.as<int64_t>(), nrows, dwmax.as<unsigned long long>());
-  ctx->launches++;
-  int64_t nnz = 0, wmax = 0;
-  GFE_CUDA_TRY(cudaMemcpyAsync(&wmax, dwmax.ptr, sizeof(int64_t), cudaMemcpyDeviceToHost,
-                               ctx->stream));
+  auto max_width = [&](int64_t* wmax) -> int {
+    GFE_CUDA_TRY(cudaMemsetAsync(dwmax.ptr, 0, sizeof(int64_t), ctx->stream));
+    k_max_i64<<<grid_for(nrows, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+        width.as<int64_t>(), nrows, dwmax.as<unsigned long long>());
+    ctx->launches++;
+    return copy_out(ctx, wmax, dwmax.ptr, sizeof(int64_t));
+  };
+  // Single pass with the row list in shared memory: a 32-column list first (enough for
+  // every Q1 mesh), then one sized by the bound (at most 128); rows wider than that take the
+  // general two-pass kernel.
+  int64_t wmax = 0;
+  bool single = false;
+  if (A->nrefs * A->cols_per_cell() > 0) {
+    GFE_TRY(A->refpos.reserve((size_t)A->nrefs * A->cols_per_cell()));
+    const int tries[2] = {32, maxw <= 64 ? 64 : 128};
+    for (int t = 0; t < 2 && !single; ++t) {
+      const int w = tries[t];
+      if (t == 1 && maxw <= 32) break;
+      if (w == 32)
+        GFE_TRY((launch_width_pos<32, 128>(ctx, A, cols, width.as<int64_t>())));
+      else if (w == 64)
+        GFE_TRY((launch_width_pos<64, 128>(ctx, A, cols, width.as<int64_t>())));
+      else
+        GFE_TRY((launch_width_pos<128, 64>(ctx, A, cols, width.as<int64_t>())));
+      GFE_TRY(check_device_error(ctx, "symbolic_loop_matrix (column ids)"));
+      GFE_TRY(max_width(&wmax));
+      single = wmax <= w;
+    }
+  }
+  if (!single) {
+    row_pattern(ctx, A, cols, false, width.as<int64_t>(), nullptr, maxw);
+    GFE_CUDA_TRY(cudaGetLastError());
+    GFE_TRY(check_device_error(ctx, "symbolic_loop_matrix (column ids)"));
+    GFE_TRY(max_width(&wmax));
+  }
+  GFE_TRY(scan_exclusive_i64(ctx, width.as<int64_t>(), rowptr64.as<int64_t>(), nrows));
+  int64_t nnz = 0;
   GFE_TRY(copy_out(ctx, &nnz, rowptr64.as<int64_t>() + nrows, sizeof(int64_t)));
   A->max_width = (int)wmax;
   A->pos_bytes = wmax <= 255 ? 1 : 2;
@@ -386,9 +581,13 @@ int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
   GFE_TRY(A->colval.reserve(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
   GFE_TRY(A->val.reserve(sizeof(double) * (nnz > 0 ? nnz : 1)));
   GFE_TRY(A->refpos.reserve((size_t)A->pos_bytes * (size_t)(A->nrefs > 0 ? A->nrefs : 1) *
-                            A->nd));
+                            A->cols_per_cell()));
   GFE_TRY(narrow_i64_to_i32(ctx, rowptr64.as<int64_t>(), A->rowptr.as<int32_t>(), nrows + 1));
-  row_pattern(ctx, A, cols, true, nullptr, rowptr64.as<int64_t>(), maxw);
+  if (single) {
+    GFE_TRY(scatter_cols(ctx, A, cols, wmax, rowptr64.as<int64_t>()));
+  } else {
+    row_pattern(ctx, A, cols, true, nullptr, rowptr64.as<int64_t>(), maxw);
+  }
   GFE_CUDA_TRY(cudaGetLastError());
   GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * (nnz > 0 ? nnz : 1),
                                ctx->stream));

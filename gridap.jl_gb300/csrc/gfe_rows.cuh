@@ -17,7 +17,9 @@ __device__ __forceinline__ void raise_err(DevError* err, int code, long long ind
 
 struct RowArgs {
   int64_t nrows;
-  int nd;
+  int nd;       // local rows per cell (leading dimension of the column-major cell matrices)
+  int ndc = 0;  // local columns per cell; 0 means nd
+  __host__ __device__ int cols() const { return ndc > 0 ? ndc : nd; }
   const int32_t* rowptr;
   const int32_t* colval;
   const int64_t* ref_ptr;
@@ -99,8 +101,9 @@ __global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
       const int64_t cell = e / a.nd;
       const int li = e - (int)(cell * a.nd);
       if (a.val) {
+        const int ndc = a.cols();
         const auto cc = src.cell(cell);  // per-cell data (coefficients) loaded once per ref
-        const PosT* pp = refpos + q * a.nd;
+        const PosT* pp = refpos + q * ndc;
         auto add = [&](int lj, PosT p) {
           if (p == (PosT)~(PosT)0) return;  // Dirichlet column
           if (p >= n) {
@@ -109,16 +112,16 @@ __global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
           }
           acc[p * R + t] += src.m(tab, cc, li, lj, a.nd);
         };
-        if (sizeof(PosT) == 1 && (a.nd & 3) == 0) {
+        if (sizeof(PosT) == 1 && (ndc & 3) == 0) {
           // byte positions four at a time (the reference's row of the table is 4-aligned)
           const uint32_t* pw = reinterpret_cast<const uint32_t*>(pp);
-          for (int w4 = 0; w4 < (a.nd >> 2); ++w4) {
+          for (int w4 = 0; w4 < (ndc >> 2); ++w4) {
             const uint32_t word = __ldg(pw + w4);
 #pragma unroll
             for (int bb = 0; bb < 4; ++bb) add(4 * w4 + bb, (PosT)((word >> (8 * bb)) & 0xffu));
           }
         } else {
-          for (int lj = 0; lj < a.nd; ++lj) add(lj, __ldg(pp + lj));
+          for (int lj = 0; lj < ndc; ++lj) add(lj, __ldg(pp + lj));
         }
       }
       if (a.b) bacc += src.v(tab, cell, li);
@@ -219,8 +222,9 @@ __global__ void __launch_bounds__(32 * kRowWarps)
     const int li = e - (int)(cell * a.nd);
     if (a.val) {
       const auto cc = src.cell(cell);
-      for (int lj = lane; lj < a.nd; lj += 32) {
-        const PosT pp = __ldg(refpos + q * a.nd + lj);
+      const int ndc = a.cols();
+      for (int lj = lane; lj < ndc; lj += 32) {
+        const PosT pp = __ldg(refpos + q * ndc + lj);
         if (pp == (PosT)~(PosT)0) continue;  // Dirichlet column
         if (pp >= n) {
           raise_err(a.err, GFE_ERR_INVALID_ARGUMENT, r);
@@ -270,11 +274,12 @@ __global__ void k_dirichlet_lift(RowArgs a, Src src) {
     const int32_t e = a.refs[q];
     const int64_t cell = e / a.nd;
     const int li = e - (int)(cell * a.nd);
-    const int32_t* ids = a.cell_cols + cell * a.nd;
+    const int ndc = a.cols();
+    const int32_t* ids = a.cell_cols + cell * ndc;
     double l = 0.0;
     bool has = false;
     const auto cc = src.cell(cell);
-    for (int lj = 0; lj < a.nd; ++lj) {
+    for (int lj = 0; lj < ndc; ++lj) {
       const int32_t col = __ldg(ids + lj);
       if (col >= 0) continue;
       const int64_t k = -(int64_t)col - 1;
@@ -315,7 +320,7 @@ static int run_rows(gfe_ctx* ctx, const RowArgs& a, const Src& src, int maxw, in
 
 template <class Src>
 static int run_rows_main(gfe_ctx* ctx, const RowArgs& a, const Src& src, int maxw, int pb) {
-  if (a.nd >= 16 && a.val) {
+  if (a.cols() >= 16 && a.val) {
     if (maxw <= 128) return launch_rows_warp<128>(ctx, a, src, pb);
     if (maxw <= 256) return launch_rows_warp<256>(ctx, a, src, pb);
     if (maxw <= 512) return launch_rows_warp<512>(ctx, a, src, pb);
@@ -335,6 +340,7 @@ static RowArgs row_args(gfe_ctx* ctx, gfe_matrix* A, double* b, bool with_matrix
   RowArgs a;
   a.nrows = A->nrows;
   a.nd = A->nd;
+  a.ndc = A->cols_per_cell();
   a.rowptr = A->rowptr.as<int32_t>();
   a.colval = A->colval.as<int32_t>();
   a.ref_ptr = A->ref_ptr.as<int64_t>();

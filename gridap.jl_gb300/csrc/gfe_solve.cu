@@ -316,8 +316,9 @@ int attach_lattice_operator(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p,
                             const double* d_coef, const double* Kref) {
   A->mf_state = 0;
   const int64_t n0 = p->partition[0], n1 = p->partition[1], n2 = p->partition[2];
-  if (p->dim != 3 || n0 < 2 || n1 < 2 || n2 < 2 || A->nd != 8 || A->ncells != n0 * n1 * n2 ||
-      A->nrows != (n0 - 1) * (n1 - 1) * (n2 - 1) || A->nrows != A->ncols)
+  if (p->dim != 3 || n0 < 2 || n1 < 2 || n2 < 2 || A->nd != 8 || A->cols_per_cell() != 8 ||
+      A->ncells != n0 * n1 * n2 || A->nrows != (n0 - 1) * (n1 - 1) * (n2 - 1) ||
+      A->nrows != A->ncols)
     return GFE_OK;
   // the operator's 32-bit strides and its (i-tiles, j-tiles, k) grid
   if (n0 * n1 >= ((int64_t)1 << 31) || n2 - 1 > 65535 || (n1 - 1 + 7) / 8 > 65535)
@@ -972,7 +973,7 @@ __global__ void __launch_bounds__(kVecBlock)
     const T ri = (T)((double)rhs[i] * scale);
     x[i] = (T)0;
     r[i] = ri;
-    const T zi = dinv[i] * ri;
+    const T zi = dinv ? dinv[i] * ri : ri;  // no diagonal: z = r (the caller preconditions)
     p[i] = zi;
     rz += (double)ri * (double)zi;
     rr += (double)ri * (double)ri;
@@ -1010,6 +1011,47 @@ __global__ void __launch_bounds__(kSpmvBlock)
     const double ri = b[i] - sell_row<double, double>(i, sptr, scol, sval, x);
     r[i] = ri;
     d = ri * ri;
+  }
+  d = block_sum<kSpmvBlock>(d, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = d;
+  double tot[1];
+  if (last_block_reduce<kSpmvBlock, 1>(ticket, partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0)
+    *out_rr = tot[0];
+}
+
+// The same residual from the CSR arrays, for solvers that need no sliced-ELL copy: LANES
+// threads per row (strided over the row's entries, then a shuffle sum), rows of a warp
+// advancing together so that every shuffle has the whole warp.
+template <int LANES>
+__global__ void __launch_bounds__(kSpmvBlock)
+    k_residual64_csr(int64_t n, const int32_t* __restrict__ rowptr,
+                     const int32_t* __restrict__ colval, const double* __restrict__ val,
+                     const double* __restrict__ x, const double* __restrict__ b,
+                     double* __restrict__ r, double* __restrict__ partials, double* out_rr,
+                     unsigned* ticket) {
+  constexpr int kRowsPerWarp = 32 / LANES;
+  __shared__ double sh[kSpmvBlock / 32];
+  const int lane = threadIdx.x & (LANES - 1);
+  const int sub = (threadIdx.x & 31) / LANES;
+  const int64_t warp = ((int64_t)blockIdx.x * kSpmvBlock + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * kSpmvBlock) >> 5;
+  double d = 0.0;
+  for (int64_t w0 = warp * kRowsPerWarp; w0 < n; w0 += nwarps * kRowsPerWarp) {
+    const int64_t i = w0 + sub;
+    double s = 0.0;
+    if (i < n) {
+      const int32_t e = __ldg(rowptr + i + 1);
+      for (int32_t k = __ldg(rowptr + i) + lane; k < e; k += LANES)
+        s = fma(__ldcs(val + k), __ldg(x + __ldcs(colval + k)), s);
+    }
+#pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (i < n && lane == 0) {
+      const double ri = b[i] - s;
+      r[i] = ri;
+      d += ri * ri;
+    }
   }
   d = block_sum<kSpmvBlock>(d, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = d;
@@ -1558,6 +1600,9 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
   w.S = ctx->scratch[SCR_REDUCE].as<SolverState>();
   w.partials = (double*)((char*)ctx->scratch[SCR_REDUCE].ptr + 256);
   w.hS = (SolverState*)ctx->h_pinned;
+  // a grown scratch buffer holds garbage: the reduction tickets must start at zero for every
+  // method (the final residual below reduces through them too)
+  GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
   // The precondition switch: Jacobi uses 1/diag, none uses ones (same kernels).
   const bool jac = o->precond == GFE_PC_JACOBI;
   if (!jac && o->precond != GFE_PC_NONE)
@@ -1763,7 +1808,12 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
               const double* d_b, double* d_x, gfe_solve_report* rep) {
   if (A->nrows != A->ncols) return set_error(GFE_ERR_INVALID_ARGUMENT, "fcg: not square");
   if (o->initial_guess) return solve_from_guess(ctx, A, pc, true, o, d_b, d_x, rep);
-  GFE_TRY(build_solver_plan(ctx, A));
+  bool lattice = false;
+  GFE_TRY(lattice_ready(ctx, A, &lattice));
+  // the multigrid FCG on the lattice operator needs neither the sliced-ELL copy nor its
+  // diagonal: its FP64 residuals read the CSR arrays
+  const bool csr_residual = lattice && pc == nullptr && o->precond == GFE_PC_MG;
+  if (!csr_residual) GFE_TRY(build_solver_plan(ctx, A));
   const int64_t n = A->nrows;
   int check_every = o->check_every > 0 ? o->check_every : 10;
   const int maxit = o->maxiter > 0 ? o->maxiter : 100000;
@@ -1772,8 +1822,6 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   GFE_TRY(ctx->scratch[SCR_SOLVER].reserve(n8 * 3 + 64));
   GFE_TRY(ctx->scratch[SCR_SOLVER2].reserve(sizeof(float) * (size_t)(npad > 0 ? npad : 64) * 5 +
                                             256));
-  bool lattice = false;
-  GFE_TRY(lattice_ready(ctx, A, &lattice));
   if (!lattice) GFE_TRY(build_dia(ctx, A));
   size_t nblk = grid_for(n, kSpmvBlock);
   if (lattice) nblk = std::max<size_t>(nblk, lattice_op(A).blocks(n));
@@ -1787,8 +1835,19 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   float* f = (float*)ctx->scratch[SCR_SOLVER2].ptr;
   float *x32 = f, *r32 = f + npad, *p32 = f + 2 * npad, *q32 = f + 3 * npad,
         *z32 = f + 4 * npad;
-  const float* dinv32 = A->dinv32.as<float>();
+  const float* dinv32 = csr_residual ? nullptr : A->dinv32.as<float>();
   const unsigned gv = (unsigned)(ctx->num_sms * 4), gs = grid_for(n, kSpmvBlock);
+  // r64 = b - A x64 in FP64, r64.r64 into *rr
+  auto residual64 = [&](double* rr) {
+    if (csr_residual)
+      k_residual64_csr<4><<<(unsigned)(ctx->num_sms * 8), kSpmvBlock, 0, ctx->stream>>>(
+          n, A->rowptr.as<int32_t>(), A->colval.as<int32_t>(), A->val.as<double>(), d_x, d_b,
+          r64, w.partials, rr, &w.S->ticket[2]);
+    else
+      k_residual64<<<gs, kSpmvBlock, 0, ctx->stream>>>(
+          n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(),
+          d_x, d_b, r64, w.partials, rr, &w.S->ticket[2]);
+  };
   // reliable updates: after the FP32 residual has dropped by delta (0.1; 1e-3 with the
   // multigrid preconditioner, which gains about a decade per iteration)
   const double delta = o->inner_rtol > 0 ? o->inner_rtol
@@ -1875,9 +1934,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       // reliable update: x64 += x32, r64 = b - A64 x64, r32 = r64 (or stop)
       k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
       timer_begin(ctx, GFE_KT_RESIDUAL64);
-      k_residual64<<<gs, kSpmvBlock, 0, ctx->stream>>>(
-          n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(),
-          d_x, d_b, r64, w.partials, &w.S->rr64, &w.S->ticket[2]);
+      residual64(&w.S->rr64);
       timer_end(ctx);
       k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, w.S);
       ctx->launches += 3;
@@ -1913,9 +1970,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   rep->ndiag = A->dia_valid ? A->dia_ndiag : 0;
   rep->fallback = fallback;
   // true FP64 residual
-  k_residual64<<<gs, kSpmvBlock, 0, ctx->stream>>>(
-      n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(), d_x,
-      d_b, r64, w.partials, &w.S->rr, &w.S->ticket[2]);
+  residual64(&w.S->rr);
   k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb, &w.S->ticket[1]);
   ctx->launches += 2;
   GFE_CUDA_TRY(cudaGetLastError());

@@ -41,6 +41,7 @@ class LearnedBlockPreconditioner:
                                              _lib.ptr(n2d), V.num_free_dofs(), _lib.ptr(kap),
                                              C.byref(h)))
         self.handle = h
+        self.ctx._own(self)
         self.nfree = V.num_free_dofs()
         self.nblocks = int(np.prod((part + 1) // 2))
 
@@ -81,10 +82,14 @@ class LearnedBlockPreconditioner:
                                                     C.byref(loss)))
         return loss.value
 
+    def _release(self):
+        h, self.handle = self.handle, None
+        if h and self.ctx.handle:
+            _lib.load().gfe_learned_pc_destroy(h)
+
     def __del__(self):
         try:
-            if self.handle:
-                _lib.load().gfe_learned_pc_destroy(self.handle)
+            self._release()
         except Exception:
             pass
 

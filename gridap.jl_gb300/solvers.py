@@ -182,8 +182,13 @@ def solve(solver, op, b=None):
         return solve_matrix_(x, ls, A, rhs)
     A, b = op.get_matrix(), op.get_vector()
     x = np.empty_like(b) if isinstance(b, np.ndarray) else b.new_empty(b.shape)
+    from .multifield import MultiFieldFESpace, MultiFieldFEFunction
+    U = op.get_trial()
+    if isinstance(U, MultiFieldFESpace) and U.is_block():
+        raise NotImplementedError("solve a block-assembled system through its blocks (or use "
+                                  "the consecutive style for one matrix)")
     ns = numerical_setup(symbolic_setup(ls, A), A)
     solve_(x, ns, b)
-    uh = FEFunction(op.get_trial(), x)
+    uh = MultiFieldFEFunction(U, x) if isinstance(U, MultiFieldFESpace) else FEFunction(U, x)
     uh.report = ns.report
     return uh

@@ -133,6 +133,24 @@ int gfe_simplex_p2_dofs(const int64_t* partition, int32_t ncomp, const uint8_t* 
 int gfe_symbolic_loop_matrix(gfe_ctx* ctx, int64_t ncells, int nd, const int32_t* cell_rows,
                              const int32_t* cell_cols, int64_t nrows, int64_t ncols,
                              gfe_matrix** A);
+/* The same for rectangular cell blocks: nd_rows row ids and nd_cols column ids per cell (an
+ * off-diagonal block of a multi-field system, e.g. velocity rows against pressure columns).
+ * Replaces the per-block symbolic loops of MultiField/BlockSparseMatrixAssemblers.jl:
+ * 197-230 (nz_counter / nz_allocation / create_from_nz over the block builders), each block
+ * being FESpaces/SparseMatrixAssemblers.jl:174-210 on its (rows, cols) id pair. */
+int gfe_symbolic_loop_matrix_rect(gfe_ctx* ctx, int64_t ncells, int nd_rows, int nd_cols,
+                                  const int32_t* cell_rows, const int32_t* cell_cols,
+                                  int64_t nrows, int64_t ncols, gfe_matrix** A);
+/* The same with a local coupling mask: local_mask[li + lj*nd_rows] (nd_rows x nd_cols bytes,
+ * host or device) zero drops every (cell_rows[c][li], cell_cols[c][lj]) touch, as for a
+ * negative id. A multi-field cell matrix is an ArrayBlock whose untouched blocks (field pairs
+ * the weak form does not couple) are `nothing` and add no entry to the pattern
+ * (MultiField/MultiFieldFESpaces.jl:460-480, the touched flags of Arrays/ArrayBlocks.jl:23-45);
+ * the mask is that block structure at local-dof resolution. */
+int gfe_symbolic_loop_matrix_masked(gfe_ctx* ctx, int64_t ncells, int nd_rows, int nd_cols,
+                                    const int32_t* cell_rows, const int32_t* cell_cols,
+                                    const uint8_t* local_mask, int64_t nrows, int64_t ncols,
+                                    gfe_matrix** A);
 /* Releases the matrix (stream-ordered; no device synchronisation). Destroy every matrix of a
  * context before the context itself. */
 int gfe_matrix_destroy(gfe_matrix* A);
@@ -147,8 +165,9 @@ int gfe_matrix_export_csr(gfe_matrix* A, int index_base, int64_t* rowptr, int64_
 int gfe_matrix_fillstored_zero(gfe_matrix* A);
 
 /* ---- assembly: numeric, caller-provided cell arrays --------------------------------------- */
-/* Adds cell matrices (FP64, nd x nd column-major per cell, ncells of them, the layout of
- * Gridap's cell matrix arrays) into A's values in cell order -- rows outer by cell, i.e. the
+/* Adds cell matrices (FP64, nd x nd column-major per cell -- nd_rows x nd_cols for a matrix
+ * from gfe_symbolic_loop_matrix_rect -- ncells of them, the layout of Gridap's cell matrix
+ * arrays) into A's values in cell order -- rows outer by cell, i.e. the
  * exact accumulation order of InserterCSC -- skipping negative ids. A must come from
  * gfe_symbolic_loop_matrix over the same cell ids.
  * Replaces FESpaces/SparseMatrixAssemblers.jl:214-248 (numeric_loop_matrix!) and
@@ -298,6 +317,78 @@ enum { GFE_REORDER_RCM = 0, GFE_REORDER_SLOAN = 1 };
 int gfe_dof_permutation(gfe_ctx* ctx, int64_t ncells, int32_t nd, const int32_t* cell_dof_ids,
                         int64_t nfree, int32_t algorithm, int32_t w1, int32_t w2,
                         int64_t* iperm);
+
+/* ---- multi-field assembly (MultiFieldFESpace, block assemblers) --------------------------- */
+/* Operators applied to a field's basis inside an integrand. */
+enum {
+  GFE_MOP_VALUE = 0, /* u (scalar) or u (vector: the basis e_c phi) */
+  GFE_MOP_GRAD = 1,  /* grad u: a vector (scalar field) or a dim x dim tensor (vector field) */
+  GFE_MOP_DIV = 2    /* div u of a vector field: a scalar */
+};
+
+/* One Lagrangian field on the common cells: ncomp components (1, or dim with the cell's
+ * local dofs component-major: comp * nnodes + node), tabulated on the reference cell at the
+ * problem's quadrature points. */
+typedef struct gfe_mf_field {
+  int32_t ncomp;
+  int32_t nnodes;           /* local nodes per cell */
+  const double* shapes;     /* nq x nnodes reference shape values */
+  const double* grads;      /* nq x nnodes x dim reference gradients */
+} gfe_mf_field;
+
+/* One term of the integrand, summed over the quadrature points with weight w_q |J_q|:
+ * bilinear (trial_field >= 0): coef * op_test(v) . op_trial(u), the dot product being the
+ *   full contraction of two operands of the same shape (scalar x scalar, vector . vector,
+ *   tensor : tensor), e.g. grad(v) : grad(u), -(div v) p, q (div u), v . grad(p);
+ * linear (trial_field = -1): coef * op_test(v) . f(x_q) with f from qdata (ncells x nq x
+ *   qdata_ncomp values, host or device, matching op_test's shape) or f = 1 when qdata is
+ *   NULL.
+ * cell_coef (ncells values, host or device, or NULL) scales the term cell by cell. */
+typedef struct gfe_mf_term {
+  int32_t test_field, trial_field;
+  int32_t test_op, trial_op;
+  double coef;
+  const double* cell_coef;
+  const double* qdata;
+  int32_t qdata_ncomp;
+} gfe_mf_term;
+
+typedef struct gfe_mf_problem {
+  int32_t dim;                  /* 2 or 3 */
+  int64_t ncells;
+  int64_t nnodes;
+  const double* node_coords;    /* nnodes x dim */
+  const int32_t* cell_node_ids; /* ncells x 2^dim, 1-based: the (multi)linear cell map */
+  int32_t nq;                   /* quadrature points per cell */
+  const double* qweights;       /* nq reference weights */
+  const double* geo_grads;      /* nq x 2^dim x dim gradients of the cell map's Q1 shapes */
+  int32_t nfields;
+  const gfe_mf_field* fields;
+  int32_t nterms;
+  const gfe_mf_term* terms;
+} gfe_mf_problem;
+
+/* Integrates the terms on every cell and assembles the block (rows of row_fields against
+ * columns of col_fields, each a list of field indices) into A and/or b:
+ *  - A (may be NULL) comes from gfe_symbolic_loop_matrix(_rect) over the cell ids of the row
+ *    fields (concatenated in row_fields order) and of the column fields; the cell matrix of
+ *    the block is ndr x ndc with ndr = sum over row fields of ncomp * nnodes;
+ *  - b (may be NULL; nrows entries -- A's rows when A is given -- added to) receives the
+ *    linear terms of the row fields;
+ *  - row_ids / col_ids are those concatenated cell ids (ncells x ndr, ncells x ndc), in the
+ *    numbering A was built with; negative ids are Dirichlet dofs, -k reading
+ *    dirichlet_values[k-1] (host or device, NULL: zero) for the lift b_i -= sum_j K_ij u_D_j.
+ * One monolithic matrix (ConsecutiveMultiFieldStyle) is the block of all fields against all
+ * fields; a block assembler calls this once per block.
+ * Replaces the multi-field cell arrays (MultiField/MultiFieldCellFields.jl, BlockMap cell
+ * matrices of MultiField/MultiFieldFESpaces.jl:460-488) and their assembly through
+ * FESpaces/SparseMatrixAssemblers.jl:214-316 per block
+ * (MultiField/BlockSparseMatrixAssemblers.jl:236-255). */
+int gfe_multifield_assemble(gfe_ctx* ctx, const gfe_mf_problem* problem, int32_t nrow_fields,
+                            const int32_t* row_fields, int32_t ncol_fields,
+                            const int32_t* col_fields, const int32_t* row_ids,
+                            const int32_t* col_ids, const double* dirichlet_values,
+                            int64_t ndirichlet, gfe_matrix* A, int64_t nrows, double* b);
 
 /* ---- linear solve ------------------------------------------------------------------------ */
 enum {

@@ -740,17 +740,27 @@ static int64_t sorted_first(const int64_t* v, int64_t x, int64_t lo, int64_t hi)
 int orc_assemble_matrix_csc(int64_t ncells, int nd, const int32_t* cell_rows,
                             const int32_t* cell_cols, const double* cellmats, int64_t nrows,
                             int64_t ncols, orc_csc* out) {
+  return orc_assemble_matrix_csc_rect(ncells, nd, nd, cell_rows, cell_cols, cellmats, nrows,
+                                      ncols, out);
+}
+
+/* Rectangular cell blocks (ndr rows x ndc cols per cell, column-major cell matrices): the
+ * assembly of one block of a multi-field system (MultiField/BlockSparseMatrixAssemblers.jl:
+ * 197-230 runs the loops below on every block's (rows, cols) pair). */
+int orc_assemble_matrix_csc_rect(int64_t ncells, int ndr, int ndc, const int32_t* cell_rows,
+                                 const int32_t* cell_cols, const double* cellmats,
+                                 int64_t nrows, int64_t ncols, orc_csc* out) {
   /* symbolic loop: CounterCSC.colnnzmax[j] += 1 for every positive (i,j) touched
    * (FESpaces/SparseMatrixAssemblers.jl:174-210, Algebra/SparseMatrixCSC.jl:72-89) */
   int64_t* colnnz = (int64_t*)calloc(ncols + 1, sizeof(int64_t));
   int64_t* colptr = (int64_t*)malloc(sizeof(int64_t) * (ncols + 1));
   if (!colnnz || !colptr) return -1;
   for (int64_t c = 0; c < ncells; ++c) {
-    const int32_t* rs = cell_rows + c * nd;
-    const int32_t* cs = cell_cols + c * nd;
-    for (int lj = 0; lj < nd; ++lj) {
+    const int32_t* rs = cell_rows + c * ndr;
+    const int32_t* cs = cell_cols + c * ndc;
+    for (int lj = 0; lj < ndc; ++lj) {
       if (cs[lj] <= 0) continue;
-      for (int li = 0; li < nd; ++li)
+      for (int li = 0; li < ndr; ++li)
         if (rs[li] > 0) colnnz[cs[lj] - 1] += 1;
     }
   }
@@ -766,16 +776,16 @@ int orc_assemble_matrix_csc(int64_t ncells, int nd, const int32_t* cell_rows,
    * (SparseMatrixAssemblers.jl:214-248, AlgebraInterfaces.jl:176-187,
    * SparseMatrixCSC.jl:124-150); arrays here are 0-based views of 1-based data. */
   for (int64_t c = 0; c < ncells; ++c) {
-    const int32_t* rs = cell_rows + c * nd;
-    const int32_t* cs = cell_cols + c * nd;
-    const double* vs = cellmats ? cellmats + c * nd * nd : NULL;
-    for (int lj = 0; lj < nd; ++lj) {
+    const int32_t* rs = cell_rows + c * ndr;
+    const int32_t* cs = cell_cols + c * ndc;
+    const double* vs = cellmats ? cellmats + c * ndr * ndc : NULL;
+    for (int lj = 0; lj < ndc; ++lj) {
       int64_t j = cs[lj];
       if (j <= 0) continue;
-      for (int li = 0; li < nd; ++li) {
+      for (int li = 0; li < ndr; ++li) {
         int64_t i = rs[li];
         if (i <= 0) continue;
-        double v = vs ? vs[li + lj * nd] : 0.0;
+        double v = vs ? vs[li + lj * ndr] : 0.0;
         int64_t pini = colptr[j - 1] - 1;
         int64_t pend = pini + colnnz[j - 1] - 1;
         int64_t p = sorted_first(rowval, i, pini, pend);

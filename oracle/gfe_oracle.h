@@ -126,6 +126,11 @@ typedef struct {
 int orc_assemble_matrix_csc(int64_t ncells, int nd, const int32_t* cell_rows,
                             const int32_t* cell_cols, const double* cellmats, int64_t nrows,
                             int64_t ncols, orc_csc* out);
+/* The same for rectangular cells: ndr row ids, ndc column ids, ndr x ndc column-major cell
+ * matrices (one block of a multi-field system). */
+int orc_assemble_matrix_csc_rect(int64_t ncells, int ndr, int ndc, const int32_t* cell_rows,
+                                 const int32_t* cell_cols, const double* cellmats,
+                                 int64_t nrows, int64_t ncols, orc_csc* out);
 void orc_csc_free(orc_csc* a);
 /* Dense vector assembly (SparseMatrixAssemblers.jl:287-316). b must be zeroed by caller. */
 void orc_assemble_vector(int64_t ncells, int nd, const int32_t* cell_rows,

@@ -60,6 +60,8 @@ def lib():
                                                    C.c_int, P, P, C.c_int, P, P, P]
         L.orc_assemble_matrix_csc.argtypes = [C.c_int64, C.c_int, P, P, P, C.c_int64, C.c_int64,
                                               C.POINTER(_CSC)]
+        L.orc_assemble_matrix_csc_rect.argtypes = [C.c_int64, C.c_int, C.c_int, P, P, P,
+                                                   C.c_int64, C.c_int64, C.POINTER(_CSC)]
         L.orc_csc_free.argtypes = [C.POINTER(_CSC)]
         L.orc_assemble_vector.argtypes = [C.c_int64, C.c_int, P, P, P]
         L.orc_pcg.argtypes = [C.POINTER(_CSC), P, P, C.c_double, C.c_int, C.c_int, C.c_int, P]
@@ -290,16 +292,19 @@ def q1_cell_arrays(D, cell_nodes, coords, degree, geom=GEOM_CARTESIAN, h=None, k
 
 # ---- assembly ------------------------------------------------------------------------------
 def assemble_csc(cell_rows, cell_cols, cellmats, nrows, ncols):
-    """Gridap's SparseMatrixCSC{Float64,Int}: returns (colptr, rowval, nzval), 1-based."""
+    """Gridap's SparseMatrixCSC{Float64,Int}: returns (colptr, rowval, nzval), 1-based.
+    cellmats[c, i, j] pairs cell_rows[c, i] with cell_cols[c, j]; the two id tables may have
+    different widths (a rectangular block)."""
     cell_rows = np.ascontiguousarray(cell_rows, np.int32)
     cell_cols = np.ascontiguousarray(cell_cols, np.int32)
-    nc, nd = cell_rows.shape
+    nc, ndr = cell_rows.shape
+    ndc = cell_cols.shape[1]
     cm = None
     if cellmats is not None:
         cm = np.ascontiguousarray(np.transpose(cellmats, (0, 2, 1)), np.float64)  # col-major
     out = _CSC()
-    st = lib().orc_assemble_matrix_csc(nc, nd, _p(cell_rows), _p(cell_cols), _p(cm), nrows,
-                                       ncols, C.byref(out))
+    st = lib().orc_assemble_matrix_csc_rect(nc, ndr, ndc, _p(cell_rows), _p(cell_cols), _p(cm),
+                                            nrows, ncols, C.byref(out))
     if st != 0:
         raise MemoryError("oracle assembly failed")
     nnz = out.nnz
@@ -741,3 +746,128 @@ def reindex_cell_dofs(cell_dofs, iperm):
     m = cd > 0
     out[m] = iperm[cd[m] - 1]
     return out.astype(np.int32)
+
+
+# ---- multi-field cell arrays (MultiFieldFESpace, Stokes-like forms) ------------------------
+MOP_VALUE, MOP_GRAD, MOP_DIV = 0, 1, 2
+
+
+def _mf_operand(op, ncomp, phi, P, D):
+    """Dense operand of every local basis function at every point: phi (nq, nn) values and
+    P (nc, nq, nn, D) physical gradients -> (nc, nq, nd) + shape, with nd = ncomp * nn and
+    local dof l = comp * nn + node (component-major, as Gridap's vector Lagrangian reffes).
+    value: phi (scalar) or e_c phi; grad: grad phi or e_c (x) grad phi (row c of the D x D
+    gradient, Fields/DiffOperators.jl); div = tr(grad) (DiffOperators.jl:7)."""
+    nc, nq, nn, _ = P.shape
+    if ncomp == 1:
+        if op == MOP_VALUE:
+            return np.broadcast_to(phi[None], (nc, nq, nn))
+        if op == MOP_GRAD:
+            return P
+        raise ValueError("div of a scalar field")
+    nd = ncomp * nn
+    if op == MOP_VALUE:
+        out = np.zeros((nc, nq, nd, D))
+        for c in range(D):
+            out[:, :, c * nn:(c + 1) * nn, c] = phi[None]
+        return out
+    if op == MOP_GRAD:
+        out = np.zeros((nc, nq, nd, D, D))
+        for c in range(D):
+            out[:, :, c * nn:(c + 1) * nn, c, :] = P
+        return out
+    out = np.zeros((nc, nq, nd))
+    for c in range(D):
+        out[:, :, c * nn:(c + 1) * nn] = P[..., c]
+    return out
+
+
+def multifield_cell_arrays(D, coords, cell_nodes, fields, terms, degree):
+    """Cell matrices per field pair and cell vectors per field of a multi-field form, by
+    Gridap's per-point evaluation (CellData/CellQuadratures.jl:138-170: sum over the
+    tensor Gauss points of integrand(x_q) w_q |det J_q|, J from the cell's Q1 map,
+    grad = J^-T grad_xi) of each product term (MultiField/MultiFieldCellFields.jl: one block
+    per (test field, trial field)), the operands contracted fully (inner / ⊙,
+    TensorValues/Operations.jl).
+    fields: [(order, ncomp)]; terms: [(test_field, test_op, trial_field or None, trial_op,
+    coef, cell_coef or None, qdata or None (ncells, nq, k))]. Returns (K, F): K[(i, j)] of
+    shape (ncells, nd_i, nd_j) [c, row, col] and F[i] (ncells, nd_i)."""
+    qx, qw = tensor_quadrature(D, degree)
+    phi1, g1 = q1_shapes(D, qx)
+    X = coords[cell_nodes - 1]                             # (nc, 2^D, D)
+    J = np.einsum("cad,qae->cqde", X, g1)                  # dx_d / dxi_e
+    det = np.linalg.det(J)
+    if np.any(det <= 0):
+        raise RuntimeError("oracle: degenerate cell")
+    JinvT = np.linalg.inv(J).transpose(0, 1, 3, 2)
+    dV = det * qw[None, :]                                 # (nc, nq)
+    tabs = []
+    for order, ncomp in fields:
+        phi, dphi = (q1_shapes(D, qx) if order == 1 else q2_shapes(D, qx))
+        P = np.einsum("cqde,qne->cqnd", JinvT, dphi)
+        tabs.append((phi, P, ncomp))
+    nc = cell_nodes.shape[0]
+    K, F = {}, {}
+    for tf, top, uf, uop, coef, cell_coef, qdata in terms:
+        phi_t, P_t, nc_t = tabs[tf]
+        Tt = _mf_operand(top, nc_t, phi_t, P_t, D)
+        w = dV * coef * (1.0 if cell_coef is None else np.asarray(cell_coef)[:, None])
+        nq, nd = Tt.shape[1], Tt.shape[2]
+        Ts = Tt.reshape(nc, nq, nd, -1)  # trailing operand dims flattened: the contraction
+        if uf is None:
+            f = (np.ones((nc, nq, 1)) if qdata is None
+                 else np.asarray(qdata).reshape(nc, nq, -1))
+            if f.shape[2] != Ts.shape[3]:
+                raise ValueError("data of another shape than the test operand")
+            val = np.einsum("cq,cqls,cqs->cl", w, Ts, f)
+            F[tf] = F.get(tf, 0.0) + val
+            continue
+        phi_u, P_u, nc_u = tabs[uf]
+        Tu = _mf_operand(uop, nc_u, phi_u, P_u, D)
+        if Tt.shape[3:] != Tu.shape[3:]:
+            raise ValueError("operands of different shapes")
+        Us = Tu.reshape(nc, nq, Tu.shape[2], -1)
+        val = np.einsum("cq,cqis,cqjs->cij", w, Ts, Us)
+        K[(tf, uf)] = K.get((tf, uf), 0.0) + val
+    return K, F
+
+
+def multifield_assemble(cell_ids, nfree_fields, K, F, uD_fields, rows_of=None):
+    """Gridap's monolithic assembly of a consecutive multi-field system: cell ids per field
+    (free ids already offset, Dirichlet ids field-local), K/F from multifield_cell_arrays,
+    Dirichlet values per field. The matrix is the sum of the per-block assemblies (each
+    (row, col) entry belongs to one field pair, whose contributions arrive in cell order);
+    the vector is sum over cells of F_c - K_c u_D,c (AttachDirichletMap,
+    CellData/AttachDirichlet.jl:59-110). Returns (scipy CSR of the matrix, b)."""
+    import scipy.sparse as sp
+    n = sum(nfree_fields)
+    nf = len(cell_ids)
+    # the blocks' entries are disjoint: their triplets side by side (a sparse sum would drop
+    # the structural zeros, e.g. the cross-component entries of a vector field's block)
+    rr, cc, vv = [], [], []
+    for (i, j), Kij in K.items():
+        cp, rv, nz = assemble_csc(cell_ids[i], cell_ids[j], Kij, n, n)
+        rr.append(rv - 1)
+        cc.append(np.repeat(np.arange(n), np.diff(cp)))
+        vv.append(nz)
+    A = sp.coo_matrix((np.concatenate(vv), (np.concatenate(rr), np.concatenate(cc))),
+                      shape=(n, n)).tocsr()
+    nc = cell_ids[0].shape[0]
+    rows = np.concatenate(cell_ids, axis=1)
+    vec = np.zeros((nc, rows.shape[1]))
+    starts = np.concatenate([[0], np.cumsum([c.shape[1] for c in cell_ids])])
+    for i in range(nf):
+        if i in F:
+            vec[:, starts[i]:starts[i + 1]] += F[i]
+    for i in range(nf):
+        lift = np.zeros((nc, cell_ids[i].shape[1]))
+        for j in range(nf):
+            if (i, j) not in K or uD_fields[j] is None:
+                continue
+            ids = cell_ids[j]
+            u = np.where(ids < 0, np.asarray(uD_fields[j])[np.maximum(-ids, 1) - 1], 0.0)
+            lift += np.einsum("cij,cj->ci", K[(i, j)], u)
+        vec[:, starts[i]:starts[i + 1]] -= lift
+    b = assemble_vector(rows, vec, n)
+    A.sort_indices()
+    return A, b

@@ -171,6 +171,69 @@ def test_rectangular_and_masked_vector_ids(gg, orc, kats):
     _assert_csr_equals_csc(A, csc, nfree)
 
 
+class _Sized:
+    """Stand-in space with a given number of free dofs (synthetic cell id tables)."""
+
+    def __init__(self, n):
+        self.n = n
+
+    def num_free_dofs(self):
+        return self.n
+
+
+@pytest.mark.parametrize("nd,ncells,ncols,hub", [
+    (4, 100, 90, 0),     # rows of <= 32 columns: the 32-column shared list
+    (3, 400, 60, 14),    # 33..64 columns, nd not a multiple of 4 (unpacked positions)
+    (8, 120, 400, 14),   # 65..128 columns, packed positions
+    (5, 200, 2000, 60),  # more than 128 columns: the general two-pass kernel
+])
+def test_pattern_width_classes_match_oracle(gg, orc, nd, ncells, ncols, hub):
+    """Random cell ids with Dirichlet (negative) entries; `hub` cells share one row so that
+    it reaches each width class of the symbolic kernels. Pattern and values are Gridap's."""
+    rng = np.random.default_rng(100 + nd)
+    # distinct ids within a cell, as in every mesh (a repeated id would make the order of the
+    # additions inside one cell matter)
+    ids = np.stack([rng.choice(np.arange(2, ncols + 1), nd, replace=False)
+                    for _ in range(ncells)]).astype(np.int32)
+    ids[:hub, 0] = 1
+    ids[rng.random(ids.shape) < 0.1] *= -1
+    cm = rng.standard_normal((ncells, nd, nd))
+    csc = orc.assemble_csc(ids, ids, cm, ncols, ncols)
+    assem = gg.SparseMatrixAssembler(_Sized(ncols), _Sized(ncols))
+    A = gg.symbolic_loop_matrix(assem, (None, ids, ids))
+    gg.numeric_loop_matrix(A, assem, (cm, ids, ids))
+    _assert_csr_equals_csc(A, csc, ncols)
+    rp = A.export_csr(0)[0]
+    lo, hi = {4: (0, 32), 3: (32, 64), 8: (64, 128), 5: (128, 512)}[nd]
+    assert lo < int(np.diff(rp).max()) <= hi
+
+
+@pytest.mark.parametrize("ndr,ndc,nrows,ncols", [(6, 3, 80, 40), (4, 9, 50, 300)])
+def test_rectangular_cell_blocks_match_oracle(gg, orc, ndr, ndc, nrows, ncols):
+    """Off-diagonal block of a multi-field system: nd_rows row ids against nd_cols column
+    ids per cell; pattern and values are Gridap's CSC of that block, bit for bit."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(ndr * 10 + ndc)
+    ncells = 150
+    rows = np.stack([rng.choice(np.arange(1, nrows + 1), ndr, replace=False)
+                     for _ in range(ncells)]).astype(np.int32)
+    cols = np.stack([rng.choice(np.arange(1, ncols + 1), ndc, replace=False)
+                     for _ in range(ncells)]).astype(np.int32)
+    rows[rng.random(rows.shape) < 0.1] *= -1
+    cols[rng.random(cols.shape) < 0.1] *= -1
+    cm = rng.standard_normal((ncells, ndr, ndc))
+    csc = orc.assemble_csc(rows, cols, cm, nrows, ncols)
+    assem = gg.SparseMatrixAssembler(_Sized(ncols), _Sized(nrows))
+    A = gg.symbolic_loop_matrix(assem, (None, rows, cols))
+    assert A.shape == (nrows, ncols)
+    gg.numeric_loop_matrix(A, assem, (cm, rows, cols))
+    S = sp.csc_matrix((csc[2], csc[1] - 1, csc[0] - 1), shape=(nrows, ncols)).tocsr()
+    S.sort_indices()
+    rp, col, nz = A.export_csr(0)
+    assert np.array_equal(rp, S.indptr) and np.array_equal(col, S.indices)
+    assert np.array_equal(nz, S.data)
+
+
 def test_determinism(gg):
     rng = np.random.default_rng(9)
     dom, part = (0, 1, 0, 1, 0, 1), (12, 10, 9)

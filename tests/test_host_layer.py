@@ -281,3 +281,84 @@ def test_coordinate_reordering_matches_oracle(gg, orc):
         assert W.num_dirichlet_dofs() == V.num_dirichlet_dofs()
         fw, _, _, _ = W.dof_points()
         assert np.array_equal(fw[ip - 1], fx)
+
+
+def test_block_field_offsets_kat(gg):
+    """MultiFieldFESpacesTests.jl:121-145: field offsets and block sizes of permuted block
+    layouts (there with Q1, Q2, Q3 fields; here Q1, Q2 and a vector Q1 field stand in)."""
+    model = gg.CartesianDiscreteModel((0.0, 1.0, 0.0, 1.0), (2, 2))
+    V1 = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, float, 1))
+    V2 = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, float, 2))
+    V3 = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, 2, 1))
+    nd = [V.num_free_dofs() for V in (V1, V2, V3)]
+    assert nd == [9, 25, 18]
+    X1 = gg.MultiFieldFESpace([V1, V2, V3], style=gg.BlockMultiFieldStyle(2, (2, 1), (1, 2, 3)))
+    X2 = gg.MultiFieldFESpace([V1, V2, V3], style=gg.BlockMultiFieldStyle(2, (2, 1), (3, 1, 2)))
+    X3 = gg.MultiFieldFESpace([V1, V2, V3], style=gg.BlockMultiFieldStyle(2, (1, 2), (1, 3, 2)))
+    assert gg.compute_field_offsets(X1) == (0, nd[0], 0)
+    assert gg.compute_field_offsets(X2) == (nd[2], 0, 0)
+    assert gg.compute_field_offsets(X3) == (0, nd[2], 0)
+    assert X1.block_num_free_dofs() == [nd[0] + nd[1], nd[2]]
+    assert X2.block_num_free_dofs() == [nd[2] + nd[0], nd[1]]
+    assert X3.block_num_free_dofs() == [nd[0], nd[2] + nd[1]]
+    # consecutive: offsets are the running sums; cell ids shift only the free dofs
+    X = gg.MultiFieldFESpace([V1, V2, V3])
+    assert gg.compute_field_offsets(X) == (0, nd[0], nd[0] + nd[1])
+    ids = X.get_cell_dof_ids()
+    assert ids.shape == (4, 4 + 9 + 8)
+    assert np.array_equal(ids[:, :4], V1.get_cell_dof_ids())
+    assert np.array_equal(ids[:, 4:13], V2.get_cell_dof_ids() + nd[0])
+    x = np.arange(X.num_free_dofs(), dtype=float)
+    assert np.array_equal(X.restrict_to_field(x, 2), x[nd[0] + nd[1]:])
+    xb = X2.zero_free_values()
+    assert [v.size for v in xb] == X2.block_num_free_dofs()
+
+
+def test_multifield_forms_are_classified(gg):
+    """Stokes' a((u,p),(v,q)) and l((v,q)) split into one term per operand pair."""
+    import importlib
+    cd = importlib.import_module(gg.__name__ + ".celldata")
+    model = gg.CartesianDiscreteModel((0.0, 1.0, 0.0, 1.0), (2, 2))
+    V = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, 2, 2), dirichlet_tags="boundary")
+    Q = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, float, 1))
+    X = gg.MultiFieldFESpace([V, Q])
+    (u, p), (v, q) = gg.get_trial_fe_basis(X), gg.get_fe_basis(X)
+    kap = gg.CellField(np.ones(4))
+    e = gg.inner(gg.grad(v), gg.grad(u)) - gg.div(v) * p + q * gg.div(u) + kap * (2.0 * q * p)
+    terms = cd.classify_multifield(e, True)
+    got = [(t.test_field, t.test_op, t.trial_field, t.trial_op, t.coef) for t in terms]
+    assert got == [(0, cd.MOP_GRAD, 0, cd.MOP_GRAD, 1.0), (0, cd.MOP_DIV, 1, cd.MOP_VALUE, -1.0),
+                   (1, cd.MOP_VALUE, 0, cd.MOP_DIV, 1.0), (1, cd.MOP_VALUE, 1, cd.MOP_VALUE, 2.0)]
+    assert terms[3].cell_coef is not None
+    f = lambda x: x  # noqa: E731
+    lt = cd.classify_multifield(gg.inner(v, f) - 3.0 * q, False)
+    assert [(t.test_field, t.test_op, t.trial_field, t.coef) for t in lt] == \
+        [(0, cd.MOP_VALUE, None, 1.0), (1, cd.MOP_VALUE, None, -3.0)]
+    assert lt[0].data is f and lt[1].data is None
+    with pytest.raises(NotImplementedError):
+        cd.classify_multifield(gg.inner(gg.grad(v), gg.grad(u)) * p, True)
+
+
+def test_lagrangian_tables_reproduce_polynomials(gg):
+    """Q1/Q2 shape tables in Gridap's node order interpolate their polynomials exactly."""
+    import importlib
+    mf = importlib.import_module(gg.__name__ + ".multifield")
+    fs = importlib.import_module(gg.__name__ + ".fespaces")
+    for D in (2, 3):
+        qx, qw = mf.tensor_gauss(D, 4)
+        assert abs(qw.sum() - 1.0) < 1e-14
+        for order in (1, 2):
+            phi, grads = mf.lagrangian_tables(D, order, qx)
+            xn = fs.ncube_node_refs(D, order)
+            c = np.arange(1, D + 1, dtype=float)
+            if order == 1:
+                p = lambda x: 1.0 + x @ c + np.prod(x[:, :2], axis=1)  # noqa: E731
+            else:
+                p = lambda x: 1.0 + x @ c + (x[:, 0] ** 2) * x[:, 1]  # noqa: E731
+            assert np.abs(phi @ p(xn) - p(qx)).max() < 1e-13
+            h = 1e-6
+            for e in range(D):
+                dx = np.zeros(D)
+                dx[e] = h
+                fd = (p(qx + dx) - p(qx - dx)) / (2 * h)
+                assert np.abs(grads[:, :, e] @ p(xn) - fd).max() < 1e-8

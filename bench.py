@@ -150,18 +150,19 @@ def mg_levels(n):
 
 def vcycle_bytes(n):
     """Algorithmic bytes of one V-cycle (FP32): per level with R rows, C cells and Rc coarse
-    rows, the first sweep (b, D read, x written: 12 R), each further sweep and the residual a
-    lattice apply (kappa 4 C, x read and t written 8 R) and an update (b, t, D, x read, x
-    written: 20 R), restriction (b, t read 8 R, 4 Rc written), prolongation (4 Rc read, x
-    read and written 8 R): 16 C + 120 R + 8 Rc per level; the coarsest level eight sweeps."""
+    rows, the first sweep (b, D read, x written: 12 R), three fused sweeps (kappa 4 C; x, b,
+    D read and x written 16 R each), the fused residual (kappa 4 C; x, b read, r written
+    12 R), restriction (r read 4 R, 4 Rc written) and prolongation (4 Rc and x read, x
+    written 8 R): 16 C + 84 R + 8 Rc per level; the coarsest level the first sweep and eight
+    fused ones."""
     lv = mg_levels(n)
     tot = 0
     for i, m in enumerate(lv):
         R, C = (m - 1) ** 3, m ** 3
         if i + 1 < len(lv):
-            tot += 16 * C + 120 * R + 8 * (lv[i + 1] - 1) ** 3
+            tot += 16 * C + 84 * R + 8 * (lv[i + 1] - 1) ** 3
         else:
-            tot += 12 * R + 7 * (4 * C + 28 * R)
+            tot += 12 * R + 8 * (4 * C + 16 * R)
     return tot
 
 
@@ -432,8 +433,9 @@ def run_gpu(args):
                                traffic=None)
         kinds["vector32"].update(kernel="k_fcg_update; k_fcg_beta + k_fcg_dir (FP32 FCG "
                                         "vector updates)", alg=22 * nfree, traffic=None)
-        kinds["vcycle"] = dict(kernel="multigrid V-cycle (CUDA graph: k_mg_apply, k_mg_jacobi, "
-                                      "k_mg_restrict, k_mg_prolong over %d levels)"
+        kinds["vcycle"] = dict(kernel="multigrid V-cycle (CUDA graph: k_mg_smooth, "
+                                      "k_mg_residual, k_mg_restrict, k_mg_prolong over %d "
+                                      "levels)"
                                       % len(mg_levels(args.n)),
                                alg=vcycle_bytes(args.n), traffic=None,
                                kt=r_mixed_kt["kt"][_lib.GFE_KT_PRECOND])

@@ -58,11 +58,15 @@ struct CartesianDiffusionQ1 {
     if (FP32) return (double)((float)kap * (float)k);
     return kap * k;
   }
-  __device__ __forceinline__ int64_t node(int64_t cell, int a) const {
-    if (cell_nodes) return (int64_t)__ldg(cell_nodes + cell * NV + a) - 1;
-    const int64_t i = cell % n0, r = cell / n0, j = r % n1, k = r / n1;
-    const int64_t np0 = n0 + 1, np1 = n1 + 1;
-    return (i + (a & 1)) + np0 * ((j + ((a >> 1) & 1)) + np1 * (k + ((a >> 2) & 1)));
+  // node of local vertex 0 of a Cartesian cell and the node strides of y and z: the cell id
+  // is split once in 32-bit arithmetic (cell ids are below 2^31), the other vertices follow
+  // by offsets (64-bit division per vertex dominated the row gather's instruction count)
+  __device__ __forceinline__ int64_t node0(int64_t cell, int64_t& sy, int64_t& sz) const {
+    const uint32_t c = (uint32_t)cell, u0 = (uint32_t)n0, u1 = (uint32_t)n1;
+    const uint32_t r = c / u0, i = c - r * u0, k = r / u1, j = r - k * u1;
+    sy = n0 + 1;
+    sz = sy * (n1 + 1);
+    return (int64_t)i + sy * j + sz * k;
   }
   __device__ __forceinline__ double v(const double* s, int64_t cell, int li) const {
     const double* Mref = s + NV * NV;
@@ -72,7 +76,20 @@ struct CartesianDiffusionQ1 {
     if (src_kind == GFE_SRC_NODAL) {
       double acc = 0.0;
 #pragma unroll
-      for (int a = 0; a < NV; ++a) acc = fma(Mref[li + a * NV], __ldg(src + node(cell, a)), acc);
+      if (cell_nodes) {
+#pragma unroll
+        for (int a = 0; a < NV; ++a)
+          acc = fma(Mref[li + a * NV], __ldg(src + (__ldg(cell_nodes + cell * NV + a) - 1)),
+                    acc);
+        return acc;
+      }
+      int64_t sy, sz;
+      const int64_t b0 = node0(cell, sy, sz);
+#pragma unroll
+      for (int a = 0; a < NV; ++a) {
+        const int64_t nd = b0 + (a & 1) + sy * ((a >> 1) & 1) + (D == 3 ? sz * (a >> 2) : 0);
+        acc = fma(Mref[li + a * NV], __ldg(src + nd), acc);
+      }
       return acc;
     }
     if (src_kind == GFE_SRC_QPOINT) {

@@ -41,17 +41,16 @@ struct LatticeQ1Op {
   }
 };
 
-// The rows of one tile: (i, j) = (32 bx + lane, 8 by + warp), k-planes kLatK bz .. + kLatK.
-// Adds p.q (and p.r for flexible CG) of the thread's rows to d1 (d2).
-template <bool FCG, bool PAD>
-__device__ __forceinline__ void lattice_tile(const LatticeQ1Op& op, int bx, int by, int bz,
-                                             const float* __restrict__ p, float* __restrict__ q,
-                                             const float* __restrict__ rr, float& d1,
-                                             float& d2) {
+// The rows of one tile: (i, j) = (32 bx + lane, 8 by + warp), k-planes KZ bz .. + KZ (KZ = 1
+// for small lattices: more blocks, shorter per-thread chains). For every row the epilogue
+// receives (row index, p at the row, (A p)_row).
+template <bool PAD, class Epi, int KZ = kLatK>
+__device__ __forceinline__ void lattice_rows(const LatticeQ1Op& op, int bx, int by, int bz,
+                                             const float* __restrict__ p, Epi& epi) {
   const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
   const int i = bx * 32 + (int)(threadIdx.x & 31);
   const int j = by * 8 + (int)(threadIdx.x >> 5);
-  const int k0 = bz * kLatK;
+  const int k0 = bz * KZ;
   if (i < m0 && j < m1) {
     const bool okx[3] = {i > 0, true, i < m0 - 1};
     const bool oky[3] = {j > 0, true, j < m1 - 1};
@@ -85,7 +84,7 @@ __device__ __forceinline__ void lattice_tile(const LatticeQ1Op& op, int bx, int 
     xplane(k0, xb);
     kplane(k0, ka);
 #pragma unroll
-    for (int t = 0; t < kLatK; ++t) {
+    for (int t = 0; t < KZ; ++t) {
       const int k = k0 + t;
       if (k < m2) {
         xplane(k + 1, xc);
@@ -108,10 +107,7 @@ __device__ __forceinline__ void lattice_tile(const LatticeQ1Op& op, int bx, int 
               }
               acc = fmaf(cz == 0 ? ka[cx + 2 * cy] : kb[cx + 2 * cy], s, acc);
             }
-        const int64_t row = col + (int64_t)sz * k;
-        q[row] = acc;
-        d1 = fmaf(xb[4], acc, d1);
-        if (FCG) d2 = fmaf(xb[4], __ldg(rr + row), d2);
+        epi(col + (int64_t)sz * k, xb[4], acc);
       }
 #pragma unroll
       for (int e = 0; e < 9; ++e) {
@@ -124,3 +120,16 @@ __device__ __forceinline__ void lattice_tile(const LatticeQ1Op& op, int bx, int 
   }
 }
 
+// q = A p over one tile; adds p.q (and p.r for flexible CG) of the thread's rows to d1 (d2).
+template <bool FCG, bool PAD>
+__device__ __forceinline__ void lattice_tile(const LatticeQ1Op& op, int bx, int by, int bz,
+                                             const float* __restrict__ p, float* __restrict__ q,
+                                             const float* __restrict__ rr, float& d1,
+                                             float& d2) {
+  auto epi = [&](int64_t row, float pc, float acc) {
+    q[row] = acc;
+    d1 = fmaf(pc, acc, d1);
+    if (FCG) d2 = fmaf(pc, __ldg(rr + row), d2);
+  };
+  lattice_rows<PAD>(op, bx, by, bz, p, epi);
+}

@@ -9,8 +9,10 @@
 // in 3-D), which for piecewise-constant kappa equals the Galerkin product P^T A P of the
 // nested Q1 spaces. Transfers are trilinear interpolation P and its transpose R = P^T (full
 // weighting 1, 1/2, 1/4, 1/8). Smoothing is damped Jacobi (omega 0.8, two sweeps before and
-// after, the first from zero), the coarsest level takes eight sweeps. All vectors are FP32 in
-// the lattice row order; every kernel returns at once when the solver's done flag is set.
+// after, the first from zero), each later sweep fused into one pass over the lattice stencil;
+// the coarsest level takes nine sweeps. All vectors are FP32 in the lattice row order; every
+// kernel returns at once when the solver's done flag is set.
+#include <utility>
 #include <vector>
 
 #include "gfe_internal.h"
@@ -26,13 +28,30 @@ constexpr int kPreSweeps = 2, kCoarseSweeps = 8;
 
 __device__ __forceinline__ bool stop(const int* done) { return done && *done; }
 
+// One damped Jacobi sweep fused into the lattice apply: xo = x + omega D^-1 (b - A x)
+// (xo != x: the sweep reads the old neighbours). Same arithmetic as an apply into t followed
+// by the update x += omega D^-1 (b - t).
+template <int KZ>
 __global__ void __launch_bounds__(kMgBlock)
-    k_mg_apply(LatticeQ1Op op, const float* __restrict__ x, float* __restrict__ y,
-               const int* done) {
+    k_mg_smooth(LatticeQ1Op op, const float* __restrict__ x, const float* __restrict__ b,
+                const float* __restrict__ dinv, float* __restrict__ xo, const int* done) {
   if (stop(done)) return;
-  float d1 = 0.f, d2 = 0.f;
-  lattice_tile<false, false>(op, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, x, y,
-                             nullptr, d1, d2);
+  auto epi = [&](int64_t row, float xc, float acc) {
+    xo[row] = fmaf(kOmega * __ldg(dinv + row), __ldg(b + row) - acc, xc);
+  };
+  lattice_rows<false, decltype(epi), KZ>(op, (int)blockIdx.x, (int)blockIdx.y,
+                                         (int)blockIdx.z, x, epi);
+}
+
+// r = b - A x (the residual the restriction takes to the coarse level)
+template <int KZ>
+__global__ void __launch_bounds__(kMgBlock)
+    k_mg_residual(LatticeQ1Op op, const float* __restrict__ x, const float* __restrict__ b,
+                  float* __restrict__ r, const int* done) {
+  if (stop(done)) return;
+  auto epi = [&](int64_t row, float, float acc) { r[row] = __ldg(b + row) - acc; };
+  lattice_rows<false, decltype(epi), KZ>(op, (int)blockIdx.x, (int)blockIdx.y,
+                                         (int)blockIdx.z, x, epi);
 }
 
 // x = omega D^-1 b  (first sweep from zero)
@@ -45,21 +64,11 @@ __global__ void k_mg_jacobi0(int64_t n, const float* __restrict__ b,
     x[i] = kOmega * dinv[i] * b[i];
 }
 
-// x += omega D^-1 (b - t), t = A x
-__global__ void k_mg_jacobi(int64_t n, const float* __restrict__ b, const float* __restrict__ t,
-                            const float* __restrict__ dinv, float* __restrict__ x,
-                            const int* done) {
-  if (stop(done)) return;
-  for (int64_t i = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * kMgBlock)
-    x[i] = fmaf(kOmega * dinv[i], b[i] - t[i], x[i]);
-}
-
-// b_c = R (b_f - t_f): coarse interior node (I, J, K) sits on fine interior node
-// (2I+1, 2J+1, 2K+1); weights prod_d (1 - |delta_d| / 2) over the 27 fine neighbours
+// b_c = R r_f: coarse interior node (I, J, K) sits on fine interior node (2I+1, 2J+1, 2K+1);
+// weights prod_d (1 - |delta_d| / 2) over the 27 fine neighbours
 __global__ void k_mg_restrict(int mf0, int mf1, int mc0, int mc1, int mc2,
-                              const float* __restrict__ bf, const float* __restrict__ tf,
-                              float* __restrict__ bc, const int* done) {
+                              const float* __restrict__ rf, float* __restrict__ bc,
+                              const int* done) {
   if (stop(done)) return;
   const int64_t nc = (int64_t)mc0 * mc1 * mc2;
   for (int64_t c = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; c < nc;
@@ -77,16 +86,16 @@ __global__ void k_mg_restrict(int mf0, int mf1, int mc0, int mc1, int mc2,
           const float w = (dx ? 0.5f : 1.f) * (dy ? 0.5f : 1.f) * (dz ? 0.5f : 1.f);
           const int64_t f = (int64_t)(2 * I + 1 + dx) +
                             (int64_t)mf0 * ((2 * J + 1 + dy) + (int64_t)mf1 * (2 * K + 1 + dz));
-          s = fmaf(w, bf[f] - tf[f], s);
+          s = fmaf(w, rf[f], s);
         }
     bc[c] = s;
   }
 }
 
-// x_f += P x_c (trilinear; coarse boundary nodes are zero)
+// xo_f = x_f + P x_c (trilinear; coarse boundary nodes are zero), out of place
 __global__ void k_mg_prolong(int mf0, int mf1, int mf2, int mc0, int mc1, int mc2,
-                             const float* __restrict__ xc, float* __restrict__ xf,
-                             const int* done) {
+                             const float* __restrict__ xc, const float* __restrict__ xf,
+                             float* __restrict__ xo, const int* done) {
   if (stop(done)) return;
   const int64_t nf = (int64_t)mf0 * mf1 * mf2;
   for (int64_t f = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; f < nf;
@@ -125,7 +134,7 @@ __global__ void k_mg_prolong(int mf0, int mf1, int mf2, int mc0, int mc1, int mc
           if (w == 0.f) continue;
           s = fmaf(w, xc[(int64_t)ci[a] + (int64_t)mc0 * (cj[bb] + (int64_t)mc1 * ck[cc])], s);
         }
-    xf[f] += s;
+    xo[f] = xf[f] + s;
   }
 }
 
@@ -198,36 +207,56 @@ unsigned vgrid(gfe_ctx* ctx, int64_t n) {
       1, std::min<int64_t>((n + kMgBlock - 1) / kMgBlock, (int64_t)ctx->num_sms * 8));
 }
 
+// The V-cycle of level l: b in L.b, the result in L.x. Sweeps alternate between L.x and L.t
+// (a fused sweep cannot run in place); the sweep counts keep the result in L.x: the first
+// sweep from zero writes L.x, one more pre-sweep moves it to L.t, the residual goes to L.x,
+// prolongation writes L.x from L.t, and the two post-sweeps return to L.x. The coarsest
+// level takes the first sweep and eight more.
 int vcycle(LatticeMG* mg, size_t l, const int* done) {
   gfe_ctx* ctx = mg->ctx;
   LatticeMG::Level& L = mg->lv[l];
   const unsigned g = vgrid(ctx, L.n);
   const dim3 ga = L.op.grid(L.n);
   const bool coarsest = l + 1 == mg->lv.size();
-  const int pre = coarsest ? kCoarseSweeps : kPreSweeps;
-  k_mg_jacobi0<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.dinv, L.x, done);
+  const int pre = coarsest ? kCoarseSweeps + 1 : kPreSweeps;
+  float* cur = L.x;
+  float* oth = L.t;
+  // lattices too small for 4 blocks per SM march one k-plane per thread
+  const bool deep = (int64_t)ga.x * ga.y * ga.z >= 4 * (int64_t)ctx->num_sms;
+  const dim3 ga1 = L.op.grid_k(1);
+  auto smooth = [&](const float* xi, float* xo) {
+    if (deep)
+      k_mg_smooth<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, xi, L.b, L.dinv, xo, done);
+    else
+      k_mg_smooth<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, xi, L.b, L.dinv, xo, done);
+    ctx->launches++;
+  };
+  k_mg_jacobi0<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.dinv, cur, done);
   ctx->launches++;
   for (int s = 1; s < pre; ++s) {
-    k_mg_apply<<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.t, done);
-    k_mg_jacobi<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.t, L.dinv, L.x, done);
-    ctx->launches += 2;
+    smooth(cur, oth);
+    std::swap(cur, oth);
   }
-  if (coarsest) return GFE_OK;
+  if (coarsest) return cur == L.x ? GFE_OK
+                                  : set_error(GFE_ERR_UNSUPPORTED, "multigrid: sweep parity");
   LatticeMG::Level& C = mg->lv[l + 1];
-  k_mg_apply<<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.t, done);
+  if (deep)
+    k_mg_residual<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, cur, L.b, oth, done);
+  else
+    k_mg_residual<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, cur, L.b, oth, done);
   k_mg_restrict<<<vgrid(ctx, C.n), kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, C.m0, C.m1, C.m2,
-                                                               L.b, L.t, C.b, done);
+                                                               oth, C.b, done);
   ctx->launches += 2;
   GFE_TRY(vcycle(mg, l + 1, done));
-  k_mg_prolong<<<g, kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, L.m2, C.m0, C.m1, C.m2, C.x, L.x,
-                                                done);
+  k_mg_prolong<<<g, kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, L.m2, C.m0, C.m1, C.m2, C.x, cur,
+                                                oth, done);
   ctx->launches++;
+  std::swap(cur, oth);
   for (int s = 0; s < kPreSweeps; ++s) {
-    k_mg_apply<<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.t, done);
-    k_mg_jacobi<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.t, L.dinv, L.x, done);
-    ctx->launches += 2;
+    smooth(cur, oth);
+    std::swap(cur, oth);
   }
-  return GFE_OK;
+  return cur == L.x ? GFE_OK : set_error(GFE_ERR_UNSUPPORTED, "multigrid: sweep parity");
 }
 
 }  // namespace

@@ -1914,6 +1914,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   GFE_TRY(read_state(ctx, w));
   int updates = 0, slow = 0, fallback = 0;
   double rr_chunk = w.hS->rr;
+  bool fresh = false;  // the loop ended on a reliable update: x64 and rr64 are current
   while (!w.hS->done) {
     for (int k = 0; k < check_every; ++k) {
       timer_begin(ctx, GFE_KT_VECTOR);
@@ -1940,7 +1941,10 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       ctx->launches += 3;
       ++updates;
       GFE_TRY(read_state(ctx, w));
-      if (w.hS->converged || w.hS->done) break;
+      if (w.hS->converged || w.hS->done) {
+        fresh = true;
+        break;
+      }
       // z, p restart from the new residual direction (keeps FCG's beta well defined)
       GFE_TRY(precond());
       k_fcg_beta<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
@@ -1961,22 +1965,28 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     }
     rr_chunk = w.hS->rr;
   }
-  // any FP32 correction not yet absorbed
-  k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
-  ctx->launches++;
+  // any FP32 correction not yet absorbed (none when the loop ended on a reliable update)
+  if (!fresh) {
+    k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
+    ctx->launches++;
+  }
   rep->iterations = w.hS->iter;
   rep->refinements = updates;
   rep->operator_format = A->dia_valid ? 1 : 0;
   rep->ndiag = A->dia_valid ? A->dia_ndiag : 0;
   rep->fallback = fallback;
-  // true FP64 residual
-  residual64(&w.S->rr);
+  // true FP64 residual (the reliable update's when it ended the loop: x has not moved since)
+  if (!fresh) {
+    residual64(&w.S->rr);
+    ctx->launches++;
+  }
   k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb, &w.S->ticket[1]);
-  ctx->launches += 2;
+  ctx->launches++;
   GFE_CUDA_TRY(cudaGetLastError());
   GFE_TRY(read_state(ctx, w));
   const double bb = w.hS->bb;
-  rep->relres = bb > 0 ? std::sqrt(w.hS->rr / bb) : 0.0;
+  const double rr = fresh ? w.hS->rr64 : w.hS->rr;
+  rep->relres = bb > 0 ? std::sqrt(rr / bb) : 0.0;
   rep->converged = std::isfinite(rep->relres) && rep->relres <= o->rtol * (1.0 + 1e-6);
   rep->status = std::isfinite(rep->relres) ? GFE_OK : GFE_ERR_NONFINITE;
   return GFE_OK;

@@ -10,8 +10,9 @@
 // nested Q1 spaces. Transfers are trilinear interpolation P and its transpose R = P^T (full
 // weighting 1, 1/2, 1/4, 1/8). Smoothing is damped Jacobi (omega 0.8, two sweeps before and
 // after, the first from zero), each later sweep fused into one pass over the lattice stencil;
-// the coarsest level takes nine sweeps. All vectors are FP32 in the lattice row order; every
-// kernel returns at once when the solver's done flag is set.
+// the coarsest level takes nine sweeps. Levels of at most 512 rows run their part of the
+// cycle in one block. All vectors are FP32 in the lattice row order; every kernel returns at
+// once when the solver's done flag is set.
 #include <utility>
 #include <vector>
 
@@ -73,9 +74,10 @@ __global__ void k_mg_restrict(int mf0, int mf1, int mc0, int mc1, int mc2,
   const int64_t nc = (int64_t)mc0 * mc1 * mc2;
   for (int64_t c = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; c < nc;
        c += (int64_t)gridDim.x * kMgBlock) {
-    const int I = (int)(c % mc0);
-    const int64_t rest = c / mc0;
-    const int J = (int)(rest % mc1), K = (int)(rest / mc1);
+    // 32-bit index split (levels hold fewer than 2^31 rows)
+    const uint32_t cu = (uint32_t)c, rest = cu / (uint32_t)mc0;
+    const int I = (int)(cu - rest * (uint32_t)mc0);
+    const int K = (int)(rest / (uint32_t)mc1), J = (int)(rest - (uint32_t)K * (uint32_t)mc1);
     float s = 0.f;
 #pragma unroll
     for (int dz = -1; dz <= 1; ++dz)
@@ -92,7 +94,43 @@ __global__ void k_mg_restrict(int mf0, int mf1, int mc0, int mc1, int mc2,
   }
 }
 
-// xo_f = x_f + P x_c (trilinear; coarse boundary nodes are zero), out of place
+// (P x_c) at fine interior node (i, j, k): trilinear, coarse boundary nodes are zero
+__device__ __forceinline__ float prolong_value(int i, int j, int k, int mc0, int mc1, int mc2,
+                                               const float* __restrict__ xc) {
+  int ci[2], cj[2], ck[2];
+  float wi[2], wj[2], wk[2];
+  auto axis = [](int p, int mc, int* cc, float* ww) {  // p = lattice position (1-based)
+    if ((p & 1) == 0) {
+      cc[0] = p / 2 - 1;
+      ww[0] = 1.f;
+      cc[1] = -1;
+      ww[1] = 0.f;
+    } else {
+      cc[0] = p / 2 - 1;  // coarse interior index of lattice p/2 (-1: boundary)
+      cc[1] = p / 2;      // of lattice p/2 + 1 (mc: boundary)
+      ww[0] = ww[1] = 0.5f;
+      if (cc[1] >= mc) cc[1] = -1;
+    }
+  };
+  axis(i + 1, mc0, ci, wi);
+  axis(j + 1, mc1, cj, wj);
+  axis(k + 1, mc2, ck, wk);
+  float s = 0.f;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+      for (int cc = 0; cc < 2; ++cc) {
+        if (ci[a] < 0 || cj[bb] < 0 || ck[cc] < 0) continue;
+        const float w = wi[a] * wj[bb] * wk[cc];
+        if (w == 0.f) continue;
+        s = fmaf(w, xc[(int64_t)ci[a] + (int64_t)mc0 * (cj[bb] + (int64_t)mc1 * ck[cc])], s);
+      }
+  return s;
+}
+
+// xo_f = x_f + P x_c, out of place
 __global__ void k_mg_prolong(int mf0, int mf1, int mf2, int mc0, int mc1, int mc2,
                              const float* __restrict__ xc, const float* __restrict__ xf,
                              float* __restrict__ xo, const int* done) {
@@ -100,41 +138,10 @@ __global__ void k_mg_prolong(int mf0, int mf1, int mf2, int mc0, int mc1, int mc
   const int64_t nf = (int64_t)mf0 * mf1 * mf2;
   for (int64_t f = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; f < nf;
        f += (int64_t)gridDim.x * kMgBlock) {
-    const int i = (int)(f % mf0);
-    const int64_t rest = f / mf0;
-    const int j = (int)(rest % mf1), k = (int)(rest / mf1);
-    // lattice positions i+1 etc.; coarse lattice position p/2 (even) or between (odd)
-    int ci[2], cj[2], ck[2];
-    float wi[2], wj[2], wk[2];
-    auto axis = [](int p, int mc, int* cc, float* ww) {  // p = lattice position (1-based)
-      if ((p & 1) == 0) {
-        cc[0] = p / 2 - 1;
-        ww[0] = 1.f;
-        cc[1] = -1;
-        ww[1] = 0.f;
-      } else {
-        cc[0] = p / 2 - 1;  // coarse interior index of lattice p/2 (-1: boundary)
-        cc[1] = p / 2;      // of lattice p/2 + 1 (mc: boundary)
-        ww[0] = ww[1] = 0.5f;
-        if (cc[1] >= mc) cc[1] = -1;
-      }
-    };
-    axis(i + 1, mc0, ci, wi);
-    axis(j + 1, mc1, cj, wj);
-    axis(k + 1, mc2, ck, wk);
-    float s = 0.f;
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-      for (int bb = 0; bb < 2; ++bb)
-#pragma unroll
-        for (int cc = 0; cc < 2; ++cc) {
-          if (ci[a] < 0 || cj[bb] < 0 || ck[cc] < 0) continue;
-          const float w = wi[a] * wj[bb] * wk[cc];
-          if (w == 0.f) continue;
-          s = fmaf(w, xc[(int64_t)ci[a] + (int64_t)mc0 * (cj[bb] + (int64_t)mc1 * ck[cc])], s);
-        }
-    xo[f] = xf[f] + s;
+    const uint32_t fu = (uint32_t)f, rest = fu / (uint32_t)mf0;
+    const int i = (int)(fu - rest * (uint32_t)mf0);
+    const int k = (int)(rest / (uint32_t)mf1), j = (int)(rest - (uint32_t)k * (uint32_t)mf1);
+    xo[f] = xf[f] + prolong_value(i, j, k, mc0, mc1, mc2, xc);
   }
 }
 
@@ -173,6 +180,143 @@ __global__ void k_mg_diag(LatticeQ1Op op, float* __restrict__ dinv) {
            op.K[lr + 8 * lr];
     }
     dinv[r] = d > 0.f ? 1.f / d : 0.f;
+  }
+}
+
+// ---- the coarse levels in one block ------------------------------------------------------
+// Levels of at most kCoarseRows rows run their whole V-cycle inside one block of kCoarseBlock
+// threads (block-stride loops, a barrier between steps): on such lattices a launch costs
+// more than its work. The row operator below follows lattice_rows' loop order exactly. (With
+// 15^3-row levels inside, the one block's issue rate made the cycle slower than launches.)
+constexpr int kCoarseBlock = 512;
+constexpr int64_t kCoarseRows = 512;
+constexpr int kMaxCoarse = 6;
+
+struct MgLevelView {
+  LatticeQ1Op op;
+  int m0, m1, m2;
+  int64_t n;
+  float *x, *b, *t, *dinv;
+};
+
+struct CoarseLevels {
+  int nl;
+  MgLevelView L[kMaxCoarse];
+};
+
+// (A p)_r at interior node (i, j, k): its 27 neighbours loaded once (0 outside the interior),
+// then the 8 cells around it, 8 local columns each, in lattice_rows' order (32-bit indexing:
+// these levels are small)
+__device__ __forceinline__ float lattice_row_value(const LatticeQ1Op& op, int i, int j, int k,
+                                                   const float* __restrict__ p) {
+  const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
+  float v[27];
+#pragma unroll
+  for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx) {
+        const int ii = i - 1 + dx, jj = j - 1 + dy, kk = k - 1 + dz;
+        const bool in = ii >= 0 && ii < m0 && jj >= 0 && jj < m1 && kk >= 0 && kk < m2;
+        v[dx + 3 * dy + 9 * dz] = in ? p[ii + op.s1 * jj + op.s2 * kk] : 0.f;
+      }
+  float acc = 0.f;
+#pragma unroll
+  for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+      for (int cx = 0; cx < 2; ++cx) {
+        const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
+        float s = 0.f;
+#pragma unroll
+        for (int lc = 0; lc < 8; ++lc)
+          s = fmaf(op.K[lr + 8 * lc],
+                   v[(cx + (lc & 1)) + 3 * (cy + ((lc >> 1) & 1)) + 9 * (cz + (lc >> 2))], s);
+        acc = fmaf(op.kap[(i + cx) + op.c1 * (j + cy) + op.c2 * (k + cz)], s, acc);
+      }
+  return acc;
+}
+
+__device__ __forceinline__ void row_ijk(const MgLevelView& L, int64_t r, int& i, int& j,
+                                        int& k) {
+  const uint32_t ru = (uint32_t)r, rest = ru / (uint32_t)L.m0;
+  i = (int)(ru - rest * (uint32_t)L.m0);
+  k = (int)(rest / (uint32_t)L.m1);
+  j = (int)(rest - (uint32_t)k * (uint32_t)L.m1);
+}
+
+// the V-cycle of levels 0 .. nl-1 of `c` (level 0's b is given, its result lands in its x);
+// same steps, sweep counts and buffer roles as the multi-launch cycle
+__global__ void __launch_bounds__(kCoarseBlock)
+    k_mg_coarse(const __grid_constant__ CoarseLevels c, const int* done) {
+  if (stop(done)) return;
+  const int t0 = threadIdx.x;
+  auto sweep = [&](const MgLevelView& L, const float* xi, float* xo) {
+    for (int64_t r = t0; r < L.n; r += kCoarseBlock) {
+      int i, j, k;
+      row_ijk(L, r, i, j, k);
+      const float acc = lattice_row_value(L.op, i, j, k, xi);
+      xo[r] = fmaf(kOmega * L.dinv[r], L.b[r] - acc, xi[r]);
+    }
+    __syncthreads();
+  };
+  auto first = [&](const MgLevelView& L) {
+    for (int64_t r = t0; r < L.n; r += kCoarseBlock) L.x[r] = kOmega * L.dinv[r] * L.b[r];
+    __syncthreads();
+  };
+  // down
+  for (int l = 0; l < c.nl; ++l) {
+    const MgLevelView& L = c.L[l];
+    first(L);
+    if (l + 1 == c.nl) {  // coarsest: eight more sweeps, ending in x
+      for (int s = 0; s < kCoarseSweeps; s += 2) {
+        sweep(L, L.x, L.t);
+        sweep(L, L.t, L.x);
+      }
+      break;
+    }
+    sweep(L, L.x, L.t);
+    for (int64_t r = t0; r < L.n; r += kCoarseBlock) {  // residual into x
+      int i, j, k;
+      row_ijk(L, r, i, j, k);
+      L.x[r] = L.b[r] - lattice_row_value(L.op, i, j, k, L.t);
+    }
+    __syncthreads();
+    const MgLevelView& C = c.L[l + 1];
+    for (int64_t q = t0; q < C.n; q += kCoarseBlock) {  // restriction
+      int I, J, K;
+      row_ijk(C, q, I, J, K);
+      float s = 0.f;
+#pragma unroll
+      for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx) {
+            const float w = (dx ? 0.5f : 1.f) * (dy ? 0.5f : 1.f) * (dz ? 0.5f : 1.f);
+            const int64_t f =
+                (int64_t)(2 * I + 1 + dx) +
+                (int64_t)L.m0 * ((2 * J + 1 + dy) + (int64_t)L.m1 * (2 * K + 1 + dz));
+            s = fmaf(w, L.x[f], s);
+          }
+      C.b[q] = s;
+    }
+    __syncthreads();
+  }
+  // up: x = t + P x_c, then two sweeps back into x
+  for (int l = c.nl - 2; l >= 0; --l) {
+    const MgLevelView& L = c.L[l];
+    const MgLevelView& C = c.L[l + 1];
+    for (int64_t r = t0; r < L.n; r += kCoarseBlock) {
+      int i, j, k;
+      row_ijk(L, r, i, j, k);
+      L.x[r] = L.t[r] + prolong_value(i, j, k, C.m0, C.m1, C.m2, C.x);
+    }
+    __syncthreads();
+    sweep(L, L.x, L.t);
+    sweep(L, L.t, L.x);
   }
 }
 
@@ -219,6 +363,18 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
   const dim3 ga = L.op.grid(L.n);
   const bool coarsest = l + 1 == mg->lv.size();
   const int pre = coarsest ? kCoarseSweeps + 1 : kPreSweeps;
+  if (L.n <= kCoarseRows && mg->lv.size() - l <= (size_t)kMaxCoarse) {
+    // this level and all coarser ones in one block
+    CoarseLevels c{};
+    c.nl = (int)(mg->lv.size() - l);
+    for (int q = 0; q < c.nl; ++q) {
+      const LatticeMG::Level& Q = mg->lv[l + q];
+      c.L[q] = MgLevelView{Q.op, Q.m0, Q.m1, Q.m2, Q.n, Q.x, Q.b, Q.t, Q.dinv};
+    }
+    k_mg_coarse<<<1, kCoarseBlock, 0, ctx->stream>>>(c, done);
+    ctx->launches++;
+    return GFE_OK;
+  }
   float* cur = L.x;
   float* oth = L.t;
   // lattices too small for 4 blocks per SM march one k-plane per thread

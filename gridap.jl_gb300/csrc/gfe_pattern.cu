@@ -545,8 +545,9 @@ int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
   // general two-pass kernel.
   int64_t wmax = 0;
   bool single = false;
-  if (A->nrefs * A->cols_per_cell() > 0) {
-    GFE_TRY(A->refpos.reserve((size_t)A->nrefs * A->cols_per_cell()));
+  const int ndc = A->cols_per_cell();
+  if (A->nrefs * ndc > 0) {
+    GFE_TRY(A->refpos.reserve((size_t)A->nrefs * ndc));
     const int tries[2] = {32, maxw <= 64 ? 64 : 128};
     for (int t = 0; t < 2 && !single; ++t) {
       const int w = tries[t];

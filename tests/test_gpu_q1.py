@@ -208,6 +208,24 @@ def test_pattern_width_classes_match_oracle(gg, orc, nd, ncells, ncols, hub):
     assert lo < int(np.diff(rp).max()) <= hi
 
 
+@pytest.mark.parametrize("nd,n", [(8, 500), (5, 300), (3, 40)])
+def test_pattern_of_permuted_ids_matches_oracle(gg, orc, nd, n):
+    """Random cell ids with the sharing of a mesh (each row in exactly nd cells, distinct
+    within a cell, 10 % Dirichlet, no locality) give Gridap's pattern and values bit for
+    bit."""
+    rng = np.random.default_rng(200 + nd)
+    shifts = rng.choice(np.arange(1, n), nd - 1, replace=False)
+    base = np.stack([np.arange(n)] + [(np.arange(n) + s) % n for s in shifts], axis=1)
+    ids = (rng.permutation(n)[base] + 1).astype(np.int32)
+    ids[rng.random(ids.shape) < 0.1] *= -1
+    cm = rng.standard_normal((n, nd, nd))
+    csc = orc.assemble_csc(ids, ids, cm, n, n)
+    assem = gg.SparseMatrixAssembler(_Sized(n), _Sized(n))
+    A = gg.symbolic_loop_matrix(assem, (None, ids, ids))
+    gg.numeric_loop_matrix(A, assem, (cm, ids, ids))
+    _assert_csr_equals_csc(A, csc, n)
+
+
 @pytest.mark.parametrize("ndr,ndc,nrows,ncols", [(6, 3, 80, 40), (4, 9, 50, 300)])
 def test_rectangular_cell_blocks_match_oracle(gg, orc, ndr, ndc, nrows, ncols):
     """Off-diagonal block of a multi-field system: nd_rows row ids against nd_cols column

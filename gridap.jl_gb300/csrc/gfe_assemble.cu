@@ -58,6 +58,14 @@ struct CartesianDiffusionQ1 {
     if (FP32) return (double)((float)kap * (float)k);
     return kap * k;
   }
+  // acc + kappa Kref[li][lj] as one FP64 fused multiply-add
+  __device__ __forceinline__ double madd(const double* s, double kap, int li, int lj, int,
+                                         double acc) const {
+    const double k = s[li + lj * NV];
+    if (coef_kind == GFE_COEF_ONE) return acc + k;
+    if (FP32) return acc + (double)((float)kap * (float)k);
+    return fma(kap, k, acc);
+  }
   // node of local vertex 0 of a Cartesian cell and the node strides of y and z: the cell id
   // is split once in 32-bit arithmetic (cell ids are below 2^31), the other vertices follow
   // by offsets (64-bit division per vertex dominated the row gather's instruction count)

@@ -7,6 +7,8 @@
 // coalesced stores. Cell values come from a source functor with
 //   load_tables(smem), m(tables, cell, li, lj, nd), v(tables, cell, li)  and  ntab.
 #pragma once
+#include <type_traits>
+
 #include "gfe_internal.h"
 
 namespace gfe {
@@ -68,6 +70,22 @@ struct StoredCells {
 };
 
 
+// acc + m(...): a source may provide madd(tables, cell data, li, lj, nd, acc) that forms the
+// sum with one fused multiply-add (FP64 issue bounds the fused-integral gathers)
+template <class S, class = void>
+struct has_madd : std::false_type {};
+template <class S>
+struct has_madd<S, std::void_t<decltype(&S::madd)>> : std::true_type {};
+
+template <class Src, class CC>
+__device__ __forceinline__ double src_madd(const Src& src, const double* tab, const CC& cc,
+                                           int li, int lj, int nd, double acc) {
+  if constexpr (has_madd<Src>::value)
+    return src.madd(tab, cc, li, lj, nd, acc);
+  else
+    return acc + src.m(tab, cc, li, lj, nd);
+}
+
 // ---- the row-gather kernel ----------------------------------------------------------------
 template <int MAXW, int R, class Src, typename PosT>
 __global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
@@ -110,7 +128,7 @@ __global__ void __launch_bounds__(R) k_assemble_rows(RowArgs a, Src src) {
             raise_err(a.err, GFE_ERR_INVALID_ARGUMENT, r);
             return;
           }
-          acc[p * R + t] += src.m(tab, cc, li, lj, a.nd);
+          acc[p * R + t] = src_madd(src, tab, cc, li, lj, a.nd, acc[p * R + t]);
         };
         if (sizeof(PosT) == 1 && (ndc & 3) == 0) {
           // byte positions four at a time (the reference's row of the table is 4-aligned)
@@ -230,7 +248,7 @@ __global__ void __launch_bounds__(32 * kRowWarps)
           raise_err(a.err, GFE_ERR_INVALID_ARGUMENT, r);
           continue;
         }
-        acc[pp] += src.m(tab, cc, li, lj, a.nd);
+        acc[pp] = src_madd(src, tab, cc, li, lj, a.nd, acc[pp]);
       }
       __syncwarp();
     }

@@ -420,8 +420,9 @@ def run_gpu(args):
                          alg=44 * nfree, kt=r_mixed_kt["kt"][_lib.GFE_KT_VECTOR],
                          traffic=profile_traffic("fp32_vector")),
         "assembly": dict(kernel="k_assemble_rows (row-gather numeric loop, FP64 cell "
-                                "integrals fused)",
-                         alg=assembly_bytes(nnz, nfree, ncells), traffic=None,
+                                "integrals fused; FP64-pipe bound)",
+                         alg=assembly_bytes(nnz, nfree, ncells),
+                         traffic=profile_traffic("assembly"),
                          kt=r_mixed_kt["kt"][_lib.GFE_KT_ASSEMBLE]),
     }
     if isinstance(mixed, gg.FCGSolver):

@@ -233,8 +233,9 @@ def run_gpu(args):
     def step(ids, kap, f, x, solver, b):
         prep = problem(ids, kap, f)
         h = ctypes.c_void_p()
-        _lib.check(lib.gfe_symbolic_loop_matrix(ctx.handle, ncells, nd, _lib.ptr(ids),
-                                                _lib.ptr(ids), nfree, nfree, ctypes.byref(h)))
+        # the symbolic loop with the model in hand, as SparseMatrixAssembler(U, V) runs it
+        _lib.check(lib.gfe_symbolic_loop_matrix_problem(ctx.handle, ctypes.byref(prep.p),
+                                                        ctypes.byref(h)))
         try:
             _lib.check(lib.gfe_assemble_matrix_and_vector(ctx.handle, ctypes.byref(prep.p), h,
                                                           _lib.ptr(b)))

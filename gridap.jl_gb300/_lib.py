@@ -119,6 +119,7 @@ SIGNATURES = {
                                            C.c_int64, C.POINTER(C.c_void_p)]),
     "gfe_symbolic_loop_matrix_rect": (C.c_int, [_P, C.c_int64, C.c_int, C.c_int, _P, _P,
                                                 C.c_int64, C.c_int64, C.POINTER(C.c_void_p)]),
+    "gfe_symbolic_loop_matrix_problem": (C.c_int, [_P, _P, C.POINTER(C.c_void_p)]),
     "gfe_symbolic_loop_matrix_masked": (C.c_int, [_P, C.c_int64, C.c_int, C.c_int, _P, _P, _P,
                                                   C.c_int64, C.c_int64,
                                                   C.POINTER(C.c_void_p)]),

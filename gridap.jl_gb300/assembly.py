@@ -173,6 +173,16 @@ def symbolic_loop_matrix(assem: SparseMatrixAssembler, matdata) -> DeviceMatrix:
     return DeviceMatrix(h, assem.ctx)
 
 
+def symbolic_loop_problem(assem: SparseMatrixAssembler, prep) -> DeviceMatrix:
+    """The pattern of a prepared problem's cell ids, built with the model in hand
+    (gfe_symbolic_loop_matrix_problem: closed form for the interior numbering of Cartesian
+    Q1 grids, the general symbolic loop otherwise)."""
+    h = C.c_void_p()
+    _lib.check(_lib.load().gfe_symbolic_loop_matrix_problem(assem.ctx.handle, C.byref(prep.p),
+                                                            C.byref(h)))
+    return DeviceMatrix(h, assem.ctx)
+
+
 def numeric_loop_matrix(A: DeviceMatrix, assem: SparseMatrixAssembler, matdata) -> DeviceMatrix:
     """Adds cell matrices (ncells, nd, nd) [row, col] into A in cell order."""
     cellmats = matdata[0]
@@ -523,8 +533,7 @@ def assemble_matrix_and_vector(a, l, U, V, assem: SparseMatrixAssembler | None =
     prep.model = Vs.model
     A = None
     if a is not None:
-        ids = Vs.cell_dof_ids
-        A = symbolic_loop_matrix(assem, (None, ids, ids))
+        A = symbolic_loop_problem(assem, prep)
     b = None
     if l is not None:
         b = np.zeros(Vs.num_free_dofs()) if b_out is None else b_out

@@ -123,7 +123,8 @@ extern "C" int gfe_ctx_kernel_time(gfe_ctx* c, int kernel, double* total_ms, int
 static int symbolic_loop(gfe_ctx* ctx, int64_t ncells, int ndr, int ndc,
                          const int32_t* cell_rows, const int32_t* cell_cols,
                          const uint8_t* local_mask, int64_t nrows, int64_t ncols,
-                         gfe_matrix** out, const char* who) {
+                         gfe_matrix** out, const char* who,
+                         const gfe_problem* structured = nullptr) {
   gfe::NvtxRange nvtx_range(who);
   clear_error();
   if (!ctx || !out || ndr < 1 || ndc < 1 || ncells < 0 || nrows < 0 || ncols < 0 ||
@@ -166,7 +167,11 @@ static int symbolic_loop(gfe_ctx* ctx, int64_t ncells, int ndr, int ndc,
       A->has_lmask = true;
     }
   }
-  if (s == GFE_OK) s = build_pattern(ctx, A);
+  bool done = false;
+  if (s == GFE_OK && structured)
+    s = build_pattern_cartesian(ctx, A, structured->partition[0], structured->partition[1],
+                                structured->partition[2], &done);
+  if (s == GFE_OK && !done) s = build_pattern(ctx, A);
   if (s != GFE_OK) {
     delete A;
     return s;
@@ -188,6 +193,19 @@ extern "C" int gfe_symbolic_loop_matrix_rect(gfe_ctx* ctx, int64_t ncells, int n
                                              int64_t ncols, gfe_matrix** out) {
   return symbolic_loop(ctx, ncells, nd_rows, nd_cols, cell_rows, cell_cols, nullptr, nrows,
                        ncols, out, "gfe_symbolic_loop_matrix_rect");
+}
+
+extern "C" int gfe_symbolic_loop_matrix_problem(gfe_ctx* ctx, const gfe_problem* p,
+                                                gfe_matrix** out) {
+  if (!p || !p->cell_dof_ids || p->nd < 1)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_symbolic_loop_matrix_problem: bad problem");
+  // Q1 hexahedra of a Cartesian grid: the closed-form pattern when the ids are its interior
+  // numbering (checked on the device), otherwise the general symbolic loop
+  const bool cart = p->dim == 3 && p->reffe == GFE_REFFE_Q1 && p->ncomp == 1 && p->nd == 8 &&
+                    p->ncells == p->partition[0] * p->partition[1] * p->partition[2];
+  return symbolic_loop(ctx, p->ncells, p->nd, p->nd, p->cell_dof_ids, p->cell_dof_ids, nullptr,
+                       p->nfree, p->nfree, out, "gfe_symbolic_loop_matrix_problem",
+                       cart ? p : nullptr);
 }
 
 extern "C" int gfe_symbolic_loop_matrix_masked(gfe_ctx* ctx, int64_t ncells, int nd_rows,

@@ -214,6 +214,11 @@ int narrow_i64_to_i32(gfe_ctx* ctx, const int64_t* in, int32_t* out, int64_t n);
 // pattern (gfe_pattern.cu)
 int build_refs(gfe_ctx* ctx, gfe_matrix* A);
 int build_pattern(gfe_ctx* ctx, gfe_matrix* A);
+// The pattern of Q1 cells of an n0 x n1 x n2 Cartesian grid numbered by interior nodes, in
+// closed form after a device check of the ids; *done false (nothing changed) when the ids
+// are not that numbering.
+int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1, int64_t n2,
+                            bool* done);
 
 // assembly (gfe_assemble.cu)
 int assemble_cellmats(gfe_ctx* ctx, gfe_matrix* A, const double* d_cellmats);

@@ -598,3 +598,155 @@ int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
 }
 
 }  // namespace gfe
+
+namespace gfe {
+
+// ---- structured fast path: Q1 hexahedra of a Cartesian grid --------------------------------
+// When the cell ids are exactly the CLagrangian numbering of the interior nodes of an
+// n0 x n1 x n2 Cartesian grid (every boundary node Dirichlet, cells and interior nodes in
+// lexicographic order), the pattern the general path computes is known in closed form: row
+// r = interior node (i, j, k) references the 8 cells (i+cx, j+cy, k+cz) in ascending order
+// (local row (1-cx) + 2(1-cy) + 4(1-cz)) and its columns are the interior nodes among its 27
+// neighbours, in ascending order. The ids are checked on the device first; any mismatch
+// falls back to the general path, so the result is always the general path's, bit for bit.
+__global__ void k_cart_check(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols,
+                             int n0, int n1, int n2, int* bad) {
+  const int64_t ncells = (int64_t)n0 * n1 * n2;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncells;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t cu = (uint32_t)c, t = cu / (uint32_t)n0;
+    const int ci = (int)(cu - t * (uint32_t)n0);
+    const int ck = (int)(t / (uint32_t)n1), cj = (int)(t - (uint32_t)ck * (uint32_t)n1);
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const int i = ci + (a & 1), j = cj + ((a >> 1) & 1), k = ck + (a >> 2);
+      const bool interior = i > 0 && j > 0 && k > 0 && i < n0 && j < n1 && k < n2;
+      const int32_t want = 1 + (i - 1) + (n0 - 1) * ((j - 1) + (n1 - 1) * (k - 1));
+      const int32_t r = rows[c * 8 + a], q = cols[c * 8 + a];
+      ok = ok && r == q && (interior ? r == want : r < 0);
+    }
+    if (!ok) atomicExch(bad, 1);
+  }
+}
+
+__device__ __forceinline__ void cart_row(int64_t r, int m0, int m1, int& i, int& j, int& k) {
+  const uint32_t ru = (uint32_t)r, t = ru / (uint32_t)m0;
+  i = (int)(ru - t * (uint32_t)m0);
+  k = (int)(t / (uint32_t)m1);
+  j = (int)(t - (uint32_t)k * (uint32_t)m1);
+}
+
+__global__ void k_cart_widths(int64_t nrows, int m0, int m1, int m2, int64_t* __restrict__ w) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cart_row(r, m0, m1, i, j, k);
+    const int nx = 1 + (i > 0) + (i < m0 - 1), ny = 1 + (j > 0) + (j < m1 - 1),
+              nz = 1 + (k > 0) + (k < m2 - 1);
+    w[r] = nx * ny * nz;
+  }
+}
+
+// refs, ref_ptr, byte positions (8 per reference, one 8-byte store) and column ids
+__global__ void k_cart_fill(int64_t nrows, int n0, int n1, int m0, int m1, int m2,
+                            const int64_t* __restrict__ rowptr, int64_t* __restrict__ ref_ptr,
+                            int32_t* __restrict__ refs, uint64_t* __restrict__ refpos,
+                            int32_t* __restrict__ colval) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cart_row(r, m0, m1, i, j, k);
+    const int xlo = i > 0 ? -1 : 0, xhi = i < m0 - 1 ? 1 : 0;
+    const int ylo = j > 0 ? -1 : 0, yhi = j < m1 - 1 ? 1 : 0;
+    const int zlo = k > 0 ? -1 : 0, zhi = k < m2 - 1 ? 1 : 0;
+    const int nx = xhi - xlo + 1, ny = yhi - ylo + 1;
+    ref_ptr[r] = 8 * r;
+    if (r == nrows - 1) ref_ptr[nrows] = 8 * nrows;
+    int q = 0;
+    for (int cz = 0; cz < 2; ++cz)
+      for (int cy = 0; cy < 2; ++cy)
+        for (int cx = 0; cx < 2; ++cx, ++q) {
+          const int64_t cell =
+              (int64_t)(i + cx) + (int64_t)n0 * ((j + cy) + (int64_t)n1 * (k + cz));
+          const int li = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
+          refs[8 * r + q] = (int32_t)(cell * 8 + li);
+          uint64_t word = 0;
+#pragma unroll
+          for (int lj = 0; lj < 8; ++lj) {
+            const int dx = cx + (lj & 1) - 1, dy = cy + ((lj >> 1) & 1) - 1,
+                      dz = cz + (lj >> 2) - 1;
+            const bool in = dx >= xlo && dx <= xhi && dy >= ylo && dy <= yhi && dz >= zlo &&
+                            dz <= zhi;
+            const uint64_t pos =
+                in ? (uint64_t)((dz - zlo) * ny * nx + (dy - ylo) * nx + (dx - xlo)) : 0xFFull;
+            word |= pos << (8 * lj);
+          }
+          refpos[8 * r + q] = word;
+        }
+    int32_t* out = colval + rowptr[r];
+    int p = 0;
+    for (int dz = zlo; dz <= zhi; ++dz)
+      for (int dy = ylo; dy <= yhi; ++dy)
+        for (int dx = xlo; dx <= xhi; ++dx)
+          out[p++] = (int32_t)((i + dx) + m0 * ((j + dy) + m1 * (k + dz)));
+  }
+}
+
+int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1, int64_t n2,
+                            bool* done) {
+  *done = false;
+  const int64_t m0 = n0 - 1, m1 = n1 - 1, m2 = n2 - 1;
+  if (A->nd != 8 || A->cols_per_cell() != 8 || A->has_lmask || n0 < 2 || n1 < 2 || n2 < 2 ||
+      A->ncells != n0 * n1 * n2 || A->nrows != m0 * m1 * m2 || A->ncols != A->nrows ||
+      n0 * n1 * n2 * 8 > (int64_t)INT32_MAX)
+    return GFE_OK;
+  const int64_t nrows = A->nrows, ncells = A->ncells;
+  DevBuf flag(ctx);
+  GFE_TRY(flag.reserve(sizeof(int)));
+  GFE_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
+  k_cart_check<<<grid_for(ncells, 256, (int64_t)ctx->num_sms * 16), 256, 0, ctx->stream>>>(
+      A->cell_rows.as<int32_t>(), A->cell_cols.as<int32_t>(), (int)n0, (int)n1, (int)n2,
+      flag.as<int>());
+  ctx->launches++;
+  int bad = 1;
+  GFE_TRY(copy_out(ctx, &bad, flag.ptr, sizeof(int)));
+  if (bad) return GFE_OK;
+  DevBuf width(ctx), rowptr64(ctx);
+  GFE_TRY(width.reserve(sizeof(int64_t) * (nrows + 1)));
+  GFE_TRY(rowptr64.reserve(sizeof(int64_t) * (nrows + 1)));
+  const unsigned g = grid_for(nrows, 256, (int64_t)ctx->num_sms * 16);
+  k_cart_widths<<<g, 256, 0, ctx->stream>>>(nrows, (int)m0, (int)m1, (int)m2,
+                                            width.as<int64_t>());
+  ctx->launches++;
+  GFE_TRY(scan_exclusive_i64(ctx, width.as<int64_t>(), rowptr64.as<int64_t>(), nrows));
+  int64_t nnz = 0;
+  GFE_TRY(copy_out(ctx, &nnz, rowptr64.as<int64_t>() + nrows, sizeof(int64_t)));
+  if (nnz > (int64_t)INT32_MAX - 64)
+    return set_error(GFE_ERR_UNSUPPORTED, "symbolic_loop_matrix: nnz %lld exceeds int32",
+                     (long long)nnz);
+  A->nrefs = 8 * nrows;
+  A->nnz = nnz;
+  A->max_width = (int)((m0 < 3 ? m0 : 3) * (m1 < 3 ? m1 : 3) * (m2 < 3 ? m2 : 3));
+  A->pos_bytes = 1;
+  GFE_TRY(A->ref_ptr.reserve(sizeof(int64_t) * (nrows + 1)));
+  GFE_TRY(A->refs.reserve(sizeof(int32_t) * (size_t)(A->nrefs > 0 ? A->nrefs : 1)));
+  GFE_TRY(A->refpos.reserve((size_t)8 * (A->nrefs > 0 ? A->nrefs : 1)));
+  GFE_TRY(A->rowptr.reserve(sizeof(int32_t) * (nrows + 1)));
+  GFE_TRY(A->colval.reserve(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
+  GFE_TRY(A->val.reserve(sizeof(double) * (nnz > 0 ? nnz : 1)));
+  k_cart_fill<<<g, 256, 0, ctx->stream>>>(nrows, (int)n0, (int)n1, (int)m0, (int)m1, (int)m2,
+                                          rowptr64.as<int64_t>(), A->ref_ptr.as<int64_t>(),
+                                          A->refs.as<int32_t>(), A->refpos.as<uint64_t>(),
+                                          A->colval.as<int32_t>());
+  ctx->launches++;
+  GFE_TRY(narrow_i64_to_i32(ctx, rowptr64.as<int64_t>(), A->rowptr.as<int32_t>(), nrows + 1));
+  GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * (nnz > 0 ? nnz : 1),
+                               ctx->stream));
+  GFE_CUDA_TRY(cudaGetLastError());
+  A->plan_valid = false;
+  *done = true;
+  return GFE_OK;
+}
+
+}  // namespace gfe

@@ -258,6 +258,15 @@ typedef struct gfe_problem {
   double law_params[4];
 } gfe_problem;
 
+/* The symbolic loop of problem->cell_dof_ids (rows and columns, nfree x nfree), with what the
+ * assembler knows about the model: for Q1 hexahedra of a Cartesian grid (dim 3, partition)
+ * whose ids are the interior-node numbering (checked on the device) the pattern, row
+ * references and position table are written in closed form -- the same arrays, bit for bit,
+ * that gfe_symbolic_loop_matrix computes, which it falls back to for any other ids.
+ * Replaces FESpaces/SparseMatrixAssemblers.jl:174-210 with the assembler's spaces in hand
+ * (SparseMatrixAssembler(U, V) holds the FE spaces and their model). */
+int gfe_symbolic_loop_matrix_problem(gfe_ctx* ctx, const gfe_problem* problem, gfe_matrix** A);
+
 /* Integrates the recognised bilinear and linear forms over every cell and assembles them
  * into A (pattern from gfe_symbolic_loop_matrix over problem->cell_dof_ids) and b (nfree
  * entries, overwritten). A or b may be NULL to skip one. With problem->dirichlet_values the

@@ -252,6 +252,41 @@ def test_rectangular_cell_blocks_match_oracle(gg, orc, ndr, ndc, nrows, ncols):
     assert np.array_equal(nz, S.data)
 
 
+@pytest.mark.parametrize("part", [(2, 3, 4), (3, 3, 3), (5, 4, 6), (7, 2, 3), (9, 8, 10)])
+def test_cartesian_closed_form_pattern_equals_general(gg, part):
+    """The problem-aware symbolic loop writes the Cartesian Q1 pattern in closed form; its
+    CSR, row references and position table equal the general symbolic loop's: both
+    matrices take the same fused assembly and come out bit-identical."""
+    import ctypes
+    import importlib
+    lib_ = importlib.import_module(gg.__name__ + "._lib")
+    model = gg.CartesianDiscreteModel((0, 1, 0, 1, 0, 1), part)
+    V = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    dO = gg.Measure(gg.Triangulation(model), 2)
+    rng = np.random.default_rng(sum(part))
+    kap = rng.uniform(0.5, 2.0, model.num_cells())
+    fn = gg.NodalField(rng.standard_normal(model.num_nodes()))
+    assem = gg.SparseMatrixAssembler(V, V)
+    prep = gg.prepare_problem(V, V, dO, gg.CellField(kap), fn)
+    ids = V.cell_dof_ids
+    A1 = gg.symbolic_loop_matrix(assem, (None, ids, ids))       # general
+    h = ctypes.c_void_p()
+    lib_.check(lib_.load().gfe_symbolic_loop_matrix_problem(assem.ctx.handle,
+                                                           ctypes.byref(prep.p), ctypes.byref(h)))
+    A2 = gg.DeviceMatrix(h, assem.ctx)                          # closed form
+    n = V.num_free_dofs()
+    outs = []
+    for A in (A1, A2):
+        b = np.zeros(n)
+        lib_.check(lib_.load().gfe_assemble_matrix_and_vector(
+            assem.ctx.handle, ctypes.byref(prep.p), A.handle, lib_.ptr(b)))
+        outs.append((A.export_csr(0), b))
+    (r1, c1, v1), b1 = outs[0]
+    (r2, c2, v2), b2 = outs[1]
+    assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
+    assert np.array_equal(v1, v2) and np.array_equal(b1, b2)
+
+
 def test_determinism(gg):
     rng = np.random.default_rng(9)
     dom, part = (0, 1, 0, 1, 0, 1), (12, 10, 9)

@@ -648,48 +648,59 @@ __global__ void k_cart_widths(int64_t nrows, int m0, int m1, int m2, int64_t* __
   }
 }
 
-// refs, ref_ptr, byte positions (8 per reference, one 8-byte store) and column ids
-__global__ void k_cart_fill(int64_t nrows, int n0, int n1, int m0, int m1, int m2,
-                            const int64_t* __restrict__ rowptr, int64_t* __restrict__ ref_ptr,
-                            int32_t* __restrict__ refs, uint64_t* __restrict__ refpos,
-                            int32_t* __restrict__ colval) {
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows;
-       r += (int64_t)gridDim.x * blockDim.x) {
+// refs, ref_ptr and byte positions: thread per (row, reference), so that consecutive threads
+// store consecutive references and 8-byte position words
+__global__ void k_cart_refs(int64_t nrows, int n0, int n1, int m0, int m1, int m2,
+                            int64_t* __restrict__ ref_ptr, int32_t* __restrict__ refs,
+                            uint64_t* __restrict__ refpos) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 8 * nrows;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t >> 3;
+    const int q = (int)(t & 7), cx = q & 1, cy = (q >> 1) & 1, cz = q >> 2;
     int i, j, k;
     cart_row(r, m0, m1, i, j, k);
     const int xlo = i > 0 ? -1 : 0, xhi = i < m0 - 1 ? 1 : 0;
     const int ylo = j > 0 ? -1 : 0, yhi = j < m1 - 1 ? 1 : 0;
     const int zlo = k > 0 ? -1 : 0, zhi = k < m2 - 1 ? 1 : 0;
     const int nx = xhi - xlo + 1, ny = yhi - ylo + 1;
-    ref_ptr[r] = 8 * r;
-    if (r == nrows - 1) ref_ptr[nrows] = 8 * nrows;
-    int q = 0;
-    for (int cz = 0; cz < 2; ++cz)
-      for (int cy = 0; cy < 2; ++cy)
-        for (int cx = 0; cx < 2; ++cx, ++q) {
-          const int64_t cell =
-              (int64_t)(i + cx) + (int64_t)n0 * ((j + cy) + (int64_t)n1 * (k + cz));
-          const int li = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
-          refs[8 * r + q] = (int32_t)(cell * 8 + li);
-          uint64_t word = 0;
+    if (q == 0) {
+      ref_ptr[r] = 8 * r;
+      if (r == nrows - 1) ref_ptr[nrows] = 8 * nrows;
+    }
+    const int64_t cell =
+        (int64_t)(i + cx) + (int64_t)n0 * ((j + cy) + (int64_t)n1 * (k + cz));
+    refs[t] = (int32_t)(cell * 8 + (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz));
+    uint64_t word = 0;
 #pragma unroll
-          for (int lj = 0; lj < 8; ++lj) {
-            const int dx = cx + (lj & 1) - 1, dy = cy + ((lj >> 1) & 1) - 1,
-                      dz = cz + (lj >> 2) - 1;
-            const bool in = dx >= xlo && dx <= xhi && dy >= ylo && dy <= yhi && dz >= zlo &&
-                            dz <= zhi;
-            const uint64_t pos =
-                in ? (uint64_t)((dz - zlo) * ny * nx + (dy - ylo) * nx + (dx - xlo)) : 0xFFull;
-            word |= pos << (8 * lj);
-          }
-          refpos[8 * r + q] = word;
-        }
-    int32_t* out = colval + rowptr[r];
-    int p = 0;
-    for (int dz = zlo; dz <= zhi; ++dz)
-      for (int dy = ylo; dy <= yhi; ++dy)
-        for (int dx = xlo; dx <= xhi; ++dx)
-          out[p++] = (int32_t)((i + dx) + m0 * ((j + dy) + m1 * (k + dz)));
+    for (int lj = 0; lj < 8; ++lj) {
+      const int dx = cx + (lj & 1) - 1, dy = cy + ((lj >> 1) & 1) - 1, dz = cz + (lj >> 2) - 1;
+      const bool in =
+          dx >= xlo && dx <= xhi && dy >= ylo && dy <= yhi && dz >= zlo && dz <= zhi;
+      const uint64_t pos =
+          in ? (uint64_t)((dz - zlo) * ny * nx + (dy - ylo) * nx + (dx - xlo)) : 0xFFull;
+      word |= pos << (8 * lj);
+    }
+    refpos[t] = word;
+  }
+}
+
+// colval: thread per (row, column slot), the slots of a row consecutive
+__global__ void k_cart_cols(int64_t nrows, int m0, int m1, int m2,
+                            const int64_t* __restrict__ rowptr, int32_t* __restrict__ colval) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 27 * nrows;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / 27;
+    const int sl = (int)(t - r * 27);
+    int i, j, k;
+    cart_row(r, m0, m1, i, j, k);
+    const int xlo = i > 0 ? -1 : 0, xhi = i < m0 - 1 ? 1 : 0;
+    const int ylo = j > 0 ? -1 : 0, yhi = j < m1 - 1 ? 1 : 0;
+    const int zlo = k > 0 ? -1 : 0, zhi = k < m2 - 1 ? 1 : 0;
+    const int nx = xhi - xlo + 1, ny = yhi - ylo + 1, nz = zhi - zlo + 1;
+    if (sl >= nx * ny * nz) continue;
+    const int px = sl % nx, py = (sl / nx) % ny, pz = sl / (nx * ny);
+    colval[rowptr[r] + sl] =
+        (int32_t)((i + xlo + px) + m0 * ((j + ylo + py) + m1 * (k + zlo + pz)));
   }
 }
 
@@ -735,11 +746,12 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
   GFE_TRY(A->rowptr.reserve(sizeof(int32_t) * (nrows + 1)));
   GFE_TRY(A->colval.reserve(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
   GFE_TRY(A->val.reserve(sizeof(double) * (nnz > 0 ? nnz : 1)));
-  k_cart_fill<<<g, 256, 0, ctx->stream>>>(nrows, (int)n0, (int)n1, (int)m0, (int)m1, (int)m2,
-                                          rowptr64.as<int64_t>(), A->ref_ptr.as<int64_t>(),
-                                          A->refs.as<int32_t>(), A->refpos.as<uint64_t>(),
-                                          A->colval.as<int32_t>());
-  ctx->launches++;
+  k_cart_refs<<<grid_for(8 * nrows, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
+      nrows, (int)n0, (int)n1, (int)m0, (int)m1, (int)m2, A->ref_ptr.as<int64_t>(),
+      A->refs.as<int32_t>(), A->refpos.as<uint64_t>());
+  k_cart_cols<<<grid_for(27 * nrows, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
+      nrows, (int)m0, (int)m1, (int)m2, rowptr64.as<int64_t>(), A->colval.as<int32_t>());
+  ctx->launches += 2;
   GFE_TRY(narrow_i64_to_i32(ctx, rowptr64.as<int64_t>(), A->rowptr.as<int32_t>(), nrows + 1));
   GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * (nnz > 0 ? nnz : 1),
                                ctx->stream));

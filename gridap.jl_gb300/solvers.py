@@ -90,7 +90,7 @@ class FCGSolver(LinearSolver):
 
     def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, pc=None,
                  inner_rtol: float = 0.0, check_every: int = 0, initial_guess: bool = False):
-        # inner_rtol 0: the library's reliable-update threshold (0.1; 1e-3 with pc="mg")
+        # inner_rtol 0: the library's reliable-update threshold (0.1; 1e-4 with pc="mg")
         super().__init__(rtol, maxiter, "jacobi", inner_rtol, check_every, initial_guess)
         if isinstance(pc, str):
             if pc != "mg":

@@ -424,7 +424,7 @@ typedef struct gfe_solver_opts {
   int32_t maxiter;      /* total inner iterations allowed */
   double inner_rtol;    /* IR_CG: relative reduction per refinement step; MIXED_CG: residual
                            reduction between reliable updates (default 0.01); FCG: the same
-                           (default 0.1, 1e-3 with GFE_PC_MG) */
+                           (default 0.1, 1e-4 with GFE_PC_MG) */
   int32_t check_every;  /* iterations between host convergence checks (0 = default) */
   int32_t initial_guess;/* 0: start from x = 0; 1: start from the values in x (a restart from a
                            saved solution): the solver runs on A d = b - A x0 with its tolerance

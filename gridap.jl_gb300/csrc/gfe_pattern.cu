@@ -684,23 +684,24 @@ __global__ void k_cart_refs(int64_t nrows, int n0, int n1, int m0, int m1, int m
   }
 }
 
-// colval: thread per (row, column slot), the slots of a row consecutive
+// colval: a warp per row, lane = column slot (27 of 32 lanes), the row's slots consecutive
 __global__ void k_cart_cols(int64_t nrows, int m0, int m1, int m2,
                             const int64_t* __restrict__ rowptr, int32_t* __restrict__ colval) {
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 27 * nrows;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = t / 27;
-    const int sl = (int)(t - r * 27);
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrows;
+       r += nwarps) {
     int i, j, k;
     cart_row(r, m0, m1, i, j, k);
     const int xlo = i > 0 ? -1 : 0, xhi = i < m0 - 1 ? 1 : 0;
     const int ylo = j > 0 ? -1 : 0, yhi = j < m1 - 1 ? 1 : 0;
     const int zlo = k > 0 ? -1 : 0, zhi = k < m2 - 1 ? 1 : 0;
     const int nx = xhi - xlo + 1, ny = yhi - ylo + 1, nz = zhi - zlo + 1;
-    if (sl >= nx * ny * nz) continue;
-    const int px = sl % nx, py = (sl / nx) % ny, pz = sl / (nx * ny);
-    colval[rowptr[r] + sl] =
-        (int32_t)((i + xlo + px) + m0 * ((j + ylo + py) + m1 * (k + zlo + pz)));
+    if (lane < nx * ny * nz) {
+      const int px = lane % nx, py = (lane / nx) % ny, pz = lane / (nx * ny);
+      colval[rowptr[r] + lane] =
+          (int32_t)((i + xlo + px) + m0 * ((j + ylo + py) + m1 * (k + zlo + pz)));
+    }
   }
 }
 
@@ -749,7 +750,7 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
   k_cart_refs<<<grid_for(8 * nrows, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
       nrows, (int)n0, (int)n1, (int)m0, (int)m1, (int)m2, A->ref_ptr.as<int64_t>(),
       A->refs.as<int32_t>(), A->refpos.as<uint64_t>());
-  k_cart_cols<<<grid_for(27 * nrows, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
+  k_cart_cols<<<grid_for(32 * nrows, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
       nrows, (int)m0, (int)m1, (int)m2, rowptr64.as<int64_t>(), A->colval.as<int32_t>());
   ctx->launches += 2;
   GFE_TRY(narrow_i64_to_i32(ctx, rowptr64.as<int64_t>(), A->rowptr.as<int32_t>(), nrows + 1));

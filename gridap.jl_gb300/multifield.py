@@ -302,8 +302,8 @@ class _MfContext:
                 T.cell_coef = _lib.ptr(t.cell_coef)
             if t.data is not None:
                 if xq is None:
-                    X0 = coords[cells - 1]  # (ncells, 2^D, D)
-                    xq = np.einsum("qa,cad->cqd", phi1, X0).reshape(-1, D)
+                    X0 = coords[cells - 1].transpose(0, 2, 1)  # (ncells, D, 2^D)
+                    xq = np.ascontiguousarray((X0 @ phi1.T).transpose(0, 2, 1)).reshape(-1, D)
                 vals = _eval_points(t.data, xq)
                 self.keep.append(vals)
                 T.qdata, T.qdata_ncomp = _lib.ptr(vals), vals.shape[1]

@@ -20,7 +20,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .celldata import MOP_DIV, MOP_GRAD, MOP_VALUE, classify_multifield
+from .celldata import classify_multifield
 from .fespaces import FEFunction, TrialFESpace, _space, ncube_node_refs
 
 

@@ -9,7 +9,7 @@
 //   1. refs:   for every row r, the flattened positions e = cell*nd + li with
 //              cell_rows[e] == r+1, in ascending order (so cells in ascending order);
 //   2. widths: thread per row, the union of the positive column ids of the cells in its
-//              ref list, kept sorted and unique in shared memory (rows of up to 128
+//              ref list, kept sorted and unique in shared memory (rows of up to 512
 //              columns; wider rows in local memory); the same pass stores each reference's
 //              column positions in the row;
 //   3. scan of widths -> rowptr; colval scattered from those positions (wider rows: a
@@ -261,15 +261,15 @@ __global__ void k_row_pattern(int64_t nrows, int ndr, int nd,
 // width MAXW+1 (its positions are then garbage); the host then takes the general two-pass
 // kernel above. (Staging the positions in shared memory for coalesced stores was measured
 // slower: the extra shared memory halves the resident blocks of this issue-bound kernel.)
-template <int MAXW, int BLOCK>
+template <int MAXW, int BLOCK, typename PosT>
 __global__ void __launch_bounds__(BLOCK)
     k_row_width_pos(int64_t nrows, int ndr, int ndc, const int64_t* __restrict__ ref_ptr,
                     const uint8_t* __restrict__ lmask, const int32_t* __restrict__ refs,
                     const int32_t* __restrict__ cell_cols,
-                    int64_t ncols, int64_t* __restrict__ width, uint8_t* __restrict__ refpos,
+                    int64_t ncols, int64_t* __restrict__ width, PosT* __restrict__ refpos,
                     DevError* err) {
-  static_assert(MAXW <= 255, "byte positions");
-  __shared__ int32_t list[MAXW * BLOCK];
+  static_assert(MAXW <= (int)(PosT)~(PosT)0, "positions fit the position type");
+  extern __shared__ int32_t list[];  // MAXW * BLOCK entries
   const int64_t r = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
   int32_t* L = list + threadIdx.x;
   if (r >= nrows) return;
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(BLOCK)
       }
     }
     width[r] = overflow ? MAXW + 1 : n;
-    const bool packed = (ndc & 3) == 0;
+    const bool packed = sizeof(PosT) == 1 && (ndc & 3) == 0;
     for (int64_t q = q0; q < q1 && !overflow; ++q) {
       const int64_t cell = refs[q] / ndr;
       const int32_t* cc = cell_cols + cell * ndc;
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(BLOCK)
       uint32_t word = 0;
       for (int lj = 0; lj < ndc; ++lj) {
         const int32_t c = cc[lj] - 1;
-        uint32_t pos = 0xFFu;
+        uint32_t pos = (PosT)~(PosT)0;
         if (c >= 0 && c < ncols && !(km && !km[lj * ndr])) {
           int lo = 0, hi = n;
           while (lo < hi) {
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(BLOCK)
             word = 0;
           }
         } else {
-          refpos[q * ndc + lj] = (uint8_t)pos;
+          refpos[q * ndc + lj] = (PosT)pos;
         }
       }
     }
@@ -348,11 +348,11 @@ __global__ void __launch_bounds__(BLOCK)
 // of the row is hit at least once (each unique column came from some reference), and every
 // write to a slot carries the same column id. The block's rows form one contiguous colval
 // range: it is put together in shared memory, then stored coalesced.
-template <int BLOCK>
+template <int BLOCK, typename PosT>
 __global__ void __launch_bounds__(BLOCK)
     k_scatter_cols(int64_t nrows, int ndr, int ndc, const int64_t* __restrict__ ref_ptr,
                    const int32_t* __restrict__ refs, const int32_t* __restrict__ cell_cols,
-                   const uint8_t* __restrict__ refpos, const int64_t* __restrict__ rowptr,
+                   const PosT* __restrict__ refpos, const int64_t* __restrict__ rowptr,
                    int32_t* __restrict__ colval) {
   extern __shared__ int32_t stage_cols[];
   const int64_t r0 = (int64_t)blockIdx.x * BLOCK;
@@ -363,8 +363,8 @@ __global__ void __launch_bounds__(BLOCK)
     int32_t* row = stage_cols + (rowptr[r] - base);
     for (int64_t q = ref_ptr[r]; q < ref_ptr[r + 1]; ++q) {
       const int32_t* cc = cell_cols + (int64_t)(refs[q] / ndr) * ndc;
-      const uint8_t* pp = refpos + q * ndc;
-      if ((ndc & 3) == 0) {
+      const PosT* pp = refpos + q * ndc;
+      if (sizeof(PosT) == 1 && (ndc & 3) == 0) {
         for (int w4 = 0; w4 < (ndc >> 2); ++w4) {
           const uint32_t word = reinterpret_cast<const uint32_t*>(pp)[w4];
 #pragma unroll
@@ -375,8 +375,8 @@ __global__ void __launch_bounds__(BLOCK)
         }
       } else {
         for (int lj = 0; lj < ndc; ++lj) {
-          const uint8_t pos = pp[lj];
-          if (pos != 0xFF) row[pos] = cc[lj] - 1;
+          const PosT pos = pp[lj];
+          if (pos != (PosT)~(PosT)0) row[pos] = cc[lj] - 1;
         }
       }
     }
@@ -419,32 +419,45 @@ static void row_pattern(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cell_cols, b
     launch_row_pattern<512>(ctx, A, cell_cols, write, width, rowptr64);
 }
 
-// Widths and positions with the shared-memory list of MAXW columns.
-template <int MAXW, int BLOCK>
+// Widths and positions with the shared-memory list of MAXW columns (16-bit positions for
+// lists of more than 255).
+template <int MAXW, int BLOCK, typename PosT>
 static int launch_width_pos(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cols, int64_t* width) {
   const uint8_t* lm = A->has_lmask ? A->lmask.as<uint8_t>() : nullptr;
-  k_row_width_pos<MAXW, BLOCK><<<grid_for(A->nrows, BLOCK), BLOCK, 0, ctx->stream>>>(
+  const size_t smem = sizeof(int32_t) * (size_t)MAXW * BLOCK;
+  if (smem > 48 * 1024)
+    GFE_CUDA_TRY(cudaFuncSetAttribute(k_row_width_pos<MAXW, BLOCK, PosT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_row_width_pos<MAXW, BLOCK, PosT><<<grid_for(A->nrows, BLOCK), BLOCK, smem, ctx->stream>>>(
       A->nrows, A->nd, A->cols_per_cell(), A->ref_ptr.as<int64_t>(), lm, A->refs.as<int32_t>(),
-      cols, A->ncols, width, A->refpos.as<uint8_t>(), ctx->d_err);
+      cols, A->ncols, width, A->refpos.as<PosT>(), ctx->d_err);
   ctx->launches++;
   GFE_CUDA_TRY(cudaGetLastError());
   return GFE_OK;
 }
 
-// colval from the positions, a block of 128 rows (at most 128 columns each) at a time
-static int scatter_cols(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cols, int64_t wmax,
-                        const int64_t* rowptr64) {
-  constexpr int kBlock = 128;
-  const size_t smem = sizeof(int32_t) * kBlock * (size_t)(wmax > 0 ? wmax : 1);
+// colval from the positions: blocks of rows whose colval range (rows x widest row) fits in
+// shared memory, assembled there and stored coalesced
+template <int ROWS, typename PosT>
+static int scatter_cols_rows(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cols, int64_t wmax,
+                             const int64_t* rowptr64) {
+  const size_t smem = sizeof(int32_t) * ROWS * (size_t)(wmax > 0 ? wmax : 1);
   if (smem > 48 * 1024)
-    GFE_CUDA_TRY(cudaFuncSetAttribute(k_scatter_cols<kBlock>,
+    GFE_CUDA_TRY(cudaFuncSetAttribute(k_scatter_cols<ROWS, PosT>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_scatter_cols<kBlock><<<grid_for(A->nrows, kBlock), kBlock, smem, ctx->stream>>>(
+  k_scatter_cols<ROWS, PosT><<<grid_for(A->nrows, ROWS), ROWS, smem, ctx->stream>>>(
       A->nrows, A->nd, A->cols_per_cell(), A->ref_ptr.as<int64_t>(), A->refs.as<int32_t>(),
-      cols, A->refpos.as<uint8_t>(), rowptr64, A->colval.as<int32_t>());
+      cols, A->refpos.as<PosT>(), rowptr64, A->colval.as<int32_t>());
   ctx->launches++;
   GFE_CUDA_TRY(cudaGetLastError());
   return GFE_OK;
+}
+
+static int scatter_cols(gfe_ctx* ctx, gfe_matrix* A, const int32_t* cols, int64_t wmax,
+                        const int64_t* rowptr64) {
+  if (A->pos_bytes == 2) return scatter_cols_rows<64, uint16_t>(ctx, A, cols, wmax, rowptr64);
+  if (wmax <= 128) return scatter_cols_rows<128, uint8_t>(ctx, A, cols, wmax, rowptr64);
+  return scatter_cols_rows<64, uint8_t>(ctx, A, cols, wmax, rowptr64);
 }
 
 __global__ void k_max_i64(const int64_t* __restrict__ v, int64_t n, unsigned long long* out) {
@@ -541,26 +554,34 @@ int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
     return copy_out(ctx, wmax, dwmax.ptr, sizeof(int64_t));
   };
   // Single pass with the row list in shared memory: a 32-column list first (enough for
-  // every Q1 mesh), then one sized by the bound (at most 128); rows wider than that take the
-  // general two-pass kernel.
+  // every Q1 mesh), then 64 or 128 columns, then (bound above 128) 255 columns with byte
+  // positions or 512 with 16-bit positions; rows wider than that take the general two-pass
+  // kernel.
   int64_t wmax = 0;
   bool single = false;
+  int single_pos = 1;
   const int ndc = A->cols_per_cell();
   if (A->nrefs * ndc > 0) {
-    GFE_TRY(A->refpos.reserve((size_t)A->nrefs * ndc));
-    const int tries[2] = {32, maxw <= 64 ? 64 : 128};
-    for (int t = 0; t < 2 && !single; ++t) {
+    const int tries[3] = {32, maxw <= 64 ? 64 : 128, maxw <= 255 ? 255 : 512};
+    const int ntries = maxw <= 32 ? 1 : (maxw <= 128 ? 2 : 3);
+    for (int t = 0; t < ntries && !single; ++t) {
       const int w = tries[t];
-      if (t == 1 && maxw <= 32) break;
+      const int pb = w > 255 ? 2 : 1;
+      GFE_TRY(A->refpos.reserve((size_t)pb * A->nrefs * ndc));
       if (w == 32)
-        GFE_TRY((launch_width_pos<32, 128>(ctx, A, cols, width.as<int64_t>())));
+        GFE_TRY((launch_width_pos<32, 128, uint8_t>(ctx, A, cols, width.as<int64_t>())));
       else if (w == 64)
-        GFE_TRY((launch_width_pos<64, 128>(ctx, A, cols, width.as<int64_t>())));
+        GFE_TRY((launch_width_pos<64, 128, uint8_t>(ctx, A, cols, width.as<int64_t>())));
+      else if (w == 128)
+        GFE_TRY((launch_width_pos<128, 64, uint8_t>(ctx, A, cols, width.as<int64_t>())));
+      else if (w == 255)
+        GFE_TRY((launch_width_pos<255, 64, uint8_t>(ctx, A, cols, width.as<int64_t>())));
       else
-        GFE_TRY((launch_width_pos<128, 64>(ctx, A, cols, width.as<int64_t>())));
+        GFE_TRY((launch_width_pos<512, 32, uint16_t>(ctx, A, cols, width.as<int64_t>())));
       GFE_TRY(check_device_error(ctx, "symbolic_loop_matrix (column ids)"));
       GFE_TRY(max_width(&wmax));
       single = wmax <= w;
+      single_pos = pb;
     }
   }
   if (!single) {
@@ -573,7 +594,7 @@ int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
   int64_t nnz = 0;
   GFE_TRY(copy_out(ctx, &nnz, rowptr64.as<int64_t>() + nrows, sizeof(int64_t)));
   A->max_width = (int)wmax;
-  A->pos_bytes = wmax <= 255 ? 1 : 2;
+  A->pos_bytes = single ? single_pos : (wmax <= 255 ? 1 : 2);
   if (nnz > (int64_t)INT32_MAX - 64)
     return set_error(GFE_ERR_UNSUPPORTED, "symbolic_loop_matrix: nnz %lld exceeds int32",
                      (long long)nnz);

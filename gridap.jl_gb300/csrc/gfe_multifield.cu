@@ -201,10 +201,22 @@ __global__ void __launch_bounds__(kMfBlock)
       for (int k = 0; k < a.nterms; ++k)
         if (a.t[k].test_field == tf && a.t[k].trial_field == uf) terms |= 1u << k;
       double acc = 0.0;
+      const MfField& TF = a.f[tf];
+      const MfField& UF = a.f[uf];
+      const bool tvec = TF.ncomp > 1, uvec = UF.ncomp > 1;
+      // value.value and grad:grad of two vector fields couple equal components only: an
+      // entry whose terms are all of that kind with tc != uc is an exact zero, skip its loop
+      if (tvec && uvec && tc != uc) {
+        unsigned live = 0u;
+        for (unsigned m = terms; m; m &= m - 1) {
+          const MfTerm& T = a.t[__ffs(m) - 1];
+          const bool per_comp = T.test_op == T.trial_op &&
+                                (T.test_op == GFE_MOP_VALUE || T.test_op == GFE_MOP_GRAD);
+          if (!per_comp) live |= m & (~m + 1u);
+        }
+        terms = live;
+      }
       if (terms) {
-        const MfField& TF = a.f[tf];
-        const MfField& UF = a.f[uf];
-        const bool tvec = TF.ncomp > 1, uvec = UF.ncomp > 1;
         for (int q = 0; q < a.nq; ++q) {
           const double tphi = TF.shapes[q * TF.nnodes + tn];
           const double uphi = UF.shapes[q * UF.nnodes + un];

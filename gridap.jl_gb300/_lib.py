@@ -23,6 +23,7 @@ GFE_ERR_ROW_TOO_WIDE = 5
 GFE_ERR_TIMEOUT = 6
 GFE_ERR_UNSUPPORTED = 7
 GFE_ERR_NONFINITE = 8
+GFE_ERR_NOT_CONVERGED = 9
 
 GFE_REFFE_Q1, GFE_REFFE_Q2 = 1, 2
 GFE_GEOM_CARTESIAN, GFE_GEOM_NODAL = 0, 1
@@ -109,6 +110,7 @@ SIGNATURES = {
     "gfe_ctx_synchronize": (C.c_int, [_P]),
     "gfe_ctx_kernel_launches": (C.c_int, [_P, _I64P]),
     "gfe_ctx_set_timing": (C.c_int, [_P, C.c_int]),
+    "gfe_ctx_set_wait_limit": (C.c_int, [_P, C.c_uint64]),
     "gfe_ctx_kernel_time": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), _I64P]),
     "gfe_cartesian_model": (C.c_int, [C.c_int, _P, _P, _P, _P, _P]),
     "gfe_clagrangian_dofs": (C.c_int, [C.c_int64, _P, C.c_int, _P, C.c_int64, C.c_int, _P, _P,

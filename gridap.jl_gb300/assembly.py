@@ -62,6 +62,11 @@ class Context:
     def set_timing(self, enable: bool) -> None:
         _lib.check(_lib.load().gfe_ctx_set_timing(self.handle, int(enable)))
 
+    def set_wait_limit(self, first_wait_ns: int) -> None:
+        """Limit of the first bounded barrier wait in the lattice SpMV (0: give up at once, a
+        switch for tests of the timeout path; default 1 s)."""
+        _lib.check(_lib.load().gfe_ctx_set_wait_limit(self.handle, int(first_wait_ns)))
+
     def kernel_time(self, kind: int) -> tuple[float, int]:
         """(total milliseconds, launches) of a kernel class since timing was enabled."""
         ms, n = C.c_double(), C.c_int64()

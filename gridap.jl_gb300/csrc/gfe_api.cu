@@ -108,6 +108,13 @@ extern "C" int gfe_ctx_set_timing(gfe_ctx* c, int enable) {
   return GFE_OK;
 }
 
+extern "C" int gfe_ctx_set_wait_limit(gfe_ctx* c, uint64_t first_wait_ns) {
+  clear_error();
+  if (!c) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_ctx_set_wait_limit: NULL");
+  c->first_wait_ns = (unsigned long long)first_wait_ns;
+  return GFE_OK;
+}
+
 extern "C" int gfe_ctx_kernel_time(gfe_ctx* c, int kernel, double* total_ms, int64_t* launches) {
   clear_error();
   if (!c || kernel < 0 || kernel >= 8 || !total_ms || !launches)

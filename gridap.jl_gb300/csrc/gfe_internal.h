@@ -118,6 +118,9 @@ struct gfe_ctx {
   // CUDA graph of one chunk of CG iterations, reused while its launch parameters match
   cudaGraphExec_t cg_exec = nullptr;
   uint64_t cg_key = 0;
+  // limit of the first wait of the bounded mbarrier waits in the lattice SpMV (ns); 0 makes
+  // that wait give up at once (gfe_ctx_set_wait_limit, for tests of the timeout path)
+  unsigned long long first_wait_ns = 1000000000ull;
 };
 
 struct gfe_matrix {

@@ -34,6 +34,7 @@ struct State {
   int iter, done, converged, maxit;
   unsigned ticket[4];
   int bad_index;  // set when rowptr/colval fail validation
+  int nonfinite;  // a reduction (r.z, r.r, p.q) came out NaN or Inf
 };
 
 // layout of the scratch array, in doubles: r | p | q | dinv | partials | state
@@ -154,6 +155,44 @@ __global__ void k_init(int64_t n, const int32_t* __restrict__ rowptr,
     v.S->maxit = maxit;
     v.S->converged = tot[1] == 0.0;
     v.S->done = tot[1] == 0.0;
+    if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+      v.S->nonfinite = 1;
+      v.S->done = 1;
+    }
+  }
+}
+
+// Restart from the current x once the recursively updated residual met the tolerance but the
+// true one did not: r = b - A x, p = D^-1 r, r.z, with the iteration count kept.
+__global__ void k_restart(int64_t n, const int32_t* __restrict__ rowptr,
+                          const int32_t* __restrict__ col, const double* __restrict__ val,
+                          const double* __restrict__ b, const double* __restrict__ x, Views v) {
+  __shared__ double sh[kBlock / 32];
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double ri = b[i] - csr_row(i, n, rowptr, col, val, x);
+    v.r[i] = ri;
+    v.p[i] = v.dinv[i] * ri;
+    rz += ri * (v.dinv[i] * ri);
+    rr += ri * ri;
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    v.partials[2 * blockIdx.x] = rz;
+    v.partials[2 * blockIdx.x + 1] = rr;
+  }
+  double tot[2];
+  if (last_block<2>(&v.S->ticket[1], v.partials, tot, sh) && threadIdx.x == 0) {
+    v.S->rz = tot[0];
+    v.S->rr = tot[1];
+    v.S->converged = 0;
+    v.S->done = 0;
+    if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+      v.S->nonfinite = 1;
+      v.S->done = 1;
+    }
   }
 }
 
@@ -172,8 +211,15 @@ __global__ void k_spmv_dot(int64_t n, const int32_t* __restrict__ rowptr,
   d = block_sum(d, sh);
   if (threadIdx.x == 0) v.partials[blockIdx.x] = d;
   double tot[1];
-  if (last_block<1>(&v.S->ticket[0], v.partials, tot, sh) && threadIdx.x == 0)
-    v.S->alpha = tot[0] != 0.0 ? v.S->rz / tot[0] : 0.0;
+  if (last_block<1>(&v.S->ticket[0], v.partials, tot, sh) && threadIdx.x == 0) {
+    if (!isfinite(tot[0])) {
+      v.S->nonfinite = 1;
+      v.S->done = 1;
+      v.S->alpha = 0.0;
+    } else {
+      v.S->alpha = tot[0] != 0.0 ? v.S->rz / tot[0] : 0.0;
+    }
+  }
 }
 
 __global__ void k_update(int64_t n, double* __restrict__ x, Views v) {
@@ -202,6 +248,7 @@ __global__ void k_update(int64_t n, double* __restrict__ x, Views v) {
     S->rr = tot[1];
     if (!isfinite(tot[0]) || !isfinite(tot[1])) {
       S->done = 1;
+      S->nonfinite = 1;
     } else if (tot[1] <= S->tol2) {
       S->done = 1;
       S->converged = 1;
@@ -259,13 +306,16 @@ static int scratch_address(int device, double** out) {
   return GFE_OK;
 }
 
-static bool on_device(const void* p) {
+// Device memory of the current GPU (a pointer into another GPU's memory would be read
+// without peer access), or managed memory.
+static bool on_device(const void* p, int dev) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     (void)cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 }  // namespace noalloc
@@ -291,12 +341,14 @@ extern "C" int gfe_cg_solve_noalloc(const int32_t* rowptr, const int32_t* colval
     if (relres) *relres = 0.0;
     return GFE_OK;
   }
-  if (!rowptr || !colval || !val || !b || !x || !on_device(rowptr) || !on_device(colval) ||
-      !on_device(val) || !on_device(b) || !on_device(x))
-    return set_error(GFE_ERR_INVALID_ARGUMENT,
-                     "gfe_cg_solve_noalloc: rowptr, colval, val, b and x must be device memory");
   int dev = 0;
   GFE_CUDA_TRY(cudaGetDevice(&dev));
+  if (!rowptr || !colval || !val || !b || !x || !on_device(rowptr, dev) ||
+      !on_device(colval, dev) || !on_device(val, dev) || !on_device(b, dev) ||
+      !on_device(x, dev))
+    return set_error(GFE_ERR_INVALID_ARGUMENT,
+                     "gfe_cg_solve_noalloc: rowptr, colval, val, b and x must be device memory "
+                     "of the current GPU");
   double* base = nullptr;
   GFE_TRY(scratch_address(dev, &base));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -321,22 +373,45 @@ extern "C" int gfe_cg_solve_noalloc(const int32_t* rowptr, const int32_t* colval
                      "gfe_cg_solve_noalloc: malformed CSR (rowptr or column ids out of range)");
   k_init<<<kVecBlocks, kBlock, 0, st>>>(n, rowptr, colval, val, b, x, v, rtol * rtol, maxiter);
   GFE_CUDA_TRY(cudaGetLastError());
-  for (;;) {
-    for (int k = 0; k < 25; ++k) {
-      k_spmv_dot<<<gs, kBlock, 0, st>>>(n, rowptr, colval, val, v);
-      k_update<<<kVecBlocks, kBlock, 0, st>>>(n, x, v);
-      k_direction<<<kVecBlocks, kBlock, 0, st>>>(n, v);
+  // The loop stops on the recursively updated residual; the true residual b - A x is then
+  // recomputed, and CG restarts from x (at most kMaxRestarts times, within maxiter) when it
+  // is still above rtol ||b||.
+  constexpr int kMaxRestarts = 3;
+  for (int restart = 0;; ++restart) {
+    for (;;) {
+      for (int k = 0; k < 25; ++k) {
+        k_spmv_dot<<<gs, kBlock, 0, st>>>(n, rowptr, colval, val, v);
+        k_update<<<kVecBlocks, kBlock, 0, st>>>(n, x, v);
+        k_direction<<<kVecBlocks, kBlock, 0, st>>>(n, v);
+      }
+      GFE_CUDA_TRY(cudaGetLastError());
+      GFE_CUDA_TRY(cudaMemcpyAsync(&h, v.S, sizeof(State), cudaMemcpyDeviceToHost, st));
+      GFE_CUDA_TRY(cudaStreamSynchronize(st));
+      if (h.done) break;
     }
+    if (h.nonfinite) break;
+    k_residual<<<gs, kBlock, 0, st>>>(n, rowptr, colval, val, b, x, v);
     GFE_CUDA_TRY(cudaGetLastError());
     GFE_CUDA_TRY(cudaMemcpyAsync(&h, v.S, sizeof(State), cudaMemcpyDeviceToHost, st));
     GFE_CUDA_TRY(cudaStreamSynchronize(st));
-    if (h.done) break;
+    const bool met = h.rr <= h.tol2;
+    if (met || !h.converged || restart == kMaxRestarts || h.iter >= h.maxit) {
+      h.converged = met;
+      break;
+    }
+    k_restart<<<kVecBlocks, kBlock, 0, st>>>(n, rowptr, colval, val, b, x, v);
+    GFE_CUDA_TRY(cudaGetLastError());
   }
-  k_residual<<<gs, kBlock, 0, st>>>(n, rowptr, colval, val, b, x, v);
-  GFE_CUDA_TRY(cudaGetLastError());
-  GFE_CUDA_TRY(cudaMemcpyAsync(&h, v.S, sizeof(State), cudaMemcpyDeviceToHost, st));
-  GFE_CUDA_TRY(cudaStreamSynchronize(st));
   if (iterations) *iterations = h.iter;
-  if (relres) *relres = h.bb > 0.0 ? sqrt(h.rr / h.bb) : 0.0;
+  if (relres) *relres = h.bb > 0.0 && !h.nonfinite ? sqrt(h.rr / h.bb) : (h.nonfinite ? NAN : 0.0);
+  if (h.nonfinite)
+    return set_error(GFE_ERR_NONFINITE,
+                     "gfe_cg_solve_noalloc: NaN or Inf in b, the matrix values or a reduction "
+                     "after %d iterations", h.iter);
+  if (!h.converged)
+    return set_error(GFE_ERR_NOT_CONVERGED,
+                     "gfe_cg_solve_noalloc: ||b - A x|| / ||b|| = %.3e above rtol %.3e after %d "
+                     "iterations (x holds the last iterate)",
+                     h.bb > 0.0 ? sqrt(h.rr / h.bb) : 0.0, rtol, h.iter);
   return GFE_OK;
 }

@@ -516,8 +516,9 @@ __device__ __forceinline__ unsigned long long gtimer_ns() {
   return t;
 }
 
-// bounded wait on phase `phase` of an mbarrier (false after kTmaWaitNs)
-__device__ __forceinline__ bool tma_bar_wait(uint32_t bar, uint32_t phase) {
+// bounded wait on phase `phase` of an mbarrier (false after limit_ns)
+__device__ __forceinline__ bool tma_bar_wait(uint32_t bar, uint32_t phase,
+                                             unsigned long long limit_ns = kTmaWaitNs) {
   const unsigned long long t0 = gtimer_ns();
   for (;;) {
     uint32_t done;
@@ -528,7 +529,7 @@ __device__ __forceinline__ bool tma_bar_wait(uint32_t bar, uint32_t phase) {
         : "r"(bar), "r"(phase)
         : "memory");
     if (done) return true;
-    if (gtimer_ns() - t0 > kTmaWaitNs) return false;
+    if (gtimer_ns() - t0 > limit_ns) return false;
   }
 }
 
@@ -546,7 +547,7 @@ __global__ void __launch_bounds__(kSpmvBlock, 6)
     k_lattice_spmv_tma(const __grid_constant__ CUtensorMap tmap_p,
                        const __grid_constant__ CUtensorMap tmap_k, LatticeQ1Op op,
                        float* __restrict__ q, double* __restrict__ partials, SolverState* S,
-                       DevError* err) {
+                       DevError* err, unsigned long long first_wait_ns) {
   __shared__ alignas(128) float sp[kTmaPZ][kTmaPY][kTmaX];
   __shared__ alignas(128) float sk[kTmaKZ][kTmaKY][kTmaX];
   __shared__ alignas(8) uint64_t bar;
@@ -570,8 +571,13 @@ __global__ void __launch_bounds__(kSpmvBlock, 6)
   // one thread polls the barrier (the others wait at bar.sync without taking issue slots)
   __shared__ int landed;
   if (threadIdx.x == 0) {
-    landed = tma_bar_wait(b, 0) ? 1 : 0;
-    if (!landed) {  // the copies did not land in time: report, wait once more, skip the tile
+    // first_wait_ns == 0 gives up without polling (the timeout path, exercised by tests)
+    landed = first_wait_ns > 0 && tma_bar_wait(b, 0, first_wait_ns) ? 1 : 0;
+    if (!landed) {
+      // the copies did not land in time: report, then wait (bounded again, kTmaWaitNs) for
+      // them to land before the block leaves its shared memory, and skip the tile; if that
+      // wait runs out too the copies may still be in flight, and the status tells the caller
+      // to discard the context
       raise_e(err, GFE_ERR_TIMEOUT, (long long)block_linear());
       tma_bar_wait(b, 0);
       S->done = 1;
@@ -1379,7 +1385,7 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
     if constexpr (std::is_same<Op, LatticeQ1Op>::value) {
       if (tma)
         k_lattice_spmv_tma<<<op.grid_k(kTmaK), kSpmvBlock, 0, ctx->stream>>>(
-            tmap_p, tmap_k, op, q, w.partials, w.S, ctx->d_err);
+            tmap_p, tmap_k, op, q, w.partials, w.S, ctx->d_err, ctx->first_wait_ns);
       else
         k_lattice_spmv<false, true><<<gs, kSpmvBlock, 0, ctx->stream>>>(op, p, q, nullptr,
                                                                         w.partials, w.S);
@@ -1414,6 +1420,7 @@ static int iterate(gfe_ctx* ctx, gfe_matrix* A, const Op& op, const T* dinv, T* 
     mix(&gv, sizeof(gv));
     mix(&vec4, sizeof(vec4));
     mix(&tma, sizeof(tma));
+    mix(&ctx->first_wait_ns, sizeof(ctx->first_wait_ns));
     const int tsize = (int)sizeof(T);
     mix(&tsize, sizeof(tsize));
     if (ctx->cg_exec && ctx->cg_key == key) exec = ctx->cg_exec;
@@ -1600,8 +1607,9 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
   w.S = ctx->scratch[SCR_REDUCE].as<SolverState>();
   w.partials = (double*)((char*)ctx->scratch[SCR_REDUCE].ptr + 256);
   w.hS = (SolverState*)ctx->h_pinned;
-  // a grown scratch buffer holds garbage: the reduction tickets must start at zero for every
-  // method (the final residual below reduces through them too)
+  // a grown scratch buffer holds garbage, and a launch cut short by a timed-out wait can
+  // leave a ticket part-counted: the reduction tickets must start at zero for every method
+  // (the final residual below reduces through them too)
   GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
   // The precondition switch: Jacobi uses 1/diag, none uses ones (same kernels).
   const bool jac = o->precond == GFE_PC_JACOBI;

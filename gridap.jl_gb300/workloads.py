@@ -19,6 +19,8 @@ import numpy as np
 from .celldata import CellField, NodalField, SinSum
 from .fespaces import FESpace, ReferenceFE, lagrangian
 from .geometry import CartesianDiscreteModel, Measure, Triangulation
+from .synthetic import (elasticity_lame, gaussian_random_field, lognormal_inputs,  # noqa: F401
+                        q2_jitter, sinsum_terms)
 
 
 @dataclass
@@ -32,33 +34,11 @@ class Workload:
     rtol: float
 
 
-def gaussian_random_field(shape, corr_cells: float, rng: np.random.Generator) -> np.ndarray:
-    """Unit-variance stationary Gaussian field on a periodic cell grid with a Gaussian
-    covariance of correlation length `corr_cells` cells (spectral filtering)."""
-    white = rng.standard_normal(shape)
-    k = [np.fft.fftfreq(n) * 2 * np.pi for n in shape]
-    kk = np.zeros(shape)
-    for d, kd in enumerate(k):
-        sh = [1] * len(shape)
-        sh[d] = shape[d]
-        kk = kk + (kd.reshape(sh)) ** 2
-    filt = np.exp(-0.25 * kk * corr_cells ** 2)
-    g = np.real(np.fft.ifftn(np.fft.fftn(white) * filt))
-    g -= g.mean()
-    g /= g.std()
-    return g
-
-
 def lognormal_3d(n: int = 128, seed: int = 5999, contrast: float = 1e4,
                  corr_cells: float = 8.0) -> Workload:
     model = CartesianDiscreteModel((0, 1, 0, 1, 0, 1), (n, n, n))
     V = FESpace(model, ReferenceFE(lagrangian, float, 1), dirichlet_tags="boundary")
-    rng = np.random.default_rng(seed)
-    # cell grid in Gridap's cell order (x fastest): field indexed [k, j, i]
-    g = gaussian_random_field((n, n, n), corr_cells, rng)
-    sigma = np.log(contrast) / (g.max() - g.min())
-    kappa = np.exp(sigma * (g - g.mean())).reshape(-1)
-    f = rng.standard_normal(model.num_nodes())
+    kappa, f = lognormal_inputs(n, seed, contrast, corr_cells)
     return Workload("lognormal_3d", model, V, Measure(Triangulation(model), 2), kappa,
                     NodalField(f), 1e-8)
 
@@ -66,9 +46,7 @@ def lognormal_3d(n: int = 128, seed: int = 5999, contrast: float = 1e4,
 def poisson_2d(n: int = 256, seed: int = 1) -> Workload:
     model = CartesianDiscreteModel((0, 1, 0, 1), (n, n))
     V = FESpace(model, ReferenceFE(lagrangian, float, 1), dirichlet_tags="boundary")
-    rng = np.random.default_rng(seed)
-    terms = np.column_stack([rng.standard_normal(8), rng.integers(1, 9, 8),
-                             rng.integers(1, 9, 8)]).astype(np.float64)
+    terms = sinsum_terms(seed)
     return Workload("poisson_2d", model, V, Measure(Triangulation(model), 2), None,
                     SinSum(terms), 1e-10)
 
@@ -117,9 +95,7 @@ def elasticity_3d(n: int = 48, seed: int = 3):
     model = simplexify(CartesianDiscreteModel((0, 1, 0, 1, 0, 1), (n, n, n)))
     model.add_tag_from_vertex_filter("x0", lambda x: np.abs(x[:, 0]) < 1e-12)
     V = FESpace(model, ReferenceFE(lagrangian, 3, 2), dirichlet_tags="x0")
-    rng = np.random.default_rng(seed)
-    lame = np.exp(rng.standard_normal((model.num_cells(), 2)))
-    lame /= lame.mean(axis=0)
+    lame = elasticity_lame(model.num_cells(), seed)
     return model, V, Measure(Triangulation(model), 4), lame, np.array([0.0, 0.0, -1.0])
 
 
@@ -127,9 +103,7 @@ def jittered_q2_3d(n: int = 64, seed: int = 2, amplitude: float = 0.2):
     """3-D Poisson on (0,1)^3 with n^3 hexahedra whose interior nodes are moved by a seeded
     uniform jitter in (-amplitude h, amplitude h)^3, Lagrangian Q2 with homogeneous Dirichlet
     data on the boundary, kappa = 1, f = 1, quadrature degree 4. Returns (model, V, measure)."""
-    nn = (n + 1) ** 3
-    rng = np.random.default_rng(seed)
-    jit = rng.uniform(-amplitude, amplitude, (nn, 3)) / n
+    jit = q2_jitter(n, seed, amplitude)
     model = CartesianDiscreteModel((0, 1, 0, 1, 0, 1), (n, n, n), node_jitter=jit)
     V = FESpace(model, ReferenceFE(lagrangian, float, 2), dirichlet_tags="boundary")
     return model, V, Measure(Triangulation(model), 4)

@@ -37,9 +37,12 @@ enum {
   GFE_ERR_OUT_OF_MEMORY = 3,
   GFE_ERR_DEGENERATE_CELL = 4, /* det(J) <= 0 or not finite at a quadrature point */
   GFE_ERR_ROW_TOO_WIDE = 5,    /* a matrix row has more entries than the kernels support */
-  GFE_ERR_TIMEOUT = 6,         /* a bounded device-side wait ran out */
+  GFE_ERR_TIMEOUT = 6,         /* a bounded device-side wait ran out (the kernel waited for
+                                  its copies in flight, bounded again, before it returned; if
+                                  that wait also ran out, destroy the context) */
   GFE_ERR_UNSUPPORTED = 7,     /* element / form / option combination not provided */
-  GFE_ERR_NONFINITE = 8        /* NaN or Inf in coefficients, matrix or vectors */
+  GFE_ERR_NONFINITE = 8,       /* NaN or Inf in coefficients, matrix or vectors */
+  GFE_ERR_NOT_CONVERGED = 9    /* gfe_cg_solve_noalloc: maxiter reached above rtol */
 };
 
 typedef struct gfe_ctx gfe_ctx;
@@ -72,6 +75,12 @@ enum {
 };
 int gfe_ctx_set_timing(gfe_ctx* ctx, int enable);
 int gfe_ctx_kernel_time(gfe_ctx* ctx, int kernel, double* total_ms, int64_t* launches);
+/* Limit (ns, default 1e9) of the first bounded wait on the tensor-copy barrier of the lattice
+ * SpMV. When it runs out the kernel records GFE_ERR_TIMEOUT, waits again (bounded, 1 s) for
+ * its copies to land, skips its tile and the solve returns GFE_ERR_TIMEOUT; the context stays
+ * usable. 0 makes the first wait give up at once: a switch for tests of that path, off by
+ * default. No counterpart in Gridap. */
+int gfe_ctx_set_wait_limit(gfe_ctx* ctx, uint64_t first_wait_ns);
 
 /* ---- FE space set-up (host) -------------------------------------------------------------- */
 /* CartesianDiscreteModel(domain, partition) arrays: node coordinates (nnodes*D, x fastest),
@@ -520,6 +529,12 @@ int gfe_solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_sol
  * address (once per device); make it before any stream capture. All calls share the array:
  * calls that overlap on the GPU race. Work is ordered on `stream` (a cudaStream_t, NULL for
  * the default stream) and complete on return.
+ * Stopping: the iteration stops on the recursively updated residual; the true residual
+ * ||b - A x|| is then recomputed and CG restarts from x (at most 3 times, within maxiter)
+ * while it is above rtol ||b||. *relres is that true relative residual. Returns GFE_OK when
+ * it meets rtol, GFE_ERR_NOT_CONVERGED when maxiter ran out first (x holds the last iterate),
+ * GFE_ERR_NONFINITE when b, the matrix or a reduction is NaN or Inf; pointers into another
+ * GPU's memory are rejected with GFE_ERR_INVALID_ARGUMENT.
  * No counterpart in Gridap: it is an extra entry point of this library. */
 int gfe_cg_solve_noalloc(const int32_t* rowptr, const int32_t* colval, const double* val,
                          int64_t n, int64_t nnz, const double* b, double* x, double rtol,

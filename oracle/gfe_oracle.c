@@ -17,6 +17,12 @@
 #endif
 
 static double det_t(int D, const double* a);
+
+/* Threads of the per-cell loops (cell matrices and vectors). 1 (the default) runs them
+ * serially, as Gridap's lazy cell arrays are evaluated; more threads split the cells, which
+ * changes no arithmetic. */
+static int g_cell_threads = 1;
+void orc_set_cell_threads(int n) { g_cell_threads = n > 0 ? n : 1; }
 static void inv_t(int D, const double* a, double* r);
 
 /* ====================================================================================== */
@@ -444,10 +450,14 @@ int orc_q2_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_vert
   double* dphi1 = (double*)malloc(sizeof(double) * nq * nv * D);
   double* phi = (double*)malloc(sizeof(double) * nq * nn);
   double* dphi = (double*)malloc(sizeof(double) * nq * nn * D);
-  double* g = (double*)malloc(sizeof(double) * nn * D);
   orc_q1_shapes(D, nq, qx, phi1, dphi1);
   orc_q2_shapes(D, nq, qx, phi, dphi);
+  int bad = 0;
+  /* cells are independent: threads (orc_set_cell_threads) split the cell range, and every
+   * cell's arithmetic is the serial one, so the arrays are identical for any thread count */
+#pragma omp parallel for schedule(dynamic, 256) num_threads(g_cell_threads) if (g_cell_threads > 1)
   for (int64_t c = 0; c < ncells; ++c) {
+    double g[27 * 3];
     const int32_t* vs = cell_vertices + c * nv;
     double* K = cellmats ? cellmats + c * nn * nn : NULL;
     double* bv = cellvecs ? cellvecs + c * nn : NULL;
@@ -463,8 +473,9 @@ int orc_q2_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_vert
       }
       const double dJ = det_t(D, Jt);
       if (!(dJ > 0.0) && !(dJ < 0.0)) {
-        free(phi1); free(dphi1); free(phi); free(dphi); free(g);
-        return -1;
+#pragma omp atomic write
+        bad = 1;
+        break;
       }
       inv_t(D, Jt, iJt);
       const double dV = fabs(dJ) * qw[q];
@@ -490,8 +501,8 @@ int orc_q2_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_vert
       }
     }
   }
-  free(phi1); free(dphi1); free(phi); free(dphi); free(g);
-  return 0;
+  free(phi1); free(dphi1); free(phi); free(dphi);
+  return bad ? -1 : 0;
 }
 
 /* ====================================================================================== */
@@ -656,9 +667,12 @@ int orc_q1_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_node
   int nv = 1 << D;
   double* phi = (double*)malloc(sizeof(double) * nq * nv);
   double* dphi = (double*)malloc(sizeof(double) * nq * nv * D);
-  double* g = (double*)malloc(sizeof(double) * nv * D);
   orc_q1_shapes(D, nq, qx, phi, dphi);
+  int bad = 0;
+  /* cells are independent (see orc_q2_cell_arrays_diffusion) */
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(g_cell_threads) if (g_cell_threads > 1)
   for (int64_t c = 0; c < ncells; ++c) {
+    double g[8 * 3];
     const int32_t* nodes = cell_nodes + c * nv;
     double* K = cellmats ? cellmats + c * nv * nv : NULL;
     double* bv = cellvecs ? cellvecs + c * nv : NULL;
@@ -679,8 +693,9 @@ int orc_q1_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_node
       }
       double dJ = det_t(D, Jt);
       if (!(dJ > 0.0) && !(dJ < 0.0)) {
-        free(phi); free(dphi); free(g);
-        return -1; /* degenerate cell */
+#pragma omp atomic write
+        bad = 1; /* degenerate cell */
+        break;
       }
       inv_t(D, Jt, iJt);
       double dV = fabs(dJ) * qw[q];
@@ -718,8 +733,7 @@ int orc_q1_cell_arrays_diffusion(int D, int64_t ncells, const int32_t* cell_node
   }
   free(phi);
   free(dphi);
-  free(g);
-  return 0;
+  return bad ? -1 : 0;
 }
 
 /* ====================================================================================== */
@@ -822,6 +836,130 @@ int orc_assemble_matrix_csc_rect(int64_t ncells, int ndr, int ndc, const int32_t
   out->nrows = nrows;
   out->ncols = ncols;
   out->nnz = colptr[ncols] - 1;
+  out->colptr = colptr;
+  out->rowval = rowval;
+  out->nzval = nzval;
+  return 0;
+}
+
+/* Greedy first-fit cell colouring: cell c (in cell order) takes the smallest colour that no
+ * earlier cell sharing a free dof with it holds (at most 64 colours). Cells of one colour
+ * share no free dof, so their additions touch disjoint rows and columns. Returns the number
+ * of colours, or -1 when 64 do not suffice. */
+int orc_color_cells(int64_t ncells, int nd, const int32_t* cell_dofs, int64_t nfree,
+                    int32_t* color) {
+  uint64_t* used = (uint64_t*)calloc(nfree + 1, sizeof(uint64_t));
+  if (!used) return -1;
+  int ncol = 0;
+  for (int64_t c = 0; c < ncells; ++c) {
+    uint64_t forbid = 0;
+    for (int a = 0; a < nd; ++a) {
+      const int32_t d = cell_dofs[c * nd + a];
+      if (d > 0) forbid |= used[d];
+    }
+    if (forbid == ~(uint64_t)0) {
+      free(used);
+      return -1;
+    }
+    int k = 0;
+    while (forbid >> k & 1u) ++k;
+    color[c] = k;
+    if (k + 1 > ncol) ncol = k + 1;
+    for (int a = 0; a < nd; ++a) {
+      const int32_t d = cell_dofs[c * nd + a];
+      if (d > 0) used[d] |= (uint64_t)1 << k;
+    }
+  }
+  free(used);
+  return ncol;
+}
+
+/* The assembly of orc_assemble_matrix_csc_rect (square, rows and columns from the same ids)
+ * run colour by colour, the cells of one colour split over `nthreads` threads: the symbolic
+ * count, the InserterCSC insertions and the vector additions of cells of one colour touch
+ * disjoint columns, so no two threads write the same column. The pattern equals the serial
+ * one; a value is the same sum taken in colour order, then cell order, instead of cell
+ * order (equal up to rounding). The OpenMP counterpart of a multi-threaded Gridap assembly.
+ * cellvecs / b may be NULL. */
+int orc_assemble_csc_colored(int64_t ncells, int nd, const int32_t* cell_dofs,
+                             const double* cellmats, const double* cellvecs, int64_t n,
+                             int ncolors, const int64_t* color_ptr, const int64_t* color_cells,
+                             int nthreads, orc_csc* out, double* b) {
+  const int nt = nthreads > 0 ? nthreads : 1;
+  if (ncolors < 0 || color_ptr[ncolors] != ncells) return -1;
+  int64_t* colnnz = (int64_t*)calloc(n + 1, sizeof(int64_t));
+  int64_t* colptr = (int64_t*)malloc(sizeof(int64_t) * (n + 1));
+  if (!colnnz || !colptr) return -1;
+  for (int k = 0; k < ncolors; ++k) {
+#pragma omp parallel for schedule(dynamic, 512) num_threads(nt) if (nt > 1)
+    for (int64_t t = color_ptr[k]; t < color_ptr[k + 1]; ++t) {
+      const int32_t* rs = cell_dofs + color_cells[t] * nd;
+      int cnt = 0;
+      for (int li = 0; li < nd; ++li) cnt += rs[li] > 0;
+      for (int lj = 0; lj < nd; ++lj)
+        if (rs[lj] > 0) colnnz[rs[lj] - 1] += cnt;
+    }
+  }
+  colptr[0] = 1;
+  for (int64_t j = 0; j < n; ++j) colptr[j + 1] = colptr[j] + colnnz[j];
+  const int64_t ndata = colptr[n] - 1;
+  int64_t* rowval = (int64_t*)malloc(sizeof(int64_t) * (ndata > 0 ? ndata : 1));
+  double* nzval = (double*)calloc(ndata > 0 ? ndata : 1, sizeof(double));
+  if (!rowval || !nzval) return -1;
+  memset(colnnz, 0, sizeof(int64_t) * (n + 1));
+  if (b) memset(b, 0, sizeof(double) * n);
+  for (int k = 0; k < ncolors; ++k) {
+#pragma omp parallel for schedule(dynamic, 512) num_threads(nt) if (nt > 1)
+    for (int64_t t = color_ptr[k]; t < color_ptr[k + 1]; ++t) {
+      const int64_t c = color_cells[t];
+      const int32_t* rs = cell_dofs + c * nd;
+      const double* vs = cellmats ? cellmats + c * nd * nd : NULL;
+      for (int lj = 0; lj < nd; ++lj) {
+        const int64_t j = rs[lj];
+        if (j <= 0) continue;
+        for (int li = 0; li < nd; ++li) {
+          const int64_t i = rs[li];
+          if (i <= 0) continue;
+          const double v = vs ? vs[li + lj * nd] : 0.0;
+          const int64_t pini = colptr[j - 1] - 1;
+          const int64_t pend = pini + colnnz[j - 1] - 1;
+          const int64_t p = sorted_first(rowval, i, pini, pend);
+          if (p > pend) {
+            colnnz[j - 1] += 1;
+            rowval[p] = i;
+            nzval[p] = v;
+          } else if (rowval[p] != i) {
+            for (int64_t q = pend; q >= p; --q) {
+              rowval[q + 1] = rowval[q];
+              nzval[q + 1] = nzval[q];
+            }
+            colnnz[j - 1] += 1;
+            rowval[p] = i;
+            nzval[p] = v;
+          } else {
+            nzval[p] += v;
+          }
+        }
+      }
+      if (b && cellvecs)
+        for (int li = 0; li < nd; ++li)
+          if (rs[li] > 0) b[rs[li] - 1] += cellvecs[c * nd + li];
+    }
+  }
+  int64_t w = 0;
+  for (int64_t j = 0; j < n; ++j) {
+    const int64_t pini = colptr[j] - 1;
+    for (int64_t p = pini; p < pini + colnnz[j]; ++p, ++w) {
+      nzval[w] = nzval[p];
+      rowval[w] = rowval[p];
+    }
+  }
+  colptr[0] = 1;
+  for (int64_t j = 0; j < n; ++j) colptr[j + 1] = colptr[j] + colnnz[j];
+  free(colnnz);
+  out->nrows = n;
+  out->ncols = n;
+  out->nnz = colptr[n] - 1;
   out->colptr = colptr;
   out->rowval = rowval;
   out->nzval = nzval;
@@ -1208,6 +1346,9 @@ int orc_p2tet_cell_arrays_elasticity(int64_t ncells, const int32_t* tet_vertices
   double* dphi = (double*)malloc(sizeof(double) * nq * 10 * 3);
   orc_p2tet_shapes(nq, qx, phi, dphi);
   static const double G1[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  int bad = 0;
+  /* cells are independent (see orc_q2_cell_arrays_diffusion) */
+#pragma omp parallel for schedule(dynamic, 64) num_threads(g_cell_threads) if (g_cell_threads > 1)
   for (int64_t c = 0; c < ncells; ++c) {
     double Jt[9] = {0}, iJt[9];
     for (int a = 0; a < 4; ++a) {
@@ -1217,9 +1358,9 @@ int orc_p2tet_cell_arrays_elasticity(int64_t ncells, const int32_t* tet_vertices
     }
     const double dJ = det_t(3, Jt);
     if (!(dJ > 0.0) && !(dJ < 0.0)) {
-      free(phi);
-      free(dphi);
-      return -1;
+#pragma omp atomic write
+      bad = 1;
+      continue;
     }
     inv_t(3, Jt, iJt);
     const double lam = lame[2 * c], mu = lame[2 * c + 1];
@@ -1266,5 +1407,5 @@ int orc_p2tet_cell_arrays_elasticity(int64_t ncells, const int32_t* tet_vertices
   }
   free(phi);
   free(dphi);
-  return 0;
+  return bad ? -1 : 0;
 }

@@ -132,6 +132,16 @@ int orc_assemble_matrix_csc_rect(int64_t ncells, int ndr, int ndc, const int32_t
                                  const int32_t* cell_cols, const double* cellmats,
                                  int64_t nrows, int64_t ncols, orc_csc* out);
 void orc_csc_free(orc_csc* a);
+/* Greedy first-fit colouring of the cells by shared free dofs; returns the colour count. */
+int orc_color_cells(int64_t ncells, int nd, const int32_t* cell_dofs, int64_t nfree,
+                    int32_t* color);
+/* Colour-parallel assembly (OpenMP): cells of one colour in parallel, colours in order. */
+int orc_assemble_csc_colored(int64_t ncells, int nd, const int32_t* cell_dofs,
+                             const double* cellmats, const double* cellvecs, int64_t n,
+                             int ncolors, const int64_t* color_ptr, const int64_t* color_cells,
+                             int nthreads, orc_csc* out, double* b);
+/* Threads of the per-cell loops (default 1: serial). */
+void orc_set_cell_threads(int n);
 /* Dense vector assembly (SparseMatrixAssemblers.jl:287-316). b must be zeroed by caller. */
 void orc_assemble_vector(int64_t ncells, int nd, const int32_t* cell_rows,
                          const double* cellvecs, double* b);

@@ -77,6 +77,10 @@ def lib():
                                             C.POINTER(C.POINTER(C.c_int64)),
                                             C.POINTER(C.POINTER(C.c_int32))]
         L.orc_free.argtypes = [P]
+        L.orc_set_cell_threads.argtypes = [C.c_int]
+        L.orc_color_cells.argtypes = [C.c_int64, C.c_int, P, C.c_int64, P]
+        L.orc_assemble_csc_colored.argtypes = [C.c_int64, C.c_int, P, P, P, C.c_int64, C.c_int,
+                                               P, P, C.c_int, C.POINTER(_CSC), P]
         L.orc_rcm_perm.argtypes = [C.c_int64, P, P, P]
         L.orc_sloan_perm.argtypes = [C.c_int64, P, P, C.c_int64, C.c_int64, P]
         _lib = L
@@ -313,6 +317,60 @@ def assemble_csc(cell_rows, cell_cols, cellmats, nrows, ncols):
     nzval = np.ctypeslib.as_array(out.nzval, (max(nnz, 1),))[:nnz].copy()
     lib().orc_csc_free(C.byref(out))
     return colptr, rowval, nzval
+
+
+def set_cell_threads(n):
+    """Threads of the oracle's per-cell loops (1 = serial, the default). The cell arrays are
+    the same for every thread count."""
+    lib().orc_set_cell_threads(int(n))
+
+
+class cell_threads:
+    """`with cell_threads(n):` runs the per-cell loops on n threads, then restores 1."""
+
+    def __init__(self, n):
+        self.n = n
+
+    def __enter__(self):
+        set_cell_threads(self.n)
+
+    def __exit__(self, *a):
+        set_cell_threads(1)
+
+
+def color_cells(cell_dofs, nfree):
+    """Greedy first-fit colours of the cells (cells of one colour share no free dof)."""
+    cd = np.ascontiguousarray(cell_dofs, np.int32)
+    col = np.empty(cd.shape[0], np.int32)
+    k = lib().orc_color_cells(cd.shape[0], cd.shape[1], _p(cd), nfree, _p(col))
+    if k < 0:
+        raise RuntimeError("oracle: more than 64 colours")
+    return col, k
+
+
+def assemble_colored(cell_dofs, cellmats, cellvecs, n, nthreads, colors=None):
+    """Colour-parallel InserterCSC assembly of a square system on `nthreads` threads:
+    (colptr, rowval, nzval) 1-based and b. Same pattern as assemble_csc; values are the same
+    sums in colour-then-cell order."""
+    cd = np.ascontiguousarray(cell_dofs, np.int32)
+    col, k = colors if colors is not None else color_cells(cd, n)
+    order = np.argsort(col, kind="stable").astype(np.int64)
+    cptr = np.zeros(k + 1, np.int64)
+    cptr[1:] = np.cumsum(np.bincount(col, minlength=k))
+    cm = np.ascontiguousarray(np.transpose(cellmats, (0, 2, 1)), np.float64)  # col-major
+    cv = None if cellvecs is None else np.ascontiguousarray(cellvecs, np.float64)
+    b = np.zeros(n) if cv is not None else None
+    out = _CSC()
+    st = lib().orc_assemble_csc_colored(cd.shape[0], cd.shape[1], _p(cd), _p(cm), _p(cv), n, k,
+                                        _p(cptr), _p(order), nthreads, C.byref(out), _p(b))
+    if st != 0:
+        raise MemoryError("oracle colour-parallel assembly failed")
+    nnz = out.nnz
+    colptr = np.ctypeslib.as_array(out.colptr, (n + 1,)).copy()
+    rowval = np.ctypeslib.as_array(out.rowval, (max(nnz, 1),))[:nnz].copy()
+    nzval = np.ctypeslib.as_array(out.nzval, (max(nnz, 1),))[:nnz].copy()
+    lib().orc_csc_free(C.byref(out))
+    return (colptr, rowval, nzval), b
 
 
 def to_scipy(colptr, rowval, nzval, nrows, ncols):

@@ -507,6 +507,32 @@ def test_errors_are_statuses_and_context_survives(gg):
     assert A.nnz == 4 * 4 + 0 or A.nnz > 0
 
 
+def test_timed_out_wait_returns_status_and_context_survives(gg):
+    """The bounded barrier wait of the TMA lattice SpMV made to give up at once (the test
+    switch): the kernel reports GFE_ERR_TIMEOUT, waits (bounded) for its copies to land and
+    returns; the solve fails with that status and the next solve on the same context
+    converges. No wait runs unbounded and nothing faults."""
+    n = 24
+    rng = np.random.default_rng(11)
+    kappa = np.exp(rng.standard_normal(n ** 3))
+    _, V, A, b = _problem(gg, (0, 1) * 3, (n, n, n), ("boundary",), kappa, 1.0)
+    ctx = gg.default_context()
+    x = np.zeros(V.nfree)
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.MixedCGSolver(rtol=1e-8), A), A)
+    gg.solve_(x, ns, b)
+    assert ns.report.converged and ns.report.operator_format == 2
+    ctx.set_wait_limit(0)
+    try:
+        with pytest.raises(gg.GfeError) as e:
+            gg.solve_(x, ns, b)
+        assert e.value.code == gg._lib.GFE_ERR_TIMEOUT
+    finally:
+        ctx.set_wait_limit(10 ** 9)
+    x[:] = 0
+    gg.solve_(x, ns, b)
+    assert ns.report.converged and ns.report.relres <= 1e-8
+
+
 def test_c5_scale_pattern_properties(gg):
     """128^3 Q1 with boundary Dirichlet: nnz, symmetry and zero row sums for rows away from
     the boundary (constants are in the kernel of the diffusion operator)."""

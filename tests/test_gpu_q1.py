@@ -520,7 +520,7 @@ def test_timed_out_wait_returns_status_and_context_survives(gg):
     x = np.zeros(V.nfree)
     ns = gg.numerical_setup(gg.symbolic_setup(gg.MixedCGSolver(rtol=1e-8), A), A)
     gg.solve_(x, ns, b)
-    assert ns.report.converged and ns.report.operator_format == 2
+    assert ns.report.converged and ns.report.operator_format == "matrix-free lattice"
     ctx.set_wait_limit(0)
     try:
         with pytest.raises(gg.GfeError) as e:

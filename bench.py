@@ -405,6 +405,15 @@ def run_gpu(args):
     # graphs. Kernel durations need CUDA events around each SpMV, which the library records
     # only on its direct-launch path, so the same steps are then repeated with kernel timing
     # on; the roofline comes from that instrumented repeat (its ms_per_step is reported too).
+    if args.profile:
+        # the headline steps alone, for a profiler's launch list (no JSON line: a number taken
+        # under a profiler is not a measurement)
+        for _ in range(args.warmup + args.steps):
+            mixed_dev()
+        barrier()
+        if rank == 0:
+            print(f"profile run: {args.warmup + args.steps} headline steps")
+        return
     with ClockSampler(local) as clk:
         clocks.append(clk)
         r_mixed = timed("mixed", mixed_dev, args.steps, args.warmup, kernel_timing=False)
@@ -1242,6 +1251,8 @@ def main():
                     help="headline solver: multigrid-preconditioned flexible CG or Jacobi mixed CG")
     ap.add_argument("--delta", type=float, default=0.01,
                     help="residual reduction between FP64 reliable updates of the mixed CG")
+    ap.add_argument("--profile", action="store_true",
+                    help="run only the headline steps and print no JSON (for ncu launch lists)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the full-size comparisons with the oracle")

@@ -143,6 +143,7 @@ SIGNATURES = {
     "gfe_learned_pc_get_weights": (C.c_int, [_P, _P]),
     "gfe_learned_pc_apply": (C.c_int, [_P, _P, _P]),
     "gfe_learned_pc_samples": (C.c_int, [_P, _P, _P, C.c_int64, _P, _P, _P]),
+    "gfe_learned_pc_samples_error": (C.c_int, [_P, _P, _P, C.c_int64, _P, _P, _P]),
     "gfe_learned_pc_train": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, C.c_int32, C.c_float,
                                        C.c_uint64, C.POINTER(C.c_float)]),
     "gfe_solve_fcg": (C.c_int, [_P, _P, _P, C.POINTER(SolverOpts), _P, _P,

@@ -118,6 +118,7 @@ int assemble_cellmats(gfe_ctx* ctx, gfe_matrix* A, const double* d_cellmats) {
   src.cs = (int64_t)A->nd * A->cols_per_cell();
   src.es = 1;
   src.ntab = 0;
+  GFE_TRY(ensure_row_refs(ctx, A));
   RowArgs a = row_args(ctx, A, nullptr, true);
   GFE_TRY(run_rows(ctx, a, src, maxw, A->pos_bytes));
   return check_device_error(ctx, "numeric_loop_matrix");
@@ -642,6 +643,7 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
       s.vcs = nn;
       s.ves = 1;
       s.ntab = 0;
+      GFE_TRY(ensure_row_refs(ctx, R));
       RowArgs a = row_args(ctx, R, d_b, A != nullptr);
       if (A) {
         GFE_TRY(run_rows(ctx, a, s, maxw, A->pos_bytes));
@@ -685,6 +687,7 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
     s.vcs = 1;
     s.ves = ncells;
     s.ntab = 0;
+    GFE_TRY(ensure_row_refs(ctx, R));
     RowArgs a = row_args(ctx, R, d_b, A != nullptr);
     if (A) {
       GFE_TRY(run_rows(ctx, a, s, maxw, A->pos_bytes));
@@ -708,6 +711,12 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
                           SCR_CELLNODES, &v));
       cn = (const int32_t*)v;
     }
+    // the closed-form lattice pattern of this grid: the class-sum kernel
+    bool lattice_done = false;
+    if (A && D == 3 && !cn)
+      GFE_TRY(assemble_cartesian_q1_lattice(ctx, A, p, d_coef, src_kind, d_src, tabs.data(),
+                                            tabs.data() + 2 * nv * nv, d_b, &lattice_done));
+    if (!lattice_done) GFE_TRY(ensure_row_refs(ctx, R));
     RowArgs a = row_args(ctx, R, d_b, A != nullptr);
     if (!A) a.rowptr = nullptr;
 #define GFE_CART(DD, F32)                                                               \
@@ -729,7 +738,8 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
       GFE_TRY(vector_only_rows(ctx, a, s));                                             \
     }                                                                                   \
   }
-    if (D == 2 && !fp32) GFE_CART(2, false)
+    if (lattice_done) {
+    } else if (D == 2 && !fp32) GFE_CART(2, false)
     else if (D == 2) GFE_CART(2, true)
     else if (!fp32) GFE_CART(3, false)
     else GFE_CART(3, true)
@@ -792,6 +802,7 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
     s.vcs = 1;
     s.ves = ncells;
     s.ntab = 0;
+    GFE_TRY(ensure_row_refs(ctx, R));
     RowArgs a = row_args(ctx, R, d_b, A != nullptr);
     if (A) {
       GFE_TRY(run_rows(ctx, a, s, maxw, A->pos_bytes));

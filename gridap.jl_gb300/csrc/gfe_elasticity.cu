@@ -218,6 +218,7 @@ int assemble_p2_elasticity(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, do
     GFE_TRY(build_refs(ctx, &tmp));
     R = &tmp;
   }
+  GFE_TRY(ensure_row_refs(ctx, R));
   RowArgs a = row_args(ctx, R, d_b, A != nullptr);
   if (!A) {
     a.rowptr = nullptr;

@@ -162,6 +162,16 @@ struct gfe_matrix {
   // other change of the values drops it. 0 none, 1 numbering check pending, 2 valid.
   int mf_state = 0;
   int64_t mf_n[3] = {0, 0, 0};
+  // the pattern is the closed form of a 3-D Cartesian Q1 grid of cart_n cells whose rows and
+  // columns are the interior nodes in node order (set by the problem-aware symbolic loop
+  // after its device check of the ids)
+  bool cart_lattice = false;
+  int64_t cart_n[3] = {0, 0, 0};
+  // ref_ptr / refs / refpos of the closed-form pattern not written yet (ensure_row_refs)
+  bool refs_pending = false;
+  // a pattern built by the general symbolic loop was checked once against the closed form
+  // of a problem's grid (cartesian_ids_match): the same ids give the same pattern
+  bool cart_checked = false;
   float mf_K[64] = {0};
   gfe::DevBuf mf_kap32, mf_flag;
 };
@@ -190,6 +200,22 @@ enum ScratchId {
   SCR_COUNT
 };
 static_assert(SCR_COUNT <= 18, "scratch slots");
+
+// The class-sum numeric assembly of 3-D uniform Cartesian Q1 diffusion into the closed-form
+// lattice pattern (gfe_assemble_lattice.cu); *done is false when the problem is not one it
+// covers (the caller then runs the generic row gather).
+int assemble_cartesian_q1_lattice(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p,
+                                  const double* d_coef, int src_kind, const double* d_src,
+                                  const double* Kref, const double* mref, double* d_b,
+                                  bool* done);
+
+// Whether A's cell ids are the interior-node numbering of an (n0, n1, n2) Cartesian Q1 grid
+// with every boundary node Dirichlet (device check); the pattern is then the closed form.
+int cartesian_ids_match(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1, int64_t n2,
+                        bool* ok);
+// Writes the row references and positions of a closed-form Cartesian pattern if they are
+// still pending (every row gather over a matrix calls it first).
+int ensure_row_refs(gfe_ctx* ctx, gfe_matrix* A);
 
 // pointer classification
 bool is_device_ptr(const void* p);
@@ -239,6 +265,10 @@ int launch_q2_cells_tf32(gfe_ctx* ctx, int64_t ncells, const int32_t* cell_verti
 // kernels return at once when non-zero
 int learned_apply(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, float* d_z,
                   const int* skip = nullptr);
+int64_t learned_ndofs(const gfe_learned_pc* pc);
+// z = base + M(r) (base may be null), e.g. a learned smoothing step x + M(b - A x)
+int learned_apply_into(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, const float* base,
+                       float* d_z, const int* skip);
 int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_opts* o,
               const double* d_b, double* d_x, gfe_solve_report* rep);
 
@@ -269,6 +299,9 @@ struct LatticeQ1Op;
 struct LatticeMG;
 int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out);
 int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done);
+// Makes the learned block preconditioner the fine level's smoother of the V-cycle (pre:
+// x = M(b); post: x += M(b - A x)); the coarser levels keep damped Jacobi.
+int mg_set_learned(LatticeMG* mg, gfe_learned_pc* pc);
 void mg_destroy(LatticeMG* mg);
 // Jacobi-preconditioned FP64 BiCGStab from x = 0 (gfe_bicgstab.cu)
 int bicgstab(gfe_ctx* ctx, gfe_matrix* A, const double* dinv, const double* d_b, double* d_x,

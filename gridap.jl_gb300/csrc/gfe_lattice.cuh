@@ -41,12 +41,28 @@ struct LatticeQ1Op {
   }
 };
 
+// p at a row index (the x of the apply)
+struct LatticeLoad {
+  const float* __restrict__ p;
+  __device__ __forceinline__ float operator()(int64_t idx) const { return __ldg(p + idx); }
+};
+
+// x0 = omega D^-1 b at a row index (the first Jacobi sweep from zero, formed on the fly)
+struct LatticeLoadJacobi0 {
+  const float* __restrict__ b;
+  const float* __restrict__ dinv;
+  float omega;
+  __device__ __forceinline__ float operator()(int64_t idx) const {
+    return omega * __ldg(dinv + idx) * __ldg(b + idx);
+  }
+};
+
 // The rows of one tile: (i, j) = (32 bx + lane, 8 by + warp), k-planes KZ bz .. + KZ (KZ = 1
 // for small lattices: more blocks, shorter per-thread chains). For every row the epilogue
-// receives (row index, p at the row, (A p)_row).
-template <bool PAD, class Epi, int KZ = kLatK>
-__device__ __forceinline__ void lattice_rows(const LatticeQ1Op& op, int bx, int by, int bz,
-                                             const float* __restrict__ p, Epi& epi) {
+// receives (row index, p at the row, (A p)_row); `load(index)` gives p.
+template <bool PAD, class Epi, int KZ = kLatK, class Load = LatticeLoad>
+__device__ __forceinline__ void lattice_rows_f(const LatticeQ1Op& op, int bx, int by, int bz,
+                                               const Load& load, Epi& epi) {
   const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
   const int i = bx * 32 + (int)(threadIdx.x & 31);
   const int j = by * 8 + (int)(threadIdx.x >> 5);
@@ -67,7 +83,7 @@ __device__ __forceinline__ void lattice_rows(const LatticeQ1Op& op, int bx, int 
         for (int dx = -1; dx <= 1; ++dx) {
           float t = 0.f;
           if (PAD || (okz && okx[dx + 1] && oky[dy + 1]))
-            t = __ldg(p + col + (int64_t)sz * kk + dx + sy * dy);
+            t = load(col + (int64_t)sz * kk + dx + sy * dy);
           v[(dx + 1) + 3 * (dy + 1)] = t;
         }
     };
@@ -79,45 +95,70 @@ __device__ __forceinline__ void lattice_rows(const LatticeQ1Op& op, int bx, int 
         for (int cx = 0; cx < 2; ++cx)
           v[cx + 2 * cy] = __ldg(kcol + (int64_t)op.c2 * kk + cx + op.c1 * cy);
     };
-    float xa[9], xb[9], xc[9], ka[4], kb[4];
+    // Kref[a][b] depends only on the axes along which local vertices a and b differ (the Q1
+    // stiffness of a box is a sum of tensor products of 1-D [[p, q], [q, p]] matrices), so
+    //   (A x)_r = sum over the 8 axis classes c of W[c] sum_{d in c} S(d) x_{r+d},
+    // S(d) the kappa sum over the cells r and r + d share (a box of 1 or 2 cells per axis).
+    // Per row: 5 adds for the new cell layer's box sums, 9 to merge it with the layer below,
+    // 27 multiply-adds over the neighbours and 8 over the classes (49 FP32 operations
+    // instead of the 72 of a cell-by-cell Kref product).
+    float W[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) W[c] = op.K[8 * c];
+    // box sums of cell layer kk, indexed e = (dx + 1) + 3 (dy + 1)
+    auto layer = [&](int kk, float* L) {
+      float v[4];
+      kplane(kk, v);
+      const float X0 = v[0] + v[1], X1 = v[2] + v[3];
+      L[0] = v[0];
+      L[1] = X0;
+      L[2] = v[1];
+      L[3] = v[0] + v[2];
+      L[4] = X0 + X1;
+      L[5] = v[1] + v[3];
+      L[6] = v[2];
+      L[7] = X1;
+      L[8] = v[3];
+    };
+    float xa[9], xb[9], xc[9], la[9], lb[9];
     xplane(k0 - 1, xa);
     xplane(k0, xb);
-    kplane(k0, ka);
+    layer(k0, la);
 #pragma unroll
     for (int t = 0; t < KZ; ++t) {
       const int k = k0 + t;
       if (k < m2) {
         xplane(k + 1, xc);
-        kplane(k + 1, kb);
+        layer(k + 1, lb);
+        float T[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) T[c] = 0.f;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+          const int cl = (e % 3 != 1 ? 1 : 0) | (e / 3 != 1 ? 2 : 0);
+          T[cl | 4] = fmaf(la[e], xa[e], T[cl | 4]);
+          T[cl] = fmaf(la[e] + lb[e], xb[e], T[cl]);
+          T[cl | 4] = fmaf(lb[e], xc[e], T[cl | 4]);
+        }
         float acc = 0.f;
 #pragma unroll
-        for (int cz = 0; cz < 2; ++cz)
-#pragma unroll
-          for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-            for (int cx = 0; cx < 2; ++cx) {
-              const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
-              float s = 0.f;
-#pragma unroll
-              for (int lc = 0; lc < 8; ++lc) {
-                const int ix = cx + (lc & 1), iy = cy + ((lc >> 1) & 1), iz = cz + (lc >> 2);
-                const float xv = iz == 0 ? xa[ix + 3 * iy] : iz == 1 ? xb[ix + 3 * iy]
-                                                                     : xc[ix + 3 * iy];
-                s = fmaf(op.K[lr + 8 * lc], xv, s);
-              }
-              acc = fmaf(cz == 0 ? ka[cx + 2 * cy] : kb[cx + 2 * cy], s, acc);
-            }
+        for (int c = 0; c < 8; ++c) acc = fmaf(W[c], T[c], acc);
         epi(col + (int64_t)sz * k, xb[4], acc);
       }
 #pragma unroll
       for (int e = 0; e < 9; ++e) {
         xa[e] = xb[e];
         xb[e] = xc[e];
+        la[e] = lb[e];
       }
-#pragma unroll
-      for (int e = 0; e < 4; ++e) ka[e] = kb[e];
     }
   }
+}
+
+template <bool PAD, class Epi, int KZ = kLatK>
+__device__ __forceinline__ void lattice_rows(const LatticeQ1Op& op, int bx, int by, int bz,
+                                             const float* __restrict__ p, Epi& epi) {
+  lattice_rows_f<PAD, Epi, KZ>(op, bx, by, bz, LatticeLoad{p}, epi);
 }
 
 // q = A p over one tile; adds p.q (and p.r for flexible CG) of the thread's rows to d1 (d2).

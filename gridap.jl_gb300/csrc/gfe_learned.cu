@@ -311,18 +311,48 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (atomicCAS(&err->code, 0, GFE_ERR_TIMEOUT) == 0) err->index = blockIdx.x;
 }
 
-// z[d] = (1 / count) * sum of the block outputs at d, in block order; optional dot with q.
+// z[d] = base[d] + (1 / count) * sum of the block outputs at d, in block order (base may be
+// null: 0).
 __global__ void k_block_gather(int64_t n, const int64_t* __restrict__ dptr,
                                const int32_t* __restrict__ dref, const float* __restrict__ yblk,
-                               float* __restrict__ z, const int* skip) {
+                               const float* base, float* z, const int* skip) {
   if (skip && *skip) return;
   for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < n;
        d += (int64_t)gridDim.x * blockDim.x) {
     const int64_t a = dptr[d], e = dptr[d + 1];
     float acc = 0.f;
     for (int64_t k = a; k < e; ++k) acc += __ldg(yblk + dref[k]);
-    z[d] = e > a ? acc / (float)(e - a) : 0.f;
+    const float v = e > a ? acc / (float)(e - a) : 0.f;
+    z[d] = base ? base[d] + v : v;
   }
+}
+
+// Training samples from a residual / error pair (r, e = x* - x, both FP64, host or device) of
+// the method's own FP64 iterations: the network input as in k_samples, the target the error
+// patch e_b in the network's units (e_b / (s_b * bscale_b), s_b the RMS of the r patch).
+__global__ void k_samples_error(int64_t nsamples, const int64_t* __restrict__ ids,
+                                const int32_t* __restrict__ bdofs, const float* __restrict__ bfeat,
+                                const float* __restrict__ bscale, const double* __restrict__ r,
+                                const double* __restrict__ e, float* __restrict__ X,
+                                float* __restrict__ T) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t sidx = (int64_t)blockIdx.x * 4 + w;
+  if (sidx >= nsamples) return;
+  const int64_t b = ids[sidx];
+  const int32_t d = lane < kP ? bdofs[b * kP + lane] : -1;
+  const double rb = d >= 0 ? r[d] : 0.0, eb = d >= 0 ? e[d] : 0.0;
+  double ss = rb * rb;
+  for (int off = 16; off > 0; off >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, off);
+  const double sc = sqrt(ss / kP);
+  const double inv = sc > 0.0 ? 1.0 / sc : 0.0;
+  for (int k = lane; k < kIn; k += 32) {
+    float xk = 0.f;
+    if (k < kP) xk = (float)(__shfl_sync(0xffffffffu, rb, k) * inv);
+    else if (k < kP + kF) xk = bfeat[b * kF + (k - kP)];
+    X[sidx * kIn + k] = xk;
+  }
+  const double tscale = (sc > 0.0) ? 1.0 / (sc * (double)bscale[b]) : 0.0;
+  if (lane < kOut) T[sidx * kOut + lane] = lane < kP ? (float)(eb * tscale) : 0.f;
 }
 
 // ---- training samples ------------------------------------------------------------------------
@@ -510,8 +540,15 @@ __global__ void k_pack_weights(const float* __restrict__ p, uint8_t* __restrict_
 // ---- host --------------------------------------------------------------------------------
 using namespace learned;
 
+int64_t learned_ndofs(const gfe_learned_pc* pc) { return pc->ndofs; }
+
 int learned_apply(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, float* d_z,
                   const int* skip) {
+  return learned_apply_into(ctx, pc, d_r, nullptr, d_z, skip);
+}
+
+int learned_apply_into(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, const float* base,
+                       float* d_z, const int* skip) {
   if (!pc->has_weights) return set_error(GFE_ERR_INVALID_ARGUMENT, "learned pc: no weights");
   const size_t sm = sizeof(Smem) + 1024;
   auto kern = k_mlp_blocks;
@@ -523,8 +560,8 @@ int learned_apply(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, float* d_z
       pc->nblocks, pc->bdofs.as<int32_t>(), pc->bfeat.as<float>(), pc->bscale.as<float>(), d_r,
       pc->wpack.as<uint8_t>(), pc->params.as<float>(), pc->yblk.as<float>(), ctx->d_err, skip);
   k_block_gather<<<grid_for(pc->ndofs, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
-      pc->ndofs, pc->dptr.as<int64_t>(), pc->dref.as<int32_t>(), pc->yblk.as<float>(), d_z,
-      skip);
+      pc->ndofs, pc->dptr.as<int64_t>(), pc->dref.as<int32_t>(), pc->yblk.as<float>(), base,
+      d_z, skip);
   timer_end(ctx);
   ctx->launches += 2;
   GFE_CUDA_TRY(cudaGetLastError());
@@ -706,6 +743,29 @@ extern "C" int gfe_learned_pc_samples(gfe_learned_pc* pc, gfe_matrix* A, const d
       nsamples, (const int64_t*)dids, pc->bdofs.as<int32_t>(), pc->bfeat.as<float>(),
       pc->bscale.as<float>(), A->rowptr.as<int32_t>(), A->colval.as<int32_t>(),
       A->val.as<double>(), (const double*)dr, X, T);
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return GFE_OK;
+}
+
+extern "C" int gfe_learned_pc_samples_error(gfe_learned_pc* pc, const double* r,
+                                            const double* e, int64_t nsamples,
+                                            const int64_t* block_ids, float* X, float* T) {
+  clear_error();
+  if (!pc || !r || !e || nsamples < 0 || !block_ids || !X || !T)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_learned_pc_samples_error: bad arguments");
+  gfe_ctx* ctx = pc->ctx;
+  if (nsamples == 0) return GFE_OK;
+  const void *dr, *de, *dids;
+  GFE_TRY(device_view(ctx, r, sizeof(double) * pc->ndofs, SCR_TMP2, &dr));
+  GFE_TRY(device_view(ctx, e, sizeof(double) * pc->ndofs, SCR_TMP1, &de));
+  GFE_TRY(device_view(ctx, block_ids, sizeof(int64_t) * nsamples, SCR_TMP3, &dids));
+  if (!is_device_ptr(X) || !is_device_ptr(T))
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_learned_pc_samples_error: X, T device memory");
+  k_samples_error<<<(unsigned)((nsamples + 3) / 4), 128, 0, ctx->stream>>>(
+      nsamples, (const int64_t*)dids, pc->bdofs.as<int32_t>(), pc->bfeat.as<float>(),
+      pc->bscale.as<float>(), (const double*)dr, (const double*)de, X, T);
   ctx->launches++;
   GFE_CUDA_TRY(cudaGetLastError());
   GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));

@@ -44,6 +44,22 @@ __global__ void __launch_bounds__(kMgBlock)
                                          (int)blockIdx.z, x, epi);
 }
 
+// The first two sweeps in one pass: x0 = omega D^-1 b (the sweep from zero, formed on the fly
+// at the neighbours) and xo = x0 + omega D^-1 (b - A x0). x0 itself is not stored: the cycle
+// reads only xo afterwards.
+template <int KZ>
+__global__ void __launch_bounds__(kMgBlock)
+    k_mg_pre(LatticeQ1Op op, const float* __restrict__ b, const float* __restrict__ dinv,
+             float* __restrict__ xo, const int* done) {
+  if (stop(done)) return;
+  const LatticeLoadJacobi0 x0{b, dinv, kOmega};
+  auto epi = [&](int64_t row, float xc, float acc) {
+    xo[row] = fmaf(kOmega * __ldg(dinv + row), __ldg(b + row) - acc, xc);
+  };
+  lattice_rows_f<false, decltype(epi), KZ>(op, (int)blockIdx.x, (int)blockIdx.y,
+                                           (int)blockIdx.z, x0, epi);
+}
+
 // r = b - A x (the residual the restriction takes to the coarse level)
 template <int KZ>
 __global__ void __launch_bounds__(kMgBlock)
@@ -206,9 +222,10 @@ struct CoarseLevels {
 
 // (A p)_r at interior node (i, j, k): its 27 neighbours loaded once (0 outside the interior),
 // then the 8 cells around it, 8 local columns each, in lattice_rows' order (32-bit indexing:
-// these levels are small)
-__device__ __forceinline__ float lattice_row_value(const LatticeQ1Op& op, int i, int j, int k,
-                                                   const float* __restrict__ p) {
+// these levels are small). `load(row)` gives p at a row.
+template <class Load>
+__device__ __forceinline__ float lattice_row_value_f(const LatticeQ1Op& op, int i, int j, int k,
+                                                     const Load& load) {
   const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
   float v[27];
 #pragma unroll
@@ -219,7 +236,7 @@ __device__ __forceinline__ float lattice_row_value(const LatticeQ1Op& op, int i,
       for (int dx = 0; dx < 3; ++dx) {
         const int ii = i - 1 + dx, jj = j - 1 + dy, kk = k - 1 + dz;
         const bool in = ii >= 0 && ii < m0 && jj >= 0 && jj < m1 && kk >= 0 && kk < m2;
-        v[dx + 3 * dy + 9 * dz] = in ? p[ii + op.s1 * jj + op.s2 * kk] : 0.f;
+        v[dx + 3 * dy + 9 * dz] = in ? load(ii + op.s1 * jj + op.s2 * kk) : 0.f;
       }
   float acc = 0.f;
 #pragma unroll
@@ -237,6 +254,11 @@ __device__ __forceinline__ float lattice_row_value(const LatticeQ1Op& op, int i,
         acc = fmaf(op.kap[(i + cx) + op.c1 * (j + cy) + op.c2 * (k + cz)], s, acc);
       }
   return acc;
+}
+
+__device__ __forceinline__ float lattice_row_value(const LatticeQ1Op& op, int i, int j, int k,
+                                                   const float* __restrict__ p) {
+  return lattice_row_value_f(op, i, j, k, [p](int row) { return p[row]; });
 }
 
 __device__ __forceinline__ void row_ijk(const MgLevelView& L, int64_t r, int& i, int& j,
@@ -338,6 +360,7 @@ struct LatticeMG {
   float* cap_z = nullptr;
   const int* cap_done = nullptr;
   long long nodes = 0;
+  gfe_learned_pc* learned = nullptr;  // the fine level's smoother when set
   explicit LatticeMG(gfe_ctx* c) : ctx(c), buf(c) {}
   ~LatticeMG() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -387,9 +410,39 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
       k_mg_smooth<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, xi, L.b, L.dinv, xo, done);
     ctx->launches++;
   };
-  k_mg_jacobi0<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.dinv, cur, done);
+  if (l == 0 && mg->learned && !coarsest) {
+    // learned smoothing on the fine level: x = M(b); r = b - A x to the coarse level;
+    // t = x + P x_c; x = t + M(b - A t)
+    LatticeMG::Level& C = mg->lv[l + 1];
+    GFE_TRY(learned_apply_into(ctx, mg->learned, L.b, nullptr, L.x, done));
+    if (deep)
+      k_mg_residual<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.b, L.t, done);
+    else
+      k_mg_residual<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.b, L.t, done);
+    k_mg_restrict<<<vgrid(ctx, C.n), kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, C.m0, C.m1, C.m2,
+                                                                 L.t, C.b, done);
+    ctx->launches += 2;
+    GFE_TRY(vcycle(mg, l + 1, done));
+    k_mg_prolong<<<g, kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, L.m2, C.m0, C.m1, C.m2, C.x, L.x,
+                                                  L.t, done);
+    if (deep)
+      k_mg_residual<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.t, L.b, L.x, done);
+    else
+      k_mg_residual<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, L.t, L.b, L.x, done);
+    ctx->launches += 2;
+    return learned_apply_into(ctx, mg->learned, L.x, L.t, L.x, done);
+  }
+  if (pre >= 2) {  // the sweep from zero and the next one in one pass
+    if (deep)
+      k_mg_pre<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.b, L.dinv, oth, done);
+    else
+      k_mg_pre<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, L.b, L.dinv, oth, done);
+    std::swap(cur, oth);
+  } else {
+    k_mg_jacobi0<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.dinv, cur, done);
+  }
   ctx->launches++;
-  for (int s = 1; s < pre; ++s) {
+  for (int s = 2; s < pre; ++s) {
     smooth(cur, oth);
     std::swap(cur, oth);
   }
@@ -519,6 +572,19 @@ int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done) {
   GFE_CUDA_TRY(cudaGraphLaunch(mg->exec, ctx->stream));
   timer_end(ctx);
   ctx->launches += mg->nodes;
+  return GFE_OK;
+}
+
+int mg_set_learned(LatticeMG* mg, gfe_learned_pc* pc) {
+  if (pc && learned_ndofs(pc) != mg->lv[0].n)
+    return set_error(GFE_ERR_INVALID_ARGUMENT, "multigrid: the learned smoother covers %lld "
+                     "dofs, the fine level %lld", (long long)learned_ndofs(pc),
+                     (long long)mg->lv[0].n);
+  if (mg->learned != pc && mg->exec) {
+    cudaGraphExecDestroy(mg->exec);
+    mg->exec = nullptr;
+  }
+  mg->learned = pc;
   return GFE_OK;
 }
 

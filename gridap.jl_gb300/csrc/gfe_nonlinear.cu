@@ -681,6 +681,7 @@ int assemble_quasilinear(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, doub
   s.vcs = 1;
   s.ves = ncells;
   s.ntab = 0;
+  GFE_TRY(ensure_row_refs(ctx, R));
   RowArgs a = row_args(ctx, R, d_b, A != nullptr);
   a.uD = nullptr;
   a.ndiri = 0;

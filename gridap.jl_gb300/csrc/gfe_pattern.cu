@@ -726,6 +726,42 @@ __global__ void k_cart_cols(int64_t nrows, int m0, int m1, int m2,
   }
 }
 
+int cartesian_ids_match(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1, int64_t n2,
+                        bool* ok) {
+  *ok = false;
+  if (A->nd != 8 || A->cols_per_cell() != 8 || A->has_lmask || n0 < 2 || n1 < 2 || n2 < 2 ||
+      A->ncells != n0 * n1 * n2 || A->nrows != (n0 - 1) * (n1 - 1) * (n2 - 1) ||
+      A->ncols != A->nrows || n0 * n1 * n2 * 8 > (int64_t)INT32_MAX)
+    return GFE_OK;
+  DevBuf flag(ctx);
+  GFE_TRY(flag.reserve(sizeof(int)));
+  GFE_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
+  k_cart_check<<<grid_for(A->ncells, 256, (int64_t)ctx->num_sms * 16), 256, 0, ctx->stream>>>(
+      A->cell_rows.as<int32_t>(), A->cell_cols.as<int32_t>(), (int)n0, (int)n1, (int)n2,
+      flag.as<int>());
+  ctx->launches++;
+  int bad = 1;
+  GFE_TRY(copy_out(ctx, &bad, flag.ptr, sizeof(int)));
+  *ok = bad == 0;
+  return GFE_OK;
+}
+
+int ensure_row_refs(gfe_ctx* ctx, gfe_matrix* A) {
+  if (!A || !A->refs_pending) return GFE_OK;
+  const int64_t n0 = A->cart_n[0], n1 = A->cart_n[1], n2 = A->cart_n[2];
+  const int64_t m0 = n0 - 1, m1 = n1 - 1, m2 = n2 - 1, nrows = A->nrows;
+  GFE_TRY(A->ref_ptr.reserve(sizeof(int64_t) * (nrows + 1)));
+  GFE_TRY(A->refs.reserve(sizeof(int32_t) * (size_t)(A->nrefs > 0 ? A->nrefs : 1)));
+  GFE_TRY(A->refpos.reserve((size_t)8 * (A->nrefs > 0 ? A->nrefs : 1)));
+  k_cart_refs<<<grid_for(8 * nrows, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
+      nrows, (int)n0, (int)n1, (int)m0, (int)m1, (int)m2, A->ref_ptr.as<int64_t>(),
+      A->refs.as<int32_t>(), A->refpos.as<uint64_t>());
+  ctx->launches++;
+  GFE_CUDA_TRY(cudaGetLastError());
+  A->refs_pending = false;
+  return GFE_OK;
+}
+
 int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1, int64_t n2,
                             bool* done) {
   *done = false;
@@ -762,23 +798,24 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
   A->nnz = nnz;
   A->max_width = (int)((m0 < 3 ? m0 : 3) * (m1 < 3 ? m1 : 3) * (m2 < 3 ? m2 : 3));
   A->pos_bytes = 1;
-  GFE_TRY(A->ref_ptr.reserve(sizeof(int64_t) * (nrows + 1)));
-  GFE_TRY(A->refs.reserve(sizeof(int32_t) * (size_t)(A->nrefs > 0 ? A->nrefs : 1)));
-  GFE_TRY(A->refpos.reserve((size_t)8 * (A->nrefs > 0 ? A->nrefs : 1)));
   GFE_TRY(A->rowptr.reserve(sizeof(int32_t) * (nrows + 1)));
   GFE_TRY(A->colval.reserve(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
   GFE_TRY(A->val.reserve(sizeof(double) * (nnz > 0 ? nnz : 1)));
-  k_cart_refs<<<grid_for(8 * nrows, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
-      nrows, (int)n0, (int)n1, (int)m0, (int)m1, (int)m2, A->ref_ptr.as<int64_t>(),
-      A->refs.as<int32_t>(), A->refpos.as<uint64_t>());
+  // the row references and positions are written when a row gather first needs them
+  // (ensure_row_refs); the class-sum assembly of this pattern does not read them
+  A->refs_pending = true;
   k_cart_cols<<<grid_for(32 * nrows, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
       nrows, (int)m0, (int)m1, (int)m2, rowptr64.as<int64_t>(), A->colval.as<int32_t>());
-  ctx->launches += 2;
+  ctx->launches += 1;
   GFE_TRY(narrow_i64_to_i32(ctx, rowptr64.as<int64_t>(), A->rowptr.as<int32_t>(), nrows + 1));
   GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * (nnz > 0 ? nnz : 1),
                                ctx->stream));
   GFE_CUDA_TRY(cudaGetLastError());
   A->plan_valid = false;
+  A->cart_lattice = true;
+  A->cart_n[0] = n0;
+  A->cart_n[1] = n1;
+  A->cart_n[2] = n2;
   *done = true;
   return GFE_OK;
 }

@@ -1067,6 +1067,75 @@ __global__ void __launch_bounds__(kSpmvBlock)
     *out_rr = tot[0];
 }
 
+// The same FP64 residual for a matrix with the closed-form lattice pattern of a 3-D
+// Cartesian Q1 grid (rows = interior nodes in node order, each row's columns its interior
+// neighbours among the 27 in (dz, dy, dx) order): the column ids follow from the row's
+// position, so only the values stream from memory (8 instead of 12 bytes per entry). A warp
+// takes 32 consecutive rows of one x-line, whose values are one contiguous slice: it copies
+// the slice into shared memory with coalesced loads, then each lane forms its row from there
+// with the neighbours' x. Persistent grid; x-lines dealt to warps in a fixed order, so the
+// reduction is deterministic.
+__global__ void __launch_bounds__(kSpmvBlock)
+    k_residual64_lattice(int m0, int m1, int m2, const int32_t* __restrict__ rowptr,
+                         const double* __restrict__ val, const double* __restrict__ x,
+                         const double* __restrict__ b, double* __restrict__ r,
+                         double* __restrict__ partials, double* out_rr, unsigned* ticket) {
+  extern __shared__ double stage_all[];
+  __shared__ double sh[kSpmvBlock / 32];
+  const int lane = (int)(threadIdx.x & 31), wib = (int)(threadIdx.x >> 5);
+  double* stage = stage_all + wib * (32 * 27);
+  const int tx = (m0 + 31) / 32;
+  const int64_t ntask = (int64_t)tx * m1 * m2;
+  const int64_t nwarps = (int64_t)gridDim.x * (kSpmvBlock / 32);
+  const int64_t sy = m0, sz = (int64_t)m0 * m1;
+  double d = 0.0;
+  for (int64_t task = (int64_t)blockIdx.x * (kSpmvBlock / 32) + wib; task < ntask;
+       task += nwarps) {
+    const int64_t line = task / tx;
+    const int i = (int)(task - line * tx) * 32 + lane;
+    const int k = (int)(line / m1), j = (int)(line - (int64_t)k * m1);
+    const bool act = i < m0;
+    const int64_t row = (int64_t)(act ? i : m0 - 1) + sy * j + sz * k;
+    int32_t rp = 0, rpn = 0;
+    if (act) {
+      rp = __ldg(rowptr + row);
+      rpn = __ldg(rowptr + row + 1);
+    }
+    const int32_t rp0 = __shfl_sync(0xffffffffu, rp, 0);
+    int32_t rend = rpn;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      rend = max(rend, __shfl_xor_sync(0xffffffffu, rend, off));
+    for (int q = lane; q < rend - rp0; q += 32) stage[q] = __ldcs(val + rp0 + q);
+    __syncwarp();
+    if (act) {
+      const bool okx[3] = {i > 0, true, i < m0 - 1};
+      const bool oky[3] = {j > 0, true, j < m1 - 1};
+      const bool okz[3] = {k > 0, true, k < m2 - 1};
+      int pos = rp - rp0;
+      double s = 0.0;
+#pragma unroll
+      for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+        for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+          for (int dx = 0; dx < 3; ++dx)
+            if (okz[dz] && oky[dy] && okx[dx])
+              s = fma(stage[pos++], __ldg(x + row + (dx - 1) + sy * (dy - 1) + sz * (dz - 1)), s);
+      const double ri = b[row] - s;
+      r[row] = ri;
+      d = fma(ri, ri, d);
+    }
+    __syncwarp();
+  }
+  d = block_sum<kSpmvBlock>(d, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = d;
+  double tot[1];
+  if (last_block_reduce<kSpmvBlock, 1>(ticket, partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0)
+    *out_rr = tot[0];
+}
+
 // x64 += s * d32
 __global__ void k_refine_update(int64_t n, double* __restrict__ x, const float* __restrict__ d,
                                 double s) {
@@ -1846,8 +1915,19 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   const float* dinv32 = csr_residual ? nullptr : A->dinv32.as<float>();
   const unsigned gv = (unsigned)(ctx->num_sms * 4), gs = grid_for(n, kSpmvBlock);
   // r64 = b - A x64 in FP64, r64.r64 into *rr
+  const size_t lat_smem = sizeof(double) * 32 * 27 * (kSpmvBlock / 32);
+  if (A->cart_lattice)
+    GFE_CUDA_TRY(cudaFuncSetAttribute(k_residual64_lattice,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)lat_smem));
   auto residual64 = [&](double* rr) {
-    if (csr_residual)
+    if (A->cart_lattice)
+      k_residual64_lattice<<<(unsigned)(ctx->num_sms * 4), kSpmvBlock, lat_smem,
+                             ctx->stream>>>((int)A->cart_n[0] - 1, (int)A->cart_n[1] - 1,
+                                            (int)A->cart_n[2] - 1, A->rowptr.as<int32_t>(),
+                                            A->val.as<double>(), d_x, d_b, r64, w.partials, rr,
+                                            &w.S->ticket[2]);
+    else if (csr_residual)
       k_residual64_csr<4><<<(unsigned)(ctx->num_sms * 8), kSpmvBlock, 0, ctx->stream>>>(
           n, A->rowptr.as<int32_t>(), A->colval.as<int32_t>(), A->val.as<double>(), d_x, d_b,
           r64, w.partials, rr, &w.S->ticket[2]);
@@ -1860,8 +1940,11 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   // multigrid preconditioner, which gains about a decade per iteration: two FP64 residuals
   // reach 1e-8 at 128^3, with the same iterations and error as 1e-3's three)
   const double delta = o->inner_rtol > 0 ? o->inner_rtol
-                                         : (pc == nullptr && o->precond == GFE_PC_MG ? 1e-4 : 0.1);
+                                         : (o->precond == GFE_PC_MG ? 1e-4 : 0.1);
   bool learned = pc != nullptr;
+  // the preconditioner in use: the V-cycle (its fine-level smoother learned when pc is
+  // given), the learned block preconditioner alone, or Jacobi (also after a fallback)
+  bool use_mg = o->precond == GFE_PC_MG;
   DiaOp<float> dop{A->dia_val32.as<float>(), n, {}};
   for (int d = 0; d < A->dia_ndiag; ++d) dop.o.off[d] = A->dia_off[d];
   dop.o.nd = A->dia_ndiag;
@@ -1890,18 +1973,19 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       if (*p) mg_destroy(*p);
     }
   } mg_release{&mg};
-  if (!learned && o->precond == GFE_PC_MG) {
+  if (use_mg) {
     if (!lattice)
       return set_error(GFE_ERR_UNSUPPORTED,
                        "solve: the multigrid preconditioner needs the lattice operator "
                        "(uniform Cartesian Q1, 3-D, interior-node numbering)");
     GFE_TRY(mg_create(ctx, lop, &mg));
+    if (learned) GFE_TRY(mg_set_learned(mg, pc));
     // a V-cycle iteration is expensive: look at the state after every one
     if (o->check_every <= 0) check_every = 1;
   }
   auto precond = [&]() -> int {
+    if (use_mg) return mg_apply(mg, r32, z32, &w.S->done);
     if (learned) return learned_apply(ctx, pc, r32, z32, &w.S->done);
-    if (mg) return mg_apply(mg, r32, z32, &w.S->done);
     k_jacobi_apply<<<gv, kVecBlock, 0, ctx->stream>>>(n, r32, dinv32, z32, w.S);
     ctx->launches++;
     return GFE_OK;
@@ -1964,11 +2048,13 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       continue;
     }
     if (w.hS->done) break;
-    // stagnation check of the learned preconditioner
+    // stagnation check of the learned preconditioner (alone, or as the V-cycle's smoother)
     if (learned) {
-      slow = (w.hS->rr > 0.25 * rr_chunk) ? slow + 1 : 0;
+      // less than a 4x residual drop per 10 iterations, scaled to the chunk's length
+      slow = (w.hS->rr > std::pow(0.25, check_every / 10.0) * rr_chunk) ? slow + 1 : 0;
       if (slow >= 2) {
         learned = false;  // Jacobi from here on
+        use_mg = false;
         fallback = 1;
       }
     }

@@ -85,17 +85,23 @@ class BiCGStabSolver(LinearSolver):
 class FCGSolver(LinearSolver):
     """Flexible CG with FP32 vectors and FP64 reliable updates, preconditioned by a
     LearnedBlockPreconditioner (`pc`), by a geometric multigrid V-cycle on the lattice
-    operator (pc="mg"; uniform Cartesian Q1 in 3-D) or by Jacobi (pc=None); a stagnating
-    learned preconditioner hands over to Jacobi (report.fallback)."""
+    operator (pc="mg"; uniform Cartesian Q1 in 3-D), by the V-cycle with the learned
+    preconditioner as its fine-level smoother (pc=learned, multigrid=True) or by Jacobi
+    (pc=None); a stagnating learned preconditioner hands over to Jacobi (report.fallback)."""
 
     def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, pc=None,
-                 inner_rtol: float = 0.0, check_every: int = 0, initial_guess: bool = False):
-        # inner_rtol 0: the library's reliable-update threshold (0.1; 1e-4 with pc="mg")
+                 inner_rtol: float = 0.0, check_every: int = 0, initial_guess: bool = False,
+                 multigrid: bool = False):
+        # inner_rtol 0: the library's reliable-update threshold (0.1; 1e-4 with multigrid)
         super().__init__(rtol, maxiter, "jacobi", inner_rtol, check_every, initial_guess)
         if isinstance(pc, str):
             if pc != "mg":
                 raise ValueError(f"unknown preconditioner {pc!r}")
             self.precond, pc = _lib.GFE_PC_MG, None
+        if multigrid:
+            if pc is None:
+                raise ValueError("multigrid=True takes the learned smoother as pc (or pc=\"mg\")")
+            self.precond = _lib.GFE_PC_MG
         self.pc = pc
 
 

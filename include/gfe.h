@@ -504,16 +504,27 @@ int gfe_learned_pc_apply(gfe_learned_pc* pc, const float* r, float* z);
  * A_b^{-1} r_b in FP64, in the network's normalised units. X and T are device arrays. */
 int gfe_learned_pc_samples(gfe_learned_pc* pc, gfe_matrix* A, const double* r,
                            int64_t nsamples, const int64_t* block_ids, float* X, float* T);
+/* Training samples from a residual / error pair of the method's own FP64 iterations: r = b - A x
+ * and e = x* - x (x* the FP64 solution; both FP64, host or device, nfree entries): for each
+ * listed block the network input (48 floats, as above) and the target e_b (32 floats) in the
+ * network's units. The targets a smoother of the V-cycle learns. X and T are device arrays.
+ * No counterpart in Gridap. */
+int gfe_learned_pc_samples_error(gfe_learned_pc* pc, const double* r, const double* e,
+                                 int64_t nsamples, const int64_t* block_ids, float* X, float* T);
 /* Adam on the mean squared error over (X, T) (device, n rows), `epochs` passes of minibatches
  * of `batch` rows; initialises the weights when the pc has none. *loss = last epoch's mean. */
 int gfe_learned_pc_train(gfe_learned_pc* pc, const float* X, const float* T, int64_t n,
                          int32_t epochs, int32_t batch, float lr, uint64_t seed, float* loss);
-/* Flexible CG (FCG(1)) with FP32 vectors and FP64 reliable updates, preconditioned by the
- * learned block preconditioner (pc != NULL), by the geometric multigrid V-cycle on the lattice
- * operator (pc == NULL, opts->precond == GFE_PC_MG; GFE_ERR_UNSUPPORTED without the lattice
- * form) or by Jacobi; stagnation of the learned preconditioner switches to Jacobi
- * (report->fallback = 1). opts->inner_rtol is the residual reduction between reliable
- * updates; stops on the FP64 relative residual. */
+/* Flexible CG (FCG(1)) with FP32 vectors and FP64 reliable updates, preconditioned by
+ *  - the geometric multigrid V-cycle on the lattice operator (opts->precond == GFE_PC_MG;
+ *    GFE_ERR_UNSUPPORTED without the lattice form), whose fine-level smoother is the learned
+ *    block preconditioner when pc != NULL (pre-smoothing x = M(b), post-smoothing
+ *    x += M(b - A x); coarser levels damped Jacobi),
+ *  - the learned block preconditioner alone (pc != NULL, another precond), or
+ *  - Jacobi.
+ * A learned preconditioner that stagnates (less than a 4x residual drop per 10 iterations,
+ * twice in a row) hands over to Jacobi (report->fallback = 1). opts->inner_rtol is the
+ * residual reduction between reliable updates; stops on the FP64 relative residual. */
 int gfe_solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_opts* opts,
                   const double* b, double* x, gfe_solve_report* report);
 

@@ -218,4 +218,6 @@ def main(ref: pathlib.Path):
 
 
 if __name__ == "__main__":
-    main(pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/extract_kats.py <path to a Gridap.jl v0.20.8 checkout>")
+    main(pathlib.Path(sys.argv[1]))

@@ -22,7 +22,7 @@ def _solve(gg, A, b, solver):
 
 @pytest.mark.parametrize("part,sigma", [((32, 32, 32), 1.5), ((48, 40, 32), 2.5),
                                         ((30, 28, 26), 1.0), ((21, 18, 16), 1.0)])
-def test_mg_fcg_meets_fp64_tolerance(gg, part, sigma):
+def test_mg_fcg_meets_fp64_tolerance(gg, orc, part, sigma):
     rng = np.random.default_rng(sum(part))
     kappa = np.exp(sigma * rng.standard_normal(int(np.prod(part))))
     fnod = rng.standard_normal(int(np.prod(np.array(part) + 1)))
@@ -33,6 +33,14 @@ def test_mg_fcg_meets_fp64_tolerance(gg, part, sigma):
     r = b - A.to_scipy() @ x
     assert np.linalg.norm(r) <= 1.01e-8 * np.linalg.norm(b)
     assert np.linalg.norm(x - x64) <= 1e-5 * np.linalg.norm(x64)
+    # against the oracle's own system and its Jacobi-PCG solution (FP64, 1e-10)
+    ref = orc.poisson_q1((0, 1) * 3, part, ("boundary",), kappa=kappa, fkind=orc.F_NODAL,
+                         fdata=fnod)
+    ro = ref["b"] - orc.csc_mul(*ref["csc"], x)
+    assert np.linalg.norm(ro) <= 1.01e-8 * np.linalg.norm(ref["b"])
+    xo, _, rro = orc.pcg(*ref["csc"], ref["b"], 1e-10)
+    assert rro <= 1e-10
+    assert np.linalg.norm(x - xo) <= 1e-5 * np.linalg.norm(xo)
     if part[0] % 4 == 0:  # at least three levels
         assert rep.iterations < 0.25 * r64.iterations
 

@@ -336,8 +336,10 @@ def run_gpu(args):
             o = solver.opts()
             rep = _lib.SolveReport()
             if isinstance(solver, gg.FCGSolver):
-                _lib.check(lib.gfe_solve_fcg(ctx.handle, h, None, ctypes.byref(o), _lib.ptr(b),
-                                             _lib.ptr(x), ctypes.byref(rep)))
+                _lib.check(lib.gfe_solve_fcg(ctx.handle, h,
+                                             solver.pc.handle if solver.pc is not None else None,
+                                             ctypes.byref(o), _lib.ptr(b), _lib.ptr(x),
+                                             ctypes.byref(rep)))
             else:
                 _lib.check(lib.gfe_solve(ctx.handle, h, ctypes.byref(o), _lib.ptr(b),
                                          _lib.ptr(x), ctypes.byref(rep)))
@@ -439,50 +441,42 @@ def run_gpu(args):
     learned_out = None
     from gridap_gb300 import learned as learned_mod
     if learned_mod.WEIGHTS_FILE.exists() and not args.no_learned:
+        # the learned preconditioner (weights trained offline on residual / error pairs of FP64
+        # solves of 64^3 draws): as the fine-level smoother of the V-cycle (the learned arm),
+        # alone, and beside them FCG with Jacobi and with the Jacobi-smoothed V-cycle; every
+        # arm is the same step as the headline (pattern, FP64 assembly, solve to 1e-8)
         pc = learned_mod.LearnedBlockPreconditioner(V, w.kappa, ctx)
         pc.load_default_weights()
-        fcg_l = gg.FCGSolver(rtol=w.rtol, pc=pc)
-        fcg_j = gg.FCGSolver(rtol=w.rtol, pc=None)
-
-        def fcg_step(solver):
-            prep = problem(ids_d, kap_d, f_d)
-            h = ctypes.c_void_p()
-            _lib.check(lib.gfe_symbolic_loop_matrix(ctx.handle, ncells, nd, _lib.ptr(ids_d),
-                                                    _lib.ptr(ids_d), nfree, nfree,
-                                                    ctypes.byref(h)))
-            try:
-                _lib.check(lib.gfe_assemble_matrix_and_vector(ctx.handle, ctypes.byref(prep.p),
-                                                              h, _lib.ptr(b_d)))
-                o = solver.opts()
-                rep = _lib.SolveReport()
-                _lib.check(lib.gfe_solve_fcg(ctx.handle, h, solver.pc.handle if solver.pc else
-                                             None, ctypes.byref(o), _lib.ptr(b_d), _lib.ptr(x_d),
-                                             ctypes.byref(rep)))
-            finally:
-                lib.gfe_matrix_destroy(h)
-            return rep
-
-        fcg_mg = gg.FCGSolver(rtol=w.rtol, pc="mg")
-        r_mg = timed("mg_fcg", lambda: fcg_step(fcg_mg), args.steps, 3, kernel_timing=False)
-        rmg = r_mg["reps"][-1]
-        r_l = timed("learned", lambda: fcg_step(fcg_l), args.steps, 3)
-        r_j = timed("fcg_jacobi", lambda: fcg_step(fcg_j), args.steps, 3)
-        rl, rj = r_l["reps"][-1], r_j["reps"][-1]
-        learned_out = {
-            "value": world * nfree / (r_l["ms"] * 1e-3), "ms_per_step": r_l["ms"],
-            "iterations": rl.iterations, "fallback_to_jacobi": bool(rl.fallback),
-            "relres": rl.relres,
-            "precond_ms_per_apply": (r_l["kt"][_lib.GFE_KT_PRECOND][0] /
-                                     max(r_l["kt"][_lib.GFE_KT_PRECOND][1], 1)),
-            "fcg_jacobi": {"value": world * nfree / (r_j["ms"] * 1e-3), "ms_per_step": r_j["ms"],
-                           "iterations": rj.iterations, "relres": rj.relres},
-            "fcg_multigrid": {"value": world * nfree / (r_mg["ms"] * 1e-3),
-                              "ms_per_step": r_mg["ms"], "iterations": rmg.iterations,
-                              "relres": rmg.relres,
-                              "preconditioner": "geometric multigrid V-cycle on the lattice "
-                                                "operator (FP32, 2+2 damped Jacobi sweeps)"},
-            "training": "residual/local-solve pairs from FP64 Jacobi-PCG solves of 200 "
-                        "independent 64^3 kappa draws (seeds 5000..5199)"}
+        arms = {"learned_mg": gg.FCGSolver(rtol=w.rtol, pc=pc, multigrid=True),
+                "learned_alone": gg.FCGSolver(rtol=w.rtol, pc=pc),
+                "fcg_jacobi": gg.FCGSolver(rtol=w.rtol, pc=None),
+                "fcg_multigrid": gg.FCGSolver(rtol=w.rtol, pc="mg")}
+        res = {}
+        for name, solver in arms.items():
+            r = timed(name, lambda: step(ids_d, kap_d, f_d, x_d, solver, b_d), args.steps, 3,
+                      kernel_timing=False)
+            rep = r["reps"][-1]
+            res[name] = {"value": world * nfree / (r["ms"] * 1e-3), "ms_per_step": r["ms"],
+                         "iterations": rep.iterations, "relres": rep.relres,
+                         "fallback_to_jacobi": bool(rep.fallback)}
+        r_kt = timed("learned_mg_kt", lambda: step(ids_d, kap_d, f_d, x_d, arms["learned_mg"],
+                                                    b_d), 1, 1)
+        lm = res["learned_mg"]
+        learned_out = dict(lm)
+        learned_out.update({
+            "solver": "flexible CG (FP32 inner, FP64 reliable updates) preconditioned by the "
+                      "multigrid V-cycle whose fine-level smoother is the learned block MLP "
+                      "(BF16 on tcgen05): pre x = M(b), post x += M(b - A x); coarser levels "
+                      "damped Jacobi; Jacobi-PCG fallback on stagnation",
+            "precond_ms_per_apply": (r_kt["kt"][_lib.GFE_KT_PRECOND][0] /
+                                     max(r_kt["kt"][_lib.GFE_KT_PRECOND][1], 1)),
+            "learned_alone": res["learned_alone"], "fcg_jacobi": res["fcg_jacobi"],
+            "fcg_multigrid": dict(res["fcg_multigrid"], preconditioner=(
+                "geometric multigrid V-cycle on the lattice operator (FP32, 2+2 damped Jacobi "
+                "sweeps)")),
+            "training": "residual / error pairs (r_k = b - A x_k, e_k = x* - x_k) of FP64 CG "
+                        "iterates from x* + white noise (k = 0, 1, 2, 4), x* the FP64 solution, "
+                        "on 200 independent 64^3 kappa draws (seeds 5000..5199)"})
 
     # dominant kernel: the CG SpMV, timed with CUDA events inside the timed regions
     def avg_ms(r, k):
@@ -613,7 +607,8 @@ def run_gpu(args):
                                    "avg_launch_ms": prof["fp64_ms"],
                                    "traffic": profile_traffic("fp64_sell")}},
         "assembly": {"row_gather_ms": prof["assemble_ms"]},
-        "learned_fcg": learned_out,
+        "learned_fcg": (dict(learned_out, over_plain_fp64=learned_out["value"] / plain_value)
+                        if learned_out else None),
         "gpu_launches": r_mixed["launches"],
         "clocks": clk.summary(),
     }
@@ -838,11 +833,12 @@ def bench_q2(args, gg, ctx, lib, timed):
     ids_d = torch.from_numpy(V.cell_dof_ids).to(dev)
     b = torch.zeros(nfree, dtype=torch.float64, device=dev)
     x = torch.zeros(nfree, dtype=torch.float64, device=dev)
-    solver = gg.MixedCGSolver(rtol=1e-8)
+    solvers = {"mixed_cg": gg.MixedCGSolver(rtol=1e-8), "pmg_fcg": gg.FCGSolver(rtol=1e-8, pc="mg")}
     preps = {p: gg.prepare_problem(V, V, dO, 1.0, 1.0, precision=p) for p in ("fp64", "fp32")}
     vals = {}
 
-    def step(prec, keep=False):
+    def step(prec, keep=False, solver_name="pmg_fcg"):
+        solver = solvers[solver_name]
         h = ctypes.c_void_p()
         _lib.check(lib.gfe_symbolic_loop_matrix(ctx.handle, ncells, nd, _lib.ptr(ids_d),
                                                 _lib.ptr(ids_d), nfree, nfree, ctypes.byref(h)))
@@ -854,15 +850,21 @@ def bench_q2(args, gg, ctx, lib, timed):
                 vals["b_" + prec] = b.cpu().numpy().copy()
             o = solver.opts()
             rep = _lib.SolveReport()
-            _lib.check(lib.gfe_solve(ctx.handle, h, ctypes.byref(o), _lib.ptr(b), _lib.ptr(x),
-                                     ctypes.byref(rep)))
+            if isinstance(solver, gg.FCGSolver):
+                _lib.check(lib.gfe_solve_fcg(ctx.handle, h, None, ctypes.byref(o), _lib.ptr(b),
+                                             _lib.ptr(x), ctypes.byref(rep)))
+            else:
+                _lib.check(lib.gfe_solve(ctx.handle, h, ctypes.byref(o), _lib.ptr(b),
+                                         _lib.ptr(x), ctypes.byref(rep)))
         finally:
             lib.gfe_matrix_destroy(h)
         return rep
 
     out = {"workload": f"{args.q2_n}^3 Q2 Poisson, jittered nodes (+-0.2h), degree 4",
            "free_dofs": nfree, "cells": ncells,
-           "solver": "mixed CG (FP32 inner, FP64 reliable updates), Jacobi, 1e-8"}
+           "solver": "flexible CG (FP32 inner, FP64 reliable updates) with the p-multigrid "
+                     "preconditioner (damped Jacobi on Q2, Q1 lattice V-cycle below), 1e-8; "
+                     "mixed CG with Jacobi beside it (`mixed_cg_jacobi`)"}
     sols = {}
     peak_tf = None
     try:
@@ -887,6 +889,12 @@ def bench_q2(args, gg, ctx, lib, timed):
                      "assembly_ms_per_launch": (r["kt"][_lib.GFE_KT_ASSEMBLE][0] /
                                                 max(r["kt"][_lib.GFE_KT_ASSEMBLE][1], 1))}
         sols[prec] = x.clone()
+        rj = timed("q2_jac_" + prec, lambda: step(prec, solver_name="mixed_cg"), 1, 1,
+                   kernel_timing=False)
+        out[prec]["mixed_cg_jacobi"] = {"value": nfree / (rj["ms"] * 1e-3),
+                                        "ms_per_step": rj["ms"],
+                                        "iterations": rj["reps"][-1].iterations,
+                                        "relres": rj["reps"][-1].relres}
     out["fp32"]["element_kernel"] = "tcgen05 kind::tf32 (M=128, N=32, K=88), FP32 accumulate"
     if peak_tf and out["fp32"]["element_tflops"]:
         out["fp32"]["element_frac_of_bf16_dense_peak"] = out["fp32"]["element_tflops"] / peak_tf

@@ -352,7 +352,10 @@ extern "C" int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* p
     GFE_TRY(ctx->scratch[SCR_VEC_B].reserve(sizeof(double) * (p->nfree > 0 ? p->nfree : 1)));
     db = ctx->scratch[SCR_VEC_B].as<double>();
   }
-  if (A) A->mf_state = 0;
+  if (A) {
+    A->mf_state = 0;
+    A->pmg_state = 0;
+  }
   struct LiftReset {
     gfe_ctx* c;
     ~LiftReset() {

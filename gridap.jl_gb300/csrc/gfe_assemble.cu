@@ -647,6 +647,7 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
       RowArgs a = row_args(ctx, R, d_b, A != nullptr);
       if (A) {
         GFE_TRY(run_rows(ctx, a, s, maxw, A->pos_bytes));
+        if (D == 3) GFE_TRY(attach_q2_pmg(ctx, A, p, d_coef));
       } else {
         GFE_TRY(vector_only_rows(ctx, a, s));
       }
@@ -691,6 +692,7 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
     RowArgs a = row_args(ctx, R, d_b, A != nullptr);
     if (A) {
       GFE_TRY(run_rows(ctx, a, s, maxw, A->pos_bytes));
+      if (D == 3) GFE_TRY(attach_q2_pmg(ctx, A, p, d_coef));
     } else {
       GFE_TRY(vector_only_rows(ctx, a, s));
     }

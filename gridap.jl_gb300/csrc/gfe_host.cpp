@@ -499,6 +499,16 @@ extern "C" int gfe_cartesian_conforming_dofs(int dim, int order, const int64_t* 
 }
 
 namespace gfe {
+// Position of each local Q2 node on the cell's 3^D node lattice, in Gridap's local order:
+// idx[a*D + d] = 0 / 1 / 2 along direction d (2*anchor along fixed directions, 1 along
+// spanned ones).
+void q2_node_lattice(int D, int* idx) {
+  unsigned fe[27], fa[27];
+  const int nn = ncube_faces(D, fe, fa);
+  for (int a = 0; a < nn; ++a)
+    for (int d = 0; d < D; ++d) idx[a * D + d] = (fe[a] >> d) & 1 ? 1 : 2 * ((fa[a] >> d) & 1);
+}
+
 // Q2 Lagrange basis on the 3^D nodes of the n-cube in Gridap's local order (vertices, edges,
 // faces, interior; one node per face at its centre): node lattice index 0 / 1 / 2 per
 // direction (2*anchor along fixed directions, 1 along spanned ones), 1-D factors the

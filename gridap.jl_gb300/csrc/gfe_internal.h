@@ -167,6 +167,14 @@ struct gfe_matrix {
   // after its device check of the ids)
   bool cart_lattice = false;
   int64_t cart_n[3] = {0, 0, 0};
+  // p-multigrid data of a 3-D Q2 matrix on a Cartesian grid (nodes possibly jittered) whose
+  // vertex dofs are the interior vertices in node order (gfe_pmg.cu): the Q2 node lattice
+  // -> free dof map and the coarse Q1 lattice operator (kappa in FP32, the reference
+  // stiffness of the uniform grid). 0 none, 1 check pending, 2 valid.
+  int pmg_state = 0;
+  int64_t pmg_n[3] = {0, 0, 0};
+  float pmg_K[64] = {0};
+  gfe::DevBuf pmg_node, pmg_kap32, pmg_flag;
   // ref_ptr / refs / refpos of the closed-form pattern not written yet (ensure_row_refs)
   bool refs_pending = false;
   // a pattern built by the general symbolic loop was checked once against the closed form
@@ -209,6 +217,14 @@ int assemble_cartesian_q1_lattice(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem
                                   const double* Kref, const double* mref, double* d_b,
                                   bool* done);
 
+// p-multigrid for 3-D Q2 (gfe_pmg.cu): attached by the Q2 assembly, used by the flexible CG
+// with GFE_PC_MG when the matrix has no Q1 lattice form.
+int attach_q2_pmg(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p, const double* d_coef);
+struct Q2PMG;
+int pmg_ready(gfe_ctx* ctx, gfe_matrix* A, bool* ok);
+int pmg_create(gfe_ctx* ctx, gfe_matrix* A, Q2PMG** out);
+int pmg_apply(Q2PMG* pmg, const float* r, float* z, const int* done);
+void pmg_destroy(Q2PMG* pmg);
 // Whether A's cell ids are the interior-node numbering of an (n0, n1, n2) Cartesian Q1 grid
 // with every boundary node Dirichlet (device check); the pattern is then the closed form.
 int cartesian_ids_match(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1, int64_t n2,
@@ -266,9 +282,10 @@ int launch_q2_cells_tf32(gfe_ctx* ctx, int64_t ncells, const int32_t* cell_verti
 int learned_apply(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, float* d_z,
                   const int* skip = nullptr);
 int64_t learned_ndofs(const gfe_learned_pc* pc);
-// z = base + M(r) (base may be null), e.g. a learned smoothing step x + M(b - A x)
+// z = base + M(r) (base may be null), e.g. a learned smoothing step x + M(b - A x); `timed`
+// false inside a captured V-cycle (the graph launch is timed as a whole)
 int learned_apply_into(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, const float* base,
-                       float* d_z, const int* skip);
+                       float* d_z, const int* skip, bool timed);
 int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_opts* o,
               const double* d_b, double* d_x, gfe_solve_report* rep);
 
@@ -292,6 +309,7 @@ void timer_release(gfe_ctx* ctx);
 int tensor_quadrature(int D, int degree, std::vector<double>& x, std::vector<double>& w);
 void q1_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
                std::vector<double>& dphi);
+void q2_node_lattice(int D, int* idx);
 void q2_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
                std::vector<double>& dphi);
 // geometric multigrid V-cycle on the lattice operator (gfe_mg.cu)
@@ -299,6 +317,9 @@ struct LatticeQ1Op;
 struct LatticeMG;
 int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out);
 int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done);
+// Records one V-cycle (b = r, result in z) on the context's stream without capturing it (for
+// a caller that captures a larger cycle around it).
+int mg_record(LatticeMG* mg, const float* r, float* z, const int* done);
 // Makes the learned block preconditioner the fine level's smoother of the V-cycle (pre:
 // x = M(b); post: x += M(b - A x)); the coarser levels keep damped Jacobi.
 int mg_set_learned(LatticeMG* mg, gfe_learned_pc* pc);

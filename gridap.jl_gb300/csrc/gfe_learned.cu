@@ -544,25 +544,25 @@ int64_t learned_ndofs(const gfe_learned_pc* pc) { return pc->ndofs; }
 
 int learned_apply(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, float* d_z,
                   const int* skip) {
-  return learned_apply_into(ctx, pc, d_r, nullptr, d_z, skip);
+  return learned_apply_into(ctx, pc, d_r, nullptr, d_z, skip, true);
 }
 
 int learned_apply_into(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, const float* base,
-                       float* d_z, const int* skip) {
+                       float* d_z, const int* skip, bool timed) {
   if (!pc->has_weights) return set_error(GFE_ERR_INVALID_ARGUMENT, "learned pc: no weights");
   const size_t sm = sizeof(Smem) + 1024;
   auto kern = k_mlp_blocks;
   GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   const int64_t ntiles = (pc->nblocks + kTile - 1) / kTile;
   const int64_t grid = ntiles < (int64_t)ctx->num_sms ? ntiles : (int64_t)ctx->num_sms;
-  timer_begin(ctx, GFE_KT_PRECOND);
+  if (timed) timer_begin(ctx, GFE_KT_PRECOND);
   kern<<<(unsigned)(grid > 0 ? grid : 1), kThreads, sm, ctx->stream>>>(
       pc->nblocks, pc->bdofs.as<int32_t>(), pc->bfeat.as<float>(), pc->bscale.as<float>(), d_r,
       pc->wpack.as<uint8_t>(), pc->params.as<float>(), pc->yblk.as<float>(), ctx->d_err, skip);
   k_block_gather<<<grid_for(pc->ndofs, 256, (int64_t)ctx->num_sms * 8), 256, 0, ctx->stream>>>(
       pc->ndofs, pc->dptr.as<int64_t>(), pc->dref.as<int32_t>(), pc->yblk.as<float>(), base,
       d_z, skip);
-  timer_end(ctx);
+  if (timed) timer_end(ctx);
   ctx->launches += 2;
   GFE_CUDA_TRY(cudaGetLastError());
   return GFE_OK;

@@ -414,7 +414,7 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
     // learned smoothing on the fine level: x = M(b); r = b - A x to the coarse level;
     // t = x + P x_c; x = t + M(b - A t)
     LatticeMG::Level& C = mg->lv[l + 1];
-    GFE_TRY(learned_apply_into(ctx, mg->learned, L.b, nullptr, L.x, done));
+    GFE_TRY(learned_apply_into(ctx, mg->learned, L.b, nullptr, L.x, done, false));
     if (deep)
       k_mg_residual<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.b, L.t, done);
     else
@@ -430,7 +430,7 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
     else
       k_mg_residual<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, L.t, L.b, L.x, done);
     ctx->launches += 2;
-    return learned_apply_into(ctx, mg->learned, L.x, L.t, L.x, done);
+    return learned_apply_into(ctx, mg->learned, L.x, L.t, L.x, done, false);
   }
   if (pre >= 2) {  // the sweep from zero and the next one in one pass
     if (deep)
@@ -573,6 +573,12 @@ int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done) {
   timer_end(ctx);
   ctx->launches += mg->nodes;
   return GFE_OK;
+}
+
+int mg_record(LatticeMG* mg, const float* r, float* z, const int* done) {
+  mg->lv[0].b = const_cast<float*>(r);
+  mg->lv[0].x = z;
+  return vcycle(mg, 0, done);
 }
 
 int mg_set_learned(LatticeMG* mg, gfe_learned_pc* pc) {

@@ -658,17 +658,6 @@ __device__ __forceinline__ void cart_row(int64_t r, int m0, int m1, int& i, int&
   j = (int)(t - (uint32_t)k * (uint32_t)m1);
 }
 
-__global__ void k_cart_widths(int64_t nrows, int m0, int m1, int m2, int64_t* __restrict__ w) {
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows;
-       r += (int64_t)gridDim.x * blockDim.x) {
-    int i, j, k;
-    cart_row(r, m0, m1, i, j, k);
-    const int nx = 1 + (i > 0) + (i < m0 - 1), ny = 1 + (j > 0) + (j < m1 - 1),
-              nz = 1 + (k > 0) + (k < m2 - 1);
-    w[r] = nx * ny * nz;
-  }
-}
-
 // refs, ref_ptr and byte positions: thread per (row, reference), so that consecutive threads
 // store consecutive references and 8-byte position words
 __global__ void k_cart_refs(int64_t nrows, int n0, int n1, int m0, int m1, int m2,
@@ -705,24 +694,76 @@ __global__ void k_cart_refs(int64_t nrows, int n0, int n1, int m0, int m1, int m
   }
 }
 
-// colval: a warp per row, lane = column slot (27 of 32 lanes), the row's slots consecutive
-__global__ void k_cart_cols(int64_t nrows, int m0, int m1, int m2,
-                            const int64_t* __restrict__ rowptr, int32_t* __restrict__ colval) {
-  const int lane = threadIdx.x & 31;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrows;
-       r += nwarps) {
+// Row widths and their prefix sums in closed form. Along an axis of m interior nodes a node
+// has 3 neighbours in the interior (itself included), 2 at either end (1 when m = 1); the
+// width of row (i, j, k) is the product nx(i) ny(j) nz(k) and its start
+//     rowptr(i, j, k) = Sz(k) Y X + nz(k) (Sy(j) X + ny(j) Sx(i)),
+// with S the prefix sums along an axis and X, Y the full sums (X = Sx(m0)).
+__device__ __forceinline__ int64_t cart_axis_n(int p, int m) {
+  return m == 1 ? 1 : (p == 0 || p == m - 1) ? 2 : 3;
+}
+__device__ __forceinline__ int64_t cart_axis_prefix(int p, int m) {  // sum over p' < p
+  if (m == 1) return p;  // p is 0 or 1
+  return p == 0 ? 0 : 2 + 3 * (int64_t)(p - 1) - (p == m ? 1 : 0);
+}
+
+__global__ void k_cart_rowptr(int64_t nrows, int m0, int m1, int m2,
+                              int32_t* __restrict__ rowptr) {
+  const int64_t X = cart_axis_prefix(m0, m0), Y = cart_axis_prefix(m1, m1);
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r <= nrows;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    if (r == nrows) {
+      rowptr[r] = (int32_t)(X * Y * cart_axis_prefix(m2, m2));
+      continue;
+    }
     int i, j, k;
     cart_row(r, m0, m1, i, j, k);
-    const int xlo = i > 0 ? -1 : 0, xhi = i < m0 - 1 ? 1 : 0;
-    const int ylo = j > 0 ? -1 : 0, yhi = j < m1 - 1 ? 1 : 0;
-    const int zlo = k > 0 ? -1 : 0, zhi = k < m2 - 1 ? 1 : 0;
-    const int nx = xhi - xlo + 1, ny = yhi - ylo + 1, nz = zhi - zlo + 1;
-    if (lane < nx * ny * nz) {
-      const int px = lane % nx, py = (lane / nx) % ny, pz = lane / (nx * ny);
-      colval[rowptr[r] + lane] =
-          (int32_t)((i + xlo + px) + m0 * ((j + ylo + py) + m1 * (k + zlo + pz)));
+    rowptr[r] = (int32_t)(cart_axis_prefix(k, m2) * Y * X +
+                          cart_axis_n(k, m2) * (cart_axis_prefix(j, m1) * X +
+                                                cart_axis_n(j, m1) * cart_axis_prefix(i, m0)));
+  }
+}
+
+// colval: a warp per x-line of 32 rows (consecutive rows, one contiguous CSR slice): each
+// lane writes its row's columns into a shared-memory stage at the row's offset, then the
+// warp stores the slice with coalesced writes
+__global__ void __launch_bounds__(256) k_cart_cols(int m0, int m1, int m2,
+                                                   const int32_t* __restrict__ rowptr,
+                                                   int32_t* __restrict__ colval) {
+  __shared__ int32_t stage_all[8][32 * 27];
+  const int lane = (int)(threadIdx.x & 31), wib = (int)(threadIdx.x >> 5);
+  int32_t* stage = stage_all[wib];
+  const int tx = (m0 + 31) / 32;
+  const int64_t ntask = (int64_t)tx * m1 * m2;
+  const int64_t nwarps = (int64_t)gridDim.x * 8;
+  for (int64_t task = (int64_t)blockIdx.x * 8 + wib; task < ntask; task += nwarps) {
+    const int64_t line = task / tx;
+    const int i = (int)(task - line * tx) * 32 + lane;
+    const int k = (int)(line / m1), j = (int)(line - (int64_t)k * m1);
+    const bool act = i < m0;
+    const int64_t r = (int64_t)(act ? i : m0 - 1) + (int64_t)m0 * (j + (int64_t)m1 * k);
+    const int32_t rp = act ? __ldg(rowptr + r) : 0;
+    const int32_t rp0 = __shfl_sync(0xffffffffu, rp, 0);
+    int32_t rend = act ? __ldg(rowptr + r + 1) : 0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      rend = max(rend, __shfl_xor_sync(0xffffffffu, rend, off));
+    if (act) {
+      int pos = rp - rp0;
+#pragma unroll
+      for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int ii = i + dx, jj = j + dy, kk = k + dz;
+            if (ii >= 0 && ii < m0 && jj >= 0 && jj < m1 && kk >= 0 && kk < m2)
+              stage[pos++] = ii + m0 * (jj + m1 * kk);
+          }
     }
+    __syncwarp();
+    for (int q = lane; q < rend - rp0; q += 32) colval[rp0 + q] = stage[q];
+    __syncwarp();
   }
 }
 
@@ -781,16 +822,8 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
   int bad = 1;
   GFE_TRY(copy_out(ctx, &bad, flag.ptr, sizeof(int)));
   if (bad) return GFE_OK;
-  DevBuf width(ctx), rowptr64(ctx);
-  GFE_TRY(width.reserve(sizeof(int64_t) * (nrows + 1)));
-  GFE_TRY(rowptr64.reserve(sizeof(int64_t) * (nrows + 1)));
-  const unsigned g = grid_for(nrows, 256, (int64_t)ctx->num_sms * 16);
-  k_cart_widths<<<g, 256, 0, ctx->stream>>>(nrows, (int)m0, (int)m1, (int)m2,
-                                            width.as<int64_t>());
-  ctx->launches++;
-  GFE_TRY(scan_exclusive_i64(ctx, width.as<int64_t>(), rowptr64.as<int64_t>(), nrows));
-  int64_t nnz = 0;
-  GFE_TRY(copy_out(ctx, &nnz, rowptr64.as<int64_t>() + nrows, sizeof(int64_t)));
+  auto axis = [](int64_t m) { return m == 1 ? (int64_t)1 : 3 * m - 2; };
+  const int64_t nnz = axis(m0) * axis(m1) * axis(m2);
   if (nnz > (int64_t)INT32_MAX - 64)
     return set_error(GFE_ERR_UNSUPPORTED, "symbolic_loop_matrix: nnz %lld exceeds int32",
                      (long long)nnz);
@@ -804,10 +837,11 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
   // the row references and positions are written when a row gather first needs them
   // (ensure_row_refs); the class-sum assembly of this pattern does not read them
   A->refs_pending = true;
-  k_cart_cols<<<grid_for(32 * nrows, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
-      nrows, (int)m0, (int)m1, (int)m2, rowptr64.as<int64_t>(), A->colval.as<int32_t>());
-  ctx->launches += 1;
-  GFE_TRY(narrow_i64_to_i32(ctx, rowptr64.as<int64_t>(), A->rowptr.as<int32_t>(), nrows + 1));
+  k_cart_rowptr<<<grid_for(nrows + 1, 256, (int64_t)ctx->num_sms * 16), 256, 0, ctx->stream>>>(
+      nrows, (int)m0, (int)m1, (int)m2, A->rowptr.as<int32_t>());
+  k_cart_cols<<<(unsigned)(ctx->num_sms * 4), 256, 0, ctx->stream>>>(
+      (int)m0, (int)m1, (int)m2, A->rowptr.as<int32_t>(), A->colval.as<int32_t>());
+  ctx->launches += 2;
   GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * (nnz > 0 ? nnz : 1),
                                ctx->stream));
   GFE_CUDA_TRY(cudaGetLastError());

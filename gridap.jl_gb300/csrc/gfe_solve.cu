@@ -334,15 +334,21 @@ int attach_lattice_operator(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p,
   const unsigned g = grid_for(nc, 256, (int64_t)ctx->num_sms * 8);
   k_coef_to_f32<<<g, 256, 0, ctx->stream>>>(d_coef, d_coef ? p->coef_kind : GFE_COEF_ONE, n0,
                                             c1, nc, A->mf_kap32.as<float>());
-  k_lattice_check<<<g, 256, 0, ctx->stream>>>(A->cell_rows.as<int32_t>(), n0, n1, n2,
-                                              A->mf_flag.as<int>());
-  ctx->launches += 2;
+  ctx->launches++;
+  // a closed-form lattice pattern of this grid has had its ids checked already
+  const bool known = A->cart_lattice && A->cart_n[0] == n0 && A->cart_n[1] == n1 &&
+                     A->cart_n[2] == n2;
+  if (!known) {
+    k_lattice_check<<<g, 256, 0, ctx->stream>>>(A->cell_rows.as<int32_t>(), n0, n1, n2,
+                                                A->mf_flag.as<int>());
+    ctx->launches++;
+  }
   GFE_CUDA_TRY(cudaGetLastError());
   for (int e = 0; e < 64; ++e) A->mf_K[e] = (float)Kref[e];
   A->mf_n[0] = n0;
   A->mf_n[1] = n1;
   A->mf_n[2] = n2;
-  A->mf_state = 1;
+  A->mf_state = known ? 2 : 1;
   return GFE_OK;
 }
 
@@ -359,34 +365,7 @@ static int lattice_ready(gfe_ctx* ctx, gfe_matrix* A, bool* ok) {
 }
 
 // ---- SpMV ---------------------------------------------------------------------------------
-// y = A x on the sliced-ELL copy; thread per row, FMA chain in the accumulation type of TV.
-template <typename TV, typename TX>
-__device__ __forceinline__ TV sell_row(int64_t r, const int64_t* __restrict__ sptr,
-                                       const int32_t* __restrict__ scol,
-                                       const TV* __restrict__ sval, const TX* __restrict__ x) {
-  const int64_t s = r >> 5;
-  const int l = (int)(r & 31);
-  const int64_t base = __ldg(sptr + s) + l;
-  const int32_t w = (int32_t)((__ldg(sptr + s + 1) - __ldg(sptr + s)) >> 5);
-  TV acc = (TV)0;
-  int32_t k = 0;
-  for (; k + 4 <= w; k += 4) {
-    const int64_t i = base + (int64_t)k * 32;
-    const int32_t c0 = __ldcs(scol + i), c1 = __ldcs(scol + i + 32), c2 = __ldcs(scol + i + 64),
-                  c3 = __ldcs(scol + i + 96);
-    const TV v0 = __ldcs(sval + i), v1 = __ldcs(sval + i + 32), v2 = __ldcs(sval + i + 64),
-             v3 = __ldcs(sval + i + 96);
-    acc = fma(v0, (TV)__ldg(x + c0), acc);
-    acc = fma(v1, (TV)__ldg(x + c1), acc);
-    acc = fma(v2, (TV)__ldg(x + c2), acc);
-    acc = fma(v3, (TV)__ldg(x + c3), acc);
-  }
-  for (; k < w; ++k) {
-    const int64_t i = base + (int64_t)k * 32;
-    acc = fma(__ldcs(sval + i), (TV)__ldg(x + __ldcs(scol + i)), acc);
-  }
-  return acc;
-}
+#include "gfe_sell.cuh"
 
 // SpMV operators (thread per row). row_index() is the row of the calling thread (or -1) and
 // blocks() the grid that covers all rows with kSpmvBlock threads per block.
@@ -1973,17 +1952,35 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       if (*p) mg_destroy(*p);
     }
   } mg_release{&mg};
+  // p-multigrid for Q2 matrices without the Q1 lattice form
+  Q2PMG* pmg = nullptr;
+  struct PmgRelease {
+    Q2PMG** p;
+    ~PmgRelease() {
+      if (*p) pmg_destroy(*p);
+    }
+  } pmg_release{&pmg};
   if (use_mg) {
-    if (!lattice)
+    bool q2 = false;
+    if (!lattice) GFE_TRY(pmg_ready(ctx, A, &q2));
+    if (!lattice && !q2)
       return set_error(GFE_ERR_UNSUPPORTED,
                        "solve: the multigrid preconditioner needs the lattice operator "
-                       "(uniform Cartesian Q1, 3-D, interior-node numbering)");
-    GFE_TRY(mg_create(ctx, lop, &mg));
-    if (learned) GFE_TRY(mg_set_learned(mg, pc));
+                       "(uniform Cartesian Q1, 3-D, interior-node numbering) or a 3-D "
+                       "Cartesian Q2 matrix whose vertex dofs are the interior vertices");
+    if (lattice) {
+      GFE_TRY(mg_create(ctx, lop, &mg));
+      if (learned) GFE_TRY(mg_set_learned(mg, pc));
+    } else {
+      if (learned)
+        return set_error(GFE_ERR_UNSUPPORTED, "solve: the learned smoother is for Q1 lattices");
+      GFE_TRY(pmg_create(ctx, A, &pmg));
+    }
     // a V-cycle iteration is expensive: look at the state after every one
     if (o->check_every <= 0) check_every = 1;
   }
   auto precond = [&]() -> int {
+    if (use_mg && pmg) return pmg_apply(pmg, r32, z32, &w.S->done);
     if (use_mg) return mg_apply(mg, r32, z32, &w.S->done);
     if (learned) return learned_apply(ctx, pc, r32, z32, &w.S->done);
     k_jacobi_apply<<<gv, kVecBlock, 0, ctx->stream>>>(n, r32, dinv32, z32, w.S);

@@ -84,10 +84,11 @@ class BiCGStabSolver(LinearSolver):
 
 class FCGSolver(LinearSolver):
     """Flexible CG with FP32 vectors and FP64 reliable updates, preconditioned by a
-    LearnedBlockPreconditioner (`pc`), by a geometric multigrid V-cycle on the lattice
-    operator (pc="mg"; uniform Cartesian Q1 in 3-D), by the V-cycle with the learned
-    preconditioner as its fine-level smoother (pc=learned, multigrid=True) or by Jacobi
-    (pc=None); a stagnating learned preconditioner hands over to Jacobi (report.fallback)."""
+    LearnedBlockPreconditioner (`pc`), by a geometric multigrid V-cycle (pc="mg": on the
+    lattice operator of uniform Cartesian Q1 in 3-D, or p-multigrid for 3-D Cartesian Q2),
+    by the V-cycle with the learned preconditioner as its fine-level smoother (pc=learned,
+    multigrid=True) or by Jacobi (pc=None); a stagnating learned preconditioner hands over
+    to Jacobi (report.fallback)."""
 
     def __init__(self, rtol: float = 1e-8, maxiter: int = 100000, pc=None,
                  inner_rtol: float = 0.0, check_every: int = 0, initial_guess: bool = False,

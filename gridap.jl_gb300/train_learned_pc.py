@@ -1,8 +1,10 @@
 """Trains the learned block preconditioner and writes data/learned_pc_q1_lognormal.npy.
 
-Residual / local-solve pairs come from FP64 Jacobi-PCG solves of 200 independent lognormal
-kappa draws (seeds 5000..5199, 64^3 cells, correlation length 8 cells, contrast 1e4); the
-network is fitted with the library's FP32 training kernels. Needs a GPU:
+Residual / error pairs come from FP64 CG solves of 200 independent lognormal kappa draws
+(seeds 5000..5199, 64^3 cells, correlation length 8 cells, contrast 1e4): the solution x*
+to 1e-12, then CG iterates x_k from x0 = x* + white noise (k = 0, 1, 2, 4), inputs from
+r_k = b - A x_k and targets e_k = x* - x_k. The network is fitted with the library's FP32
+training kernels. Needs a GPU:
 
     python gridap.jl_gb300/train_learned_pc.py [--n 64] [--draws 200] [--out PATH]
 """

@@ -355,6 +355,7 @@ extern "C" int gfe_assemble_matrix_and_vector(gfe_ctx* ctx, const gfe_problem* p
   if (A) {
     A->mf_state = 0;
     A->pmg_state = 0;
+    A->p2mg_state = 0;
   }
   struct LiftReset {
     gfe_ctx* c;

@@ -253,6 +253,7 @@ int assemble_p2_elasticity(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, do
     };
     if (fp32) GFE_TRY(go(CartesianElasticityP2<true>{}));
     else GFE_TRY(go(CartesianElasticityP2<false>{}));
+    if (A) GFE_TRY(attach_p2_pmg(ctx, A, p, d_coef));
     return check_device_error(ctx, "assemble (P2 elasticity)");
   }
 

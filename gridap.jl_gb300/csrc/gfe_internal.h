@@ -175,6 +175,14 @@ struct gfe_matrix {
   int64_t pmg_n[3] = {0, 0, 0};
   float pmg_K[64] = {0};
   gfe::DevBuf pmg_node, pmg_kap32, pmg_flag;
+  // two-level data of a vector P2 elasticity matrix on a simplexified Cartesian box
+  // (gfe_pmg.cu): the box and the Lame coefficients (2 per tet, or 2 constants) from which
+  // the P1 coarse operator is assembled. 0 none, 2 attached.
+  int p2mg_state = 0;
+  int64_t p2mg_part[3] = {0, 0, 0};
+  double p2mg_dom[6] = {0, 0, 0, 0, 0, 0};
+  int p2mg_coef_kind = 0;
+  gfe::DevBuf p2mg_lame;
   // ref_ptr / refs / refpos of the closed-form pattern not written yet (ensure_row_refs)
   bool refs_pending = false;
   // a pattern built by the general symbolic loop was checked once against the closed form
@@ -221,6 +229,12 @@ int assemble_cartesian_q1_lattice(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem
 // with GFE_PC_MG when the matrix has no Q1 lattice form.
 int attach_q2_pmg(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p, const double* d_coef);
 struct Q2PMG;
+// two-level P2 -> P1 preconditioner of vector P2 elasticity (gfe_pmg.cu)
+int attach_p2_pmg(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p, const double* d_coef);
+struct P2PMG;
+int p2mg_create(gfe_ctx* ctx, gfe_matrix* A, P2PMG** out);
+int p2mg_apply(P2PMG* pm, const float* r, float* z, const int* done);
+void p2mg_destroy(P2PMG* pm);
 int pmg_ready(gfe_ctx* ctx, gfe_matrix* A, bool* ok);
 int pmg_create(gfe_ctx* ctx, gfe_matrix* A, Q2PMG** out);
 int pmg_apply(Q2PMG* pmg, const float* r, float* z, const int* done);

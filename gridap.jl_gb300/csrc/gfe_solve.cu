@@ -1954,33 +1954,41 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   } mg_release{&mg};
   // p-multigrid for Q2 matrices without the Q1 lattice form
   Q2PMG* pmg = nullptr;
+  P2PMG* p2mg = nullptr;
   struct PmgRelease {
     Q2PMG** p;
+    P2PMG** q;
     ~PmgRelease() {
       if (*p) pmg_destroy(*p);
+      if (*q) p2mg_destroy(*q);
     }
-  } pmg_release{&pmg};
+  } pmg_release{&pmg, &p2mg};
   if (use_mg) {
     bool q2 = false;
     if (!lattice) GFE_TRY(pmg_ready(ctx, A, &q2));
-    if (!lattice && !q2)
+    const bool p2 = !lattice && !q2 && A->p2mg_state == 2;
+    if (!lattice && !q2 && !p2)
       return set_error(GFE_ERR_UNSUPPORTED,
                        "solve: the multigrid preconditioner needs the lattice operator "
-                       "(uniform Cartesian Q1, 3-D, interior-node numbering) or a 3-D "
-                       "Cartesian Q2 matrix whose vertex dofs are the interior vertices");
+                       "(uniform Cartesian Q1, 3-D, interior-node numbering), a 3-D "
+                       "Cartesian Q2 matrix whose vertex dofs are the interior vertices, or "
+                       "vector P2 elasticity on a simplexified box");
+    if (learned && !lattice)
+      return set_error(GFE_ERR_UNSUPPORTED, "solve: the learned smoother is for Q1 lattices");
     if (lattice) {
       GFE_TRY(mg_create(ctx, lop, &mg));
       if (learned) GFE_TRY(mg_set_learned(mg, pc));
-    } else {
-      if (learned)
-        return set_error(GFE_ERR_UNSUPPORTED, "solve: the learned smoother is for Q1 lattices");
+    } else if (q2) {
       GFE_TRY(pmg_create(ctx, A, &pmg));
+    } else {
+      GFE_TRY(p2mg_create(ctx, A, &p2mg));
     }
     // a V-cycle iteration is expensive: look at the state after every one
     if (o->check_every <= 0) check_every = 1;
   }
   auto precond = [&]() -> int {
     if (use_mg && pmg) return pmg_apply(pmg, r32, z32, &w.S->done);
+    if (use_mg && p2mg) return p2mg_apply(p2mg, r32, z32, &w.S->done);
     if (use_mg) return mg_apply(mg, r32, z32, &w.S->done);
     if (learned) return learned_apply(ctx, pc, r32, z32, &w.S->done);
     k_jacobi_apply<<<gv, kVecBlock, 0, ctx->stream>>>(n, r32, dinv32, z32, w.S);

@@ -27,18 +27,7 @@ constexpr int kMgBlock = 256;
 constexpr float kOmega = 0.8f;
 constexpr int kPreSweeps = 2, kCoarseSweeps = 8;
 
-// Every kernel of the cycle is launched with programmatic dependent launch: it lets the next
-// kernel of the chain be scheduled (launch_dependents) and waits for the previous one to have
-// completed and flushed its writes (griddepcontrol.wait) before it reads anything. Both are
-// no-ops for a kernel launched the ordinary way.
-__device__ __forceinline__ void pdl_enter() {
-  asm volatile("griddepcontrol.launch_dependents;");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-}
-__device__ __forceinline__ bool stop(const int* done) {
-  pdl_enter();
-  return done && *done;
-}
+__device__ __forceinline__ bool stop(const int* done) { return done && *done; }
 
 // One damped Jacobi sweep fused into the lattice apply: xo = x + omega D^-1 (b - A x)
 // (xo != x: the sweep reads the old neighbours). Same arithmetic as an apply into t followed
@@ -380,23 +369,6 @@ struct LatticeMG {
 
 namespace {
 
-// launch with programmatic stream serialization: the kernel may start while its predecessor
-// drains and waits for it in griddepcontrol.wait (see pdl_enter)
-template <typename... KArgs, typename... Args>
-void launch_pdl(gfe_ctx* ctx, void (*kern)(KArgs...), dim3 grid, dim3 block, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = ctx->stream;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kern, args...);
-}
-
 unsigned vgrid(gfe_ctx* ctx, int64_t n) {
   return (unsigned)std::max<int64_t>(
       1, std::min<int64_t>((n + kMgBlock - 1) / kMgBlock, (int64_t)ctx->num_sms * 8));
@@ -422,7 +394,7 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
       const LatticeMG::Level& Q = mg->lv[l + q];
       c.L[q] = MgLevelView{Q.op, Q.m0, Q.m1, Q.m2, Q.n, Q.x, Q.b, Q.t, Q.dinv};
     }
-    launch_pdl(ctx, k_mg_coarse, dim3(1), dim3(kCoarseBlock), c, done);
+    k_mg_coarse<<<1, kCoarseBlock, 0, ctx->stream>>>(c, done);
     ctx->launches++;
     return GFE_OK;
   }
@@ -433,11 +405,9 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
   const dim3 ga1 = L.op.grid_k(1);
   auto smooth = [&](const float* xi, float* xo) {
     if (deep)
-      launch_pdl(ctx, k_mg_smooth<kLatK>, dim3(ga), dim3(kMgBlock), L.op, xi,
-                 (const float*)L.b, (const float*)L.dinv, xo, done);
+      k_mg_smooth<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, xi, L.b, L.dinv, xo, done);
     else
-      launch_pdl(ctx, k_mg_smooth<1>, dim3(ga1), dim3(kMgBlock), L.op, xi, (const float*)L.b,
-                 (const float*)L.dinv, xo, done);
+      k_mg_smooth<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, xi, L.b, L.dinv, xo, done);
     ctx->launches++;
   };
   if (l == 0 && mg->learned && !coarsest) {
@@ -446,37 +416,30 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
     LatticeMG::Level& C = mg->lv[l + 1];
     GFE_TRY(learned_apply_into(ctx, mg->learned, L.b, nullptr, L.x, done, false));
     if (deep)
-      launch_pdl(ctx, k_mg_residual<kLatK>, dim3(ga), dim3(kMgBlock), L.op,
-                 (const float*)L.x, (const float*)L.b, L.t, done);
+      k_mg_residual<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.b, L.t, done);
     else
-      launch_pdl(ctx, k_mg_residual<1>, dim3(ga1), dim3(kMgBlock), L.op,
-                 (const float*)L.x, (const float*)L.b, L.t, done);
-    launch_pdl(ctx, k_mg_restrict, dim3(vgrid(ctx, C.n)), dim3(kMgBlock), L.m0, L.m1, C.m0,
-               C.m1, C.m2, (const float*)L.t, C.b, done);
+      k_mg_residual<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.b, L.t, done);
+    k_mg_restrict<<<vgrid(ctx, C.n), kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, C.m0, C.m1, C.m2,
+                                                                 L.t, C.b, done);
     ctx->launches += 2;
     GFE_TRY(vcycle(mg, l + 1, done));
-    launch_pdl(ctx, k_mg_prolong, dim3(g), dim3(kMgBlock), L.m0, L.m1, L.m2, C.m0, C.m1, C.m2,
-               (const float*)C.x, (const float*)L.x, L.t, done);
+    k_mg_prolong<<<g, kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, L.m2, C.m0, C.m1, C.m2, C.x, L.x,
+                                                  L.t, done);
     if (deep)
-      launch_pdl(ctx, k_mg_residual<kLatK>, dim3(ga), dim3(kMgBlock), L.op,
-                 (const float*)L.t, (const float*)L.b, L.x, done);
+      k_mg_residual<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.t, L.b, L.x, done);
     else
-      launch_pdl(ctx, k_mg_residual<1>, dim3(ga1), dim3(kMgBlock), L.op,
-                 (const float*)L.t, (const float*)L.b, L.x, done);
+      k_mg_residual<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, L.t, L.b, L.x, done);
     ctx->launches += 2;
     return learned_apply_into(ctx, mg->learned, L.x, L.t, L.x, done, false);
   }
   if (pre >= 2) {  // the sweep from zero and the next one in one pass
     if (deep)
-      launch_pdl(ctx, k_mg_pre<kLatK>, dim3(ga), dim3(kMgBlock), L.op, (const float*)L.b,
-                 (const float*)L.dinv, oth, done);
+      k_mg_pre<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.b, L.dinv, oth, done);
     else
-      launch_pdl(ctx, k_mg_pre<1>, dim3(ga1), dim3(kMgBlock), L.op, (const float*)L.b,
-                 (const float*)L.dinv, oth, done);
+      k_mg_pre<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, L.b, L.dinv, oth, done);
     std::swap(cur, oth);
   } else {
-    launch_pdl(ctx, k_mg_jacobi0, dim3(g), dim3(kMgBlock), L.n, (const float*)L.b,
-               (const float*)L.dinv, cur, done);
+    k_mg_jacobi0<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.dinv, cur, done);
   }
   ctx->launches++;
   for (int s = 2; s < pre; ++s) {
@@ -487,17 +450,15 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
                                   : set_error(GFE_ERR_UNSUPPORTED, "multigrid: sweep parity");
   LatticeMG::Level& C = mg->lv[l + 1];
   if (deep)
-    launch_pdl(ctx, k_mg_residual<kLatK>, dim3(ga), dim3(kMgBlock), L.op,
-                 (const float*)cur, (const float*)L.b, oth, done);
+    k_mg_residual<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, cur, L.b, oth, done);
   else
-    launch_pdl(ctx, k_mg_residual<1>, dim3(ga1), dim3(kMgBlock), L.op,
-                 (const float*)cur, (const float*)L.b, oth, done);
-  launch_pdl(ctx, k_mg_restrict, dim3(vgrid(ctx, C.n)), dim3(kMgBlock), L.m0, L.m1, C.m0, C.m1,
-             C.m2, (const float*)oth, C.b, done);
+    k_mg_residual<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, cur, L.b, oth, done);
+  k_mg_restrict<<<vgrid(ctx, C.n), kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, C.m0, C.m1, C.m2,
+                                                               oth, C.b, done);
   ctx->launches += 2;
   GFE_TRY(vcycle(mg, l + 1, done));
-  launch_pdl(ctx, k_mg_prolong, dim3(g), dim3(kMgBlock), L.m0, L.m1, L.m2, C.m0, C.m1, C.m2,
-             (const float*)C.x, (const float*)cur, oth, done);
+  k_mg_prolong<<<g, kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, L.m2, C.m0, C.m1, C.m2, C.x, cur,
+                                                oth, done);
   ctx->launches++;
   std::swap(cur, oth);
   for (int s = 0; s < kPreSweeps; ++s) {

@@ -166,10 +166,10 @@ def vcycle_bytes(n):
     return tot
 
 
-def assembly_bytes(nnz, n, ncells):
-    """Row-gather numeric loop of Q1 diffusion: per cell reference its id (4 B), the 8-byte
-    position table row and kappa (8 B); every stored value and b written (8 B)."""
-    return ncells * 8 * (4 + 8 + 8) + nnz * 8 + n * 8
+def assembly_bytes(nnz, n, ncells, nnodes):
+    """Class-sum numeric assembly of Cartesian Q1 diffusion: kappa (8 B per cell) and the
+    nodal source (8 B per node) read, every stored value and b written (8 B)."""
+    return ncells * 8 + nnodes * 8 + nnz * 8 + n * 8
 
 
 def spmv_bytes(nnz, n, s):
@@ -525,9 +525,9 @@ def run_gpu(args):
         "vector32": dict(kernel="k_cg_update4 + k_cg_direction4 (FP32 CG vector updates)",
                          alg=44 * nfree, kt=r_mixed_kt["kt"][_lib.GFE_KT_VECTOR],
                          traffic=profile_traffic("fp32_vector")),
-        "assembly": dict(kernel="k_assemble_rows (row-gather numeric loop, FP64 cell "
-                                "integrals fused; FP64-pipe bound)",
-                         alg=assembly_bytes(nnz, nfree, ncells),
+        "assembly": dict(kernel="k_assemble_cart_q1 (class-sum numeric assembly, FP64; "
+                                "FP64-pipe bound)",
+                         alg=assembly_bytes(nnz, nfree, ncells, (args.n + 1) ** 3),
                          traffic=profile_traffic("assembly"),
                          kt=r_mixed_kt["kt"][_lib.GFE_KT_ASSEMBLE]),
     }
@@ -537,7 +537,7 @@ def run_gpu(args):
         # graph launch timed as a whole
         kinds["spmv32"].update(kernel="k_lattice_spmv<true, false> (matrix-free FP32 Q1 "
                                       "operator + p.q, p.r)", alg=ncells * 4 + nfree * 12,
-                               traffic=None)
+                               traffic=profile_traffic("fp32_lattice_fcg"))
         kinds["vector32"].update(kernel="k_fcg_update; k_fcg_beta + k_fcg_dir (FP32 FCG "
                                         "vector updates)", alg=22 * nfree, traffic=None)
         kinds["vcycle"] = dict(kernel="multigrid V-cycle (CUDA graph: k_mg_smooth, "
@@ -572,7 +572,8 @@ def run_gpu(args):
                               f"mixed CG: FP32 Jacobi-PCG with FP64 reliable updates "
                               f"(delta {args.delta}), FP64 x and true residual; inner "
                               f"operator {rep_m.operator_format}"),
-                   "assembly": "FP64 cell integrals, FP64 row-gather scatter"},
+                   "assembly": "FP64 class-sum assembly into the closed-form Cartesian "
+                               "CSR pattern"},
         "iterations": {"mixed": rep_m.iterations, "mixed_reliable_updates": rep_m.refinements,
                        "plain_fp64": rep_p.iterations},
         "plain_fp64": {"value": plain_value, "ms_per_step": r_plain["ms"],
@@ -606,7 +607,7 @@ def run_gpu(args):
                                    "algorithmic_bytes_per_launch": alg64,
                                    "avg_launch_ms": prof["fp64_ms"],
                                    "traffic": profile_traffic("fp64_sell")}},
-        "assembly": {"row_gather_ms": prof["assemble_ms"]},
+        "assembly": {"class_sum_ms": prof["assemble_ms"]},
         "learned_fcg": (dict(learned_out, over_plain_fp64=learned_out["value"] / plain_value)
                         if learned_out else None),
         "gpu_launches": r_mixed["launches"],
@@ -642,8 +643,10 @@ def run_gpu(args):
 def bench_batched(args, gg, ctx, lib, barrier):
     """256 independent diffusion problems div(kappa grad u) = 1 on unit cubes with n^3 cells,
     n uniform in 16..64, per-cell lognormal kappa (sigma 1.5), u = 0 on the boundary: one
-    batched assemble+solve call against the same problems solved one after the other through
-    the single-problem path (symbolic + numeric assembly + FP64 Jacobi-PCG per problem)."""
+    batched assemble+solve call (one persistent launch: matrix-free FP32 Jacobi-PCG per problem
+    with FP64 reliable updates, autotuned launch shape) against the same problems solved one
+    after the other through the single-problem path (symbolic + numeric assembly + FP64
+    Jacobi-PCG per problem)."""
     import ctypes
     import torch
     from gridap_gb300 import _lib, workloads
@@ -717,6 +720,7 @@ def bench_batched(args, gg, ctx, lib, barrier):
             "sizes": "n^3 cells, n uniform in 16..64 (seeded)", "rtol": rtol,
             "ms_per_step": 1e3 * t_batch, "problems_per_s": len(sizes) / t_batch,
             "dof_per_s": dofs / t_batch, "gpu_launches_per_step": launches,
+            "launch_shape": {"threads_per_cta": B.shape()[0], "ctas_per_problem": B.shape()[1]},
             "max_iterations": int(it_b.max()), "mean_iterations": float(it_b.mean()),
             "sequential": {"ms": 1e3 * t_seq, "problems_per_s": len(sizes) / t_seq,
                            "dof_per_s": dofs / t_seq, "timing": "host clock, one pass"},

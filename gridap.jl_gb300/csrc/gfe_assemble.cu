@@ -358,6 +358,16 @@ static void cartesian_tables(int D, const double* h, int nq, const std::vector<d
   }
 }
 
+// W[c] = Kref[0, c] of the unit cube's Q1 stiffness (degree-2 rule): the entry between two
+// vertices that differ along the axes in the bit set c (bit 0 x, bit 1 y, bit 2 z).
+void q1_unit_stiffness_classes(double W[8]) {
+  std::vector<double> qx, qw, tabs;
+  tensor_quadrature(3, 2, qx, qw);
+  const double h[3] = {1.0, 1.0, 1.0};
+  cartesian_tables(3, h, (int)qw.size(), qx, qw, tabs);
+  for (int c = 0; c < 8; ++c) W[c] = tabs[0 + 8 * c];
+}
+
 // ---- Q2 (27-node HEX, 9-node QUAD) cell integrals ----------------------------------------
 // The diffusion cell matrix on a cell with (multi)linear geometry is
 //     K = B^T D B,   B[(q,k), i] = d phi_hat_i / d xi_k (xi_q)   (same for every cell),

@@ -321,6 +321,7 @@ void timer_release(gfe_ctx* ctx);
 
 // host set-up (gfe_host.cpp)
 int tensor_quadrature(int D, int degree, std::vector<double>& x, std::vector<double>& w);
+void q1_unit_stiffness_classes(double W[8]);
 void q1_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
                std::vector<double>& dphi);
 void q2_node_lattice(int D, int* idx);

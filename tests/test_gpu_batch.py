@@ -3,9 +3,11 @@ problems assembled and solved in one call.
 
 Each problem's solution is compared with the oracle's assembly of the same problem (Gridap's
 CLagrangian numbering, FP64 cell integrals, InserterCSC assembly) solved by the oracle's
-Jacobi-PCG to the same rtol: the two iterate the same algorithm on the same system, so the
-iteration counts agree within one and the solutions within the CG tolerance (1e-10 relative
-residual -> solutions agree to 1e-7 relative after conditioning of these small problems).
+Jacobi-PCG to the same rtol. The batched solver iterates in FP32 between FP64 reliable
+updates, so its iteration counts track the FP64 ones within a few iterations (tolerance below:
+15 % + 2), its FP64 true residual meets rtol against the oracle's matrix, and the solutions
+agree within the CG tolerance (1e-10 relative residual -> 1e-7 relative solutions after the
+conditioning of these small problems).
 """
 import numpy as np
 import pytest
@@ -25,14 +27,14 @@ def test_batch_matches_oracle_per_problem(gg, orc):
     kappas = [np.exp(rng.standard_normal(n ** 3)) for n in sizes]
     B = gg.BatchedPoissonProblems(sizes, kappas)
     assert B.nfree == sum((n - 1) ** 3 for n in sizes)
-    assert B.nrows % 256 == 0
+    assert B.nrows == B.nfree
     x = B.assemble_solve(source=2.5, rtol=1e-10)
     assert B.nconverged == len(sizes)
     for i, (n, k, xi) in enumerate(zip(sizes, kappas, B.split(x))):
         P = _oracle_problem(orc, n, k, 2.5)
         colptr, rowval, nzval = P["csc"]
         xr, it, relres = orc.pcg(colptr, rowval, nzval, P["b"], 1e-10)
-        assert abs(int(B.iterations[i]) - it) <= 1, (n, B.iterations[i], it)
+        assert abs(int(B.iterations[i]) - it) <= 2 + 0.15 * it, (n, B.iterations[i], it)
         A = orc.to_scipy(colptr, rowval, nzval, P["nfree"], P["nfree"])
         rel = np.linalg.norm(P["b"] - A @ xi) / np.linalg.norm(P["b"])
         assert rel <= 1.01e-10, (n, rel)
@@ -76,7 +78,8 @@ def test_batch_matches_single_problem_cg(gg):
     x = np.empty_like(b)
     ns = gg.numerical_setup(gg.symbolic_setup(gg.CGSolver(rtol=1e-10), A), A)
     gg.solve_(x, ns, b)
-    assert abs(ns.report.iterations - int(B.iterations[0])) <= 1
+    it = ns.report.iterations
+    assert abs(it - int(B.iterations[0])) <= 2 + 0.15 * it
     assert np.linalg.norm(xb - x) <= 1e-7 * np.linalg.norm(x)
 
 
@@ -89,3 +92,66 @@ def test_batch_rejects_non_cubic_partitions(gg):
     st = lib.gfe_batch_create(gg.default_context().handle, 1, gg._lib.ptr(parts),
                               gg._lib.ptr(kap), C.byref(h))
     assert st == gg._lib.GFE_ERR_UNSUPPORTED
+
+
+def test_batch_one_launch_autotuned_shape_device_output(gg):
+    """One kernel launch per solve after tuning, a tuned shape among the candidates, and the
+    device-resident output equal to the host-output solve."""
+    import torch
+    rng = np.random.default_rng(14)
+    sizes = [int(n) for n in rng.integers(4, 20, 48)]
+    kappas = [np.exp(1.5 * rng.standard_normal(n ** 3)) for n in sizes]
+    ctx = gg.default_context()
+    B = gg.BatchedPoissonProblems(sizes, kappas, ctx)
+    assert B.shape() == (0, 0)
+    xh = B.assemble_solve(source=1.0, rtol=1e-8)
+    assert B.shape() in {(256, 1), (1024, 1), (1024, 2), (512, 4), (1024, 4), (1024, 8)}
+    xd = torch.empty(B.nfree, dtype=torch.float64, device="cuda")
+    l0 = ctx.kernel_launches()
+    B.assemble_solve(source=1.0, rtol=1e-8, x=xd)
+    assert ctx.kernel_launches() - l0 == 1
+    assert np.array_equal(xd.cpu().numpy(), xh)
+    assert B.nconverged == len(sizes)
+
+
+def test_batch_iteration_cap_reports_unconverged(gg):
+    rng = np.random.default_rng(15)
+    sizes = [12, 3, 9]
+    kappas = [np.exp(2.0 * rng.standard_normal(n ** 3)) for n in sizes]
+    B = gg.BatchedPoissonProblems(sizes, kappas)
+    B.assemble_solve(source=1.0, rtol=1e-12, maxiter=3)
+    assert B.nconverged < len(sizes)
+    assert int(B.iterations.max()) <= 3
+    # the 2^3-node problem (one free dof) converges in one iteration
+    assert int(B.iterations[1]) <= 3
+
+
+def test_batch_zero_source_and_single_cell(gg):
+    """f = 0 gives x = 0 without iterating; n = 1 has no free dof."""
+    B = gg.BatchedPoissonProblems([1, 5], [np.ones(1), np.ones(125)])
+    x = B.assemble_solve(source=0.0, rtol=1e-8)
+    assert x.shape == (64,) and np.all(x == 0.0)
+    assert B.nconverged == 2 and int(B.iterations.max()) == 0
+
+
+def test_batch_every_shape_agrees(gg):
+    """Each candidate launch shape (fixed by set_shape) converges every problem to rtol; the
+    solutions agree within the CG tolerance."""
+    rng = np.random.default_rng(16)
+    sizes = [int(n) for n in rng.integers(3, 26, 20)]
+    kappas = [np.exp(1.5 * rng.standard_normal(n ** 3)) for n in sizes]
+    B = gg.BatchedPoissonProblems(sizes, kappas)
+    ref = None
+    for shape in [(256, 1), (1024, 1), (1024, 2), (512, 4), (1024, 4), (1024, 8)]:
+        try:
+            B.set_shape(*shape)
+        except gg._lib.GfeError:
+            continue  # a cluster shape this device cannot co-schedule
+        x = B.assemble_solve(source=1.0, rtol=1e-9)
+        assert B.nconverged == len(sizes) and B.shape() == shape
+        if ref is None:
+            ref = x
+        else:
+            for a, b in zip(B.split(x), B.split(ref)):
+                assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b)
+    assert ref is not None

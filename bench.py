@@ -828,13 +828,14 @@ def bench_elasticity(args, gg, ctx, lib, timed):
     return out
 
 
-# ---- Q2 on jittered hexahedra: FP64 cells vs TF32 tensor-core cells -------------------------
+# ---- Q2 on jittered hexahedra: FP64 cells vs tensor-core cells ------------------------------
 def bench_q2(args, gg, ctx, lib, timed):
     """64^3 Q2 Poisson on jittered hexahedra (2,048,383 free dofs): symbolic + numeric
     assembly + mixed CG (FP32 inner, FP64 reliable updates) to 1e-8, once with FP64 cell
-    matrices and once with TF32 tensor-core cell matrices (tcgen05, FP32 accumulation, FP64
-    Jacobians), FP64 scatter in both. Reports the element kernel's rate against the dense
-    bf16/tf32 tensor peak it runs on, and the TF32 result's error against FP64."""
+    matrices and once with tensor-core cell matrices (tcgen05 kind::f16, per-cell-scaled FP16
+    operands with TF32's 11 significant bits, FP32 accumulation and geometry), FP64 scatter in
+    both. Reports the element kernel's rate against the dense bf16 tensor peak, and the
+    tensor-core result's error against FP64."""
     import ctypes
     import torch
     from gridap_gb300 import _lib, workloads
@@ -907,7 +908,13 @@ def bench_q2(args, gg, ctx, lib, timed):
                                         "ms_per_step": rj["ms"],
                                         "iterations": rj["reps"][-1].iterations,
                                         "relres": rj["reps"][-1].relres}
-    out["fp32"]["element_kernel"] = "tcgen05 kind::tf32 (M=128, N=32, K=88), FP32 accumulate"
+    out["fp32"]["element_kernel"] = ("k_q2_metric (FP32 geometry -> FP16 metric tiles in the "
+                                     "MMA operand layout, FP32 load vectors) + k_q2_cells_tc "
+                                     "(tcgen05 kind::f16, per-cell-scaled FP16 operands with "
+                                     "TF32's 11 significant bits, FP32 accumulate: every cell "
+                                     "matrix one column of [729 x 176] x [176 x cells], M=128 "
+                                     "matrix entries, N=64 cells, K=176; metric tiles by TMA "
+                                     "bulk copies; zero row sums kept exact)")
     if peak_tf and out["fp32"]["element_tflops"]:
         out["fp32"]["element_frac_of_bf16_dense_peak"] = out["fp32"]["element_tflops"] / peak_tf
     rp, _, z64 = vals["fp64"]

@@ -640,9 +640,9 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
       if (src_kind == GFE_SRC_NONE)
         GFE_CUDA_TRY(cudaMemsetAsync(bf, 0, sizeof(float) * (size_t)ncells * nn, ctx->stream));
       timer_begin(ctx, GFE_KT_ELEMENT);
-      GFE_TRY(launch_q2_cells_tf32(ctx, ncells, (const int32_t*)vn, (const double*)vc,
-                                   ctx->scratch[SCR_TMP1].as<double>(), p->coef_kind, d_coef,
-                                   src_kind, d_src, Kf, bf));
+      GFE_TRY(launch_q2_cells_tc(ctx, ncells, (const int32_t*)vn, (const double*)vc,
+                                 ctx->scratch[SCR_TMP1].as<double>(), tabs.data(),
+                                 p->coef_kind, d_coef, src_kind, d_src, Kf, bf));
       timer_end(ctx);
       GFE_TRY(check_device_error(ctx, "assemble (Q2 tensor-core cell integrals)"));
       StoredCellsF32 s{};

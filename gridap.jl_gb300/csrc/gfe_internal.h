@@ -121,6 +121,7 @@ struct gfe_ctx {
   // limit of the first wait of the bounded mbarrier waits in the lattice SpMV (ns); 0 makes
   // that wait give up at once (gfe_ctx_set_wait_limit, for tests of the timeout path)
   unsigned long long first_wait_ns = 1000000000ull;
+  bool q2tab_valid = false;  // scratch[SCR_Q2TAB] holds the tensor-core Q2 E table
 };
 
 struct gfe_matrix {
@@ -213,6 +214,7 @@ enum ScratchId {
   SCR_SOLVER2,
   SCR_REDUCE,
   SCR_DIRI,
+  SCR_Q2TAB,  // the tensor-core Q2 kernel's E table (built once per context)
   SCR_COUNT
 };
 static_assert(SCR_COUNT <= 18, "scratch slots");
@@ -285,11 +287,12 @@ int assemble_cellvecs(gfe_ctx* ctx, int64_t ncells, int nd, const int32_t* d_row
                       const double* d_cellvecs, int64_t nrows, double* d_b);
 int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* d_b);
 
-// tensor-core Q2 cell integrals (gfe_q2_tc.cu)
-int launch_q2_cells_tf32(gfe_ctx* ctx, int64_t ncells, const int32_t* cell_vertices,
-                         const double* coords, const double* tabs, int coef_kind,
-                         const double* coef, int src_kind, const double* src, float* K,
-                         float* bvec);
+// tensor-core Q2 cell integrals (gfe_q2_tc.cu); tabs (device) and htabs (host) hold the same
+// FP64 reference tables w | phi2 | dphi1 | B
+int launch_q2_cells_tc(gfe_ctx* ctx, int64_t ncells, const int32_t* cell_vertices,
+                       const double* coords, const double* tabs, const double* htabs,
+                       int coef_kind, const double* coef, int src_kind, const double* src,
+                       float* K, float* bvec);
 
 // learned block preconditioner (gfe_learned.cu); `skip` (device int, may be null) makes the
 // kernels return at once when non-zero

@@ -6,7 +6,7 @@ Sizes (stated here, as the oracle's cost sets them):
     configuration, assembled by the closed-form Cartesian pattern and the fused row gather,
     solved by the multigrid-preconditioned mixed-precision FCG;
   - 64^3 jittered Q2 Poisson (2,048,383 free dofs, nnz 127,263,527): the whole configuration,
-    FP64 cells and TF32 tensor-core cells;
+    FP64 cells and tensor-core cells (FP16 operands with TF32's 11 significant bits);
   - simplexify(24^3) vector P2 elasticity (345,744 free dofs): the oracle restates Gridap's
     per-point steps and needs about half a minute here; the 48^3 configuration runs the same
     kernels on a larger grid (the benchmark compares it at full size).
@@ -15,7 +15,7 @@ Tolerances:
   - CSR pattern: bit-exact (the oracle's CSC arrays are the CSR arrays of these symmetric
     matrices);
   - FP64 matrix values: |a - a_ref| <= 1e-12 * max |row of a_ref|; vectors: 1e-12 * max |b_ref|;
-  - TF32 tensor-core Q2 cells: 2e-3 of the row maximum (matrix) and of max |b_ref| (vector);
+  - tensor-core Q2 cells: 2e-3 of the row maximum (matrix) and of max |b_ref| (vector);
   - solutions: the FP64 relative residual of the device solution in the oracle's own system
     <= rtol (1 + 1e-3), and the distance to the oracle's solution <= 1e3 * rtol relative.
 """

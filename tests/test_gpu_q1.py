@@ -586,9 +586,10 @@ def test_q2_fp64_matches_oracle(gg, orc, part, jit):
 
 
 def test_q2_tensor_core_cells_close_to_fp64(gg, orc):
-    """TF32 tensor-core Q2 cell matrices (tcgen05, FP32 accumulate, FP64 Jacobians) against
-    the FP64 path on distorted cells: |A_tf32 - A_fp64| <= 2e-3 * row max (TF32 keeps 10
-    mantissa bits; the scatter-add is FP64 in both)."""
+    """Tensor-core Q2 cell matrices (tcgen05 kind::f16 with per-cell-scaled FP16 operands,
+    FP32 accumulate, FP32 geometry) against the FP64 path on distorted cells:
+    |A_tc - A_fp64| <= 2e-3 * row max (the operands keep 11 significant bits, as TF32; the
+    scatter-add is FP64 in both); the FP32 cell vectors within 1e-5."""
     rng = np.random.default_rng(71)
     part = (7, 6, 5)
     nn = 8 * 7 * 6

@@ -797,6 +797,43 @@ def bench_elasticity(args, gg, ctx, lib, timed):
                                  "iterations": rj["reps"][-1].iterations,
                                  "relres": rj["reps"][-1].relres}
     out["nnz"] = info.get("nnz")
+    # the element kernels of general affine tets (node coordinates) on the same mesh: the
+    # FP32 cells come from the tensor cores (k_p2_metric + k_p2_cells_tc), the FP64 cells from
+    # the CUDA-core kernel; assembly only
+    preps_n = {p: gg.prepare_problem(V, V, dO, (lam, mu), force, precision=p, geometry="nodal")
+               for p in ("fp64", "fp32")}
+
+    def assemble_nodal(prec):
+        h = ctypes.c_void_p()
+        _lib.check(lib.gfe_symbolic_loop_matrix(ctx.handle, ncells, nd, _lib.ptr(ids_d),
+                                                _lib.ptr(ids_d), nfree, nfree, ctypes.byref(h)))
+        try:
+            _lib.check(lib.gfe_assemble_matrix_and_vector(
+                ctx.handle, ctypes.byref(preps_n[prec].p), h, _lib.ptr(b)))
+        finally:
+            lib.gfe_matrix_destroy(h)
+
+    tc = {}
+    peak, _ = peaks()
+    for prec in ("fp32", "fp64"):
+        r = timed("elast_nodal_" + prec, lambda: assemble_nodal(prec), 2, 1)
+        el_tot, el_n = r["kt"][_lib.GFE_KT_ELEMENT]
+        el_ms = el_tot / el_n if el_n else float("nan")
+        # algorithmic: the 9 x 9 by 9 x 100 product per cell; bytes: the FP32 (FP64) cell
+        # matrix and the FP64 cell vector written, vertex ids, coordinates and Lame read
+        flops = 2.0 * 900 * 9 * ncells
+        esz = 4 if prec == "fp32" else 8
+        nbytes = ncells * (900 * esz + 30 * 8 + 4 * 4 + 4 * 3 * 8 + 16)
+        tc[prec] = {"element_kernel_ms": el_ms,
+                    "element_tflops": flops / (el_ms * 1e-3) / 1e12,
+                    "element_gbs": nbytes / (el_ms * 1e-3) / 1e9,
+                    "element_frac_of_hbm": nbytes / (el_ms * 1e-3) / 1e9 / peak,
+                    "assembly_ms_per_step": r["ms"]}
+    tc["fp32"]["kernel"] = ("k_p2_metric + k_p2_cells_tc: tcgen05 kind::f16 with split FP16 "
+                            "operands (about 22 significant bits), M=128 entries, N=144 (9 "
+                            "(k,l) x 16 cells), K=32; output-bound")
+    tc["fp64"]["kernel"] = "k_p2_elasticity_cells<double> (thread per tet, CUDA cores)"
+    out["general_tet_element_kernels"] = tc
     out["fp32_cells_solution_rel_l2_vs_fp64"] = float(
         torch.linalg.norm(sols["fp32"] - sols["fp64"]) / torch.linalg.norm(sols["fp64"]))
     if not args.no_parity:

@@ -16,7 +16,8 @@
 //     so the cell matrix is lambda_c Kl[t] + mu_c Km[t] from 2 x 6 tables (built on the host
 //     from Gridap's per-quadrature-point steps in extended precision);
 //   - general affine tets (node coordinates + tet vertex ids): an element kernel evaluates the
-//     formula above per cell, with the Jacobian, its inverse and determinant in FP64.
+//     formula above per cell, with the Jacobian, its inverse and determinant in FP64 (FP32
+//     cell matrices: the tensor-core kernels of gfe_p2_tc.cu).
 #include <cmath>
 #include <vector>
 
@@ -275,22 +276,25 @@ int assemble_p2_elasticity(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, do
   GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   const double* dG = ctx->scratch[SCR_TMP1].as<double>();
   const size_t esz = fp32 ? sizeof(float) : sizeof(double);
-  if (A) GFE_TRY(ctx->scratch[SCR_CELLMAT].reserve(esz * (size_t)ncells * 900));
+  const int64_t ncells16 = (ncells + 15) / 16 * 16;  // whole tiles of the tensor-core layout
+  if (A) GFE_TRY(ctx->scratch[SCR_CELLMAT].reserve(esz * (size_t)ncells16 * 900));
   if (d_b) GFE_TRY(ctx->scratch[SCR_CELLVEC].reserve(sizeof(double) * (size_t)ncells * 30));
   double* bv = d_b ? ctx->scratch[SCR_CELLVEC].as<double>() : nullptr;
   const unsigned g = (unsigned)((ncells + 127) / 128);
   if (A) {
     timer_begin(ctx, GFE_KT_ELEMENT);
-    if (fp32)
-      k_p2_elasticity_cells<float><<<g, 128, 0, ctx->stream>>>(
-          ncells, (const double*)vc, (const int32_t*)vn, p->coef_kind, d_coef, d_f, dG,
-          dG + 900, ctx->scratch[SCR_CELLMAT].as<float>(), bv, ctx->d_err);
-    else
+    if (fp32) {
+      // the tensor-core cells (gfe_p2_tc.cu): split FP16 operands, FP32 accuracy
+      GFE_TRY(launch_p2_cells_tc(ctx, ncells, (const double*)vc, (const int32_t*)vn,
+                                 p->coef_kind, d_coef, d_f, dG + 900, G.data(),
+                                 ctx->scratch[SCR_CELLMAT].as<float>(), bv));
+    } else {
       k_p2_elasticity_cells<double><<<g, 128, 0, ctx->stream>>>(
           ncells, (const double*)vc, (const int32_t*)vn, p->coef_kind, d_coef, d_f, dG,
           dG + 900, ctx->scratch[SCR_CELLMAT].as<double>(), bv, ctx->d_err);
+      ctx->launches++;
+    }
     timer_end(ctx);
-    ctx->launches++;
   } else if (bv) {
     // vector only: the element kernel without matrix output is not worth a separate path
     GFE_TRY(ctx->scratch[SCR_CELLMAT].reserve(sizeof(float) * (size_t)ncells * 900));
@@ -315,11 +319,8 @@ int assemble_p2_elasticity(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, do
   am.b = nullptr;
   const bool lift = A && bv && a.uD;
   if (fp32) {
-    StoredCellsF32 src{};
+    TiledCellsF32 src{};
     src.mat = A ? ctx->scratch[SCR_CELLMAT].as<float>() : nullptr;
-    src.cs = 1;
-    src.es = ncells;
-    src.vec = nullptr;
     src.ntab = 0;
     if (A) GFE_TRY(run_rows(ctx, am, src, maxw, A->pos_bytes));
     if (lift) GFE_TRY(dirichlet_lift(ctx, a, src));

@@ -293,6 +293,13 @@ int launch_q2_cells_tc(gfe_ctx* ctx, int64_t ncells, const int32_t* cell_vertice
                        const double* coords, const double* tabs, const double* htabs,
                        int coef_kind, const double* coef, int src_kind, const double* src,
                        float* K, float* bvec);
+// tensor-core P2 elasticity cells of affine tets (gfe_p2_tc.cu): K tile-major FP32
+// (K[((cell/16)*900 + li + lj*30)*16 + cell%16], room for whole 16-cell tiles), b entry-major
+// FP64 (b[li*ncells + cell]); hGref the host reference integrals
+int launch_p2_cells_tc(gfe_ctx* ctx, int64_t ncells, const double* coords,
+                       const int32_t* tet_vertices, int coef_kind, const double* coef,
+                       const double* f, const double* mref, const double* hGref, float* K,
+                       double* bvec);
 
 // learned block preconditioner (gfe_learned.cu); `skip` (device int, may be null) makes the
 // kernels return at once when non-zero

@@ -52,6 +52,20 @@ struct StoredCellsF32 {
   }
 };
 
+// FP32 cell matrices in 16-cell tiles (the tensor-core P2 kernels' layout): entry e = li +
+// lj*nd of cell c at mat[((c / 16) * nd*nd + e) * 16 + c % 16], so the 16 cells of a tile are
+// contiguous per entry. No cell vectors.
+struct TiledCellsF32 {
+  const float* mat;
+  int ntab;
+  __device__ void load_tables(double*) const {}
+  __device__ __forceinline__ int64_t cell(int64_t c) const { return c; }
+  __device__ __forceinline__ double m(const double*, int64_t cell, int li, int lj, int nd) const {
+    return (double)__ldg(mat + (((cell >> 4) * nd * nd + li + lj * nd) << 4) + (cell & 15));
+  }
+  __device__ __forceinline__ double v(const double*, int64_t, int) const { return 0.0; }
+};
+
 // Stored cell arrays. Entry (cell, li, lj) at mat[cell*cs + (li + lj*nd)*es].
 struct StoredCells {
   const double* mat;

@@ -165,3 +165,53 @@ def test_p2_two_level_fcg(gg, orc, part):
     ref = orc.elasticity_p2((0, 1) * 3, part, lame)
     ro = ref["b"] - orc.csc_mul(*ref["csc"], x)
     assert np.linalg.norm(ro) <= 1.01e-8 * np.linalg.norm(ref["b"])
+
+
+def _oracle_jittered(orc, part, lame, jit, f=(0.0, 0.0, -1.0)):
+    """The oracle's elasticity_p2 on a simplexified box whose nodes are displaced by `jit`
+    (the clamped face chosen on the undisplaced nodes, as the model's tag is)."""
+    part = np.asarray(part, np.int64)
+    coords, _, _ = orc.cartesian_model((0, 1) * 3, part)
+    tv = orc.simplex_cells(part)
+    vmask = np.abs(coords[:, 0]) < 1e-12
+    cd, nfree, _ = orc.simplex_p2_numbering(part, vmask)
+    x, w, _ = orc.wv_tet_degree5()
+    xj = np.ascontiguousarray(coords + jit)
+    nc = tv.shape[0]
+    mats = np.empty((nc, 30, 30))
+    vecs = np.empty((nc, 30))
+    lm = np.ascontiguousarray(lame, np.float64).reshape(-1)
+    fv = np.ascontiguousarray(f, np.float64)
+    rc = orc.lib().orc_p2tet_cell_arrays_elasticity(nc, orc._p(tv), orc._p(xj), orc._p(lm), 14,
+                                                    orc._p(x), orc._p(w), orc._p(fv),
+                                                    orc._p(mats), orc._p(vecs))
+    assert rc == 0
+    mats = np.ascontiguousarray(np.transpose(mats, (0, 2, 1)))
+    return dict(nfree=nfree, csc=orc.assemble_csc(cd, cd, mats, nfree, nfree),
+                b=orc.assemble_vector(cd, vecs, nfree))
+
+
+@pytest.mark.parametrize("part", [(3, 3, 2), (5, 4, 4)])
+def test_p2_tensor_core_cells_jittered_match_oracle(gg, orc, part):
+    """FP32 cell matrices of general affine tets from the tensor cores (tcgen05 kind::f16
+    with split FP16 operands: about 22 significant bits) against the oracle's FP64 cell
+    integrals on displaced nodes: within 1e-5 of each row's largest entry (the FP32 path's
+    tolerance), the load vector (FP64) within 1e-12, the pattern bit-exact."""
+    rng = np.random.default_rng(95 + part[0])
+    m, V = _space(gg, part)
+    h = 1.0 / np.asarray(part, np.float64)
+    jit = rng.uniform(-0.1, 0.1, m.node_coords.shape) * h
+    m.node_coords[:] += jit
+    lame = np.exp(rng.standard_normal((m.num_cells(), 2)))
+    ref = _oracle_jittered(orc, part, lame, jit)
+    assert V.nfree == ref["nfree"]
+    A, b = _assemble(gg, V, m, lame, precision="fp32", geometry="nodal")
+    rp, cv, nz = A.export_csr(1)
+    cp, rv, zv = ref["csc"]
+    assert np.array_equal(rp, cp) and np.array_equal(cv, rv)
+    assert _rowscaled_err(rp - 1, nz, zv) <= 1e-5
+    assert np.abs(b - ref["b"]).max() <= 1e-12 * np.abs(ref["b"]).max()
+    # and the FP64 path on the same displaced nodes
+    A64, b64 = _assemble(gg, V, m, lame, precision="fp64", geometry="nodal")
+    _, _, nz64 = A64.export_csr(1)
+    assert _rowscaled_err(rp - 1, nz64, zv) <= TOL_VAL

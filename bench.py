@@ -153,7 +153,7 @@ def vcycle_bytes(n):
     rows, the first sweep (b, D read, x written: 12 R), three fused sweeps (kappa 4 C; x, b,
     D read and x written 16 R each), the fused residual (kappa 4 C; x, b read, r written
     12 R), restriction (r read 4 R, 4 Rc written) and prolongation (4 Rc and x read, x
-    written 8 R): 16 C + 84 R + 8 Rc per level; the coarsest level the first sweep and eight
+    written 8 R): 16 C + 84 R + 8 Rc per level; the coarsest level the first sweep and four
     fused ones."""
     lv = mg_levels(n)
     tot = 0
@@ -162,7 +162,7 @@ def vcycle_bytes(n):
         if i + 1 < len(lv):
             tot += 16 * C + 84 * R + 8 * (lv[i + 1] - 1) ** 3
         else:
-            tot += 12 * R + 8 * (4 * C + 16 * R)
+            tot += 12 * R + 4 * (4 * C + 16 * R)
     return tot
 
 
@@ -544,7 +544,7 @@ def run_gpu(args):
                                       "k_mg_residual, k_mg_restrict, k_mg_prolong over %d "
                                       "levels)"
                                       % len(mg_levels(args.n)),
-                               alg=vcycle_bytes(args.n), traffic=None,
+                               alg=vcycle_bytes(args.n), traffic=profile_traffic("vcycle"),
                                kt=r_mixed_kt["kt"][_lib.GFE_KT_PRECOND])
     table = {}
     for k, d in kinds.items():
@@ -613,6 +613,18 @@ def run_gpu(args):
         "gpu_launches": r_mixed["launches"],
         "clocks": clk.summary(),
     }
+    if "vcycle" in table:
+        # the V-cycle's vectors and kappa stay in L2 between its kernels: its bound is L2
+        # latency and launch overhead, its L2 traffic the relevant byte count
+        m = re.search(r"l2_bytes_per_launch_vcycle:\s*([0-9.eE+]+)",
+                      "".join(p.read_text() for p in sorted((ROOT / "profiles").glob("*.md"))))
+        l2b = float(m.group(1)) if m else None
+        vc = table["vcycle"]
+        out["roofline"]["vcycle_l2"] = {
+            "l2_bytes_per_launch": l2b,
+            "l2_gbs": l2b / (vc["avg_launch_ms"] * 1e-3) / 1e9 if l2b else None,
+            "note": "L2-resident (8.2 MB vectors at 128^3); DRAM traffic per cycle is the "
+                    "cold-cache ncu figure; bound by L2 latency and launch overhead"}
     if not args.no_batch:
         out["batched"] = bench_batched(args, gg, ctx, lib, barrier)
     if not args.no_elasticity:

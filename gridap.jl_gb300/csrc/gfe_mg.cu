@@ -10,7 +10,7 @@
 // nested Q1 spaces. Transfers are trilinear interpolation P and its transpose R = P^T (full
 // weighting 1, 1/2, 1/4, 1/8). Smoothing is damped Jacobi (omega 0.8, two sweeps before and
 // after, the first from zero), each later sweep fused into one pass over the lattice stencil;
-// the coarsest level takes nine sweeps. Levels of at most 512 rows run their part of the
+// the coarsest level takes five sweeps. Levels of at most 512 rows run their part of the
 // cycle in one block. All vectors are FP32 in the lattice row order; every kernel returns at
 // once when the solver's done flag is set.
 #include <utility>
@@ -25,7 +25,7 @@ namespace {
 
 constexpr int kMgBlock = 256;
 constexpr float kOmega = 0.8f;
-constexpr int kPreSweeps = 2, kCoarseSweeps = 8;
+constexpr int kPreSweeps = 2, kPostSweeps = 2, kCoarseSweeps = 4;
 
 __device__ __forceinline__ bool stop(const int* done) { return done && *done; }
 
@@ -146,10 +146,10 @@ __device__ __forceinline__ float prolong_value(int i, int j, int k, int mc0, int
   return s;
 }
 
-// xo_f = x_f + P x_c, out of place
+// xo_f = x_f + P x_c (xo may be xf: each thread reads and writes its own rows only)
 __global__ void k_mg_prolong(int mf0, int mf1, int mf2, int mc0, int mc1, int mc2,
-                             const float* __restrict__ xc, const float* __restrict__ xf,
-                             float* __restrict__ xo, const int* done) {
+                             const float* __restrict__ xc, const float* xf, float* xo,
+                             const int* done) {
   if (stop(done)) return;
   const int64_t nf = (int64_t)mf0 * mf1 * mf2;
   for (int64_t f = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; f < nf;
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(kCoarseBlock)
   for (int l = 0; l < c.nl; ++l) {
     const MgLevelView& L = c.L[l];
     first(L);
-    if (l + 1 == c.nl) {  // coarsest: eight more sweeps, ending in x
+    if (l + 1 == c.nl) {  // coarsest: four more sweeps, ending in x
       for (int s = 0; s < kCoarseSweeps; s += 2) {
         sweep(L, L.x, L.t);
         sweep(L, L.t, L.x);
@@ -378,7 +378,7 @@ unsigned vgrid(gfe_ctx* ctx, int64_t n) {
 // (a fused sweep cannot run in place); the sweep counts keep the result in L.x: the first
 // sweep from zero writes L.x, one more pre-sweep moves it to L.t, the residual goes to L.x,
 // prolongation writes L.x from L.t, and the two post-sweeps return to L.x. The coarsest
-// level takes the first sweep and eight more.
+// level takes the first sweep and four more.
 int vcycle(LatticeMG* mg, size_t l, const int* done) {
   gfe_ctx* ctx = mg->ctx;
   LatticeMG::Level& L = mg->lv[l];
@@ -457,11 +457,15 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
                                                                oth, C.b, done);
   ctx->launches += 2;
   GFE_TRY(vcycle(mg, l + 1, done));
+  // x + P x_c into the buffer that the post-sweeps then leave the result in L.x from (in
+  // place when that is where x already is)
+  float* post0 = kPostSweeps % 2 == 0 ? L.x : L.t;
   k_mg_prolong<<<g, kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, L.m2, C.m0, C.m1, C.m2, C.x, cur,
-                                                oth, done);
+                                                post0, done);
   ctx->launches++;
-  std::swap(cur, oth);
-  for (int s = 0; s < kPreSweeps; ++s) {
+  cur = post0;
+  oth = post0 == L.x ? L.t : L.x;
+  for (int s = 0; s < kPostSweeps; ++s) {
     smooth(cur, oth);
     std::swap(cur, oth);
   }

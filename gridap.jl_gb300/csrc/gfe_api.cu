@@ -155,12 +155,15 @@ static int symbolic_loop(gfe_ctx* ctx, int64_t ncells, int ndr, int ndc,
   A->ncells = ncells;
   const size_t rsz = sizeof(int32_t) * (size_t)ncells * ndr;
   const size_t csz = sizeof(int32_t) * (size_t)ncells * ndc;
+  // square cells given one array for rows and columns (every FESpace assembled against
+  // itself): one copy serves both
+  A->cols_alias = cell_cols == cell_rows && ndc == ndr;
   int s = A->cell_rows.reserve(rsz);
-  if (s == GFE_OK) s = A->cell_cols.reserve(csz);
+  if (s == GFE_OK && !A->cols_alias) s = A->cell_cols.reserve(csz);
   if (s == GFE_OK && rsz) {
     cudaError_t e = cudaMemcpyAsync(A->cell_rows.ptr, cell_rows, rsz, cudaMemcpyDefault,
                                     ctx->stream);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && !A->cols_alias)
       e = cudaMemcpyAsync(A->cell_cols.ptr, cell_cols, csz, cudaMemcpyDefault, ctx->stream);
     if (e != cudaSuccess) s = set_error(GFE_ERR_CUDA, "copy cell ids: %s", cudaGetErrorString(e));
   }

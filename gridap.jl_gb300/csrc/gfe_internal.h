@@ -139,6 +139,11 @@ struct gfe_matrix {
   gfe::DevBuf rowptr, colval, val;
   // cell ids the pattern was built from (device copies)
   gfe::DevBuf cell_rows, cell_cols;
+  // the column ids are the row ids (square cells given the same array): cell_cols stays empty
+  bool cols_alias = false;
+  const int32_t* col_ids() const {
+    return cols_alias ? cell_rows.as<int32_t>() : cell_cols.as<int32_t>();
+  }
   // row -> (cell*nd + local row) references, sorted by cell: the row-gather assembly lists
   gfe::DevBuf ref_ptr, refs;
   // position of every (reference, local column) in its row's column list, cols_per_cell()

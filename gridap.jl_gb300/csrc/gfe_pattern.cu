@@ -519,7 +519,7 @@ int build_refs(gfe_ctx* ctx, gfe_matrix* A) {
 }
 
 int build_pattern(gfe_ctx* ctx, gfe_matrix* A) {
-  const int32_t* cols = A->cell_cols.as<int32_t>();
+  const int32_t* cols = A->col_ids();
   const int64_t nrows = A->nrows;
   // 1. refs (ctx scratch TMP0 keeps the per-row reference counts afterwards)
   GFE_TRY(build_refs(ctx, A));
@@ -778,7 +778,7 @@ int cartesian_ids_match(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1, int
   GFE_TRY(flag.reserve(sizeof(int)));
   GFE_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
   k_cart_check<<<grid_for(A->ncells, 256, (int64_t)ctx->num_sms * 16), 256, 0, ctx->stream>>>(
-      A->cell_rows.as<int32_t>(), A->cell_cols.as<int32_t>(), (int)n0, (int)n1, (int)n2,
+      A->cell_rows.as<int32_t>(), A->col_ids(), (int)n0, (int)n1, (int)n2,
       flag.as<int>());
   ctx->launches++;
   int bad = 1;
@@ -816,7 +816,7 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
   GFE_TRY(flag.reserve(sizeof(int)));
   GFE_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
   k_cart_check<<<grid_for(ncells, 256, (int64_t)ctx->num_sms * 16), 256, 0, ctx->stream>>>(
-      A->cell_rows.as<int32_t>(), A->cell_cols.as<int32_t>(), (int)n0, (int)n1, (int)n2,
+      A->cell_rows.as<int32_t>(), A->col_ids(), (int)n0, (int)n1, (int)n2,
       flag.as<int>());
   ctx->launches++;
   int bad = 1;

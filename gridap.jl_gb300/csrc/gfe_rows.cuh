@@ -377,7 +377,7 @@ static RowArgs row_args(gfe_ctx* ctx, gfe_matrix* A, double* b, bool with_matrix
   a.colval = A->colval.as<int32_t>();
   a.ref_ptr = A->ref_ptr.as<int64_t>();
   a.refs = A->refs.as<int32_t>();
-  a.cell_cols = A->cell_cols.as<int32_t>();
+  a.cell_cols = A->col_ids();
   a.refpos = A->refpos.ptr;
   a.val = with_matrix ? A->val.as<double>() : nullptr;
   a.b = b;

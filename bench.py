@@ -732,7 +732,8 @@ def bench_batched(args, gg, ctx, lib, barrier):
             "sizes": "n^3 cells, n uniform in 16..64 (seeded)", "rtol": rtol,
             "ms_per_step": 1e3 * t_batch, "problems_per_s": len(sizes) / t_batch,
             "dof_per_s": dofs / t_batch, "gpu_launches_per_step": launches,
-            "launch_shape": {"threads_per_cta": B.shape()[0], "ctas_per_problem": B.shape()[1]},
+            "launch_shape": {"threads_per_cta": B.shape()[0], "ctas_per_cluster": B.shape()[1],
+                             "cluster_threshold": B.shape()[2]},
             "max_iterations": int(it_b.max()), "mean_iterations": float(it_b.mean()),
             "sequential": {"ms": 1e3 * t_seq, "problems_per_s": len(sizes) / t_seq,
                            "dof_per_s": dofs / t_seq, "timing": "host clock, one pass"},

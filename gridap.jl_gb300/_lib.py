@@ -160,8 +160,8 @@ SIGNATURES = {
     "gfe_batch_create": (C.c_int, [_P, C.c_int32, _P, _P, C.POINTER(C.c_void_p)]),
     "gfe_batch_destroy": (C.c_int, [_P]),
     "gfe_batch_info": (C.c_int, [_P, _I64P, _I64P, _I64P]),
-    "gfe_batch_shape": (C.c_int, [_P, _P, _P]),
-    "gfe_batch_set_shape": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "gfe_batch_shape": (C.c_int, [_P, _P, _P, _P]),
+    "gfe_batch_set_shape": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_double]),
     "gfe_batch_assemble_solve": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32, _P, _P,
                                            C.POINTER(C.c_int32)]),
     "gfe_cg_solve_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, _P, _P, C.c_double,

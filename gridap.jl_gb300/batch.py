@@ -5,10 +5,11 @@ Each problem is -div(kappa grad u) = f on the unit cube with an (n, n, n) Cartes
 per-cell kappa (Gridap's cell order), constant f and homogeneous Dirichlet data on the
 boundary; the free dofs follow Gridap's CLagrangian numbering of a space with
 dirichlet_tags="boundary" (interior nodes in node order). One persistent kernel launch solves
-them all: CTAs, or thread-block clusters of CTAs, take problems largest first from a work
-counter and each runs a Jacobi-PCG on its problem, the operator applied matrix-free in FP32
-from the cell coefficients, with FP64 reliable updates whose FP64 true residual decides
-convergence (||b - A x|| <= rtol ||b||). Gridap has no batched driver: the per-problem result equals
+them all: thread-block clusters take the large problems largest first from a work counter and
+solve each together, then every CTA takes the small ones alone from a second counter; each
+problem runs a Jacobi-PCG, the operator applied matrix-free in FP32 from the cell
+coefficients, with FP64 reliable updates whose FP64 true residual decides convergence
+(||b - A x|| <= rtol ||b||). Gridap has no batched driver: the per-problem result equals
 AffineFEOperator + solve with a Jacobi-preconditioned CG to the same tolerance.
 """
 from __future__ import annotations
@@ -57,15 +58,17 @@ class BatchedPoissonProblems:
         return out
 
     def shape(self):
-        """(threads per CTA, CTAs per problem) the autotuner chose; (0, 0) before a solve."""
-        t, b = C.c_int32(), C.c_int32()
-        _lib.check(_lib.load().gfe_batch_shape(self.handle, C.byref(t), C.byref(b)))
-        return t.value, b.value
+        """(threads per CTA, CTAs per cluster, cluster threshold) the autotuner chose;
+        (0, 0, 0.0) before a solve."""
+        t, c, g = C.c_int32(), C.c_int32(), C.c_double()
+        _lib.check(_lib.load().gfe_batch_shape(self.handle, C.byref(t), C.byref(c), C.byref(g)))
+        return t.value, c.value, round(g.value, 6)
 
-    def set_shape(self, threads, ctas_per_problem):
-        """Fixes the launch shape (one of the candidates); (0, 0) re-enables autotuning."""
+    def set_shape(self, threads, ctas_per_problem, cluster_threshold=0.0):
+        """Fixes the schedule (one of the candidates); (0, 0) re-enables autotuning."""
         _lib.check(_lib.load().gfe_batch_set_shape(self.handle, int(threads),
-                                                   int(ctas_per_problem)))
+                                                   int(ctas_per_problem),
+                                                   float(cluster_threshold)))
 
     def split(self, x):
         return [x[self.offsets[i]:self.offsets[i + 1]] for i in range(len(self.sizes))]

@@ -42,12 +42,14 @@ struct PArgs {
   int32_t nproblems;
   const BProb* probs;
   const int32_t* order;   // problems by decreasing size
-  int* counter;           // work counter (zeroed before the launch)
+  int* counter;           // work counter of the large problems (zeroed before the launch)
+  int* counter2;          // work counter of the small problems
+  int32_t nlarge;         // order[0 .. nlarge) are solved by clusters, the rest by single CTAs
   const double* coef;     // kappa / h^2 per cell, problems one after the other
   double f;               // the load at every row (constant source)
   double rtol2;
   int32_t maxit;
-  float* scratch;         // per thread block: kap32 | d | x | r | p | q
+  float* scratch;         // per CTA: kap32 | d | x | r | p | q (a cluster uses its rank 0's)
   int64_t cell_stride, row_stride;
   double* x;              // FP64 solutions, problems one after the other
   int32_t* iters;
@@ -280,25 +282,198 @@ __device__ __forceinline__ float march_tile(int n, int c1, int bx, int by, int k
   return pq;
 }
 
-// The solve of every problem: CS CTAs (one cluster; CS = 1: one CTA) per problem, problems
-// from the work counter largest first. The operator phase splits the problem's tiles between
-// the cluster's CTAs (tile t to rank t mod CS), the vector phases its rows (contiguous
-// ranges). Every branch depends only on cluster-wide sums, which all CTAs form in the same
-// order, so all CTAs of a cluster take the same path through the same barriers.
+// One problem solved by a group of CS CTAs (a cluster; CS = 1: one CTA): the operator phase
+// splits the problem's tiles between the group's CTAs (tile t to rank t mod CS), the vector
+// phases its rows (contiguous ranges). Every branch depends only on group-wide sums, which
+// all CTAs form in the same order, so all CTAs of a group take the same path through the
+// same barriers. base: the group's scratch (kap32 | d | x | r | p | q).
 template <int NT, int CS>
-__global__ void __launch_bounds__(NT, (1024 / NT > 0 ? 1024 / NT : 1)) k_b_solve(const __grid_constant__ PArgs a) {
-  __shared__ BShared<NT> sh;
+__device__ __forceinline__ void solve_one(const PArgs& a, BShared<NT>& sh, int& slot,
+                                          uint32_t rank, float* base, int pi) {
   const int tid = threadIdx.x;
-  const uint32_t rank = CS > 1 ? cluster_rank() : 0u;
-  const int64_t group = (int64_t)blockIdx.x / CS;
-  float* kap32 = a.scratch + group * (a.cell_stride + 5 * a.row_stride);
+  float* kap32 = base;
   float* dv = kap32 + a.cell_stride;
   float* x32 = dv + a.row_stride;
   float* r32 = x32 + a.row_stride;
   float* p32 = r32 + a.row_stride;
   float* q32 = p32 + a.row_stride;
   const float* W = a.W32;  // kernel parameter space, read through the constant cache
+  const BProb P = a.probs[pi];
+  const int n = P.n, m = n - 1;
+  const int c1 = (n + 3) & ~3;
+  const int R = m * m * m;  // < 2^31 (n <= 1024)
+  const double* kap = a.coef + P.cell0;
+  double* x64 = a.x + P.xoff;
+  const int r0 = (int)((int64_t)R * rank / CS), r1 = (int)((int64_t)R * (rank + 1) / CS);
+  const int tx = (m + 31) / 32, ty = (m + NT / 32 - 1) / (NT / 32), tz = (m + kBZ - 1) / kBZ;
+  const int ntile = tx * ty * tz;
+  int iters = 0, converged = 0;
+  if (R > 0) {
+    // set-up: FP32 kappa (this CTA's cell layers), Jacobi diagonal, x = 0, r = b = f,
+    // p = D^-1 r
+    const int64_t nlay = (int64_t)n * n;
+    for (int64_t c = (int64_t)rank * nlay * n / CS + tid;
+         c < ((int64_t)rank + 1) * nlay * n / CS; c += NT) {
+      const int64_t ck = c / nlay, rest = c - ck * nlay, cj = rest / n, ci = rest - cj * n;
+      kap32[ci + (int64_t)c1 * (cj + (int64_t)n * ck)] = (float)kap[c];
+    }
+    double rz = 0.0, bb = 0.0;
+    const float fb = (float)a.f;
+    for (int r = r0 + tid; r < r1; r += NT) {
+      int i, j, k;
+      row_ijk3(r, m, i, j, k);
+      float ks = 0.f;
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        ks += (float)kap[(i + (e & 1)) + (int64_t)n * ((j + ((e >> 1) & 1)) +
+                                                        (int64_t)n * (k + (e >> 2)))];
+      const float d = 1.f / (W[0] * ks);
+      dv[r] = d;
+      x64[r] = 0.0;
+      x32[r] = 0.f;
+      r32[r] = fb;
+      p32[r] = d * fb;
+      rz += (double)fb * (double)(d * fb);
+      bb += a.f * a.f;
+    }
+    group_sum2<NT, CS>(rz, bb, sh, slot);  // also publishes kap32 and p32 to the cluster
+    const double tol2 = a.rtol2 * bb;
+    double rmax2 = bb;
+    bool done = !(bb > 0.0);
+    converged = done;
+    while (!done) {
+      // q = A p over this CTA's tiles; p.q
+      double pq = 0.0, unused = 0.0;
+      for (int t = (int)rank; t < ntile; t += CS) {
+        const int bx = t % tx, by = (t / tx) % ty, bz = t / (tx * ty);
+        pq += (double)march_tile<NT>(n, c1, bx, by, bz * kBZ, kap32, p32, q32, W);
+      }
+      group_sum2<NT, CS>(pq, unused, sh, slot);
+      const float alpha = (float)(rz / pq);
+      // x += alpha p, r -= alpha q over this CTA's rows; r.z and r.r
+      double rzn = 0.0, rr = 0.0;
+      for (int base = r0 + tid; base < r1; base += kU * NT) {
+        // kU rows a thread: all loads issued before the first use
+        float xv[kU], pv[kU], qv[kU], rv[kU], dd[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int r = base + u * NT;
+          if (r < r1) {
+            xv[u] = x32[r];
+            pv[u] = p32[r];
+            qv[u] = q32[r];
+            rv[u] = r32[r];
+            dd[u] = dv[r];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int r = base + u * NT;
+          if (r < r1) {
+            x32[r] = fmaf(alpha, pv[u], xv[u]);
+            const float ri = fmaf(-alpha, qv[u], rv[u]);
+            r32[r] = ri;
+            rzn += (double)ri * (double)(dd[u] * ri);
+            rr += (double)ri * ri;
+          }
+        }
+      }
+      group_sum2<NT, CS>(rzn, rr, sh, slot);
+      ++iters;
+      if (!isfinite(rr) || !isfinite(rzn) || !isfinite(pq)) {
+        if (tid == 0 && rank == 0 && atomicCAS(&a.err->code, 0, GFE_ERR_NONFINITE) == 0)
+          a.err->index = pi;
+        break;
+      }
+      if (rr <= (double)kDelta * kDelta * rmax2 || rr <= tol2 || iters >= a.maxit) {
+        // reliable update: x64 += x32, then r = b - A x64 in FP64 from the FP64 kappa
+        for (int base = r0 + tid; base < r1; base += kU * NT) {
+          double xv[kU];
+          float xs[kU];
+#pragma unroll
+          for (int u = 0; u < kU; ++u) {
+            const int r = base + u * NT;
+            if (r < r1) {
+              xv[u] = x64[r];
+              xs[u] = x32[r];
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < kU; ++u) {
+            const int r = base + u * NT;
+            if (r < r1) {
+              x64[r] = xv[u] + (double)xs[u];
+              x32[r] = 0.f;
+            }
+          }
+        }
+        group_sync<CS>();
+        double rr64 = 0.0;
+        rzn = 0.0;
+        for (int r = r0 + tid; r < r1; r += NT) {
+          int i, j, k;
+          row_ijk3(r, m, i, j, k);
+          const double res = a.f - class_apply<double>(i, j, k, m, n, kap, x64, a.W64);
+          const float rf = (float)res;
+          r32[r] = rf;
+          rr64 += res * res;
+          rzn += (double)rf * (double)(dv[r] * rf);
+        }
+        group_sum2<NT, CS>(rr64, rzn, sh, slot);
+        rmax2 = rr64;
+        if (rr64 <= tol2) {
+          converged = 1;
+          break;
+        }
+        if (iters >= a.maxit) break;
+      }
+      const float beta = (float)(rzn / rz);
+      rz = rzn;
+      for (int base = r0 + tid; base < r1; base += kU * NT) {
+        float pv[kU], dd[kU], rv[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int r = base + u * NT;
+          if (r < r1) {
+            pv[u] = p32[r];
+            dd[u] = dv[r];
+            rv[u] = r32[r];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int r = base + u * NT;
+          if (r < r1) p32[r] = fmaf(beta, pv[u], dd[u] * rv[u]);
+        }
+      }
+      group_sync<CS>();
+    }
+  } else {
+    converged = 1;
+  }
+  if (tid == 0 && rank == 0) {
+    a.iters[pi] = iters;
+    a.conv[pi] = converged;
+  }
+  // the next problem's set-up rewrites this group's scratch, which peers may still read
+  group_sync<CS>();
+}
+
+// The solve of every problem in one launch. Phase 1: each cluster of CS CTAs takes the large
+// problems (order[0 .. nlarge)) from the first work counter and solves them together. Phase
+// 2 (once that counter is exhausted for the cluster): every CTA takes the small problems
+// from the second counter and solves each alone, with CTA barriers only. A cluster leaves
+// phase 1 together (the task is broadcast) and its CTAs touch no peer's shared memory after
+// that, so none waits on another CTA in phase 2.
+template <int NT, int CS>
+__global__ void __launch_bounds__(NT, (1024 / NT > 0 ? 1024 / NT : 1))
+    k_b_solve(const __grid_constant__ PArgs a) {
+  __shared__ BShared<NT> sh;
+  const int tid = threadIdx.x;
+  const uint32_t rank = CS > 1 ? cluster_rank() : 0u;
+  const int64_t stride = a.cell_stride + 5 * a.row_stride;
   int slot = 0;
+  float* gbase = a.scratch + ((int64_t)blockIdx.x - rank) * stride;
   for (;;) {
     if (tid == 0 && rank == 0) sh.task = atomicAdd(a.counter, 1);
     group_sync<CS>();
@@ -319,167 +494,19 @@ __global__ void __launch_bounds__(NT, (1024 / NT > 0 ? 1024 / NT : 1)) k_b_solve
       task = sh.task;
       __syncthreads();
     }
-    if (task >= a.nproblems) break;
-    const int pi = a.order[task];
-    const BProb P = a.probs[pi];
-    const int n = P.n, m = n - 1;
-    const int c1 = (n + 3) & ~3;
-    const int R = m * m * m;  // < 2^31 (n <= 1024)
-    const double* kap = a.coef + P.cell0;
-    double* x64 = a.x + P.xoff;
-    const int r0 = (int)((int64_t)R * rank / CS), r1 = (int)((int64_t)R * (rank + 1) / CS);
-    const int tx = (m + 31) / 32, ty = (m + NT / 32 - 1) / (NT / 32), tz = (m + kBZ - 1) / kBZ;
-    const int ntile = tx * ty * tz;
-    int iters = 0, converged = 0;
-    if (R > 0) {
-      // set-up: FP32 kappa (this CTA's cell layers), Jacobi diagonal, x = 0, r = b = f,
-      // p = D^-1 r
-      const int64_t nlay = (int64_t)n * n;
-      for (int64_t c = (int64_t)rank * nlay * n / CS + tid;
-           c < ((int64_t)rank + 1) * nlay * n / CS; c += NT) {
-        const int64_t ck = c / nlay, rest = c - ck * nlay, cj = rest / n, ci = rest - cj * n;
-        kap32[ci + (int64_t)c1 * (cj + (int64_t)n * ck)] = (float)kap[c];
-      }
-      double rz = 0.0, bb = 0.0;
-      const float fb = (float)a.f;
-      for (int r = r0 + tid; r < r1; r += NT) {
-        int i, j, k;
-        row_ijk3(r, m, i, j, k);
-        float ks = 0.f;
-#pragma unroll
-        for (int e = 0; e < 8; ++e)
-          ks += (float)kap[(i + (e & 1)) + (int64_t)n * ((j + ((e >> 1) & 1)) +
-                                                          (int64_t)n * (k + (e >> 2)))];
-        const float d = 1.f / (W[0] * ks);
-        dv[r] = d;
-        x64[r] = 0.0;
-        x32[r] = 0.f;
-        r32[r] = fb;
-        p32[r] = d * fb;
-        rz += (double)fb * (double)(d * fb);
-        bb += a.f * a.f;
-      }
-      group_sum2<NT, CS>(rz, bb, sh, slot);  // also publishes kap32 and p32 to the cluster
-      const double tol2 = a.rtol2 * bb;
-      double rmax2 = bb;
-      bool done = !(bb > 0.0);
-      converged = done;
-      while (!done) {
-        // q = A p over this CTA's tiles; p.q
-        double pq = 0.0, unused = 0.0;
-        for (int t = (int)rank; t < ntile; t += CS) {
-          const int bx = t % tx, by = (t / tx) % ty, bz = t / (tx * ty);
-          pq += (double)march_tile<NT>(n, c1, bx, by, bz * kBZ, kap32, p32, q32, W);
-        }
-        group_sum2<NT, CS>(pq, unused, sh, slot);
-        const float alpha = (float)(rz / pq);
-        // x += alpha p, r -= alpha q over this CTA's rows; r.z and r.r
-        double rzn = 0.0, rr = 0.0;
-        for (int base = r0 + tid; base < r1; base += kU * NT) {
-          // kU rows a thread: all loads issued before the first use
-          float xv[kU], pv[kU], qv[kU], rv[kU], dd[kU];
-#pragma unroll
-          for (int u = 0; u < kU; ++u) {
-            const int r = base + u * NT;
-            if (r < r1) {
-              xv[u] = x32[r];
-              pv[u] = p32[r];
-              qv[u] = q32[r];
-              rv[u] = r32[r];
-              dd[u] = dv[r];
-            }
-          }
-#pragma unroll
-          for (int u = 0; u < kU; ++u) {
-            const int r = base + u * NT;
-            if (r < r1) {
-              x32[r] = fmaf(alpha, pv[u], xv[u]);
-              const float ri = fmaf(-alpha, qv[u], rv[u]);
-              r32[r] = ri;
-              rzn += (double)ri * (double)(dd[u] * ri);
-              rr += (double)ri * ri;
-            }
-          }
-        }
-        group_sum2<NT, CS>(rzn, rr, sh, slot);
-        ++iters;
-        if (!isfinite(rr) || !isfinite(rzn) || !isfinite(pq)) {
-          if (tid == 0 && rank == 0 && atomicCAS(&a.err->code, 0, GFE_ERR_NONFINITE) == 0)
-            a.err->index = pi;
-          break;
-        }
-        if (rr <= (double)kDelta * kDelta * rmax2 || rr <= tol2 || iters >= a.maxit) {
-          // reliable update: x64 += x32, then r = b - A x64 in FP64 from the FP64 kappa
-          for (int base = r0 + tid; base < r1; base += kU * NT) {
-            double xv[kU];
-            float xs[kU];
-#pragma unroll
-            for (int u = 0; u < kU; ++u) {
-              const int r = base + u * NT;
-              if (r < r1) {
-                xv[u] = x64[r];
-                xs[u] = x32[r];
-              }
-            }
-#pragma unroll
-            for (int u = 0; u < kU; ++u) {
-              const int r = base + u * NT;
-              if (r < r1) {
-                x64[r] = xv[u] + (double)xs[u];
-                x32[r] = 0.f;
-              }
-            }
-          }
-          group_sync<CS>();
-          double rr64 = 0.0;
-          rzn = 0.0;
-          for (int r = r0 + tid; r < r1; r += NT) {
-            int i, j, k;
-            row_ijk3(r, m, i, j, k);
-            const double res = a.f - class_apply<double>(i, j, k, m, n, kap, x64, a.W64);
-            const float rf = (float)res;
-            r32[r] = rf;
-            rr64 += res * res;
-            rzn += (double)rf * (double)(dv[r] * rf);
-          }
-          group_sum2<NT, CS>(rr64, rzn, sh, slot);
-          rmax2 = rr64;
-          if (rr64 <= tol2) {
-            converged = 1;
-            break;
-          }
-          if (iters >= a.maxit) break;
-        }
-        const float beta = (float)(rzn / rz);
-        rz = rzn;
-        for (int base = r0 + tid; base < r1; base += kU * NT) {
-          float pv[kU], dd[kU], rv[kU];
-#pragma unroll
-          for (int u = 0; u < kU; ++u) {
-            const int r = base + u * NT;
-            if (r < r1) {
-              pv[u] = p32[r];
-              dd[u] = dv[r];
-              rv[u] = r32[r];
-            }
-          }
-#pragma unroll
-          for (int u = 0; u < kU; ++u) {
-            const int r = base + u * NT;
-            if (r < r1) p32[r] = fmaf(beta, pv[u], dd[u] * rv[u]);
-          }
-        }
-        group_sync<CS>();
-      }
-    } else {
-      converged = 1;
+    if (task >= a.nlarge) break;
+    solve_one<NT, CS>(a, sh, slot, rank, gbase, a.order[task]);
+  }
+  if constexpr (CS > 1) {
+    float* cbase = a.scratch + (int64_t)blockIdx.x * stride;
+    for (;;) {
+      if (tid == 0) sh.task = atomicAdd(a.counter2, 1);
+      __syncthreads();
+      const int task = a.nlarge + sh.task;
+      __syncthreads();
+      if (task >= a.nproblems) break;
+      solve_one<NT, 1>(a, sh, slot, 0u, cbase, a.order[task]);
     }
-    if (tid == 0 && rank == 0) {
-      a.iters[pi] = iters;
-      a.conv[pi] = converged;
-    }
-    // the next problem's set-up rewrites this group's scratch, which peers may still read
-    group_sync<CS>();
   }
 }
 
@@ -492,16 +519,28 @@ struct gfe_batch {
   int64_t ncells = 0, nfree_total = 0;
   int64_t cell_stride = 0, row_stride = 0;  // per-block scratch: largest problem, rounded to 32
   std::vector<int64_t> nfree;               // per problem
+  std::vector<int64_t> nfree_sorted;        // the same, largest first
+  int64_t rmax = 0;                         // the largest problem's rows
   gfe::DevBuf coef, probs, order, counter, status, xbuf, scratch;
   int nt = 0, cs = 0;                       // tuned threads per CTA and CTAs per problem
+  float large = 0.f;                        // and the cluster threshold (relative rows)
   double W64[8] = {0};
   float W32[8] = {0};
 };
 
 namespace gfe {
 
-// the launch shapes the autotuner times: (threads per CTA, CTAs per problem = cluster size)
-static const int kShapes[][2] = {{256, 1}, {1024, 1}, {1024, 2}, {512, 4}, {1024, 4}, {1024, 8}};
+// the schedules the autotuner times: threads per CTA, CTAs per problem (cluster size) and the
+// row count, relative to the largest problem's, from which a problem goes to a cluster (the
+// smaller ones go to single CTAs once the clusters have run out of large problems; 0: every
+// problem to a cluster)
+struct Schedule {
+  int nt, cs;
+  float large;
+};
+static const Schedule kShapes[] = {{256, 1, 0.f},  {1024, 1, 0.f},  {1024, 2, 0.f},
+                                   {512, 4, 0.f},  {512, 4, 0.3f},  {1024, 4, 0.3f},
+                                   {1024, 8, 0.f}, {1024, 8, 0.3f}};
 constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
 constexpr size_t kScratchCap = (size_t)8 << 30;  // scratch bytes the launch may hold at most
 
@@ -541,43 +580,56 @@ static int launch_shape(gfe_ctx* ctx, const batch::PArgs& a, int64_t groups, boo
 
 static int dispatch_shape(gfe_ctx* ctx, int s, const batch::PArgs& a, int64_t groups,
                           bool query, int64_t* max_groups) {
-  switch (s) {
-    case 0: return launch_shape<256, 1>(ctx, a, groups, query, max_groups);
-    case 1: return launch_shape<1024, 1>(ctx, a, groups, query, max_groups);
-    case 2: return launch_shape<1024, 2>(ctx, a, groups, query, max_groups);
-    case 3: return launch_shape<512, 4>(ctx, a, groups, query, max_groups);
-    case 4: return launch_shape<1024, 4>(ctx, a, groups, query, max_groups);
-    default: return launch_shape<1024, 8>(ctx, a, groups, query, max_groups);
-  }
+  const int nt = kShapes[s].nt, cs = kShapes[s].cs;
+  if (nt == 256 && cs == 1) return launch_shape<256, 1>(ctx, a, groups, query, max_groups);
+  if (nt == 1024 && cs == 1) return launch_shape<1024, 1>(ctx, a, groups, query, max_groups);
+  if (nt == 1024 && cs == 2) return launch_shape<1024, 2>(ctx, a, groups, query, max_groups);
+  if (nt == 512 && cs == 4) return launch_shape<512, 4>(ctx, a, groups, query, max_groups);
+  if (nt == 1024 && cs == 4) return launch_shape<1024, 4>(ctx, a, groups, query, max_groups);
+  return launch_shape<1024, 8>(ctx, a, groups, query, max_groups);
 }
 
-// problem groups (CTAs, or clusters) of one launch of shape s: as many as can be resident,
-// at most one per problem and within the scratch cap; 0 if the shape cannot run here
+// problem groups (CTAs, or clusters) of one launch of schedule s: as many as can be
+// resident, at most one per problem and within the scratch cap (scratch is per CTA); 0 if the
+// schedule cannot run here
 static int64_t batch_groups(gfe_ctx* ctx, const gfe_batch* B, int s) {
   int64_t res = 0;
   batch::PArgs dummy{};
   dispatch_shape(ctx, s, dummy, 0, true, &res);
   if (res < 1) return 0;
-  const int64_t blk_bytes = (int64_t)sizeof(float) * (B->cell_stride + 5 * B->row_stride);
+  const int64_t grp_bytes =
+      (int64_t)sizeof(float) * (B->cell_stride + 5 * B->row_stride) * kShapes[s].cs;
   const int64_t cap =
-      std::max<int64_t>(1, (int64_t)(kScratchCap / (size_t)std::max<int64_t>(blk_bytes, 1)));
+      std::max<int64_t>(1, (int64_t)(kScratchCap / (size_t)std::max<int64_t>(grp_bytes, 1)));
   return std::max<int64_t>(1, std::min<int64_t>({res, (int64_t)B->nproblems, cap}));
 }
 
-// One launch solving every problem with shape s into x (device, nfree_total entries).
+// problems that schedule s gives to clusters: a prefix of the largest-first order
+static int32_t batch_nlarge(const gfe_batch* B, int s) {
+  if (kShapes[s].cs == 1 || !(kShapes[s].large > 0.f)) return B->nproblems;
+  const double t = (double)kShapes[s].large * (double)B->rmax;
+  int32_t k = 0;
+  while (k < B->nproblems && (double)B->nfree_sorted[k] >= t) ++k;
+  return k;
+}
+
+// One launch solving every problem with schedule s into x (device, nfree_total entries).
 static int batch_launch(gfe_ctx* ctx, gfe_batch* B, int s, double source, double rtol,
                         int32_t maxit, double* x) {
   using namespace batch;
   const int64_t groups = batch_groups(ctx, B, s);
-  if (groups < 1) return set_error(GFE_ERR_UNSUPPORTED, "batch: launch shape %d cannot run", s);
-  GFE_TRY(B->scratch.reserve(sizeof(float) * (size_t)groups *
+  if (groups < 1)
+    return set_error(GFE_ERR_UNSUPPORTED, "batch: launch schedule %d cannot run", s);
+  GFE_TRY(B->scratch.reserve(sizeof(float) * (size_t)(groups * kShapes[s].cs) *
                              (size_t)(B->cell_stride + 5 * B->row_stride)));
-  GFE_CUDA_TRY(cudaMemsetAsync(B->counter.ptr, 0, sizeof(int), ctx->stream));
+  GFE_CUDA_TRY(cudaMemsetAsync(B->counter.ptr, 0, 2 * sizeof(int), ctx->stream));
   PArgs a;
   a.nproblems = B->nproblems;
   a.probs = B->probs.as<BProb>();
   a.order = B->order.as<int32_t>();
   a.counter = B->counter.as<int>();
+  a.counter2 = a.counter + 1;
+  a.nlarge = batch_nlarge(B, s);
   a.coef = B->coef.as<double>();
   a.f = source;
   a.rtol2 = rtol * rtol;
@@ -653,6 +705,8 @@ extern "C" int gfe_batch_create(gfe_ctx* ctx, int32_t nproblems, const int64_t* 
   B->ncells = cells;
   B->nfree_total = nf_total;
   B->nfree = nfree;
+  B->rmax = rmax;
+  for (int32_t p = 0; p < nproblems; ++p) B->nfree_sorted.push_back(nfree[order[p]]);
   B->cell_stride = (cmax + 31) / 32 * 32;
   B->row_stride = (rmax + 31) / 32 * 32;
   q1_unit_stiffness_classes(B->W64);
@@ -671,7 +725,7 @@ extern "C" int gfe_batch_create(gfe_ctx* ctx, int32_t nproblems, const int64_t* 
   up(B->coef, coef.data(), coef.size() * sizeof(double));
   up(B->probs, probs.data(), probs.size() * sizeof(batch::BProb));
   up(B->order, order.data(), order.size() * sizeof(int32_t));
-  if (st == GFE_OK) st = B->counter.reserve(sizeof(int));
+  if (st == GFE_OK) st = B->counter.reserve(2 * sizeof(int));
   if (st == GFE_OK) st = B->status.reserve(sizeof(int32_t) * 2 * (size_t)nproblems);
   if (st == GFE_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess)
     st = set_error(GFE_ERR_CUDA, "gfe_batch_create: sync failed");
@@ -698,35 +752,41 @@ extern "C" int gfe_batch_info(gfe_batch* B, int64_t* nrows, int64_t* nfree, int6
   return GFE_OK;
 }
 
-extern "C" int gfe_batch_shape(gfe_batch* B, int32_t* threads, int32_t* ctas_per_problem) {
+extern "C" int gfe_batch_shape(gfe_batch* B, int32_t* threads, int32_t* ctas_per_problem,
+                               double* cluster_threshold) {
   clear_error();
   if (!B) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_batch_shape: NULL");
   if (threads) *threads = B->nt;
   if (ctas_per_problem) *ctas_per_problem = B->cs;
+  if (cluster_threshold) *cluster_threshold = B->large;
   return GFE_OK;
 }
 
-// Fixes the launch shape (one of the autotuner's candidates) instead of tuning it; (0, 0)
-// re-enables the autotuner. Shapes sum in different orders, so fixing one makes results
+// Fixes the launch schedule (one of the autotuner's candidates) instead of tuning it; (0, 0)
+// re-enables the autotuner. Schedules sum in different orders, so fixing one makes results
 // reproducible across batches.
-extern "C" int gfe_batch_set_shape(gfe_batch* B, int32_t threads, int32_t ctas_per_problem) {
+extern "C" int gfe_batch_set_shape(gfe_batch* B, int32_t threads, int32_t ctas_per_problem,
+                                   double cluster_threshold) {
   clear_error();
   if (!B) return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_batch_set_shape: NULL");
   if (threads == 0 && ctas_per_problem == 0) {
     B->nt = B->cs = 0;
+    B->large = 0.f;
     return GFE_OK;
   }
   for (int s = 0; s < kNumShapes; ++s)
-    if (kShapes[s][0] == threads && kShapes[s][1] == ctas_per_problem) {
+    if (kShapes[s].nt == threads && kShapes[s].cs == ctas_per_problem &&
+        std::fabs((double)kShapes[s].large - cluster_threshold) < 1e-6) {
       if (batch_groups(B->ctx, B, s) < 1)
         return set_error(GFE_ERR_UNSUPPORTED, "gfe_batch_set_shape: (%d, %d) cannot run on "
                          "this device", (int)threads, (int)ctas_per_problem);
       B->nt = threads;
       B->cs = ctas_per_problem;
+      B->large = kShapes[s].large;
       return GFE_OK;
     }
-  return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_batch_set_shape: (%d, %d) is not a candidate "
-                   "shape", (int)threads, (int)ctas_per_problem);
+  return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_batch_set_shape: (%d, %d, %g) is not a "
+                   "candidate schedule", (int)threads, (int)ctas_per_problem, cluster_threshold);
 }
 
 // Assembles and solves every problem (one persistent launch; see the file comment). x (host
@@ -788,11 +848,14 @@ extern "C" int gfe_batch_assemble_solve(gfe_batch* B, double source, double rtol
     GFE_TRY(st);
     if (best < 0) return set_error(GFE_ERR_UNSUPPORTED, "gfe_batch_assemble_solve: no launch "
                                    "shape can run on this device");
-    B->nt = kShapes[best][0];
-    B->cs = kShapes[best][1];
+    B->nt = kShapes[best].nt;
+    B->cs = kShapes[best].cs;
+    B->large = kShapes[best].large;
   }
   int s = 0;
-  while (s < kNumShapes && !(kShapes[s][0] == B->nt && kShapes[s][1] == B->cs)) ++s;
+  while (s < kNumShapes && !(kShapes[s].nt == B->nt && kShapes[s].cs == B->cs &&
+                             kShapes[s].large == B->large))
+    ++s;
   GFE_TRY(batch_launch(ctx, B, s, source, rtol, maxit, xd));
   // results: per-problem iterations and convergence, x to the caller's host array
   int32_t* hs = (int32_t*)ctx->h_pinned;

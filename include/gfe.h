@@ -467,13 +467,15 @@ int gfe_matrix_mul(gfe_ctx* ctx, gfe_matrix* A, const double* x, double* y);
 /* Many independent scalar Q1 diffusion problems -div(kappa grad u) = f on unit cubes with
  * their own partitions (partitions[3*p..3*p+2], equal entries: cubic cells, n <= 1024), per-cell
  * kappa (concatenated in problem and Gridap cell order), homogeneous Dirichlet on the boundary,
- * assembled and solved together in ONE persistent kernel launch: CTAs, or thread-block
- * clusters of 2-8 CTAs, take problems from a work counter (largest first; nothing waits on
- * another group) and each runs a whole Jacobi-PCG on its problem with the operator applied
- * matrix-free in FP32 from the cell coefficients and FP64 reliable updates (the FP64 true
- * residual b - A x decides convergence: ||b - A x|| <= rtol ||b|| in FP64). The launch shape
- * (threads per CTA, CTAs per problem) is autotuned on the first solve of a batch, which runs
- * once with each of six candidates.
+ * assembled and solved together in ONE persistent kernel launch. Each problem runs a whole
+ * Jacobi-PCG with the operator applied matrix-free in FP32 from the cell coefficients and
+ * FP64 reliable updates (the FP64 true residual b - A x decides convergence:
+ * ||b - A x|| <= rtol ||b|| in FP64). Thread-block clusters of 2-8 CTAs take the large
+ * problems from a work counter, largest first, and solve each together; once those are
+ * gone every CTA takes the smaller problems from a second counter and solves each alone.
+ * Nothing waits on another group. The schedule (threads per CTA, CTAs per cluster, and the
+ * size, relative to the largest problem, from which a problem goes to a cluster) is
+ * autotuned on the first solve of a batch, which runs once with each of eight candidates.
  * Repeated calls give identical results.
  * No counterpart in Gridap (which solves one operator at a time). */
 typedef struct gfe_batch gfe_batch;
@@ -482,12 +484,17 @@ int gfe_batch_create(gfe_ctx* ctx, int32_t nproblems, const int64_t* partitions,
 int gfe_batch_destroy(gfe_batch* batch);
 /* nrows = nfree = sum over problems of (n - 1)^3; ncells = sum of n^3. */
 int gfe_batch_info(gfe_batch* batch, int64_t* nrows, int64_t* nfree, int64_t* ncells);
-/* The launch shape the autotuner chose (0, 0 before the first solve). */
-int gfe_batch_shape(gfe_batch* batch, int32_t* threads, int32_t* ctas_per_problem);
-/* Fixes the shape to one of the candidates (256,1) (1024,1) (1024,2) (512,4) (1024,4)
- * (1024,8) instead of autotuning; (0, 0) re-enables the autotuner. Shapes sum in different
- * orders: a fixed shape makes results reproducible across batches. */
-int gfe_batch_set_shape(gfe_batch* batch, int32_t threads, int32_t ctas_per_problem);
+/* The schedule the autotuner chose (0, 0, 0 before the first solve): threads per CTA, CTAs
+ * per cluster, and the cluster threshold (problems with at least that fraction of the largest
+ * problem's rows go to clusters; 0: all of them). */
+int gfe_batch_shape(gfe_batch* batch, int32_t* threads, int32_t* ctas_per_problem,
+                    double* cluster_threshold);
+/* Fixes the schedule to one of the candidates (256,1,0) (1024,1,0) (1024,2,0) (512,4,0)
+ * (512,4,0.3) (1024,4,0.3) (1024,8,0) (1024,8,0.3) instead of autotuning; (0, 0, 0)
+ * re-enables the autotuner. Schedules sum in different orders: a fixed one makes results
+ * reproducible across batches. */
+int gfe_batch_set_shape(gfe_batch* batch, int32_t threads, int32_t ctas_per_problem,
+                        double cluster_threshold);
 /* x (host, or device memory of the context's device) receives the problems' free-dof
  * solutions one after the other (sum of nfree entries); iterations[nproblems] (optional, host)
  * each problem's CG iterations; *nconverged how many reached rtol within maxiter (0 = 100000). */

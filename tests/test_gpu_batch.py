@@ -14,6 +14,10 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
+# the autotuner's candidate schedules: threads per CTA, CTAs per cluster, cluster threshold
+SCHEDULES = {(256, 1, 0.0), (1024, 1, 0.0), (1024, 2, 0.0), (512, 4, 0.0), (512, 4, 0.3),
+             (1024, 4, 0.3), (1024, 8, 0.0), (1024, 8, 0.3)}
+
 
 def _oracle_problem(orc, n, kappa, f):
     P = orc.poisson_q1((0.0, 1.0) * 3, (n, n, n), kappa=kappa, fkind=orc.F_CONST,
@@ -103,9 +107,9 @@ def test_batch_one_launch_autotuned_shape_device_output(gg):
     kappas = [np.exp(1.5 * rng.standard_normal(n ** 3)) for n in sizes]
     ctx = gg.default_context()
     B = gg.BatchedPoissonProblems(sizes, kappas, ctx)
-    assert B.shape() == (0, 0)
+    assert B.shape() == (0, 0, 0.0)
     xh = B.assemble_solve(source=1.0, rtol=1e-8)
-    assert B.shape() in {(256, 1), (1024, 1), (1024, 2), (512, 4), (1024, 4), (1024, 8)}
+    assert B.shape() in SCHEDULES
     xd = torch.empty(B.nfree, dtype=torch.float64, device="cuda")
     l0 = ctx.kernel_launches()
     B.assemble_solve(source=1.0, rtol=1e-8, x=xd)
@@ -135,14 +139,14 @@ def test_batch_zero_source_and_single_cell(gg):
 
 
 def test_batch_every_shape_agrees(gg):
-    """Each candidate launch shape (fixed by set_shape) converges every problem to rtol; the
+    """Each candidate schedule (fixed by set_shape) converges every problem to rtol; the
     solutions agree within the CG tolerance."""
     rng = np.random.default_rng(16)
     sizes = [int(n) for n in rng.integers(3, 26, 20)]
     kappas = [np.exp(1.5 * rng.standard_normal(n ** 3)) for n in sizes]
     B = gg.BatchedPoissonProblems(sizes, kappas)
     ref = None
-    for shape in [(256, 1), (1024, 1), (1024, 2), (512, 4), (1024, 4), (1024, 8)]:
+    for shape in sorted(SCHEDULES):
         try:
             B.set_shape(*shape)
         except gg._lib.GfeError:

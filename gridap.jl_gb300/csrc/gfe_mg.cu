@@ -11,8 +11,9 @@
 // weighting 1, 1/2, 1/4, 1/8). Smoothing is damped Jacobi (omega 0.8, two sweeps before and
 // after, the first from zero), each later sweep fused into one pass over the lattice stencil;
 // the coarsest level takes five sweeps. Levels of at most 512 rows run their part of the
-// cycle in one block. All vectors are FP32 in the lattice row order; every kernel returns at
-// once when the solver's done flag is set.
+// cycle in one block, out of shared memory. All vectors are FP32 in the lattice row order;
+// every kernel returns at once when the solver's done flag is set. The cycle is captured once
+// as a CUDA graph whose kernels are chained by programmatic dependent launch.
 #include <utility>
 #include <vector>
 
@@ -27,7 +28,32 @@ constexpr int kMgBlock = 256;
 constexpr float kOmega = 0.8f;
 constexpr int kPreSweeps = 2, kPostSweeps = 2, kCoarseSweeps = 4;
 
-__device__ __forceinline__ bool stop(const int* done) { return done && *done; }
+// Every kernel of the cycle is launched with programmatic stream serialisation (launch_pdl):
+// its blocks may become resident while the kernel before it on the stream still runs, and
+// wait in stop() -- before any memory access -- until that kernel has completed and its
+// writes are visible; each then lets the next kernel launch at once. Without that launch
+// attribute the wait returns immediately.
+__device__ __forceinline__ bool stop(const int* done) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  return done && *done;
+}
+
+template <class... P, class... A>
+cudaError_t launch_pdl(void (*kern)(P...), dim3 grid, int block, size_t smem, cudaStream_t st,
+                       A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
 
 // One damped Jacobi sweep fused into the lattice apply: xo = x + omega D^-1 (b - A x)
 // (xo != x: the sweep reads the old neighbours). Same arithmetic as an apply into t followed
@@ -201,97 +227,121 @@ __global__ void k_mg_diag(LatticeQ1Op op, float* __restrict__ dinv) {
 
 // ---- the coarse levels in one block ------------------------------------------------------
 // Levels of at most kCoarseRows rows run their whole V-cycle inside one block of kCoarseBlock
-// threads (block-stride loops, a barrier between steps): on such lattices a launch costs
-// more than its work. The row operator below follows lattice_rows' loop order exactly. (With
-// 15^3-row levels inside, the one block's issue rate made the cycle slower than launches.)
-constexpr int kCoarseBlock = 512;
+// threads: on such lattices a launch costs more than its work. The block copies kappa and
+// D^-1 of these levels and b of the first one into shared memory, runs every step there
+// (block-stride loops, a barrier between steps; x, b and t of every level live in shared
+// memory only) and writes x of the first level back.
 constexpr int64_t kCoarseRows = 512;
+constexpr int kCoarseBlock = kCoarseRows > 512 ? 1024 : 512;
 constexpr int kMaxCoarse = 6;
 
-struct MgLevelView {
-  LatticeQ1Op op;
-  int m0, m1, m2;
-  int64_t n;
-  float *x, *b, *t, *dinv;
+// one level of the block: float offsets of its vectors and kappa in the shared buffer
+struct MgCoarseLevel {
+  int m0, m1, m2, n;        // interior nodes per direction, rows
+  int c1, c2, ncell;        // kappa strides (as in LatticeQ1Op), kappa entries c2 * n2
+  int x, b, t, dinv, kap;   // offsets into the shared buffer
+  float W[8];               // class weights Kref[0][c]
+  const float* gkap;        // kappa and D^-1 in global memory
+  const float* gdinv;
 };
 
 struct CoarseLevels {
   int nl;
-  MgLevelView L[kMaxCoarse];
+  int floats;       // shared buffer size
+  const float* b0;  // b of the first level
+  float* x0;        // its result
+  MgCoarseLevel L[kMaxCoarse];
 };
 
-// (A p)_r at interior node (i, j, k): its 27 neighbours loaded once (0 outside the interior),
-// then the 8 cells around it, 8 local columns each, in lattice_rows' order (32-bit indexing:
-// these levels are small). `load(row)` gives p at a row.
-template <class Load>
-__device__ __forceinline__ float lattice_row_value_f(const LatticeQ1Op& op, int i, int j, int k,
-                                                     const Load& load) {
-  const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
-  float v[27];
+// (A p)_r at interior node (i, j, k) of a level held in shared memory: the class-sum form of
+// the lattice rows, (A p)_r = sum_c W[c] sum_{d in class c} S(d) p_{r+d}, S(d) the kappa sum
+// over the cells r and r + d share; one x-plane of 9 neighbours at a time (0 outside the
+// interior).
+__device__ __forceinline__ float coarse_row(const MgCoarseLevel& L, const float* sm, int i,
+                                            int j, int k, const float* p) {
+  const float* kp = sm + L.kap + i + L.c1 * j + L.c2 * k;
+  // box sums of one cell layer, indexed e = (dx + 1) + 3 (dy + 1)
+  auto layer = [&](const float* q, float* Lb) {
+    const float v0 = q[0], v1 = q[1], v2 = q[L.c1], v3 = q[L.c1 + 1];
+    const float X0 = v0 + v1, X1 = v2 + v3;
+    Lb[0] = v0;
+    Lb[1] = X0;
+    Lb[2] = v1;
+    Lb[3] = v0 + v2;
+    Lb[4] = X0 + X1;
+    Lb[5] = v1 + v3;
+    Lb[6] = v2;
+    Lb[7] = X1;
+    Lb[8] = v3;
+  };
+  float la[9], lb[9];
+  layer(kp, la);
+  layer(kp + L.c2, lb);
+  float T[8];
 #pragma unroll
-  for (int dz = 0; dz < 3; ++dz)
+  for (int c = 0; c < 8; ++c) T[c] = 0.f;
 #pragma unroll
-    for (int dy = 0; dy < 3; ++dy)
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int kk = k + dz;
+    const bool okz = kk >= 0 && kk < L.m2;
 #pragma unroll
-      for (int dx = 0; dx < 3; ++dx) {
-        const int ii = i - 1 + dx, jj = j - 1 + dy, kk = k - 1 + dz;
-        const bool in = ii >= 0 && ii < m0 && jj >= 0 && jj < m1 && kk >= 0 && kk < m2;
-        v[dx + 3 * dy + 9 * dz] = in ? load(ii + op.s1 * jj + op.s2 * kk) : 0.f;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int jj = j + dy;
+      const bool oky = okz && jj >= 0 && jj < L.m1;
+#pragma unroll
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int ii = i + dx;
+        const int e = (dx + 1) + 3 * (dy + 1);
+        const int cl = (dx ? 1 : 0) | (dy ? 2 : 0) | (dz ? 4 : 0);
+        const float xv = oky && ii >= 0 && ii < L.m0 ? p[ii + L.m0 * (jj + L.m1 * kk)] : 0.f;
+        const float S = dz < 0 ? la[e] : (dz > 0 ? lb[e] : la[e] + lb[e]);
+        T[cl] = fmaf(S, xv, T[cl]);
       }
+    }
+  }
   float acc = 0.f;
 #pragma unroll
-  for (int cz = 0; cz < 2; ++cz)
-#pragma unroll
-    for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-      for (int cx = 0; cx < 2; ++cx) {
-        const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
-        float s = 0.f;
-#pragma unroll
-        for (int lc = 0; lc < 8; ++lc)
-          s = fmaf(op.K[lr + 8 * lc],
-                   v[(cx + (lc & 1)) + 3 * (cy + ((lc >> 1) & 1)) + 9 * (cz + (lc >> 2))], s);
-        acc = fmaf(op.kap[(i + cx) + op.c1 * (j + cy) + op.c2 * (k + cz)], s, acc);
-      }
+  for (int c = 0; c < 8; ++c) acc = fmaf(L.W[c], T[c], acc);
   return acc;
 }
 
-__device__ __forceinline__ float lattice_row_value(const LatticeQ1Op& op, int i, int j, int k,
-                                                   const float* __restrict__ p) {
-  return lattice_row_value_f(op, i, j, k, [p](int row) { return p[row]; });
-}
-
-__device__ __forceinline__ void row_ijk(const MgLevelView& L, int64_t r, int& i, int& j,
-                                        int& k) {
+__device__ __forceinline__ void coarse_ijk(const MgCoarseLevel& L, int r, int& i, int& j,
+                                           int& k) {
   const uint32_t ru = (uint32_t)r, rest = ru / (uint32_t)L.m0;
   i = (int)(ru - rest * (uint32_t)L.m0);
   k = (int)(rest / (uint32_t)L.m1);
   j = (int)(rest - (uint32_t)k * (uint32_t)L.m1);
 }
 
-// the V-cycle of levels 0 .. nl-1 of `c` (level 0's b is given, its result lands in its x);
+// the V-cycle of levels 0 .. nl-1 of `c` (b of level 0 given, its result written to x0); the
 // same steps, sweep counts and buffer roles as the multi-launch cycle
 __global__ void __launch_bounds__(kCoarseBlock)
     k_mg_coarse(const __grid_constant__ CoarseLevels c, const int* done) {
   if (stop(done)) return;
+  extern __shared__ float sm[];
   const int t0 = threadIdx.x;
-  auto sweep = [&](const MgLevelView& L, const float* xi, float* xo) {
-    for (int64_t r = t0; r < L.n; r += kCoarseBlock) {
+  for (int l = 0; l < c.nl; ++l) {
+    const MgCoarseLevel& L = c.L[l];
+    for (int e = t0; e < L.ncell; e += kCoarseBlock) sm[L.kap + e] = L.gkap[e];
+    for (int r = t0; r < L.n; r += kCoarseBlock) sm[L.dinv + r] = L.gdinv[r];
+  }
+  for (int r = t0; r < c.L[0].n; r += kCoarseBlock) sm[c.L[0].b + r] = c.b0[r];
+  __syncthreads();
+  auto sweep = [&](const MgCoarseLevel& L, int xi, int xo) {
+    for (int r = t0; r < L.n; r += kCoarseBlock) {
       int i, j, k;
-      row_ijk(L, r, i, j, k);
-      const float acc = lattice_row_value(L.op, i, j, k, xi);
-      xo[r] = fmaf(kOmega * L.dinv[r], L.b[r] - acc, xi[r]);
+      coarse_ijk(L, r, i, j, k);
+      const float acc = coarse_row(L, sm, i, j, k, sm + xi);
+      sm[xo + r] = fmaf(kOmega * sm[L.dinv + r], sm[L.b + r] - acc, sm[xi + r]);
     }
-    __syncthreads();
-  };
-  auto first = [&](const MgLevelView& L) {
-    for (int64_t r = t0; r < L.n; r += kCoarseBlock) L.x[r] = kOmega * L.dinv[r] * L.b[r];
     __syncthreads();
   };
   // down
   for (int l = 0; l < c.nl; ++l) {
-    const MgLevelView& L = c.L[l];
-    first(L);
+    const MgCoarseLevel& L = c.L[l];
+    for (int r = t0; r < L.n; r += kCoarseBlock)  // the sweep from zero
+      sm[L.x + r] = kOmega * sm[L.dinv + r] * sm[L.b + r];
+    __syncthreads();
     if (l + 1 == c.nl) {  // coarsest: four more sweeps, ending in x
       for (int s = 0; s < kCoarseSweeps; s += 2) {
         sweep(L, L.x, L.t);
@@ -300,16 +350,16 @@ __global__ void __launch_bounds__(kCoarseBlock)
       break;
     }
     sweep(L, L.x, L.t);
-    for (int64_t r = t0; r < L.n; r += kCoarseBlock) {  // residual into x
+    for (int r = t0; r < L.n; r += kCoarseBlock) {  // residual into x
       int i, j, k;
-      row_ijk(L, r, i, j, k);
-      L.x[r] = L.b[r] - lattice_row_value(L.op, i, j, k, L.t);
+      coarse_ijk(L, r, i, j, k);
+      sm[L.x + r] = sm[L.b + r] - coarse_row(L, sm, i, j, k, sm + L.t);
     }
     __syncthreads();
-    const MgLevelView& C = c.L[l + 1];
-    for (int64_t q = t0; q < C.n; q += kCoarseBlock) {  // restriction
+    const MgCoarseLevel& C = c.L[l + 1];
+    for (int q = t0; q < C.n; q += kCoarseBlock) {  // restriction
       int I, J, K;
-      row_ijk(C, q, I, J, K);
+      coarse_ijk(C, q, I, J, K);
       float s = 0.f;
 #pragma unroll
       for (int dz = -1; dz <= 1; ++dz)
@@ -318,28 +368,27 @@ __global__ void __launch_bounds__(kCoarseBlock)
 #pragma unroll
           for (int dx = -1; dx <= 1; ++dx) {
             const float w = (dx ? 0.5f : 1.f) * (dy ? 0.5f : 1.f) * (dz ? 0.5f : 1.f);
-            const int64_t f =
-                (int64_t)(2 * I + 1 + dx) +
-                (int64_t)L.m0 * ((2 * J + 1 + dy) + (int64_t)L.m1 * (2 * K + 1 + dz));
-            s = fmaf(w, L.x[f], s);
+            const int f = (2 * I + 1 + dx) + L.m0 * ((2 * J + 1 + dy) + L.m1 * (2 * K + 1 + dz));
+            s = fmaf(w, sm[L.x + f], s);
           }
-      C.b[q] = s;
+      sm[C.b + q] = s;
     }
     __syncthreads();
   }
   // up: x = t + P x_c, then two sweeps back into x
   for (int l = c.nl - 2; l >= 0; --l) {
-    const MgLevelView& L = c.L[l];
-    const MgLevelView& C = c.L[l + 1];
-    for (int64_t r = t0; r < L.n; r += kCoarseBlock) {
+    const MgCoarseLevel& L = c.L[l];
+    const MgCoarseLevel& C = c.L[l + 1];
+    for (int r = t0; r < L.n; r += kCoarseBlock) {
       int i, j, k;
-      row_ijk(L, r, i, j, k);
-      L.x[r] = L.t[r] + prolong_value(i, j, k, C.m0, C.m1, C.m2, C.x);
+      coarse_ijk(L, r, i, j, k);
+      sm[L.x + r] = sm[L.t + r] + prolong_value(i, j, k, C.m0, C.m1, C.m2, sm + C.x);
     }
     __syncthreads();
     sweep(L, L.x, L.t);
     sweep(L, L.t, L.x);
   }
+  for (int r = t0; r < c.L[0].n; r += kCoarseBlock) c.x0[r] = sm[c.L[0].x + r];
 }
 
 }  // namespace
@@ -374,6 +423,42 @@ unsigned vgrid(gfe_ctx* ctx, int64_t n) {
       1, std::min<int64_t>((n + kMgBlock - 1) / kMgBlock, (int64_t)ctx->num_sms * 8));
 }
 
+// whether level l and all coarser ones run in one block
+bool coarse_from(const LatticeMG* mg, size_t l) {
+  return mg->lv[l].n <= kCoarseRows && mg->lv.size() - l <= (size_t)kMaxCoarse;
+}
+
+// the block's view of levels l .. end: shared-memory offsets, weights and global sources
+CoarseLevels coarse_levels(const LatticeMG* mg, size_t l) {
+  CoarseLevels c{};
+  c.nl = (int)(mg->lv.size() - l);
+  int off = 0;
+  for (int q = 0; q < c.nl; ++q) {
+    const LatticeMG::Level& Q = mg->lv[l + q];
+    MgCoarseLevel& S = c.L[q];
+    S.m0 = Q.m0;
+    S.m1 = Q.m1;
+    S.m2 = Q.m2;
+    S.n = (int)Q.n;
+    S.c1 = Q.op.c1;
+    S.c2 = Q.op.c2;
+    S.ncell = Q.op.c2 * Q.op.n2;
+    S.x = off;
+    S.b = off + S.n;
+    S.t = off + 2 * S.n;
+    S.dinv = off + 3 * S.n;
+    S.kap = off + 4 * S.n;
+    off += 4 * S.n + S.ncell;
+    for (int e = 0; e < 8; ++e) S.W[e] = Q.op.K[8 * e];
+    S.gkap = Q.op.kap;
+    S.gdinv = Q.dinv;
+  }
+  c.floats = off;
+  c.b0 = mg->lv[l].b;
+  c.x0 = mg->lv[l].x;
+  return c;
+}
+
 // The V-cycle of level l: b in L.b, the result in L.x. Sweeps alternate between L.x and L.t
 // (a fused sweep cannot run in place); the sweep counts keep the result in L.x: the first
 // sweep from zero writes L.x, one more pre-sweep moves it to L.t, the residual goes to L.x,
@@ -381,20 +466,16 @@ unsigned vgrid(gfe_ctx* ctx, int64_t n) {
 // level takes the first sweep and four more.
 int vcycle(LatticeMG* mg, size_t l, const int* done) {
   gfe_ctx* ctx = mg->ctx;
+  cudaStream_t st = ctx->stream;
   LatticeMG::Level& L = mg->lv[l];
   const unsigned g = vgrid(ctx, L.n);
   const dim3 ga = L.op.grid(L.n);
   const bool coarsest = l + 1 == mg->lv.size();
   const int pre = coarsest ? kCoarseSweeps + 1 : kPreSweeps;
-  if (L.n <= kCoarseRows && mg->lv.size() - l <= (size_t)kMaxCoarse) {
-    // this level and all coarser ones in one block
-    CoarseLevels c{};
-    c.nl = (int)(mg->lv.size() - l);
-    for (int q = 0; q < c.nl; ++q) {
-      const LatticeMG::Level& Q = mg->lv[l + q];
-      c.L[q] = MgLevelView{Q.op, Q.m0, Q.m1, Q.m2, Q.n, Q.x, Q.b, Q.t, Q.dinv};
-    }
-    k_mg_coarse<<<1, kCoarseBlock, 0, ctx->stream>>>(c, done);
+  if (coarse_from(mg, l)) {  // this level and all coarser ones in one block
+    const CoarseLevels c = coarse_levels(mg, l);
+    GFE_CUDA_TRY(launch_pdl(k_mg_coarse, dim3(1), kCoarseBlock, sizeof(float) * c.floats, st,
+                            c, done));
     ctx->launches++;
     return GFE_OK;
   }
@@ -403,70 +484,80 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
   // lattices too small for 4 blocks per SM march one k-plane per thread
   const bool deep = (int64_t)ga.x * ga.y * ga.z >= 4 * (int64_t)ctx->num_sms;
   const dim3 ga1 = L.op.grid_k(1);
-  auto smooth = [&](const float* xi, float* xo) {
+  auto smooth = [&](const float* xi, float* xo) -> int {
     if (deep)
-      k_mg_smooth<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, xi, L.b, L.dinv, xo, done);
+      GFE_CUDA_TRY(launch_pdl(k_mg_smooth<kLatK>, ga, kMgBlock, 0, st, L.op, xi, L.b, L.dinv,
+                              xo, done));
     else
-      k_mg_smooth<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, xi, L.b, L.dinv, xo, done);
+      GFE_CUDA_TRY(launch_pdl(k_mg_smooth<1>, ga1, kMgBlock, 0, st, L.op, xi, L.b, L.dinv,
+                              xo, done));
     ctx->launches++;
+    return GFE_OK;
+  };
+  auto residual = [&](const float* x, float* r) -> int {
+    if (deep)
+      GFE_CUDA_TRY(launch_pdl(k_mg_residual<kLatK>, ga, kMgBlock, 0, st, L.op, x, L.b, r,
+                              done));
+    else
+      GFE_CUDA_TRY(launch_pdl(k_mg_residual<1>, ga1, kMgBlock, 0, st, L.op, x, L.b, r, done));
+    ctx->launches++;
+    return GFE_OK;
+  };
+  auto restrict_to = [&](const LatticeMG::Level& C, const float* r) -> int {
+    GFE_CUDA_TRY(launch_pdl(k_mg_restrict, dim3(vgrid(ctx, C.n)), kMgBlock, 0, st, L.m0, L.m1,
+                            C.m0, C.m1, C.m2, r, C.b, done));
+    ctx->launches++;
+    return GFE_OK;
+  };
+  auto prolong = [&](const LatticeMG::Level& C, const float* xf, float* xo) -> int {
+    GFE_CUDA_TRY(launch_pdl(k_mg_prolong, dim3(g), kMgBlock, 0, st, L.m0, L.m1, L.m2, C.m0,
+                            C.m1, C.m2, (const float*)C.x, xf, xo, done));
+    ctx->launches++;
+    return GFE_OK;
   };
   if (l == 0 && mg->learned && !coarsest) {
     // learned smoothing on the fine level: x = M(b); r = b - A x to the coarse level;
     // t = x + P x_c; x = t + M(b - A t)
     LatticeMG::Level& C = mg->lv[l + 1];
     GFE_TRY(learned_apply_into(ctx, mg->learned, L.b, nullptr, L.x, done, false));
-    if (deep)
-      k_mg_residual<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.b, L.t, done);
-    else
-      k_mg_residual<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, L.x, L.b, L.t, done);
-    k_mg_restrict<<<vgrid(ctx, C.n), kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, C.m0, C.m1, C.m2,
-                                                                 L.t, C.b, done);
-    ctx->launches += 2;
+    GFE_TRY(residual(L.x, L.t));
+    GFE_TRY(restrict_to(C, L.t));
     GFE_TRY(vcycle(mg, l + 1, done));
-    k_mg_prolong<<<g, kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, L.m2, C.m0, C.m1, C.m2, C.x, L.x,
-                                                  L.t, done);
-    if (deep)
-      k_mg_residual<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.t, L.b, L.x, done);
-    else
-      k_mg_residual<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, L.t, L.b, L.x, done);
-    ctx->launches += 2;
+    GFE_TRY(prolong(C, L.x, L.t));
+    GFE_TRY(residual(L.t, L.x));
     return learned_apply_into(ctx, mg->learned, L.x, L.t, L.x, done, false);
   }
   if (pre >= 2) {  // the sweep from zero and the next one in one pass
     if (deep)
-      k_mg_pre<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, L.b, L.dinv, oth, done);
+      GFE_CUDA_TRY(launch_pdl(k_mg_pre<kLatK>, ga, kMgBlock, 0, st, L.op, (const float*)L.b,
+                              (const float*)L.dinv, oth, done));
     else
-      k_mg_pre<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, L.b, L.dinv, oth, done);
+      GFE_CUDA_TRY(launch_pdl(k_mg_pre<1>, ga1, kMgBlock, 0, st, L.op, (const float*)L.b,
+                              (const float*)L.dinv, oth, done));
     std::swap(cur, oth);
   } else {
-    k_mg_jacobi0<<<g, kMgBlock, 0, ctx->stream>>>(L.n, L.b, L.dinv, cur, done);
+    GFE_CUDA_TRY(launch_pdl(k_mg_jacobi0, dim3(g), kMgBlock, 0, st, L.n, (const float*)L.b,
+                            (const float*)L.dinv, cur, done));
   }
   ctx->launches++;
   for (int s = 2; s < pre; ++s) {
-    smooth(cur, oth);
+    GFE_TRY(smooth(cur, oth));
     std::swap(cur, oth);
   }
   if (coarsest) return cur == L.x ? GFE_OK
                                   : set_error(GFE_ERR_UNSUPPORTED, "multigrid: sweep parity");
   LatticeMG::Level& C = mg->lv[l + 1];
-  if (deep)
-    k_mg_residual<kLatK><<<ga, kMgBlock, 0, ctx->stream>>>(L.op, cur, L.b, oth, done);
-  else
-    k_mg_residual<1><<<ga1, kMgBlock, 0, ctx->stream>>>(L.op, cur, L.b, oth, done);
-  k_mg_restrict<<<vgrid(ctx, C.n), kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, C.m0, C.m1, C.m2,
-                                                               oth, C.b, done);
-  ctx->launches += 2;
+  GFE_TRY(residual(cur, oth));
+  GFE_TRY(restrict_to(C, oth));
   GFE_TRY(vcycle(mg, l + 1, done));
   // x + P x_c into the buffer that the post-sweeps then leave the result in L.x from (in
   // place when that is where x already is)
   float* post0 = kPostSweeps % 2 == 0 ? L.x : L.t;
-  k_mg_prolong<<<g, kMgBlock, 0, ctx->stream>>>(L.m0, L.m1, L.m2, C.m0, C.m1, C.m2, C.x, cur,
-                                                post0, done);
-  ctx->launches++;
+  GFE_TRY(prolong(C, cur, post0));
   cur = post0;
   oth = post0 == L.x ? L.t : L.x;
   for (int s = 0; s < kPostSweeps; ++s) {
-    smooth(cur, oth);
+    GFE_TRY(smooth(cur, oth));
     std::swap(cur, oth);
   }
   return cur == L.x ? GFE_OK : set_error(GFE_ERR_UNSUPPORTED, "multigrid: sweep parity");
@@ -533,6 +624,14 @@ int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out) {
     k_mg_diag<<<vgrid(ctx, L.n), kMgBlock, 0, ctx->stream>>>(L.op, L.dinv);
     ctx->launches++;
     mg->lv.push_back(L);
+  }
+  for (size_t l = 0; l < mg->lv.size(); ++l) {
+    if (!coarse_from(mg, l)) continue;
+    const size_t bytes = sizeof(float) * (size_t)coarse_levels(mg, l).floats;
+    if (bytes > 48 * 1024)
+      GFE_CUDA_TRY(cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)bytes));
+    break;
   }
   GFE_CUDA_TRY(cudaGetLastError());
   return GFE_OK;

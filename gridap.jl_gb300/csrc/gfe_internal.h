@@ -241,10 +241,14 @@ int attach_p2_pmg(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p, const doubl
 struct P2PMG;
 int p2mg_create(gfe_ctx* ctx, gfe_matrix* A, P2PMG** out);
 int p2mg_apply(P2PMG* pm, const float* r, float* z, const int* done);
+// one cycle launched on the context's stream without a graph of its own (direct, or inside a
+// caller's capture)
+int p2mg_record(P2PMG* pm, const float* r, float* z, const int* done);
 void p2mg_destroy(P2PMG* pm);
 int pmg_ready(gfe_ctx* ctx, gfe_matrix* A, bool* ok);
 int pmg_create(gfe_ctx* ctx, gfe_matrix* A, Q2PMG** out);
 int pmg_apply(Q2PMG* pmg, const float* r, float* z, const int* done);
+int pmg_record(Q2PMG* pmg, const float* r, float* z, const int* done);
 void pmg_destroy(Q2PMG* pmg);
 // Whether A's cell ids are the interior-node numbering of an (n0, n1, n2) Cartesian Q1 grid
 // with every boundary node Dirichlet (device check); the pattern is then the closed form.

@@ -27,6 +27,10 @@ namespace {
 constexpr int kMgBlock = 256;
 constexpr float kOmega = 0.8f;
 constexpr int kPreSweeps = 2, kPostSweeps = 2, kCoarseSweeps = 4;
+// On deep lattices (the march of kLatK planes per thread) the first sweep from zero runs as a
+// pass of its own followed by a plain sweep: the fused pass, which forms omega D^-1 b at every
+// neighbour, loads twice the vectors per row and measured slower there.
+constexpr bool kFusePreDeep = false;
 
 // Every kernel of the cycle is launched with programmatic stream serialisation (launch_pdl):
 // its blocks may become resident while the kernel before it on the stream still runs, and
@@ -108,31 +112,36 @@ __global__ void k_mg_jacobi0(int64_t n, const float* __restrict__ b,
 }
 
 // b_c = R r_f: coarse interior node (I, J, K) sits on fine interior node (2I+1, 2J+1, 2K+1);
-// weights prod_d (1 - |delta_d| / 2) over the 27 fine neighbours
-__global__ void k_mg_restrict(int mf0, int mf1, int mc0, int mc1, int mc2,
-                              const float* __restrict__ rf, float* __restrict__ bc,
-                              const int* done) {
+// weights prod_d (1 - |delta_d| / 2) over its 27 fine neighbours, all interior (m_f = 2 m_c +
+// 1). A block covers a 32 x 8 tile of coarse (I, J) and KZ coarse planes; each thread marches
+// up its column, the weighted 3 x 3 sum of the fine plane between two coarse planes formed
+// once for both.
+template <int KZ>
+__global__ void __launch_bounds__(kMgBlock)
+    k_mg_restrict(int mf0, int mf1, int mc0, int mc1, int mc2, const float* __restrict__ rf,
+                  float* __restrict__ bc, const int* done) {
   if (stop(done)) return;
-  const int64_t nc = (int64_t)mc0 * mc1 * mc2;
-  for (int64_t c = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; c < nc;
-       c += (int64_t)gridDim.x * kMgBlock) {
-    // 32-bit index split (levels hold fewer than 2^31 rows)
-    const uint32_t cu = (uint32_t)c, rest = cu / (uint32_t)mc0;
-    const int I = (int)(cu - rest * (uint32_t)mc0);
-    const int K = (int)(rest / (uint32_t)mc1), J = (int)(rest - (uint32_t)K * (uint32_t)mc1);
-    float s = 0.f;
+  const int I = (int)blockIdx.x * 32 + (int)(threadIdx.x & 31);
+  const int J = (int)blockIdx.y * 8 + (int)(threadIdx.x >> 5);
+  if (I >= mc0 || J >= mc1) return;
+  const int K0 = (int)blockIdx.z * KZ;
+  const int64_t fs2 = (int64_t)mf0 * mf1;
+  const float* col = rf + (2 * I + 1) + (int64_t)mf0 * (2 * J + 1);  // fine (2I+1, 2J+1, 0)
+  auto plane = [&](int kz) {
+    const float* q = col + fs2 * kz;
+    const float r0 = fmaf(0.5f, q[-mf0 - 1] + q[-mf0 + 1], q[-mf0]);
+    const float r1 = fmaf(0.5f, q[-1] + q[1], q[0]);
+    const float r2 = fmaf(0.5f, q[mf0 - 1] + q[mf0 + 1], q[mf0]);
+    return fmaf(0.5f, r0 + r2, r1);
+  };
+  float lo = plane(2 * K0);
 #pragma unroll
-    for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-      for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-        for (int dx = -1; dx <= 1; ++dx) {
-          const float w = (dx ? 0.5f : 1.f) * (dy ? 0.5f : 1.f) * (dz ? 0.5f : 1.f);
-          const int64_t f = (int64_t)(2 * I + 1 + dx) +
-                            (int64_t)mf0 * ((2 * J + 1 + dy) + (int64_t)mf1 * (2 * K + 1 + dz));
-          s = fmaf(w, rf[f], s);
-        }
-    bc[c] = s;
+  for (int t = 0; t < KZ; ++t) {
+    const int K = K0 + t;
+    if (K >= mc2) break;
+    const float mid = plane(2 * K + 1), hi = plane(2 * K + 2);
+    bc[I + (int64_t)mc0 * (J + (int64_t)mc1 * K)] = fmaf(0.5f, lo + hi, mid);
+    lo = hi;
   }
 }
 
@@ -172,18 +181,64 @@ __device__ __forceinline__ float prolong_value(int i, int j, int k, int mc0, int
   return s;
 }
 
-// xo_f = x_f + P x_c (xo may be xf: each thread reads and writes its own rows only)
-__global__ void k_mg_prolong(int mf0, int mf1, int mf2, int mc0, int mc1, int mc2,
-                             const float* __restrict__ xc, const float* xf, float* xo,
-                             const int* done) {
+// xo = x_f + P x_c at the fine interior nodes: per axis, an even lattice position 2Q takes
+// coarse position Q, an odd one the mean of Q and Q + 1 (coarse boundary positions 0 and
+// m_c + 1 hold zero). A block covers a 32 x 8 tile of fine (i, j) and KZ fine planes; each
+// thread forms the (x, y)-interpolated value of a coarse plane once and marches up its column.
+// xo may be xf: each thread reads and writes its own rows only.
+template <int KZ>
+__global__ void __launch_bounds__(kMgBlock)
+    k_mg_prolong(int mf0, int mf1, int mf2, int mc0, int mc1, int mc2,
+                 const float* __restrict__ xc, const float* xf, float* xo, const int* done) {
   if (stop(done)) return;
-  const int64_t nf = (int64_t)mf0 * mf1 * mf2;
-  for (int64_t f = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; f < nf;
-       f += (int64_t)gridDim.x * kMgBlock) {
-    const uint32_t fu = (uint32_t)f, rest = fu / (uint32_t)mf0;
-    const int i = (int)(fu - rest * (uint32_t)mf0);
-    const int k = (int)(rest / (uint32_t)mf1), j = (int)(rest - (uint32_t)k * (uint32_t)mf1);
-    xo[f] = xf[f] + prolong_value(i, j, k, mc0, mc1, mc2, xc);
+  const int i = (int)blockIdx.x * 32 + (int)(threadIdx.x & 31);
+  const int j = (int)blockIdx.y * 8 + (int)(threadIdx.x >> 5);
+  if (i >= mf0 || j >= mf1) return;
+  // the two coarse interior indices along an axis and their weights (lattice position p);
+  // indices out of range are clamped and weighted 0
+  auto axis = [](int p, int mc, int& a0, int& a1, float& w0, float& w1) {
+    a0 = p / 2 - 1;
+    a1 = p / 2;
+    w0 = (p & 1) ? 0.5f : 1.f;
+    w1 = (p & 1) ? 0.5f : 0.f;
+    if (a0 < 0) {
+      a0 = 0;
+      w0 = 0.f;
+    }
+    if (a1 >= mc) {
+      a1 = mc - 1;
+      w1 = 0.f;
+    }
+  };
+  int ax0, ax1, ay0, ay1;
+  float wx0, wx1, wy0, wy1;
+  axis(i + 1, mc0, ax0, ax1, wx0, wx1);
+  axis(j + 1, mc1, ay0, ay1, wy0, wy1);
+  const int o00 = ax0 + mc0 * ay0, o10 = ax1 + mc0 * ay0;
+  const int o01 = ax0 + mc0 * ay1, o11 = ax1 + mc0 * ay1;
+  const int64_t cs2 = (int64_t)mc0 * mc1;
+  auto cplane = [&](int q) -> float {  // coarse lattice plane q (interior: 1 .. mc2)
+    if (q < 1 || q > mc2) return 0.f;
+    const float* c = xc + cs2 * (q - 1);
+    return fmaf(wy1, fmaf(wx1, c[o11], wx0 * c[o01]), wy0 * fmaf(wx1, c[o10], wx0 * c[o00]));
+  };
+  const int k0 = (int)blockIdx.z * KZ;
+  int q = (k0 + 1) >> 1;  // the coarse plane at or below fine lattice position k + 1
+  float vlo = cplane(q), vhi = cplane(q + 1);
+  const int64_t base = i + (int64_t)mf0 * j, fs2 = (int64_t)mf0 * mf1;
+#pragma unroll
+  for (int t = 0; t < KZ; ++t) {
+    const int k = k0 + t;
+    if (k >= mf2) break;
+    const int pz = k + 1;
+    if ((pz >> 1) != q) {
+      ++q;
+      vlo = vhi;
+      vhi = cplane(q + 1);
+    }
+    const float v = (pz & 1) ? 0.5f * (vlo + vhi) : vlo;
+    const int64_t row = base + fs2 * k;
+    xo[row] = xf[row] + v;
   }
 }
 
@@ -504,14 +559,23 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
     return GFE_OK;
   };
   auto restrict_to = [&](const LatticeMG::Level& C, const float* r) -> int {
-    GFE_CUDA_TRY(launch_pdl(k_mg_restrict, dim3(vgrid(ctx, C.n)), kMgBlock, 0, st, L.m0, L.m1,
-                            C.m0, C.m1, C.m2, r, C.b, done));
+    const dim3 gc = C.op.grid(C.n);
+    if ((int64_t)gc.x * gc.y * gc.z >= 4 * (int64_t)ctx->num_sms)
+      GFE_CUDA_TRY(launch_pdl(k_mg_restrict<kLatK>, gc, kMgBlock, 0, st, L.m0, L.m1, C.m0,
+                              C.m1, C.m2, r, C.b, done));
+    else
+      GFE_CUDA_TRY(launch_pdl(k_mg_restrict<1>, C.op.grid_k(1), kMgBlock, 0, st, L.m0, L.m1,
+                              C.m0, C.m1, C.m2, r, C.b, done));
     ctx->launches++;
     return GFE_OK;
   };
   auto prolong = [&](const LatticeMG::Level& C, const float* xf, float* xo) -> int {
-    GFE_CUDA_TRY(launch_pdl(k_mg_prolong, dim3(g), kMgBlock, 0, st, L.m0, L.m1, L.m2, C.m0,
-                            C.m1, C.m2, (const float*)C.x, xf, xo, done));
+    if (deep)
+      GFE_CUDA_TRY(launch_pdl(k_mg_prolong<kLatK>, ga, kMgBlock, 0, st, L.m0, L.m1, L.m2,
+                              C.m0, C.m1, C.m2, (const float*)C.x, xf, xo, done));
+    else
+      GFE_CUDA_TRY(launch_pdl(k_mg_prolong<1>, ga1, kMgBlock, 0, st, L.m0, L.m1, L.m2, C.m0,
+                              C.m1, C.m2, (const float*)C.x, xf, xo, done));
     ctx->launches++;
     return GFE_OK;
   };
@@ -527,7 +591,8 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
     GFE_TRY(residual(L.t, L.x));
     return learned_apply_into(ctx, mg->learned, L.x, L.t, L.x, done, false);
   }
-  if (pre >= 2) {  // the sweep from zero and the next one in one pass
+  const bool fuse_pre = pre >= 2 && (kFusePreDeep || !deep);
+  if (fuse_pre) {  // the sweep from zero and the next one in one pass
     if (deep)
       GFE_CUDA_TRY(launch_pdl(k_mg_pre<kLatK>, ga, kMgBlock, 0, st, L.op, (const float*)L.b,
                               (const float*)L.dinv, oth, done));
@@ -540,7 +605,7 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
                             (const float*)L.dinv, cur, done));
   }
   ctx->launches++;
-  for (int s = 2; s < pre; ++s) {
+  for (int s = fuse_pre ? 2 : 1; s < pre; ++s) {
     GFE_TRY(smooth(cur, oth));
     std::swap(cur, oth);
   }

@@ -300,7 +300,7 @@ int pmg_create(gfe_ctx* ctx, gfe_matrix* A, Q2PMG** out) {
 }
 
 // one V-cycle: z = M(r)
-static int pmg_record(Q2PMG* pm, const float* r, float* z, const int* done) {
+int pmg_record(Q2PMG* pm, const float* r, float* z, const int* done) {
   gfe_ctx* ctx = pm->ctx;
   gfe_matrix* A = pm->A;
   const int64_t n = A->nrows;
@@ -892,7 +892,7 @@ int p2mg_create(gfe_ctx* ctx, gfe_matrix* A, P2PMG** out) {
   return GFE_OK;
 }
 
-static int p2mg_record(P2PMG* pm, const float* r, float* z, const int* done) {
+int p2mg_record(P2PMG* pm, const float* r, float* z, const int* done) {
   gfe_ctx* ctx = pm->ctx;
   gfe_matrix* A = pm->A;
   gfe_matrix* Ac = pm->Ac;

@@ -1379,6 +1379,11 @@ __global__ void k_fcg_restart(int64_t n, const double* __restrict__ r64, float* 
   }
 }
 
+// the condition of the device-driven FCG loop: repeat while the state is not done
+__global__ void k_fcg_continue(cudaGraphConditionalHandle h, const SolverState* S) {
+  cudaGraphSetConditional(h, S->done ? 0u : 1u);
+}
+
 // ---- host drivers -------------------------------------------------------------------------
 struct SolverWork {
   SolverState* S;      // device
@@ -1986,10 +1991,20 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     // a V-cycle iteration is expensive: look at the state after every one
     if (o->check_every <= 0) check_every = 1;
   }
+  // Without kernel timing and without the learned preconditioner's stagnation check, the
+  // iterations run as one device-driven loop: a CUDA graph whose WHILE node repeats [update,
+  // preconditioner, beta, direction, SpMV] until the state's done flag is set (converged,
+  // reliable update due, maxit reached or non-finite), so that the host waits only where the
+  // loop stops. The preconditioner's launches are then recorded into that graph, and issued
+  // directly outside it, instead of replaying a graph of their own.
+  bool device_loop = !ctx->timer.enabled && !learned;
   auto precond = [&]() -> int {
-    if (use_mg && pmg) return pmg_apply(pmg, r32, z32, &w.S->done);
-    if (use_mg && p2mg) return p2mg_apply(p2mg, r32, z32, &w.S->done);
-    if (use_mg) return mg_apply(mg, r32, z32, &w.S->done);
+    if (use_mg && pmg) return device_loop ? pmg_record(pmg, r32, z32, &w.S->done)
+                                          : pmg_apply(pmg, r32, z32, &w.S->done);
+    if (use_mg && p2mg) return device_loop ? p2mg_record(p2mg, r32, z32, &w.S->done)
+                                           : p2mg_apply(p2mg, r32, z32, &w.S->done);
+    if (use_mg) return device_loop ? mg_record(mg, r32, z32, &w.S->done)
+                                   : mg_apply(mg, r32, z32, &w.S->done);
     if (learned) return learned_apply(ctx, pc, r32, z32, &w.S->done);
     k_jacobi_apply<<<gv, kVecBlock, 0, ctx->stream>>>(n, r32, dinv32, z32, w.S);
     ctx->launches++;
@@ -2009,26 +2024,85 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   GFE_CUDA_TRY(cudaMemcpyAsync(p32, z32, sizeof(float) * n, cudaMemcpyDeviceToDevice,
                                ctx->stream));
   spmv();
+  // the loop graph, built while the device runs the first iteration's work
+  struct LoopExec {
+    cudaGraphExec_t e = nullptr;
+    ~LoopExec() {
+      if (e) cudaGraphExecDestroy(e);
+    }
+  } loop;
+  long long body_launches = 0;
+  if (device_loop) {
+    cudaGraph_t g = nullptr;
+    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+    cudaGraphConditionalHandle h{};
+    cudaGraphNodeParams np = {};
+    cudaGraphNode_t node;
+    ok = ok && cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) ==
+                   cudaSuccess;
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    ok = ok && cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+    if (ok && cudaStreamBeginCaptureToGraph(ctx->stream, np.conditional.phGraph_out[0], nullptr,
+                                            nullptr, 0,
+                                            cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const long long l0 = ctx->launches;
+      k_fcg_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S);
+      const int st = precond();
+      k_fcg_beta<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
+      k_fcg_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
+      spmv();
+      k_fcg_continue<<<1, 1, 0, ctx->stream>>>(h, w.S);
+      body_launches = ctx->launches - l0 + 4;
+      ctx->launches = l0;
+      cudaGraph_t body = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &body);
+      if (st != GFE_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+      }
+      ok = ce == cudaSuccess && cudaGraphInstantiate(&loop.e, g, 0) == cudaSuccess;
+    } else {
+      ok = false;
+    }
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+      // conditional graphs unavailable: the host-driven loop below (direct launches)
+      (void)cudaGetLastError();
+      if (loop.e) cudaGraphExecDestroy(loop.e);
+      loop.e = nullptr;
+    }
+  }
   GFE_TRY(read_state(ctx, w));
   int updates = 0, slow = 0, fallback = 0;
   double rr_chunk = w.hS->rr;
   bool fresh = false;  // the loop ended on a reliable update: x64 and rr64 are current
   while (!w.hS->done) {
-    for (int k = 0; k < check_every; ++k) {
-      timer_begin(ctx, GFE_KT_VECTOR);
-      k_fcg_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S);
-      timer_end(ctx);
-      ctx->launches++;
-      GFE_TRY(precond());
-      timer_begin(ctx, GFE_KT_VECTOR);
-      k_fcg_beta<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
-      k_fcg_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
-      timer_end(ctx);
-      ctx->launches += 2;
-      spmv();
+    if (loop.e) {
+      const int it0 = w.hS->iter;
+      GFE_CUDA_TRY(cudaGraphLaunch(loop.e, ctx->stream));
+      GFE_TRY(read_state(ctx, w));
+      ctx->launches += (long long)(w.hS->iter - it0) * body_launches;
+    } else {
+      for (int k = 0; k < check_every; ++k) {
+        timer_begin(ctx, GFE_KT_VECTOR);
+        k_fcg_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials,
+                                                        w.S);
+        timer_end(ctx);
+        ctx->launches++;
+        GFE_TRY(precond());
+        timer_begin(ctx, GFE_KT_VECTOR);
+        k_fcg_beta<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
+        k_fcg_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
+        timer_end(ctx);
+        ctx->launches += 2;
+        spmv();
+      }
+      GFE_CUDA_TRY(cudaGetLastError());
+      GFE_TRY(read_state(ctx, w));
     }
-    GFE_CUDA_TRY(cudaGetLastError());
-    GFE_TRY(read_state(ctx, w));
     if (w.hS->done && (w.hS->need_update || w.hS->converged)) {
       // reliable update: x64 += x32, r64 = b - A64 x64, r32 = r64 (or stop)
       k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);

@@ -409,7 +409,10 @@ def run_gpu(args):
     # on; the roofline comes from that instrumented repeat (its ms_per_step is reported too).
     if args.profile:
         # the headline steps alone, for a profiler's launch list (no JSON line: a number taken
-        # under a profiler is not a measurement)
+        # under a profiler is not a measurement). Kernel timing is on, so that the solver
+        # launches its iterations from the host: kernels inside the device-driven loop (a
+        # graph with a conditional node) are invisible to a per-kernel profiler.
+        ctx.set_timing(True)
         for _ in range(args.warmup + args.steps):
             mixed_dev()
         barrier()

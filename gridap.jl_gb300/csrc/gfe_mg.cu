@@ -145,42 +145,6 @@ __global__ void __launch_bounds__(kMgBlock)
   }
 }
 
-// (P x_c) at fine interior node (i, j, k): trilinear, coarse boundary nodes are zero
-__device__ __forceinline__ float prolong_value(int i, int j, int k, int mc0, int mc1, int mc2,
-                                               const float* __restrict__ xc) {
-  int ci[2], cj[2], ck[2];
-  float wi[2], wj[2], wk[2];
-  auto axis = [](int p, int mc, int* cc, float* ww) {  // p = lattice position (1-based)
-    if ((p & 1) == 0) {
-      cc[0] = p / 2 - 1;
-      ww[0] = 1.f;
-      cc[1] = -1;
-      ww[1] = 0.f;
-    } else {
-      cc[0] = p / 2 - 1;  // coarse interior index of lattice p/2 (-1: boundary)
-      cc[1] = p / 2;      // of lattice p/2 + 1 (mc: boundary)
-      ww[0] = ww[1] = 0.5f;
-      if (cc[1] >= mc) cc[1] = -1;
-    }
-  };
-  axis(i + 1, mc0, ci, wi);
-  axis(j + 1, mc1, cj, wj);
-  axis(k + 1, mc2, ck, wk);
-  float s = 0.f;
-#pragma unroll
-  for (int a = 0; a < 2; ++a)
-#pragma unroll
-    for (int bb = 0; bb < 2; ++bb)
-#pragma unroll
-      for (int cc = 0; cc < 2; ++cc) {
-        if (ci[a] < 0 || cj[bb] < 0 || ck[cc] < 0) continue;
-        const float w = wi[a] * wj[bb] * wk[cc];
-        if (w == 0.f) continue;
-        s = fmaf(w, xc[(int64_t)ci[a] + (int64_t)mc0 * (cj[bb] + (int64_t)mc1 * ck[cc])], s);
-      }
-  return s;
-}
-
 // xo = x_f + P x_c at the fine interior nodes: per axis, an even lattice position 2Q takes
 // coarse position Q, an odd one the mean of Q and Q + 1 (coarse boundary positions 0 and
 // m_c + 1 hold zero). A block covers a 32 x 8 tile of fine (i, j) and KZ fine planes; each
@@ -284,19 +248,23 @@ __global__ void k_mg_diag(LatticeQ1Op op, float* __restrict__ dinv) {
 // Levels of at most kCoarseRows rows run their whole V-cycle inside one block of kCoarseBlock
 // threads: on such lattices a launch costs more than its work. The block copies kappa and
 // D^-1 of these levels and b of the first one into shared memory, runs every step there
-// (block-stride loops, a barrier between steps; x, b and t of every level live in shared
-// memory only) and writes x of the first level back.
+// (a barrier between steps; x, b and t of every level live in shared memory only) and writes
+// x of the first level back. x and t are held with a zero halo (so that no neighbour needs a
+// bounds check); a thread takes a segment of `ks` rows up one (i, j) column and marches it
+// with three x-planes and the kappa box sums of two cell layers in registers.
 constexpr int64_t kCoarseRows = 512;
 constexpr int kCoarseBlock = kCoarseRows > 512 ? 1024 : 512;
 constexpr int kMaxCoarse = 6;
 
-// one level of the block: float offsets of its vectors and kappa in the shared buffer
+// one level of the block: float offsets of its arrays in the shared buffer
 struct MgCoarseLevel {
-  int m0, m1, m2, n;        // interior nodes per direction, rows
-  int c1, c2, ncell;        // kappa strides (as in LatticeQ1Op), kappa entries c2 * n2
-  int x, b, t, dinv, kap;   // offsets into the shared buffer
-  float W[8];               // class weights Kref[0][c]
-  const float* gkap;        // kappa and D^-1 in global memory
+  int m0, m1, m2, n;       // interior nodes per direction, rows
+  int q0, q1;              // strides of the zero-halo layout of x and t: m0 + 2, q0 (m1 + 2)
+  int c1, c2, ncell;       // kappa strides (as in LatticeQ1Op), kappa entries c2 * n2
+  int ks, nseg;            // rows per column segment, segments per column
+  int x, t, b, dinv, kap;  // offsets into the shared buffer (x, t: q1 (m2 + 2) entries)
+  float W[8];              // class weights Kref[0][c]
+  const float* gkap;       // kappa and D^-1 in global memory
   const float* gdinv;
 };
 
@@ -308,64 +276,73 @@ struct CoarseLevels {
   MgCoarseLevel L[kMaxCoarse];
 };
 
-// (A p)_r at interior node (i, j, k) of a level held in shared memory: the class-sum form of
-// the lattice rows, (A p)_r = sum_c W[c] sum_{d in class c} S(d) p_{r+d}, S(d) the kappa sum
-// over the cells r and r + d share; one x-plane of 9 neighbours at a time (0 outside the
-// interior).
-__device__ __forceinline__ float coarse_row(const MgCoarseLevel& L, const float* sm, int i,
-                                            int j, int k, const float* p) {
-  const float* kp = sm + L.kap + i + L.c1 * j + L.c2 * k;
-  // box sums of one cell layer, indexed e = (dx + 1) + 3 (dy + 1)
-  auto layer = [&](const float* q, float* Lb) {
-    const float v0 = q[0], v1 = q[1], v2 = q[L.c1], v3 = q[L.c1 + 1];
-    const float X0 = v0 + v1, X1 = v2 + v3;
-    Lb[0] = v0;
-    Lb[1] = X0;
-    Lb[2] = v1;
-    Lb[3] = v0 + v2;
-    Lb[4] = X0 + X1;
-    Lb[5] = v1 + v3;
-    Lb[6] = v2;
-    Lb[7] = X1;
-    Lb[8] = v3;
-  };
-  float la[9], lb[9];
-  layer(kp, la);
-  layer(kp + L.c2, lb);
-  float T[8];
+// The rows of one phase on level L: every (column, segment) item; `epi(row, padded index, x
+// at the row, (A x)_row)` receives each row of the item. x is a zero-halo vector in shared
+// memory. (A x)_r in class-sum form as the lattice rows: sum_c W[c] sum_{d in c} S(d) x_{r+d},
+// S(d) the kappa sum over the cells r and r + d share.
+template <class Epi>
+__device__ __forceinline__ void coarse_rows(const MgCoarseLevel& L, const float* sm,
+                                            const float* x, Epi epi) {
+  const float* kap = sm + L.kap;
+  const int items = L.m0 * L.m1 * L.nseg;
+  for (int it = (int)threadIdx.x; it < items; it += kCoarseBlock) {
+    const int col = it / L.nseg, seg = it - col * L.nseg;
+    const int j = col / L.m0, i = col - j * L.m0;
+    const int k0 = seg * L.ks, k1 = min(k0 + L.ks, L.m2);
+    // x at padded (i + 1 + dx, j + 1 + dy, kk + 1), dx, dy in -1 .. 1
+    const float* xc = x + (i + 1) + L.q0 * (j + 1);
+    auto xplane = [&](int kk, float* v) {
+      const float* p = xc + L.q1 * (kk + 1);
 #pragma unroll
-  for (int c = 0; c < 8; ++c) T[c] = 0.f;
+      for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
-  for (int dz = -1; dz <= 1; ++dz) {
-    const int kk = k + dz;
-    const bool okz = kk >= 0 && kk < L.m2;
+        for (int dx = -1; dx <= 1; ++dx) v[(dx + 1) + 3 * (dy + 1)] = p[dx + L.q0 * dy];
+    };
+    // box sums of cell layer kk (cells (i + cx, j + cy, kk)), indexed (dx + 1) + 3 (dy + 1)
+    const float* kc = kap + i + L.c1 * j;
+    auto layer = [&](int kk, float* Lb) {
+      const float* q = kc + L.c2 * kk;
+      const float v0 = q[0], v1 = q[1], v2 = q[L.c1], v3 = q[L.c1 + 1];
+      const float X0 = v0 + v1, X1 = v2 + v3;
+      Lb[0] = v0;
+      Lb[1] = X0;
+      Lb[2] = v1;
+      Lb[3] = v0 + v2;
+      Lb[4] = X0 + X1;
+      Lb[5] = v1 + v3;
+      Lb[6] = v2;
+      Lb[7] = X1;
+      Lb[8] = v3;
+    };
+    float xa[9], xb[9], xn[9], la[9], lb[9];
+    xplane(k0 - 1, xa);
+    xplane(k0, xb);
+    layer(k0, la);
+    for (int k = k0; k < k1; ++k) {
+      xplane(k + 1, xn);
+      layer(k + 1, lb);
+      float T[8];
 #pragma unroll
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int jj = j + dy;
-      const bool oky = okz && jj >= 0 && jj < L.m1;
+      for (int c = 0; c < 8; ++c) T[c] = 0.f;
 #pragma unroll
-      for (int dx = -1; dx <= 1; ++dx) {
-        const int ii = i + dx;
-        const int e = (dx + 1) + 3 * (dy + 1);
-        const int cl = (dx ? 1 : 0) | (dy ? 2 : 0) | (dz ? 4 : 0);
-        const float xv = oky && ii >= 0 && ii < L.m0 ? p[ii + L.m0 * (jj + L.m1 * kk)] : 0.f;
-        const float S = dz < 0 ? la[e] : (dz > 0 ? lb[e] : la[e] + lb[e]);
-        T[cl] = fmaf(S, xv, T[cl]);
+      for (int e = 0; e < 9; ++e) {
+        const int cl = (e % 3 != 1 ? 1 : 0) | (e / 3 != 1 ? 2 : 0);
+        T[cl | 4] = fmaf(la[e], xa[e], T[cl | 4]);
+        T[cl] = fmaf(la[e] + lb[e], xb[e], T[cl]);
+        T[cl | 4] = fmaf(lb[e], xn[e], T[cl | 4]);
+      }
+      float acc = 0.f;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc = fmaf(L.W[c], T[c], acc);
+      epi(i + L.m0 * (j + L.m1 * k), (i + 1) + L.q0 * (j + 1) + L.q1 * (k + 1), xb[4], acc);
+#pragma unroll
+      for (int e = 0; e < 9; ++e) {
+        xa[e] = xb[e];
+        xb[e] = xn[e];
+        la[e] = lb[e];
       }
     }
   }
-  float acc = 0.f;
-#pragma unroll
-  for (int c = 0; c < 8; ++c) acc = fmaf(L.W[c], T[c], acc);
-  return acc;
-}
-
-__device__ __forceinline__ void coarse_ijk(const MgCoarseLevel& L, int r, int& i, int& j,
-                                           int& k) {
-  const uint32_t ru = (uint32_t)r, rest = ru / (uint32_t)L.m0;
-  i = (int)(ru - rest * (uint32_t)L.m0);
-  k = (int)(rest / (uint32_t)L.m1);
-  j = (int)(rest - (uint32_t)k * (uint32_t)L.m1);
 }
 
 // the V-cycle of levels 0 .. nl-1 of `c` (b of level 0 given, its result written to x0); the
@@ -375,27 +352,39 @@ __global__ void __launch_bounds__(kCoarseBlock)
   if (stop(done)) return;
   extern __shared__ float sm[];
   const int t0 = threadIdx.x;
+  // zero-halo x and t (whole arrays), kappa, D^-1 and the first level's b
   for (int l = 0; l < c.nl; ++l) {
     const MgCoarseLevel& L = c.L[l];
+    const int np = L.q1 * (L.m2 + 2);
+    for (int e = t0; e < 2 * np; e += kCoarseBlock) sm[L.x + e] = 0.f;  // t follows x
     for (int e = t0; e < L.ncell; e += kCoarseBlock) sm[L.kap + e] = L.gkap[e];
     for (int r = t0; r < L.n; r += kCoarseBlock) sm[L.dinv + r] = L.gdinv[r];
   }
   for (int r = t0; r < c.L[0].n; r += kCoarseBlock) sm[c.L[0].b + r] = c.b0[r];
   __syncthreads();
-  auto sweep = [&](const MgCoarseLevel& L, int xi, int xo) {
+  // the interior rows of level L: f(row, padded index)
+  auto rows = [&](const MgCoarseLevel& L, auto f) {
     for (int r = t0; r < L.n; r += kCoarseBlock) {
-      int i, j, k;
-      coarse_ijk(L, r, i, j, k);
-      const float acc = coarse_row(L, sm, i, j, k, sm + xi);
-      sm[xo + r] = fmaf(kOmega * sm[L.dinv + r], sm[L.b + r] - acc, sm[xi + r]);
+      const int jk = r / L.m0, i = r - jk * L.m0;
+      const int k = jk / L.m1, j = jk - k * L.m1;
+      f(r, (i + 1) + L.q0 * (j + 1) + L.q1 * (k + 1), i, j, k);
     }
+  };
+  auto sweep = [&](const MgCoarseLevel& L, int xi, int xo) {
+    float* out = sm + xo;
+    const float* b = sm + L.b;
+    const float* dv = sm + L.dinv;
+    coarse_rows(L, sm, sm + xi, [&](int r, int pr, float xc, float acc) {
+      out[pr] = fmaf(kOmega * dv[r], b[r] - acc, xc);
+    });
     __syncthreads();
   };
   // down
   for (int l = 0; l < c.nl; ++l) {
     const MgCoarseLevel& L = c.L[l];
-    for (int r = t0; r < L.n; r += kCoarseBlock)  // the sweep from zero
-      sm[L.x + r] = kOmega * sm[L.dinv + r] * sm[L.b + r];
+    rows(L, [&](int r, int pr, int, int, int) {  // the sweep from zero
+      sm[L.x + pr] = kOmega * sm[L.dinv + r] * sm[L.b + r];
+    });
     __syncthreads();
     if (l + 1 == c.nl) {  // coarsest: four more sweeps, ending in x
       for (int s = 0; s < kCoarseSweeps; s += 2) {
@@ -405,45 +394,46 @@ __global__ void __launch_bounds__(kCoarseBlock)
       break;
     }
     sweep(L, L.x, L.t);
-    for (int r = t0; r < L.n; r += kCoarseBlock) {  // residual into x
-      int i, j, k;
-      coarse_ijk(L, r, i, j, k);
-      sm[L.x + r] = sm[L.b + r] - coarse_row(L, sm, i, j, k, sm + L.t);
+    {  // residual into x
+      float* out = sm + L.x;
+      const float* b = sm + L.b;
+      coarse_rows(L, sm, sm + L.t,
+                  [&](int r, int pr, float, float acc) { out[pr] = b[r] - acc; });
     }
     __syncthreads();
     const MgCoarseLevel& C = c.L[l + 1];
-    for (int q = t0; q < C.n; q += kCoarseBlock) {  // restriction
-      int I, J, K;
-      coarse_ijk(C, q, I, J, K);
-      float s = 0.f;
-#pragma unroll
-      for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-        for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-          for (int dx = -1; dx <= 1; ++dx) {
-            const float w = (dx ? 0.5f : 1.f) * (dy ? 0.5f : 1.f) * (dz ? 0.5f : 1.f);
-            const int f = (2 * I + 1 + dx) + L.m0 * ((2 * J + 1 + dy) + L.m1 * (2 * K + 1 + dz));
-            s = fmaf(w, sm[L.x + f], s);
-          }
-      sm[C.b + q] = s;
-    }
+    rows(C, [&](int q, int, int I, int J, int K) {  // restriction from the fine x
+      const float* f = sm + L.x + (2 * I + 2) + L.q0 * (2 * J + 2) + L.q1 * (2 * K + 2);
+      auto plane = [&](const float* p) {
+        const float r0 = fmaf(0.5f, p[-L.q0 - 1] + p[-L.q0 + 1], p[-L.q0]);
+        const float r1 = fmaf(0.5f, p[-1] + p[1], p[0]);
+        const float r2 = fmaf(0.5f, p[L.q0 - 1] + p[L.q0 + 1], p[L.q0]);
+        return fmaf(0.5f, r0 + r2, r1);
+      };
+      sm[C.b + q] = fmaf(0.5f, plane(f - L.q1) + plane(f + L.q1), plane(f));
+    });
     __syncthreads();
   }
-  // up: x = t + P x_c, then two sweeps back into x
+  // up: x = t + P x_c (trilinear over the zero-halo coarse x: an even lattice position p
+  // reads coarse position p / 2 twice, an odd one p / 2 and p / 2 + 1), then two sweeps
   for (int l = c.nl - 2; l >= 0; --l) {
     const MgCoarseLevel& L = c.L[l];
     const MgCoarseLevel& C = c.L[l + 1];
-    for (int r = t0; r < L.n; r += kCoarseBlock) {
-      int i, j, k;
-      coarse_ijk(L, r, i, j, k);
-      sm[L.x + r] = sm[L.t + r] + prolong_value(i, j, k, C.m0, C.m1, C.m2, sm + C.x);
-    }
+    const float* xc = sm + C.x;
+    rows(L, [&](int, int pr, int i, int j, int k) {
+      const int a0 = (i + 1) >> 1, a1 = (i + 2) >> 1;
+      const int b0 = C.q0 * ((j + 1) >> 1), b1 = C.q0 * ((j + 2) >> 1);
+      const int g0 = C.q1 * ((k + 1) >> 1), g1 = C.q1 * ((k + 2) >> 1);
+      const float v0 = (xc[a0 + b0 + g0] + xc[a1 + b0 + g0]) + (xc[a0 + b1 + g0] + xc[a1 + b1 + g0]);
+      const float v1 = (xc[a0 + b0 + g1] + xc[a1 + b0 + g1]) + (xc[a0 + b1 + g1] + xc[a1 + b1 + g1]);
+      sm[L.x + pr] = fmaf(0.125f, v0 + v1, sm[L.t + pr]);
+    });
     __syncthreads();
     sweep(L, L.x, L.t);
     sweep(L, L.t, L.x);
   }
-  for (int r = t0; r < c.L[0].n; r += kCoarseBlock) c.x0[r] = sm[c.L[0].x + r];
+  const MgCoarseLevel& L0 = c.L[0];
+  rows(L0, [&](int r, int pr, int, int, int) { c.x0[r] = sm[L0.x + pr]; });
 }
 
 }  // namespace
@@ -495,15 +485,22 @@ CoarseLevels coarse_levels(const LatticeMG* mg, size_t l) {
     S.m1 = Q.m1;
     S.m2 = Q.m2;
     S.n = (int)Q.n;
+    S.q0 = Q.m0 + 2;
+    S.q1 = S.q0 * (Q.m1 + 2);
     S.c1 = Q.op.c1;
     S.c2 = Q.op.c2;
     S.ncell = Q.op.c2 * Q.op.n2;
+    // segments: enough (column, segment) items for the block, at most 8 rows each
+    const int cols = Q.m0 * Q.m1;
+    S.ks = std::max(1, std::min(8, cols * Q.m2 / kCoarseBlock));
+    S.nseg = (Q.m2 + S.ks - 1) / S.ks;
+    const int np = S.q1 * (Q.m2 + 2);
     S.x = off;
-    S.b = off + S.n;
-    S.t = off + 2 * S.n;
-    S.dinv = off + 3 * S.n;
-    S.kap = off + 4 * S.n;
-    off += 4 * S.n + S.ncell;
+    S.t = off + np;
+    S.b = off + 2 * np;
+    S.dinv = S.b + S.n;
+    S.kap = S.dinv + S.n;
+    off = S.kap + S.ncell;
     for (int e = 0; e < 8; ++e) S.W[e] = Q.op.K[8 * e];
     S.gkap = Q.op.kap;
     S.gdinv = Q.dinv;

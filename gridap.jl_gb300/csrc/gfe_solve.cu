@@ -247,7 +247,6 @@ int build_dia(gfe_ctx* ctx, gfe_matrix* A) {
   GFE_TRY(tmp.reserve(64 + sizeof(int32_t) * 64));
   unsigned long long* drow = tmp.as<unsigned long long>();
   int* dbad = (int*)((char*)tmp.ptr + 16);
-  int32_t* dcols = (int32_t*)((char*)tmp.ptr + 64);
   const unsigned long long init = ~0ull;
   GFE_CUDA_TRY(cudaMemcpyAsync(drow, &init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
   GFE_CUDA_TRY(cudaMemsetAsync(dbad, 0, sizeof(int), ctx->stream));
@@ -1379,6 +1378,147 @@ __global__ void k_fcg_restart(int64_t n, const double* __restrict__ r64, float* 
   }
 }
 
+// The same three FCG vector steps over float4 groups (16-byte aligned vectors), two groups in
+// flight per thread per trip; a scalar tail covers n % 4 entries. Same arithmetic per entry.
+__global__ void __launch_bounds__(kVecBlock)
+    k_fcg_update4(int64_t n, float* __restrict__ x, float* __restrict__ r,
+                  const float* __restrict__ p, const float* __restrict__ q,
+                  double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kVecBlock / 32];
+  if (S->done) return;
+  const float a = (float)S->alpha;
+  float rr_t = 0.f;
+  const int64_t n4 = n >> 2;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = tid; i0 < n4; i0 += 2 * nth) {
+    float4 xv[2], rv[2], pv[2], qv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t i = i0 + u * nth;
+      if (i < n4) {
+        xv[u] = reinterpret_cast<float4*>(x)[i];
+        rv[u] = reinterpret_cast<float4*>(r)[i];
+        pv[u] = __ldg(reinterpret_cast<const float4*>(p) + i);
+        qv[u] = __ldg(reinterpret_cast<const float4*>(q) + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t i = i0 + u * nth;
+      if (i < n4) {
+        float* xs = &xv[u].x;
+        float* rs = &rv[u].x;
+        const float* ps = &pv[u].x;
+        const float* qs = &qv[u].x;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          xs[c] = fmaf(a, ps[c], xs[c]);
+          rs[c] = fmaf(-a, qs[c], rs[c]);
+          rr_t = fmaf(rs[c], rs[c], rr_t);
+        }
+        reinterpret_cast<float4*>(x)[i] = xv[u];
+        reinterpret_cast<float4*>(r)[i] = rv[u];
+      }
+    }
+  }
+  for (int64_t i = 4 * n4 + tid; i < n; i += nth) {
+    x[i] = fmaf(a, p[i], x[i]);
+    const float ri = fmaf(-a, q[i], r[i]);
+    r[i] = ri;
+    rr_t = fmaf(ri, ri, rr_t);
+  }
+  const double rr = block_sum<kVecBlock>((double)rr_t, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = rr;
+  double tot[1];
+  if (last_block_reduce<kVecBlock, 1>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->iter += 1;
+    S->rr = tot[0];
+    if (!isfinite(tot[0])) {
+      S->done = 1;
+    } else if (tot[0] <= S->tol2) {
+      S->done = 1;
+      S->converged = 1;
+    } else if (S->iter >= S->maxit) {
+      S->done = 1;
+    } else if (S->delta2 > 0.0 && tot[0] < S->delta2 * S->rmax2) {
+      S->done = 1;
+      S->need_update = 1;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kVecBlock)
+    k_fcg_beta4(int64_t n, const float* __restrict__ z, const float* __restrict__ q,
+                double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kVecBlock / 32];
+  if (S->done) return;
+  float t = 0.f;
+  const int64_t n4 = n >> 2;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = tid; i0 < n4; i0 += 2 * nth) {
+    float4 zv[2], qv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t i = i0 + u * nth;
+      if (i < n4) {
+        zv[u] = __ldg(reinterpret_cast<const float4*>(z) + i);
+        qv[u] = __ldg(reinterpret_cast<const float4*>(q) + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      if (i0 + u * nth < n4) {
+        t = fmaf(zv[u].x, qv[u].x, t);
+        t = fmaf(zv[u].y, qv[u].y, t);
+        t = fmaf(zv[u].z, qv[u].z, t);
+        t = fmaf(zv[u].w, qv[u].w, t);
+      }
+  }
+  for (int64_t i = 4 * n4 + tid; i < n; i += nth) t = fmaf(z[i], q[i], t);
+  const double d = block_sum<kVecBlock>((double)t, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = d;
+  double tot[1];
+  if (last_block_reduce<kVecBlock, 1>(&S->ticket[3], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0)
+    S->beta = S->pq != 0.0 ? -tot[0] / S->pq : 0.0;
+}
+
+__global__ void __launch_bounds__(kVecBlock)
+    k_fcg_dir4(int64_t n, float* __restrict__ p, const float* __restrict__ z,
+               const SolverState* S) {
+  if (S->done) return;
+  const float beta = (float)S->beta;
+  const int64_t n4 = n >> 2;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = tid; i0 < n4; i0 += 2 * nth) {
+    float4 pv[2], zv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t i = i0 + u * nth;
+      if (i < n4) {
+        pv[u] = reinterpret_cast<float4*>(p)[i];
+        zv[u] = __ldg(reinterpret_cast<const float4*>(z) + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t i = i0 + u * nth;
+      if (i < n4) {
+        pv[u].x = fmaf(beta, pv[u].x, zv[u].x);
+        pv[u].y = fmaf(beta, pv[u].y, zv[u].y);
+        pv[u].z = fmaf(beta, pv[u].z, zv[u].z);
+        pv[u].w = fmaf(beta, pv[u].w, zv[u].w);
+        reinterpret_cast<float4*>(p)[i] = pv[u];
+      }
+    }
+  }
+  for (int64_t i = 4 * n4 + tid; i < n; i += nth) p[i] = fmaf(beta, p[i], z[i]);
+}
+
 // the condition of the device-driven FCG loop: repeat while the state is not done
 __global__ void k_fcg_continue(cudaGraphConditionalHandle h, const SolverState* S) {
   cudaGraphSetConditional(h, S->done ? 0u : 1u);
@@ -1898,6 +2038,24 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
         *z32 = f + 4 * npad;
   const float* dinv32 = csr_residual ? nullptr : A->dinv32.as<float>();
   const unsigned gv = (unsigned)(ctx->num_sms * 4), gs = grid_for(n, kSpmvBlock);
+  // the FP32 vectors sit at multiples of 64 entries from a 256-byte aligned base: the float4
+  // kernels apply
+  const bool vec4 = (reinterpret_cast<uintptr_t>(f) & 15) == 0;
+  auto fcg_update = [&]() {
+    if (vec4)
+      k_fcg_update4<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S);
+    else
+      k_fcg_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S);
+  };
+  auto fcg_beta_dir = [&]() {
+    if (vec4) {
+      k_fcg_beta4<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
+      k_fcg_dir4<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
+    } else {
+      k_fcg_beta<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
+      k_fcg_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
+    }
+  };
   // r64 = b - A x64 in FP64, r64.r64 into *rr
   const size_t lat_smem = sizeof(double) * 32 * 27 * (kSpmvBlock / 32);
   if (A->cart_lattice)
@@ -2049,10 +2207,9 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
                                             nullptr, 0,
                                             cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const long long l0 = ctx->launches;
-      k_fcg_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S);
+      fcg_update();
       const int st = precond();
-      k_fcg_beta<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
-      k_fcg_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
+      fcg_beta_dir();
       spmv();
       k_fcg_continue<<<1, 1, 0, ctx->stream>>>(h, w.S);
       body_launches = ctx->launches - l0 + 4;
@@ -2088,14 +2245,12 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     } else {
       for (int k = 0; k < check_every; ++k) {
         timer_begin(ctx, GFE_KT_VECTOR);
-        k_fcg_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials,
-                                                        w.S);
+        fcg_update();
         timer_end(ctx);
         ctx->launches++;
         GFE_TRY(precond());
         timer_begin(ctx, GFE_KT_VECTOR);
-        k_fcg_beta<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
-        k_fcg_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
+        fcg_beta_dir();
         timer_end(ctx);
         ctx->launches += 2;
         spmv();
@@ -2119,8 +2274,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       }
       // z, p restart from the new residual direction (keeps FCG's beta well defined)
       GFE_TRY(precond());
-      k_fcg_beta<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
-      k_fcg_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
+      fcg_beta_dir();
       ctx->launches += 2;
       spmv();
       rr_chunk = w.hS->rr;

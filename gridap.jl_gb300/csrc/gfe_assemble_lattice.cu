@@ -21,7 +21,8 @@
 // below (9 sums), and multiplies 18 entries (the 9 entries towards the layer below are the
 // products formed one step earlier for the layer above); the load vector takes 11 operations
 // (x-, y- and z-passes of the separable stencil). 43 FP64 operations per row against 128 in the
-// generic row gather. Both rows of a symmetric pair form the same sums in the same order, so the
+// generic row gather; 34 on cubic cells, whose face classes carry no weight (their entries are
+// stored as zeros without forming the sums). Both rows of a symmetric pair form the same sums in the same order, so the
 // matrix is exactly symmetric.
 //
 // Stores: a warp holds 32 consecutive rows (one x-line), whose CSR slice is contiguous; the
@@ -69,6 +70,10 @@ struct LayerSums {
   }
 };
 
+// ZF: the face classes 1, 2 and 4 (vertices differing along one axis) carry no weight, as
+// on cubic cells; their entries are stored as zeros without forming S (21 % of the FP64
+// operations per row).
+template <bool ZF>
 __global__ void __launch_bounds__(kCqBlock) k_assemble_cart_q1(const CartQ1Lattice a) {
   extern __shared__ double stage_all[];
   const int lane = (int)(threadIdx.x & 31), warp = (int)(threadIdx.x >> 5);
@@ -112,10 +117,15 @@ __global__ void __launch_bounds__(kCqBlock) k_assemble_cart_q1(const CartQ1Latti
   LayerSums lo, up;
   layer(k0, lo);
   double carry[9];  // dz = -1 entries: W[class | z] * box of the layer below
+  // the entry of class cls from box sum S: W[cls] * S, or 0 for a weightless class
+  auto entry = [&](int cls, double S) -> double {
+    if (ZF && (cls == 1 || cls == 2 || cls == 4)) return 0.0;
+    return a.W[cls] * S;
+  };
 #pragma unroll
   for (int e = 0; e < 9; ++e) {
     const int cls = (e % 3 != 1 ? 1 : 0) | (e / 3 != 1 ? 2 : 0) | 4;
-    carry[e] = a.W[cls] * lo.box(e);
+    carry[e] = entry(cls, lo.box(e));
   }
   double u0 = 0.0, u1 = 0.0;
   if (nodal) {
@@ -153,14 +163,14 @@ __global__ void __launch_bounds__(kCqBlock) k_assemble_cart_q1(const CartQ1Latti
         const int dx = e % 3 - 1, dy = e / 3 - 1;
         const bool okxy = (dx < 0 ? xm : dx > 0 ? xp : true) && (dy < 0 ? ym : dy > 0 ? yp : true);
         const int cls = (dx ? 1 : 0) | (dy ? 2 : 0);
-        put(okxy, a.W[cls] * (lo.box(e) + up.box(e)));
+        put(okxy, ZF && (cls == 1 || cls == 2) ? 0.0 : a.W[cls] * (lo.box(e) + up.box(e)));
       }
 #pragma unroll
       for (int e = 0; e < 9; ++e) {  // dz = +1: the layer above; kept for the next plane
         const int dx = e % 3 - 1, dy = e / 3 - 1;
         const bool okxy = (dx < 0 ? xm : dx > 0 ? xp : true) && (dy < 0 ? ym : dy > 0 ? yp : true);
         const int cls = (dx ? 1 : 0) | (dy ? 2 : 0) | 4;
-        const double v = a.W[cls] * up.box(e);
+        const double v = entry(cls, up.box(e));
         carry[e] = v;
         put(zp && okxy, v);
       }
@@ -171,7 +181,7 @@ __global__ void __launch_bounds__(kCqBlock) k_assemble_cart_q1(const CartQ1Latti
 #pragma unroll
       for (int e = 0; e < 9; ++e) {
         const int cls = (e % 3 != 1 ? 1 : 0) | (e / 3 != 1 ? 2 : 0) | 4;
-        carry[e] = a.W[cls] * up.box(e);
+        carry[e] = entry(cls, up.box(e));
       }
     }
     if (a.b) {
@@ -253,14 +263,22 @@ int assemble_cartesian_q1_lattice(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem
     for (int c = 0; c < 8; ++c) m += mref[c];
     a.fscale = fc * m;
   }
-  for (int c = 0; c < 8; ++c) a.W[c] = Kref[0 + 8 * c];
+  double wmax = 0.0;
+  for (int c = 0; c < 8; ++c) {
+    a.W[c] = Kref[0 + 8 * c];
+    wmax = std::max(wmax, std::fabs(a.W[c]));
+  }
+  // cubic cells: the face-class weights vanish up to the rounding of the reference integral
+  // (|W| below 1e-13 of the largest weight), and their entries are stored as exact zeros
+  const bool zf = std::fabs(a.W[1]) <= 1e-13 * wmax && std::fabs(a.W[2]) <= 1e-13 * wmax &&
+                  std::fabs(a.W[4]) <= 1e-13 * wmax;
+  auto kern = zf ? k_assemble_cart_q1<true> : k_assemble_cart_q1<false>;
   const size_t smem = sizeof(double) * kCqStage * (kCqBlock / 32);
-  GFE_CUDA_TRY(cudaFuncSetAttribute(k_assemble_cart_q1,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  GFE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const dim3 grid((unsigned)((a.m0 + 31) / 32), (unsigned)((a.m1 + 7) / 8),
                   (unsigned)((a.m2 + kCqKZ - 1) / kCqKZ));
   timer_begin(ctx, GFE_KT_ASSEMBLE);
-  k_assemble_cart_q1<<<grid, kCqBlock, smem, ctx->stream>>>(a);
+  kern<<<grid, kCqBlock, smem, ctx->stream>>>(a);
   timer_end(ctx);
   ctx->launches++;
   GFE_CUDA_TRY(cudaGetLastError());

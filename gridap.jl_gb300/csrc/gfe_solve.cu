@@ -1519,6 +1519,75 @@ __global__ void __launch_bounds__(kVecBlock)
   for (int64_t i = 4 * n4 + tid; i < n; i += nth) p[i] = fmaf(beta, p[i], z[i]);
 }
 
+// FCG start from x = 0 over float4 groups (16-byte aligned b, x, r): x = 0, r = (float) b,
+// partial r.r (z = r: the preconditioner is applied by the caller); the state as k_cg_init
+// leaves it (r.r in FP32 per thread: it sets the stopping threshold, the final relative
+// residual takes ||b|| in FP64)
+__global__ void __launch_bounds__(kVecBlock)
+    k_fcg_init4(int64_t n, const double* __restrict__ b, float* __restrict__ x,
+                float* __restrict__ r, double* __restrict__ partials, SolverState* S,
+                double rtol2) {
+  __shared__ double sh[kVecBlock / 32];
+  float rr_t = 0.f;
+  const int64_t n4 = n >> 2;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = tid; i < n4; i += nth) {
+    const double2 b0 = __ldg(reinterpret_cast<const double2*>(b) + 2 * i);
+    const double2 b1 = __ldg(reinterpret_cast<const double2*>(b) + 2 * i + 1);
+    const float4 rv = make_float4((float)b0.x, (float)b0.y, (float)b1.x, (float)b1.y);
+    reinterpret_cast<float4*>(r)[i] = rv;
+    reinterpret_cast<float4*>(x)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    rr_t = fmaf(rv.x, rv.x, rr_t);
+    rr_t = fmaf(rv.y, rv.y, rr_t);
+    rr_t = fmaf(rv.z, rv.z, rr_t);
+    rr_t = fmaf(rv.w, rv.w, rr_t);
+  }
+  for (int64_t i = 4 * n4 + tid; i < n; i += nth) {
+    const float ri = (float)b[i];
+    r[i] = ri;
+    x[i] = 0.f;
+    rr_t = fmaf(ri, ri, rr_t);
+  }
+  const double rr = block_sum<kVecBlock>((double)rr_t, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = rr;
+  double tot[1];
+  if (last_block_reduce<kVecBlock, 1>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
+      threadIdx.x == 0) {
+    S->rz = tot[0];
+    S->rr = tot[0];
+    S->bb = tot[0];
+    S->tol2 = rtol2 * tot[0];
+    S->iter = 0;
+    S->converged = 0;
+    S->done = (tot[0] == 0.0) ? 1 : 0;
+    if (tot[0] == 0.0) S->converged = 1;
+  }
+}
+
+// x64 += x32; x32 = 0 over float4 groups (16-byte aligned x64 and x32)
+__global__ void k_merge4(int64_t n, double* __restrict__ x64, float* __restrict__ x32) {
+  const int64_t n4 = n >> 2;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = tid; i < n4; i += nth) {
+    const float4 d = reinterpret_cast<const float4*>(x32)[i];
+    double2 a0 = reinterpret_cast<double2*>(x64)[2 * i];
+    double2 a1 = reinterpret_cast<double2*>(x64)[2 * i + 1];
+    a0.x += (double)d.x;
+    a0.y += (double)d.y;
+    a1.x += (double)d.z;
+    a1.y += (double)d.w;
+    reinterpret_cast<double2*>(x64)[2 * i] = a0;
+    reinterpret_cast<double2*>(x64)[2 * i + 1] = a1;
+    reinterpret_cast<float4*>(x32)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  for (int64_t i = 4 * n4 + tid; i < n; i += nth) {
+    x64[i] += (double)x32[i];
+    x32[i] = 0.f;
+  }
+}
+
 // the condition of the device-driven FCG loop: repeat while the state is not done
 __global__ void k_fcg_continue(cudaGraphConditionalHandle h, const SolverState* S) {
   cudaGraphSetConditional(h, S->done ? 0u : 1u);
@@ -2174,8 +2243,21 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   int maxit_field = maxit;
   GFE_CUDA_TRY(cudaMemcpyAsync(&w.S->maxit, &maxit_field, sizeof(int), cudaMemcpyHostToDevice,
                                ctx->stream));
-  k_cg_init<float, double><<<gv, kVecBlock, 0, ctx->stream>>>(
-      n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
+  auto merge = [&]() {
+    if (vec4 && (reinterpret_cast<uintptr_t>(d_x) & 15) == 0)
+      k_merge4<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
+    else
+      k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
+  };
+  // b and x64 are the caller's buffers: the float4 kernels where they are 16-byte aligned
+  const bool vec4_bx = vec4 && ((reinterpret_cast<uintptr_t>(d_b) |
+                                 reinterpret_cast<uintptr_t>(d_x)) & 15) == 0;
+  if (vec4_bx && !dinv32)
+    k_fcg_init4<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, x32, r32, w.partials, w.S,
+                                                   o->rtol * o->rtol);
+  else
+    k_cg_init<float, double><<<gv, kVecBlock, 0, ctx->stream>>>(
+        n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
   k_set_reliable<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta);
   ctx->launches += 2;
   GFE_TRY(precond());
@@ -2260,7 +2342,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     }
     if (w.hS->done && (w.hS->need_update || w.hS->converged)) {
       // reliable update: x64 += x32, r64 = b - A64 x64, r32 = r64 (or stop)
-      k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
+      merge();
       timer_begin(ctx, GFE_KT_RESIDUAL64);
       residual64(&w.S->rr64);
       timer_end(ctx);
@@ -2295,7 +2377,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   }
   // any FP32 correction not yet absorbed (none when the loop ended on a reliable update)
   if (!fresh) {
-    k_merge<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
+    merge();
     ctx->launches++;
   }
   rep->iterations = w.hS->iter;

@@ -8,12 +8,13 @@
 // the reference stiffness doubles (a Q1 stiffness on a box of sizes 2h is twice the one on h,
 // in 3-D), which for piecewise-constant kappa equals the Galerkin product P^T A P of the
 // nested Q1 spaces. Transfers are trilinear interpolation P and its transpose R = P^T (full
-// weighting 1, 1/2, 1/4, 1/8). Smoothing is damped Jacobi (omega 0.8, two sweeps before and
+// weighting 1, 1/2, 1/4, 1/8). Smoothing is Chebyshev-paired damped Jacobi (two sweeps before and
 // after, the first from zero), each later sweep fused into one pass over the lattice stencil;
 // the coarsest level takes five sweeps. Levels of at most 512 rows run their part of the
 // cycle in one block, out of shared memory. All vectors are FP32 in the lattice row order;
-// every kernel returns at once when the solver's done flag is set. The cycle is captured once
-// as a CUDA graph whose kernels are chained by programmatic dependent launch.
+// every kernel returns at once when the solver's done flag is set. The cycle's kernels are
+// chained by programmatic dependent launch; the solver records them into its own loop graph,
+// or replays the cycle as a graph captured once.
 #include <utility>
 #include <vector>
 
@@ -25,7 +26,46 @@ namespace gfe {
 namespace {
 
 constexpr int kMgBlock = 256;
-constexpr float kOmega = 0.8f;
+// Smoothing runs in pairs of damped Jacobi sweeps whose factors are the reciprocals of the
+// roots of the degree-2 Chebyshev polynomial on [kChebLo B, kChebHi B]: the pair's error
+// polynomial (1 - w1 l)(1 - w2 l) is the minimax one of degree 2 on that interval. B bounds the
+// spectrum of D^-1 A for every kappa >= 0: x^T A x = sum_K kappa_K x_K^T Kref x_K <=
+// lmax(Kref) sum_K kappa_K |x_K|^2 = (lmax(Kref) / Kref_00) x^T D x, so B = lmax(Kref) / Kref_00,
+// 1.5 on cubes (the high-frequency modes of the constant-coefficient stencil span 0.5 .. 1.5)
+// and larger on elongated boxes; on [0, B] the pair's factor is at most 1 in magnitude.
+// Every level shares B (coarsening halves every axis and doubles Kref). On the 128^3
+// lognormal problem the flexible CG needs 7 iterations with these pairs against 8 with damped
+// Jacobi (omega 0.8 or 1).
+constexpr float kChebLo = 0.4f / 1.5f, kChebHi = 1.6f / 1.5f;
+
+// the two factors of the pair for the spectral bound B
+struct SweepPair {
+  float w1, w2;
+  __host__ __device__ float at(int s) const { return (s & 1) ? w2 : w1; }  // sweep s (0 first)
+};
+SweepPair sweep_pair(double B) {
+  const double lo = kChebLo * B, hi = kChebHi * B;
+  const double th = 0.5 * (hi + lo), de = 0.5 * (hi - lo) * 0.70710678118654752;
+  return SweepPair{(float)(1.0 / (th + de)), (float)(1.0 / (th - de))};
+}
+
+// B = lmax(Kref) / Kref_00 of a box Q1 stiffness (Kref[li + 8 lj]): its eigenvectors are the
+// 8 tensor-product sign patterns over the vertices
+double stiffness_spectral_bound(const float* K) {
+  double best = 0.0;
+  for (int s = 0; s < 8; ++s) {
+    double v[8], q = 0.0;
+    for (int a = 0; a < 8; ++a) {
+      v[a] = 1.0;
+      for (int d = 0; d < 3; ++d)
+        if (((s >> d) & 1) && ((a >> d) & 1)) v[a] = -v[a];
+    }
+    for (int a = 0; a < 8; ++a)
+      for (int b = 0; b < 8; ++b) q += v[a] * (double)K[a + 8 * b] * v[b];
+    best = std::max(best, q / 8.0);
+  }
+  return K[0] > 0.f ? best / (double)K[0] : 2.0;
+}
 constexpr int kPreSweeps = 2, kPostSweeps = 2, kCoarseSweeps = 4;
 // On deep lattices (the march of kLatK planes per thread) the first sweep from zero runs as a
 // pass of its own followed by a plain sweep: the fused pass, which forms omega D^-1 b at every
@@ -59,32 +99,33 @@ cudaError_t launch_pdl(void (*kern)(P...), dim3 grid, int block, size_t smem, cu
   return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
 }
 
-// One damped Jacobi sweep fused into the lattice apply: xo = x + omega D^-1 (b - A x)
+// One damped Jacobi sweep fused into the lattice apply: xo = x + w D^-1 (b - A x)
 // (xo != x: the sweep reads the old neighbours). Same arithmetic as an apply into t followed
 // by the update x += omega D^-1 (b - t).
 template <int KZ>
 __global__ void __launch_bounds__(kMgBlock)
     k_mg_smooth(LatticeQ1Op op, const float* __restrict__ x, const float* __restrict__ b,
-                const float* __restrict__ dinv, float* __restrict__ xo, const int* done) {
+                const float* __restrict__ dinv, float* __restrict__ xo, float w,
+                const int* done) {
   if (stop(done)) return;
   auto epi = [&](int64_t row, float xc, float acc) {
-    xo[row] = fmaf(kOmega * __ldg(dinv + row), __ldg(b + row) - acc, xc);
+    xo[row] = fmaf(w * __ldg(dinv + row), __ldg(b + row) - acc, xc);
   };
   lattice_rows<false, decltype(epi), KZ>(op, (int)blockIdx.x, (int)blockIdx.y,
                                          (int)blockIdx.z, x, epi);
 }
 
-// The first two sweeps in one pass: x0 = omega D^-1 b (the sweep from zero, formed on the fly
-// at the neighbours) and xo = x0 + omega D^-1 (b - A x0). x0 itself is not stored: the cycle
-// reads only xo afterwards.
+// The first two sweeps in one pass: x0 = w0 D^-1 b (the sweep from zero, formed on the fly at
+// the neighbours) and xo = x0 + w1 D^-1 (b - A x0). x0 itself is not stored: the cycle reads
+// only xo afterwards.
 template <int KZ>
 __global__ void __launch_bounds__(kMgBlock)
     k_mg_pre(LatticeQ1Op op, const float* __restrict__ b, const float* __restrict__ dinv,
-             float* __restrict__ xo, const int* done) {
+             float* __restrict__ xo, float w0, float w1, const int* done) {
   if (stop(done)) return;
-  const LatticeLoadJacobi0 x0{b, dinv, kOmega};
+  const LatticeLoadJacobi0 x0{b, dinv, w0};
   auto epi = [&](int64_t row, float xc, float acc) {
-    xo[row] = fmaf(kOmega * __ldg(dinv + row), __ldg(b + row) - acc, xc);
+    xo[row] = fmaf(w1 * __ldg(dinv + row), __ldg(b + row) - acc, xc);
   };
   lattice_rows_f<false, decltype(epi), KZ>(op, (int)blockIdx.x, (int)blockIdx.y,
                                            (int)blockIdx.z, x0, epi);
@@ -101,14 +142,14 @@ __global__ void __launch_bounds__(kMgBlock)
                                          (int)blockIdx.z, x, epi);
 }
 
-// x = omega D^-1 b  (first sweep from zero)
+// x = w D^-1 b  (first sweep from zero)
 __global__ void k_mg_jacobi0(int64_t n, const float* __restrict__ b,
-                             const float* __restrict__ dinv, float* __restrict__ x,
+                             const float* __restrict__ dinv, float* __restrict__ x, float w,
                              const int* done) {
   if (stop(done)) return;
   for (int64_t i = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kMgBlock)
-    x[i] = kOmega * dinv[i] * b[i];
+    x[i] = w * dinv[i] * b[i];
 }
 
 // b_c = R r_f: coarse interior node (I, J, K) sits on fine interior node (2I+1, 2J+1, 2K+1);
@@ -270,6 +311,7 @@ struct MgCoarseLevel {
 
 struct CoarseLevels {
   int nl;
+  SweepPair w;      // smoothing factors
   int floats;       // shared buffer size
   const float* b0;  // b of the first level
   float* x0;        // its result
@@ -370,12 +412,12 @@ __global__ void __launch_bounds__(kCoarseBlock)
       f(r, (i + 1) + L.q0 * (j + 1) + L.q1 * (k + 1), i, j, k);
     }
   };
-  auto sweep = [&](const MgCoarseLevel& L, int xi, int xo) {
+  auto sweep = [&](const MgCoarseLevel& L, int xi, int xo, float w) {
     float* out = sm + xo;
     const float* b = sm + L.b;
     const float* dv = sm + L.dinv;
     coarse_rows(L, sm, sm + xi, [&](int r, int pr, float xc, float acc) {
-      out[pr] = fmaf(kOmega * dv[r], b[r] - acc, xc);
+      out[pr] = fmaf(w * dv[r], b[r] - acc, xc);
     });
     __syncthreads();
   };
@@ -383,17 +425,17 @@ __global__ void __launch_bounds__(kCoarseBlock)
   for (int l = 0; l < c.nl; ++l) {
     const MgCoarseLevel& L = c.L[l];
     rows(L, [&](int r, int pr, int, int, int) {  // the sweep from zero
-      sm[L.x + pr] = kOmega * sm[L.dinv + r] * sm[L.b + r];
+      sm[L.x + pr] = c.w.at(0) * sm[L.dinv + r] * sm[L.b + r];
     });
     __syncthreads();
     if (l + 1 == c.nl) {  // coarsest: four more sweeps, ending in x
       for (int s = 0; s < kCoarseSweeps; s += 2) {
-        sweep(L, L.x, L.t);
-        sweep(L, L.t, L.x);
+        sweep(L, L.x, L.t, c.w.at(s + 1));
+        sweep(L, L.t, L.x, c.w.at(s + 2));
       }
       break;
     }
-    sweep(L, L.x, L.t);
+    sweep(L, L.x, L.t, c.w.at(1));
     {  // residual into x
       float* out = sm + L.x;
       const float* b = sm + L.b;
@@ -429,8 +471,8 @@ __global__ void __launch_bounds__(kCoarseBlock)
       sm[L.x + pr] = fmaf(0.125f, v0 + v1, sm[L.t + pr]);
     });
     __syncthreads();
-    sweep(L, L.x, L.t);
-    sweep(L, L.t, L.x);
+    sweep(L, L.x, L.t, c.w.at(0));
+    sweep(L, L.t, L.x, c.w.at(1));
   }
   const MgCoarseLevel& L0 = c.L[0];
   rows(L0, [&](int r, int pr, int, int, int) { c.x0[r] = sm[L0.x + pr]; });
@@ -455,6 +497,7 @@ struct LatticeMG {
   const int* cap_done = nullptr;
   long long nodes = 0;
   gfe_learned_pc* learned = nullptr;  // the fine level's smoother when set
+  SweepPair w{0.8f, 0.8f};             // smoothing factors of every level
   explicit LatticeMG(gfe_ctx* c) : ctx(c), buf(c) {}
   ~LatticeMG() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -506,6 +549,7 @@ CoarseLevels coarse_levels(const LatticeMG* mg, size_t l) {
     S.gdinv = Q.dinv;
   }
   c.floats = off;
+  c.w = mg->w;
   c.b0 = mg->lv[l].b;
   c.x0 = mg->lv[l].x;
   return c;
@@ -536,13 +580,13 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
   // lattices too small for 4 blocks per SM march one k-plane per thread
   const bool deep = (int64_t)ga.x * ga.y * ga.z >= 4 * (int64_t)ctx->num_sms;
   const dim3 ga1 = L.op.grid_k(1);
-  auto smooth = [&](const float* xi, float* xo) -> int {
+  auto smooth = [&](const float* xi, float* xo, float w) -> int {
     if (deep)
       GFE_CUDA_TRY(launch_pdl(k_mg_smooth<kLatK>, ga, kMgBlock, 0, st, L.op, xi, L.b, L.dinv,
-                              xo, done));
+                              xo, w, done));
     else
       GFE_CUDA_TRY(launch_pdl(k_mg_smooth<1>, ga1, kMgBlock, 0, st, L.op, xi, L.b, L.dinv,
-                              xo, done));
+                              xo, w, done));
     ctx->launches++;
     return GFE_OK;
   };
@@ -592,18 +636,18 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
   if (fuse_pre) {  // the sweep from zero and the next one in one pass
     if (deep)
       GFE_CUDA_TRY(launch_pdl(k_mg_pre<kLatK>, ga, kMgBlock, 0, st, L.op, (const float*)L.b,
-                              (const float*)L.dinv, oth, done));
+                              (const float*)L.dinv, oth, mg->w.at(0), mg->w.at(1), done));
     else
       GFE_CUDA_TRY(launch_pdl(k_mg_pre<1>, ga1, kMgBlock, 0, st, L.op, (const float*)L.b,
-                              (const float*)L.dinv, oth, done));
+                              (const float*)L.dinv, oth, mg->w.at(0), mg->w.at(1), done));
     std::swap(cur, oth);
   } else {
     GFE_CUDA_TRY(launch_pdl(k_mg_jacobi0, dim3(g), kMgBlock, 0, st, L.n, (const float*)L.b,
-                            (const float*)L.dinv, cur, done));
+                            (const float*)L.dinv, cur, mg->w.at(0), done));
   }
   ctx->launches++;
   for (int s = fuse_pre ? 2 : 1; s < pre; ++s) {
-    GFE_TRY(smooth(cur, oth));
+    GFE_TRY(smooth(cur, oth, mg->w.at(s)));
     std::swap(cur, oth);
   }
   if (coarsest) return cur == L.x ? GFE_OK
@@ -619,7 +663,7 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
   cur = post0;
   oth = post0 == L.x ? L.t : L.x;
   for (int s = 0; s < kPostSweeps; ++s) {
-    GFE_TRY(smooth(cur, oth));
+    GFE_TRY(smooth(cur, oth, mg->w.at(s)));
     std::swap(cur, oth);
   }
   return cur == L.x ? GFE_OK : set_error(GFE_ERR_UNSUPPORTED, "multigrid: sweep parity");
@@ -631,6 +675,7 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
 int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out) {
   LatticeMG* mg = new LatticeMG(ctx);
   *out = mg;
+  mg->w = sweep_pair(stiffness_spectral_bound(fine.K));
   std::vector<LatticeQ1Op> ops{fine};
   while (ops.size() < 12) {
     const LatticeQ1Op& f = ops.back();

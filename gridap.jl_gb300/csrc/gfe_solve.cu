@@ -42,6 +42,8 @@ struct SolverState {
   int iter, done, converged, maxit;
   int need_update;
   unsigned ticket[4];
+  int defer_update;  // flexible CG in the device loop: a due reliable update does not stop it
+  int updates;       // reliable updates made by the device loop
 };
 
 __device__ __forceinline__ void raise_e(DevError* err, int code, long long index) {
@@ -1280,13 +1282,17 @@ __global__ void __launch_bounds__(kVecBlock)
     if (!isfinite(tot[0])) {
       S->done = 1;
     } else if (tot[0] <= S->tol2) {
-      S->done = 1;
-      S->converged = 1;
+      if (S->defer_update) {  // the FP64 residual decides (the loop's reliable update)
+        S->need_update = 1;
+      } else {
+        S->done = 1;
+        S->converged = 1;
+      }
     } else if (S->iter >= S->maxit) {
       S->done = 1;
     } else if (S->delta2 > 0.0 && tot[0] < S->delta2 * S->rmax2) {
-      S->done = 1;
       S->need_update = 1;
+      if (!S->defer_update) S->done = 1;
     }
   }
 }
@@ -1366,6 +1372,7 @@ __global__ void k_fcg_restart(int64_t n, const double* __restrict__ r64, float* 
     r32[i] = (float)r64[i];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     S->need_update = 0;
+    S->updates += 1;
     if (conv) {
       S->converged = 1;
       S->done = 1;
@@ -1438,13 +1445,17 @@ __global__ void __launch_bounds__(kVecBlock)
     if (!isfinite(tot[0])) {
       S->done = 1;
     } else if (tot[0] <= S->tol2) {
-      S->done = 1;
-      S->converged = 1;
+      if (S->defer_update) {  // the FP64 residual decides (the loop's reliable update)
+        S->need_update = 1;
+      } else {
+        S->done = 1;
+        S->converged = 1;
+      }
     } else if (S->iter >= S->maxit) {
       S->done = 1;
     } else if (S->delta2 > 0.0 && tot[0] < S->delta2 * S->rmax2) {
-      S->done = 1;
       S->need_update = 1;
+      if (!S->defer_update) S->done = 1;
     }
   }
 }
@@ -1592,6 +1603,13 @@ __global__ void k_merge4(int64_t n, double* __restrict__ x64, float* __restrict_
 __global__ void k_fcg_continue(cudaGraphConditionalHandle h, const SolverState* S) {
   cudaGraphSetConditional(h, S->done ? 0u : 1u);
 }
+
+// the condition of the loop's reliable update: due after this iteration's update
+__global__ void k_fcg_if_update(cudaGraphConditionalHandle h, const SolverState* S) {
+  cudaGraphSetConditional(h, S->need_update && !S->done ? 1u : 0u);
+}
+
+__global__ void k_set_defer(SolverState* S) { S->defer_update = 1; }
 
 // ---- host drivers -------------------------------------------------------------------------
 struct SolverWork {
@@ -2260,6 +2278,11 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
         n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
   k_set_reliable<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta);
   ctx->launches += 2;
+  if (device_loop) {  // ||b||^2 in FP64 for the relative residual, ahead of the loop
+    k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb,
+                                                  &w.S->ticket[1]);
+    ctx->launches++;
+  }
   GFE_TRY(precond());
   GFE_CUDA_TRY(cudaMemcpyAsync(p32, z32, sizeof(float) * n, cudaMemcpyDeviceToDevice,
                                ctx->stream));
@@ -2271,11 +2294,15 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       if (e) cudaGraphExecDestroy(e);
     }
   } loop;
-  long long body_launches = 0;
+  long long body_launches = 0, if_launches = 0, if_counted = 0;
   if (device_loop) {
+    // WHILE (not done) { update; IF (reliable update due) { x64 += x32; r64 = b - A x64;
+    // r32 = r64 or stop }; preconditioner; beta; direction; SpMV }: the reliable updates run
+    // inside the loop too, so that the host waits once per solve. The IF node is added to the
+    // body in the middle of its capture, and its own body captured on a second stream.
     cudaGraph_t g = nullptr;
     bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
-    cudaGraphConditionalHandle h{};
+    cudaGraphConditionalHandle h{}, hif{};
     cudaGraphNodeParams np = {};
     cudaGraphNode_t node;
     ok = ok && cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) ==
@@ -2285,27 +2312,70 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     np.conditional.type = cudaGraphCondTypeWhile;
     np.conditional.size = 1;
     ok = ok && cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
-    if (ok && cudaStreamBeginCaptureToGraph(ctx->stream, np.conditional.phGraph_out[0], nullptr,
-                                            nullptr, 0,
+    cudaGraph_t body = ok ? np.conditional.phGraph_out[0] : nullptr;
+    ok = ok && cudaGraphConditionalHandleCreate(&hif, body, 0, 0) == cudaSuccess;
+    cudaStream_t s2 = nullptr;
+    ok = ok && cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok && cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
                                             cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const long long l0 = ctx->launches;
       fcg_update();
+      k_fcg_if_update<<<1, 1, 0, ctx->stream>>>(hif, w.S);
+      // the IF node after the captured work so far
+      cudaStreamCaptureStatus cs;
+      cudaGraph_t cg = nullptr;
+      const cudaGraphNode_t* deps = nullptr;
+      const cudaGraphEdgeData* ed = nullptr;
+      size_t nd = 0;
+      cudaGraphNodeParams ip = {};
+      cudaGraphNode_t ifnode = nullptr;
+      bool okif = cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &cg, &deps, &ed, &nd) ==
+                  cudaSuccess;
+      ip.type = cudaGraphNodeTypeConditional;
+      ip.conditional.handle = hif;
+      ip.conditional.type = cudaGraphCondTypeIf;
+      ip.conditional.size = 1;
+      okif = okif && cudaGraphAddNode(&ifnode, cg, deps, ed, nd, &ip) == cudaSuccess;
+      if (okif && cudaStreamBeginCaptureToGraph(s2, ip.conditional.phGraph_out[0], nullptr,
+                                                nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal) ==
+                      cudaSuccess) {
+        cudaStream_t main = ctx->stream;
+        ctx->stream = s2;  // the reliable update's launches go to the IF body
+        const long long li = ctx->launches;
+        merge();
+        residual64(&w.S->rr64);
+        k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, w.S);
+        if_counted = ctx->launches - li;
+        if_launches = if_counted + 2;  // merge and restart are not counted by their lambdas
+        ctx->stream = main;
+        cudaGraph_t ifb = nullptr;
+        okif = cudaStreamEndCapture(s2, &ifb) == cudaSuccess;
+      } else {
+        okif = false;
+      }
+      okif = okif && cudaStreamUpdateCaptureDependencies(ctx->stream, &ifnode, nullptr, 1,
+                                                         cudaStreamSetCaptureDependencies) ==
+                         cudaSuccess;
       const int st = precond();
       fcg_beta_dir();
       spmv();
       k_fcg_continue<<<1, 1, 0, ctx->stream>>>(h, w.S);
-      body_launches = ctx->launches - l0 + 4;
+      // + update, IF condition, beta, direction and WHILE condition
+      body_launches = ctx->launches - l0 - if_counted + 5;
       ctx->launches = l0;
-      cudaGraph_t body = nullptr;
-      const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &body);
+      cudaGraph_t bodyg = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &bodyg);
       if (st != GFE_OK) {
         if (g) cudaGraphDestroy(g);
+        if (s2) cudaStreamDestroy(s2);
         return st;
       }
-      ok = ce == cudaSuccess && cudaGraphInstantiate(&loop.e, g, 0) == cudaSuccess;
+      ok = okif && ce == cudaSuccess && cudaGraphInstantiate(&loop.e, g, 0) == cudaSuccess;
     } else {
       ok = false;
     }
+    if (s2) cudaStreamDestroy(s2);
     if (g) cudaGraphDestroy(g);
     if (!ok) {
       // conditional graphs unavailable: the host-driven loop below (direct launches)
@@ -2314,32 +2384,36 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       loop.e = nullptr;
     }
   }
-  GFE_TRY(read_state(ctx, w));
   int updates = 0, slow = 0, fallback = 0;
-  double rr_chunk = w.hS->rr;
   bool fresh = false;  // the loop ended on a reliable update: x64 and rr64 are current
-  while (!w.hS->done) {
-    if (loop.e) {
-      const int it0 = w.hS->iter;
-      GFE_CUDA_TRY(cudaGraphLaunch(loop.e, ctx->stream));
-      GFE_TRY(read_state(ctx, w));
-      ctx->launches += (long long)(w.hS->iter - it0) * body_launches;
-    } else {
-      for (int k = 0; k < check_every; ++k) {
-        timer_begin(ctx, GFE_KT_VECTOR);
-        fcg_update();
-        timer_end(ctx);
-        ctx->launches++;
-        GFE_TRY(precond());
-        timer_begin(ctx, GFE_KT_VECTOR);
-        fcg_beta_dir();
-        timer_end(ctx);
-        ctx->launches += 2;
-        spmv();
-      }
-      GFE_CUDA_TRY(cudaGetLastError());
-      GFE_TRY(read_state(ctx, w));
+  if (loop.e) {
+    // the whole iteration, reliable updates included, on the device: one wait
+    k_set_defer<<<1, 1, 0, ctx->stream>>>(w.S);
+    GFE_CUDA_TRY(cudaGraphLaunch(loop.e, ctx->stream));
+    GFE_TRY(read_state(ctx, w));
+    updates = w.hS->updates;
+    fresh = w.hS->converged != 0;  // only the loop's reliable update declares convergence
+    ctx->launches += 1 + (long long)w.hS->iter * body_launches + (long long)updates * if_launches;
+  } else {
+    // host-driven loop (kernel timing, the learned preconditioner, no conditional graphs)
+    GFE_TRY(read_state(ctx, w));
+  }
+  double rr_chunk = w.hS->rr;
+  while (!loop.e && !w.hS->done) {
+    for (int k = 0; k < check_every; ++k) {
+      timer_begin(ctx, GFE_KT_VECTOR);
+      fcg_update();
+      timer_end(ctx);
+      ctx->launches++;
+      GFE_TRY(precond());
+      timer_begin(ctx, GFE_KT_VECTOR);
+      fcg_beta_dir();
+      timer_end(ctx);
+      ctx->launches += 2;
+      spmv();
     }
+    GFE_CUDA_TRY(cudaGetLastError());
+    GFE_TRY(read_state(ctx, w));
     if (w.hS->done && (w.hS->need_update || w.hS->converged)) {
       // reliable update: x64 += x32, r64 = b - A64 x64, r32 = r64 (or stop)
       merge();
@@ -2390,10 +2464,13 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     residual64(&w.S->rr);
     ctx->launches++;
   }
-  k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb, &w.S->ticket[1]);
-  ctx->launches++;
+  if (!device_loop) {  // (the device loop formed ||b||^2 ahead of it)
+    k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb,
+                                                  &w.S->ticket[1]);
+    ctx->launches++;
+  }
   GFE_CUDA_TRY(cudaGetLastError());
-  GFE_TRY(read_state(ctx, w));
+  if (!(loop.e && fresh)) GFE_TRY(read_state(ctx, w));
   const double bb = w.hS->bb;
   const double rr = fresh ? w.hS->rr64 : w.hS->rr;
   rep->relres = bb > 0 ? std::sqrt(rr / bb) : 0.0;

@@ -260,6 +260,7 @@ extern "C" int gfe_matrix_export_csr(gfe_matrix* A, int index_base, int64_t* row
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_matrix_export_csr: bad arguments");
   gfe_ctx* ctx = A->ctx;
   DeviceGuard g(ctx->device);
+  GFE_TRY(ensure_values(ctx, A));
   auto widen = [&](const int32_t* src, int64_t n, int64_t* dst) -> int {
     if (!dst || n == 0) return GFE_OK;
     const bool dev = is_device_ptr(dst);
@@ -287,6 +288,7 @@ extern "C" int gfe_matrix_fillstored_zero(gfe_matrix* A) {
   DeviceGuard g(A->ctx->device);
   if (A->nnz)
     GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * A->nnz, A->ctx->stream));
+  A->val_pending = false;
   A->plan_valid = false;
   A->dia_checked = false;
   A->mf_state = 0;
@@ -300,6 +302,7 @@ extern "C" int gfe_numeric_loop_matrix(gfe_ctx* ctx, gfe_matrix* A, const double
   if (!ctx || !A || (A->ncells > 0 && !cellmats) || A->ctx != ctx)
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_numeric_loop_matrix: bad arguments");
   DeviceGuard g(ctx->device);
+  GFE_TRY(ensure_values(ctx, A));
   const void* d;
   GFE_TRY(device_view(ctx, cellmats, sizeof(double) * (size_t)A->ncells * A->nd * A->cols_per_cell(),
                       SCR_CELLMAT, &d));
@@ -394,6 +397,7 @@ extern "C" int gfe_solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* opt
   if (!(opts->rtol > 0.0))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_solve: rtol must be positive");
   DeviceGuard g(ctx->device);
+  GFE_TRY(ensure_values(ctx, A));
   const size_t n8 = sizeof(double) * (size_t)A->nrows;
   const void* db;
   GFE_TRY(device_view(ctx, b, n8, SCR_VEC_B, &db));
@@ -419,6 +423,7 @@ extern "C" int gfe_matrix_mul(gfe_ctx* ctx, gfe_matrix* A, const double* x, doub
   if (!ctx || !A || !x || !y || A->ctx != ctx)
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_matrix_mul: bad arguments");
   DeviceGuard g(ctx->device);
+  GFE_TRY(ensure_values(ctx, A));
   const void* dx;
   GFE_TRY(device_view(ctx, x, sizeof(double) * (size_t)A->ncols, SCR_TMP2, &dx));
   const bool ydev = is_device_ptr(y);

@@ -504,6 +504,13 @@ __global__ void __launch_bounds__(256)
 
 // ---- host: fused integrate + assemble -----------------------------------------------------
 int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* d_b) {
+  // the values of a closed-form Cartesian pattern are zeroed lazily: only the class-sum
+  // kernel, which writes every entry, may find them pending
+  const bool lattice_candidate = A && A->val_pending && p->dim == 3 &&
+                                 p->reffe == GFE_REFFE_Q1 && p->ncomp == 1 &&
+                                 p->form == GFE_FORM_DIFFUSION &&
+                                 p->geometry == GFE_GEOM_CARTESIAN;
+  if (!lattice_candidate) GFE_TRY(ensure_values(ctx, A));
   if (p->reffe == GFE_REFFE_P2_TET) return assemble_p2_elasticity(ctx, p, A, d_b);
   if (p->form == GFE_FORM_QUASILINEAR) return assemble_quasilinear(ctx, p, A, d_b);
   const int D = p->dim;
@@ -725,9 +732,17 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
     }
     // the closed-form lattice pattern of this grid: the class-sum kernel
     bool lattice_done = false;
-    if (A && D == 3 && !cn)
+    if (A && D == 3 && !cn) {
+      // the coefficient and source checks report before the class-sum kernel, which raises
+      // no device errors itself: the call then returns without waiting for it
+      GFE_TRY(check_device_error(ctx, "assemble_matrix_and_vector"));
       GFE_TRY(assemble_cartesian_q1_lattice(ctx, A, p, d_coef, src_kind, d_src, tabs.data(),
                                             tabs.data() + 2 * nv * nv, d_b, &lattice_done));
+    }
+    if (lattice_done)
+      A->val_pending = false;
+    else
+      GFE_TRY(ensure_values(ctx, A));
     if (!lattice_done) GFE_TRY(ensure_row_refs(ctx, R));
     RowArgs a = row_args(ctx, R, d_b, A != nullptr);
     if (!A) a.rowptr = nullptr;
@@ -757,6 +772,10 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
     else GFE_CART(3, true)
 #undef GFE_CART
     if (A && D == 3) GFE_TRY(attach_lattice_operator(ctx, A, p, d_coef, tabs.data()));
+    if (lattice_done) {
+      GFE_CUDA_TRY(cudaGetLastError());
+      return GFE_OK;
+    }
   } else {
     // nodal geometry: element kernel into entry-major scratch, then the row gather
     if (!p->node_coords || !p->cell_node_ids)

@@ -93,6 +93,14 @@ int copy_out(gfe_ctx* ctx, void* dst, const void* src, size_t n) {
   return GFE_OK;
 }
 
+int ensure_values(gfe_ctx* ctx, gfe_matrix* A) {
+  if (!A || !A->val_pending) return GFE_OK;
+  if (A->nnz > 0)
+    GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * (size_t)A->nnz, ctx->stream));
+  A->val_pending = false;
+  return GFE_OK;
+}
+
 int check_device_error(gfe_ctx* ctx, const char* where) {
   DevError h;
   GFE_CUDA_TRY(cudaMemcpyAsync(&h, ctx->d_err, sizeof(DevError), cudaMemcpyDeviceToHost,

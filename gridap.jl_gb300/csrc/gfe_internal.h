@@ -141,6 +141,9 @@ struct gfe_matrix {
   gfe::DevBuf cell_rows, cell_cols;
   // the column ids are the row ids (square cells given the same array): cell_cols stays empty
   bool cols_alias = false;
+  // values not yet zeroed (the closed-form Cartesian pattern defers it: the class-sum
+  // assembly writes every entry); ensure_values zeroes them before any other use
+  bool val_pending = false;
   const int32_t* col_ids() const {
     return cols_alias ? cell_rows.as<int32_t>() : cell_cols.as<int32_t>();
   }
@@ -267,6 +270,8 @@ int device_view(gfe_ctx* ctx, const void* p, size_t n, int slot, const void** ou
 int copy_out(gfe_ctx* ctx, void* dst, const void* src, size_t n);
 // Reads and resets the device error word; returns its code (GFE_OK if none).
 int check_device_error(gfe_ctx* ctx, const char* where);
+// zeroes A's values when their zeroing was deferred (val_pending)
+int ensure_values(gfe_ctx* ctx, gfe_matrix* A);
 
 inline unsigned grid_for(int64_t n, int block, int64_t cap = 1 << 30) {
   int64_t g = (n + block - 1) / block;

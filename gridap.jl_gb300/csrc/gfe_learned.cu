@@ -707,6 +707,7 @@ extern "C" int gfe_solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc,
   clear_error();
   if (!ctx || !A || !opts || !b || !x || A->ctx != ctx || (pc && pc->ndofs != A->nrows))
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_solve_fcg: bad arguments");
+  GFE_TRY(ensure_values(ctx, A));
   const size_t n8 = sizeof(double) * (size_t)A->nrows;
   const void* db;
   GFE_TRY(device_view(ctx, b, n8, SCR_VEC_B, &db));
@@ -734,6 +735,7 @@ extern "C" int gfe_learned_pc_samples(gfe_learned_pc* pc, gfe_matrix* A, const d
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_learned_pc_samples: bad arguments");
   gfe_ctx* ctx = pc->ctx;
   if (nsamples == 0) return GFE_OK;
+  GFE_TRY(ensure_values(ctx, A));
   const void *dr, *dids;
   GFE_TRY(device_view(ctx, r, sizeof(double) * pc->ndofs, SCR_TMP2, &dr));
   GFE_TRY(device_view(ctx, block_ids, sizeof(int64_t) * nsamples, SCR_TMP3, &dids));

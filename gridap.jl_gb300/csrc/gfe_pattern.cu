@@ -812,6 +812,9 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
       n0 * n1 * n2 * 8 > (int64_t)INT32_MAX)
     return GFE_OK;
   const int64_t nrows = A->nrows, ncells = A->ncells;
+  auto axis = [](int64_t m) { return m == 1 ? (int64_t)1 : 3 * m - 2; };
+  const int64_t nnz = axis(m0) * axis(m1) * axis(m2);
+  if (nnz > (int64_t)INT32_MAX - 64) return GFE_OK;  // the general loop reports it
   DevBuf flag(ctx);
   GFE_TRY(flag.reserve(sizeof(int)));
   GFE_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
@@ -819,31 +822,38 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
       A->cell_rows.as<int32_t>(), A->col_ids(), (int)n0, (int)n1, (int)n2,
       flag.as<int>());
   ctx->launches++;
-  int bad = 1;
-  GFE_TRY(copy_out(ctx, &bad, flag.ptr, sizeof(int)));
-  if (bad) return GFE_OK;
-  auto axis = [](int64_t m) { return m == 1 ? (int64_t)1 : 3 * m - 2; };
-  const int64_t nnz = axis(m0) * axis(m1) * axis(m2);
-  if (nnz > (int64_t)INT32_MAX - 64)
-    return set_error(GFE_ERR_UNSUPPORTED, "symbolic_loop_matrix: nnz %lld exceeds int32",
-                     (long long)nnz);
-  A->nrefs = 8 * nrows;
-  A->nnz = nnz;
-  A->max_width = (int)((m0 < 3 ? m0 : 3) * (m1 < 3 ? m1 : 3) * (m2 < 3 ? m2 : 3));
-  A->pos_bytes = 1;
+  // the check's verdict comes back through pinned memory on an event, while the closed-form
+  // row pointers and columns are built behind it (discarded, and rebuilt by the general loop,
+  // when the ids are not the interior numbering)
+  int* hflag = reinterpret_cast<int*>(static_cast<char*>(ctx->h_pinned) + 3072);
+  *hflag = 1;
+  GFE_CUDA_TRY(cudaMemcpyAsync(hflag, flag.ptr, sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  cudaEvent_t verdict;
+  GFE_CUDA_TRY(cudaEventCreateWithFlags(&verdict, cudaEventDisableTiming));
+  struct EventRelease {
+    cudaEvent_t e;
+    ~EventRelease() { cudaEventDestroy(e); }
+  } verdict_release{verdict};
+  GFE_CUDA_TRY(cudaEventRecord(verdict, ctx->stream));
   GFE_TRY(A->rowptr.reserve(sizeof(int32_t) * (nrows + 1)));
   GFE_TRY(A->colval.reserve(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
   GFE_TRY(A->val.reserve(sizeof(double) * (nnz > 0 ? nnz : 1)));
-  // the row references and positions are written when a row gather first needs them
-  // (ensure_row_refs); the class-sum assembly of this pattern does not read them
-  A->refs_pending = true;
   k_cart_rowptr<<<grid_for(nrows + 1, 256, (int64_t)ctx->num_sms * 16), 256, 0, ctx->stream>>>(
       nrows, (int)m0, (int)m1, (int)m2, A->rowptr.as<int32_t>());
   k_cart_cols<<<(unsigned)(ctx->num_sms * 4), 256, 0, ctx->stream>>>(
       (int)m0, (int)m1, (int)m2, A->rowptr.as<int32_t>(), A->colval.as<int32_t>());
   ctx->launches += 2;
-  GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * (nnz > 0 ? nnz : 1),
-                               ctx->stream));
+  GFE_CUDA_TRY(cudaEventSynchronize(verdict));
+  if (*hflag) return GFE_OK;
+  A->nrefs = 8 * nrows;
+  A->nnz = nnz;
+  A->max_width = (int)((m0 < 3 ? m0 : 3) * (m1 < 3 ? m1 : 3) * (m2 < 3 ? m2 : 3));
+  A->pos_bytes = 1;
+  // the row references and positions are written when a row gather first needs them
+  // (ensure_row_refs); the class-sum assembly of this pattern does not read them
+  A->refs_pending = true;
+  A->val_pending = true;  // zeroed on first use unless the class-sum assembly writes them all
   GFE_CUDA_TRY(cudaGetLastError());
   A->plan_valid = false;
   A->cart_lattice = true;

@@ -62,6 +62,7 @@ extern "C" int gfe_ctx_destroy(gfe_ctx* c) {
   DeviceGuard g(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
+  gfe::fcg_cache_release(c);
   for (auto& s : c->scratch) s.release();
   timer_release(c);
   if (c->stream) cudaStreamSynchronize(c->stream);

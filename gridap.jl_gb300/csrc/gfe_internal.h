@@ -83,6 +83,8 @@ struct DevBuf {
 
 // ---- context ------------------------------------------------------------------------------
 struct ScratchSlot;
+struct FcgLoopCache;  // the flexible CG's device loop and multigrid hierarchy (gfe_solve.cu)
+void fcg_cache_release(gfe_ctx* ctx);
 
 }  // namespace gfe
 
@@ -122,6 +124,9 @@ struct gfe_ctx {
   // that wait give up at once (gfe_ctx_set_wait_limit, for tests of the timeout path)
   unsigned long long first_wait_ns = 1000000000ull;
   bool q2tab_valid = false;  // scratch[SCR_Q2TAB] holds the tensor-core Q2 E table
+  // the flexible CG's device loop graph and its multigrid hierarchy, kept while the buffers
+  // they were built on stay the same
+  gfe::FcgLoopCache* fcg_cache = nullptr;
 };
 
 struct gfe_matrix {
@@ -355,6 +360,9 @@ void q2_shapes(int D, int nq, const double* qx, std::vector<double>& phi,
 struct LatticeQ1Op;
 struct LatticeMG;
 int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out);
+// Re-forms the coarse kappa and D^-1 of a hierarchy from its fine kappa (same array and
+// dimensions as at creation, new values)
+int mg_refresh(LatticeMG* mg, const LatticeQ1Op& fine);
 int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done);
 // Records one V-cycle (b = r, result in z) on the context's stream without capturing it (for
 // a caller that captures a larger cycle around it).

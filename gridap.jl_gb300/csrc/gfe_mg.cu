@@ -718,20 +718,12 @@ int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out) {
     L.dinv = (float*)(p + 3 * vb);
     p += 4 * vb;
     if (l) {
-      float* kc = (float*)p;
+      L.op.kap = (float*)p;  // kappa of this level, formed by mg_refresh
       p += al(sizeof(float) * (size_t)L.op.c2 * L.op.n2);
-      const LatticeQ1Op& f = mg->lv.back().op;
-      GFE_CUDA_TRY(cudaMemsetAsync(kc, 0, sizeof(float) * (size_t)L.op.c2 * L.op.n2,
-                                   ctx->stream));
-      k_mg_kappa<<<vgrid(ctx, (int64_t)L.op.n0 * L.op.n1 * L.op.n2), kMgBlock, 0,
-                   ctx->stream>>>(L.op.n0, L.op.n1, L.op.n2, f.c1, f.n1, L.op.c1, f.kap, kc);
-      ctx->launches++;
-      L.op.kap = kc;
     }
-    k_mg_diag<<<vgrid(ctx, L.n), kMgBlock, 0, ctx->stream>>>(L.op, L.dinv);
-    ctx->launches++;
     mg->lv.push_back(L);
   }
+  GFE_TRY(mg_refresh(mg, fine));
   for (size_t l = 0; l < mg->lv.size(); ++l) {
     if (!coarse_from(mg, l)) continue;
     const size_t bytes = sizeof(float) * (size_t)coarse_levels(mg, l).floats;
@@ -739,6 +731,29 @@ int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out) {
       GFE_CUDA_TRY(cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)bytes));
     break;
+  }
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+// The coarse kappa and D^-1 of every level from the fine operator's kappa (the same
+// dimensions and kappa array as the hierarchy was created for; its values may have changed)
+int mg_refresh(LatticeMG* mg, const LatticeQ1Op& fine) {
+  gfe_ctx* ctx = mg->ctx;
+  mg->lv[0].op.kap = fine.kap;
+  for (size_t l = 0; l < mg->lv.size(); ++l) {
+    LatticeMG::Level& L = mg->lv[l];
+    if (l) {
+      const LatticeQ1Op& f = mg->lv[l - 1].op;
+      float* kc = const_cast<float*>(L.op.kap);
+      GFE_CUDA_TRY(cudaMemsetAsync(kc, 0, sizeof(float) * (size_t)L.op.c2 * L.op.n2,
+                                   ctx->stream));
+      k_mg_kappa<<<vgrid(ctx, (int64_t)L.op.n0 * L.op.n1 * L.op.n2), kMgBlock, 0,
+                   ctx->stream>>>(L.op.n0, L.op.n1, L.op.n2, f.c1, f.n1, L.op.c1, f.kap, kc);
+      ctx->launches++;
+    }
+    k_mg_diag<<<vgrid(ctx, L.n), kMgBlock, 0, ctx->stream>>>(L.op, L.dinv);
+    ctx->launches++;
   }
   GFE_CUDA_TRY(cudaGetLastError());
   return GFE_OK;

@@ -2089,6 +2089,37 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
 }
 
 
+// The flexible CG's device loop on the lattice multigrid, kept in the context between solves:
+// the hierarchy (refreshed from the new kappa each solve) while the fine operator's array and
+// dimensions stay the same, and the instantiated loop graph while every buffer it reads is
+// the same one (the key). Steps that rebuild the same matrix over the same buffers (the
+// stream-ordered pool returns them in the same order) skip the graph build.
+struct FcgLoopCache {
+  LatticeMG* mg = nullptr;
+  LatticeQ1Op fine{};
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uintptr_t> key;
+  long long body_launches = 0, if_launches = 0;
+  ~FcgLoopCache() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (mg) mg_destroy(mg);
+  }
+};
+
+void fcg_cache_release(gfe_ctx* ctx) {
+  delete ctx->fcg_cache;
+  ctx->fcg_cache = nullptr;
+}
+
+static bool same_lattice_op(const LatticeQ1Op& a, const LatticeQ1Op& b) {
+  if (a.kap != b.kap || a.n0 != b.n0 || a.n1 != b.n1 || a.n2 != b.n2 || a.s1 != b.s1 ||
+      a.s2 != b.s2 || a.c1 != b.c1 || a.c2 != b.c2 || a.p1 != b.p1 || a.p2 != b.p2)
+    return false;
+  for (int e = 0; e < 64; ++e)
+    if (a.K[e] != b.K[e]) return false;
+  return true;
+}
+
 // Flexible CG with the learned block preconditioner (pc != nullptr) or Jacobi, FP32 vectors
 // with FP64 reliable updates. Falls back to Jacobi when the learned preconditioner stagnates
 // (the FP32 residual fails to halve over `check_every` iterations twice in a row).
@@ -2196,12 +2227,14 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   };
   // geometric multigrid V-cycle on the lattice operator (GFE_PC_MG without a learned pc)
   LatticeMG* mg = nullptr;
+  bool mg_cached = false;  // owned by the context's cache
   struct MgRelease {
     LatticeMG** p;
+    const bool* cached;
     ~MgRelease() {
-      if (*p) mg_destroy(*p);
+      if (*p && !*cached) mg_destroy(*p);
     }
-  } mg_release{&mg};
+  } mg_release{&mg, &mg_cached};
   // p-multigrid for Q2 matrices without the Q1 lattice form
   Q2PMG* pmg = nullptr;
   P2PMG* p2mg = nullptr;
@@ -2213,6 +2246,8 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       if (*q) p2mg_destroy(*q);
     }
   } pmg_release{&pmg, &p2mg};
+  // the lattice hierarchy and loop graph may come from (and go to) the context's cache
+  const bool cacheable = lattice && use_mg && !learned && !ctx->timer.enabled;
   if (use_mg) {
     bool q2 = false;
     if (!lattice) GFE_TRY(pmg_ready(ctx, A, &q2));
@@ -2225,7 +2260,19 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
                        "vector P2 elasticity on a simplexified box");
     if (learned && !lattice)
       return set_error(GFE_ERR_UNSUPPORTED, "solve: the learned smoother is for Q1 lattices");
-    if (lattice) {
+    if (lattice && cacheable) {
+      FcgLoopCache*& C = ctx->fcg_cache;
+      if (C && C->mg && same_lattice_op(C->fine, lop)) {
+        GFE_TRY(mg_refresh(C->mg, lop));
+      } else {
+        fcg_cache_release(ctx);
+        C = new FcgLoopCache();
+        GFE_TRY(mg_create(ctx, lop, &C->mg));
+        C->fine = lop;
+      }
+      mg = C->mg;
+      mg_cached = true;
+    } else if (lattice) {
       GFE_TRY(mg_create(ctx, lop, &mg));
       if (learned) GFE_TRY(mg_set_learned(mg, pc));
     } else if (q2) {
@@ -2290,12 +2337,29 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   // the loop graph, built while the device runs the first iteration's work
   struct LoopExec {
     cudaGraphExec_t e = nullptr;
+    bool cached = false;  // owned by the context's cache
     ~LoopExec() {
-      if (e) cudaGraphExecDestroy(e);
+      if (e && !cached) cudaGraphExecDestroy(e);
     }
   } loop;
   long long body_launches = 0, if_launches = 0, if_counted = 0;
-  if (device_loop) {
+  // everything the loop graph reads, by address
+  std::vector<uintptr_t> key;
+  if (device_loop && mg_cached) {
+    key = {(uintptr_t)n, (uintptr_t)d_x, (uintptr_t)d_b, (uintptr_t)A->rowptr.ptr,
+           (uintptr_t)A->val.ptr, (uintptr_t)f, (uintptr_t)r64, (uintptr_t)w.S,
+           (uintptr_t)w.partials, (uintptr_t)mg, (uintptr_t)(vec4 ? 1 : 0) | (vec4_bx ? 2 : 0),
+           (uintptr_t)gv, (uintptr_t)lat_smem, (uintptr_t)A->cart_n[0],
+           (uintptr_t)A->cart_n[1], (uintptr_t)A->cart_n[2], (uintptr_t)A->cart_lattice};
+    FcgLoopCache* C = ctx->fcg_cache;
+    if (C && C->exec && C->key == key) {
+      loop.e = C->exec;
+      loop.cached = true;
+      body_launches = C->body_launches;
+      if_launches = C->if_launches;
+    }
+  }
+  if (device_loop && !loop.e) {
     // WHILE (not done) { update; IF (reliable update due) { x64 += x32; r64 = b - A x64;
     // r32 = r64 or stop }; preconditioner; beta; direction; SpMV }: the reliable updates run
     // inside the loop too, so that the host waits once per solve. The IF node is added to the
@@ -2382,6 +2446,14 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       (void)cudaGetLastError();
       if (loop.e) cudaGraphExecDestroy(loop.e);
       loop.e = nullptr;
+    } else if (mg_cached) {  // hand the graph to the cache
+      FcgLoopCache* C = ctx->fcg_cache;
+      if (C->exec) cudaGraphExecDestroy(C->exec);
+      C->exec = loop.e;
+      C->key = key;
+      C->body_launches = body_launches;
+      C->if_launches = if_launches;
+      loop.cached = true;
     }
   }
   int updates = 0, slow = 0, fallback = 0;

@@ -86,3 +86,34 @@ def test_q2_pmultigrid_fcg(gg, orc, part, jit):
                          jitter=jitter)
     ro = ref["b"] - orc.csc_mul(*ref["csc"], x)
     assert np.linalg.norm(ro) <= 1.01e-8 * np.linalg.norm(ref["b"])
+
+
+def test_mg_fcg_cached_loop_follows_new_kappa(gg):
+    """The context keeps the multigrid hierarchy and the device loop graph between solves
+    while the buffers they read stay the same: a solve after re-assembling with a new kappa,
+    and after a solve of another size in between, must equal the same solve with the cache
+    out of play (kernel timing on: a fresh hierarchy and the host-driven loop)."""
+    rng = np.random.default_rng(77)
+    part = (24, 24, 24)
+    ncells = int(np.prod(part))
+    fnod = rng.standard_normal(int(np.prod(np.array(part) + 1)))
+    kaps = [np.exp(1.5 * rng.standard_normal(ncells)) for _ in range(2)]
+
+    def run(kap, p=part, f=fnod):
+        _, _, A, b = _problem(gg, (0, 1) * 3, p, ("boundary",), kap, gg.NodalField(f))
+        return _solve(gg, A, b, gg.FCGSolver(rtol=1e-8, pc="mg"))
+
+    x0, r0 = run(kaps[0])
+    x1, r1 = run(kaps[1])           # same buffers, new kappa: the hierarchy is refreshed
+    run(np.ones(8 ** 3), (8, 8, 8), np.ones(9 ** 3))  # another size in between
+    x1b, r1b = run(kaps[1])
+    ctx = gg.default_context()
+    ctx.set_timing(True)
+    try:
+        x1ref, r1ref = run(kaps[1])
+    finally:
+        ctx.set_timing(False)
+    for x, r in ((x1, r1), (x1b, r1b)):
+        assert r.converged and r.iterations == r1ref.iterations
+        assert np.linalg.norm(x - x1ref) <= 1e-12 * np.linalg.norm(x1ref)
+    assert r0.converged and np.linalg.norm(x0 - x1) > 1e-3 * np.linalg.norm(x1)

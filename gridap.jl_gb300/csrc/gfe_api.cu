@@ -290,6 +290,7 @@ extern "C" int gfe_matrix_fillstored_zero(gfe_matrix* A) {
   if (A->nnz)
     GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * A->nnz, A->ctx->stream));
   A->val_pending = false;
+  A->zf_values = false;
   A->plan_valid = false;
   A->dia_checked = false;
   A->mf_state = 0;
@@ -304,6 +305,7 @@ extern "C" int gfe_numeric_loop_matrix(gfe_ctx* ctx, gfe_matrix* A, const double
     return set_error(GFE_ERR_INVALID_ARGUMENT, "gfe_numeric_loop_matrix: bad arguments");
   DeviceGuard g(ctx->device);
   GFE_TRY(ensure_values(ctx, A));
+  A->zf_values = false;
   const void* d;
   GFE_TRY(device_view(ctx, cellmats, sizeof(double) * (size_t)A->ncells * A->nd * A->cols_per_cell(),
                       SCR_CELLMAT, &d));

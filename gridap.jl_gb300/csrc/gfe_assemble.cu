@@ -511,6 +511,7 @@ int assemble_problem(gfe_ctx* ctx, const gfe_problem* p, gfe_matrix* A, double* 
                                  p->form == GFE_FORM_DIFFUSION &&
                                  p->geometry == GFE_GEOM_CARTESIAN;
   if (!lattice_candidate) GFE_TRY(ensure_values(ctx, A));
+  if (A) A->zf_values = false;  // set again by the class-sum kernel when it writes them
   if (p->reffe == GFE_REFFE_P2_TET) return assemble_p2_elasticity(ctx, p, A, d_b);
   if (p->form == GFE_FORM_QUASILINEAR) return assemble_quasilinear(ctx, p, A, d_b);
   const int D = p->dim;

@@ -280,6 +280,7 @@ int assemble_cartesian_q1_lattice(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem
   timer_begin(ctx, GFE_KT_ASSEMBLE);
   kern<<<grid, kCqBlock, smem, ctx->stream>>>(a);
   timer_end(ctx);
+  A->zf_values = zf;
   ctx->launches++;
   GFE_CUDA_TRY(cudaGetLastError());
   *done = true;

@@ -339,6 +339,7 @@ extern "C" int gfe_assemble_boundary_matrix(gfe_ctx* ctx, const gfe_problem* p, 
   const bool lift = p->dirichlet_values && p->ndirichlet > 0 && b;
   DeviceGuard g(ctx->device);
   GFE_TRY(ensure_values(ctx, A));
+  A->zf_values = false;  // facet terms add into the values
   FacetTables t;
   GFE_TRY(facet_tables(p, degree, t));
   const int nd = t.nd, nq = t.nq, D = t.D;

@@ -98,6 +98,7 @@ int ensure_values(gfe_ctx* ctx, gfe_matrix* A) {
   if (A->nnz > 0)
     GFE_CUDA_TRY(cudaMemsetAsync(A->val.ptr, 0, sizeof(double) * (size_t)A->nnz, ctx->stream));
   A->val_pending = false;
+  A->zf_values = false;
   return GFE_OK;
 }
 

@@ -149,6 +149,10 @@ struct gfe_matrix {
   // values not yet zeroed (the closed-form Cartesian pattern defers it: the class-sum
   // assembly writes every entry); ensure_values zeroes them before any other use
   bool val_pending = false;
+  // the values are the class-sum kernel's on cubic cells, unchanged since: the entries of
+  // the face classes (neighbours along one axis) are exact zeros, which the FP64 lattice
+  // residual skips
+  bool zf_values = false;
   const int32_t* col_ids() const {
     return cols_alias ? cell_rows.as<int32_t>() : cell_cols.as<int32_t>();
   }

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <limits>
 #include <type_traits>
 
 #include <cuda.h>  // CUtensorMap (the encoder is looked up at run time)
@@ -1621,6 +1622,13 @@ __global__ void k_fcg_if_update(cudaGraphConditionalHandle h, const SolverState*
 __global__ void k_set_defer(SolverState* S) { S->defer_update = 1; }
 
 // ---- host drivers -------------------------------------------------------------------------
+// ||r|| / ||b|| from the squares: not finite when either is (a NaN in b must not read as a
+// zero residual), 0 for b = 0
+static double rel_residual(double rr, double bb) {
+  if (!std::isfinite(rr) || !std::isfinite(bb)) return std::numeric_limits<double>::quiet_NaN();
+  return bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
+}
+
 struct SolverWork {
   SolverState* S;      // device
   SolverState* hS;     // pinned host mirror
@@ -1849,7 +1857,7 @@ static int solve_from_guess(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, boo
   if (h.bb == 0.0 || h.rr <= o->rtol * o->rtol * h.bb) {
     if (h.bb == 0.0) GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
     rep->converged = 1;
-    rep->relres = h.bb > 0.0 ? std::sqrt(h.rr / h.bb) : 0.0;
+    rep->relres = rel_residual(h.rr, h.bb);
     return GFE_OK;
   }
   gfe_solver_opts o2 = *o;
@@ -1859,7 +1867,7 @@ static int solve_from_guess(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, boo
   k_axpy64<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, d);
   ctx->launches++;
   GFE_TRY(residual(d_x));
-  rep->relres = std::sqrt(h.rr / h.bb);
+  rep->relres = rel_residual(h.rr, h.bb);
   rep->converged = std::isfinite(rep->relres) && rep->relres <= o->rtol * (1.0 + 1e-6);
   return GFE_OK;
 }
@@ -2090,7 +2098,7 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
     GFE_CUDA_TRY(cudaGetLastError());
     GFE_TRY(read_state(ctx, w));
     const double bb = w.hS->bb;
-    rep->relres = bb > 0 ? std::sqrt(w.hS->rr / bb) : 0.0;
+    rep->relres = rel_residual(w.hS->rr, bb);
     rep->converged = std::isfinite(rep->relres) && rep->relres <= o->rtol * (1.0 + 1e-6);
     if (!std::isfinite(rep->relres)) rep->status = GFE_ERR_NONFINITE;
   }
@@ -2559,7 +2567,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   if (!(loop.e && fresh)) GFE_TRY(read_state(ctx, w));
   const double bb = w.hS->bb;
   const double rr = fresh ? w.hS->rr64 : w.hS->rr;
-  rep->relres = bb > 0 ? std::sqrt(rr / bb) : 0.0;
+  rep->relres = rel_residual(rr, bb);
   rep->converged = std::isfinite(rep->relres) && rep->relres <= o->rtol * (1.0 + 1e-6);
   rep->status = std::isfinite(rep->relres) ? GFE_OK : GFE_ERR_NONFINITE;
   return GFE_OK;

@@ -117,3 +117,32 @@ def test_mg_fcg_cached_loop_follows_new_kappa(gg):
         assert r.converged and r.iterations == r1ref.iterations
         assert np.linalg.norm(x - x1ref) <= 1e-12 * np.linalg.norm(x1ref)
     assert r0.converged and np.linalg.norm(x0 - x1) > 1e-3 * np.linalg.norm(x1)
+
+
+def test_mg_fcg_device_loop_limits(gg):
+    """The device-driven loop stops at maxiter (not converged, the FP64 residual of the
+    iterate it reached, equal to the uncached host-driven loop's), solves b = 0 at once, and a
+    NaN in b ends the solve with a non-finite residual instead of running on."""
+    rng = np.random.default_rng(5)
+    part = (16, 16, 16)
+    kappa = np.exp(rng.standard_normal(int(np.prod(part))))
+    fnod = rng.standard_normal(int(np.prod(np.array(part) + 1)))
+    _, _, A, b = _problem(gg, (0, 1) * 3, part, ("boundary",), kappa, gg.NodalField(fnod))
+    x, rep = _solve(gg, A, b, gg.FCGSolver(rtol=1e-12, pc="mg", maxiter=2))
+    assert not rep.converged and rep.iterations == 2
+    r = b - A.to_scipy() @ x
+    assert abs(rep.relres - np.linalg.norm(r) / np.linalg.norm(b)) <= 1e-6 * rep.relres
+    ctx = gg.default_context()
+    ctx.set_timing(True)
+    try:
+        xh, reph = _solve(gg, A, b, gg.FCGSolver(rtol=1e-12, pc="mg", maxiter=2))
+    finally:
+        ctx.set_timing(False)
+    assert reph.iterations == 2 and np.linalg.norm(x - xh) <= 1e-12 * np.linalg.norm(xh)
+    x0, rep0 = _solve(gg, A, np.zeros_like(b), gg.FCGSolver(rtol=1e-8, pc="mg"))
+    assert rep0.converged and rep0.iterations == 0 and not np.any(x0)
+    bn = b.copy()
+    bn[7] = np.nan
+    xn, repn = _solve(gg, A, bn, gg.FCGSolver(rtol=1e-8, pc="mg", maxiter=50))
+    assert not repn.converged and repn.iterations <= 50
+    assert repn.status == gg._lib.GFE_ERR_NONFINITE or not np.isfinite(repn.relres)

@@ -367,10 +367,25 @@ int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out);
 // Re-forms the coarse kappa and D^-1 of a hierarchy from its fine kappa (same array and
 // dimensions as at creation, new values)
 int mg_refresh(LatticeMG* mg, const LatticeQ1Op& fine);
-int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done);
+// A dot product of the V-cycle's result z that the cycle's last kernel reduces (the flexible
+// CG's beta, v = q = A p and den = p.q): *out = -(z . v) / *den, 0 when *den is 0. partials
+// holds one entry per block of the fine level's sweep (at most twice LatticeQ1Op::blocks).
+struct MgDot {
+  const float* v = nullptr;
+  double* partials = nullptr;
+  unsigned* ticket = nullptr;
+  const double* den = nullptr;
+  double* out = nullptr;
+};
+int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done,
+             const MgDot* dot = nullptr);
 // Records one V-cycle (b = r, result in z) on the context's stream without capturing it (for
 // a caller that captures a larger cycle around it).
-int mg_record(LatticeMG* mg, const float* r, float* z, const int* done);
+int mg_record(LatticeMG* mg, const float* r, float* z, const int* done,
+              const MgDot* dot = nullptr);
+// Whether the cycle's last kernel forms an MgDot: not when the fine level runs inside the
+// one-block coarse kernel or with the learned smoother.
+bool mg_fuses_dot(const LatticeMG* mg);
 // Makes the learned block preconditioner the fine level's smoother of the V-cycle (pre:
 // x = M(b); post: x += M(b - A x)); the coarser levels keep damped Jacobi.
 int mg_set_learned(LatticeMG* mg, gfe_learned_pc* pc);

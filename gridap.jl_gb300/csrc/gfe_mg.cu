@@ -22,6 +22,7 @@
 
 namespace gfe {
 #include "gfe_lattice.cuh"
+#include "gfe_reduce.cuh"
 
 namespace {
 
@@ -113,6 +114,34 @@ __global__ void __launch_bounds__(kMgBlock)
   };
   lattice_rows<false, decltype(epi), KZ>(op, (int)blockIdx.x, (int)blockIdx.y,
                                          (int)blockIdx.z, x, epi);
+}
+
+// The cycle's last sweep, with the dot product the caller asked for: xo as k_mg_smooth, and
+// *d.out = -(xo . d.v) / *d.den (0 when *d.den is 0), FP32 per thread and FP64 across the
+// block's warps, the block partials added in block order by the last block.
+template <int KZ>
+__global__ void __launch_bounds__(kMgBlock)
+    k_mg_smooth_dot(LatticeQ1Op op, const float* __restrict__ x, const float* __restrict__ b,
+                    const float* __restrict__ dinv, float* __restrict__ xo, float w,
+                    const int* done, MgDot d) {
+  __shared__ double sh[kMgBlock / 32];
+  if (stop(done)) return;
+  float s = 0.f;
+  auto epi = [&](int64_t row, float xc, float acc) {
+    const float v = fmaf(w * __ldg(dinv + row), __ldg(b + row) - acc, xc);
+    xo[row] = v;
+    s = fmaf(v, __ldg(d.v + row), s);
+  };
+  lattice_rows<false, decltype(epi), KZ>(op, (int)blockIdx.x, (int)blockIdx.y,
+                                         (int)blockIdx.z, x, epi);
+  const double bs = block_sum_f<kMgBlock>(s, sh);
+  if (threadIdx.x == 0) d.partials[block_linear()] = bs;
+  double tot[1];
+  if (last_block_reduce<kMgBlock, 1>(d.ticket, d.partials, (int)grid_blocks(), tot, sh) &&
+      threadIdx.x == 0) {
+    const double den = *d.den;
+    *d.out = den != 0.0 ? -tot[0] / den : 0.0;
+  }
 }
 
 // The first two sweeps in one pass: x0 = w0 D^-1 b (the sweep from zero, formed on the fly at
@@ -496,8 +525,10 @@ struct LatticeMG {
   float* cap_z = nullptr;
   const int* cap_done = nullptr;
   long long nodes = 0;
+  MgDot cap_dot{};
   gfe_learned_pc* learned = nullptr;  // the fine level's smoother when set
   SweepPair w{0.8f, 0.8f};             // smoothing factors of every level
+  MgDot dot{};                         // formed by the cycle's last sweep when dot.v is set
   explicit LatticeMG(gfe_ctx* c) : ctx(c), buf(c) {}
   ~LatticeMG() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -590,6 +621,17 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
     ctx->launches++;
     return GFE_OK;
   };
+  // the last sweep of the fine level, with the caller's dot product
+  auto smooth_dot = [&](const float* xi, float* xo, float w) -> int {
+    if (deep)
+      GFE_CUDA_TRY(launch_pdl(k_mg_smooth_dot<kLatK>, ga, kMgBlock, 0, st, L.op, xi, L.b,
+                              L.dinv, xo, w, done, mg->dot));
+    else
+      GFE_CUDA_TRY(launch_pdl(k_mg_smooth_dot<1>, ga1, kMgBlock, 0, st, L.op, xi, L.b, L.dinv,
+                              xo, w, done, mg->dot));
+    ctx->launches++;
+    return GFE_OK;
+  };
   auto residual = [&](const float* x, float* r) -> int {
     if (deep)
       GFE_CUDA_TRY(launch_pdl(k_mg_residual<kLatK>, ga, kMgBlock, 0, st, L.op, x, L.b, r,
@@ -663,7 +705,10 @@ int vcycle(LatticeMG* mg, size_t l, const int* done) {
   cur = post0;
   oth = post0 == L.x ? L.t : L.x;
   for (int s = 0; s < kPostSweeps; ++s) {
-    GFE_TRY(smooth(cur, oth, mg->w.at(s)));
+    if (l == 0 && mg->dot.v && s + 1 == kPostSweeps)
+      GFE_TRY(smooth_dot(cur, oth, mg->w.at(s)));
+    else
+      GFE_TRY(smooth(cur, oth, mg->w.at(s)));
     std::swap(cur, oth);
   }
   return cur == L.x ? GFE_OK : set_error(GFE_ERR_UNSUPPORTED, "multigrid: sweep parity");
@@ -759,16 +804,33 @@ int mg_refresh(LatticeMG* mg, const LatticeQ1Op& fine) {
   return GFE_OK;
 }
 
+bool mg_fuses_dot(const LatticeMG* mg) {
+  return !mg->learned && mg->lv.size() > 1 && !coarse_from(mg, 0);
+}
+
+namespace {
+MgDot dot_or_none(const LatticeMG* mg, const MgDot* dot) {
+  return dot && mg_fuses_dot(mg) ? *dot : MgDot{};
+}
+bool same_dot(const MgDot& a, const MgDot& b) {
+  return a.v == b.v && a.partials == b.partials && a.ticket == b.ticket && a.den == b.den &&
+         a.out == b.out;
+}
+}  // namespace
+
 // z = V-cycle(r) on the fine lattice rows
-int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done) {
+int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done, const MgDot* dot) {
   gfe_ctx* ctx = mg->ctx;
-  if (!mg->exec || mg->cap_r != r || mg->cap_z != z || mg->cap_done != done) {
+  const MgDot d = dot_or_none(mg, dot);
+  if (!mg->exec || mg->cap_r != r || mg->cap_z != z || mg->cap_done != done ||
+      !same_dot(mg->cap_dot, d)) {
     if (mg->exec) {
       cudaGraphExecDestroy(mg->exec);
       mg->exec = nullptr;
     }
     mg->lv[0].b = const_cast<float*>(r);
     mg->lv[0].x = z;
+    mg->dot = d;
     const long long l0 = ctx->launches;
     cudaGraph_t graph = nullptr;
     GFE_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -791,6 +853,7 @@ int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done) {
     mg->cap_r = r;
     mg->cap_z = z;
     mg->cap_done = done;
+    mg->cap_dot = d;
     mg->nodes = (long long)nodes;
   }
   timer_begin(ctx, GFE_KT_PRECOND);
@@ -800,9 +863,10 @@ int mg_apply(LatticeMG* mg, const float* r, float* z, const int* done) {
   return GFE_OK;
 }
 
-int mg_record(LatticeMG* mg, const float* r, float* z, const int* done) {
+int mg_record(LatticeMG* mg, const float* r, float* z, const int* done, const MgDot* dot) {
   mg->lv[0].b = const_cast<float*>(r);
   mg->lv[0].x = z;
+  mg->dot = dot_or_none(mg, dot);
   return vcycle(mg, 0, done);
 }
 

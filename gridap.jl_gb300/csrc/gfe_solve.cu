@@ -51,67 +51,12 @@ __device__ __forceinline__ void raise_e(DevError* err, int code, long long index
   if (atomicCAS(&err->code, 0, code) == 0) err->index = index;
 }
 
-// Block sum of a double (all threads get the result in thread 0).
-template <int NT>
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) sh[w] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < NT / 32; ++i) s += sh[i];
-  __syncthreads();
-  return s;
-}
-
-// Block sum of FP32 values: FP32 within each warp (shuffles), FP64 across the block's warps
-// in warp order. Deterministic; avoids FP64 shuffles, which cost a full warp instruction on
-// the FP64 pipe each.
-template <int NT>
-__device__ __forceinline__ double block_sum_f(float v, double* sh) {
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) sh[w] = (double)v;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < NT / 32; ++i) s += sh[i];
-  __syncthreads();
-  return s;
-}
+#include "gfe_reduce.cuh"
 
 template <int NT, typename T>
 __device__ __forceinline__ double block_sum_t(T v, double* sh) {
   if constexpr (sizeof(T) == 4) return block_sum_f<NT>(v, sh);
   else return block_sum<NT>((double)v, sh);
-}
-
-// Linear block id and block count of 1-, 2- or 3-D grids.
-__device__ __forceinline__ unsigned block_linear() {
-  return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-}
-__device__ __forceinline__ unsigned grid_blocks() { return gridDim.x * gridDim.y * gridDim.z; }
-
-// Called by every block after writing its partial(s). Returns true in the last block, with
-// the partial sums of all blocks reduced in block order into out[0..nv).
-template <int NT, int NV>
-__device__ bool last_block_reduce(unsigned* ticket, const double* partials, int nblocks,
-                                  double* out, double* sh) {
-  __shared__ bool last;
-  __threadfence();
-  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == (unsigned)nblocks - 1);
-  __syncthreads();
-  if (!last) return false;
-  __threadfence();
-  for (int v = 0; v < NV; ++v) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < nblocks; i += NT) s += __ldcg(partials + (size_t)i * NV + v);
-    s = block_sum<NT>(s, sh);
-    if (threadIdx.x == 0) out[v] = s;
-  }
-  if (threadIdx.x == 0) *ticket = 0u;
-  return true;
 }
 
 // ---- sliced-ELL plan ----------------------------------------------------------------------
@@ -471,6 +416,45 @@ __global__ void __launch_bounds__(kSpmvBlock)
              threadIdx.x == 0) {
     S->pq = tot[0];
     S->alpha = tot[0] != 0.0 ? S->rz / tot[0] : 0.0;
+  }
+}
+
+// The flexible CG's direction update folded into its SpMV on the lattice operator: p = z +
+// beta p, and q = A p formed as A z + beta q (A p_new = A z + beta A p_old, q holding A p_old),
+// so that the stencil reads z and every other vector only at the thread's own row; partials
+// of p.q and p.r and the last-block alpha = (p.r) / (p.q) as k_lattice_spmv<true, false>.
+// beta (S->beta) is formed by the preconditioner's last kernel; beta = 0 (a first direction)
+// reads neither p nor q.
+__global__ void __launch_bounds__(kSpmvBlock)
+    k_lattice_spmv_dir(LatticeQ1Op op, const float* __restrict__ z, float* __restrict__ p,
+                       float* __restrict__ q, const float* __restrict__ r,
+                       double* __restrict__ partials, SolverState* S) {
+  __shared__ double sh[kSpmvBlock / 32];
+  if (S->done) return;
+  const float beta = (float)S->beta;
+  const bool keep = beta != 0.f;
+  float d1 = 0.f, d2 = 0.f;
+  auto epi = [&](int64_t row, float zc, float acc) {
+    const float pn = keep ? fmaf(beta, p[row], zc) : zc;
+    const float qn = keep ? fmaf(beta, q[row], acc) : acc;
+    p[row] = pn;
+    q[row] = qn;
+    d1 = fmaf(pn, qn, d1);
+    d2 = fmaf(pn, __ldg(r + row), d2);
+  };
+  lattice_rows<false>(op, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, z, epi);
+  const double s1 = block_sum_f<kSpmvBlock>(d1, sh);
+  const double s2 = block_sum_f<kSpmvBlock>(d2, sh);
+  const unsigned bl = block_linear();
+  if (threadIdx.x == 0) {
+    partials[2 * bl] = s1;
+    partials[2 * bl + 1] = s2;
+  }
+  double tot[2];
+  if (last_block_reduce<kSpmvBlock, 2>(&S->ticket[0], partials, grid_blocks(), tot, sh) &&
+      threadIdx.x == 0) {
+    S->pq = tot[0];
+    S->alpha = tot[0] != 0.0 ? tot[1] / tot[0] : 0.0;
   }
 }
 
@@ -2182,7 +2166,12 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     else
       k_fcg_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S);
   };
+  // with the multigrid V-cycle on the lattice operator, beta comes from the cycle's last sweep
+  // and the direction update runs inside the SpMV (k_lattice_spmv_dir)
+  bool fuse_dir = false;
+  MgDot mgdot;
   auto fcg_beta_dir = [&]() {
+    if (fuse_dir) return;
     if (vec4) {
       k_fcg_beta4<<<gv, kVecBlock, 0, ctx->stream>>>(n, z32, q32, w.partials, w.S);
       k_fcg_dir4<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
@@ -2234,7 +2223,10 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   const LatticeQ1Op lop = lattice ? lattice_op(A) : LatticeQ1Op{};
   auto spmv = [&]() {
     timer_begin(ctx, GFE_KT_SPMV32);
-    if (lattice)
+    if (lattice && fuse_dir)
+      k_lattice_spmv_dir<<<lop.grid(n), kSpmvBlock, 0, ctx->stream>>>(lop, z32, p32, q32, r32,
+                                                                      w.partials, w.S);
+    else if (lattice)
       k_lattice_spmv<true, false><<<lop.grid(n), kSpmvBlock, 0, ctx->stream>>>(
           lop, p32, q32, r32, w.partials, w.S);
     else if (A->dia_valid)
@@ -2303,7 +2295,17 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     }
     // a V-cycle iteration is expensive: look at the state after every one
     if (o->check_every <= 0) check_every = 1;
+    if (mg && mg_fuses_dot(mg)) {
+      fuse_dir = true;
+      mgdot.v = q32;
+      mgdot.partials = w.partials;
+      mgdot.ticket = &w.S->ticket[3];
+      mgdot.den = &w.S->pq;
+      mgdot.out = &w.S->beta;
+    }
   }
+  // launches of fcg_beta_dir
+  const int beta_dir_launches = fuse_dir ? 0 : 2;
   // Without kernel timing and without the learned preconditioner's stagnation check, the
   // iterations run as one device-driven loop: a CUDA graph whose WHILE node repeats [update,
   // preconditioner, beta, direction, SpMV] until the state's done flag is set (converged,
@@ -2316,8 +2318,9 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
                                           : pmg_apply(pmg, r32, z32, &w.S->done);
     if (use_mg && p2mg) return device_loop ? p2mg_record(p2mg, r32, z32, &w.S->done)
                                            : p2mg_apply(p2mg, r32, z32, &w.S->done);
-    if (use_mg) return device_loop ? mg_record(mg, r32, z32, &w.S->done)
-                                   : mg_apply(mg, r32, z32, &w.S->done);
+    const MgDot* dot = fuse_dir ? &mgdot : nullptr;
+    if (use_mg) return device_loop ? mg_record(mg, r32, z32, &w.S->done, dot)
+                                   : mg_apply(mg, r32, z32, &w.S->done, dot);
     if (learned) return learned_apply(ctx, pc, r32, z32, &w.S->done);
     k_jacobi_apply<<<gv, kVecBlock, 0, ctx->stream>>>(n, r32, dinv32, z32, w.S);
     ctx->launches++;
@@ -2352,8 +2355,10 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     ctx->launches++;
   }
   GFE_TRY(precond());
-  GFE_CUDA_TRY(cudaMemcpyAsync(p32, z32, sizeof(float) * n, cudaMemcpyDeviceToDevice,
-                               ctx->stream));
+  // p = z (the fused SpMV forms it: beta is 0 while p.q is)
+  if (!fuse_dir)
+    GFE_CUDA_TRY(cudaMemcpyAsync(p32, z32, sizeof(float) * n, cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
   spmv();
   // the loop graph, built while the device runs the first iteration's work
   struct LoopExec {
@@ -2369,7 +2374,8 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   if (device_loop && mg_cached) {
     key = {(uintptr_t)n, (uintptr_t)d_x, (uintptr_t)d_b, (uintptr_t)A->rowptr.ptr,
            (uintptr_t)A->val.ptr, (uintptr_t)f, (uintptr_t)r64, (uintptr_t)w.S,
-           (uintptr_t)w.partials, (uintptr_t)mg, (uintptr_t)(vec4 ? 1 : 0) | (vec4_bx ? 2 : 0),
+           (uintptr_t)w.partials, (uintptr_t)mg,
+           (uintptr_t)(vec4 ? 1 : 0) | (vec4_bx ? 2 : 0) | (fuse_dir ? 4 : 0),
            (uintptr_t)gv, (uintptr_t)lat_smem, (uintptr_t)A->cart_n[0],
            (uintptr_t)A->cart_n[1], (uintptr_t)A->cart_n[2], (uintptr_t)A->cart_lattice,
            (uintptr_t)A->zf_values};
@@ -2447,8 +2453,8 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       fcg_beta_dir();
       spmv();
       k_fcg_continue<<<1, 1, 0, ctx->stream>>>(h, w.S);
-      // + update, IF condition, beta, direction and WHILE condition
-      body_launches = ctx->launches - l0 - if_counted + 5;
+      // + update, IF condition, beta and direction (unless fused), WHILE condition
+      body_launches = ctx->launches - l0 - if_counted + 3 + beta_dir_launches;
       ctx->launches = l0;
       cudaGraph_t bodyg = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &bodyg);
@@ -2500,10 +2506,12 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       timer_end(ctx);
       ctx->launches++;
       GFE_TRY(precond());
-      timer_begin(ctx, GFE_KT_VECTOR);
-      fcg_beta_dir();
-      timer_end(ctx);
-      ctx->launches += 2;
+      if (!fuse_dir) {
+        timer_begin(ctx, GFE_KT_VECTOR);
+        fcg_beta_dir();
+        timer_end(ctx);
+      }
+      ctx->launches += beta_dir_launches;
       spmv();
     }
     GFE_CUDA_TRY(cudaGetLastError());
@@ -2525,7 +2533,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       // z, p restart from the new residual direction (keeps FCG's beta well defined)
       GFE_TRY(precond());
       fcg_beta_dir();
-      ctx->launches += 2;
+      ctx->launches += beta_dir_launches;
       spmv();
       rr_chunk = w.hS->rr;
       continue;

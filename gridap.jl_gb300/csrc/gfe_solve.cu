@@ -1251,12 +1251,50 @@ __global__ void k_set_reliable(SolverState* S, double delta2) {
 //   x += a p; r -= a q; z = M(r); beta = -(z.q)/(p.q); p = z + beta p; q = A p; a = (p.r)/(p.q)
 // (Notay's truncated flexible CG with one previous direction). FP32 vectors; x and the true
 // residual in FP64 through reliable updates, as the mixed CG.
+
+// The conditions of the device-driven loop's WHILE node (repeat while not done) and IF node
+// (the reliable update is due), set by the kernels that decide them; on = 0 outside that graph.
+struct LoopConds {
+  cudaGraphConditionalHandle w, i;
+  int on;
+};
+__device__ __forceinline__ void set_conds(const LoopConds& c, const SolverState* S) {
+  if (!c.on) return;
+  cudaGraphSetConditional(c.i, S->need_update && !S->done ? 1u : 0u);
+  cudaGraphSetConditional(c.w, S->done ? 0u : 1u);
+}
+
+// After an update with the FP32 residual rr: count the iteration, then stop (not finite,
+// converged, maxit) or ask for a reliable update (residual dropped by delta; with
+// defer_update, in the device loop, also at convergence, which the FP64 residual confirms)
+__device__ __forceinline__ void fcg_decide(SolverState* S, double rr) {
+  S->iter += 1;
+  S->rr = rr;
+  if (!isfinite(rr)) {
+    S->done = 1;
+  } else if (rr <= S->tol2) {
+    if (S->defer_update) {
+      S->need_update = 1;
+    } else {
+      S->done = 1;
+      S->converged = 1;
+    }
+  } else if (S->iter >= S->maxit) {
+    S->done = 1;
+  } else if (S->delta2 > 0.0 && rr < S->delta2 * S->rmax2) {
+    S->need_update = 1;
+    if (!S->defer_update) S->done = 1;
+  }
+}
 __global__ void __launch_bounds__(kVecBlock)
     k_fcg_update(int64_t n, float* __restrict__ x, float* __restrict__ r,
                  const float* __restrict__ p, const float* __restrict__ q,
-                 double* __restrict__ partials, SolverState* S) {
+                 double* __restrict__ partials, SolverState* S, LoopConds c) {
   __shared__ double sh[kVecBlock / 32];
-  if (S->done) return;
+  if (S->done) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_conds(c, S);
+    return;
+  }
   const float a = (float)S->alpha;
   float rr_t = 0.f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -1271,23 +1309,8 @@ __global__ void __launch_bounds__(kVecBlock)
   double tot[1];
   if (last_block_reduce<kVecBlock, 1>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
       threadIdx.x == 0) {
-    S->iter += 1;
-    S->rr = tot[0];
-    if (!isfinite(tot[0])) {
-      S->done = 1;
-    } else if (tot[0] <= S->tol2) {
-      if (S->defer_update) {  // the FP64 residual decides (the loop's reliable update)
-        S->need_update = 1;
-      } else {
-        S->done = 1;
-        S->converged = 1;
-      }
-    } else if (S->iter >= S->maxit) {
-      S->done = 1;
-    } else if (S->delta2 > 0.0 && tot[0] < S->delta2 * S->rmax2) {
-      S->need_update = 1;
-      if (!S->defer_update) S->done = 1;
-    }
+    fcg_decide(S, tot[0]);
+    set_conds(c, S);
   }
 }
 
@@ -1359,7 +1382,7 @@ __global__ void __launch_bounds__(kSpmvBlock)
 // r32 = (float) r64 after a reliable update (no orthogonalisation needed: FCG takes alpha from
 // p.r and beta from z.q with the current vectors); stop when the FP64 residual meets rtol.
 __global__ void k_fcg_restart(int64_t n, const double* __restrict__ r64, float* __restrict__ r32,
-                              SolverState* S) {
+                              SolverState* S, LoopConds c) {
   const bool conv = S->rr64 <= S->tol2;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n && !conv;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -1376,6 +1399,7 @@ __global__ void k_fcg_restart(int64_t n, const double* __restrict__ r64, float* 
       S->converged = 0;
       S->done = S->iter >= S->maxit ? 1 : 0;
     }
+    set_conds(c, S);
   }
 }
 
@@ -1384,9 +1408,12 @@ __global__ void k_fcg_restart(int64_t n, const double* __restrict__ r64, float* 
 __global__ void __launch_bounds__(kVecBlock)
     k_fcg_update4(int64_t n, float* __restrict__ x, float* __restrict__ r,
                   const float* __restrict__ p, const float* __restrict__ q,
-                  double* __restrict__ partials, SolverState* S) {
+                  double* __restrict__ partials, SolverState* S, LoopConds c) {
   __shared__ double sh[kVecBlock / 32];
-  if (S->done) return;
+  if (S->done) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_conds(c, S);
+    return;
+  }
   const float a = (float)S->alpha;
   float rr_t = 0.f;
   const int64_t n4 = n >> 2;
@@ -1434,23 +1461,8 @@ __global__ void __launch_bounds__(kVecBlock)
   double tot[1];
   if (last_block_reduce<kVecBlock, 1>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
       threadIdx.x == 0) {
-    S->iter += 1;
-    S->rr = tot[0];
-    if (!isfinite(tot[0])) {
-      S->done = 1;
-    } else if (tot[0] <= S->tol2) {
-      if (S->defer_update) {  // the FP64 residual decides (the loop's reliable update)
-        S->need_update = 1;
-      } else {
-        S->done = 1;
-        S->converged = 1;
-      }
-    } else if (S->iter >= S->maxit) {
-      S->done = 1;
-    } else if (S->delta2 > 0.0 && tot[0] < S->delta2 * S->rmax2) {
-      S->need_update = 1;
-      if (!S->defer_update) S->done = 1;
-    }
+    fcg_decide(S, tot[0]);
+    set_conds(c, S);
   }
 }
 
@@ -1593,17 +1605,14 @@ __global__ void k_merge4(int64_t n, double* __restrict__ x64, float* __restrict_
   }
 }
 
-// the condition of the device-driven FCG loop: repeat while the state is not done
-__global__ void k_fcg_continue(cudaGraphConditionalHandle h, const SolverState* S) {
-  cudaGraphSetConditional(h, S->done ? 0u : 1u);
+// the flexible CG's settings in the zeroed state, after its start (which sets ||b||^2)
+__global__ void k_fcg_setup(SolverState* S, double delta2, int maxit, int defer) {
+  S->delta2 = delta2;
+  S->rmax2 = S->bb;
+  S->rr64 = S->bb;
+  S->maxit = maxit;
+  S->defer_update = defer;
 }
-
-// the condition of the loop's reliable update: due after this iteration's update
-__global__ void k_fcg_if_update(cudaGraphConditionalHandle h, const SolverState* S) {
-  cudaGraphSetConditional(h, S->need_update && !S->done ? 1u : 0u);
-}
-
-__global__ void k_set_defer(SolverState* S) { S->defer_update = 1; }
 
 // ---- host drivers -------------------------------------------------------------------------
 // ||r|| / ||b|| from the squares: not finite when either is (a NaN in b must not read as a
@@ -2160,11 +2169,14 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   // the FP32 vectors sit at multiples of 64 entries from a 256-byte aligned base: the float4
   // kernels apply
   const bool vec4 = (reinterpret_cast<uintptr_t>(f) & 15) == 0;
-  auto fcg_update = [&]() {
+  // (conds: the device loop's condition handles, when captured into it)
+  auto fcg_update = [&](LoopConds conds) {
     if (vec4)
-      k_fcg_update4<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S);
+      k_fcg_update4<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S,
+                                                       conds);
     else
-      k_fcg_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S);
+      k_fcg_update<<<gv, kVecBlock, 0, ctx->stream>>>(n, x32, r32, p32, q32, w.partials, w.S,
+                                                      conds);
   };
   // with the multigrid V-cycle on the lattice operator, beta comes from the cycle's last sweep
   // and the direction update runs inside the SpMV (k_lattice_spmv_dir)
@@ -2326,12 +2338,10 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     ctx->launches++;
     return GFE_OK;
   };
-  // start: x = 0, r = b, z = M r, p = z, q = A p, alpha
+  // start: x = 0, r = b (z = M r, p = z, q = A p and alpha follow, as the first iteration of
+  // the device loop or ahead of the host-driven one)
   GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
   GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
-  int maxit_field = maxit;
-  GFE_CUDA_TRY(cudaMemcpyAsync(&w.S->maxit, &maxit_field, sizeof(int), cudaMemcpyHostToDevice,
-                               ctx->stream));
   auto merge = [&]() {
     if (vec4 && (reinterpret_cast<uintptr_t>(d_x) & 15) == 0)
       k_merge4<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
@@ -2347,20 +2357,12 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   else
     k_cg_init<float, double><<<gv, kVecBlock, 0, ctx->stream>>>(
         n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
-  k_set_reliable<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta);
-  ctx->launches += 2;
+  ctx->launches++;
   if (device_loop) {  // ||b||^2 in FP64 for the relative residual, ahead of the loop
     k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb,
                                                   &w.S->ticket[1]);
     ctx->launches++;
   }
-  GFE_TRY(precond());
-  // p = z (the fused SpMV forms it: beta is 0 while p.q is)
-  if (!fuse_dir)
-    GFE_CUDA_TRY(cudaMemcpyAsync(p32, z32, sizeof(float) * n, cudaMemcpyDeviceToDevice,
-                                 ctx->stream));
-  spmv();
-  // the loop graph, built while the device runs the first iteration's work
   struct LoopExec {
     cudaGraphExec_t e = nullptr;
     bool cached = false;  // owned by the context's cache
@@ -2368,7 +2370,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       if (e && !cached) cudaGraphExecDestroy(e);
     }
   } loop;
-  long long body_launches = 0, if_launches = 0, if_counted = 0;
+  long long body_launches = 0, if_launches = 0;
   // everything the loop graph reads, by address
   std::vector<uintptr_t> key;
   if (device_loop && mg_cached) {
@@ -2388,10 +2390,11 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     }
   }
   if (device_loop && !loop.e) {
-    // WHILE (not done) { update; IF (reliable update due) { x64 += x32; r64 = b - A x64;
-    // r32 = r64 or stop }; preconditioner; beta; direction; SpMV }: the reliable updates run
-    // inside the loop too, so that the host waits once per solve. The IF node is added to the
-    // body in the middle of its capture, and its own body captured on a second stream.
+    // WHILE (not done) { preconditioner; beta; direction; SpMV; update; IF (reliable update
+    // due) { x64 += x32; r64 = b - A x64; r32 = r64 or stop } }: the update and the restart
+    // set the two conditions, and the reliable updates run inside the loop too, so that the
+    // host waits once per solve. The IF node is added to the body at the end of its capture,
+    // and its own body captured on a second stream.
     cudaGraph_t g = nullptr;
     bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
     cudaGraphConditionalHandle h{}, hif{};
@@ -2406,14 +2409,20 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     ok = ok && cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
     cudaGraph_t body = ok ? np.conditional.phGraph_out[0] : nullptr;
     ok = ok && cudaGraphConditionalHandleCreate(&hif, body, 0, 0) == cudaSuccess;
+    const LoopConds conds{h, hif, 1};
     cudaStream_t s2 = nullptr;
     ok = ok && cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) == cudaSuccess;
     if (ok && cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
                                             cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       const long long l0 = ctx->launches;
-      fcg_update();
-      k_fcg_if_update<<<1, 1, 0, ctx->stream>>>(hif, w.S);
-      // the IF node after the captured work so far
+      const int st = precond();
+      fcg_beta_dir();
+      spmv();
+      fcg_update(conds);
+      // precond and SpMV count their launches; + beta and direction (unless fused), update
+      body_launches = ctx->launches - l0 + beta_dir_launches + 1;
+      ctx->launches = l0;
+      // the IF node after the captured work
       cudaStreamCaptureStatus cs;
       cudaGraph_t cg = nullptr;
       const cudaGraphNode_t* deps = nullptr;
@@ -2434,12 +2443,10 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
                       cudaSuccess) {
         cudaStream_t main = ctx->stream;
         ctx->stream = s2;  // the reliable update's launches go to the IF body
-        const long long li = ctx->launches;
         merge();
         residual64(&w.S->rr64);
-        k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, w.S);
-        if_counted = ctx->launches - li;
-        if_launches = if_counted + 2;  // merge and restart are not counted by their lambdas
+        k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, w.S, conds);
+        if_launches = 3;
         ctx->stream = main;
         cudaGraph_t ifb = nullptr;
         okif = cudaStreamEndCapture(s2, &ifb) == cudaSuccess;
@@ -2449,13 +2456,6 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       okif = okif && cudaStreamUpdateCaptureDependencies(ctx->stream, &ifnode, nullptr, 1,
                                                          cudaStreamSetCaptureDependencies) ==
                          cudaSuccess;
-      const int st = precond();
-      fcg_beta_dir();
-      spmv();
-      k_fcg_continue<<<1, 1, 0, ctx->stream>>>(h, w.S);
-      // + update, IF condition, beta and direction (unless fused), WHILE condition
-      body_launches = ctx->launches - l0 - if_counted + 3 + beta_dir_launches;
-      ctx->launches = l0;
       cudaGraph_t bodyg = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &bodyg);
       if (st != GFE_OK) {
@@ -2486,23 +2486,33 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   }
   int updates = 0, slow = 0, fallback = 0;
   bool fresh = false;  // the loop ended on a reliable update: x64 and rr64 are current
+  k_fcg_setup<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta, maxit, loop.e ? 1 : 0);
+  ctx->launches++;
   if (loop.e) {
-    // the whole iteration, reliable updates included, on the device: one wait
-    k_set_defer<<<1, 1, 0, ctx->stream>>>(w.S);
+    // the whole solve, reliable updates included, on the device: one wait. The first
+    // iteration's beta is 0 (p.q is); the unfused direction update still reads p.
+    if (!fuse_dir)
+      GFE_CUDA_TRY(cudaMemsetAsync(p32, 0, sizeof(float) * n, ctx->stream));
     GFE_CUDA_TRY(cudaGraphLaunch(loop.e, ctx->stream));
     GFE_TRY(read_state(ctx, w));
     updates = w.hS->updates;
     fresh = w.hS->converged != 0;  // only the loop's reliable update declares convergence
-    ctx->launches += 1 + (long long)w.hS->iter * body_launches + (long long)updates * if_launches;
+    ctx->launches += (long long)w.hS->iter * body_launches + (long long)updates * if_launches;
   } else {
     // host-driven loop (kernel timing, the learned preconditioner, no conditional graphs)
+    GFE_TRY(precond());
+    // p = z (the fused SpMV forms it: beta is 0 while p.q is)
+    if (!fuse_dir)
+      GFE_CUDA_TRY(cudaMemcpyAsync(p32, z32, sizeof(float) * n, cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
+    spmv();
     GFE_TRY(read_state(ctx, w));
   }
   double rr_chunk = w.hS->rr;
   while (!loop.e && !w.hS->done) {
     for (int k = 0; k < check_every; ++k) {
       timer_begin(ctx, GFE_KT_VECTOR);
-      fcg_update();
+      fcg_update(LoopConds{});
       timer_end(ctx);
       ctx->launches++;
       GFE_TRY(precond());
@@ -2522,7 +2532,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       timer_begin(ctx, GFE_KT_RESIDUAL64);
       residual64(&w.S->rr64);
       timer_end(ctx);
-      k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, w.S);
+      k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, w.S, LoopConds{});
       ctx->launches += 3;
       ++updates;
       GFE_TRY(read_state(ctx, w));

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <limits>
 #include <type_traits>
 
@@ -2100,16 +2101,16 @@ int solve(gfe_ctx* ctx, gfe_matrix* A, const gfe_solver_opts* o, const double* d
 
 
 // The flexible CG's device loop on the lattice multigrid, kept in the context between solves:
-// the hierarchy (refreshed from the new kappa each solve) while the fine operator's array and
-// dimensions stay the same, and the instantiated loop graph while every buffer it reads is
-// the same one (the key). Steps that rebuild the same matrix over the same buffers (the
+// the hierarchy (refreshed from the new kappa by each solve's start) while the fine operator's
+// array and dimensions stay the same, and the instantiated loop graph, start included, while
+// every buffer it reads and every setting its start takes is the same (the key). Steps that rebuild the same matrix over the same buffers (the
 // stream-ordered pool returns them in the same order) skip the graph build.
 struct FcgLoopCache {
   LatticeMG* mg = nullptr;
   LatticeQ1Op fine{};
   cudaGraphExec_t exec = nullptr;
   std::vector<uintptr_t> key;
-  long long body_launches = 0, if_launches = 0;
+  long long start_launches = 0, body_launches = 0, if_launches = 0;
   ~FcgLoopCache() {
     if (exec) cudaGraphExecDestroy(exec);
     if (mg) mg_destroy(mg);
@@ -2273,6 +2274,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   } pmg_release{&pmg, &p2mg};
   // the lattice hierarchy and loop graph may come from (and go to) the context's cache
   const bool cacheable = lattice && use_mg && !learned && !ctx->timer.enabled;
+  bool refresh = false;  // the cached hierarchy's coarse kappa and D^-1 are re-formed
   if (use_mg) {
     bool q2 = false;
     if (!lattice) GFE_TRY(pmg_ready(ctx, A, &q2));
@@ -2288,7 +2290,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     if (lattice && cacheable) {
       FcgLoopCache*& C = ctx->fcg_cache;
       if (C && C->mg && same_lattice_op(C->fine, lop)) {
-        GFE_TRY(mg_refresh(C->mg, lop));
+        refresh = true;  // kappa may have new values: with the solve's start
       } else {
         fcg_cache_release(ctx);
         C = new FcgLoopCache();
@@ -2338,10 +2340,6 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     ctx->launches++;
     return GFE_OK;
   };
-  // start: x = 0, r = b (z = M r, p = z, q = A p and alpha follow, as the first iteration of
-  // the device loop or ahead of the host-driven one)
-  GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
-  GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
   auto merge = [&]() {
     if (vec4 && (reinterpret_cast<uintptr_t>(d_x) & 15) == 0)
       k_merge4<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_x, x32);
@@ -2351,18 +2349,37 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   // b and x64 are the caller's buffers: the float4 kernels where they are 16-byte aligned
   const bool vec4_bx = vec4 && ((reinterpret_cast<uintptr_t>(d_b) |
                                  reinterpret_cast<uintptr_t>(d_x)) & 15) == 0;
-  if (vec4_bx && !dinv32)
-    k_fcg_init4<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, x32, r32, w.partials, w.S,
-                                                   o->rtol * o->rtol);
-  else
-    k_cg_init<float, double><<<gv, kVecBlock, 0, ctx->stream>>>(
-        n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
-  ctx->launches++;
-  if (device_loop) {  // ||b||^2 in FP64 for the relative residual, ahead of the loop
+  // The start: the hierarchy's refresh, x = 0, r = b, the zeroed state and its settings
+  // (defer: the device loop's reliable updates), ||b||^2 in FP64 for the relative residual.
+  // z = M r, p = z, q = A p and alpha follow, as the device loop's first iteration or ahead of
+  // the host-driven one. *launches: the kernels it launched.
+  auto start = [&](bool defer, long long* launches) -> int {
+    *launches = 0;
+    if (refresh) {
+      const long long l0 = ctx->launches;
+      GFE_TRY(mg_refresh(mg, lop));
+      *launches += ctx->launches - l0;
+      ctx->launches = l0;
+    }
+    GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
+    GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
+    if (vec4_bx && !dinv32)
+      k_fcg_init4<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, x32, r32, w.partials, w.S,
+                                                     o->rtol * o->rtol);
+    else
+      k_cg_init<float, double><<<gv, kVecBlock, 0, ctx->stream>>>(
+          n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
     k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb,
                                                   &w.S->ticket[1]);
-    ctx->launches++;
-  }
+    k_fcg_setup<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta, maxit, defer ? 1 : 0);
+    *launches += 3;
+    // the device loop's first iteration takes beta = 0 (p.q is); the unfused direction update
+    // still reads p
+    if (defer && !fuse_dir)
+      GFE_CUDA_TRY(cudaMemsetAsync(p32, 0, sizeof(float) * n, ctx->stream));
+    GFE_CUDA_TRY(cudaGetLastError());
+    return GFE_OK;
+  };
   struct LoopExec {
     cudaGraphExec_t e = nullptr;
     bool cached = false;  // owned by the context's cache
@@ -2370,31 +2387,38 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       if (e && !cached) cudaGraphExecDestroy(e);
     }
   } loop;
-  long long body_launches = 0, if_launches = 0;
-  // everything the loop graph reads, by address
+  long long start_launches = 0, body_launches = 0, if_launches = 0;
+  // everything the loop graph reads, by address, and the settings its start takes
   std::vector<uintptr_t> key;
   if (device_loop && mg_cached) {
+    const double rtol2 = o->rtol * o->rtol, delta2 = delta * delta;
+    uint64_t rb, db;
+    std::memcpy(&rb, &rtol2, 8);
+    std::memcpy(&db, &delta2, 8);
     key = {(uintptr_t)n, (uintptr_t)d_x, (uintptr_t)d_b, (uintptr_t)A->rowptr.ptr,
            (uintptr_t)A->val.ptr, (uintptr_t)f, (uintptr_t)r64, (uintptr_t)w.S,
            (uintptr_t)w.partials, (uintptr_t)mg,
-           (uintptr_t)(vec4 ? 1 : 0) | (vec4_bx ? 2 : 0) | (fuse_dir ? 4 : 0),
+           (uintptr_t)(vec4 ? 1 : 0) | (vec4_bx ? 2 : 0) | (fuse_dir ? 4 : 0) |
+               (refresh ? 8 : 0),
            (uintptr_t)gv, (uintptr_t)lat_smem, (uintptr_t)A->cart_n[0],
            (uintptr_t)A->cart_n[1], (uintptr_t)A->cart_n[2], (uintptr_t)A->cart_lattice,
-           (uintptr_t)A->zf_values};
+           (uintptr_t)A->zf_values, (uintptr_t)rb, (uintptr_t)db, (uintptr_t)maxit};
     FcgLoopCache* C = ctx->fcg_cache;
     if (C && C->exec && C->key == key) {
       loop.e = C->exec;
       loop.cached = true;
+      start_launches = C->start_launches;
       body_launches = C->body_launches;
       if_launches = C->if_launches;
     }
   }
   if (device_loop && !loop.e) {
-    // WHILE (not done) { preconditioner; beta; direction; SpMV; update; IF (reliable update
-    // due) { x64 += x32; r64 = b - A x64; r32 = r64 or stop } }: the update and the restart
-    // set the two conditions, and the reliable updates run inside the loop too, so that the
-    // host waits once per solve. The IF node is added to the body at the end of its capture,
-    // and its own body captured on a second stream.
+    // [start] WHILE (not done) { preconditioner; beta; direction; SpMV; update; IF (reliable
+    // update due) { x64 += x32; r64 = b - A x64; r32 = r64 or stop } }: the update and the
+    // restart set the two conditions, and the reliable updates run inside the loop too, so
+    // that the host waits once per solve. The start is captured into the graph, the WHILE node
+    // added after it, and the bodies captured into the nodes' graphs (the IF body on a second
+    // stream, its node added at the end of the loop body's capture).
     cudaGraph_t g = nullptr;
     bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
     cudaGraphConditionalHandle h{}, hif{};
@@ -2402,11 +2426,30 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     cudaGraphNode_t node;
     ok = ok && cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) ==
                    cudaSuccess;
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = h;
-    np.conditional.type = cudaGraphCondTypeWhile;
-    np.conditional.size = 1;
-    ok = ok && cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+    // the start, then the WHILE node after it
+    if (ok && cudaStreamBeginCaptureToGraph(ctx->stream, g, nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const int sst = start(true, &start_launches);
+      cudaStreamCaptureStatus cs;
+      cudaGraph_t cg = nullptr;
+      const cudaGraphNode_t* deps = nullptr;
+      const cudaGraphEdgeData* ed = nullptr;
+      size_t nd = 0;
+      ok = sst == GFE_OK && cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &cg, &deps, &ed,
+                                               &nd) == cudaSuccess;
+      np.type = cudaGraphNodeTypeConditional;
+      np.conditional.handle = h;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      ok = ok && cudaGraphAddNode(&node, cg, deps, ed, nd, &np) == cudaSuccess;
+      ok = ok && cudaStreamUpdateCaptureDependencies(ctx->stream, &node, nullptr, 1,
+                                                     cudaStreamSetCaptureDependencies) ==
+                     cudaSuccess;
+      cudaGraph_t top = nullptr;
+      ok = cudaStreamEndCapture(ctx->stream, &top) == cudaSuccess && ok;
+    } else {
+      ok = false;
+    }
     cudaGraph_t body = ok ? np.conditional.phGraph_out[0] : nullptr;
     ok = ok && cudaGraphConditionalHandleCreate(&hif, body, 0, 0) == cudaSuccess;
     const LoopConds conds{h, hif, 1};
@@ -2479,6 +2522,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       if (C->exec) cudaGraphExecDestroy(C->exec);
       C->exec = loop.e;
       C->key = key;
+      C->start_launches = start_launches;
       C->body_launches = body_launches;
       C->if_launches = if_launches;
       loop.cached = true;
@@ -2486,20 +2530,19 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   }
   int updates = 0, slow = 0, fallback = 0;
   bool fresh = false;  // the loop ended on a reliable update: x64 and rr64 are current
-  k_fcg_setup<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta, maxit, loop.e ? 1 : 0);
-  ctx->launches++;
   if (loop.e) {
-    // the whole solve, reliable updates included, on the device: one wait. The first
-    // iteration's beta is 0 (p.q is); the unfused direction update still reads p.
-    if (!fuse_dir)
-      GFE_CUDA_TRY(cudaMemsetAsync(p32, 0, sizeof(float) * n, ctx->stream));
+    // the whole solve, reliable updates included, on the device: one wait
     GFE_CUDA_TRY(cudaGraphLaunch(loop.e, ctx->stream));
     GFE_TRY(read_state(ctx, w));
     updates = w.hS->updates;
     fresh = w.hS->converged != 0;  // only the loop's reliable update declares convergence
-    ctx->launches += (long long)w.hS->iter * body_launches + (long long)updates * if_launches;
+    ctx->launches += start_launches + (long long)w.hS->iter * body_launches +
+                     (long long)updates * if_launches;
   } else {
     // host-driven loop (kernel timing, the learned preconditioner, no conditional graphs)
+    long long sl = 0;
+    GFE_TRY(start(false, &sl));
+    ctx->launches += sl;
     GFE_TRY(precond());
     // p = z (the fused SpMV forms it: beta is 0 while p.q is)
     if (!fuse_dir)

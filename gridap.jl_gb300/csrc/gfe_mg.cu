@@ -276,41 +276,35 @@ __global__ void __launch_bounds__(kMgBlock)
   }
 }
 
-// coarse kappa = mean of the 8 children (padded row strides cf1, cc1)
-__global__ void k_mg_kappa(int nc0, int nc1, int nc2, int cf1, int nf1, int cc1,
-                           const float* __restrict__ kf, float* __restrict__ kc) {
-  const int64_t n = (int64_t)nc0 * nc1 * nc2;
-  for (int64_t c = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * kMgBlock) {
-    const int I = (int)(c % nc0);
-    const int64_t rest = c / nc0;
-    const int J = (int)(rest % nc1), K = (int)(rest / nc1);
-    float s = 0.f;
-    for (int e = 0; e < 8; ++e) {
-      const int i = 2 * I + (e & 1), j = 2 * J + ((e >> 1) & 1), k = 2 * K + (e >> 2);
-      s += kf[(int64_t)i + (int64_t)cf1 * (j + (int64_t)nf1 * k)];
-    }
-    kc[(int64_t)I + (int64_t)cc1 * (J + (int64_t)nc1 * K)] = 0.125f * s;
+// One level's refresh in one pass over its interior nodes (i, j, k) = (32 bx + lane, 8 by +
+// warp, bz): D^-1 of the node, D = sum of kappa_K Kref[l, l] over the 8 cells around it, and
+// at even (i, j, k) kappa of the coarse cell (i/2, j/2, k/2), the mean of its 8 children
+// (kc null on the coarsest level; cc1, cc2 its row and plane strides). Each level's pass is
+// launched after the one above with programmatic serialisation and waits for its kappa.
+__global__ void __launch_bounds__(kMgBlock)
+    k_mg_refresh(LatticeQ1Op op, float* __restrict__ dinv, float* __restrict__ kc, int cc1,
+                 int64_t cc2) {
+  if (stop(nullptr)) return;
+  const int m0 = op.n0 - 1, m1 = op.n1 - 1;
+  const int i = (int)blockIdx.x * 32 + (int)(threadIdx.x & 31);
+  const int j = (int)blockIdx.y * 8 + (int)(threadIdx.x >> 5);
+  const int k = (int)blockIdx.z;
+  if (i >= m0 || j >= m1) return;
+  const float* kap = op.kap + ((int64_t)i + (int64_t)op.c1 * j + (int64_t)op.c2 * k);
+  float d = 0.f;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int cx = e & 1, cy = (e >> 1) & 1, cz = e >> 2;
+    const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
+    d += kap[cx + (int64_t)op.c1 * cy + (int64_t)op.c2 * cz] * op.K[lr + 8 * lr];
   }
-}
-
-// D^-1 of a lattice operator: D_r = sum of kappa_K Kref[l_r, l_r] over the 8 cells around r
-__global__ void k_mg_diag(LatticeQ1Op op, float* __restrict__ dinv) {
-  const int m0 = op.n0 - 1, m1 = op.n1 - 1, m2 = op.n2 - 1;
-  const int64_t n = (int64_t)m0 * m1 * m2;
-  for (int64_t r = (int64_t)blockIdx.x * kMgBlock + threadIdx.x; r < n;
-       r += (int64_t)gridDim.x * kMgBlock) {
-    const int i = (int)(r % m0);
-    const int64_t rest = r / m0;
-    const int j = (int)(rest % m1), k = (int)(rest / m1);
-    float d = 0.f;
-    for (int e = 0; e < 8; ++e) {
-      const int cx = e & 1, cy = (e >> 1) & 1, cz = e >> 2;
-      const int lr = (1 - cx) + 2 * (1 - cy) + 4 * (1 - cz);
-      d += op.kap[(int64_t)(i + cx) + (int64_t)op.c1 * (j + cy) + (int64_t)op.c2 * (k + cz)] *
-           op.K[lr + 8 * lr];
-    }
-    dinv[r] = d > 0.f ? 1.f / d : 0.f;
+  dinv[i + (int64_t)m0 * (j + (int64_t)m1 * k)] = d > 0.f ? 1.f / d : 0.f;
+  if (kc && !((i | j | k) & 1)) {
+    float s = 0.f;
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+      s += kap[(e & 1) + (int64_t)op.c1 * ((e >> 1) & 1) + (int64_t)op.c2 * (e >> 2)];
+    kc[(i >> 1) + (int64_t)cc1 * (j >> 1) + cc2 * (k >> 1)] = 0.125f * s;
   }
 }
 
@@ -768,6 +762,11 @@ int mg_create(gfe_ctx* ctx, const LatticeQ1Op& fine, LatticeMG** out) {
     }
     mg->lv.push_back(L);
   }
+  // the coarse kappa arrays' padding columns (every refresh writes the cells only)
+  for (size_t l = 1; l < mg->lv.size(); ++l)
+    GFE_CUDA_TRY(cudaMemsetAsync(const_cast<float*>(mg->lv[l].op.kap), 0,
+                                 sizeof(float) * (size_t)mg->lv[l].op.c2 * mg->lv[l].op.n2,
+                                 ctx->stream));
   GFE_TRY(mg_refresh(mg, fine));
   for (size_t l = 0; l < mg->lv.size(); ++l) {
     if (!coarse_from(mg, l)) continue;
@@ -787,20 +786,15 @@ int mg_refresh(LatticeMG* mg, const LatticeQ1Op& fine) {
   gfe_ctx* ctx = mg->ctx;
   mg->lv[0].op.kap = fine.kap;
   for (size_t l = 0; l < mg->lv.size(); ++l) {
-    LatticeMG::Level& L = mg->lv[l];
-    if (l) {
-      const LatticeQ1Op& f = mg->lv[l - 1].op;
-      float* kc = const_cast<float*>(L.op.kap);
-      GFE_CUDA_TRY(cudaMemsetAsync(kc, 0, sizeof(float) * (size_t)L.op.c2 * L.op.n2,
-                                   ctx->stream));
-      k_mg_kappa<<<vgrid(ctx, (int64_t)L.op.n0 * L.op.n1 * L.op.n2), kMgBlock, 0,
-                   ctx->stream>>>(L.op.n0, L.op.n1, L.op.n2, f.c1, f.n1, L.op.c1, f.kap, kc);
-      ctx->launches++;
-    }
-    k_mg_diag<<<vgrid(ctx, L.n), kMgBlock, 0, ctx->stream>>>(L.op, L.dinv);
+    const LatticeMG::Level& L = mg->lv[l];
+    const LatticeQ1Op* C = l + 1 < mg->lv.size() ? &mg->lv[l + 1].op : nullptr;
+    GFE_CUDA_TRY(launch_pdl(k_mg_refresh, dim3((unsigned)((L.m0 + 31) / 32),
+                                              (unsigned)((L.m1 + 7) / 8), (unsigned)L.m2),
+                            kMgBlock, 0, ctx->stream, L.op, L.dinv,
+                            C ? const_cast<float*>(C->kap) : nullptr, C ? C->c1 : 0,
+                            C ? (int64_t)C->c2 : (int64_t)0));
     ctx->launches++;
   }
-  GFE_CUDA_TRY(cudaGetLastError());
   return GFE_OK;
 }
 

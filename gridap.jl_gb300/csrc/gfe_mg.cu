@@ -23,6 +23,7 @@
 namespace gfe {
 #include "gfe_lattice.cuh"
 #include "gfe_reduce.cuh"
+#include "gfe_pdl.cuh"
 
 namespace {
 
@@ -73,31 +74,12 @@ constexpr int kPreSweeps = 2, kPostSweeps = 2, kCoarseSweeps = 4;
 // neighbour, loads twice the vectors per row and measured slower there.
 constexpr bool kFusePreDeep = false;
 
-// Every kernel of the cycle is launched with programmatic stream serialisation (launch_pdl):
-// its blocks may become resident while the kernel before it on the stream still runs, and
-// wait in stop() -- before any memory access -- until that kernel has completed and its
-// writes are visible; each then lets the next kernel launch at once. Without that launch
-// attribute the wait returns immediately.
+// Every kernel of the cycle is launched with programmatic stream serialisation (launch_pdl)
+// and waits in stop() for the kernel before it; each returns at once when the solver's done
+// flag is set.
 __device__ __forceinline__ bool stop(const int* done) {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  pdl_wait();
   return done && *done;
-}
-
-template <class... P, class... A>
-cudaError_t launch_pdl(void (*kern)(P...), dim3 grid, int block, size_t smem, cudaStream_t st,
-                       A&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = dim3((unsigned)block);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
 }
 
 // One damped Jacobi sweep fused into the lattice apply: xo = x + w D^-1 (b - A x)

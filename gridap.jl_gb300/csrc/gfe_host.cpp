@@ -102,25 +102,45 @@ int ensure_values(gfe_ctx* ctx, gfe_matrix* A) {
   return GFE_OK;
 }
 
+// the error of a device error word read on the host (resets the device word when set)
+static int report_device_error(gfe_ctx* ctx, const DevError& h, const char* where) {
+  if (h.code == GFE_OK) return GFE_OK;
+  GFE_CUDA_TRY(cudaMemsetAsync(ctx->d_err, 0, sizeof(DevError), ctx->stream));
+  const char* what = "device error";
+  switch (h.code) {
+    case GFE_ERR_DEGENERATE_CELL: what = "degenerate cell (det J <= 0 or not finite)"; break;
+    case GFE_ERR_ROW_TOO_WIDE: what = "matrix row wider than supported"; break;
+    case GFE_ERR_INVALID_ARGUMENT: what = "id out of range"; break;
+    case GFE_ERR_NONFINITE: what = "non-finite value"; break;
+    case GFE_ERR_TIMEOUT: what = "bounded wait ran out"; break;
+    default: break;
+  }
+  return set_error(h.code, "%s: %s at index %lld", where, what, h.index);
+}
+
 int check_device_error(gfe_ctx* ctx, const char* where) {
+  ctx->err_staged = false;
   DevError h;
   GFE_CUDA_TRY(cudaMemcpyAsync(&h, ctx->d_err, sizeof(DevError), cudaMemcpyDeviceToHost,
                                ctx->stream));
   GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  if (h.code != GFE_OK) {
-    GFE_CUDA_TRY(cudaMemsetAsync(ctx->d_err, 0, sizeof(DevError), ctx->stream));
-    const char* what = "device error";
-    switch (h.code) {
-      case GFE_ERR_DEGENERATE_CELL: what = "degenerate cell (det J <= 0 or not finite)"; break;
-      case GFE_ERR_ROW_TOO_WIDE: what = "matrix row wider than supported"; break;
-      case GFE_ERR_INVALID_ARGUMENT: what = "id out of range"; break;
-      case GFE_ERR_NONFINITE: what = "non-finite value"; break;
-      case GFE_ERR_TIMEOUT: what = "bounded wait ran out"; break;
-      default: break;
-    }
-    return set_error(h.code, "%s: %s at index %lld", where, what, h.index);
-  }
+  return report_device_error(ctx, h, where);
+}
+
+int stage_device_error(gfe_ctx* ctx) {
+  GFE_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(ctx->h_pinned) + kStagedErrorOffset,
+                               ctx->d_err, sizeof(DevError), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  ctx->err_staged = true;
   return GFE_OK;
+}
+
+int check_staged_error(gfe_ctx* ctx, const char* where) {
+  if (!ctx->err_staged) return check_device_error(ctx, where);
+  ctx->err_staged = false;
+  DevError h;
+  std::memcpy(&h, static_cast<const char*>(ctx->h_pinned) + kStagedErrorOffset, sizeof(h));
+  return report_device_error(ctx, h, where);
 }
 
 // ---- kernel timing ------------------------------------------------------------------------

@@ -116,6 +116,9 @@ struct gfe_ctx {
   int64_t lift_ndiri = 0;
   // pinned staging for small device->host reads
   void* h_pinned = nullptr;
+  // the device error word copied into h_pinned + kStagedErrorOffset ahead of a wait, for the
+  // check that follows it (stage_device_error)
+  bool err_staged = false;
   gfe::KernelTimer timer;
   // CUDA graph of one chunk of CG iterations, reused while its launch parameters match
   cudaGraphExec_t cg_exec = nullptr;
@@ -279,6 +282,13 @@ int device_view(gfe_ctx* ctx, const void* p, size_t n, int slot, const void** ou
 int copy_out(gfe_ctx* ctx, void* dst, const void* src, size_t n);
 // Reads and resets the device error word; returns its code (GFE_OK if none).
 int check_device_error(gfe_ctx* ctx, const char* where);
+// Issues the copy of the device error word into pinned staging, to be read after the caller's
+// next wait by check_staged_error (no device work may come between the two).
+constexpr size_t kStagedErrorOffset = 2048;
+int stage_device_error(gfe_ctx* ctx);
+// check_device_error from the staged copy, without a wait of its own (or with one when
+// nothing was staged)
+int check_staged_error(gfe_ctx* ctx, const char* where);
 // zeroes A's values when their zeroing was deferred (val_pending)
 int ensure_values(gfe_ctx* ctx, gfe_matrix* A);
 
@@ -333,6 +343,7 @@ int64_t learned_ndofs(const gfe_learned_pc* pc);
 // false inside a captured V-cycle (the graph launch is timed as a whole)
 int learned_apply_into(gfe_ctx* ctx, gfe_learned_pc* pc, const float* d_r, const float* base,
                        float* d_z, const int* skip, bool timed);
+// (the solve's last wait brings the device error word along: check_staged_error follows)
 int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_opts* o,
               const double* d_b, double* d_x, gfe_solve_report* rep);
 

@@ -721,10 +721,13 @@ extern "C" int gfe_solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc,
   }
   gfe_solve_report rep;
   memset(&rep, 0, sizeof(rep));
+  ctx->err_staged = false;
   GFE_TRY(solve_fcg(ctx, A, pc, opts, (const double*)db, dx, &rep));
   if (!xdev) GFE_TRY(copy_out(ctx, x, dx, n8));
   if (report) *report = rep;
-  return check_device_error(ctx, "gfe_solve_fcg");
+  // the error word came back with the solve's last wait (nothing ran after it)
+  return opts->initial_guess ? check_device_error(ctx, "gfe_solve_fcg")
+                             : check_staged_error(ctx, "gfe_solve_fcg");
 }
 
 extern "C" int gfe_learned_pc_samples(gfe_learned_pc* pc, gfe_matrix* A, const double* r,

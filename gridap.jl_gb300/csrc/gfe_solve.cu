@@ -1630,9 +1630,11 @@ struct SolverWork {
   unsigned* tickets;   // device (inside S)
 };
 
-static int read_state(gfe_ctx* ctx, SolverWork& w, bool flush = true) {
+// (stage_err: the device error word comes along, for the caller's check after this wait)
+static int read_state(gfe_ctx* ctx, SolverWork& w, bool flush = true, bool stage_err = false) {
   GFE_CUDA_TRY(cudaMemcpyAsync(w.hS, w.S, sizeof(SolverState), cudaMemcpyDeviceToHost,
                                ctx->stream));
+  if (stage_err) GFE_TRY(stage_device_error(ctx));
   GFE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return flush ? timer_flush(ctx) : GFE_OK;
 }
@@ -2533,7 +2535,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   if (loop.e) {
     // the whole solve, reliable updates included, on the device: one wait
     GFE_CUDA_TRY(cudaGraphLaunch(loop.e, ctx->stream));
-    GFE_TRY(read_state(ctx, w));
+    GFE_TRY(read_state(ctx, w, true, true));
     updates = w.hS->updates;
     fresh = w.hS->converged != 0;  // only the loop's reliable update declares convergence
     ctx->launches += start_launches + (long long)w.hS->iter * body_launches +
@@ -2625,7 +2627,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     ctx->launches++;
   }
   GFE_CUDA_TRY(cudaGetLastError());
-  if (!(loop.e && fresh)) GFE_TRY(read_state(ctx, w));
+  if (!(loop.e && fresh)) GFE_TRY(read_state(ctx, w, true, true));
   const double bb = w.hS->bb;
   const double rr = fresh ? w.hS->rr64 : w.hS->rr;
   rep->relres = rel_residual(rr, bb);

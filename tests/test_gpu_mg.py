@@ -146,3 +146,37 @@ def test_mg_fcg_device_loop_limits(gg):
     xn, repn = _solve(gg, A, bn, gg.FCGSolver(rtol=1e-8, pc="mg", maxiter=50))
     assert not repn.converged and repn.iterations <= 50
     assert repn.status == gg._lib.GFE_ERR_NONFINITE or not np.isfinite(repn.relres)
+
+
+def test_mg_fcg_pinned_host_x(gg):
+    """A page-locked host x (the e2e route) must get what a device x gets: repeated solves
+    into new buffers, a solve stopped by maxiter, and a NaN in b (reported from the error word
+    that comes back with the solve's last wait)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11)
+    part = (24, 20, 16)
+    kappa = np.exp(1.5 * rng.standard_normal(int(np.prod(part))))
+    fnod = rng.standard_normal(int(np.prod(np.array(part) + 1)))
+    _, _, A, b = _problem(gg, (0, 1) * 3, part, ("boundary",), kappa, gg.NodalField(fnod))
+    n = b.size
+    for maxiter, bb in ((100, b), (100, 2.0 * b), (3, b)):
+        xd = torch.zeros(n, dtype=torch.float64, device="cuda")
+        _, repd = _solve_into(gg, A, bb, xd, maxiter)
+        for _ in range(2):
+            xp = torch.full((n,), -1.0, dtype=torch.float64).pin_memory()
+            _, repp = _solve_into(gg, A, bb, xp, maxiter)
+            assert repp.iterations == repd.iterations and repp.converged == repd.converged
+            assert np.array_equal(xp.numpy(), xd.cpu().numpy())
+    bn = b.copy()
+    bn[3] = np.nan
+    xp = torch.zeros(n, dtype=torch.float64).pin_memory()
+    _, repn = _solve_into(gg, A, bn, xp, 50)
+    assert not repn.converged
+    assert repn.status == gg._lib.GFE_ERR_NONFINITE or not np.isfinite(repn.relres)
+
+
+def _solve_into(gg, A, b, x, maxiter):
+    ns = gg.numerical_setup(gg.symbolic_setup(gg.FCGSolver(rtol=1e-8, pc="mg",
+                                                             maxiter=maxiter), A), A)
+    gg.solve_(x, ns, b)
+    return x, ns.report

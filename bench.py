@@ -535,19 +535,24 @@ def run_gpu(args):
                          kt=r_mixed_kt["kt"][_lib.GFE_KT_ASSEMBLE]),
     }
     if isinstance(mixed, gg.FCGSolver):
-        # FCG: the lattice SpMV also reads r (p.r), its vector kernels move x, r, p, q (update)
-        # and z, q, p (beta + direction) in two timed pairs per iteration; the V-cycle is one
-        # graph launch timed as a whole
-        kinds["spmv32"].update(kernel="k_lattice_spmv<true, false> (matrix-free FP32 Q1 "
-                                      "operator + p.q, p.r)", alg=ncells * 4 + nfree * 12,
-                               traffic=profile_traffic("fp32_lattice_fcg"))
-        kinds["vector32"].update(kernel="k_fcg_update; k_fcg_beta + k_fcg_dir (FP32 FCG "
-                                        "vector updates)", alg=22 * nfree, traffic=None)
-        kinds["vcycle"] = dict(kernel="multigrid V-cycle (CUDA graph: k_mg_smooth, "
-                                      "k_mg_residual, k_mg_restrict, k_mg_prolong over %d "
-                                      "levels)"
+        # FCG on the lattice multigrid: the SpMV applies the operator to z and folds in the
+        # direction update (kappa per cell, z read; p, q read and written; r read: 4 C + 24 R),
+        # the update kernel moves x, r, p, q (x, r, p, q read, x, r written: 24 R), and the
+        # V-cycle, one graph launch timed as a whole, also reads q in its last sweep (the beta
+        # dot: 4 R)
+        kinds["spmv32"].update(kernel="k_lattice_spmv_dir (matrix-free FP32 Q1 operator on z; "
+                                      "p = z + beta p, q = A z + beta q; p.q, p.r)",
+                               alg=ncells * 4 + nfree * 24,
+                               traffic=profile_traffic("fp32_lattice_dir"))
+        kinds["vector32"].update(kernel="k_fcg_update4 (x += a p, r -= a q, r.r)",
+                                 alg=24 * nfree, traffic=None)
+        kinds["vcycle"] = dict(kernel="multigrid V-cycle (CUDA graph over %d levels: "
+                                      "k_mg_jacobi0, k_mg_smooth, k_mg_pre, k_mg_residual, "
+                                      "k_mg_restrict, k_mg_prolong, k_mg_coarse; the last "
+                                      "sweep k_mg_smooth_dot forms the FCG beta)"
                                       % len(mg_levels(args.n)),
-                               alg=vcycle_bytes(args.n), traffic=profile_traffic("vcycle"),
+                               alg=vcycle_bytes(args.n) + 4 * nfree,
+                               traffic=profile_traffic("vcycle"),
                                kt=r_mixed_kt["kt"][_lib.GFE_KT_PRECOND])
     table = {}
     for k, d in kinds.items():

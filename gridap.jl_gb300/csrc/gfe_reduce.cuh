@@ -41,14 +41,18 @@ __device__ __forceinline__ unsigned grid_blocks() {
   return gridDim.x * gridDim.y * gridDim.z;
 }
 
-// Called by every block after writing its partial(s). Returns true in the last block, with
-// the partial sums of all blocks reduced in block order into out[0..nv).
+// Called by every block after its thread 0 has written the block's partial(s). Returns true
+// in the last block, with the partial sums of all blocks reduced in block order into
+// out[0..nv). Only thread 0 fences before taking its ticket: the partials are its own writes,
+// and a fence in every thread would wait for all of the block's outstanding stores.
 template <int NT, int NV>
 __device__ bool last_block_reduce(unsigned* ticket, const double* partials, int nblocks,
                                   double* out, double* sh) {
   __shared__ bool last;
-  __threadfence();
-  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == (unsigned)nblocks - 1);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = (atomicAdd(ticket, 1u) == (unsigned)nblocks - 1);
+  }
   __syncthreads();
   if (!last) return false;
   __threadfence();

@@ -8,7 +8,7 @@ linear solve to ||b - A x|| <= 1e-8 ||b|| (FP64 residual).
 
   value (headline arm)  mixed precision: FP32 Jacobi-PCG with FP64 reliable updates (x and
                         the true residual in FP64), inputs resident in HBM;
-  plain_fp64            FP64 assembly + FP64 Jacobi-PCG, same inputs (the north-star base);
+  plain_fp64            FP64 assembly + FP64 Jacobi-PCG, same inputs (the plain FP64 base path);
   e2e                   the headline arm through the C ABI with pinned host buffers:
                         cell ids, kappa and f copied in, x copied out, every step.
 

@@ -822,20 +822,20 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
       A->cell_rows.as<int32_t>(), A->col_ids(), (int)n0, (int)n1, (int)n2,
       flag.as<int>());
   ctx->launches++;
-  // the check's verdict comes back through pinned memory on an event, while the closed-form
+  // the check's result comes back through pinned memory on an event, while the closed-form
   // row pointers and columns are built behind it (discarded, and rebuilt by the general loop,
   // when the ids are not the interior numbering)
   int* hflag = reinterpret_cast<int*>(static_cast<char*>(ctx->h_pinned) + 3072);
   *hflag = 1;
   GFE_CUDA_TRY(cudaMemcpyAsync(hflag, flag.ptr, sizeof(int), cudaMemcpyDeviceToHost,
                                ctx->stream));
-  cudaEvent_t verdict;
-  GFE_CUDA_TRY(cudaEventCreateWithFlags(&verdict, cudaEventDisableTiming));
+  cudaEvent_t checked;
+  GFE_CUDA_TRY(cudaEventCreateWithFlags(&checked, cudaEventDisableTiming));
   struct EventRelease {
     cudaEvent_t e;
     ~EventRelease() { cudaEventDestroy(e); }
-  } verdict_release{verdict};
-  GFE_CUDA_TRY(cudaEventRecord(verdict, ctx->stream));
+  } checked_release{checked};
+  GFE_CUDA_TRY(cudaEventRecord(checked, ctx->stream));
   GFE_TRY(A->rowptr.reserve(sizeof(int32_t) * (nrows + 1)));
   GFE_TRY(A->colval.reserve(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
   GFE_TRY(A->val.reserve(sizeof(double) * (nnz > 0 ? nnz : 1)));
@@ -844,7 +844,7 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
   k_cart_cols<<<(unsigned)(ctx->num_sms * 4), 256, 0, ctx->stream>>>(
       (int)m0, (int)m1, (int)m2, A->rowptr.as<int32_t>(), A->colval.as<int32_t>());
   ctx->launches += 2;
-  GFE_CUDA_TRY(cudaEventSynchronize(verdict));
+  GFE_CUDA_TRY(cudaEventSynchronize(checked));
   if (*hflag) return GFE_OK;
   A->nrefs = 8 * nrows;
   A->nnz = nnz;

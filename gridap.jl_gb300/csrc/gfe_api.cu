@@ -69,6 +69,9 @@ extern "C" int gfe_ctx_destroy(gfe_ctx* c) {
   if (c->pool) cudaMemPoolDestroy(c->pool);
   if (c->d_err) cudaFree(c->d_err);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  if (c->copy_fork) cudaEventDestroy(c->copy_fork);
+  if (c->copy_join) cudaEventDestroy(c->copy_join);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return GFE_OK;
@@ -161,7 +164,11 @@ static int symbolic_loop(gfe_ctx* ctx, int64_t ncells, int ndr, int ndc,
   A->cols_alias = cell_cols == cell_rows && ndc == ndr;
   int s = A->cell_rows.reserve(rsz);
   if (s == GFE_OK && !A->cols_alias) s = A->cell_cols.reserve(csz);
-  if (s == GFE_OK && rsz) {
+  // a structured problem's ids in host memory: the closed-form pattern build copies them
+  // itself, beside its own kernels
+  const bool host_ids = structured && A->cols_alias && !local_mask && rsz &&
+                        !is_device_ptr(cell_rows);
+  if (s == GFE_OK && rsz && !host_ids) {
     cudaError_t e = cudaMemcpyAsync(A->cell_rows.ptr, cell_rows, rsz, cudaMemcpyDefault,
                                     ctx->stream);
     if (e == cudaSuccess && !A->cols_alias)
@@ -181,7 +188,8 @@ static int symbolic_loop(gfe_ctx* ctx, int64_t ncells, int ndr, int ndc,
   bool done = false;
   if (s == GFE_OK && structured)
     s = build_pattern_cartesian(ctx, A, structured->partition[0], structured->partition[1],
-                                structured->partition[2], &done);
+                                structured->partition[2], &done,
+                                host_ids ? cell_rows : nullptr);
   if (s == GFE_OK && !done) s = build_pattern(ctx, A);
   if (s != GFE_OK) {
     delete A;

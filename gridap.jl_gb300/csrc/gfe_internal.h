@@ -104,6 +104,10 @@ struct KernelTimer {
 struct gfe_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // a second stream for host-to-device copies that overlap work on `stream` (created on first
+  // use), with the events that order it against `stream`
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_fork = nullptr, copy_join = nullptr;
   cudaMemPool_t pool = nullptr;  // stream-ordered pool of this context's device buffers
   int num_sms = 0;
   long long launches = 0;
@@ -311,8 +315,11 @@ int build_pattern(gfe_ctx* ctx, gfe_matrix* A);
 // The pattern of Q1 cells of an n0 x n1 x n2 Cartesian grid numbered by interior nodes, in
 // closed form after a device check of the ids; *done false (nothing changed) when the ids
 // are not that numbering.
+// host_ids: ids still in host memory (A->cell_rows reserved, not yet filled); they are copied
+// into A->cell_rows on the context's copy stream while the closed-form row pointers and
+// columns are built, or on the main stream when the closed form does not apply.
 int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1, int64_t n2,
-                            bool* done);
+                            bool* done, const int32_t* host_ids = nullptr);
 
 // assembly (gfe_assemble.cu)
 int assemble_cellmats(gfe_ctx* ctx, gfe_matrix* A, const double* d_cellmats);

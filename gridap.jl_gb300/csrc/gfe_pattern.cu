@@ -804,27 +804,63 @@ int ensure_row_refs(gfe_ctx* ctx, gfe_matrix* A) {
 }
 
 int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1, int64_t n2,
-                            bool* done) {
+                            bool* done, const int32_t* host_ids) {
   *done = false;
+  const size_t idsz = sizeof(int32_t) * (size_t)A->ncells * A->nd;
+  // the ids on the main stream (the general loop follows)
+  auto copy_ids = [&]() -> int {
+    if (host_ids)
+      GFE_CUDA_TRY(cudaMemcpyAsync(A->cell_rows.ptr, host_ids, idsz, cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    return GFE_OK;
+  };
   const int64_t m0 = n0 - 1, m1 = n1 - 1, m2 = n2 - 1;
   if (A->nd != 8 || A->cols_per_cell() != 8 || A->has_lmask || n0 < 2 || n1 < 2 || n2 < 2 ||
       A->ncells != n0 * n1 * n2 || A->nrows != m0 * m1 * m2 || A->ncols != A->nrows ||
       n0 * n1 * n2 * 8 > (int64_t)INT32_MAX)
-    return GFE_OK;
+    return copy_ids();
   const int64_t nrows = A->nrows, ncells = A->ncells;
   auto axis = [](int64_t m) { return m == 1 ? (int64_t)1 : 3 * m - 2; };
   const int64_t nnz = axis(m0) * axis(m1) * axis(m2);
-  if (nnz > (int64_t)INT32_MAX - 64) return GFE_OK;  // the general loop reports it
+  if (nnz > (int64_t)INT32_MAX - 64) return copy_ids();  // the general loop reports it
   DevBuf flag(ctx);
   GFE_TRY(flag.reserve(sizeof(int)));
   GFE_CUDA_TRY(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
+  auto closed_form = [&]() -> int {
+    GFE_TRY(A->rowptr.reserve(sizeof(int32_t) * (nrows + 1)));
+    GFE_TRY(A->colval.reserve(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
+    GFE_TRY(A->val.reserve(sizeof(double) * (nnz > 0 ? nnz : 1)));
+    k_cart_rowptr<<<grid_for(nrows + 1, 256, (int64_t)ctx->num_sms * 16), 256, 0,
+                    ctx->stream>>>(nrows, (int)m0, (int)m1, (int)m2, A->rowptr.as<int32_t>());
+    k_cart_cols<<<(unsigned)(ctx->num_sms * 4), 256, 0, ctx->stream>>>(
+        (int)m0, (int)m1, (int)m2, A->rowptr.as<int32_t>(), A->colval.as<int32_t>());
+    ctx->launches += 2;
+    return GFE_OK;
+  };
+  if (host_ids) {
+    // the ids cross the host link on the copy stream (after the buffers' allocation on the
+    // main stream) while the closed-form row pointers and columns are built; the check waits
+    // for both
+    if (!ctx->copy_stream) {
+      GFE_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+      GFE_CUDA_TRY(cudaEventCreateWithFlags(&ctx->copy_fork, cudaEventDisableTiming));
+      GFE_CUDA_TRY(cudaEventCreateWithFlags(&ctx->copy_join, cudaEventDisableTiming));
+    }
+    GFE_CUDA_TRY(cudaEventRecord(ctx->copy_fork, ctx->stream));
+    GFE_TRY(closed_form());
+    GFE_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_fork, 0));
+    GFE_CUDA_TRY(cudaMemcpyAsync(A->cell_rows.ptr, host_ids, idsz, cudaMemcpyHostToDevice,
+                                 ctx->copy_stream));
+    GFE_CUDA_TRY(cudaEventRecord(ctx->copy_join, ctx->copy_stream));
+    GFE_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->copy_join, 0));
+  }
   k_cart_check<<<grid_for(ncells, 256, (int64_t)ctx->num_sms * 16), 256, 0, ctx->stream>>>(
       A->cell_rows.as<int32_t>(), A->col_ids(), (int)n0, (int)n1, (int)n2,
       flag.as<int>());
   ctx->launches++;
-  // the check's result comes back through pinned memory on an event, while the closed-form
-  // row pointers and columns are built behind it (discarded, and rebuilt by the general loop,
-  // when the ids are not the interior numbering)
+  // the check's result comes back through pinned memory on an event, while (device ids) the
+  // closed-form row pointers and columns are built behind it (discarded, and rebuilt by the
+  // general loop, when the ids are not the interior numbering)
   int* hflag = reinterpret_cast<int*>(static_cast<char*>(ctx->h_pinned) + 3072);
   *hflag = 1;
   GFE_CUDA_TRY(cudaMemcpyAsync(hflag, flag.ptr, sizeof(int), cudaMemcpyDeviceToHost,
@@ -836,14 +872,7 @@ int build_pattern_cartesian(gfe_ctx* ctx, gfe_matrix* A, int64_t n0, int64_t n1,
     ~EventRelease() { cudaEventDestroy(e); }
   } checked_release{checked};
   GFE_CUDA_TRY(cudaEventRecord(checked, ctx->stream));
-  GFE_TRY(A->rowptr.reserve(sizeof(int32_t) * (nrows + 1)));
-  GFE_TRY(A->colval.reserve(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
-  GFE_TRY(A->val.reserve(sizeof(double) * (nnz > 0 ? nnz : 1)));
-  k_cart_rowptr<<<grid_for(nrows + 1, 256, (int64_t)ctx->num_sms * 16), 256, 0, ctx->stream>>>(
-      nrows, (int)m0, (int)m1, (int)m2, A->rowptr.as<int32_t>());
-  k_cart_cols<<<(unsigned)(ctx->num_sms * 4), 256, 0, ctx->stream>>>(
-      (int)m0, (int)m1, (int)m2, A->rowptr.as<int32_t>(), A->colval.as<int32_t>());
-  ctx->launches += 2;
+  if (!host_ids) GFE_TRY(closed_form());
   GFE_CUDA_TRY(cudaEventSynchronize(checked));
   if (*hflag) return GFE_OK;
   A->nrefs = 8 * nrows;

@@ -612,3 +612,48 @@ def test_q2_tensor_core_cells_close_to_fp64(gg, orc):
     # and the FP64 path itself matches the oracle
     ref = orc.poisson_q2((0, 1) * 3, part, ("boundary",), kappa=kappa, fconst=1.0, jitter=jit)
     assert _rowscaled_err(rp, z64, ref["csc"][2]) <= TOL_VAL
+
+
+@pytest.mark.parametrize("where", ["host", "device"])
+@pytest.mark.parametrize("permute", [False, True])
+def test_problem_symbolic_loop_host_and_device_ids(gg, where, permute):
+    """The problem-aware symbolic loop takes the ids from host memory (copied on a second
+    stream while the closed-form pattern is built) or from the device; with the interior
+    numbering it gives the closed form, with the free ids permuted (the device check fails) the
+    general loop's pattern, in both cases equal to the general symbolic loop on the same ids."""
+    import ctypes
+    import importlib
+    torch = pytest.importorskip("torch")
+    lib_ = importlib.import_module(gg.__name__ + "._lib")
+    part = (9, 7, 8)
+    model = gg.CartesianDiscreteModel((0, 1, 0, 1, 0, 1), part)
+    V = gg.FESpace(model, gg.ReferenceFE(gg.lagrangian, float, 1), dirichlet_tags="boundary")
+    dO = gg.Measure(gg.Triangulation(model), 2)
+    rng = np.random.default_rng(31)
+    kap = rng.uniform(0.5, 2.0, model.num_cells())
+    fn = gg.NodalField(rng.standard_normal(model.num_nodes()))
+    n = V.num_free_dofs()
+    ids = V.cell_dof_ids.copy()
+    if permute:
+        perm = rng.permutation(n).astype(ids.dtype)
+        free = ids > 0
+        ids[free] = perm[ids[free] - 1] + 1
+    ids_in = ids if where == "host" else torch.from_numpy(ids).cuda()
+    assem = gg.SparseMatrixAssembler(V, V)
+    prep = gg.prepare_problem(V, V, dO, gg.CellField(kap), fn, cell_dof_ids=ids_in)
+    A1 = gg.symbolic_loop_matrix(assem, (None, ids, ids))       # general
+    h = ctypes.c_void_p()
+    lib_.check(lib_.load().gfe_symbolic_loop_matrix_problem(assem.ctx.handle,
+                                                           ctypes.byref(prep.p), ctypes.byref(h)))
+    A2 = gg.DeviceMatrix(h, assem.ctx)
+    outs = []
+    for A in (A1, A2):
+        b = np.zeros(n)
+        lib_.check(lib_.load().gfe_assemble_matrix_and_vector(
+            assem.ctx.handle, ctypes.byref(prep.p), A.handle, lib_.ptr(b)))
+        outs.append((A.export_csr(0), b))
+    (r1, c1, v1), b1 = outs[0]
+    (r2, c2, v2), b2 = outs[1]
+    assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
+    assert np.allclose(v1, v2, rtol=1e-13, atol=1e-13 * np.abs(v1).max())
+    assert np.allclose(b1, b2, rtol=1e-13, atol=1e-13 * np.abs(b1).max())

@@ -1049,7 +1049,8 @@ __global__ void __launch_bounds__(kSpmvBlock)
     k_residual64_lattice(int m0, int m1, int m2, const int32_t* __restrict__ rowptr,
                          const double* __restrict__ val, const double* __restrict__ x,
                          const double* __restrict__ b, double* __restrict__ r,
-                         double* __restrict__ partials, double* out_rr, unsigned* ticket) {
+                         float* __restrict__ r32, double* __restrict__ partials, double* out_rr,
+                         unsigned* ticket) {
   extern __shared__ double stage_all[];
   __shared__ double sh[kSpmvBlock / 32];
   const int lane = (int)(threadIdx.x & 31), wib = (int)(threadIdx.x >> 5);
@@ -1098,7 +1099,10 @@ __global__ void __launch_bounds__(kSpmvBlock)
               ++pos;
             }
       const double ri = b[row] - s;
-      r[row] = ri;
+      if (r32)  // the FP32 residual the inner iterations restart from
+        r32[row] = (float)ri;
+      else if (r)
+        r[row] = ri;
       d = fma(ri, ri, d);
     }
     __syncwarp();
@@ -1382,10 +1386,11 @@ __global__ void __launch_bounds__(kSpmvBlock)
 
 // r32 = (float) r64 after a reliable update (no orthogonalisation needed: FCG takes alpha from
 // p.r and beta from z.q with the current vectors); stop when the FP64 residual meets rtol.
+// (r64 null: the FP64 residual kernel wrote r32 itself)
 __global__ void k_fcg_restart(int64_t n, const double* __restrict__ r64, float* __restrict__ r32,
                               SolverState* S, LoopConds c) {
   const bool conv = S->rr64 <= S->tol2;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n && !conv;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r64 && i < n && !conv;
        i += (int64_t)gridDim.x * blockDim.x)
     r32[i] = (float)r64[i];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1538,15 +1543,14 @@ __global__ void __launch_bounds__(kVecBlock)
 }
 
 // FCG start from x = 0 over float4 groups (16-byte aligned b, x, r): x = 0, r = (float) b,
-// partial r.r (z = r: the preconditioner is applied by the caller); the state as k_cg_init
-// leaves it (r.r in FP32 per thread: it sets the stopping threshold, the final relative
-// residual takes ||b|| in FP64)
+// and ||b||^2 in FP64 (the relative residual's denominator; it also sets the stopping
+// threshold and the starting r.r); z = r is left to the caller's preconditioner
 __global__ void __launch_bounds__(kVecBlock)
     k_fcg_init4(int64_t n, const double* __restrict__ b, float* __restrict__ x,
                 float* __restrict__ r, double* __restrict__ partials, SolverState* S,
                 double rtol2) {
   __shared__ double sh[kVecBlock / 32];
-  float rr_t = 0.f;
+  double bb_t = 0.0;
   const int64_t n4 = n >> 2;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nth = (int64_t)gridDim.x * blockDim.x;
@@ -1556,19 +1560,19 @@ __global__ void __launch_bounds__(kVecBlock)
     const float4 rv = make_float4((float)b0.x, (float)b0.y, (float)b1.x, (float)b1.y);
     reinterpret_cast<float4*>(r)[i] = rv;
     reinterpret_cast<float4*>(x)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    rr_t = fmaf(rv.x, rv.x, rr_t);
-    rr_t = fmaf(rv.y, rv.y, rr_t);
-    rr_t = fmaf(rv.z, rv.z, rr_t);
-    rr_t = fmaf(rv.w, rv.w, rr_t);
+    bb_t = fma(b0.x, b0.x, bb_t);
+    bb_t = fma(b0.y, b0.y, bb_t);
+    bb_t = fma(b1.x, b1.x, bb_t);
+    bb_t = fma(b1.y, b1.y, bb_t);
   }
   for (int64_t i = 4 * n4 + tid; i < n; i += nth) {
-    const float ri = (float)b[i];
-    r[i] = ri;
+    const double bi = b[i];
+    r[i] = (float)bi;
     x[i] = 0.f;
-    rr_t = fmaf(ri, ri, rr_t);
+    bb_t = fma(bi, bi, bb_t);
   }
-  const double rr = block_sum<kVecBlock>((double)rr_t, sh);
-  if (threadIdx.x == 0) partials[blockIdx.x] = rr;
+  const double bb = block_sum<kVecBlock>(bb_t, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = bb;
   double tot[1];
   if (last_block_reduce<kVecBlock, 1>(&S->ticket[1], partials, gridDim.x, tot, sh) &&
       threadIdx.x == 0) {
@@ -2195,7 +2199,8 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       k_fcg_dir<<<gv, kVecBlock, 0, ctx->stream>>>(n, p32, z32, w.S);
     }
   };
-  // r64 = b - A x64 in FP64, r64.r64 into *rr
+  // r64 = b - A x64 in FP64, r64.r64 into *rr; on the lattice pattern the residual goes
+  // straight to r32 for a restart (restart true) and is not stored otherwise
   const size_t lat_smem = sizeof(double) * 32 * 27 * (kSpmvBlock / 32);
   if (A->cart_lattice) {
     GFE_CUDA_TRY(cudaFuncSetAttribute(k_residual64_lattice<true>,
@@ -2205,13 +2210,13 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)lat_smem));
   }
-  auto residual64 = [&](double* rr) {
+  auto residual64 = [&](double* rr, bool restart) {
     if (A->cart_lattice)
       (A->zf_values ? k_residual64_lattice<true> : k_residual64_lattice<false>)
           <<<(unsigned)(ctx->num_sms * 4), kSpmvBlock, lat_smem, ctx->stream>>>(
               (int)A->cart_n[0] - 1, (int)A->cart_n[1] - 1, (int)A->cart_n[2] - 1,
-              A->rowptr.as<int32_t>(), A->val.as<double>(), d_x, d_b, r64, w.partials, rr,
-              &w.S->ticket[2]);
+              A->rowptr.as<int32_t>(), A->val.as<double>(), d_x, d_b, nullptr,
+              restart ? r32 : nullptr, w.partials, rr, &w.S->ticket[2]);
     else if (csr_residual)
       k_residual64_csr<4><<<(unsigned)(ctx->num_sms * 8), kSpmvBlock, 0, ctx->stream>>>(
           n, A->rowptr.as<int32_t>(), A->colval.as<int32_t>(), A->val.as<double>(), d_x, d_b,
@@ -2221,6 +2226,8 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
           n, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val64.as<double>(),
           d_x, d_b, r64, w.partials, rr, &w.S->ticket[2]);
   };
+  // the restart's source of r32 (none on the lattice pattern: the residual wrote it)
+  const double* restart_src = A->cart_lattice ? nullptr : r64;
   // reliable updates: after the FP32 residual has dropped by delta (0.1; 1e-4 with the
   // multigrid preconditioner, which gains about a decade per iteration: two FP64 residuals
   // reach 1e-8 at 128^3, with the same iterations and error as 1e-3's three)
@@ -2351,6 +2358,8 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   // b and x64 are the caller's buffers: the float4 kernels where they are 16-byte aligned
   const bool vec4_bx = vec4 && ((reinterpret_cast<uintptr_t>(d_b) |
                                  reinterpret_cast<uintptr_t>(d_x)) & 15) == 0;
+  // the float4 start forms ||b||^2 in FP64 itself
+  const bool bb_from_init = vec4_bx && !dinv32;
   // The start: the hierarchy's refresh, x = 0, r = b, the zeroed state and its settings
   // (defer: the device loop's reliable updates), ||b||^2 in FP64 for the relative residual.
   // z = M r, p = z, q = A p and alpha follow, as the device loop's first iteration or ahead of
@@ -2365,16 +2374,18 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
     }
     GFE_CUDA_TRY(cudaMemsetAsync(d_x, 0, n8, ctx->stream));
     GFE_CUDA_TRY(cudaMemsetAsync(w.S, 0, sizeof(SolverState), ctx->stream));
-    if (vec4_bx && !dinv32)
+    if (bb_from_init) {
       k_fcg_init4<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, x32, r32, w.partials, w.S,
                                                      o->rtol * o->rtol);
-    else
+    } else {
       k_cg_init<float, double><<<gv, kVecBlock, 0, ctx->stream>>>(
           n, d_b, 1.0, x32, r32, p32, dinv32, w.partials, w.S, o->rtol * o->rtol);
-    k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb,
-                                                  &w.S->ticket[1]);
+      k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb,
+                                                    &w.S->ticket[1]);
+      *launches += 1;
+    }
     k_fcg_setup<<<1, 1, 0, ctx->stream>>>(w.S, delta * delta, maxit, defer ? 1 : 0);
-    *launches += 3;
+    *launches += 2;
     // the device loop's first iteration takes beta = 0 (p.q is); the unfused direction update
     // still reads p
     if (defer && !fuse_dir)
@@ -2489,8 +2500,8 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
         cudaStream_t main = ctx->stream;
         ctx->stream = s2;  // the reliable update's launches go to the IF body
         merge();
-        residual64(&w.S->rr64);
-        k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, w.S, conds);
+        residual64(&w.S->rr64, true);
+        k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, restart_src, r32, w.S, conds);
         if_launches = 3;
         ctx->stream = main;
         cudaGraph_t ifb = nullptr;
@@ -2575,9 +2586,9 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
       // reliable update: x64 += x32, r64 = b - A64 x64, r32 = r64 (or stop)
       merge();
       timer_begin(ctx, GFE_KT_RESIDUAL64);
-      residual64(&w.S->rr64);
+      residual64(&w.S->rr64, true);
       timer_end(ctx);
-      k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, r64, r32, w.S, LoopConds{});
+      k_fcg_restart<<<gv, kVecBlock, 0, ctx->stream>>>(n, restart_src, r32, w.S, LoopConds{});
       ctx->launches += 3;
       ++updates;
       GFE_TRY(read_state(ctx, w));
@@ -2618,12 +2629,7 @@ int solve_fcg(gfe_ctx* ctx, gfe_matrix* A, gfe_learned_pc* pc, const gfe_solver_
   rep->fallback = fallback;
   // true FP64 residual (the reliable update's when it ended the loop: x has not moved since)
   if (!fresh) {
-    residual64(&w.S->rr);
-    ctx->launches++;
-  }
-  if (!device_loop) {  // (the device loop formed ||b||^2 ahead of it)
-    k_dot_self<<<gv, kVecBlock, 0, ctx->stream>>>(n, d_b, w.partials, &w.S->bb,
-                                                  &w.S->ticket[1]);
+    residual64(&w.S->rr, false);
     ctx->launches++;
   }
   GFE_CUDA_TRY(cudaGetLastError());

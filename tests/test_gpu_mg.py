@@ -180,3 +180,27 @@ def _solve_into(gg, A, b, x, maxiter):
                                                              maxiter=maxiter), A), A)
     gg.solve_(x, ns, b)
     return x, ns.report
+
+
+def test_mg_fcg_cached_graph_follows_settings(gg):
+    """The cached solve graph bakes in its start's settings (rtol, maxiter): alternating them on
+    one matrix must give each setting's own result, equal to a first solve with it."""
+    rng = np.random.default_rng(23)
+    part = (20, 16, 24)
+    kappa = np.exp(1.2 * rng.standard_normal(int(np.prod(part))))
+    fnod = rng.standard_normal(int(np.prod(np.array(part) + 1)))
+    _, _, A, b = _problem(gg, (0, 1) * 3, part, ("boundary",), kappa, gg.NodalField(fnod))
+    settings = [(1e-4, 1000), (1e-10, 1000), (1e-10, 3), (1e-4, 1000), (1e-10, 1000)]
+    first = {}
+    for rtol, maxiter in settings:
+        x, rep = _solve(gg, A, b, gg.FCGSolver(rtol=rtol, pc="mg", maxiter=maxiter))
+        if maxiter > 3:
+            assert rep.converged and rep.relres <= rtol * (1 + 1e-6)
+        else:
+            assert not rep.converged and rep.iterations == 3
+        key = (rtol, maxiter)
+        if key in first:
+            x0, rep0 = first[key]
+            assert rep.iterations == rep0.iterations and np.array_equal(x, x0)
+        else:
+            first[key] = (x, rep)

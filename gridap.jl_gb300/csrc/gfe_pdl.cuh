@@ -3,10 +3,8 @@
 // the kernel before it still runs; it waits in pdl_wait(), before any memory access, until
 // that kernel has completed and its writes are visible, and then lets the next kernel launch
 // at once. Without the launch attribute both instructions return immediately. Included
-// inside namespace gfe.
+// inside namespace gfe, after <utility> (std::forward).
 #pragma once
-
-#include <utility>
 
 __device__ __forceinline__ void pdl_wait() {
   asm volatile("griddepcontrol.wait;" ::: "memory");

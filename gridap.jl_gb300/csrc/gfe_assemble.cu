@@ -318,9 +318,21 @@ __global__ void k_sinsum_qpoints(int64_t ncells, int64_t n0, int64_t n1, double 
   fq[idx] = f;
 }
 
+// (pairs of doubles where v is 16-byte aligned; the reported index is the element's)
 __global__ void k_check_finite(const double* __restrict__ v, int64_t n, DevError* err) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  int64_t done = 0;
+  if ((reinterpret_cast<uintptr_t>(v) & 15) == 0) {
+    const int64_t n2 = n >> 1;
+    for (int64_t i = tid; i < n2; i += nth) {
+      const double2 w = __ldg(reinterpret_cast<const double2*>(v) + i);
+      if (!isfinite(w.x)) raise_err(err, GFE_ERR_NONFINITE, 2 * i);
+      if (!isfinite(w.y)) raise_err(err, GFE_ERR_NONFINITE, 2 * i + 1);
+    }
+    done = 2 * n2;
+  }
+  for (int64_t i = done + tid; i < n; i += nth)
     if (!isfinite(v[i])) raise_err(err, GFE_ERR_NONFINITE, i);
 }
 

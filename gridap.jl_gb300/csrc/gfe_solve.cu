@@ -252,12 +252,14 @@ __global__ void k_lattice_check(const int32_t* __restrict__ ids, int64_t n0, int
 
 // kappa in FP32 at the lattice operator's cell layout: rows of n0 cells padded to a
 // multiple of 4 (16-byte row strides, as the tensor-map copies of the operator require)
+// (cells (i, line), line = j + n1 k: i over x-blocks and threads, lines over y-blocks)
 __global__ void k_coef_to_f32(const double* __restrict__ c, int kind, int64_t n0, int64_t c1,
-                              int64_t n, float* __restrict__ out) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    out[(i % n0) + c1 * (i / n0)] =
-        kind == GFE_COEF_CELL ? (float)c[i] : kind == GFE_COEF_CONST ? (float)c[0] : 1.f;
+                              int64_t nlines, float* __restrict__ out) {
+  const float cst = kind == GFE_COEF_CONST ? (float)c[0] : 1.f;
+  for (int64_t l = blockIdx.y; l < nlines; l += gridDim.y)
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n0;
+         i += (int64_t)gridDim.x * blockDim.x)
+      out[i + c1 * l] = kind == GFE_COEF_CELL ? (float)c[i + n0 * l] : cst;
 }
 
 int attach_lattice_operator(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p,
@@ -280,8 +282,9 @@ int attach_lattice_operator(gfe_ctx* ctx, gfe_matrix* A, const gfe_problem* p,
   GFE_TRY(A->mf_flag.reserve(sizeof(int) * 4));
   GFE_CUDA_TRY(cudaMemsetAsync(A->mf_flag.ptr, 0, sizeof(int), ctx->stream));
   const unsigned g = grid_for(nc, 256, (int64_t)ctx->num_sms * 8);
-  k_coef_to_f32<<<g, 256, 0, ctx->stream>>>(d_coef, d_coef ? p->coef_kind : GFE_COEF_ONE, n0,
-                                            c1, nc, A->mf_kap32.as<float>());
+  const dim3 gc((unsigned)((n0 + 127) / 128), (unsigned)std::min<int64_t>(n1 * n2, 65535));
+  k_coef_to_f32<<<gc, 128, 0, ctx->stream>>>(d_coef, d_coef ? p->coef_kind : GFE_COEF_ONE, n0,
+                                             c1, n1 * n2, A->mf_kap32.as<float>());
   ctx->launches++;
   // a closed-form lattice pattern of this grid has had its ids checked already
   const bool known = A->cart_lattice && A->cart_n[0] == n0 && A->cart_n[1] == n1 &&
